@@ -1,0 +1,135 @@
+"""ctypes mirror of include/charm_gpu.h and the loader of libcharm_gpu.so.
+
+The library is the product: every GPU computation goes through these C
+entry points.  There is no Python or CPU fallback; if the shared library is
+missing, loading fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libcharm_gpu.so")
+
+MAX_COMP = 8
+MAX_CP = 8
+MAX_BND = 16
+BASIS = 4
+
+# status codes
+OK, EINVAL, ENOMEM, ECUDA, ENONFINITE, ENEGATIVE, EHLLC, ETIMEDOUT, ESTATE, ENOTSUP = range(10)
+STATUS_NAMES = {0: "OK", 1: "EINVAL", 2: "ENOMEM", 3: "ECUDA", 4: "ENONFINITE", 5: "ENEGATIVE", 6: "EHLLC",
+                7: "ETIMEDOUT", 8: "ESTATE", 9: "ENOTSUP"}
+
+MODEL = {"EULER": 0, "NS": 1}
+FLUX = {"LF": 0, "GODUNOV": 1, "HLLC": 2, "CD": 3}
+LIMITER = {"NONE": 0, "BJ": 1}
+EOS = {"IDEAL": 0, "MIX": 1}
+PRECISION = {"FP64": 0, "MIXED": 1}
+DT_MODE = {"TAU": 0, "CFL": 1}
+BND = {"BOUND_INLET": 0, "BOUND_OUTLET": 1, "BOUND_WALL_SLIP": 2, "BOUND_WALL_NO_SLIP": 3, "BOUND_MASS_FLOW": 4}
+CP_TYPE = {"CONST": 0, "POLYNOM": 1}
+LAW = {"CONST": 0, "SATHERLAND": 1}
+
+
+class Comp(C.Structure):
+    _fields_ = [("m", C.c_double), ("ml0", C.c_double), ("kp0", C.c_double), ("t0", C.c_double),
+                ("ts", C.c_double), ("sig", C.c_double), ("ek", C.c_double), ("h0", C.c_double),
+                ("cp_type", C.c_int), ("kp_type", C.c_int), ("ml_type", C.c_int), ("n_cp", C.c_int),
+                ("cp", C.c_double * MAX_CP)]
+
+
+class Bnd(C.Structure):
+    _fields_ = [("type", C.c_int), ("params", C.c_double * (7 + MAX_COMP))]
+
+
+class Config(C.Structure):
+    _fields_ = [("model", C.c_int), ("flux", C.c_int), ("limiter", C.c_int), ("eos", C.c_int),
+                ("precision", C.c_int), ("dt_mode", C.c_int), ("n_comp", C.c_int),
+                ("comp", Comp * MAX_COMP), ("n_bnd", C.c_int), ("bnd", Bnd * MAX_BND),
+                ("grav", C.c_double * 3), ("tau", C.c_double), ("cfl", C.c_double), ("t_ref", C.c_double),
+                ("use_visc", C.c_int), ("check_every", C.c_int)]
+
+
+class Mesh(C.Structure):
+    _fields_ = [("n_elem", C.c_int64), ("center", C.POINTER(C.c_double)), ("level", C.POINTER(C.c_int8)),
+                ("tree_len", C.c_double * 3), ("n_face", C.c_int64), ("face_elem", C.POINTER(C.c_int32)),
+                ("face_info", C.POINTER(C.c_uint8)), ("n_bface", C.c_int64),
+                ("bface_elem", C.POINTER(C.c_int32)), ("bface_face", C.POINTER(C.c_int8)),
+                ("bface_bnd", C.POINTER(C.c_int8))]
+
+
+# Every entry point declared in include/charm_gpu.h: (name, restype, argtypes).
+_P = C.c_void_p
+_I64P = C.POINTER(C.c_int64)
+_DP = C.POINTER(C.c_double)
+SIGNATURES = [
+    ("charm_gpu_version", C.c_char_p, []),
+    ("charm_gpu_last_error", C.c_char_p, []),
+    ("charm_gpu_create", C.c_int, [C.POINTER(_P), C.POINTER(Config), C.c_int]),
+    ("charm_gpu_destroy", C.c_int, [_P]),
+    ("charm_gpu_upload_mesh", C.c_int, [_P, C.POINTER(Mesh)]),
+    ("charm_gpu_set_state", C.c_int, [_P, _P, C.c_int]),
+    ("charm_gpu_get_state", C.c_int, [_P, _P, C.c_int]),
+    ("charm_gpu_step", C.c_int, [_P, C.c_double, _DP]),
+    ("charm_gpu_run", C.c_int, [_P, C.c_int, C.c_double]),
+    ("charm_gpu_get_dt", C.c_int, [_P, _DP]),
+    ("charm_gpu_residual", C.c_int, [_P, _P, C.c_int]),
+    ("charm_gpu_limit", C.c_int, [_P]),
+    ("charm_gpu_refine_flags", C.c_int, [_P, C.c_double, _P, _P]),
+    ("charm_gpu_set_stream", C.c_int, [_P, _P]),
+    ("charm_gpu_sync", C.c_int, [_P, C.c_double]),
+    ("charm_gpu_set_timing", C.c_int, [_P, C.c_int]),
+    ("charm_gpu_kernel_stats", C.c_int, [_P, _I64P, _DP]),
+    ("charm_gpu_reset_stats", C.c_int, [_P]),
+    ("charm_gpu_dims", C.c_int, [_P, _I64P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    ("charm_host_forest_new", C.c_int, [C.POINTER(_P), _P, _P, _P, _P, C.c_int]),
+    ("charm_host_forest_free", C.c_int, [_P]),
+    ("charm_host_forest_count", C.c_int64, [_P]),
+    ("charm_host_forest_set_bnd", C.c_int, [_P, _P]),
+    ("charm_host_forest_adapt", C.c_int, [_P, _P, C.c_int, C.c_int, _I64P]),
+    ("charm_host_forest_flatten", C.c_int, [_P, C.POINTER(Mesh)]),
+    ("charm_host_forest_leaves", C.c_int, [_P, _P, _P]),
+]
+
+_lib = None
+
+
+def load(path: str | None = None) -> C.CDLL:
+    """Load libcharm_gpu.so (building it first if this checkout has not)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        from . import build as _build
+        _build.build()
+    lib = C.CDLL(p)
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class CharmGpuError(RuntimeError):
+    def __init__(self, code: int, where: str):
+        msg = ""
+        if _lib is not None:
+            raw = _lib.charm_gpu_last_error()
+            msg = raw.decode() if raw else ""
+        super().__init__(f"{where}: {STATUS_NAMES.get(code, code)} ({msg})")
+        self.code = code
+
+
+def check(code: int, where: str) -> None:
+    if code != OK:
+        raise CharmGpuError(code, where)
+
+
+def ptr(a: np.ndarray, ctype=C.c_double):
+    return a.ctypes.data_as(C.POINTER(ctype))

@@ -1,0 +1,402 @@
+/*
+ * Host octree forest: see charm_forest.h.
+ *
+ * The operations mirror what CHARM_3D asks of p4est on its hot path:
+ *   - p4est_new_ext at a uniform level (src/charm_3d.c:36),
+ *   - face iteration with full / hanging sides (p4est_iterate, used by every
+ *     face callback, e.g. src/models/ns/charm_model_ns_conv.c:174-331),
+ *   - p4est_refine_ext / p4est_coarsen_ext (non-recursive) and
+ *     p4est_balance_ext(CHARM_CONNECT_FACE) with a replace callback
+ *     (src/charm_amr.c:601-608).
+ */
+#include "charm_forest.h"
+
+#include <stdlib.h>
+#include <string.h>
+
+/* ---- Morton keys ------------------------------------------------------- */
+
+static uint64_t spread3(uint32_t v)
+{
+    /* spread the low 21 bits of v so that bit i moves to bit 3i */
+    uint64_t x = v & 0x1fffffu;
+    x = (x | (x << 32)) & 0x1f00000000ffffull;
+    x = (x | (x << 16)) & 0x1f0000ff0000ffull;
+    x = (x | (x << 8))  & 0x100f00f00f00f00full;
+    x = (x | (x << 4))  & 0x10c30c30c30c30c3ull;
+    x = (x | (x << 2))  & 0x1249249249249249ull;
+    return x;
+}
+
+static uint64_t morton(int32_t x, int32_t y, int32_t z)
+{
+    /* x is the least significant coordinate, as in p4est */
+    return spread3((uint32_t) x) | (spread3((uint32_t) y) << 1) | (spread3((uint32_t) z) << 2);
+}
+
+static int leaf_cmp(const charm_leaf_t *a, const charm_leaf_t *b)
+{
+    if (a->tree != b->tree) return a->tree < b->tree ? -1 : 1;
+    uint64_t ka = morton(a->x, a->y, a->z), kb = morton(b->x, b->y, b->z);
+    if (ka != kb) return ka < kb ? -1 : 1;
+    if (a->level != b->level) return a->level < b->level ? -1 : 1;
+    return 0;
+}
+
+int charm_leaf_child_id(const charm_leaf_t *q)
+{
+    if (q->level == 0) return 0;
+    int32_t len = CHARM_FOREST_QLEN(q->level);
+    return ((q->x & len) ? 1 : 0) | ((q->y & len) ? 2 : 0) | ((q->z & len) ? 4 : 0);
+}
+
+/* ---- storage ------------------------------------------------------------ */
+
+static int reserve(charm_forest_t *f, int64_t n)
+{
+    if (n <= f->cap) return 0;
+    int64_t cap = f->cap ? f->cap : 64;
+    while (cap < n) cap *= 2;
+    charm_leaf_t *p = (charm_leaf_t *) realloc(f->leaf, (size_t) cap * sizeof(charm_leaf_t));
+    if (!p) return -1;
+    f->leaf = p;
+    f->cap = cap;
+    return 0;
+}
+
+int charm_forest_init_uniform(charm_forest_t *f, const int32_t ntree[3], const int32_t periodic[3],
+                              const double origin[3], const double tree_len[3], int level)
+{
+    memset(f, 0, sizeof(*f));
+    if (level < 0 || level > CHARM_FOREST_MAXLEVEL - 1) return -1;
+    for (int d = 0; d < 3; d++) {
+        if (ntree[d] < 1) return -1;
+        f->ntree[d] = ntree[d];
+        f->periodic[d] = periodic ? (periodic[d] != 0) : 0;
+        f->origin[d] = origin ? origin[d] : 0.0;
+        f->tree_len[d] = tree_len ? tree_len[d] : 1.0;
+    }
+    int64_t nt = (int64_t) ntree[0] * ntree[1] * ntree[2];
+    int64_t per = (int64_t) 1 << (3 * level);
+    if (reserve(f, nt * per)) return -1;
+    int32_t len = CHARM_FOREST_QLEN(level);
+    int64_t k = 0;
+    for (int32_t t = 0; t < nt; t++) {
+        for (int64_t m = 0; m < per; m++) {
+            /* de-interleave m into (i,j,l) at `level` bits each */
+            int32_t i = 0, j = 0, l = 0;
+            for (int b = 0; b < level; b++) {
+                i |= (int32_t) ((m >> (3 * b)) & 1) << b;
+                j |= (int32_t) ((m >> (3 * b + 1)) & 1) << b;
+                l |= (int32_t) ((m >> (3 * b + 2)) & 1) << b;
+            }
+            charm_leaf_t *q = &f->leaf[k++];
+            q->x = i * len; q->y = j * len; q->z = l * len;
+            q->tree = t; q->level = (int8_t) level;
+        }
+    }
+    f->n = k;
+    return 0;
+}
+
+void charm_forest_free(charm_forest_t *f)
+{
+    free(f->leaf);
+    memset(f, 0, sizeof(*f));
+}
+
+int charm_forest_copy(charm_forest_t *dst, const charm_forest_t *src)
+{
+    *dst = *src;
+    dst->leaf = NULL;
+    dst->cap = 0;
+    if (reserve(dst, src->n > 0 ? src->n : 1)) return -1;
+    memcpy(dst->leaf, src->leaf, (size_t) src->n * sizeof(charm_leaf_t));
+    return 0;
+}
+
+/* ---- queries ------------------------------------------------------------ */
+
+int64_t charm_forest_find(const charm_forest_t *f, int32_t t, int32_t x, int32_t y, int32_t z)
+{
+    if (x < 0 || y < 0 || z < 0 || x >= CHARM_FOREST_ROOT_LEN || y >= CHARM_FOREST_ROOT_LEN ||
+        z >= CHARM_FOREST_ROOT_LEN)
+        return -1;
+    uint64_t key = morton(x, y, z);
+    int64_t lo = 0, hi = f->n - 1, best = -1;
+    while (lo <= hi) {       /* last leaf with (tree,key) <= (t,key) */
+        int64_t mid = lo + (hi - lo) / 2;
+        const charm_leaf_t *q = &f->leaf[mid];
+        int le = (q->tree < t) || (q->tree == t && morton(q->x, q->y, q->z) <= key);
+        if (le) { best = mid; lo = mid + 1; } else hi = mid - 1;
+    }
+    if (best < 0) return -1;
+    const charm_leaf_t *q = &f->leaf[best];
+    if (q->tree != t) return -1;
+    int32_t len = CHARM_FOREST_QLEN(q->level);
+    if (x < q->x || x >= q->x + len || y < q->y || y >= q->y + len || z < q->z || z >= q->z + len) return -1;
+    return best;
+}
+
+/* Map tree-local point p (possibly one root length outside along axis d) to
+ * the tree that holds it.  Returns the tree id or -1 at a non-periodic
+ * boundary; *wrap receives -1/+1 when a periodic wrap was taken. */
+static int32_t locate_tree(const charm_forest_t *f, int32_t t, int d, int32_t p[3], int *wrap)
+{
+    int32_t ti[3];
+    ti[0] = t % f->ntree[0];
+    ti[1] = (t / f->ntree[0]) % f->ntree[1];
+    ti[2] = t / (f->ntree[0] * f->ntree[1]);
+    *wrap = 0;
+    if (p[d] < 0) {
+        p[d] += CHARM_FOREST_ROOT_LEN;
+        ti[d] -= 1;
+        if (ti[d] < 0) {
+            if (!f->periodic[d]) return -1;
+            ti[d] += f->ntree[d];
+            *wrap = -1;
+        }
+    } else if (p[d] >= CHARM_FOREST_ROOT_LEN) {
+        p[d] -= CHARM_FOREST_ROOT_LEN;
+        ti[d] += 1;
+        if (ti[d] >= f->ntree[d]) {
+            if (!f->periodic[d]) return -1;
+            ti[d] -= f->ntree[d];
+            *wrap = +1;
+        }
+    }
+    return ti[0] + f->ntree[0] * (ti[1] + f->ntree[1] * ti[2]);
+}
+
+void charm_forest_face_neighbor(const charm_forest_t *f, int64_t i, int face, charm_face_nb_t *nb)
+{
+    const charm_leaf_t *q = &f->leaf[i];
+    int d = face / 2, up = face & 1;
+    int32_t len = CHARM_FOREST_QLEN(q->level);
+    int32_t p[3] = {q->x, q->y, q->z};
+    p[d] += up ? len : -len;          /* lower corner of the same-size neighbour */
+    int wrap;
+    int32_t nt = locate_tree(f, q->tree, d, p, &wrap);
+    nb->wrap = wrap;
+    nb->idx[0] = nb->idx[1] = nb->idx[2] = nb->idx[3] = -1;
+    if (nt < 0) { nb->kind = CHARM_NB_BOUNDARY; return; }
+    int64_t j = charm_forest_find(f, nt, p[0], p[1], p[2]);
+    const charm_leaf_t *r = &f->leaf[j];
+    if (r->level == q->level) { nb->kind = CHARM_NB_SAME; nb->idx[0] = j; return; }
+    if (r->level < q->level) {
+        nb->kind = (r->level == q->level - 1) ? CHARM_NB_BIGGER : CHARM_NB_UNBALANCED;
+        nb->idx[0] = j;
+        return;
+    }
+    /* neighbour region is subdivided: the four children adjacent to our face */
+    int s = (d == 0) ? 1 : 0, tt = (d == 2) ? 1 : 2;
+    int32_t h = len / 2;
+    nb->kind = CHARM_NB_SMALLER;
+    for (int k = 0; k < 4; k++) {
+        int32_t c[3] = {p[0], p[1], p[2]};
+        if (!up) c[d] += h;          /* the half of the region touching our face */
+        c[s] += (k & 1) ? h : 0;
+        c[tt] += (k & 2) ? h : 0;
+        int64_t m = charm_forest_find(f, nt, c[0], c[1], c[2]);
+        nb->idx[k] = m;
+        if (f->leaf[m].level != q->level + 1) nb->kind = CHARM_NB_UNBALANCED;
+    }
+}
+
+void charm_forest_leaf_geom(const charm_forest_t *f, int64_t i, double c[3], double h[3])
+{
+    const charm_leaf_t *q = &f->leaf[i];
+    int32_t ti[3];
+    ti[0] = q->tree % f->ntree[0];
+    ti[1] = (q->tree / f->ntree[0]) % f->ntree[1];
+    ti[2] = q->tree / (f->ntree[0] * f->ntree[1]);
+    int32_t qc[3] = {q->x, q->y, q->z};
+    double inv = 1.0 / (double) CHARM_FOREST_ROOT_LEN;
+    int32_t len = CHARM_FOREST_QLEN(q->level);
+    for (int d = 0; d < 3; d++) {
+        h[d] = f->tree_len[d] * ((double) len * inv);
+        c[d] = f->origin[d] + f->tree_len[d] * ((double) ti[d] + ((double) qc[d] + 0.5 * (double) len) * inv);
+    }
+}
+
+/* ---- refine / coarsen / balance ---------------------------------------- */
+
+static void child_of(const charm_leaf_t *p, int c, charm_leaf_t *out)
+{
+    int32_t h = CHARM_FOREST_QLEN(p->level + 1);
+    out->x = p->x + ((c & 1) ? h : 0);
+    out->y = p->y + ((c & 2) ? h : 0);
+    out->z = p->z + ((c & 4) ? h : 0);
+    out->tree = p->tree;
+    out->level = (int8_t) (p->level + 1);
+}
+
+int64_t charm_forest_refine(charm_forest_t *f, const int8_t *flag, int maxlevel,
+                            charm_forest_replace_fn replace, void *user)
+{
+    if (maxlevel < 0 || maxlevel > CHARM_FOREST_MAXLEVEL - 1) maxlevel = CHARM_FOREST_MAXLEVEL - 1;
+    int64_t nref = 0;
+    for (int64_t i = 0; i < f->n; i++)
+        if (flag[i] && f->leaf[i].level < maxlevel) nref++;
+    if (nref == 0) return 0;
+    int64_t nn = f->n + 7 * nref;
+    charm_leaf_t *nl = (charm_leaf_t *) malloc((size_t) nn * sizeof(charm_leaf_t));
+    int64_t *map = (int64_t *) malloc((size_t) f->n * sizeof(int64_t));
+    if (!nl || !map) { free(nl); free(map); return -1; }
+    int64_t k = 0;
+    for (int64_t i = 0; i < f->n; i++) {
+        map[i] = k;
+        if (flag[i] && f->leaf[i].level < maxlevel) {
+            for (int c = 0; c < 8; c++) child_of(&f->leaf[i], c, &nl[k++]);
+        } else {
+            nl[k++] = f->leaf[i];
+        }
+    }
+    if (replace) {
+        for (int64_t i = 0; i < f->n; i++) {
+            if (flag[i] && f->leaf[i].level < maxlevel) {
+                int64_t in_idx[8];
+                for (int c = 0; c < 8; c++) in_idx[c] = map[i] + c;
+                replace(user, f->leaf, &i, 1, nl, in_idx, 8);
+            }
+        }
+    }
+    free(map);
+    free(f->leaf);
+    f->leaf = nl;
+    f->n = nn;
+    f->cap = nn;
+    return nref;
+}
+
+static int is_family(const charm_forest_t *f, int64_t i)
+{
+    const charm_leaf_t *q = &f->leaf[i];
+    if (q->level == 0 || i + 7 >= f->n || charm_leaf_child_id(q) != 0) return 0;
+    for (int c = 1; c < 8; c++) {
+        charm_leaf_t want;
+        charm_leaf_t parent = *q;
+        parent.level = (int8_t) (q->level - 1);
+        child_of(&parent, c, &want);
+        const charm_leaf_t *r = &f->leaf[i + c];
+        if (r->tree != want.tree || r->level != want.level || r->x != want.x || r->y != want.y || r->z != want.z)
+            return 0;
+    }
+    return 1;
+}
+
+int64_t charm_forest_coarsen(charm_forest_t *f, int minlevel, charm_forest_coarsen_fn pred,
+                             charm_forest_replace_fn replace, void *user)
+{
+    if (f->n < 8) return 0;
+    int8_t *merge = (int8_t *) calloc((size_t) f->n, 1);
+    if (!merge) return -1;
+    int64_t nm = 0;
+    for (int64_t i = 0; i + 7 < f->n; i++) {
+        if (!is_family(f, i)) continue;
+        if (f->leaf[i].level <= minlevel) { i += 7; continue; }
+        int64_t idx[8];
+        for (int c = 0; c < 8; c++) idx[c] = i + c;
+        if (pred && pred(user, f->leaf, idx)) { merge[i] = 1; nm++; }
+        i += 7;
+    }
+    if (nm == 0) { free(merge); return 0; }
+    int64_t nn = f->n - 7 * nm;
+    charm_leaf_t *nl = (charm_leaf_t *) malloc((size_t) nn * sizeof(charm_leaf_t));
+    int64_t *pidx = (int64_t *) malloc((size_t) nm * 2 * sizeof(int64_t));
+    if (!nl || !pidx) { free(nl); free(pidx); free(merge); return -1; }
+    int64_t k = 0, m = 0;
+    for (int64_t i = 0; i < f->n;) {
+        if (merge[i]) {
+            charm_leaf_t p = f->leaf[i];
+            p.level = (int8_t) (p.level - 1);
+            int32_t len = CHARM_FOREST_QLEN(p.level);
+            p.x &= ~(len - 1); p.y &= ~(len - 1); p.z &= ~(len - 1);
+            pidx[2 * m] = i; pidx[2 * m + 1] = k; m++;
+            nl[k++] = p;
+            i += 8;
+        } else {
+            nl[k++] = f->leaf[i++];
+        }
+    }
+    if (replace) {
+        for (int64_t j = 0; j < nm; j++) {
+            int64_t out_idx[8];
+            for (int c = 0; c < 8; c++) out_idx[c] = pidx[2 * j] + c;
+            replace(user, f->leaf, out_idx, 8, nl, &pidx[2 * j + 1], 1);
+        }
+    }
+    free(pidx);
+    free(merge);
+    free(f->leaf);
+    f->leaf = nl;
+    f->n = nn;
+    f->cap = nn;
+    return nm;
+}
+
+/* A leaf must be refined when some leaf two or more levels finer touches one
+ * of its faces: the same-size neighbour region is split and at least one of
+ * its four children next to our face is split again. */
+static int needs_split(const charm_forest_t *f, int64_t i)
+{
+    charm_face_nb_t nb;
+    for (int face = 0; face < 6; face++) {
+        charm_forest_face_neighbor(f, i, face, &nb);
+        if (nb.kind == CHARM_NB_UNBALANCED) {
+            /* UNBALANCED is reported from both sides; only the coarse side splits */
+            const charm_leaf_t *q = &f->leaf[i];
+            for (int k = 0; k < 4; k++)
+                if (nb.idx[k] >= 0 && f->leaf[nb.idx[k]].level > q->level + 1) return 1;
+        }
+    }
+    return 0;
+}
+
+int64_t charm_forest_balance_marks(const charm_forest_t *f, int8_t *flag)
+{
+    int64_t marks = 0;
+    for (int64_t i = 0; i < f->n; i++) {
+        flag[i] = (int8_t) needs_split(f, i);
+        marks += flag[i];
+    }
+    return marks;
+}
+
+int64_t charm_forest_balance(charm_forest_t *f, charm_forest_replace_fn replace, void *user)
+{
+    int64_t total = 0;
+    for (;;) {
+        int8_t *flag = (int8_t *) calloc((size_t) f->n, 1);
+        if (!flag) return -1;
+        int64_t marks = 0;
+        for (int64_t i = 0; i < f->n; i++) {
+            if (needs_split(f, i)) { flag[i] = 1; marks++; }
+        }
+        if (marks == 0) { free(flag); break; }
+        int64_t r = charm_forest_refine(f, flag, -1, replace, user);
+        free(flag);
+        if (r < 0) return -1;
+        total += r;
+    }
+    return total;
+}
+
+int charm_forest_is_balanced(const charm_forest_t *f)
+{
+    charm_face_nb_t nb;
+    for (int64_t i = 0; i < f->n; i++)
+        for (int face = 0; face < 6; face++) {
+            charm_forest_face_neighbor(f, i, face, &nb);
+            if (nb.kind == CHARM_NB_UNBALANCED) return 0;
+        }
+    return 1;
+}
+
+/* keep leaf_cmp referenced for debug builds that validate ordering */
+int charm_forest_check_sorted(const charm_forest_t *f)
+{
+    for (int64_t i = 1; i < f->n; i++)
+        if (leaf_cmp(&f->leaf[i - 1], &f->leaf[i]) >= 0) return 0;
+    return 1;
+}

@@ -1,0 +1,206 @@
+"""Host-side mirror of the reference's time-step plugin, over the C ABI.
+
+The reference registers ``timestep_single_fn`` / ``get_dt_fn`` and calls
+them from ``charm_timesteps`` (reference src/charm_timesteps.c:23-51).
+``Solver.step()`` / ``Solver.get_dt()`` are those two calls; ``Forest`` is the
+CPU octree (p4est's role) whose flattened arrays are uploaded after each
+adapt.  All compute happens in libcharm_gpu.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .case import Case
+
+
+class MeshArrays:
+    """Owned numpy copies of a flattened mesh plus the ctypes view of them."""
+
+    def __init__(self, m: abi.Mesh):
+        E, F, Fb = m.n_elem, m.n_face, m.n_bface
+        self.n_elem, self.n_face, self.n_bface = E, F, Fb
+        self.tree_len = tuple(m.tree_len)
+        self.center = np.ctypeslib.as_array(m.center, (3 * E,)).reshape(3, E).copy()
+        self.level = np.ctypeslib.as_array(m.level, (E,)).copy()
+        self.face_elem = np.ctypeslib.as_array(m.face_elem, (2 * F,)).reshape(2, F).copy() if F else np.zeros((2, 0), np.int32)
+        self.face_info = np.ctypeslib.as_array(m.face_info, (F,)).copy() if F else np.zeros(0, np.uint8)
+        self.bface_elem = np.ctypeslib.as_array(m.bface_elem, (Fb,)).copy() if Fb else np.zeros(0, np.int32)
+        self.bface_face = np.ctypeslib.as_array(m.bface_face, (Fb,)).copy() if Fb else np.zeros(0, np.int8)
+        self.bface_bnd = np.ctypeslib.as_array(m.bface_bnd, (Fb,)).copy() if Fb else np.zeros(0, np.int8)
+        self._struct = None
+
+    def struct(self) -> abi.Mesh:
+        m = abi.Mesh()
+        m.n_elem, m.n_face, m.n_bface = self.n_elem, self.n_face, self.n_bface
+        for d in range(3):
+            m.tree_len[d] = self.tree_len[d]
+        self._keep = [np.ascontiguousarray(a) for a in (self.center, self.level, self.face_elem, self.face_info,
+                                                          self.bface_elem, self.bface_face, self.bface_bnd)]
+        c, lv, fe, fi, be, bf, bb = self._keep
+        m.center = abi.ptr(c)
+        m.level = abi.ptr(lv, C.c_int8)
+        m.face_elem = abi.ptr(fe, C.c_int32)
+        m.face_info = abi.ptr(fi, C.c_uint8)
+        m.bface_elem = abi.ptr(be, C.c_int32)
+        m.bface_face = abi.ptr(bf, C.c_int8)
+        m.bface_bnd = abi.ptr(bb, C.c_int8)
+        self._struct = m
+        return m
+
+
+class Forest:
+    """The CPU octree of a brick case (charm_host_forest_* in the C ABI)."""
+
+    def __init__(self, case: Case, level: int | None = None):
+        self.lib = abi.load()
+        self.h = C.c_void_p()
+        nt = np.array(case.brick, np.int32)
+        per = np.array(case.periodic, np.int32)
+        org = np.array(case.origin, np.float64)
+        tl = np.array(case.tree_len, np.float64)
+        lv = case.level if level is None else level
+        abi.check(self.lib.charm_host_forest_new(C.byref(self.h), nt.ctypes.data, per.ctypes.data, org.ctypes.data,
+                                                 tl.ctypes.data, lv), "charm_host_forest_new")
+        bnd = np.array(case.bnd_of_side, np.int8)
+        abi.check(self.lib.charm_host_forest_set_bnd(self.h, bnd.ctypes.data), "charm_host_forest_set_bnd")
+
+    def __len__(self) -> int:
+        return int(self.lib.charm_host_forest_count(self.h))
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.charm_host_forest_free(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def flatten(self) -> MeshArrays:
+        m = abi.Mesh()
+        abi.check(self.lib.charm_host_forest_flatten(self.h, C.byref(m)), "charm_host_forest_flatten")
+        return MeshArrays(m)
+
+    def adapt(self, flags: np.ndarray, minlevel: int, maxlevel: int) -> int:
+        f = np.ascontiguousarray(flags, dtype=np.int8)
+        n = C.c_int64()
+        abi.check(self.lib.charm_host_forest_adapt(self.h, f.ctypes.data, minlevel, maxlevel, C.byref(n)),
+                  "charm_host_forest_adapt")
+        return n.value
+
+    def leaves(self) -> tuple[np.ndarray, np.ndarray]:
+        n = len(self)
+        q = np.empty((n, 4), np.int32)
+        lv = np.empty(n, np.int8)
+        abi.check(self.lib.charm_host_forest_leaves(self.h, q.ctypes.data, lv.ctypes.data), "charm_host_forest_leaves")
+        return q, lv
+
+
+class Solver:
+    """One GPU solver handle (charm_gpu_* in the C ABI)."""
+
+    def __init__(self, case: Case | abi.Config, device: int = 0):
+        self.lib = abi.load()
+        self.cfg = case.config() if isinstance(case, Case) else case
+        self.h = C.c_void_p()
+        abi.check(self.lib.charm_gpu_create(C.byref(self.h), C.byref(self.cfg), device), "charm_gpu_create")
+        self.n_var = 4 + self.cfg.n_comp
+        self.n_elem = 0
+        self.mesh = None
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.charm_gpu_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, mesh: MeshArrays) -> None:
+        self.mesh = mesh
+        s = mesh.struct()
+        abi.check(self.lib.charm_gpu_upload_mesh(self.h, C.byref(s)), "charm_gpu_upload_mesh")
+        self.n_elem = mesh.n_elem
+
+    def shape(self) -> tuple[int, int, int]:
+        return (self.n_var, abi.BASIS, self.n_elem)
+
+    def set_state(self, u) -> None:
+        if isinstance(u, np.ndarray):
+            a = np.ascontiguousarray(u, dtype=np.float64)
+            assert a.shape == self.shape(), (a.shape, self.shape())
+            abi.check(self.lib.charm_gpu_set_state(self.h, a.ctypes.data, 0), "charm_gpu_set_state")
+        else:   # device pointer (int)
+            abi.check(self.lib.charm_gpu_set_state(self.h, C.c_void_p(int(u)), 1), "charm_gpu_set_state")
+
+    def get_state(self, out=None) -> np.ndarray:
+        if out is not None and not isinstance(out, np.ndarray):
+            abi.check(self.lib.charm_gpu_get_state(self.h, C.c_void_p(int(out)), 1), "charm_gpu_get_state")
+            return out
+        a = out if out is not None else np.empty(self.shape())
+        abi.check(self.lib.charm_gpu_get_state(self.h, a.ctypes.data, 0), "charm_gpu_get_state")
+        return a
+
+    def step(self, dt: float = 0.0) -> float:
+        dto = C.c_double()
+        abi.check(self.lib.charm_gpu_step(self.h, dt, C.byref(dto)), "charm_gpu_step")
+        return dto.value
+
+    def run(self, nsteps: int, dt: float = 0.0) -> None:
+        abi.check(self.lib.charm_gpu_run(self.h, nsteps, dt), "charm_gpu_run")
+
+    def get_dt(self) -> float:
+        d = C.c_double()
+        abi.check(self.lib.charm_gpu_get_dt(self.h, C.byref(d)), "charm_gpu_get_dt")
+        return d.value
+
+    def residual(self) -> np.ndarray:
+        a = np.empty(self.shape())
+        abi.check(self.lib.charm_gpu_residual(self.h, a.ctypes.data, 0), "charm_gpu_residual")
+        return a
+
+    def limit(self) -> None:
+        abi.check(self.lib.charm_gpu_limit(self.h), "charm_gpu_limit")
+
+    def sync(self, timeout_s: float = 600.0) -> None:
+        abi.check(self.lib.charm_gpu_sync(self.h, timeout_s), "charm_gpu_sync")
+
+    def sync_status(self, timeout_s: float = 600.0) -> int:
+        return int(self.lib.charm_gpu_sync(self.h, timeout_s))
+
+    def set_stream(self, stream: int | None) -> None:
+        abi.check(self.lib.charm_gpu_set_stream(self.h, C.c_void_p(stream or 0)), "charm_gpu_set_stream")
+
+    def set_timing(self, on: bool) -> None:
+        abi.check(self.lib.charm_gpu_set_timing(self.h, 1 if on else 0), "charm_gpu_set_timing")
+
+    def kernel_stats(self) -> tuple[np.ndarray, np.ndarray]:
+        n = np.zeros(4, np.int64)
+        ms = np.zeros(4, np.float64)
+        abi.check(self.lib.charm_gpu_kernel_stats(self.h, n.ctypes.data_as(C.POINTER(C.c_int64)),
+                                                  ms.ctypes.data_as(C.POINTER(C.c_double))), "charm_gpu_kernel_stats")
+        return n, ms
+
+    def reset_stats(self) -> None:
+        abi.check(self.lib.charm_gpu_reset_stats(self.h), "charm_gpu_reset_stats")
+
+
+def build_case(case: Case, device: int = 0, precision: str | None = None):
+    """Forest + flattened mesh + solver with the case's initial state uploaded."""
+    if precision is not None:
+        case.precision = precision
+    forest = Forest(case)
+    mesh = forest.flatten()
+    solver = Solver(case, device)
+    solver.upload(mesh)
+    u0 = case.initial_state(mesh.center)
+    solver.set_state(u0)
+    return forest, mesh, solver, u0

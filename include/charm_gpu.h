@@ -1,0 +1,231 @@
+/*
+ * charm_gpu.h - C ABI of the GB300 DG time-step library (libcharm_gpu.so).
+ *
+ * The library replaces CHARM_3D's per-step model plugin, i.e. the pair
+ *   charm_timestep_single_fn_t  (reference include/charm_globals.h:239)
+ *   charm_get_timestep_fn_t     (reference include/charm_globals.h:240)
+ * registered by charm_model_ns_init / charm_model_euler_init
+ * (reference src/models/ns/charm_model_ns_init.cpp:79-88,
+ *  src/models/euler/charm_model_euler_init.cpp:14-18) and called once per
+ * step by charm_timesteps (reference src/charm_timesteps.c:42).
+ *
+ * The host keeps the octree (refine, 2:1 balance, coarsen) on the CPU.  After
+ * each adapt it flattens leaves and faces into the structure-of-arrays mesh
+ * below and uploads it; the conserved state then stays resident in HBM.
+ * The plugin function pointers of the reference (flux_fn, lim_fn, eos_fn,
+ * bnd_fn; reference include/charm_globals.h:122,236-238) become enum
+ * selectors in charm_gpu_config_t.
+ *
+ * Conventions
+ *   - Every entry point returns an int status (CHARM_GPU_OK == 0); none of
+ *     them exits the process (the reference's charm_abort calls exit(1),
+ *     src/charm_globals.c:459-470).
+ *   - State arrays are double [V][B][E]: variable-major, then basis
+ *     coefficient, then element (Morton order of the uploaded mesh).
+ *     V = 4 + n_comp in the reference's order (ru, rv, rw, re, rc_0..);
+ *     density is the sum of the partial densities rc_i.
+ *   - A handle is used by one host thread at a time; calls are ordered on the
+ *     handle's CUDA stream.  `stream` arguments are cudaStream_t values passed
+ *     as void* (NULL = the handle's own stream).
+ */
+#ifndef CHARM_GPU_H
+#define CHARM_GPU_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define CHARM_GPU_OK          0
+#define CHARM_GPU_EINVAL      1   /* bad argument or configuration */
+#define CHARM_GPU_ENOMEM      2   /* device or host allocation failed */
+#define CHARM_GPU_ECUDA       3   /* CUDA runtime error */
+#define CHARM_GPU_ENONFINITE  4   /* device error word: non-finite state */
+#define CHARM_GPU_ENEGATIVE   5   /* device error word: density or pressure <= 0 */
+#define CHARM_GPU_EHLLC       6   /* device error word: HLLC wave-speed order broken
+                                     (reference src/charm_fluxes.c:354-357 aborts) */
+#define CHARM_GPU_ETIMEDOUT   7   /* bounded host wait ran out */
+#define CHARM_GPU_ESTATE      8   /* call order (e.g. step before upload) */
+#define CHARM_GPU_ENOTSUP     9   /* configuration not implemented on the GPU */
+
+/* ---- selectors (reference strings in src/charm_init_yaml.cpp) ------------- */
+enum { CHARM_GPU_MODEL_EULER = 0,   /* "EULER": one forward-Euler stage
+                                       (src/models/euler/charm_model.c:454-540) */
+       CHARM_GPU_MODEL_NS    = 1 }; /* "NS": 3-stage SSP-RK with limiter per stage
+                                       (src/models/ns/charm_model.c:187-273) */
+
+enum { CHARM_GPU_FLUX_LF = 0, CHARM_GPU_FLUX_GODUNOV = 1, CHARM_GPU_FLUX_HLLC = 2,
+       CHARM_GPU_FLUX_CD = 3 };                        /* :352-368 */
+enum { CHARM_GPU_LIM_NONE = 0, CHARM_GPU_LIM_BJ = 1 };  /* :370-380 */
+enum { CHARM_GPU_EOS_IDEAL = 0, CHARM_GPU_EOS_MIX = 1 };/* :174-186 */
+enum { CHARM_GPU_PREC_FP64 = 0,     /* drop-in: all arithmetic in FP64 */
+       CHARM_GPU_PREC_MIXED = 1 };  /* FP32 residual, FP64 state/update/dt */
+enum { CHARM_GPU_DT_TAU = 0,        /* fixed TAU: the reference's get_dt_fn
+                                       (src/models/ns/charm_model.c:49) */
+       CHARM_GPU_DT_CFL = 1 };      /* CFL*volume/(|u|+c), min over cells (the
+                                       reference's unreachable code, :50-59) */
+
+/* boundary types, same numbering as charm_bnd_types_t
+ * (reference include/charm_globals.h:432-439) */
+enum { CHARM_GPU_BND_INLET = 0, CHARM_GPU_BND_OUTLET = 1, CHARM_GPU_BND_WALL_SLIP = 2,
+       CHARM_GPU_BND_WALL_NO_SLIP = 3, CHARM_GPU_BND_MASS_FLOW = 4 };
+
+/* component property laws (reference include/charm_globals.h:206-221) */
+enum { CHARM_GPU_CP_CONST = 0, CHARM_GPU_CP_POLYNOM = 1 };
+enum { CHARM_GPU_LAW_CONST = 0, CHARM_GPU_LAW_SUTHERLAND = 1 };
+
+#define CHARM_GPU_MAX_COMP   8    /* species on the device (reference: 128 slots) */
+#define CHARM_GPU_MAX_CP     8    /* cp polynomial coefficients */
+#define CHARM_GPU_MAX_BND   16    /* boundary-condition table entries */
+#define CHARM_GPU_BASIS      4    /* p1 Taylor basis (CHARM_BASE_FN_COUNT, charm_def.h:177) */
+
+typedef struct charm_gpu_comp {      /* charm_comp_t, include/charm_globals.h:224-240 */
+    double m, ml0, kp0, t0, ts, sig, ek, h0;
+    int    cp_type, kp_type, ml_type;
+    int    n_cp;
+    double cp[CHARM_GPU_MAX_CP];
+} charm_gpu_comp_t;
+
+typedef struct charm_gpu_bnd {       /* charm_bnd_t, include/charm_globals.h:441-448 */
+    int    type;
+    /* inlet: V.x V.y V.z T P; wall_no_slip: T; mass_flow: M P T CosX CosY CosZ P c_0.. */
+    double params[7 + CHARM_GPU_MAX_COMP];
+} charm_gpu_bnd_t;
+
+typedef struct charm_gpu_config {
+    int    model, flux, limiter, eos, precision, dt_mode;
+    int    n_comp;
+    charm_gpu_comp_t comp[CHARM_GPU_MAX_COMP];
+    int    n_bnd;
+    charm_gpu_bnd_t bnd[CHARM_GPU_MAX_BND];
+    double grav[3];      /* region gravity (charm_reg_t.grav), uniform over the mesh */
+    double tau;          /* control.TAU */
+    double cfl;          /* control.CFL */
+    double t_ref;        /* control.MODEL.t_ref */
+    int    use_visc;     /* must be 0 on this path (viscous terms not implemented) */
+    int    check_every;  /* steps between device error-word checks (0 = only at sync) */
+} charm_gpu_config_t;
+
+/*
+ * Flattened mesh.  Elements are the octree leaves in Morton order.  Each leaf
+ * is an axis-aligned box; `level` with `tree_len` gives its edge lengths
+ * h = tree_len / 2^level (the reference's dh, src/charm_geom.c:157-169).
+ *
+ * Interior faces join side 0 (lower coordinate along `dir`, its face 2*dir+1)
+ * and side 1 (its face 2*dir); this is p4est_iterate's side order.  A hanging
+ * face of a 2:1 mesh is stored as 4 sub-face records ("1-to-4 mortar"), each
+ * joining one small leaf with the big one; quadrature points then lie on the
+ * small leaf's face (src/models/euler/charm_model.c:282-285).
+ *
+ * face_info bits: 0-1 dir | 2-3 kind (0 conforming, 1 side 0 is the small
+ * leaf, 2 side 1 is the small leaf) | 4-5 sub (position of the small face in
+ * the big face: bit 4 along the lower tangential axis, bit 5 along the upper)
+ * | 6 periodic wrap.
+ */
+typedef struct charm_gpu_mesh {
+    int64_t        n_elem;
+    const double  *center;      /* [3][n_elem] */
+    const int8_t  *level;       /* [n_elem] */
+    double         tree_len[3];
+    int64_t        n_face;
+    const int32_t *face_elem;   /* [2][n_face] */
+    const uint8_t *face_info;   /* [n_face] */
+    int64_t        n_bface;
+    const int32_t *bface_elem;  /* [n_bface] */
+    const int8_t  *bface_face;  /* [n_bface] 0..5 (-x,+x,-y,+y,-z,+z) */
+    const int8_t  *bface_bnd;   /* [n_bface] index into charm_gpu_config_t.bnd */
+} charm_gpu_mesh_t;
+
+typedef struct charm_gpu_handle_s *charm_gpu_handle_t;
+
+/* Library version and the text of the last error on this thread. */
+const char *charm_gpu_version(void);
+const char *charm_gpu_last_error(void);
+
+/* Create a solver on CUDA device `device` (replaces charm_model_*_init). */
+int charm_gpu_create(charm_gpu_handle_t *h, const charm_gpu_config_t *cfg, int device);
+int charm_gpu_destroy(charm_gpu_handle_t h);
+
+/* Upload a flattened mesh (after each adapt).  The caller owns the arrays;
+ * the library copies them.  Resets the state to zero. */
+int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh);
+
+/* State in/out, layout [V][B][E] (reference charm_data_t.par.c,
+ * include/charm_globals.h:329-338).  `on_device` != 0: `u` is a device pointer. */
+int charm_gpu_set_state(charm_gpu_handle_t h, const double *u, int on_device);
+int charm_gpu_get_state(charm_gpu_handle_t h, double *u, int on_device);
+
+/* One time step (1 stage for EULER, 3 SSP-RK stages for NS, each followed by
+ * the limiter).  dt_in > 0 is used as the step; dt_in <= 0 takes the step
+ * from the configured dt mode.  *dt_out (may be NULL) receives the step
+ * taken.  Replaces charm_timestep_single_fn_t. */
+int charm_gpu_step(charm_gpu_handle_t h, double dt_in, double *dt_out);
+
+/* n steps back to back (no host round trip between them). */
+int charm_gpu_run(charm_gpu_handle_t h, int nsteps, double dt_in);
+
+/* Time step of the configured mode (replaces charm_get_timestep_fn_t). */
+int charm_gpu_get_dt(charm_gpu_handle_t h, double *dt);
+
+/* Residual int_*[V][B][E] of the current state: volume plus surface
+ * integrals, before M^-1 (reference int_ru..int_rc, charm_globals.h:403-407). */
+int charm_gpu_residual(charm_gpu_handle_t h, double *res, int on_device);
+
+/* Apply the configured limiter once to the current state. */
+int charm_gpu_limit(charm_gpu_handle_t h);
+
+/* Density-gradient refinement indicator of charm_adapt
+ * (reference src/charm_amr.c:12-48, 350-573): flags[e] = 1 where
+ * |grad rho|^2/12 * V^(5/3) > max_err^2 * V.  grad_out ([3][E], may be NULL)
+ * receives the gradient estimate. */
+int charm_gpu_refine_flags(charm_gpu_handle_t h, double max_err, int8_t *flags, double *grad_out);
+
+/* Stream control and synchronisation.  charm_gpu_sync waits at most
+ * timeout_s seconds (bounded polling) and then reports the device error word. */
+int charm_gpu_set_stream(charm_gpu_handle_t h, void *stream);
+int charm_gpu_sync(charm_gpu_handle_t h, double timeout_s);
+
+/* Kernel accounting for measurement: launches since the last reset, and the
+ * summed CUDA-event duration per kernel class when timing is enabled.
+ * Classes: 0 face, 1 cell (volume + gather + update), 2 limiter, 3 other. */
+int charm_gpu_set_timing(charm_gpu_handle_t h, int enable);
+int charm_gpu_kernel_stats(charm_gpu_handle_t h, int64_t launches[4], double ms[4]);
+int charm_gpu_reset_stats(charm_gpu_handle_t h);
+
+/* Element count, variables and basis size of the uploaded mesh. */
+int charm_gpu_dims(charm_gpu_handle_t h, int64_t *n_elem, int *n_var, int *n_basis);
+
+/* ---- host octree (the CPU side of the boundary) -------------------------- */
+
+typedef struct charm_host_forest_s *charm_host_forest_t;
+
+/* Brick of ntree[0]*ntree[1]*ntree[2] cubic trees, uniform `level`. */
+int charm_host_forest_new(charm_host_forest_t *f, const int32_t ntree[3], const int32_t periodic[3],
+                          const double origin[3], const double tree_len[3], int level);
+int charm_host_forest_free(charm_host_forest_t f);
+int64_t charm_host_forest_count(charm_host_forest_t f);
+
+/* Boundary id per domain side (-x,+x,-y,+y,-z,+z) used when flattening. */
+int charm_host_forest_set_bnd(charm_host_forest_t f, const int8_t bnd_of_side[6]);
+
+/* Refine flagged leaves (level < maxlevel), then coarsen complete families
+ * whose 8 flags are all -1 (level > minlevel), then 2:1 face-balance.
+ * Returns the new leaf count via *n_new. */
+int charm_host_forest_adapt(charm_host_forest_t f, const int8_t *flags, int minlevel, int maxlevel,
+                            int64_t *n_new);
+
+/* Flatten into a mesh view whose arrays live inside the forest object and
+ * stay valid until the next adapt/flatten/free. */
+int charm_host_forest_flatten(charm_host_forest_t f, charm_gpu_mesh_t *mesh);
+
+/* Leaf coordinates: qcoord[4*i..] = x, y, z, tree; level[i]. */
+int charm_host_forest_leaves(charm_host_forest_t f, int32_t *qcoord, int8_t *level);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CHARM_GPU_H */

@@ -1,0 +1,941 @@
+/*
+ * CPU restatement of CHARM_3D's explicit DG time step (test infrastructure).
+ *
+ * ORACLE ONLY.  Used by the tests, by __graft_entry__.smoke() as the checker
+ * and by bench.py's CPU-baseline leg; never part of the GPU product path.
+ *
+ * It runs on the same flattened mesh the GPU library consumes
+ * (charm_gpu_mesh_t, include/charm_gpu.h) and restates the reference's
+ * arithmetic in plain C99, FP64, following each reference function in order:
+ * per-element geometry and mass matrix (src/charm_geom.c), basis functions
+ * (src/charm_base_func.c), cons<->prim and EOS (src/charm_globals.c:183-223,
+ * src/charm_eos.c), fluxes (src/charm_fluxes.c), boundary conditions
+ * (src/charm_bnd_cond.c), volume and surface integrals
+ * (src/models/ns/charm_model_ns_conv.c), update and SSP-RK3
+ * (src/models/ns/charm_model.c) and the Barth-Jespersen limiter
+ * (src/limiters/charm_limiter_bj.c).  Unlike the GPU kernels it evaluates
+ * the basis from coordinates, builds and inverts each mass matrix, and
+ * takes cell means by quadrature, as the reference does.
+ *
+ * Pinned against the reference's own code (oracle/_ref, built by
+ * oracle/build_ref.py) and against the committed fixtures in tests/golden/.
+ *
+ * Compile with -ffp-contract=off so that x86 and Arm give the same bits.
+ */
+#include "charm_gpu.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define NB 4
+#define NQ 8
+#define NFQ 6
+#define MAXV (4 + CHARM_GPU_MAX_COMP)
+
+static const double gR = 8.31446261815324;   /* src/charm_eos.c:8 */
+static const double EPS = 1.e-12;            /* include/charm_def.h:158 */
+
+typedef struct {
+    double r, u, v, w, e, e_tot, p, t, cz, gam, cp, cv, m;
+    double c[CHARM_GPU_MAX_COMP];
+} prim_t;
+
+typedef struct {
+    double c[3], dh[3], vol;
+    double qgp[NQ][3], qgj[NQ];
+    double a_inv[NB][NB];
+} elem_geom_t;
+
+typedef struct oracle {
+    charm_gpu_config_t cfg;
+    int64_t E, F, Fb;
+    int V;
+    elem_geom_t *g;
+    int32_t *face_elem;
+    uint8_t *face_info;
+    int32_t *bface_elem;
+    int8_t *bface_face, *bface_bnd;
+    double *u, *u_old, *res;        /* [V][B][E] */
+    double *lim_nb;                 /* [E][6][V] limiter neighbour values */
+} oracle_t;
+
+/* ---- component laws and EOS --------------------------------------------- */
+
+static double comp_cp(const charm_gpu_comp_t *c, double t)
+{   /* charm_comp_calc_cp, src/charm_globals.c:603-625 (ml_type guards the polynomial) */
+    if (c->cp_type == CHARM_GPU_CP_CONST) return c->cp[0];
+    if (c->ml_type == CHARM_GPU_CP_POLYNOM) {
+        double res = 0., tt = 1.;
+        for (int i = 0; i < c->n_cp; i++) { res += tt * c->cp[i]; tt *= t; }
+        return res;
+    }
+    return c->cp[0];
+}
+
+static double comp_cp_dt(const charm_gpu_comp_t *c, double t)
+{   /* :628-648 */
+    double res = 0., tt = 1.;
+    for (int i = 1; i < c->n_cp; i++) { res += tt * c->cp[i] * i; tt *= t; }
+    return res;
+}
+
+static void calc_t(const oracle_t *o, prim_t *p)
+{   /* _calc_t, src/charm_eos.c:12-54 */
+    double m_ = 0.0, tt = 1.0;
+    for (int i = 0; i < o->cfg.n_comp; i++) m_ += p->c[i] / o->cfg.comp[i].m;
+    double rm = gR * m_;
+    for (int j = 0; j < 100; j++) {
+        double cp = 0.0, cp_dt = 0.0;
+        for (int i = 0; i < o->cfg.n_comp; i++) {
+            cp += p->c[i] * comp_cp(&o->cfg.comp[i], tt);
+            cp_dt += p->c[i] * comp_cp_dt(&o->cfg.comp[i], tt);
+        }
+        double ft = (cp - rm) * tt - p->e;
+        double ft_dt = (cp - rm) + cp_dt * tt;
+        double tt1 = tt - ft / ft_dt;
+        if (pow(tt1 - tt, 2) < EPS) { tt = tt1; break; }
+        tt = tt1;
+    }
+    p->t = tt;
+}
+
+static void eos_switch(prim_t *p, int flag)
+{   /* _charm_mat_eos_switch, src/charm_eos.c:57-96 */
+    switch (flag) {
+    case 0:
+        if (p->r < EPS) p->r = EPS;
+        p->p = p->r * p->e * (p->gam - 1);
+        p->cz = sqrt(p->gam * p->p / p->r);
+        break;
+    case 1:
+        if (p->r < EPS) p->r = EPS;
+        if (p->p < EPS) p->p = EPS;
+        p->e = p->p / (p->r * (p->gam - 1));
+        p->t = p->e / p->cv;
+        break;
+    case 2:
+        if (p->p < EPS) p->p = EPS;
+        p->r = p->p * p->m / (p->t * gR);
+        p->cz = sqrt(p->gam * p->p / p->r);
+        break;
+    case 3:
+        if (p->p < EPS) p->p = EPS;
+        p->r = p->p * p->m / (p->t * gR);
+        p->cz = sqrt(p->gam * p->p / p->r);
+        p->e = p->p / (p->r * (p->gam - 1));
+        break;
+    case 4:
+        if (p->r < EPS) p->r = EPS;
+        p->p = p->r * p->e * (p->gam - 1);
+        p->cz = sqrt(p->gam * p->p / p->r);
+        p->t = p->e / p->cv;
+        break;
+    }
+}
+
+static void eos(const oracle_t *o, prim_t *p, int flag)
+{   /* charm_mat_eos_ideal / charm_mat_eos_mix, src/charm_eos.c:98-148 */
+    const charm_gpu_comp_t *c0 = &o->cfg.comp[0];
+    if (c0->cp_type == CHARM_GPU_CP_POLYNOM && (flag == 1 || flag == 4)) calc_t(o, p);
+    double t = p->t;
+    if (o->cfg.eos == CHARM_GPU_EOS_IDEAL) {
+        p->cp = comp_cp(c0, t);
+        p->m = c0->m;
+    } else {
+        double M_ = 0.;
+        p->cp = 0.;
+        for (int i = 0; i < o->cfg.n_comp; i++) {
+            M_ += p->c[i] / o->cfg.comp[i].m;
+            p->cp += p->c[i] * comp_cp(&o->cfg.comp[i], t);
+        }
+        p->m = 1. / M_;
+    }
+    p->cv = p->cp - gR / p->m;
+    p->gam = p->cp / p->cv;
+    eos_switch(p, flag);
+}
+
+static void cons_to_prim(const oracle_t *o, const double *U, prim_t *p)
+{   /* charm_param_cons_to_prim, src/charm_globals.c:183-208 */
+    int nc = o->cfg.n_comp;
+    p->r = 0.;
+    for (int i = 0; i < nc; i++) p->r += U[4 + i];
+    p->u = U[0] / p->r;
+    p->v = U[1] / p->r;
+    p->w = U[2] / p->r;
+    p->e_tot = U[3] / p->r;
+    p->e = p->e_tot - 0.5 * (p->u * p->u + p->v * p->v + p->w * p->w);
+    for (int i = 0; i < nc; i++) {
+        p->c[i] = U[4 + i] / p->r;
+        if (p->c[i] < 0.) p->c[i] = 0.;
+        if (p->c[i] > 1.) p->c[i] = 1.;
+    }
+    p->t = 0.;
+    eos(o, p, 4);
+}
+
+static void prim_to_cons(const oracle_t *o, const prim_t *p, double *U)
+{   /* charm_param_prim_to_cons, :211-223 */
+    U[0] = p->r * p->u;
+    U[1] = p->r * p->v;
+    U[2] = p->r * p->w;
+    U[3] = p->r * (p->e + 0.5 * (p->u * p->u + p->v * p->v + p->w * p->w));
+    for (int i = 0; i < o->cfg.n_comp; i++) U[4 + i] = p->r * p->c[i];
+}
+
+/* ---- boundary conditions (src/charm_bnd_cond.c:21-146) -------------------- */
+
+static void bnd_cond(const oracle_t *o, int bid, const prim_t *in, prim_t *out, const double n[3])
+{
+    const charm_gpu_bnd_t *b = &o->cfg.bnd[bid];
+    *out = *in;
+    switch (b->type) {
+    case CHARM_GPU_BND_INLET:
+        out->u = b->params[0]; out->v = b->params[1]; out->w = b->params[2];
+        out->t = b->params[3]; out->p = b->params[4];
+        break;
+    case CHARM_GPU_BND_WALL_SLIP: {
+        double v[3] = {in->u, in->v, in->w};
+        double svn = v[0] * n[0] + v[1] * n[1] + v[2] * n[2];
+        double vv[3] = {n[0] * svn, n[1] * svn, n[2] * svn};
+        for (int i = 0; i < 3; i++) { v[i] -= vv[i]; v[i] -= vv[i]; }
+        out->u = v[0]; out->v = v[1]; out->w = v[2];
+        break;
+    }
+    case CHARM_GPU_BND_WALL_NO_SLIP: {
+        double v[3] = {in->u, in->v, in->w};
+        double svn = v[0] * n[0] + v[1] * n[1] + v[2] * n[2];
+        double vv[3] = {n[0] * svn, n[1] * svn, n[2] * svn};
+        for (int i = 0; i < 3; i++) v[i] -= vv[i];
+        out->u = v[0]; out->v = v[1]; out->w = v[2];
+        out->t = b->params[0];
+        break;
+    }
+    case CHARM_GPU_BND_MASS_FLOW: {
+        const double *par = b->params;
+        double flow_dir = n[0] * par[3] + n[1] * par[4] + n[2] * par[5];
+        if (flow_dir > 0.) {
+            double vel = out->u * n[0] + out->v * n[1] + out->w * n[2];
+            if (vel < out->cz) out->p = par[6];   /* stored pressure, not written back */
+        } else {
+            for (int i = 0; i < o->cfg.n_comp; i++) out->c[i] = par[7 + i];
+            eos(o, out, 0);
+            double v2 = out->u * out->u + out->v * out->v + out->w * out->w;
+            if (v2 > out->cz * out->cz) out->p = par[1];
+            double k = pow(par[0] * (out->cp - out->cv) / (out->p * flow_dir), 2.) / (2. * out->cp);
+            out->t = (-1 + sqrt(1.0 + 4.0 * k * par[2])) / (2. * k);
+            double vel = fabs(par[0] / (out->r * flow_dir));
+            out->u = par[3] * vel; out->v = par[4] * vel; out->w = par[5] * vel;
+        }
+        break;
+    }
+    default:
+        break;   /* outlet */
+    }
+    eos(o, out, 3);
+    out->e_tot = out->e + 0.5 * (out->u * out->u + out->v * out->v + out->w * out->w);
+}
+
+/* ---- fluxes (src/charm_fluxes.c) ------------------------------------------- */
+
+static void flux_lf(const oracle_t *o, const prim_t pr[2], const double n[3], double *q)
+{   /* :255-315 */
+    int fc = 4 + o->cfg.n_comp;
+    double ff[MAXV][2], uu[MAXV][2], vn[2];
+    for (int i = 0; i < 2; i++) {
+        vn[i] = pr[i].u * n[0] + pr[i].v * n[1] + pr[i].w * n[2];
+        uu[0][i] = pr[i].r * pr[i].u;
+        uu[1][i] = pr[i].r * pr[i].v;
+        uu[2][i] = pr[i].r * pr[i].w;
+        uu[3][i] = pr[i].r * pr[i].e_tot;
+        ff[0][i] = pr[i].r * vn[i] * pr[i].u + pr[i].p * n[0];
+        ff[1][i] = pr[i].r * vn[i] * pr[i].v + pr[i].p * n[1];
+        ff[2][i] = pr[i].r * vn[i] * pr[i].w + pr[i].p * n[2];
+        ff[3][i] = (pr[i].r * pr[i].e_tot + pr[i].p) * vn[i];
+        for (int j = 4; j < fc; j++) {
+            uu[j][i] = pr[i].r * pr[i].c[j - 4];
+            ff[j][i] = pr[i].r * vn[i] * pr[i].c[j - 4];
+        }
+    }
+    double a0 = fabs(vn[0]) + pr[0].cz, a1 = fabs(vn[1]) + pr[1].cz;
+    double alpha = a0 > a1 ? a0 : a1;
+    for (int i = 0; i < fc; i++) q[i] = 0.5 * (ff[i][1] + ff[i][0] - alpha * (uu[i][1] - uu[i][0]));
+}
+
+static void flux_cd(const oracle_t *o, const prim_t pr[2], const double n[3], double *q)
+{   /* :513-559 */
+    int fc = 4 + o->cfg.n_comp;
+    double ff[MAXV][2], vn[2];
+    for (int i = 0; i < 2; i++) {
+        vn[i] = pr[i].u * n[0] + pr[i].v * n[1] + pr[i].w * n[2];
+        ff[0][i] = pr[i].r * vn[i] * pr[i].u + pr[i].p * n[0];
+        ff[1][i] = pr[i].r * vn[i] * pr[i].v + pr[i].p * n[1];
+        ff[2][i] = pr[i].r * vn[i] * pr[i].w + pr[i].p * n[2];
+        ff[3][i] = (pr[i].r * pr[i].e_tot + pr[i].p) * vn[i];
+        for (int j = 4; j < fc; j++) ff[j][i] = pr[i].r * pr[i].c[j - 4] * vn[i];
+    }
+    for (int i = 0; i < fc; i++) q[i] = 0.5 * (ff[i][1] + ff[i][0]);
+}
+
+static void normal_frame(const double n[3], double nt[3][3])
+{   /* :458-488 */
+    nt[0][0] = n[0]; nt[0][1] = n[1]; nt[0][2] = n[2];
+    double ri = sqrt(n[0] * n[0] + n[1] * n[1]);
+    if (ri > EPS) {
+        nt[1][0] = -n[1] / ri; nt[1][1] = n[0] / ri; nt[1][2] = 0.;
+    } else {
+        ri = sqrt(n[1] * n[1] + n[2] * n[2]);
+        if (ri > EPS) {
+            nt[1][0] = 0.; nt[1][1] = -n[2] / ri; nt[1][2] = n[1] / ri;
+        } else {
+            ri = sqrt(n[0] * n[0] + n[2] * n[2]);
+            nt[1][0] = -n[2] / ri; nt[1][1] = 0.; nt[1][2] = n[0] / ri;
+        }
+    }
+    nt[2][0] = nt[0][1] * nt[1][2] - nt[0][2] * nt[1][1];
+    nt[2][1] = -nt[0][0] * nt[1][2] + nt[0][2] * nt[1][0];
+    nt[2][2] = nt[0][0] * nt[1][1] - nt[0][1] * nt[1][0];
+}
+
+#define F_HLLC_U(UK, FK, SK, SS, PK, RK, VK) (((SS) * ((SK) * (UK) - (FK)) + (SK) * ((PK) + (RK) * ((SK) - (VK)) * ((SS) - (VK)))) / ((SK) - (SS)))
+#define F_HLLC_V(UK, FK, SK, SS, PK, RK, VK) (((SS) * ((SK) * (UK) - (FK))) / ((SK) - (SS)))
+#define F_HLLC_E(UK, FK, SK, SS, PK, RK, VK) (((SS) * ((SK) * (UK) - (FK)) + (SK) * ((PK) + (RK) * ((SK) - (VK)) * ((SS) - (VK))) * (SS)) / ((SK) - (SS)))
+
+static void hllc_x(const oracle_t *o, const prim_t pr[2], double *qu, double *qv, double *qw, double *qe, double *qc)
+{   /* _charm_calc_flux_hllc_x_1, :324-437 */
+    int nc = o->cfg.n_comp;
+    double p_pvrs = 0.5 * (pr[0].p + pr[1].p) - 0.5 * (pr[1].u - pr[0].u) * 0.25 * (pr[0].r + pr[1].r) * (pr[0].cz + pr[1].cz);
+    double p_star = (p_pvrs > 0.) ? p_pvrs : 0.;
+    double ql = (p_star <= pr[0].p) ? 1 : sqrt(1. + (pr[0].gam + 1.) * (p_star / pr[0].p - 1.) / (2. * pr[0].gam));
+    double qr = (p_star <= pr[1].p) ? 1 : sqrt(1. + (pr[1].gam + 1.) * (p_star / pr[1].p - 1.) / (2. * pr[1].gam));
+    double sl = pr[0].u - pr[0].cz * ql, sr = pr[1].u + pr[1].cz * qr;
+    if (sl > sr) { double t = sl; sl = sr; sr = t; }
+    double s_star = pr[1].p - pr[0].p;
+    s_star += pr[0].r * pr[0].u * (sl - pr[0].u);
+    s_star -= pr[1].r * pr[1].u * (sr - pr[1].u);
+    s_star /= (pr[0].r * (sl - pr[0].u) - pr[1].r * (sr - pr[1].u));
+    if (s_star < sl) s_star = sl;
+    if (s_star > sr) s_star = sr;
+    if (sl >= 0.) {
+        *qu = pr[0].r * pr[0].u * pr[0].u + pr[0].p;
+        *qv = pr[0].r * pr[0].v * pr[0].u;
+        *qw = pr[0].r * pr[0].w * pr[0].u;
+        *qe = (pr[0].r * pr[0].e_tot + pr[0].p) * pr[0].u;
+        for (int i = 0; i < nc; i++) qc[i] = pr[0].r * pr[0].u * pr[0].c[i];
+    } else if (sr <= 0.) {
+        *qu = pr[1].r * pr[1].u * pr[1].u + pr[1].p;
+        *qv = pr[1].r * pr[1].v * pr[1].u;
+        *qw = pr[1].r * pr[1].w * pr[1].u;
+        *qe = (pr[1].r * pr[1].e_tot + pr[1].p) * pr[1].u;
+        for (int i = 0; i < nc; i++) qc[i] = pr[1].r * pr[1].u * pr[1].c[i];
+    } else {
+        int k = (s_star >= 0) ? 0 : 1;
+        double sk = k ? sr : sl;
+        const prim_t *p = &pr[k];
+        *qu = F_HLLC_U(p->r * p->u, p->r * p->u * p->u + p->p, sk, s_star, p->p, p->r, p->u);
+        *qv = F_HLLC_V(p->r * p->v, p->r * p->u * p->v, sk, s_star, p->p, p->r, p->u);
+        *qw = F_HLLC_V(p->r * p->w, p->r * p->u * p->w, sk, s_star, p->p, p->r, p->u);
+        *qe = F_HLLC_E(p->r * p->e_tot, (p->r * p->e_tot + p->p) * p->u, sk, s_star, p->p, p->r, p->u);
+        for (int i = 0; i < nc; i++) qc[i] = F_HLLC_V(p->r * p->c[i], p->r * p->c[i] * p->u, sk, s_star, p->p, p->r, p->u);
+    }
+}
+
+static void flux_hllc(const oracle_t *o, const prim_t pr[2], const double n[3], double *q)
+{   /* charm_calc_flux_hllc, :439-510 */
+    double nt[3][3];
+    normal_frame(n, nt);
+    prim_t pp[2];
+    for (int i = 0; i < 2; i++) {
+        double vv[3] = {pr[i].u, pr[i].v, pr[i].w};
+        pp[i] = pr[i];
+        pp[i].u = vv[0] * nt[0][0] + vv[1] * nt[0][1] + vv[2] * nt[0][2];
+        pp[i].v = vv[0] * nt[1][0] + vv[1] * nt[1][1] + vv[2] * nt[1][2];
+        pp[i].w = vv[0] * nt[2][0] + vv[1] * nt[2][1] + vv[2] * nt[2][2];
+    }
+    double fu, fv, fw;
+    hllc_x(o, pp, &fu, &fv, &fw, &q[3], &q[4]);
+    q[0] = fu * nt[0][0] + fv * nt[1][0] + fw * nt[2][0];
+    q[1] = fu * nt[0][1] + fv * nt[1][1] + fw * nt[2][1];
+    q[2] = fu * nt[0][2] + fv * nt[1][2] + fw * nt[2][2];
+}
+
+/* rim_orig, :8-180 */
+static void rim_orig(double *RI, double *EI, double *PI, double *UI, double *VI, double *WI, double RB, double PB,
+                     double UB, double VB, double WB, double RE, double PE, double UE, double VE, double WE, double gam)
+{
+    double AGAM = (gam - 1.0), DGAM = (2.0 / AGAM), EGAM = (AGAM / (gam + 1.0));
+    double GGAM = (sqrt(gam * AGAM)), HGAM = (AGAM / 2.0), FGAM = (3.0 * gam - 1.0), OGAM = (AGAM / (2.0 * gam));
+    double QGAM = (gam + 1.0), PGAM = (QGAM / (2.0 * gam)), RGAM = (4.0 * gam), SGAM = (gam * AGAM), TGAM = (QGAM / 2.0);
+    (void) EGAM;
+    double RF = 0, RS = 0, EF = 0, ES = 0, SBL, SFL, SSL, SEL, D, FS1, F1, ZNB, PKB, ZFB, PKE, ZNE, F2, FS2, ZFE, DP,
+           UBD, RUBD, UF = 0, UED, RUED, US = 0, PPE, PPB, P;
+    double eps = 1.e-5;
+    double CB = sqrt(gam * PB / RB), CE = sqrt(gam * PE / RE);
+    double EB = CB * CB / SGAM, EE = CE * CE / SGAM;
+    double RCB = RB * CB, RCE = RE * CE, DU = UB - UE;
+    if (DU < -2.0 * (CB + CE) / AGAM) {
+        RF = RS = EF = ES = 0.0;
+        SBL = UB - CB; SFL = UB + 2.0 * CB / AGAM; SSL = UE - 2.0 * CE / AGAM; SEL = UE + CE;
+    } else {
+        P = (PB * RCE + PE * RCB + DU * RCB * RCE) / (RCB + RCE);
+        int step = 0;
+        do {
+            if (P < eps) P = eps;
+            PPB = P / PB;
+            if (PB <= P) {
+                PKB = PGAM * PPB + OGAM; ZNB = RCB * sqrt(PKB);
+                F1 = (P - PB) / ZNB; FS1 = (QGAM * PPB + FGAM) / (RGAM * ZNB * PKB);
+            } else {
+                ZFB = CB * exp(log(PPB) * OGAM); F1 = DGAM * (ZFB - CB); FS1 = ZFB / (gam * P);
+            }
+            PPE = P / PE;
+            if (PE <= P) {
+                PKE = PGAM * PPE + OGAM; ZNE = RCE * sqrt(PKE);
+                F2 = (P - PE) / ZNE; FS2 = (QGAM * PPE + FGAM) / (RGAM * ZNE * PKE);
+            } else {
+                ZFE = CE * exp(log(PPE) * OGAM); F2 = DGAM * (ZFE - CE); FS2 = ZFE / (gam * P);
+            }
+            DP = (DU - F1 - F2) / (FS1 + FS2);
+            P = P + DP;
+        } while ((fabs(DU - F1 - F2) > eps) && (++step < 5000));
+        PPB = P / PB; PPE = P / PE;
+        ZFB = CB * exp(log(PPB) * OGAM); ZFE = CE * exp(log(PPE) * OGAM);
+        if (PB <= P) {
+            D = UB - sqrt((TGAM * P + HGAM * PB) / RB);
+            UBD = UB - D; RUBD = RB * UBD;
+            RF = RUBD * RUBD / (PB - P + RUBD * UBD);
+            UF = D + RUBD / RF; EF = P / (AGAM * RF); SBL = D; SFL = D;
+        } else {
+            EF = ZFB * ZFB / SGAM; UF = UB + DGAM * (CB - ZFB); RF = P / (AGAM * EF);
+            SBL = UB - CB; SFL = UF - ZFB;
+        }
+        if (PE <= P) {
+            D = UE + sqrt((TGAM * P + HGAM * PE) / RE);
+            UED = UE - D; RUED = RE * UED;
+            RS = RUED * RUED / (PE - P + RUED * UED);
+            US = D + RUED / RS; ES = P / (AGAM * RS); SEL = D; SSL = D;
+        } else {
+            ES = ZFE * ZFE / SGAM; US = UE - DGAM * (CE - ZFE); RS = P / (AGAM * ES);
+            SSL = US + ZFE; SEL = UE + CE;
+        }
+    }
+    if (SEL <= 0.0) { *RI = RE; *EI = EE; *UI = UE; *VI = VE; *WI = WE; *PI = AGAM * (*EI) * (*RI); return; }
+    if (SBL >= 0.0) { *RI = RB; *EI = EB; *UI = UB; *VI = VB; *WI = WB; *PI = AGAM * (*EI) * (*RI); return; }
+    if ((SSL >= 0.0) && (SFL <= 0.0)) {
+        if (US >= 0.0) { *RI = RF; *EI = EF; *UI = UF; *VI = VB; *WI = WB; }
+        else { *RI = RS; *EI = ES; *UI = US; *VI = VE; *WI = WE; }
+        *PI = AGAM * (*EI) * (*RI);
+        return;
+    }
+    if (SFL > 0.0) {
+        *UI = (UB + DGAM * GGAM * sqrt(EB)) / (1 + DGAM); *VI = VB; *WI = WB;
+        *EI = ((*UI) * (*UI)) / SGAM; *RI = RB * exp(log((*EI) / EB) * (1 / AGAM));
+    } else {
+        *UI = (UE - DGAM * GGAM * sqrt(EE)) / (1 + DGAM); *VI = VE; *WI = WE;
+        *EI = ((*UI) * (*UI)) / SGAM; *RI = RE * exp(log((*EI) / EE) * (1 / AGAM));
+    }
+    *PI = AGAM * (*EI) * (*RI);
+}
+
+static void flux_godunov(const oracle_t *o, const prim_t pr[2], const double n[3], double *q)
+{   /* the commented-out body of charm_calc_flux_godunov (:182-253), completed:
+       species upwinded by the interface mass flux, gamma of side 0 */
+    double nt[3][3], vn[2][3], ri, ei, pi, uu[3], uv[3];
+    normal_frame(n, nt);
+    for (int i = 0; i < 2; i++) {
+        double vv[3] = {pr[i].u, pr[i].v, pr[i].w};
+        for (int j = 0; j < 3; j++) vn[i][j] = vv[0] * nt[j][0] + vv[1] * nt[j][1] + vv[2] * nt[j][2];
+    }
+    rim_orig(&ri, &ei, &pi, &uu[0], &uu[1], &uu[2], pr[0].r, pr[0].p, vn[0][0], vn[0][1], vn[0][2], pr[1].r, pr[1].p,
+             vn[1][0], vn[1][1], vn[1][2], pr[0].gam);
+    for (int i = 0; i < 3; i++) {
+        uv[i] = 0.;
+        for (int j = 0; j < 3; j++) uv[i] += nt[j][i] * uu[j];
+    }
+    double qr = ri * uu[0];
+    q[0] = qr * uv[0] + pi * n[0];
+    q[1] = qr * uv[1] + pi * n[1];
+    q[2] = qr * uv[2] + pi * n[2];
+    q[3] = (ri * (ei + 0.5 * (uv[0] * uv[0] + uv[1] * uv[1] + uv[2] * uv[2])) + pi) * uu[0];
+    for (int i = 0; i < o->cfg.n_comp; i++) q[4 + i] = qr * ((qr >= 0.) ? pr[0].c[i] : pr[1].c[i]);
+}
+
+static void num_flux(const oracle_t *o, const prim_t pr[2], const double n[3], double *q)
+{
+    switch (o->cfg.flux) {
+    case CHARM_GPU_FLUX_LF: flux_lf(o, pr, n, q); break;
+    case CHARM_GPU_FLUX_HLLC: flux_hllc(o, pr, n, q); break;
+    case CHARM_GPU_FLUX_CD: flux_cd(o, pr, n, q); break;
+    default: flux_godunov(o, pr, n, q); break;
+    }
+}
+
+/* ---- geometry (src/charm_geom.c) ------------------------------------------ */
+
+static double base_func(const double *x, int k, const double c[3], const double dh[3])
+{   /* charm_base_func, src/charm_base_func.c:8-35 (p1) */
+    switch (k) {
+    case 0: return 1.;
+    case 1: return (x[0] - c[0]) / dh[0];
+    case 2: return (x[1] - c[1]) / dh[1];
+    case 3: return (x[2] - c[2]) / dh[2];
+    default: return 0.;
+    }
+}
+
+static double base_func_d(int k, int dir, const double dh[3])
+{   /* charm_base_func_dx/dy/dz, :38-125 (p1) */
+    return (k == dir + 1) ? 1. / dh[dir] : 0.;
+}
+
+static void matr_inv(double a_src[NB][NB], double am[NB][NB])
+{   /* Gauss-Jordan with partial pivoting, src/charm_globals.c:285-394 */
+    double a[NB][NB];
+    int mask[NB], i, j, ni, nj;
+    memcpy(a, a_src, sizeof(a));
+    for (i = 0; i < NB; i++)
+        for (j = 0; j < NB; j++) am[i][j] = (i == j) ? 1.0 : 0.0;
+    for (i = 0; i < NB; i++) mask[i] = i;
+    for (i = 0; i < NB; i++) {
+        int maxind = i;
+        double fmaxval = fabs(a[i][i]);
+        for (ni = i + 1; ni < NB; ni++)
+            if (fabs(fmaxval) <= fabs(a[ni][i])) { fmaxval = fabs(a[ni][i]); maxind = ni; }
+        if (i != maxind) {
+            for (nj = 0; nj < NB; nj++) {
+                double t = a[i][nj]; a[i][nj] = a[maxind][nj]; a[maxind][nj] = t;
+                t = am[i][nj]; am[i][nj] = am[maxind][nj]; am[maxind][nj] = t;
+            }
+            int ti = mask[i]; mask[i] = mask[maxind]; mask[maxind] = ti;
+        }
+        double aii = a[i][i];
+        for (j = 0; j < NB; j++) { a[i][j] /= aii; am[i][j] /= aii; }
+        for (ni = 0; ni < NB; ni++) {
+            if (ni == i) continue;
+            double fc = a[ni][i];
+            for (nj = 0; nj < NB; nj++) { a[ni][nj] -= fc * a[i][nj]; am[ni][nj] -= fc * am[i][nj]; }
+        }
+    }
+}
+
+static void trilinear(const double v[8][3], const double ref[3], double x[3])
+{   /* point of the trilinear map, src/charm_geom.c:47-66 */
+    double wx[2] = {1. - ref[0], 1. + ref[0]}, wy[2] = {1. - ref[1], 1. + ref[1]}, wz[2] = {1. - ref[2], 1. + ref[2]};
+    int vi = 0;
+    x[0] = x[1] = x[2] = 0.;
+    for (int iz = 0; iz < 2; iz++)
+        for (int iy = 0; iy < 2; iy++) {
+            double yf = wz[iz] * wy[iy];
+            for (int ix = 0; ix < 2; ix++) {
+                double xf = yf * wx[ix] / 8.;
+                for (int k = 0; k < 3; k++) x[k] += xf * v[vi][k];
+                vi++;
+            }
+        }
+}
+
+static void elem_vertices(const elem_geom_t *g, double v[8][3])
+{   /* box vertices, x fastest (charm_quad_get_vertices, src/charm_geom.c:12-31) */
+    for (int i = 0; i < 8; i++) {
+        v[i][0] = g->c[0] + ((i & 1) ? 0.5 : -0.5) * g->dh[0];
+        v[i][1] = g->c[1] + ((i & 2) ? 0.5 : -0.5) * g->dh[1];
+        v[i][2] = g->c[2] + ((i & 4) ? 0.5 : -0.5) * g->dh[2];
+    }
+}
+
+static void elem_geom(elem_geom_t *g, const double c[3], const double h[3])
+{   /* charm_geom_quad_calc for a box (src/charm_geom.c:496-530) */
+    double v[8][3];
+    const double s3 = 1. / sqrt(3.);
+    for (int k = 0; k < 3; k++) { g->c[k] = c[k]; g->dh[k] = h[k]; }
+    elem_vertices(g, v);
+    g->vol = 0.;
+    for (int i = 0; i < NQ; i++) {
+        double ref[3] = {(i & 1) ? s3 : -s3, (i & 2) ? s3 : -s3, (i & 4) ? s3 : -s3};
+        trilinear(v, ref, g->qgp[i]);
+        g->qgj[i] = (h[0] * 0.5) * (h[1] * 0.5) * (h[2] * 0.5);   /* det J of a box */
+        g->vol += g->qgj[i];
+    }
+    double a[NB][NB];
+    for (int i = 0; i < NB; i++)
+        for (int j = 0; j < NB; j++) {
+            a[i][j] = 0.;
+            for (int q = 0; q < NQ; q++)
+                a[i][j] += g->qgj[q] * base_func(g->qgp[q], i, g->c, g->dh) * base_func(g->qgp[q], j, g->c, g->dh);
+        }
+    matr_inv(a, g->a_inv);
+}
+
+/* Face quadrature points of face f of a box (_charm_face_calc_gp_by_tri,
+ * src/charm_geom.c:443-494) and the per-point weight gw*gj. */
+static void face_points(const elem_geom_t *g, int f, double gp[NFQ][3], double gwj[NFQ])
+{
+    static const int ftv[6][4] = {{0, 2, 4, 6}, {1, 3, 5, 7}, {0, 1, 4, 5}, {2, 3, 6, 7}, {0, 1, 2, 3}, {4, 5, 6, 7}};
+    double v8[8][3], v[4][3];
+    elem_vertices(g, v8);
+    for (int i = 0; i < 4; i++)
+        for (int k = 0; k < 3; k++) v[i][k] = v8[ftv[f][i]][k];
+    const double a = 2.0 / 3.0, b = 1.0 / 6.0;
+    for (int i = 0; i < 2; i++) {
+        double pt[3][3];
+        for (int j = 0; j < 3; j++)
+            for (int k = 0; k < 3; k++) pt[j][k] = v[i + j][k];
+        double a1 = pt[0][0] - pt[2][0], a2 = pt[1][0] - pt[2][0], a3 = pt[2][0];
+        double b1 = pt[0][1] - pt[2][1], b2 = pt[1][1] - pt[2][1], b3 = pt[2][1];
+        double c1 = pt[0][2] - pt[2][2], c2 = pt[1][2] - pt[2][2], c3 = pt[2][2];
+        double E_ = a1 * a1 + b1 * b1 + c1 * c1, F_ = a2 * a2 + b2 * b2 + c2 * c2, G_ = a1 * a2 + b1 * b2 + c1 * c2;
+        double gj = sqrt(E_ * F_ - G_ * G_);
+        gp[3 * i + 0][0] = a * a1 + b * a2 + a3; gp[3 * i + 0][1] = a * b1 + b * b2 + b3; gp[3 * i + 0][2] = a * c1 + b * c2 + c3;
+        gp[3 * i + 1][0] = b * a1 + a * a2 + a3; gp[3 * i + 1][1] = b * b1 + a * b2 + b3; gp[3 * i + 1][2] = b * c1 + a * c2 + c3;
+        gp[3 * i + 2][0] = b * a1 + b * a2 + a3; gp[3 * i + 2][1] = b * b1 + b * b2 + b3; gp[3 * i + 2][2] = b * c1 + b * c2 + c3;
+        for (int j = 0; j < 3; j++) gwj[3 * i + j] = gj * (1. / 6.);
+    }
+}
+
+/* Face normal of face f made to point out of the element (src/charm_geom.c:181-211
+ * and the flip of src/models/euler/charm_model.c:332-344). */
+static void outward_normal(int f, double n[3])
+{
+    n[0] = n[1] = n[2] = 0.;
+    n[f / 2] = (f & 1) ? 1. : -1.;
+}
+
+/* ---- state helpers ---------------------------------------------------------- */
+
+static void get_fields(const oracle_t *o, const double *u, int64_t e, const double c[3], const double dh[3],
+                       const double *x, double *U)
+{   /* charm_get_fields, src/charm_base_func.c:198-211 */
+    for (int v = 0; v < o->V; v++) {
+        double r = 0.;
+        for (int k = 0; k < NB; k++) r += u[(v * NB + k) * o->E + e] * base_func(x, k, c, dh);
+        U[v] = r;
+    }
+}
+
+static void get_fields_avg(const oracle_t *o, const double *u, int64_t e, double *U)
+{   /* charm_get_fields_avg, :214-240 */
+    const elem_geom_t *g = &o->g[e];
+    for (int v = 0; v < o->V; v++) U[v] = 0.;
+    for (int q = 0; q < NQ; q++) {
+        double Uq[MAXV];
+        double gjw = g->qgj[q] / g->vol;
+        get_fields(o, u, e, g->c, g->dh, g->qgp[q], Uq);
+        for (int v = 0; v < o->V; v++) U[v] += Uq[v] * gjw;
+    }
+}
+
+/* centre of the side-1 element as seen from side 0 (periodic wraps put the
+ * neighbour one period away; use the adjacent image) */
+static void side1_center(const oracle_t *o, int64_t f, double c1[3])
+{
+    const int32_t e0 = o->face_elem[f], e1 = o->face_elem[o->F + f];
+    const int d = o->face_info[f] & 3;
+    memcpy(c1, o->g[e1].c, sizeof(double) * 3);
+    if (o->face_info[f] & 0x40) c1[d] = o->g[e0].c[d] + 0.5 * (o->g[e0].dh[d] + o->g[e1].dh[d]);
+}
+
+/* ---- residual (src/models/ns/charm_model_ns_conv.c) ------------------------ */
+
+static void residual(oracle_t *o, const double *u, double *res)
+{
+    const int64_t E = o->E;
+    const int V = o->V;
+    memset(res, 0, sizeof(double) * (size_t) V * NB * (size_t) E);
+    /* volume integrals (:23-89) */
+    for (int64_t e = 0; e < E; e++) {
+        const elem_geom_t *g = &o->g[e];
+        for (int q = 0; q < NQ; q++) {
+            const double *x = g->qgp[q];
+            double U[MAXV];
+            prim_t p;
+            get_fields(o, u, e, g->c, g->dh, x, U);
+            cons_to_prim(o, U, &p);
+            double F[3][MAXV];
+            F[0][0] = U[0] * p.u + p.p; F[0][1] = U[0] * p.v; F[0][2] = U[0] * p.w; F[0][3] = U[0] * p.e_tot + p.p * p.u;
+            F[1][0] = U[1] * p.u; F[1][1] = U[1] * p.v + p.p; F[1][2] = U[1] * p.w; F[1][3] = U[1] * p.e_tot + p.p * p.v;
+            F[2][0] = U[2] * p.u; F[2][1] = U[2] * p.v; F[2][2] = U[2] * p.w + p.p; F[2][3] = U[2] * p.e_tot + p.p * p.w;
+            for (int i = 0; i < o->cfg.n_comp; i++) {
+                F[0][4 + i] = U[0] * p.c[i]; F[1][4 + i] = U[1] * p.c[i]; F[2][4 + i] = U[2] * p.c[i];
+            }
+            const double gjw = g->qgj[q];
+            for (int k = 0; k < NB; k++) {
+                double px = base_func_d(k, 0, g->dh) * gjw, py = base_func_d(k, 1, g->dh) * gjw,
+                       pz = base_func_d(k, 2, g->dh) * gjw, phi = base_func(x, k, g->c, g->dh) * gjw;
+                for (int v = 0; v < V; v++) {
+                    double gr = (v < 3) ? p.r * o->cfg.grav[v] * phi : 0.;
+                    res[(v * NB + k) * E + e] -= (F[0][v] * px + F[1][v] * py + F[2][v] * pz) + gr;
+                }
+            }
+        }
+    }
+    /* interior faces, conforming and hanging (:174-331) */
+    for (int64_t f = 0; f < o->F; f++) {
+        const int32_t e[2] = {o->face_elem[f], o->face_elem[o->F + f]};
+        const int d = o->face_info[f] & 3, kind = (o->face_info[f] >> 2) & 3;
+        double c1[3];
+        side1_center(o, f, c1);
+        const double *cs[2] = {o->g[e[0]].c, c1};
+        /* points on side 0's face (conforming / side 0 small) or side 1's face */
+        const int hs = (kind == 2) ? 1 : 0;
+        elem_geom_t pg = o->g[e[hs]];
+        memcpy(pg.c, cs[hs], sizeof(double) * 3);
+        double gp[NFQ][3], gwj[NFQ], n[3];
+        face_points(&pg, hs ? 2 * d : 2 * d + 1, gp, gwj);
+        outward_normal(2 * d + 1, n);
+        for (int q = 0; q < NFQ; q++) {
+            prim_t pr[2];
+            for (int s = 0; s < 2; s++) {
+                double U[MAXV];
+                get_fields(o, u, e[s], cs[s], o->g[e[s]].dh, gp[q], U);
+                cons_to_prim(o, U, &pr[s]);
+            }
+            double qf[MAXV];
+            num_flux(o, pr, n, qf);
+            for (int s = 0; s < 2; s++)
+                for (int k = 0; k < NB; k++) {
+                    double bfv = (s ? -1. : 1.) * base_func(gp[q], k, cs[s], o->g[e[s]].dh) * gwj[q];
+                    for (int v = 0; v < V; v++) res[(v * NB + k) * E + e[s]] += qf[v] * bfv;
+                }
+        }
+    }
+    /* boundary faces (:96-171) */
+    for (int64_t j = 0; j < o->Fb; j++) {
+        const int32_t e = o->bface_elem[j];
+        const int f = o->bface_face[j], bid = o->bface_bnd[j];
+        const elem_geom_t *g = &o->g[e];
+        double gp[NFQ][3], gwj[NFQ], n[3];
+        face_points(g, f, gp, gwj);
+        outward_normal(f, n);
+        for (int q = 0; q < NFQ; q++) {
+            double U[MAXV];
+            prim_t pr[2];
+            get_fields(o, u, e, g->c, g->dh, gp[q], U);
+            cons_to_prim(o, U, &pr[0]);
+            bnd_cond(o, bid, &pr[0], &pr[1], n);
+            double qf[MAXV];
+            num_flux(o, pr, n, qf);
+            for (int k = 0; k < NB; k++) {
+                double bfv = base_func(gp[q], k, g->c, g->dh) * gwj[q];
+                for (int v = 0; v < V; v++) res[(v * NB + k) * E + e] += qf[v] * bfv;
+            }
+        }
+    }
+}
+
+/* u -= dt * A^-1 * int (src/models/ns/charm_model.c:68-99) */
+static void update(oracle_t *o, double *u, const double *res, double dt)
+{
+    for (int64_t e = 0; e < o->E; e++)
+        for (int v = 0; v < o->V; v++) {
+            double rhs[NB];
+            for (int i = 0; i < NB; i++) {
+                rhs[i] = 0.;
+                for (int j = 0; j < NB; j++) rhs[i] += o->g[e].a_inv[i][j] * res[(v * NB + j) * o->E + e];
+            }
+            for (int i = 0; i < NB; i++) u[(v * NB + i) * o->E + e] -= dt * rhs[i];
+        }
+}
+
+/* ---- Barth-Jespersen limiter (src/limiters/charm_limiter_bj.c) ------------- */
+
+static void limiter(oracle_t *o, double *u)
+{
+    const int64_t E = o->E;
+    const int V = o->V;
+    /* neighbour values per (element, face) */
+    double *self = (double *) malloc(sizeof(double) * (size_t) V * (size_t) E);
+    for (int64_t e = 0; e < E; e++) get_fields_avg(o, u, e, &self[e * V]);   /* init (:11-27) */
+    /* boundary (:30-92) */
+    for (int64_t j = 0; j < o->Fb; j++) {
+        const int32_t e = o->bface_elem[j];
+        const int f = o->bface_face[j];
+        double n[3];
+        prim_t pr[2];
+        outward_normal(f, n);
+        cons_to_prim(o, &self[e * V], &pr[0]);
+        bnd_cond(o, o->bface_bnd[j], &pr[0], &pr[1], n);
+        prim_to_cons(o, &pr[1], &o->lim_nb[(e * 6 + f) * V]);
+    }
+    /* interior (:95-223) */
+    for (int64_t f = 0; f < o->F; f++) {
+        const int32_t e0 = o->face_elem[f], e1 = o->face_elem[o->F + f];
+        const int d = o->face_info[f] & 3, kind = (o->face_info[f] >> 2) & 3;
+        if (kind == 0) {
+            memcpy(&o->lim_nb[(e0 * 6 + 2 * d + 1) * V], &self[e1 * V], sizeof(double) * V);
+            memcpy(&o->lim_nb[(e1 * 6 + 2 * d) * V], &self[e0 * V], sizeof(double) * V);
+            continue;
+        }
+        /* hanging: each of the 4 records; the big side is done once (sub 0) */
+        const int32_t small = (kind == 1) ? e0 : e1, big = (kind == 1) ? e1 : e0;
+        const int fs = (kind == 1) ? 2 * d + 1 : 2 * d, fbig = (kind == 1) ? 2 * d : 2 * d + 1;
+        double cb[MAXV];
+        get_fields(o, u, big, o->g[big].c, o->g[big].dh, o->g[big].c, cb);   /* value at the big centre */
+        memcpy(&o->lim_nb[(small * 6 + fs) * V], cb, sizeof(double) * V);
+        if (((o->face_info[f] >> 4) & 3) == 0) {
+            double acc[MAXV], svol = 0.;
+            for (int v = 0; v < V; v++) acc[v] = 0.;
+            for (int k = 0; k < 4; k++) {
+                const int64_t fk = f + k;
+                const int32_t sk = (((o->face_info[fk] >> 2) & 3) == 1) ? o->face_elem[fk] : o->face_elem[o->F + fk];
+                double cj[MAXV];
+                get_fields(o, u, sk, o->g[sk].c, o->g[sk].dh, o->g[sk].c, cj);
+                double vol = o->g[sk].vol;
+                svol += vol;
+                for (int v = 0; v < V; v++) acc[v] += cj[v] * vol;
+            }
+            for (int v = 0; v < V; v++) acc[v] /= svol;
+            memcpy(&o->lim_nb[(big * 6 + fbig) * V], acc, sizeof(double) * V);
+        }
+    }
+    /* calc (:241-315) */
+    for (int64_t e = 0; e < E; e++) {
+        const elem_geom_t *g = &o->g[e];
+        double umin[MAXV], umax[MAXV], psi[MAXV], v8[8][3];
+        const double *u0 = &self[e * V];
+        for (int v = 0; v < V; v++) {
+            umin[v] = umax[v] = u0[v];
+            for (int f = 0; f < 6; f++) {
+                double x = o->lim_nb[(e * 6 + f) * V + v];
+                if (umin[v] > x) umin[v] = x;
+                if (umax[v] < x) umax[v] = x;
+            }
+            psi[v] = 1.;
+        }
+        elem_vertices(g, v8);
+        for (int i = 0; i < 8; i++) {
+            double fv[MAXV];
+            get_fields(o, u, e, g->c, g->dh, v8[i], fv);
+            for (int v = 0; v < V; v++) {
+                double pt = 1.;
+                if (fabs(fv[v] - u0[v]) > EPS) {
+                    if (fv[v] - u0[v] > 0) { double r = (umax[v] - u0[v]) / (fv[v] - u0[v]); pt = r < 1 ? r : 1; }
+                    else if (fv[v] - u0[v] < 0) { double r = (umin[v] - u0[v]) / (fv[v] - u0[v]); pt = r < 1 ? r : 1; }
+                }
+                if (pt < psi[v]) psi[v] = pt;
+            }
+        }
+        for (int k = 1; k < NB; k++)
+            for (int v = 0; v < V; v++) u[(v * NB + k) * E + e] *= psi[v];
+    }
+    free(self);
+}
+
+/* ---- API --------------------------------------------------------------------- */
+
+void oracle_free(oracle_t *o)
+{
+    if (!o) return;
+    free(o->g); free(o->face_elem); free(o->face_info); free(o->bface_elem); free(o->bface_face); free(o->bface_bnd);
+    free(o->u); free(o->u_old); free(o->res); free(o->lim_nb);
+    free(o);
+}
+
+oracle_t *oracle_new(const charm_gpu_config_t *cfg, const charm_gpu_mesh_t *m)
+{
+    oracle_t *o = (oracle_t *) calloc(1, sizeof(oracle_t));
+    if (!o) return NULL;
+    o->cfg = *cfg;
+    o->E = m->n_elem; o->F = m->n_face; o->Fb = m->n_bface;
+    o->V = 4 + cfg->n_comp;
+    const size_t st = sizeof(double) * (size_t) o->V * NB * (size_t) o->E;
+    o->g = (elem_geom_t *) malloc(sizeof(elem_geom_t) * (size_t) o->E);
+    o->face_elem = (int32_t *) malloc(sizeof(int32_t) * 2 * (size_t) (o->F + 1));
+    o->face_info = (uint8_t *) malloc((size_t) o->F + 1);
+    o->bface_elem = (int32_t *) malloc(sizeof(int32_t) * (size_t) (o->Fb + 1));
+    o->bface_face = (int8_t *) malloc((size_t) o->Fb + 1);
+    o->bface_bnd = (int8_t *) malloc((size_t) o->Fb + 1);
+    o->u = (double *) calloc(1, st);
+    o->u_old = (double *) calloc(1, st);
+    o->res = (double *) calloc(1, st);
+    o->lim_nb = (double *) calloc((size_t) o->E * 6 * (size_t) o->V, sizeof(double));
+    if (!o->g || !o->face_elem || !o->face_info || !o->bface_elem || !o->bface_face || !o->bface_bnd || !o->u ||
+        !o->u_old || !o->res || !o->lim_nb) {
+        oracle_free(o);
+        return NULL;
+    }
+    for (int64_t e = 0; e < o->E; e++) {
+        double c[3] = {m->center[e], m->center[o->E + e], m->center[2 * o->E + e]}, h[3];
+        for (int d = 0; d < 3; d++) h[d] = ldexp(m->tree_len[d], -m->level[e]);
+        elem_geom(&o->g[e], c, h);
+    }
+    memcpy(o->face_elem, m->face_elem, sizeof(int32_t) * 2 * (size_t) o->F);
+    memcpy(o->face_info, m->face_info, (size_t) o->F);
+    memcpy(o->bface_elem, m->bface_elem, sizeof(int32_t) * (size_t) o->Fb);
+    memcpy(o->bface_face, m->bface_face, (size_t) o->Fb);
+    memcpy(o->bface_bnd, m->bface_bnd, (size_t) o->Fb);
+    return o;
+}
+
+int oracle_set_state(oracle_t *o, const double *u)
+{
+    memcpy(o->u, u, sizeof(double) * (size_t) o->V * NB * (size_t) o->E);
+    return 0;
+}
+
+int oracle_get_state(oracle_t *o, double *u)
+{
+    memcpy(u, o->u, sizeof(double) * (size_t) o->V * NB * (size_t) o->E);
+    return 0;
+}
+
+int oracle_residual(oracle_t *o, double *res)
+{
+    residual(o, o->u, res);
+    return 0;
+}
+
+int oracle_limit(oracle_t *o)
+{
+    if (o->cfg.limiter == CHARM_GPU_LIM_BJ) limiter(o, o->u);
+    return 0;
+}
+
+/* One time step, as charm_model_ns_timestep_single / ..._euler_... */
+int oracle_step(oracle_t *o, double dt)
+{
+    const size_t n = (size_t) o->V * NB * (size_t) o->E;
+    const int lim = o->cfg.limiter == CHARM_GPU_LIM_BJ;
+    if (o->cfg.model == CHARM_GPU_MODEL_EULER) {
+        residual(o, o->u, o->res);
+        update(o, o->u, o->res, dt);
+        if (lim) limiter(o, o->u);
+        return 0;
+    }
+    memcpy(o->u_old, o->u, sizeof(double) * n);             /* rk_0 (:119-133) */
+    for (int s = 0; s < 3; s++) {
+        residual(o, o->u, o->res);
+        update(o, o->u, o->res, dt);
+        if (lim) limiter(o, o->u);
+        if (s == 1)                                           /* rk_1 (:136-157) */
+            for (size_t i = 0; i < n; i++) { o->u[i] *= 0.25; o->u[i] += 0.75 * o->u_old[i]; }
+        if (s == 2)                                           /* rk_2 (:160-184) */
+            for (size_t i = 0; i < n; i++) { o->u[i] *= 2.; o->u[i] /= 3.; o->u[i] += o->u_old[i] / 3.; }
+    }
+    return 0;
+}
+
+int oracle_run(oracle_t *o, int nsteps, double dt)
+{
+    for (int s = 0; s < nsteps; s++) oracle_step(o, dt);
+    return 0;
+}
+
+/* Point flux on two primitive states (r u v w p each), for unit tests. */
+int oracle_point_flux(oracle_t *o, const double *prim2, const double n[3], double *q)
+{
+    prim_t pr[2];
+    for (int s = 0; s < 2; s++) {
+        prim_t p;
+        double U[MAXV];
+        memset(&p, 0, sizeof(p));
+        p.r = prim2[5 * s]; p.u = prim2[5 * s + 1]; p.v = prim2[5 * s + 2]; p.w = prim2[5 * s + 3]; p.p = prim2[5 * s + 4];
+        for (int i = 0; i < o->cfg.n_comp; i++) p.c[i] = i == 0 ? 1. : 0.;
+        eos(o, &p, 1);
+        p.e_tot = p.e + 0.5 * (p.u * p.u + p.v * p.v + p.w * p.w);
+        prim_to_cons(o, &p, U);
+        cons_to_prim(o, U, &pr[s]);
+    }
+    num_flux(o, pr, n, q);
+    return 0;
+}

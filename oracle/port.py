@@ -1,0 +1,83 @@
+"""ctypes wrapper of the CPU restatement (oracle/charm_oracle.c).  Oracle only."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import build_oracle
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        lib = C.CDLL(build_oracle.build())
+        lib.oracle_new.restype = C.c_void_p
+        lib.oracle_new.argtypes = [C.c_void_p, C.c_void_p]
+        lib.oracle_free.argtypes = [C.c_void_p]
+        for name in ("oracle_set_state", "oracle_get_state", "oracle_residual"):
+            getattr(lib, name).argtypes = [C.c_void_p, C.c_void_p]
+        lib.oracle_limit.argtypes = [C.c_void_p]
+        lib.oracle_step.argtypes = [C.c_void_p, C.c_double]
+        lib.oracle_run.argtypes = [C.c_void_p, C.c_int, C.c_double]
+        lib.oracle_point_flux.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib = lib
+    return _lib
+
+
+class Port:
+    """The oracle on one flattened mesh (charm_3d_gb300.solver.MeshArrays)."""
+
+    def __init__(self, cfg, mesh):
+        self.lib = load()
+        self.mesh = mesh
+        self._m = mesh.struct()
+        self.cfg = cfg
+        self.h = self.lib.oracle_new(C.addressof(cfg), C.addressof(self._m))
+        if not self.h:
+            raise MemoryError("oracle_new failed")
+        self.shape = (4 + cfg.n_comp, 4, mesh.n_elem)
+
+    def close(self):
+        if self.h:
+            self.lib.oracle_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, u: np.ndarray) -> None:
+        a = np.ascontiguousarray(u, dtype=np.float64)
+        assert a.shape == self.shape
+        self.lib.oracle_set_state(self.h, a.ctypes.data)
+
+    def get_state(self) -> np.ndarray:
+        a = np.empty(self.shape)
+        self.lib.oracle_get_state(self.h, a.ctypes.data)
+        return a
+
+    def residual(self) -> np.ndarray:
+        a = np.empty(self.shape)
+        self.lib.oracle_residual(self.h, a.ctypes.data)
+        return a
+
+    def limit(self) -> None:
+        self.lib.oracle_limit(self.h)
+
+    def step(self, dt: float) -> None:
+        self.lib.oracle_step(self.h, dt)
+
+    def run(self, nsteps: int, dt: float) -> None:
+        self.lib.oracle_run(self.h, nsteps, dt)
+
+    def point_flux(self, prim2, n) -> np.ndarray:
+        p = np.ascontiguousarray(prim2, dtype=np.float64)
+        nn = np.ascontiguousarray(n, dtype=np.float64)
+        q = np.zeros(4 + self.cfg.n_comp)
+        self.lib.oracle_point_flux(self.h, p.ctypes.data, nn.ctypes.data, q.ctypes.data)
+        return q

@@ -1,0 +1,138 @@
+"""ctypes wrapper of the reference build (oracle/_ref/libcharm_ref*.so).  Oracle only.
+
+Available only where the reference checkout exists (the libraries are built
+from its sources by oracle/build_ref.py); tests skip otherwise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import build_ref
+
+
+class Region(C.Structure):
+    _fields_ = [("v", C.c_double * 3), ("t", C.c_double), ("p", C.c_double), ("c", C.c_double * 8)]
+
+
+def available() -> bool:
+    return build_ref.reference_root() is not None
+
+
+_libs: dict[str, C.CDLL] = {}
+
+
+def load(variant: str = "ref") -> C.CDLL:
+    if variant not in _libs:
+        paths = build_ref.build()
+        lib = C.CDLL(paths[variant], mode=C.RTLD_LOCAL)
+        lib.ref_setup.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                  C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int]
+        lib.ref_count.restype = C.c_int64
+        lib.ref_set_state.argtypes = [C.c_void_p]
+        lib.ref_get_state.argtypes = [C.c_void_p]
+        lib.ref_run.argtypes = [C.c_int, C.c_void_p]
+        lib.ref_residual.argtypes = [C.c_void_p]
+        lib.ref_geometry.argtypes = [C.c_void_p]
+        lib.ref_faces_count.restype = C.c_int64
+        lib.ref_faces_copy.argtypes = [C.c_void_p]
+        lib.ref_leaves.argtypes = [C.c_void_p]
+        lib.ref_adapt.restype = C.c_int64
+        lib.ref_grad.argtypes = [C.c_void_p]
+        lib.ref_point_flux.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.ref_refine_flags.argtypes = [C.c_void_p, C.c_int]
+        lib.ref_refine_flags.restype = C.c_int64
+        _libs[variant] = lib
+    return _libs[variant]
+
+
+class RefSolver:
+    """The reference's own time step on a brick case (one at a time per variant)."""
+
+    def __init__(self, case, variant: str = "ref"):
+        self.lib = load(variant)
+        self.case = case
+        self.cfg = case.config()
+        reg = Region()
+        r = case.ref_region()
+        for k in range(3):
+            reg.v[k] = r["v"][k]
+        reg.t, reg.p = r["t"], r["p"]
+        for k, v in enumerate(r["c"]):
+            reg.c[k] = v
+        self._keep = [np.array(case.brick, np.int32), np.array(case.periodic, np.int32),
+                      np.array(case.origin, np.float64), np.array(case.tree_len, np.float64),
+                      np.array(case.bnd_of_side, np.int8)]
+        b, p, o, t, s = self._keep
+        rc = self.lib.ref_setup(C.addressof(self.cfg), b.ctypes.data, p.ctypes.data, o.ctypes.data, t.ctypes.data,
+                                case.level, s.ctypes.data, C.addressof(reg), case.max_err, case.min_level,
+                                case.max_level, case.refine_period)
+        if rc:
+            raise RuntimeError(f"ref_setup failed: {rc}")
+        self.n_var = 4 + case.n_comp
+
+    @property
+    def n_elem(self) -> int:
+        return int(self.lib.ref_count())
+
+    def shape(self):
+        return (self.n_var, 4, self.n_elem)
+
+    def set_state(self, u: np.ndarray) -> None:
+        a = np.ascontiguousarray(u, dtype=np.float64)
+        assert a.shape == self.shape()
+        self.lib.ref_set_state(a.ctypes.data)
+
+    def get_state(self) -> np.ndarray:
+        a = np.empty(self.shape())
+        self.lib.ref_get_state(a.ctypes.data)
+        return a
+
+    def run(self, nsteps: int) -> float:
+        dt = C.c_double()
+        self.lib.ref_run(nsteps, C.byref(dt))
+        return dt.value
+
+    def residual(self) -> np.ndarray:
+        a = np.empty(self.shape())
+        self.lib.ref_residual(a.ctypes.data)
+        return a
+
+    def limit(self) -> None:
+        self.lib.ref_limit()
+
+    def geometry(self) -> np.ndarray:
+        a = np.empty((self.n_elem, 29))
+        self.lib.ref_geometry(a.ctypes.data)
+        return a
+
+    def faces(self) -> np.ndarray:
+        n = self.lib.ref_faces_count()
+        a = np.empty((n, 13), np.int64)
+        self.lib.ref_faces_copy(a.ctypes.data)
+        return a
+
+    def leaves(self) -> np.ndarray:
+        a = np.empty((self.n_elem, 5), np.int32)
+        self.lib.ref_leaves(a.ctypes.data)
+        return a
+
+    def adapt(self) -> int:
+        return int(self.lib.ref_adapt())
+
+    def grad(self) -> np.ndarray:
+        a = np.empty((self.n_elem, 3))
+        self.lib.ref_grad(a.ctypes.data)
+        return a
+
+    def refine_flags(self, flags: np.ndarray, maxlevel: int) -> int:
+        f = np.ascontiguousarray(flags, dtype=np.int8)
+        return int(self.lib.ref_refine_flags(f.ctypes.data, maxlevel))
+
+    def point_flux(self, prim2, n) -> np.ndarray:
+        p = np.ascontiguousarray(prim2, dtype=np.float64)
+        nn = np.ascontiguousarray(n, dtype=np.float64)
+        q = np.zeros(4 + self.case.n_comp)
+        self.lib.ref_point_flux(p.ctypes.data, nn.ctypes.data, q.ctypes.data)
+        return q
