@@ -1,0 +1,407 @@
+"""Benchmark: DG DOF-updates/s of the explicit SSP-RK3 time step on one GB300.
+
+Workload (default): Euler isentropic vortex, periodic [0,10]^3, uniform
+level 7 (128^3 = 2,097,152 hex), p1 Taylor basis (4 coefficients), 5
+conserved variables, HLLC flux, no limiter, seeded +-1e-3 density noise.
+One bench step = one full SSP-RK3 time step (3 stages) over the whole mesh.
+
+  DOF-updates/s = E * V * B * 3 stages * steps / seconds
+
+Lines printed (rank 0, one JSON object each run):
+  * our arm: plain FP64 path (the drop-in) as `value`, with
+      - `e2e`: the same metric through the C ABI with host buffers (state
+        H2D + step + state D2H every step),
+      - `mixed`: the FP32-residual / FP64-state form on the same steps with
+        its error against the FP64 path,
+      - `roofline`, `cpu_baseline`, `clocks`, `gpu_launches`.
+  * --impl reference: the reference's CPU algorithm (the oracle
+    restatement, all host cores) on a bounded sample of the same workload.
+
+Multi-GPU: the path is run as independent replicas (one per rank, weak
+scaling); there is no data-path collective.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "DG DOF-updates/s (SSP-RK3 stage DOF updates per second)"
+UNIT = "DOF-updates/s"
+STAGES = 3
+L2_BYTES = 129e6
+
+
+def peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "src": "measured"}
+    return {"hbm_gbs": 6800.0, "src": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self) -> dict:
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names[1:], parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def workload(level: int, brick: int = 1):
+    """The vortex workload; brick > 1 stretches the box along x (profiling sizes)."""
+    from charm_3d_gb300 import synthetic
+    c = synthetic("vortex", level=level)
+    if brick > 1:
+        c.brick = (brick, 1, 1)
+    return c
+
+
+def dof_per_step(E: int, V: int) -> int:
+    return E * V * 4 * STAGES
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (oracle restatement), used by our arm and by --impl reference
+# ---------------------------------------------------------------------------
+
+def _port_worker(args):
+    level, seconds = args
+    sys.path.insert(0, ROOT)
+    from charm_3d_gb300.solver import Forest
+    from oracle.port import Port
+    case = workload(level)
+    f = Forest(case)
+    mesh = f.flatten()
+    port = Port(case.config(), mesh)
+    port.set_state(case.initial_state(mesh.center))
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        port.step(case.tau)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    return mesh.n_elem, 4 + case.n_comp, steps, el
+
+
+def cpu_baseline(level: int, seconds: float, cores: int) -> dict:
+    if cores <= 1:
+        E, V, steps, el = _port_worker((level, seconds))
+        rate = dof_per_step(E, V) * steps / el
+    else:
+        import multiprocessing as mp
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(cores) as pool:
+            res = pool.map(_port_worker, [(level, seconds)] * cores)
+        rate = sum(dof_per_step(E, V) * s / el for E, V, s, el in res)
+        E, V, steps, el = res[0]
+    return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"vortex level {level} ({E} hex), {steps} SSP-RK3 steps per process in {el:.1f} s, "
+                      f"{cores} independent process(es); oracle/charm_oracle.c -O2"}
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+
+def run_gpu(args, rank: int, world: int, device: int) -> dict | None:
+    from charm_3d_gb300 import abi
+    from charm_3d_gb300.solver import Forest, Solver
+
+    case = workload(args.level, args.brick)
+    t0 = time.perf_counter()
+    forest = Forest(case)
+    mesh = forest.flatten()
+    u0 = case.initial_state(mesh.center)
+    t_mesh = time.perf_counter() - t0
+    E, V = mesh.n_elem, case.n_var
+    state_bytes = u0.nbytes
+
+    if args.only == "mixed":
+        return run_mixed_only(args, case, mesh, u0, device, world)
+    # ---- plain FP64 (drop-in) ----
+    case.precision = "FP64"
+    gpu = Solver(case, device)
+    gpu.upload(mesh)
+    gpu.set_state(u0)
+    gpu.run(args.warmup, case.tau)
+    gpu.sync()
+    gpu.set_state(u0)
+    gpu.reset_stats()
+    gpu.set_timing(True)
+    barrier(world)
+    with ClockSampler(device) as clk:
+        ms = gpu.time_run(args.steps, case.tau)
+    gpu.set_timing(False)
+    launches, kms = gpu.kernel_stats()
+    ms = max_over_ranks(ms, world)
+    u64 = gpu.get_state()
+    value = dof_per_step(E, V) * args.steps * world / (ms * 1e-3)
+
+    if args.only == "fp64":
+        gpu.close()
+        if rank == 0:
+            print(json.dumps({"only": "fp64", "ms_per_step": ms / args.steps, "value": value,
+                              "kernel_ms": kms.tolist(), "launches": launches.tolist()}))
+        return None
+    # ---- mixed form on the same steps ----
+    case.precision = "MIXED"
+    g32 = Solver(case, device)
+    g32.upload(mesh)
+    g32.set_state(u0)
+    g32.run(args.warmup, case.tau)
+    g32.sync()
+    g32.set_state(u0)
+    g32.reset_stats()
+    barrier(world)
+    ms32 = max_over_ranks(g32.time_run(args.steps, case.tau), world)
+    u32 = g32.get_state()
+    rho64, rho32 = u64[4:].sum(axis=0), u32[4:].sum(axis=0)
+    mass64 = float(np.sum(rho64[0])) ; mass32 = float(np.sum(rho32[0]))
+    mass0 = float(np.sum(u0[4:].sum(axis=0)[0]))
+    mixed = {"value": dof_per_step(E, V) * args.steps * world / (ms32 * 1e-3), "unit": UNIT,
+             "ms_per_step": ms32 / args.steps, "speedup_vs_fp64": ms / ms32,
+             "rel_l2_density_vs_fp64": float(np.linalg.norm(rho32 - rho64) / np.linalg.norm(rho64)),
+             "rel_l2_state_vs_fp64": float(np.linalg.norm(u32 - u64) / np.linalg.norm(u64)),
+             "mass_drift_fp64": (mass64 - mass0) / mass0, "mass_drift_mixed": (mass32 - mass0) / mass0,
+             "dtype": "f32 residual / f64 state"}
+    g32.close()
+
+    # ---- e2e through the C ABI with host buffers ----
+    if args.skip_e2e:
+        e2e = None
+        gpu.close()
+        return finish(args, rank, world, device, case, mesh, E, V, state_bytes, t_mesh, value, ms, launches, kms,
+                      mixed, e2e, clk)
+    import torch
+    pin_in = torch.empty(u0.shape, dtype=torch.float64, pin_memory=True).numpy()
+    pin_out = torch.empty(u0.shape, dtype=torch.float64, pin_memory=True).numpy()
+    pin_in[...] = u0
+    n_e2e = max(1, min(args.steps, 5))
+    gpu.set_state(pin_in)
+    gpu.step(case.tau)
+    gpu.get_state(pin_out)
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(n_e2e):
+        gpu.set_state(pin_in)
+        gpu.step(case.tau)
+        gpu.get_state(pin_out)
+    t_e2e = max_over_ranks(time.perf_counter() - t0, world)
+    e2e = {"value": dof_per_step(E, V) * n_e2e * world / t_e2e, "unit": UNIT, "h2d_bytes_per_step": state_bytes,
+           "d2h_bytes_per_step": state_bytes, "steps": n_e2e,
+           "path": "charm_gpu_set_state(host) + charm_gpu_step + charm_gpu_get_state(host), pinned buffers"}
+    gpu.close()
+    return finish(args, rank, world, device, case, mesh, E, V, state_bytes, t_mesh, value, ms, launches, kms, mixed,
+                  e2e, clk)
+
+
+def run_mixed_only(args, case, mesh, u0, device, world):
+    from charm_3d_gb300.solver import Solver
+    case.precision = "MIXED"
+    g32 = Solver(case, device)
+    g32.upload(mesh)
+    g32.set_state(u0)
+    g32.run(args.warmup, case.tau)
+    g32.sync()
+    g32.set_state(u0)
+    g32.reset_stats()
+    g32.set_timing(True)
+    ms32 = g32.time_run(args.steps, case.tau)
+    g32.set_timing(False)
+    launches, kms = g32.kernel_stats()
+    g32.close()
+    print(json.dumps({"only": "mixed", "ms_per_step": ms32 / args.steps, "kernel_ms": kms.tolist(),
+                      "launches": launches.tolist()}))
+    return None
+
+
+def finish(args, rank, world, device, case, mesh, E, V, state_bytes, t_mesh, value, ms, launches, kms, mixed, e2e,
+           clk):
+    from charm_3d_gb300 import abi
+    if rank != 0:
+        return None
+
+    # ---- roofline for the dominant kernel ----
+    pk = peaks()
+    names = ["face", "cell", "limiter", "other"]
+    dom = int(np.argmax(kms))
+    per_launch_ms = kms[dom] / max(launches[dom], 1)
+    F = mesh.n_face + mesh.n_bface
+    # algorithmic bytes per launch (FP64): face kernel reads the stage state
+    # once (V*B*8 per element) and the face records (9 B per face); the cell
+    # kernel reads the stage state and u^n and writes the new state, plus the
+    # element level byte.  Slot buffers are intermediate and not counted.
+    alg = {"face": E * V * 4 * 8 + F * 9, "cell": E * (3 * V * 4 * 8 + 1), "limiter": E * (3 * V * 4 * 8 + 24),
+           "other": E * V * 8}
+    achieved = alg[names[dom]] / (per_launch_ms * 1e-3) / 1e9
+    fp64_peak = probe(abi, device, 0)
+    roofline = {"bound": "hbm", "kernel": names[dom] + "_kernel<double>", "achieved": achieved,
+                "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
+                "peak_src": pk["src"], "traffic": None,
+                "algorithmic_bytes_per_launch": alg[names[dom]], "launch_ms": per_launch_ms,
+                "kernel_share": {n: float(kms[i] / kms.sum()) for i, n in enumerate(names)},
+                "fp64_pipe": {"peak_tflops_measured": fp64_peak,
+                              "note": "plain FP64 path is bound by the FP64 pipe, see profiles/"}}
+    cpu = cpu_baseline(args.cpu_level, args.cpu_seconds, 1) if args.cpu_seconds > 0 else None
+    n_launch = int(launches.sum())
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded isentropic vortex + 1e-3 density noise)",
+            "config": {"workload": f"Euler isentropic vortex, periodic [0,10]^3, level {args.level} "
+                                   f"({E} hex), p1, HLLC, no limiter, SSP-RK3",
+                       "elements": E, "variables": V, "basis": 4, "stages_per_step": STAGES,
+                       "parallelism": f"replicas x{world}",
+                       "l2": f"inputs larger than L2 (state {state_bytes / 1e6:.0f} MB > 129 MB)",
+                       "mesh_build_s": t_mesh},
+            "e2e": e2e, "mixed": mixed, "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": n_launch,
+            "clocks": clk.summary()}
+
+
+def probe(abi, device: int, which: int) -> float | None:
+    import ctypes as C
+    lib = abi.load()
+    v = C.c_double()
+    return v.value if lib.charm_gpu_probe_peak(device, which, C.byref(v)) == 0 else None
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (replicas; only barrier and max-reduce of times)
+# ---------------------------------------------------------------------------
+
+_DIST = {"on": False}
+
+
+def init_dist(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if args.impl != "reference" else "gloo")
+        _DIST["on"] = True
+    return rank, world, local
+
+
+def barrier(world: int):
+    if world > 1 and _DIST["on"]:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world > 1 and _DIST["on"]:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+    return x
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--level", type=int, default=7)
+    ap.add_argument("--cpu-level", type=int, default=5)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--brick", type=int, default=1, help="trees along x (profiling sizes)")
+    ap.add_argument("--only", default="both", choices=["both", "fp64", "mixed"])
+    ap.add_argument("--skip-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    if args.impl == "reference":
+        rank = int(os.environ.get("RANK", "0"))
+        if rank != 0:
+            return
+        cores = os.cpu_count() or 1
+        res = cpu_baseline(args.cpu_level, max(2.0, args.cpu_seconds / 2), cores)
+        out = {"metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+               "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+               "dtype": "f64", "data": "synthetic (seeded isentropic vortex + 1e-3 density noise)",
+               "impl": "reference",
+               "config": {"workload": f"Euler isentropic vortex, periodic [0,10]^3, level {args.level}, p1, HLLC, "
+                                      f"no limiter, SSP-RK3; timed on a bounded sample (level {args.cpu_level})",
+                          "parallelism": f"{cores} CPU processes"},
+               "cpu_baseline": res,
+               "e2e": {"value": res["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+               "note": "reference CPU algorithm = oracle/charm_oracle.c, the C restatement pinned to the "
+                       "reference's own sources (the reference's MPI build cannot be built here: no p4est/MPI)"}
+        print(json.dumps(out))
+        return
+
+    rank, world, local = init_dist(args)
+    res = run_gpu(args, rank, world, local)
+    if rank == 0 and res is not None:
+        print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()

@@ -196,7 +196,11 @@ class Case:
             rho = 1.0 + 0.2 * rng.uniform(-1, 1, E)
             p = 1.0 + 0.2 * rng.uniform(-1, 1, E)
             vel = 0.3 * rng.uniform(-1, 1, (3, E))
-            U = self.cons_from_prim(rho, vel[0], vel[1], vel[2], p)
+            c = None
+            if self.n_comp > 1:
+                c = rng.uniform(0.05, 1.0, (self.n_comp, E))
+                c /= c.sum(axis=0)
+            U = self.cons_from_prim(rho, vel[0], vel[1], vel[2], p, c)
             out = np.zeros((self.n_var, abi.BASIS, E))
             out[:, 0, :] = U
             slope = a.get("slope", 0.05)

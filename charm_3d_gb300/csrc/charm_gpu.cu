@@ -726,6 +726,71 @@ int charm_gpu_reset_stats(charm_gpu_handle_t h)
     return CHARM_GPU_OK;
 }
 
+int charm_gpu_time_run(charm_gpu_handle_t h, int nsteps, double dt_in, double *ms)
+{
+    int rc = check_ready(h);
+    if (rc) return rc;
+    if (!ms) return fail(CHARM_GPU_EINVAL, "null argument");
+    cudaEvent_t a, b;
+    CUDA_TRY(cudaEventCreate(&a));
+    CUDA_TRY(cudaEventCreate(&b));
+    CUDA_TRY(cudaEventRecord(a, h->stream));
+    rc = charm_gpu_run(h, nsteps, dt_in);
+    if (rc) { cudaEventDestroy(a); cudaEventDestroy(b); return rc; }
+    CUDA_TRY(cudaEventRecord(b, h->stream));
+    rc = charm_gpu_sync(h, 3600.0);
+    float f = 0.f;
+    if (!rc) {
+        cudaError_t e = cudaEventElapsedTime(&f, a, b);
+        if (e != cudaSuccess) rc = fail(CHARM_GPU_ECUDA, cudaGetErrorString(e));
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *ms = f;
+    return rc;
+}
+
+int charm_gpu_probe_peak(int device, int which, double *tflops)
+{
+    if (!tflops || (which != 0 && which != 1)) return fail(CHARM_GPU_EINVAL, "bad argument");
+    CUDA_TRY(cudaSetDevice(device));
+    int nsm = 0;
+    CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
+    const int threads = 256, blocks = nsm * 8, iters = (which == 0) ? 4096 : 65536;
+    void *buf = nullptr;
+    CUDA_TRY(cudaMalloc(&buf, (size_t) blocks * threads * sizeof(double)));
+    cudaEvent_t a, b;
+    CUDA_TRY(cudaEventCreate(&a));
+    CUDA_TRY(cudaEventCreate(&b));
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; rep++) {
+        CUDA_TRY(cudaEventRecord(a, 0));
+        if (which == 0) fma_peak_kernel<double><<<blocks, threads>>>(static_cast<double *>(buf), iters);
+        else fma_peak_kernel<float><<<blocks, threads>>>(static_cast<float *>(buf), iters);
+        CUDA_TRY(cudaEventRecord(b, 0));
+        CUDA_TRY(cudaEventSynchronize(b));
+        float ms = 0.f;
+        CUDA_TRY(cudaEventElapsedTime(&ms, a, b));
+        if (rep > 0 && ms < best) best = ms;   // first launch is a warm-up
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(buf);
+    const double flops = 2.0 * kPeakChains * (double) iters * blocks * threads;
+    *tflops = flops / (best * 1e-3) / 1e12;
+    return CHARM_GPU_OK;
+}
+
+int charm_gpu_abi_sizes(int64_t out[4])
+{
+    if (!out) return fail(CHARM_GPU_EINVAL, "null argument");
+    out[0] = sizeof(charm_gpu_config_t);
+    out[1] = sizeof(charm_gpu_mesh_t);
+    out[2] = sizeof(charm_gpu_comp_t);
+    out[3] = sizeof(charm_gpu_bnd_t);
+    return CHARM_GPU_OK;
+}
+
 int charm_gpu_dims(charm_gpu_handle_t h, int64_t *n_elem, int *nv, int *nb)
 {
     if (!h) return fail(CHARM_GPU_EINVAL, "null handle");

@@ -516,4 +516,28 @@ cfl_dt_kernel(MeshDev m, const double *__restrict__ u, double cfl, unsigned long
     }
 }
 
+// ---------------------------------------------------------------------------
+// Arithmetic peak probe: kPeakChains independent FMA chains per thread, the
+// result stored so the compiler keeps them.  Used only to measure the
+// roofline denominator of the CUDA-core pipes on the running GPU.
+// ---------------------------------------------------------------------------
+constexpr int kPeakChains = 8;
+
+template <typename T>
+__global__ void __launch_bounds__(256) fma_peak_kernel(T *out, int iters)
+{
+    T a[kPeakChains];
+    const T x = T(1) + T(threadIdx.x) * T(1e-7), y = T(0.999999);
+#pragma unroll
+    for (int k = 0; k < kPeakChains; k++) a[k] = T(k) * T(1e-3);
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < kPeakChains; k++) a[k] = fma(a[k], y, x);
+    }
+    T s = T(0);
+#pragma unroll
+    for (int k = 0; k < kPeakChains; k++) s += a[k];
+    out[(size_t) blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 }  // namespace charm

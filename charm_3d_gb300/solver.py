@@ -157,6 +157,12 @@ class Solver:
     def run(self, nsteps: int, dt: float = 0.0) -> None:
         abi.check(self.lib.charm_gpu_run(self.h, nsteps, dt), "charm_gpu_run")
 
+    def time_run(self, nsteps: int, dt: float = 0.0) -> float:
+        """Device time in ms of nsteps, from CUDA events on the solver's stream."""
+        ms = C.c_double()
+        abi.check(self.lib.charm_gpu_time_run(self.h, nsteps, dt, C.byref(ms)), "charm_gpu_time_run")
+        return ms.value
+
     def get_dt(self) -> float:
         d = C.c_double()
         abi.check(self.lib.charm_gpu_get_dt(self.h, C.byref(d)), "charm_gpu_get_dt")

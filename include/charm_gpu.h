@@ -195,6 +195,18 @@ int charm_gpu_set_timing(charm_gpu_handle_t h, int enable);
 int charm_gpu_kernel_stats(charm_gpu_handle_t h, int64_t launches[4], double ms[4]);
 int charm_gpu_reset_stats(charm_gpu_handle_t h);
 
+/* Run nsteps (as charm_gpu_run) between two CUDA events recorded on the
+ * handle's stream and return the elapsed device time in *ms. */
+int charm_gpu_time_run(charm_gpu_handle_t h, int nsteps, double dt_in, double *ms);
+
+/* Measured arithmetic peak of this GPU's CUDA cores, for roofline
+ * denominators: which = 0 FP64 FMA, 1 FP32 FMA; *tflops in TFLOP/s. */
+int charm_gpu_probe_peak(int device, int which, double *tflops);
+
+/* sizeof of the ABI structs as compiled into the library, for binding checks:
+ * out[0] config, out[1] mesh, out[2] comp, out[3] bnd. */
+int charm_gpu_abi_sizes(int64_t out[4]);
+
 /* Element count, variables and basis size of the uploaded mesh. */
 int charm_gpu_dims(charm_gpu_handle_t h, int64_t *n_elem, int *n_var, int *n_basis);
 

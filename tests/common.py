@@ -1,0 +1,64 @@
+"""Shared helpers for the tests: cases, meshes with hanging faces, error norms."""
+from __future__ import annotations
+
+import numpy as np
+
+from charm_3d_gb300 import Boundary, Case, Component, synthetic
+from charm_3d_gb300.solver import Forest
+
+
+def rel_l2(a: np.ndarray, b: np.ndarray) -> float:
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def rel_max(a: np.ndarray, b: np.ndarray) -> float:
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def small_case(kind: str, flux: str = "LF", limiter: str = "BJ", level: int = 3, model: str = "NS") -> Case:
+    """Small parity cases."""
+    if kind == "sod":
+        c = synthetic("sod", level=level)
+    elif kind == "vortex":
+        c = synthetic("vortex", level=level)
+    elif kind == "random":
+        c = synthetic("sod", level=level)
+        c.init = "random"
+        c.seed = 7
+    elif kind == "walls":
+        # every boundary type of the reference on one box (src/charm_bnd_cond.c)
+        c = synthetic("sod", level=level)
+        c.init = "random"
+        c.seed = 11
+        T_in = 1.0 * 0.02869409 / (1.0 * 8.31446261815324)
+        c.boundaries = [Boundary("IN", "BOUND_INLET", (0.3, 0.0, 0.0, T_in, 1.0)),
+                        Boundary("OUT", "BOUND_OUTLET"),
+                        Boundary("SLIP", "BOUND_WALL_SLIP"),
+                        Boundary("NOSLIP", "BOUND_WALL_NO_SLIP", (T_in,))]
+        c.bnd_of_side = (0, 1, 2, 2, 3, 2)
+    elif kind == "mix2":
+        # two species, mixture EOS (src/charm_eos.c:120-148), constant cp
+        c = synthetic("sod", level=level)
+        c.init = "random"
+        c.seed = 5
+        c.eos = "MIX"
+        c.components = [Component("A", m=0.02869409, cp=(1014.16,)), Component("B", m=0.018, cp=(1850.0,))]
+    else:
+        raise ValueError(kind)
+    c.flux, c.limiter, c.model = flux, limiter, model
+    c.steps = 3
+    if kind in ("random", "walls", "mix2"):
+        # random slopes and no limiter: keep the step well inside p1 DG's CFL limit
+        c.tau = 0.1 * (1.0 / 2 ** level) / 1.5
+    return c
+
+
+def hanging_forest(case: Case, frac: float = 0.2, seed: int = 3) -> tuple[Forest, np.ndarray]:
+    """Forest of `case` with a random subset of leaves refined once and 2:1 balanced.
+    Scales case.tau by 1/4 so that the finer leaves stay well inside the CFL limit."""
+    f = Forest(case)
+    case.tau *= 0.25
+    rng = np.random.default_rng(seed)
+    flags = (rng.uniform(size=len(f)) < frac).astype(np.int8)
+    f.adapt(flags, case.level, case.level + 1)
+    return f, flags

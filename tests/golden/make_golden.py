@@ -1,0 +1,95 @@
+"""Generate tests/golden/*.npz from the reference's own code (oracle/_ref).
+
+Run where the reference checkout exists:  python tests/golden/make_golden.py
+Each fixture holds the initial state, the reference's residual int_* of it,
+and the reference's state after `steps` calls of timestep_single_fn, on a
+small brick mesh built by the host octree (identical leaves on both sides;
+the script checks that).  Mesh and initial data are rebuilt from the case
+name by tests/common.py, so only arrays are stored.
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from charm_3d_gb300.solver import Forest  # noqa: E402
+from oracle.ref import RefSolver  # noqa: E402
+from tests.common import hanging_forest, small_case  # noqa: E402
+
+# name: (kind, flux, limiter, model, level, steps, hanging)
+FIXTURES = {
+    "sod_lf_bj": ("random", "LF", "BJ", "NS", 3, 3, False),
+    "sod_step_lf_bj": ("sod", "LF", "BJ", "NS", 3, 4, False),
+    "vortex_hllc": ("vortex", "HLLC", "NONE", "NS", 3, 3, False),
+    "walls_hllc_bj": ("walls", "HLLC", "BJ", "NS", 2, 3, False),
+    "walls_cd": ("walls", "CD", "NONE", "NS", 2, 1, False),
+    "euler_lf_bj": ("random", "LF", "BJ", "EULER", 3, 2, False),
+    "mix2_hllc_bj": ("mix2", "HLLC", "BJ", "NS", 2, 2, False),
+    "hanging_hllc_bj": ("random", "HLLC", "BJ", "NS", 2, 2, True),
+    "hanging_lf": ("random", "LF", "NONE", "NS", 2, 2, True),
+}
+
+
+def make(name: str) -> dict:
+    kind, flux, lim, model, level, steps, hanging = FIXTURES[name]
+    case = small_case(kind, flux, lim, level=level, model=model)
+    variant = "patched" if hanging else "ref"
+    if hanging:
+        forest, flags = hanging_forest(case)   # also scales case.tau for the finer leaves
+        ref = RefSolver(case, variant)
+        n = ref.refine_flags(flags, case.level + 1)
+        q, lv = forest.leaves()
+        rl = ref.leaves()
+        assert n == len(forest), (n, len(forest))
+        assert (rl[:, :4] == q).all() and (rl[:, 4] == lv).all(), "reference forest differs from host octree"
+    else:
+        ref = RefSolver(case, variant)
+        forest = Forest(case)
+    mesh = forest.flatten()
+    u0 = case.initial_state(mesh.center)
+    ref.set_state(u0)
+    res = ref.residual()
+    ref.set_state(u0)
+    dt = ref.run(steps)
+    out = ref.get_state()
+    return {"u0": u0, "residual": res, "state": out, "steps": np.array(steps), "dt": np.array(dt),
+            "meta": np.array(json.dumps({"kind": kind, "flux": flux, "limiter": lim, "model": model, "level": level,
+                                         "steps": steps, "hanging": hanging, "variant": variant}))}
+
+
+def point_fluxes() -> dict:
+    """Reference LF/HLLC/CD fluxes for random state pairs and random unit normals."""
+    rng = np.random.default_rng(2024)
+    n = 64
+    prim = np.stack([rng.uniform(0.2, 2.0, n), rng.uniform(-1.5, 1.5, n), rng.uniform(-1.5, 1.5, n),
+                     rng.uniform(-1.5, 1.5, n), rng.uniform(0.2, 2.0, n)], axis=1)
+    prim2 = np.stack([prim, np.roll(prim, 7, axis=0) * rng.uniform(0.8, 1.2, (n, 5))], axis=1)   # [n,2,5]
+    normals = rng.normal(size=(n, 3))
+    normals /= np.linalg.norm(normals, axis=1, keepdims=True)
+    normals[:6] = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1]], float)
+    out = {"prim2": prim2, "normals": normals}
+    for flux in ("LF", "HLLC", "CD"):
+        case = small_case("random", flux, "NONE", level=1)
+        ref = RefSolver(case)
+        out[flux] = np.stack([ref.point_flux(prim2[i].ravel(), normals[i]) for i in range(n)])
+    return out
+
+
+def main() -> None:
+    for name in FIXTURES:
+        d = make(name)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+        print(name, d["u0"].shape, "dt", float(d["dt"]))
+    np.savez_compressed(os.path.join(HERE, "point_fluxes.npz"), **point_fluxes())
+    print("point_fluxes")
+
+
+if __name__ == "__main__":
+    main()
