@@ -13,6 +13,10 @@ oracle/ref_driver.c, into two shared libraries:
                                        hanging-face branch also stores the
                                        species means (the original leaves those
                                        limiter slots stale, :174-193)
+  oracle/_ref/libcharm_ref_plugin.so   the reference plus the GPU model plugin
+                                       (charm_3d_gb300/csrc/plugin), linked to
+                                       libcharm_gpu.so, to test the drop-in
+                                       boundary against the reference's types
 
 Sources are read from the reference checkout (default /root/reference, or
 $CHARM_REFERENCE); nothing is copied into the repository.  Outputs go to
@@ -85,11 +89,14 @@ def build(force: bool = False) -> dict[str, str]:
     ref = reference_root()
     if ref is None:
         raise FileNotFoundError("reference sources not found (set CHARM_REFERENCE)")
-    libs = {"ref": os.path.join(OUT, "libcharm_ref.so"), "patched": os.path.join(OUT, "libcharm_ref_patched.so")}
+    libs = {"ref": os.path.join(OUT, "libcharm_ref.so"), "patched": os.path.join(OUT, "libcharm_ref_patched.so"),
+            "plugin": os.path.join(OUT, "libcharm_ref_plugin.so")}
+    plugin_src = os.path.join(ROOT, "charm_3d_gb300", "csrc", "plugin", "charm_model_gpu.c")
+    glue_src = os.path.join(HERE, "ref_plugin_glue.c")
     ours = [os.path.join(HERE, "p4est_shim", "p4est_shim.c"), os.path.join(HERE, "ref_driver.c"),
             os.path.join(ROOT, "charm_3d_gb300", "csrc", "host", "charm_forest.c")]
     deps = ours + [os.path.join(HERE, "p4est_shim", f) for f in os.listdir(os.path.join(HERE, "p4est_shim"))]
-    deps.append(__file__)
+    deps += [__file__, plugin_src, glue_src]
     if not force and all(os.path.exists(p) for p in libs.values()):
         if min(os.path.getmtime(p) for p in libs.values()) >= max(os.path.getmtime(p) for p in deps):
             return libs
@@ -114,10 +121,18 @@ def build(force: bool = False) -> dict[str, str]:
         jobs.append((flags + [src, "-o", obj] + inc, obj))
         objs_ref.append(obj)
         objs_pat.append(obj)
+    objs_plug = []
+    for src in (plugin_src, glue_src):
+        obj = os.path.join(OUT, "obj", os.path.basename(src) + ".o")
+        jobs.append((flags + [src, "-o", obj] + inc, obj))
+        objs_plug.append(obj)
     with cf.ThreadPoolExecutor(max_workers=8) as ex:
         list(ex.map(_compile, jobs))
     for key, objs in (("ref", objs_ref), ("patched", objs_pat)):
         _compile((["gcc", "-shared", "-o", libs[key]] + objs + ["-lm"], libs[key]))
+    gpu_dir = os.path.join(ROOT, "charm_3d_gb300")
+    _compile((["gcc", "-shared", "-o", libs["plugin"]] + objs_ref + objs_plug +
+              ["-L" + gpu_dir, "-lcharm_gpu", "-Wl,-rpath," + gpu_dir, "-lm"], libs["plugin"]))
     return libs
 
 

@@ -138,10 +138,37 @@ static void *new_data(p4est_t *p, int nan_fill)
     return d;
 }
 
+/* Counts and the per-tree views p4est keeps: tree t's quadrants are the
+ * leaves [quadrants_offset, quadrants_offset + count) of the global order. */
 static void sync_counts(p4est_t *p)
 {
-    p->local_num_quadrants = (p4est_locidx_t) p->shim->f.n;
-    p->global_num_quadrants = p->shim->f.n;
+    struct charm_shim_state *s = p->shim;
+    p->local_num_quadrants = (p4est_locidx_t) s->f.n;
+    p->global_num_quadrants = s->f.n;
+    if (!p->trees) p->trees = sc_array_new(sizeof(p4est_tree_t));
+    sc_array_resize(p->trees, (size_t) p->connectivity->num_trees);
+    int64_t i = 0;
+    for (p4est_topidx_t t = 0; t < p->connectivity->num_trees; t++) {
+        p4est_tree_t *tr = p4est_tree_array_index(p->trees, t);
+        int64_t start = i;
+        int8_t ml = 0;
+        while (i < s->f.n && s->f.leaf[i].tree == t) {
+            if (s->f.leaf[i].level > ml) ml = s->f.leaf[i].level;
+            i++;
+        }
+        tr->quadrants.elem_size = sizeof(p4est_quadrant_t);
+        tr->quadrants.elem_count = (size_t) (i - start);
+        tr->quadrants.byte_alloc = -1;
+        tr->quadrants.array = (char *) (s->q + start);
+        tr->quadrants_offset = (p4est_locidx_t) start;
+        tr->maxlevel = ml;
+    }
+}
+
+/* index of a local leaf within its tree, as p4est reports quadid */
+static p4est_locidx_t tree_local(p4est_t *p, int64_t i)
+{
+    return (p4est_locidx_t) (i - p4est_tree_array_index(p->trees, p->shim->f.leaf[i].tree)->quadrants_offset);
 }
 
 p4est_connectivity_t *charm_shim_conn_brick(int nx, int ny, int nz, const int periodic[3], const double origin[3],
@@ -246,6 +273,7 @@ p4est_t *p4est_new_ext(sc_MPI_Comm mpicomm, p4est_connectivity_t *conn, p4est_lo
 void p4est_destroy(p4est_t *p)
 {
     if (!p) return;
+    sc_array_destroy(p->trees);
     for (int64_t i = 0; i < p->shim->f.n; i++) free(p->shim->q[i].p.user_data);
     free(p->shim->q);
     charm_forest_free(&p->shim->f);
@@ -574,7 +602,7 @@ void p4est_iterate(p4est_t *p, p4est_ghost_t *g, void *ud, p4est_iter_volume_t v
             info.p4est = p;
             info.ghost_layer = g;
             info.quad = &s->q[i];
-            info.quadid = (p4est_locidx_t) i;
+            info.quadid = tree_local(p, i);
             info.treeid = f->leaf[i].tree;
             vol_fn(&info, ud);
         }
@@ -590,7 +618,7 @@ void p4est_iterate(p4est_t *p, p4est_ghost_t *g, void *ud, p4est_iter_volume_t v
             charm_forest_face_neighbor(f, i, face, &nb);
             switch (nb.kind) {
             case CHARM_NB_BOUNDARY:
-                side_full(&sides[0], ti, face, &s->q[i], 0, (p4est_locidx_t) i);
+                side_full(&sides[0], ti, face, &s->q[i], 0, tree_local(p, i));
                 call_face(p, g, ud, face_fn, 1, sides, 1);
                 break;
             case CHARM_NB_SAME: {
@@ -598,17 +626,17 @@ void p4est_iterate(p4est_t *p, p4est_ghost_t *g, void *ud, p4est_iter_volume_t v
                 const int32_t tj = f->leaf[j].tree;
                 if (!nb.wrap) {
                     if (!up) break;
-                    side_full(&sides[0], ti, face, &s->q[i], 0, (p4est_locidx_t) i);
-                    side_full(&sides[1], tj, face ^ 1, &s->q[j], 0, (p4est_locidx_t) j);
+                    side_full(&sides[0], ti, face, &s->q[i], 0, tree_local(p, i));
+                    side_full(&sides[1], tj, face ^ 1, &s->q[j], 0, tree_local(p, j));
                     call_face(p, g, ud, face_fn, 2, sides, ti != tj);
                 } else {
                     const int64_t gk = ghost_id(p, g, j, d, nb.wrap);
                     if (up) {
-                        side_full(&sides[0], ti, face, &s->q[i], 0, (p4est_locidx_t) i);
+                        side_full(&sides[0], ti, face, &s->q[i], 0, tree_local(p, i));
                         side_full(&sides[1], tj, face ^ 1, &ghq[gk], 1, (p4est_locidx_t) gk);
                     } else {
                         side_full(&sides[0], tj, face ^ 1, &ghq[gk], 1, (p4est_locidx_t) gk);
-                        side_full(&sides[1], ti, face, &s->q[i], 0, (p4est_locidx_t) i);
+                        side_full(&sides[1], ti, face, &s->q[i], 0, tree_local(p, i));
                     }
                     call_face(p, g, ud, face_fn, 2, sides, 1);
                 }
@@ -624,15 +652,15 @@ void p4est_iterate(p4est_t *p, p4est_ghost_t *g, void *ud, p4est_iter_volume_t v
                         const int64_t gk = ghost_id(p, g, nb.idx[k], d, nb.wrap);
                         hq[k] = &ghq[gk]; hg[k] = 1; hid[k] = (p4est_locidx_t) gk;
                     } else {
-                        hq[k] = &s->q[nb.idx[k]]; hg[k] = 0; hid[k] = (p4est_locidx_t) nb.idx[k];
+                        hq[k] = &s->q[nb.idx[k]]; hg[k] = 0; hid[k] = tree_local(p, nb.idx[k]);
                     }
                 }
                 if (up) {
-                    side_full(&sides[0], ti, face, &s->q[i], 0, (p4est_locidx_t) i);
+                    side_full(&sides[0], ti, face, &s->q[i], 0, tree_local(p, i));
                     side_hanging(&sides[1], tj, face ^ 1, hq, hg, hid);
                 } else {
                     side_hanging(&sides[0], tj, face ^ 1, hq, hg, hid);
-                    side_full(&sides[1], ti, face, &s->q[i], 0, (p4est_locidx_t) i);
+                    side_full(&sides[1], ti, face, &s->q[i], 0, tree_local(p, i));
                 }
                 call_face(p, g, ud, face_fn, 2, sides, ti != tj || nb.wrap);
                 break;
@@ -648,7 +676,7 @@ void p4est_iterate(p4est_t *p, p4est_ghost_t *g, void *ud, p4est_iter_volume_t v
                 p4est_quadrant_t *hq[4];
                 int8_t hg[4] = {0, 0, 0, 0};
                 p4est_locidx_t hid[4];
-                for (int k = 0; k < 4; k++) { hq[k] = &s->q[back.idx[k]]; hid[k] = (p4est_locidx_t) back.idx[k]; }
+                for (int k = 0; k < 4; k++) { hq[k] = &s->q[back.idx[k]]; hid[k] = tree_local(p, back.idx[k]); }
                 const int32_t tb = f->leaf[big].tree;
                 if (up) {
                     side_hanging(&sides[0], ti, face, hq, hg, hid);

@@ -133,9 +133,15 @@ typedef struct p4est {
     p4est_topidx_t first_local_tree, last_local_tree;
     p4est_locidx_t local_num_quadrants;
     p4est_gloidx_t global_num_quadrants;
+    sc_array_t *trees;          /* p4est_tree_t per tree; quadrants are views */
     p4est_connectivity_t *connectivity;
     struct charm_shim_state *shim;
 } p4est_t;
+
+static inline p4est_tree_t *p4est_tree_array_index(sc_array_t *array, p4est_topidx_t it)
+{
+    return (p4est_tree_t *) sc_array_index(array, (size_t) it);
+}
 
 typedef struct p4est_ghost {
     int mpisize;

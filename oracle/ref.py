@@ -43,6 +43,9 @@ def load(variant: str = "ref") -> C.CDLL:
         lib.ref_point_flux.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         lib.ref_refine_flags.argtypes = [C.c_void_p, C.c_int]
         lib.ref_refine_flags.restype = C.c_int64
+        if variant == "plugin":
+            lib.ref_plugin_flatten.argtypes = [C.c_void_p]
+            lib.ref_plugin_config.argtypes = [C.c_int, C.c_void_p]
         _libs[variant] = lib
     return _libs[variant]
 
@@ -129,6 +132,24 @@ class RefSolver:
     def refine_flags(self, flags: np.ndarray, maxlevel: int) -> int:
         f = np.ascontiguousarray(flags, dtype=np.int8)
         return int(self.lib.ref_refine_flags(f.ctypes.data, maxlevel))
+
+    def plugin_flatten(self):
+        """Flattened mesh as the GPU model plugin builds it from p4est_iterate."""
+        from charm_3d_gb300 import abi
+        from charm_3d_gb300.solver import MeshArrays
+        m = abi.Mesh()
+        rc = self.lib.ref_plugin_flatten(C.addressof(m))
+        if rc:
+            raise RuntimeError(f"charm_model_gpu_flatten: {rc}")
+        return MeshArrays(m)
+
+    def plugin_config(self, precision: int = 0):
+        from charm_3d_gb300 import abi
+        cfg = abi.Config()
+        rc = self.lib.ref_plugin_config(precision, C.addressof(cfg))
+        if rc:
+            raise RuntimeError(f"charm_model_gpu_config: {rc}")
+        return cfg
 
     def point_flux(self, prim2, n) -> np.ndarray:
         p = np.ascontiguousarray(prim2, dtype=np.float64)

@@ -509,3 +509,5 @@ int64_t ref_refine_flags(const int8_t *flags, int maxlevel)
     free_ghost();
     return charm_shim_count(g_p4est);
 }
+
+p4est_t *ref_driver_p4est(void) { return g_p4est; }

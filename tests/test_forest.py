@@ -1,0 +1,168 @@
+"""Host octree and flattening: checked against a brute-force geometric face matcher.
+
+Connectivity must be exact: every face of every leaf appears exactly once,
+as a conforming face, one of four mortar sub-faces, or a boundary face, with
+p4est's side order (side 0 at the lower coordinate).
+"""
+import itertools
+
+import numpy as np
+import pytest
+
+from charm_3d_gb300 import Case
+from charm_3d_gb300.solver import Forest
+
+from .common import hanging_forest
+
+
+def boxes(forest, case):
+    q, lv = forest.leaves()
+    nt = np.array(case.brick)
+    t = q[:, 3]
+    ti = np.stack([t % nt[0], (t // nt[0]) % nt[1], t // (nt[0] * nt[1])], axis=1)
+    R = 1 << 19
+    lo = ti * R + q[:, :3]
+    ln = (1 << (19 - lv.astype(np.int64)))
+    return lo.astype(np.int64), ln.astype(np.int64), lv
+
+
+def brute_force_faces(forest, case):
+    """All face adjacencies from box geometry (integer coordinates, O(E^2))."""
+    lo, ln, lv = boxes(forest, case)
+    E = len(ln)
+    ext = np.array(case.brick, np.int64) * (1 << 19)
+    conf, hang, bnd = set(), set(), set()
+    for i in range(E):
+        for d in range(3):
+            s, t = [a for a in range(3) if a != d]
+            # + side of i
+            x = lo[i, d] + ln[i]
+            wrap = False
+            if x == ext[d]:
+                if case.periodic[d]:
+                    x, wrap = 0, True
+                else:
+                    bnd.add((i, 2 * d + 1))
+            if lo[i, d] == 0 and not case.periodic[d]:
+                bnd.add((i, 2 * d))
+            if x == ext[d] and not case.periodic[d]:
+                continue
+            for j in range(E):
+                if lo[j, d] != x:
+                    continue
+                # tangential overlap with positive area
+                if lo[j, s] >= lo[i, s] + ln[i] or lo[i, s] >= lo[j, s] + ln[j]:
+                    continue
+                if lo[j, t] >= lo[i, t] + ln[i] or lo[i, t] >= lo[j, t] + ln[j]:
+                    continue
+                if ln[i] == ln[j]:
+                    conf.add((i, j, d))
+                else:
+                    hang.add((i, j, d))
+    return conf, hang, bnd
+
+
+def flattened_faces(mesh):
+    conf, hang, bnd = set(), set(), set()
+    for k in range(mesh.n_face):
+        a, b = int(mesh.face_elem[0, k]), int(mesh.face_elem[1, k])
+        info = int(mesh.face_info[k])
+        d, kind = info & 3, (info >> 2) & 3
+        (conf if kind == 0 else hang).add((a, b, d))
+    for k in range(mesh.n_bface):
+        bnd.add((int(mesh.bface_elem[k]), int(mesh.bface_face[k])))
+    return conf, hang, bnd
+
+
+CASES = [Case(level=2), Case(level=2, periodic=(1, 1, 1)), Case(level=1, brick=(2, 3, 1)),
+         Case(level=1, brick=(3, 1, 2), periodic=(1, 0, 1))]
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("refine", [False, True])
+def test_flatten_matches_brute_force(case, refine):
+    forest = hanging_forest(case, frac=0.25, seed=9)[0] if refine else Forest(case)
+    mesh = forest.flatten()
+    got = flattened_faces(mesh)
+    want = brute_force_faces(forest, case)
+    assert got[0] == want[0]
+    assert got[1] == want[1]
+    assert got[2] == want[2]
+    # every face record appears once
+    assert mesh.n_face == len(got[0]) + len(got[1])
+    assert mesh.n_bface == len(got[2])
+
+
+@pytest.mark.parametrize("level,per", [(3, 0), (3, 1)])
+def test_uniform_counts(level, per):
+    case = Case(level=level, periodic=(per, per, per))
+    mesh = Forest(case).flatten()
+    N = 2 ** level
+    assert mesh.n_elem == N ** 3
+    assert mesh.n_face == (3 * N ** 3 if per else 3 * N * N * (N - 1))
+    assert mesh.n_bface == (0 if per else 6 * N * N)
+    assert ((mesh.face_info >> 6) & 1).sum() == (3 * N * N if per else 0)
+
+
+def test_mortar_records_are_consecutive_and_ordered():
+    case = Case(level=2)
+    mesh = hanging_forest(case, frac=0.3, seed=1)[0].flatten()
+    info = mesh.face_info
+    kind, sub = (info >> 2) & 3, (info >> 4) & 3
+    idx = np.nonzero(kind > 0)[0]
+    assert idx.size % 4 == 0 and idx.size > 0
+    for k in range(0, idx.size, 4):
+        blk = idx[k:k + 4]
+        assert (np.diff(blk) == 1).all()
+        assert list(sub[blk]) == [0, 1, 2, 3]
+        big = [mesh.face_elem[1 if kind[j] == 1 else 0, j] for j in blk]
+        assert len(set(big)) == 1
+
+
+def test_balance_is_two_to_one_after_deep_refinement():
+    case = Case(level=1)
+    f = Forest(case)
+    for _ in range(4):   # keep refining the leaf at the origin corner
+        q, lv = f.leaves()
+        flags = np.zeros(len(f), np.int8)
+        flags[0] = 1
+        f.adapt(flags, 0, 10)
+    lo, ln, lv = boxes(f, case)
+    conf, hang, _ = brute_force_faces(f, case)
+    for a, b, _ in hang:
+        assert abs(int(lv[a]) - int(lv[b])) == 1
+    mesh = f.flatten()   # flatten refuses unbalanced forests
+    assert mesh.n_elem == len(f)
+
+
+def test_watertight_face_areas():
+    """Sum of face areas seen from each element = its closed surface."""
+    case = Case(level=2, tree_len=(1.0, 2.0, 0.5))
+    mesh = hanging_forest(case, frac=0.3, seed=4)[0].flatten()
+    E = mesh.n_elem
+    h = np.array(case.tree_len)[:, None] / (2.0 ** mesh.level[None, :])
+    area = np.zeros(E)
+    for k in range(mesh.n_face):
+        info = int(mesh.face_info[k])
+        d, kind = info & 3, (info >> 2) & 3
+        s, t = [a for a in range(3) if a != d]
+        a, b = mesh.face_elem[:, k]
+        small = a if kind in (0, 1) else b
+        ar = h[s, small] * h[t, small]
+        area[a] += ar
+        area[b] += ar
+    for k in range(mesh.n_bface):
+        e, fc = mesh.bface_elem[k], mesh.bface_face[k]
+        s, t = [a for a in range(3) if a != fc // 2]
+        area[e] += h[s, e] * h[t, e]
+    surf = 2 * (h[0] * h[1] + h[1] * h[2] + h[0] * h[2])
+    assert np.allclose(area, surf, rtol=1e-14)
+
+
+def test_adapt_coarsens_complete_families_only():
+    case = Case(level=2)
+    f = Forest(case)
+    flags = -np.ones(len(f), np.int8)
+    flags[:3] = 0          # first family keeps three non-coarsening members
+    n = f.adapt(flags, 0, 5)
+    assert n == 8 + 7      # first family stays, the other 7 merge

@@ -1,0 +1,84 @@
+"""Connectivity, geometry and refinement of the host octree against the reference build.
+
+These tests run the reference's own code (oracle/_ref) and therefore only
+where the reference checkout exists.
+"""
+import numpy as np
+import pytest
+
+from charm_3d_gb300 import Case
+from charm_3d_gb300.solver import Forest
+from oracle.ref import RefSolver
+
+from .common import hanging_forest, small_case
+
+pytestmark = pytest.mark.reference
+
+
+@pytest.mark.parametrize("hang", [False, True])
+def test_reference_face_iteration_matches_flattened_mesh(hang):
+    case = small_case("random", "LF", "NONE", level=2)
+    if hang:
+        forest, flags = hanging_forest(case)
+        ref = RefSolver(case, "patched")
+        ref.refine_flags(flags, case.level + 1)
+    else:
+        forest = Forest(case)
+        ref = RefSolver(case)
+    mesh = forest.flatten()
+    faces = ref.faces()
+    conf, hang_set, bnd = set(), set(), set()
+    for r in faces:
+        ns = r[0]
+        if ns == 1:
+            bnd.add((int(r[3]), int(r[1])))
+            continue
+        f0, h0, f1, h1 = r[1], r[2], r[7], r[8]
+        assert f0 % 2 == 1 and f1 == f0 - 1, "side 0 must be the lower leaf"
+        if not h0 and not h1:
+            conf.add((int(r[3]), int(r[9]), int(f0 // 2)))
+        elif h1:
+            for k in range(4):
+                hang_set.add((int(r[3]), int(r[9 + k]), int(f0 // 2), k))
+        else:
+            for k in range(4):
+                hang_set.add((int(r[3 + k]), int(r[9]), int(f0 // 2), k))
+    got_c, got_h = set(), set()
+    for k in range(mesh.n_face):
+        a, b = (int(x) for x in mesh.face_elem[:, k])
+        info = int(mesh.face_info[k])
+        d, kind, sub = info & 3, (info >> 2) & 3, (info >> 4) & 3
+        if kind == 0:
+            got_c.add((a, b, d))
+        else:
+            got_h.add((a, b, d, sub))
+    got_b = {(int(e), int(f)) for e, f in zip(mesh.bface_elem, mesh.bface_face)}
+    assert got_c == conf and got_h == hang_set and got_b == bnd
+
+
+def test_reference_geometry_matches_box_formulas():
+    case = Case(level=2, tree_len=(1.0, 2.0, 0.5), brick=(2, 1, 1))
+    ref = RefSolver(case)
+    mesh = Forest(case).flatten()
+    g = ref.geometry()
+    h = np.array(case.tree_len)[:, None] / (2.0 ** mesh.level[None, :])
+    assert np.allclose(g[:, 0:3], mesh.center.T, rtol=0, atol=1e-15)
+    assert np.allclose(g[:, 3:6], h.T, rtol=1e-15)
+    vol = h.prod(axis=0)
+    assert np.allclose(g[:, 6], vol, rtol=1e-14)
+    ainv = g[:, 7:23].reshape(-1, 4, 4)
+    diag = np.stack([1 / vol, 12 / vol, 12 / vol, 12 / vol], axis=1)
+    assert np.allclose(np.diagonal(ainv, axis1=1, axis2=2), diag, rtol=1e-13)
+    off = ainv - np.einsum("ij,jk->ijk", diag, np.eye(4))
+    assert np.abs(off).max() <= 1e-13 * np.abs(diag).max()
+
+
+def test_reference_refinement_matches_host_adapt():
+    case = small_case("random", "HLLC", "BJ", level=2)
+    forest, flags = hanging_forest(case, frac=0.3, seed=17)
+    ref = RefSolver(case, "patched")
+    n = ref.refine_flags(flags, case.level + 1)
+    q, lv = forest.leaves()
+    rl = ref.leaves()
+    assert n == len(forest)
+    assert (rl[:, :4] == q).all() and (rl[:, 4] == lv).all()
