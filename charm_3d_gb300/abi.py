@@ -88,6 +88,7 @@ SIGNATURES = [
     ("charm_gpu_time_run", C.c_int, [_P, C.c_int, C.c_double, _DP]),
     ("charm_gpu_probe_peak", C.c_int, [C.c_int, C.c_int, _DP]),
     ("charm_gpu_abi_sizes", C.c_int, [_I64P]),
+    ("charm_gpu_residual_static", C.c_int, [C.POINTER(Config), C.POINTER(Mesh), _P, _P, _P]),
     ("charm_gpu_dims", C.c_int, [_P, _I64P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("charm_host_forest_new", C.c_int, [C.POINTER(_P), _P, _P, _P, _P, C.c_int]),
     ("charm_host_forest_free", C.c_int, [_P]),

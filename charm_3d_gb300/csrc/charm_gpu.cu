@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <chrono>
+#include <mutex>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -801,3 +802,291 @@ int charm_gpu_dims(charm_gpu_handle_t h, int64_t *n_elem, int *nv, int *nb)
 }
 
 }  // extern "C"
+
+// ============================================================================
+// Allocation-free residual: charm_gpu_residual_static (include/charm_gpu.h)
+// ============================================================================
+//
+// For callers that cannot allocate device memory themselves or let a library
+// do it for them -- code that runs where cudaMalloc is forbidden or unsafe,
+// such as a host framework that owns all device memory through its own pool
+// allocator, or a step inside a real-time loop that must not allocate.
+// They pass the mesh, the state and the output as device buffers they own;
+// the face projections this computation needs between its kernels live in
+// one file-scope __device__ array of CHARM_GPU_STATIC_SCRATCH_BYTES, which
+// every GPU that loads the library holds until the process exits.
+//
+// Set-up: the first call on a device, with that device current, resolves
+// the array's device address with cudaGetSymbolAddress.  Make that first
+// call before any stream capture.  All calls share the one array and each
+// call rewrites what it uses (control words cleared, face table reset at the
+// start of every call), so calls that overlap on the GPU (different streams
+// or host threads, or a handle's kernels running at the same time) race:
+// serialise them.
+//
+// Kernels: a table kernel (validates the face records and writes, per
+// element face, where its flux projection will be), the regular path's face
+// kernel writing into the scratch, and a gather kernel (volume integral +
+// the element's projections -> residual).
+
+namespace {
+
+constexpr size_t kScratchBytes = CHARM_GPU_STATIC_SCRATCH_BYTES;
+constexpr size_t kCtrlBytes = 256;      // control words at the start of the scratch
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_static_scratch[kScratchBytes];
+
+void *g_scratch_addr[kMaxDevices];
+std::mutex g_setup_mutex;
+
+// control words
+enum : int { kCtlBadRecord = 0, kCtlMissingFace = 1, kCtlDeviceErr = 2 };
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Per element face: (slot << 2) | tag; tag 0 = one slot, tag 1 = big side of
+// a mortar whose 4 sub-face records start at the face of `slot >> 1`.
+// Entries start at -1 (memset 0xff) and every element face must be written.
+__global__ void static_table_kernel(MeshDev m, int n_bnd, int32_t *ef, unsigned *ctl)
+{
+    const int64_t t = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t E = m.n_elem, F = m.n_face;
+    if (t < F) {
+        const int a = m.face_elem[t], b = m.face_elem[F + t];
+        const unsigned info = m.face_info[t];
+        const int d = info & 3, kind = (info >> 2) & 3, sub = (info >> 4) & 3;
+        if (a < 0 || a >= E || b < 0 || b >= E || d > 2 || kind > 2) { atomicOr(&ctl[kCtlBadRecord], 1u); return; }
+        const int fa = 2 * d + 1, fb = 2 * d;
+        if (kind == 0) {
+            ef[(int64_t) fa * E + a] = (int32_t) ((2 * t) << 2);
+            ef[(int64_t) fb * E + b] = (int32_t) ((2 * t + 1) << 2);
+            return;
+        }
+        const int small = (kind == 1) ? a : b, big = (kind == 1) ? b : a;
+        const int fs = (kind == 1) ? fa : fb, fbig = (kind == 1) ? fb : fa;
+        const int64_t ss = (kind == 1) ? 2 * t : 2 * t + 1, sb = (kind == 1) ? 2 * t + 1 : 2 * t;
+        ef[(int64_t) fs * E + small] = (int32_t) (ss << 2);
+        if (sub == 0) {
+            if (t + 3 >= F) { atomicOr(&ctl[kCtlBadRecord], 2u); return; }
+            for (int k = 1; k < 4; k++) {
+                const unsigned ik = m.face_info[t + k];
+                const int bk = (((ik >> 2) & 3) == 1) ? m.face_elem[F + t + k] : m.face_elem[t + k];
+                if (((ik >> 4) & 3) != (unsigned) k || (ik & 3) != (unsigned) d || bk != big || ((ik >> 2) & 3) != (unsigned) kind) {
+                    atomicOr(&ctl[kCtlBadRecord], 4u);
+                    return;
+                }
+            }
+            ef[(int64_t) fbig * E + big] = (int32_t) ((sb << 2) | 1);
+        }
+    } else if (t < F + m.n_bface) {
+        const int64_t j = t - F;
+        const int e = m.bface_elem[j], f = m.bface_face[j], bid = m.bface_bnd[j];
+        if (e < 0 || e >= E || f < 0 || f > 5 || bid < 0 || bid >= n_bnd) { atomicOr(&ctl[kCtlBadRecord], 8u); return; }
+        ef[(int64_t) f * E + e] = (int32_t) ((2 * F + j) << 2);
+    }
+}
+
+// Volume integral of element e plus its face projections -> res[V][B][E].
+template <typename T, int NC>
+__global__ void __launch_bounds__(128)
+static_gather_kernel(MeshDev m, const double *__restrict__ u, const T *__restrict__ slots,
+                     const int32_t *__restrict__ ef, double *__restrict__ res, unsigned *ctl)
+{
+    constexpr int V = 4 + NC;
+    const int64_t e = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t E = m.n_elem, S = m.n_slot;
+    if (e >= E) return;
+    const int lev = m.level[e];
+    const double hx = level_h(m, lev, 0), hy = level_h(m, lev, 1), hz = level_h(m, lev, 2);
+    const double vol = hx * hy * hz;
+    T c[V][kNB];
+    load_coef<T, V>(u, E, e, c);
+    T F[V], G[V], H[V];
+#pragma unroll
+    for (int v = 0; v < V; v++) F[v] = G[v] = H[v] = T(0);
+    T gr[3][kNB];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int k = 0; k < kNB; k++) gr[a][k] = T(0);
+    const bool grav = c_cfg.has_grav != 0;
+#pragma unroll 1
+    for (int g = 0; g < 8; g++) {
+        const T px = T((g & 1) ? kGaussPhi : -kGaussPhi);
+        const T py = T((g & 2) ? kGaussPhi : -kGaussPhi);
+        const T pz = T((g & 4) ? kGaussPhi : -kGaussPhi);
+        T U[V];
+#pragma unroll
+        for (int v = 0; v < V; v++) U[v] = c[v][0] + px * c[v][1] + py * c[v][2] + pz * c[v][3];
+        Prim<T, NC> p;
+        cons_to_prim<T, NC>(U, p);
+        F[0] += U[0] * p.u + p.p; F[1] += U[0] * p.v; F[2] += U[0] * p.w; F[3] += U[0] * p.e_tot + p.p * p.u;
+        G[0] += U[1] * p.u; G[1] += U[1] * p.v + p.p; G[2] += U[1] * p.w; G[3] += U[1] * p.e_tot + p.p * p.v;
+        H[0] += U[2] * p.u; H[1] += U[2] * p.v; H[2] += U[2] * p.w + p.p; H[3] += U[2] * p.e_tot + p.p * p.w;
+#pragma unroll
+        for (int i = 0; i < NC; i++) {
+            F[4 + i] += U[0] * p.c[i];
+            G[4 + i] += U[1] * p.c[i];
+            H[4 + i] += U[2] * p.c[i];
+        }
+        if (grav) {
+            const T phi[4] = {T(1), px, py, pz};
+#pragma unroll
+            for (int a = 0; a < 3; a++)
+#pragma unroll
+                for (int k = 0; k < kNB; k++) gr[a][k] += p.r * T(c_cfg.grav[a]) * phi[k];
+        }
+    }
+    const double w8 = vol * 0.125;
+    double R[V][kNB];
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+        R[v][0] = 0.0;
+        R[v][1] = -(double) F[v] * (w8 / hx);
+        R[v][2] = -(double) G[v] * (w8 / hy);
+        R[v][3] = -(double) H[v] * (w8 / hz);
+    }
+    if (grav) {
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+            for (int k = 0; k < kNB; k++) R[a][k] -= (double) gr[a][k] * w8;
+    }
+#pragma unroll 1
+    for (int f = 0; f < 6; f++) {
+        const int32_t code = ef[(int64_t) f * E + e];
+        if (code < 0) { atomicOr(&ctl[kCtlMissingFace], 1u); return; }
+        const int64_t slot = code >> 2;
+        const int nsub = (code & 1) ? 4 : 1;
+        for (int k = 0; k < nsub; k++) {
+            const int64_t sl = slot + 2 * k;
+#pragma unroll
+            for (int v = 0; v < V; v++)
+#pragma unroll
+                for (int b = 0; b < kNB; b++) R[v][b] += (double) slots[(int64_t) (v * kNB + b) * S + sl];
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < V; v++)
+#pragma unroll
+        for (int b = 0; b < kNB; b++) res[(int64_t) (v * kNB + b) * E + e] = R[v][b];
+}
+
+template <typename T, int NC>
+void launch_face_static(const charm_gpu_config_t *cfg, const MeshDev &m, const double *u, T *slots, unsigned *err,
+                        cudaStream_t st)
+{
+    const int bs = 128;
+    const int64_t nbi = (m.n_face + bs - 1) / bs, nbb = (m.n_bface + bs - 1) / bs;
+    if (nbi + nbb == 0) return;
+    const unsigned g = (unsigned) (nbi + nbb);
+    switch (cfg->flux) {
+    case CHARM_GPU_FLUX_LF: face_kernel<T, NC, CHARM_GPU_FLUX_LF><<<g, bs, 0, st>>>(m, u, slots, nbi, err); break;
+    case CHARM_GPU_FLUX_HLLC: face_kernel<T, NC, CHARM_GPU_FLUX_HLLC><<<g, bs, 0, st>>>(m, u, slots, nbi, err); break;
+    case CHARM_GPU_FLUX_CD: face_kernel<T, NC, CHARM_GPU_FLUX_CD><<<g, bs, 0, st>>>(m, u, slots, nbi, err); break;
+    default: face_kernel<T, NC, CHARM_GPU_FLUX_GODUNOV><<<g, bs, 0, st>>>(m, u, slots, nbi, err); break;
+    }
+}
+
+template <typename T, int NC>
+void run_static(const charm_gpu_config_t *cfg, const MeshDev &m, const double *u, unsigned char *base, size_t ef_off,
+                size_t slot_off, double *res, cudaStream_t st)
+{
+    unsigned *ctl = reinterpret_cast<unsigned *>(base);
+    int32_t *ef = reinterpret_cast<int32_t *>(base + ef_off);
+    T *slots = reinterpret_cast<T *>(base + slot_off);
+    launch_face_static<T, NC>(cfg, m, u, slots, &ctl[kCtlDeviceErr], st);
+    const int bs = 128;
+    static_gather_kernel<T, NC><<<(unsigned) ((m.n_elem + bs - 1) / bs), bs, 0, st>>>(m, u, slots, ef, res, ctl);
+}
+
+}  // namespace
+
+extern "C" int charm_gpu_residual_static(const charm_gpu_config_t *cfg, const charm_gpu_mesh_t *mesh, const double *u,
+                                         double *res, void *stream)
+{
+    if (!cfg || !mesh || !u || !res) return fail(CHARM_GPU_EINVAL, "null argument");
+    if (cfg->n_comp < 1 || cfg->n_comp > 2) return fail(CHARM_GPU_ENOTSUP, "1 or 2 species only");
+    if (cfg->flux < 0 || cfg->flux > 3 || cfg->n_bnd < 0 || cfg->n_bnd > CHARM_GPU_MAX_BND || cfg->use_visc ||
+        (cfg->precision != CHARM_GPU_PREC_FP64 && cfg->precision != CHARM_GPU_PREC_MIXED) ||
+        (cfg->eos != CHARM_GPU_EOS_IDEAL && cfg->eos != CHARM_GPU_EOS_MIX))
+        return fail(CHARM_GPU_EINVAL, "invalid configuration");
+    for (int i = 0; i < cfg->n_comp; i++)
+        if (!(cfg->comp[i].m > 0) || cfg->comp[i].n_cp < 1 || cfg->comp[i].n_cp > CHARM_GPU_MAX_CP)
+            return fail(CHARM_GPU_EINVAL, "invalid component");
+    const int64_t E = mesh->n_elem, F = mesh->n_face, Fb = mesh->n_bface;
+    if (E <= 0 || F < 0 || Fb < 0 || E >= (int64_t) INT32_MAX) return fail(CHARM_GPU_EINVAL, "bad mesh sizes");
+    if (!mesh->level || (F && (!mesh->face_elem || !mesh->face_info)) ||
+        (Fb && (!mesh->bface_elem || !mesh->bface_face || !mesh->bface_bnd)))
+        return fail(CHARM_GPU_EINVAL, "null mesh array");
+    const int V = 4 + cfg->n_comp;
+    const size_t tsize = cfg->precision == CHARM_GPU_PREC_MIXED ? sizeof(float) : sizeof(double);
+    int64_t S = 2 * F + Fb;
+    S += (S & 1);
+    const size_t ef_off = kCtrlBytes;
+    const size_t slot_off = align256(ef_off + (size_t) 6 * (size_t) E * sizeof(int32_t));
+    const size_t need = slot_off + (size_t) V * CHARM_GPU_BASIS * (size_t) (S > 0 ? S : 2) * tsize;
+    if (need > kScratchBytes)
+        return fail(CHARM_GPU_EINVAL, "mesh too large for charm_gpu_residual_static: needs " + std::to_string(need) +
+                                          " bytes of scratch, the static array holds " + std::to_string(kScratchBytes));
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return fail(CHARM_GPU_ECUDA, "cudaGetDevice failed");
+    if (dev < 0 || dev >= kMaxDevices) return fail(CHARM_GPU_ENOTSUP, "device index above 63");
+    {
+        // set-up, once per device, with that device current
+        std::lock_guard<std::mutex> lock(g_setup_mutex);
+        if (!g_scratch_addr[dev]) {
+            void *p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+            if (e != cudaSuccess || !p)
+                return fail(CHARM_GPU_ECUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+            g_scratch_addr[dev] = p;
+        }
+    }
+    unsigned char *base = static_cast<unsigned char *>(g_scratch_addr[dev]);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    DevCfg dcfg;
+    build_devcfg(cfg, &dcfg);
+    cudaError_t e;
+    g_cfg_owner = nullptr;   // handles re-upload their own configuration on their next launch
+    if ((e = cudaMemcpyToSymbolAsync(c_cfg, &dcfg, sizeof(DevCfg), 0, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return fail(CHARM_GPU_ECUDA, cudaGetErrorString(e));
+    // clear the control words, and mark every element face unset
+    if ((e = cudaMemsetAsync(base, 0, kCtrlBytes, st)) != cudaSuccess) return fail(CHARM_GPU_ECUDA, cudaGetErrorString(e));
+    if ((e = cudaMemsetAsync(base + ef_off, 0xff, (size_t) 6 * E * sizeof(int32_t), st)) != cudaSuccess)
+        return fail(CHARM_GPU_ECUDA, cudaGetErrorString(e));
+    MeshDev m;
+    memset(&m, 0, sizeof(m));
+    m.n_elem = E; m.n_face = F; m.n_bface = Fb; m.n_slot = S;
+    m.center = mesh->center; m.level = mesh->level;
+    m.face_elem = mesh->face_elem; m.face_info = mesh->face_info;
+    m.bface_elem = mesh->bface_elem; m.bface_face = mesh->bface_face; m.bface_bnd = mesh->bface_bnd;
+    for (int d = 0; d < 3; d++) m.tree_len[d] = mesh->tree_len[d];
+    const int bs = 256;
+    const int64_t nt = F + Fb;
+    unsigned *ctl = reinterpret_cast<unsigned *>(base);
+    if (nt > 0)
+        static_table_kernel<<<(unsigned) ((nt + bs - 1) / bs), bs, 0, st>>>(m, cfg->n_bnd,
+                                                                           reinterpret_cast<int32_t *>(base + ef_off), ctl);
+    unsigned h_ctl[4] = {0, 0, 0, 0};
+    if ((e = cudaMemcpyAsync(h_ctl, ctl, sizeof(h_ctl), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return fail(CHARM_GPU_ECUDA, cudaGetErrorString(e));
+    if (h_ctl[kCtlBadRecord]) return fail(CHARM_GPU_EINVAL, "face record out of range or mortar records not consecutive");
+    const bool mixed = cfg->precision == CHARM_GPU_PREC_MIXED;
+    switch (cfg->n_comp * 2 + (mixed ? 1 : 0)) {
+    case 2: run_static<double, 1>(cfg, m, u, base, ef_off, slot_off, res, st); break;
+    case 3: run_static<float, 1>(cfg, m, u, base, ef_off, slot_off, res, st); break;
+    case 4: run_static<double, 2>(cfg, m, u, base, ef_off, slot_off, res, st); break;
+    default: run_static<float, 2>(cfg, m, u, base, ef_off, slot_off, res, st); break;
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) return fail(CHARM_GPU_ECUDA, cudaGetErrorString(e));
+    if ((e = cudaMemcpyAsync(h_ctl, ctl, sizeof(h_ctl), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return fail(CHARM_GPU_ECUDA, cudaGetErrorString(e));
+    if (h_ctl[kCtlMissingFace]) return fail(CHARM_GPU_EINVAL, "an element face has no face record");
+    if (h_ctl[kCtlDeviceErr] & kErrNonFinite) return fail(CHARM_GPU_ENONFINITE, "non-finite state");
+    if (h_ctl[kCtlDeviceErr] & kErrHllc) return fail(CHARM_GPU_EHLLC, "HLLC: SL <= S* <= SR violated");
+    return CHARM_GPU_OK;
+}

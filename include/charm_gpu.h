@@ -207,6 +207,26 @@ int charm_gpu_probe_peak(int device, int which, double *tflops);
  * out[0] config, out[1] mesh, out[2] comp, out[3] bnd. */
 int charm_gpu_abi_sizes(int64_t out[4]);
 
+/*
+ * Residual R(u) (as charm_gpu_residual) without allocating any device
+ * memory.  No counterpart in the reference: it exists for callers that
+ * cannot call cudaMalloc, or have a library call it for them -- code whose
+ * device memory is owned by another allocator (a framework's memory pool)
+ * or that runs in a loop where allocation is not allowed.  The caller
+ * passes device buffers it owns: the mesh arrays (mesh holds DEVICE
+ * pointers, same layout as for charm_gpu_upload_mesh), the state u
+ * [V][B][E] and the output res [V][B][E].  The face projections between the
+ * kernels live in one static device array of CHARM_GPU_STATIC_SCRATCH_BYTES
+ * (about 1 KB per element in FP64, so up to ~65,000 elements); larger
+ * meshes are rejected with CHARM_GPU_EINVAL and a message.  The first call
+ * on a device (with that device current) looks up the array's address:
+ * make it before any stream capture.  All calls share the array, so calls
+ * that overlap on the GPU race; serialise them.  Synchronises `stream`.
+ */
+#define CHARM_GPU_STATIC_SCRATCH_BYTES ((size_t) 64 << 20)
+int charm_gpu_residual_static(const charm_gpu_config_t *cfg, const charm_gpu_mesh_t *mesh, const double *u, double *res,
+                              void *stream);
+
 /* Element count, variables and basis size of the uploaded mesh. */
 int charm_gpu_dims(charm_gpu_handle_t h, int64_t *n_elem, int *n_var, int *n_basis);
 
