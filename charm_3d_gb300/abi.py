@@ -95,6 +95,8 @@ SIGNATURES = [
     ("charm_host_forest_count", C.c_int64, [_P]),
     ("charm_host_forest_set_bnd", C.c_int, [_P, _P]),
     ("charm_host_forest_adapt", C.c_int, [_P, _P, C.c_int, C.c_int, _I64P]),
+    ("charm_host_forest_adapt_state", C.c_int, [_P, _P, C.c_double, C.c_int, C.c_int, C.c_int, _P, _I64P]),
+    ("charm_host_forest_state", C.c_int, [_P, C.POINTER(_DP)]),
     ("charm_host_forest_flatten", C.c_int, [_P, C.POINTER(Mesh)]),
     ("charm_host_forest_leaves", C.c_int, [_P, _P, _P]),
 ]

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <chrono>
+#include <cmath>
 #include <mutex>
 #include <cstdio>
 #include <cstring>
@@ -71,6 +72,8 @@ struct charm_gpu_handle_s {
     // state and work buffers
     double *d_u = nullptr, *d_ua = nullptr, *d_ub = nullptr;
     void *d_slots = nullptr;           // double or float [V*B][S]
+    // mixed form: FP32 hi/lo planes of u, ua, ub ([V][B][E] each)
+    float *d_fh[3] = {nullptr, nullptr, nullptr}, *d_fl[3] = {nullptr, nullptr, nullptr};
     double *d_dt = nullptr;            // CFL step (bits as unsigned long long)
     unsigned *d_err = nullptr;
     bool mesh_ready = false;
@@ -95,6 +98,11 @@ void free_mesh(charm_gpu_handle_s *h)
                     h->d_ua, h->d_ub, h->d_slots};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    for (int k = 0; k < 3; k++) {
+        if (h->d_fh[k]) cudaFree(h->d_fh[k]);
+        if (h->d_fl[k]) cudaFree(h->d_fl[k]);
+        h->d_fh[k] = h->d_fl[k] = nullptr;
+    }
     h->d_center = nullptr; h->d_level = nullptr; h->d_face_elem = nullptr; h->d_face_info = nullptr;
     h->d_bface_elem = nullptr; h->d_bface_face = nullptr; h->d_bface_bnd = nullptr;
     h->d_gather_ptr = nullptr; h->d_gather_slot = nullptr; h->d_lim_idx = nullptr; h->d_lim_kind = nullptr;
@@ -154,6 +162,7 @@ void build_devcfg(const charm_gpu_config_t *c, DevCfg *d)
         d->ideal_m = c->comp[0].m;
         d->ideal_cv = d->ideal_cp - kGasR / d->ideal_m;
         d->ideal_gam = d->ideal_cp / d->ideal_cv;
+        d->ideal_inv_cv = 1.0 / d->ideal_cv;
     }
     d->n_bnd = c->n_bnd;
     for (int b = 0; b < c->n_bnd; b++) {
@@ -162,6 +171,16 @@ void build_devcfg(const charm_gpu_config_t *c, DevCfg *d)
     }
     for (int a = 0; a < 3; a++) d->grav[a] = c->grav[a];
     d->has_grav = (c->grav[0] != 0.0 || c->grav[1] != 0.0 || c->grav[2] != 0.0);
+    // float mirrors for the FP32 instantiations
+    d->ideal_cp_f = (float) d->ideal_cp; d->ideal_m_f = (float) d->ideal_m; d->ideal_cv_f = (float) d->ideal_cv;
+    d->ideal_gam_f = (float) d->ideal_gam; d->ideal_inv_cv_f = (float) d->ideal_inv_cv;
+    for (int i = 0; i < CHARM_GPU_MAX_COMP; i++) {
+        d->comp_m_f[i] = (float) d->comp_m[i];
+        for (int k = 0; k < CHARM_GPU_MAX_CP; k++) d->comp_cp_f[i][k] = (float) d->comp_cp[i][k];
+    }
+    for (int b = 0; b < CHARM_GPU_MAX_BND; b++)
+        for (int k = 0; k < 7 + CHARM_GPU_MAX_COMP; k++) d->bnd_par_f[b][k] = (float) d->bnd_par[b][k];
+    for (int a = 0; a < 3; a++) d->grav_f[a] = (float) d->grav[a];
 }
 
 int ensure_cfg(charm_gpu_handle_s *h)
@@ -181,7 +200,10 @@ MeshDev mesh_view(const charm_gpu_handle_s *h)
     m.bface_elem = h->d_bface_elem; m.bface_face = h->d_bface_face; m.bface_bnd = h->d_bface_bnd;
     m.gather_ptr = h->d_gather_ptr; m.gather_slot = h->d_gather_slot;
     m.lim_idx = h->d_lim_idx; m.lim_kind = h->d_lim_kind;
-    for (int d = 0; d < 3; d++) m.tree_len[d] = h->tree_len[d];
+    for (int d = 0; d < 3; d++) {
+        m.tree_len[d] = h->tree_len[d];
+        m.tree_len_f[d] = (float) h->tree_len[d];
+    }
     return m;
 }
 
@@ -347,6 +369,112 @@ int step_impl(charm_gpu_handle_s *h, double dt, const double *dt_dev)
     return stage<T, NC>(h, h->d_ua, h->d_u, h->d_u, dt, dt_dev, 2.0 / 3.0, 1.0 / 3.0);
 }
 
+// ---- mixed form on FP32 hi/lo planes ---------------------------------------
+
+int64_t n_state(const charm_gpu_handle_s *h) { return (int64_t) n_var(h) * CHARM_GPU_BASIS * h->E; }
+
+// hi/lo <- d_u (to_ff) or d_u <- hi/lo of buffer 0
+int ff_convert(charm_gpu_handle_s *h, bool to_ff)
+{
+    const int64_t n = n_state(h);
+    const int bs = 256;
+    TimedLaunch t;
+    begin_launch(h, 3, &t);
+    if (to_ff) ff_from_double_kernel<<<(unsigned) ((n + bs - 1) / bs), bs, 0, h->stream>>>(h->d_u, h->d_fh[0], h->d_fl[0], n);
+    else ff_to_double_kernel<<<(unsigned) ((n + bs - 1) / bs), bs, 0, h->stream>>>(h->d_fh[0], h->d_fl[0], h->d_u, n);
+    end_launch(h, &t);
+    CUDA_TRY(cudaGetLastError());
+    return CHARM_GPU_OK;
+}
+
+struct FFCoef {
+    float h, l;
+};
+FFCoef ff_split(double x)
+{
+    const float hi = (float) x;
+    return {hi, (float) (x - (double) hi)};
+}
+
+template <int NC>
+int launch_ff_stage(charm_gpu_handle_s *h, int in, int u0, int out, FFCoef dt, const double *dt_dev, FFCoef a, FFCoef b,
+                    bool comb)
+{
+    MeshDev m = mesh_view(h);
+    const int bs = 128;
+    const unsigned nb = (unsigned) ((h->E + bs - 1) / bs);
+    const float *u0h = (u0 >= 0) ? h->d_fh[u0] : nullptr, *u0l = (u0 >= 0) ? h->d_fl[u0] : nullptr;
+    TimedLaunch t;
+    begin_launch(h, 1, &t);
+#define FF_STAGE(FL) ff_stage_kernel<NC, FL><<<nb, bs, 0, h->stream>>>(m, h->d_fh[in], h->d_fl[in], u0h, u0l, \
+        h->d_fh[out], h->d_fl[out], dt.h, dt.l, dt_dev, a.h, a.l, b.h, b.l, comb ? 1 : 0, h->d_err)
+    switch (h->cfg.flux) {
+    case CHARM_GPU_FLUX_LF: FF_STAGE(CHARM_GPU_FLUX_LF); break;
+    case CHARM_GPU_FLUX_HLLC: FF_STAGE(CHARM_GPU_FLUX_HLLC); break;
+    case CHARM_GPU_FLUX_CD: FF_STAGE(CHARM_GPU_FLUX_CD); break;
+    default: FF_STAGE(CHARM_GPU_FLUX_GODUNOV); break;
+    }
+#undef FF_STAGE
+    end_launch(h, &t);
+    CUDA_TRY(cudaGetLastError());
+    return CHARM_GPU_OK;
+}
+
+template <int NC>
+int launch_ff_limit(charm_gpu_handle_s *h, int in, int u0, int out, FFCoef a, FFCoef b, bool comb)
+{
+    MeshDev m = mesh_view(h);
+    const int bs = 128;
+    const float *u0h = (u0 >= 0) ? h->d_fh[u0] : nullptr, *u0l = (u0 >= 0) ? h->d_fl[u0] : nullptr;
+    TimedLaunch t;
+    begin_launch(h, 2, &t);
+    ff_limit_kernel<NC><<<(unsigned) ((h->E + bs - 1) / bs), bs, 0, h->stream>>>(
+        m, h->d_fh[in], h->d_fl[in], u0h, u0l, h->d_fh[out], h->d_fl[out], a.h, a.l, b.h, b.l, comb ? 1 : 0);
+    end_launch(h, &t);
+    CUDA_TRY(cudaGetLastError());
+    return CHARM_GPU_OK;
+}
+
+// one stage of the mixed form: out = a*L(in - dt*M^-1*R(in)) + b*u0
+template <int NC>
+int ff_stage(charm_gpu_handle_s *h, int in, int u0, int out, FFCoef dt, const double *dt_dev, FFCoef a, FFCoef b,
+             bool comb)
+{
+    const FFCoef one = {1.f, 0.f}, zero = {0.f, 0.f};
+    int rc;
+    if (h->cfg.limiter == CHARM_GPU_LIM_BJ) {
+        // ua (1) holds the updated stage value before the limiter
+        if ((rc = launch_ff_stage<NC>(h, in, -1, 1, dt, dt_dev, one, zero, false))) return rc;
+        return launch_ff_limit<NC>(h, 1, u0, out, a, b, comb);
+    }
+    return launch_ff_stage<NC>(h, in, u0, out, dt, dt_dev, a, b, comb);
+}
+
+// buffers: 0 = u, 1 = ua, 2 = ub (same roles as the FP64 path)
+template <int NC>
+int ff_step_impl(charm_gpu_handle_s *h, double dt, const double *dt_dev)
+{
+    int rc;
+    const FFCoef d = ff_split(dt), one = {1.f, 0.f}, zero = {0.f, 0.f};
+    const FFCoef q1 = {0.25f, 0.f}, q3 = {0.75f, 0.f}, t2 = ff_split(2.0 / 3.0), t1 = ff_split(1.0 / 3.0);
+    const bool lim = h->cfg.limiter == CHARM_GPU_LIM_BJ;
+    if (h->cfg.model == CHARM_GPU_MODEL_EULER) {
+        if (lim) return ff_stage<NC>(h, 0, -1, 0, d, dt_dev, one, zero, false);
+        if ((rc = ff_stage<NC>(h, 0, -1, 2, d, dt_dev, one, zero, false))) return rc;
+        std::swap(h->d_fh[0], h->d_fh[2]);
+        std::swap(h->d_fl[0], h->d_fl[2]);
+        return CHARM_GPU_OK;
+    }
+    if (lim) {
+        if ((rc = ff_stage<NC>(h, 0, -1, 2, d, dt_dev, one, zero, false))) return rc;
+        if ((rc = ff_stage<NC>(h, 2, 0, 2, d, dt_dev, q1, q3, true))) return rc;
+        return ff_stage<NC>(h, 2, 0, 0, d, dt_dev, t2, t1, true);
+    }
+    if ((rc = ff_stage<NC>(h, 0, -1, 2, d, dt_dev, one, zero, false))) return rc;
+    if ((rc = ff_stage<NC>(h, 2, 0, 1, d, dt_dev, q1, q3, true))) return rc;
+    return ff_stage<NC>(h, 1, 0, 0, d, dt_dev, t2, t1, true);
+}
+
 template <typename T>
 int step_dispatch_t(charm_gpu_handle_s *h, double dt, const double *dt_dev)
 {
@@ -359,12 +487,22 @@ int step_dispatch_t(charm_gpu_handle_s *h, double dt, const double *dt_dev)
 
 int step_dispatch(charm_gpu_handle_s *h, double dt, const double *dt_dev)
 {
-    if (h->cfg.precision == CHARM_GPU_PREC_MIXED) return step_dispatch_t<float>(h, dt, dt_dev);
+    if (h->cfg.precision == CHARM_GPU_PREC_MIXED) {
+        switch (h->cfg.n_comp) {
+        case 1: return ff_step_impl<1>(h, dt, dt_dev);
+        case 2: return ff_step_impl<2>(h, dt, dt_dev);
+        default: return fail(CHARM_GPU_ENOTSUP, "species count not instantiated");
+        }
+    }
     return step_dispatch_t<double>(h, dt, dt_dev);
 }
 
 int cfl_dispatch(charm_gpu_handle_s *h)
 {
+    if (h->cfg.precision == CHARM_GPU_PREC_MIXED) {
+        int rc = ff_convert(h, false);
+        if (rc) return rc;
+    }
     switch (h->cfg.n_comp) {
     case 1: return launch_cfl<1>(h, h->d_u);
     case 2: return launch_cfl<2>(h, h->d_u);
@@ -477,7 +615,7 @@ int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh)
             const int sub = (info >> 4) & 3;
             const int32_t small = (kind == 1) ? a : b, big = (kind == 1) ? b : a;
             const int fs = (kind == 1) ? fa : fb, fbig = (kind == 1) ? fb : fa;
-            lim_kind[fs * E + small] = 3; lim_idx[fs * E + small] = big;
+            lim_kind[fs * E + small] = (int8_t) (3 | (sub << 4)); lim_idx[fs * E + small] = big;
             if (sub == 0) {
                 // the 4 sub-faces of one big face must be consecutive records
                 if (i + 3 >= F) return fail(CHARM_GPU_EINVAL, "incomplete mortar");
@@ -535,6 +673,14 @@ int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh)
     CUDA_TRY(cudaMalloc(&h->d_ua, st));
     CUDA_TRY(cudaMalloc(&h->d_ub, st));
     CUDA_TRY(cudaMalloc(&h->d_slots, sl));
+    if (h->cfg.precision == CHARM_GPU_PREC_MIXED) {
+        for (int k = 0; k < 3; k++) {
+            CUDA_TRY(cudaMalloc(&h->d_fh[k], st / 2));
+            CUDA_TRY(cudaMalloc(&h->d_fl[k], st / 2));
+            CUDA_TRY(cudaMemset(h->d_fh[k], 0, st / 2));
+            CUDA_TRY(cudaMemset(h->d_fl[k], 0, st / 2));
+        }
+    }
     CUDA_TRY(cudaMemcpy(h->d_center, mesh->center, 3 * E * sizeof(double), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(h->d_level, mesh->level, E, cudaMemcpyHostToDevice));
     if (F) {
@@ -567,6 +713,10 @@ int charm_gpu_set_state(charm_gpu_handle_t h, const double *u, int on_device)
     CUDA_TRY(cudaSetDevice(h->device));
     const size_t st = (size_t) n_var(h) * CHARM_GPU_BASIS * h->E * sizeof(double);
     CUDA_TRY(cudaMemcpyAsync(h->d_u, u, st, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
+    if (h->cfg.precision == CHARM_GPU_PREC_MIXED) {
+        int rc = ff_convert(h, true);
+        if (rc) return rc;
+    }
     if (!on_device) CUDA_TRY(cudaStreamSynchronize(h->stream));
     return CHARM_GPU_OK;
 }
@@ -577,6 +727,10 @@ int charm_gpu_get_state(charm_gpu_handle_t h, double *u, int on_device)
     if (!h->mesh_ready) return fail(CHARM_GPU_ESTATE, "no mesh uploaded");
     CUDA_TRY(cudaSetDevice(h->device));
     const size_t st = (size_t) n_var(h) * CHARM_GPU_BASIS * h->E * sizeof(double);
+    if (h->cfg.precision == CHARM_GPU_PREC_MIXED) {
+        int rc = ff_convert(h, false);
+        if (rc) return rc;
+    }
     CUDA_TRY(cudaMemcpyAsync(u, h->d_u, st, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream));
     if (!on_device) CUDA_TRY(cudaStreamSynchronize(h->stream));
     return CHARM_GPU_OK;
@@ -635,6 +789,7 @@ int charm_gpu_residual(charm_gpu_handle_t h, double *res, int on_device)
     if (rc) return rc;
     if (!res) return fail(CHARM_GPU_EINVAL, "null argument");
     const bool mixed = h->cfg.precision == CHARM_GPU_PREC_MIXED;
+    if (mixed && (rc = ff_convert(h, false))) return rc;   // d_u <- hi + lo
     switch (h->cfg.n_comp * 2 + (mixed ? 1 : 0)) {
     case 2: rc = launch_face<double, 1>(h, h->d_u); if (!rc) rc = launch_cell<double, 1>(h, h->d_u, nullptr, h->d_ua, 0, nullptr, 1, 0, kCellResidual); break;
     case 3: rc = launch_face<float, 1>(h, h->d_u); if (!rc) rc = launch_cell<float, 1>(h, h->d_u, nullptr, h->d_ua, 0, nullptr, 1, 0, kCellResidual); break;
@@ -655,18 +810,58 @@ int charm_gpu_limit(charm_gpu_handle_t h)
     if (rc) return rc;
     if (h->cfg.limiter != CHARM_GPU_LIM_BJ) return CHARM_GPU_OK;
     const size_t st = (size_t) n_var(h) * CHARM_GPU_BASIS * h->E * sizeof(double);
+    const bool mixed = h->cfg.precision == CHARM_GPU_PREC_MIXED;
+    if (mixed && (rc = ff_convert(h, false))) return rc;   // d_u <- hi + lo
     CUDA_TRY(cudaMemcpyAsync(h->d_ua, h->d_u, st, cudaMemcpyDeviceToDevice, h->stream));
     switch (h->cfg.n_comp) {
-    case 1: return launch_limit<1>(h, h->d_ua, nullptr, h->d_u, 1.0, 0.0);
-    case 2: return launch_limit<2>(h, h->d_ua, nullptr, h->d_u, 1.0, 0.0);
+    case 1: rc = launch_limit<1>(h, h->d_ua, nullptr, h->d_u, 1.0, 0.0); break;
+    case 2: rc = launch_limit<2>(h, h->d_ua, nullptr, h->d_u, 1.0, 0.0); break;
     default: return fail(CHARM_GPU_ENOTSUP, "species count not instantiated");
     }
+    if (!rc && mixed) rc = ff_convert(h, true);
+    return rc;
 }
 
 int charm_gpu_refine_flags(charm_gpu_handle_t h, double max_err, int8_t *flags, double *grad_out)
 {
-    (void) h; (void) max_err; (void) flags; (void) grad_out;
-    return fail(CHARM_GPU_ENOTSUP, "refine indicator not built yet");
+    int rc = check_ready(h);
+    if (rc) return rc;
+    if (!flags && !grad_out) return fail(CHARM_GPU_EINVAL, "null argument");
+    if (h->cfg.precision == CHARM_GPU_PREC_MIXED && (rc = ff_convert(h, false))) return rc;   // d_u <- hi + lo
+    // the gradient goes through the (idle) slot buffer: 3*E doubles fit in it
+    MeshDev m = mesh_view(h);
+    double *d_grad = h->d_ua;
+    const int bs = 128;
+    TimedLaunch t;
+    begin_launch(h, 3, &t);
+    switch (h->cfg.n_comp) {
+    case 1: amr_grad_kernel<1><<<(unsigned) ((h->E + bs - 1) / bs), bs, 0, h->stream>>>(m, h->d_u, d_grad); break;
+    case 2: amr_grad_kernel<2><<<(unsigned) ((h->E + bs - 1) / bs), bs, 0, h->stream>>>(m, h->d_u, d_grad); break;
+    default: return fail(CHARM_GPU_ENOTSUP, "species count not instantiated");
+    }
+    end_launch(h, &t);
+    CUDA_TRY(cudaGetLastError());
+    std::vector<double> g(grad_out ? 0 : (size_t) (3 * h->E));
+    double *hg = grad_out ? grad_out : g.data();
+    CUDA_TRY(cudaMemcpyAsync(hg, d_grad, sizeof(double) * 3 * h->E, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    if (flags) {
+        // charm_refine_err_estimate (src/charm_amr.c:12-48), on the host with
+        // the same libm calls, so the flags follow the reference's rounding
+        std::vector<int8_t> lev((size_t) h->E);
+        CUDA_TRY(cudaMemcpy(lev.data(), h->d_level, (size_t) h->E, cudaMemcpyDeviceToHost));
+        const double err2_max = max_err * max_err;
+        for (int64_t e = 0; e < h->E; e++) {
+            double hh[3];
+            for (int d = 0; d < 3; d++) hh[d] = ldexp(h->tree_len[d], -lev[e]);
+            const double vol = hh[0] * hh[1] * hh[2];
+            double diff2 = 0.0;
+            for (int d = 0; d < 3; d++) diff2 += hg[d * h->E + e] * hg[d * h->E + e];
+            const double err2 = diff2 * (1. / 12.) * exp(log(vol) * 5. / 3.);
+            flags[e] = (err2 > err2_max * vol) ? 1 : 0;
+        }
+    }
+    return CHARM_GPU_OK;
 }
 
 int charm_gpu_set_stream(charm_gpu_handle_t h, void *stream)
@@ -1062,7 +1257,10 @@ extern "C" int charm_gpu_residual_static(const charm_gpu_config_t *cfg, const ch
     m.center = mesh->center; m.level = mesh->level;
     m.face_elem = mesh->face_elem; m.face_info = mesh->face_info;
     m.bface_elem = mesh->bface_elem; m.bface_face = mesh->bface_face; m.bface_bnd = mesh->bface_bnd;
-    for (int d = 0; d < 3; d++) m.tree_len[d] = mesh->tree_len[d];
+    for (int d = 0; d < 3; d++) {
+        m.tree_len[d] = mesh->tree_len[d];
+        m.tree_len_f[d] = (float) mesh->tree_len[d];
+    }
     const int bs = 256;
     const int64_t nt = F + Fb;
     unsigned *ctl = reinterpret_cast<unsigned *>(base);

@@ -35,7 +35,7 @@ struct DevCfg {
     int    eos;            // CHARM_GPU_EOS_*
     int    ideal_fast;     // IDEAL EOS with constant cp: cp, m, cv, gam precomputed
     int    newton_t;       // comp[0] has a cp polynomial: T by Newton (src/charm_eos.c:105,129)
-    double ideal_cp, ideal_m, ideal_cv, ideal_gam;
+    double ideal_cp, ideal_m, ideal_cv, ideal_gam, ideal_inv_cv;
     double comp_m[kMaxComp];
     double comp_cp[kMaxComp][kMaxCp];
     int    comp_ncp[kMaxComp];
@@ -46,9 +46,26 @@ struct DevCfg {
     double bnd_par[kMaxBnd][7 + kMaxComp];
     double grav[3];
     int    has_grav;
+    // FP32 mirrors (each the float rounding of the double above), read by the
+    // float instantiations so that they issue no double->float conversions:
+    // on GB300 those run on the narrow FP64 pipe.
+    float  ideal_cp_f, ideal_m_f, ideal_cv_f, ideal_gam_f, ideal_inv_cv_f;
+    float  comp_m_f[kMaxComp];
+    float  comp_cp_f[kMaxComp][kMaxCp];
+    float  bnd_par_f[kMaxBnd][7 + kMaxComp];
+    float  grav_f[3];
 };
 
 __constant__ DevCfg c_cfg;
+
+// Constant of the configuration in the arithmetic type T: the double for
+// T = double, its float mirror for T = float.
+template <typename T>
+__device__ __forceinline__ T cfgv(const double &d, const float &f)
+{
+    if constexpr (sizeof(T) == sizeof(float)) return f;
+    else return d;
+}
 
 __device__ __forceinline__ void set_error(unsigned *err, unsigned bit)
 {
@@ -68,20 +85,20 @@ struct Prim {
 template <typename T>
 __device__ __forceinline__ T comp_cp(int i, T t)
 {
-    if (c_cfg.comp_cp_type[i] == CHARM_GPU_CP_CONST) return T(c_cfg.comp_cp[i][0]);
+    if (c_cfg.comp_cp_type[i] == CHARM_GPU_CP_CONST) return cfgv<T>(c_cfg.comp_cp[i][0], c_cfg.comp_cp_f[i][0]);
     if (c_cfg.comp_ml_type[i] == CHARM_GPU_CP_POLYNOM) {
         T res = T(0), tt = T(1);
-        for (int k = 0; k < c_cfg.comp_ncp[i]; k++) { res += tt * T(c_cfg.comp_cp[i][k]); tt *= t; }
+        for (int k = 0; k < c_cfg.comp_ncp[i]; k++) { res += tt * cfgv<T>(c_cfg.comp_cp[i][k], c_cfg.comp_cp_f[i][k]); tt *= t; }
         return res;
     }
-    return T(c_cfg.comp_cp[i][0]);
+    return cfgv<T>(c_cfg.comp_cp[i][0], c_cfg.comp_cp_f[i][0]);
 }
 
 template <typename T>
 __device__ __forceinline__ T comp_cp_dt(int i, T t)
 {
     T res = T(0), tt = T(1);
-    for (int k = 1; k < c_cfg.comp_ncp[i]; k++) { res += tt * T(c_cfg.comp_cp[i][k]) * T(k); tt *= t; }
+    for (int k = 1; k < c_cfg.comp_ncp[i]; k++) { res += tt * cfgv<T>(c_cfg.comp_cp[i][k], c_cfg.comp_cp_f[i][k]) * T(k); tt *= t; }
     return res;
 }
 
@@ -92,7 +109,7 @@ template <typename T, int NC>
 __device__ void eos_calc_t(Prim<T, NC> &p)
 {
     T m_ = T(0);
-    for (int i = 0; i < NC; i++) m_ += p.c[i] / T(c_cfg.comp_m[i]);
+    for (int i = 0; i < NC; i++) m_ += p.c[i] / cfgv<T>(c_cfg.comp_m[i], c_cfg.comp_m_f[i]);
     T rm = T(kGasR) * m_;
     T tt = T(1);
     for (int j = 0; j < 100; j++) {
@@ -114,18 +131,21 @@ template <typename T, int NC>
 __device__ __forceinline__ void eos_props(Prim<T, NC> &p, int flag)
 {
     if (c_cfg.ideal_fast) {
-        p.cp = T(c_cfg.ideal_cp); p.m = T(c_cfg.ideal_m);
-        p.cv = T(c_cfg.ideal_cv); p.gam = T(c_cfg.ideal_gam);
+        p.cp = cfgv<T>(c_cfg.ideal_cp, c_cfg.ideal_cp_f); p.m = cfgv<T>(c_cfg.ideal_m, c_cfg.ideal_m_f);
+        p.cv = cfgv<T>(c_cfg.ideal_cv, c_cfg.ideal_cv_f); p.gam = cfgv<T>(c_cfg.ideal_gam, c_cfg.ideal_gam_f);
         return;
     }
     if (c_cfg.newton_t && (flag == 1 || flag == 4)) eos_calc_t<T, NC>(p);
     T t = p.t;
     if (c_cfg.eos == CHARM_GPU_EOS_IDEAL) {
         p.cp = comp_cp<T>(0, t);
-        p.m  = T(c_cfg.comp_m[0]);
+        p.m  = cfgv<T>(c_cfg.comp_m[0], c_cfg.comp_m_f[0]);
     } else {
         T cp = T(0), M_ = T(0);
-        for (int i = 0; i < NC; i++) { M_ += p.c[i] / T(c_cfg.comp_m[i]); cp += p.c[i] * comp_cp<T>(i, t); }
+        for (int i = 0; i < NC; i++) {
+            M_ += p.c[i] / cfgv<T>(c_cfg.comp_m[i], c_cfg.comp_m_f[i]);
+            cp += p.c[i] * comp_cp<T>(i, t);
+        }
         p.cp = cp;
         p.m  = T(1) / M_;
     }
@@ -187,6 +207,16 @@ __device__ __forceinline__ void cons_to_prim(const T *U, Prim<T, NC> &p)
         p.c[i] = c;
     }
     p.t = T(0);
+    if (c_cfg.ideal_fast && r >= T(kEps)) {
+        // eos flag 4 for a constant-cp ideal gas (src/charm_eos.c:86-90),
+        // with 1/r and 1/cv reused instead of dividing again
+        p.cp = cfgv<T>(c_cfg.ideal_cp, c_cfg.ideal_cp_f); p.m = cfgv<T>(c_cfg.ideal_m, c_cfg.ideal_m_f);
+        p.cv = cfgv<T>(c_cfg.ideal_cv, c_cfg.ideal_cv_f); p.gam = cfgv<T>(c_cfg.ideal_gam, c_cfg.ideal_gam_f);
+        p.p = r * p.e * (p.gam - T(1));
+        p.cz = sqrt(p.gam * p.p * ir);
+        p.t = p.e * cfgv<T>(c_cfg.ideal_inv_cv, c_cfg.ideal_inv_cv_f);
+        return;
+    }
     eos<T, NC>(p, 4);
 }
 
@@ -212,11 +242,13 @@ __device__ void bnd_cond(int bid, const Prim<T, NC> &in, Prim<T, NC> &out, const
 {
     out = in;
     const int type = c_cfg.bnd_type[bid];
-    const double *par = c_cfg.bnd_par[bid];
+    const double *pard = c_cfg.bnd_par[bid];
+    const float *parf = c_cfg.bnd_par_f[bid];
+#define par(k) cfgv<T>(pard[k], parf[k])
     switch (type) {
     case CHARM_GPU_BND_INLET:
-        out.u = T(par[0]); out.v = T(par[1]); out.w = T(par[2]);
-        out.t = T(par[3]); out.p = T(par[4]);
+        out.u = par(0); out.v = par(1); out.w = par(2);
+        out.t = par(3); out.p = par(4);
         break;
     case CHARM_GPU_BND_WALL_SLIP: {
         T svn = in.u * n[0] + in.v * n[1] + in.w * n[2];
@@ -231,30 +263,31 @@ __device__ void bnd_cond(int bid, const Prim<T, NC> &in, Prim<T, NC> &out, const
         out.u = in.u - n[0] * svn;
         out.v = in.v - n[1] * svn;
         out.w = in.w - n[2] * svn;
-        out.t = T(par[0]);
+        out.t = par(0);
         break;
     }
     case CHARM_GPU_BND_MASS_FLOW: {
-        T flow_dir = n[0] * T(par[3]) + n[1] * T(par[4]) + n[2] * T(par[5]);
+        T flow_dir = n[0] * par(3) + n[1] * par(4) + n[2] * par(5);
         if (flow_dir > T(0)) {
             T vel = out.u * n[0] + out.v * n[1] + out.w * n[2];
-            if (vel < out.cz) out.p = T(par[6]);
+            if (vel < out.cz) out.p = par(6);
         } else {
-            for (int i = 0; i < NC; i++) out.c[i] = T(par[7 + i]);
+            for (int i = 0; i < NC; i++) out.c[i] = par(7 + i);
             eos<T, NC>(out, 0);
             T v2 = out.u * out.u + out.v * out.v + out.w * out.w;
-            if (v2 > out.cz * out.cz) out.p = T(par[1]);
-            T a = T(par[0]) * (out.cp - out.cv) / (out.p * flow_dir);
+            if (v2 > out.cz * out.cz) out.p = par(1);
+            T a = par(0) * (out.cp - out.cv) / (out.p * flow_dir);
             T k = a * a / (T(2) * out.cp);
-            out.t = (T(-1) + sqrt(T(1) + T(4) * k * T(par[2]))) / (T(2) * k);
-            T vel = fabs(T(par[0]) / (out.r * flow_dir));
-            out.u = T(par[3]) * vel; out.v = T(par[4]) * vel; out.w = T(par[5]) * vel;
+            out.t = (T(-1) + sqrt(T(1) + T(4) * k * par(2))) / (T(2) * k);
+            T vel = fabs(par(0) / (out.r * flow_dir));
+            out.u = par(3) * vel; out.v = par(4) * vel; out.w = par(5) * vel;
         }
         break;
     }
     default:   // OUTLET: copy
         break;
     }
+#undef par
     eos<T, NC>(out, 3);
     out.e_tot = out.e + T(0.5) * (out.u * out.u + out.v * out.v + out.w * out.w);
 }
@@ -316,16 +349,17 @@ __device__ __forceinline__ void normal_frame(const T n[3], T nt[3][3])
     nt[2][2] = nt[0][0] * nt[1][1] - nt[0][1] * nt[1][0];
 }
 
-// F_HLLC_U / F_HLLC_V / F_HLLC_E (:319-321).
+// F_HLLC_U / F_HLLC_V / F_HLLC_E (:319-321), with the common divisor
+// 1/(SK - SS) computed once per star state (inv).
 template <typename T>
-__device__ __forceinline__ T f_hllc_u(T uk, T fk, T sk, T ss, T pk, T rk, T vk)
-{ return ((ss) * ((sk) * (uk) - (fk)) + (sk) * ((pk) + (rk) * ((sk) - (vk)) * ((ss) - (vk)))) / ((sk) - (ss)); }
+__device__ __forceinline__ T f_hllc_u(T uk, T fk, T sk, T ss, T pk, T rk, T vk, T inv)
+{ return ((ss) * ((sk) * (uk) - (fk)) + (sk) * ((pk) + (rk) * ((sk) - (vk)) * ((ss) - (vk)))) * inv; }
 template <typename T>
-__device__ __forceinline__ T f_hllc_v(T uk, T fk, T sk, T ss)
-{ return ((ss) * ((sk) * (uk) - (fk))) / ((sk) - (ss)); }
+__device__ __forceinline__ T f_hllc_v(T uk, T fk, T sk, T ss, T inv)
+{ return ((ss) * ((sk) * (uk) - (fk))) * inv; }
 template <typename T>
-__device__ __forceinline__ T f_hllc_e(T uk, T fk, T sk, T ss, T pk, T rk, T vk)
-{ return ((ss) * ((sk) * (uk) - (fk)) + (sk) * ((pk) + (rk) * ((sk) - (vk)) * ((ss) - (vk))) * (ss)) / ((sk) - (ss)); }
+__device__ __forceinline__ T f_hllc_e(T uk, T fk, T sk, T ss, T pk, T rk, T vk, T inv)
+{ return ((ss) * ((sk) * (uk) - (fk)) + (sk) * ((pk) + (rk) * ((sk) - (vk)) * ((ss) - (vk))) * (ss)) * inv; }
 
 // _charm_calc_flux_hllc_x_1 (:324-437) on states already in the normal frame
 // (u is the normal velocity), then rotated back (:505-509).
@@ -371,17 +405,19 @@ __device__ void flux_hllc(const Prim<T, NC> &pa, const Prim<T, NC> &pb, const T 
         q[3] = (pb.r * pb.e_tot + pb.p) * ub;
         for (int i = 0; i < NC; i++) q[4 + i] = pb.r * ub * pb.c[i];
     } else if (s_star >= T(0)) {
-        fu = f_hllc_u<T>(pa.r * ua, pa.r * ua * ua + pa.p, sl, s_star, pa.p, pa.r, ua);
-        fv = f_hllc_v<T>(pa.r * va, pa.r * ua * va, sl, s_star);
-        fw = f_hllc_v<T>(pa.r * wa, pa.r * ua * wa, sl, s_star);
-        q[3] = f_hllc_e<T>(pa.r * pa.e_tot, (pa.r * pa.e_tot + pa.p) * ua, sl, s_star, pa.p, pa.r, ua);
-        for (int i = 0; i < NC; i++) q[4 + i] = f_hllc_v<T>(pa.r * pa.c[i], pa.r * pa.c[i] * ua, sl, s_star);
+        const T inv = T(1) / (sl - s_star);
+        fu = f_hllc_u<T>(pa.r * ua, pa.r * ua * ua + pa.p, sl, s_star, pa.p, pa.r, ua, inv);
+        fv = f_hllc_v<T>(pa.r * va, pa.r * ua * va, sl, s_star, inv);
+        fw = f_hllc_v<T>(pa.r * wa, pa.r * ua * wa, sl, s_star, inv);
+        q[3] = f_hllc_e<T>(pa.r * pa.e_tot, (pa.r * pa.e_tot + pa.p) * ua, sl, s_star, pa.p, pa.r, ua, inv);
+        for (int i = 0; i < NC; i++) q[4 + i] = f_hllc_v<T>(pa.r * pa.c[i], pa.r * pa.c[i] * ua, sl, s_star, inv);
     } else {
-        fu = f_hllc_u<T>(pb.r * ub, pb.r * ub * ub + pb.p, sr, s_star, pb.p, pb.r, ub);
-        fv = f_hllc_v<T>(pb.r * vb, pb.r * ub * vb, sr, s_star);
-        fw = f_hllc_v<T>(pb.r * wb, pb.r * ub * wb, sr, s_star);
-        q[3] = f_hllc_e<T>(pb.r * pb.e_tot, (pb.r * pb.e_tot + pb.p) * ub, sr, s_star, pb.p, pb.r, ub);
-        for (int i = 0; i < NC; i++) q[4 + i] = f_hllc_v<T>(pb.r * pb.c[i], pb.r * pb.c[i] * ub, sr, s_star);
+        const T inv = T(1) / (sr - s_star);
+        fu = f_hllc_u<T>(pb.r * ub, pb.r * ub * ub + pb.p, sr, s_star, pb.p, pb.r, ub, inv);
+        fv = f_hllc_v<T>(pb.r * vb, pb.r * ub * vb, sr, s_star, inv);
+        fw = f_hllc_v<T>(pb.r * wb, pb.r * ub * wb, sr, s_star, inv);
+        q[3] = f_hllc_e<T>(pb.r * pb.e_tot, (pb.r * pb.e_tot + pb.p) * ub, sr, s_star, pb.p, pb.r, ub, inv);
+        for (int i = 0; i < NC; i++) q[4 + i] = f_hllc_v<T>(pb.r * pb.c[i], pb.r * pb.c[i] * ub, sr, s_star, inv);
     }
     q[0] = fu * nt[0][0] + fv * nt[1][0] + fw * nt[2][0];
     q[1] = fu * nt[0][1] + fv * nt[1][1] + fw * nt[2][1];

@@ -35,6 +35,24 @@ namespace charm {
 // coordinates (s, t) on [0,1]^2, s = the lower tangential axis:
 __constant__ double c_face_s[6] = {1.0 / 6.0, 2.0 / 3.0, 1.0 / 6.0, 5.0 / 6.0, 1.0 / 3.0, 5.0 / 6.0};
 __constant__ double c_face_t[6] = {1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0, 1.0 / 3.0, 5.0 / 6.0, 5.0 / 6.0};
+// the same points as float basis values s - 1/2, t - 1/2 (FP32 paths)
+__constant__ float c_face_psf[6] = {(float) (1.0 / 6.0 - 0.5), (float) (2.0 / 3.0 - 0.5), (float) (1.0 / 6.0 - 0.5),
+                                    (float) (5.0 / 6.0 - 0.5), (float) (1.0 / 3.0 - 0.5), (float) (5.0 / 6.0 - 0.5)};
+__constant__ float c_face_ptf[6] = {(float) (1.0 / 6.0 - 0.5), (float) (1.0 / 6.0 - 0.5), (float) (2.0 / 3.0 - 0.5),
+                                    (float) (1.0 / 3.0 - 0.5), (float) (5.0 / 6.0 - 0.5), (float) (5.0 / 6.0 - 0.5)};
+
+template <typename T>
+__device__ __forceinline__ T face_ps(int g)
+{
+    if constexpr (sizeof(T) == sizeof(float)) return c_face_psf[g];
+    else return c_face_s[g] - 0.5;
+}
+template <typename T>
+__device__ __forceinline__ T face_pt(int g)
+{
+    if constexpr (sizeof(T) == sizeof(float)) return c_face_ptf[g];
+    else return c_face_t[g] - 0.5;
+}
 
 // Cell quadrature: 2x2x2 Gauss points at +-1/sqrt(3) of the half edge, x
 // fastest (reference src/charm_geom.c:139-155).  Taylor basis value there:
@@ -53,13 +71,23 @@ struct MeshDev {
     const int32_t *gather_ptr;   // [E+1]
     const int32_t *gather_slot;  // [gather_ptr[E]]
     const int32_t *lim_idx;      // [6][E]
-    const int8_t  *lim_kind;     // [6][E]  0 same, 1 boundary, 2 big side of mortar, 3 small side
+    const int8_t  *lim_kind;     // [6][E]  bits 0-1: 0 same, 1 boundary, 2 big side of mortar,
+                                 // 3 small side (bits 4-5: its position in the big face)
     double tree_len[3];
+    float  tree_len_f[3];
 };
 
 __device__ __forceinline__ double level_h(const MeshDev &m, int lev, int d)
 {
     return ldexp(m.tree_len[d], -lev);
+}
+
+// edge length in the arithmetic type T (exact scaling by 2^-lev in both)
+template <typename T>
+__device__ __forceinline__ T level_ht(const MeshDev &m, int lev, int d)
+{
+    if constexpr (sizeof(T) == sizeof(float)) return ldexpf(m.tree_len_f[d], -lev);
+    else return ldexp(m.tree_len[d], -lev);
 }
 
 template <typename T>
@@ -109,7 +137,7 @@ __device__ __forceinline__ void interior_face(const MeshDev &m, const double *__
     // the small leaf of a mortar (src/models/euler/charm_model.c:282-285)
     const int ep = (kind == 2) ? e1 : e0;
     const int lev = m.level[ep];
-    const T w = T(level_h(m, lev, s) * level_h(m, lev, t) * (1.0 / 6.0));
+    const T w = level_ht<T>(m, lev, s) * level_ht<T>(m, lev, t) * (T(1) / T(6));
     // tangential offsets of the big side in a mortar
     const T os = T((sub & 1) ? 0.25 : -0.25), ot = T((sub & 2) ? 0.25 : -0.25);
 
@@ -128,7 +156,7 @@ __device__ __forceinline__ void interior_face(const MeshDev &m, const double *__
 
 #pragma unroll 1
     for (int g = 0; g < 6; g++) {
-        const T ps = T(c_face_s[g] - 0.5), pt = T(c_face_t[g] - 0.5);
+        const T ps = face_ps<T>(g), pt = face_pt<T>(g);
         // tangential basis values on each side
         T ps0 = ps, pt0 = pt, ps1 = ps, pt1 = pt;
         if (kind == 1) { ps1 = T(0.5) * ps + os; pt1 = T(0.5) * pt + ot; }
@@ -176,7 +204,7 @@ __device__ __forceinline__ void boundary_face(const MeshDev &m, const double *__
     constexpr int s = (D == 0) ? 1 : 0, t = (D == 2) ? 1 : 2;
     const int64_t S = m.n_slot;
     const int lev = m.level[e];
-    const T w = T(level_h(m, lev, s) * level_h(m, lev, t) * (1.0 / 6.0));
+    const T w = level_ht<T>(m, lev, s) * level_ht<T>(m, lev, t) * (T(1) / T(6));
     T c[V][kNB];
     load_coef<T, V>(u, m.n_elem, e, c);
     // outward normal (src/models/euler/charm_model.c:175-187)
@@ -187,7 +215,7 @@ __device__ __forceinline__ void boundary_face(const MeshDev &m, const double *__
     for (int v = 0; v < V; v++) S0[v] = Ss[v] = St[v] = T(0);
 #pragma unroll 1
     for (int g = 0; g < 6; g++) {
-        const T ps = T(c_face_s[g] - 0.5), pt = T(c_face_t[g] - 0.5);
+        const T ps = face_ps<T>(g), pt = face_pt<T>(g);
         T U[V];
 #pragma unroll
         for (int v = 0; v < V; v++) U[v] = c[v][0] + T(0.5) * sg * c[v][1 + D] + ps * c[v][1 + s] + pt * c[v][1 + t];
@@ -309,7 +337,7 @@ cell_kernel(MeshDev m, const double *__restrict__ u, const T *__restrict__ slots
 #pragma unroll
             for (int a = 0; a < 3; a++)
 #pragma unroll
-                for (int k = 0; k < kNB; k++) gr[a][k] += p.r * T(c_cfg.grav[a]) * phi[k];
+                for (int k = 0; k < kNB; k++) gr[a][k] += p.r * cfgv<T>(c_cfg.grav[a], c_cfg.grav_f[a]) * phi[k];
         }
     }
     const double w8 = vol * 0.125;
@@ -405,7 +433,7 @@ limit_kernel(MeshDev m, const double *__restrict__ ua, const double *u0, double 
 
 #pragma unroll 1
     for (int f = 0; f < 6; f++) {
-        const int kind = m.lim_kind[(int64_t) f * E + e];
+        const int kind = m.lim_kind[(int64_t) f * E + e] & 3;
         const int idx = m.lim_idx[(int64_t) f * E + e];
         double nbv[V];
         if (kind == 0 || kind == 3) {
@@ -538,6 +566,569 @@ __global__ void __launch_bounds__(256) fma_peak_kernel(T *out, int iters)
 #pragma unroll
     for (int k = 0; k < kPeakChains; k++) s += a[k];
     out[(size_t) blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+
+// ===========================================================================
+// Mixed form: element-owned fused stage on an FP32 hi/lo state
+// ===========================================================================
+//
+// The stage state of the mixed form is kept as two FP32 planes, u = hi + lo
+// (same 8 bytes per coefficient as FP64, ~48-bit significand), so that the
+// stage kernel issues no FP64 instruction: on GB300 the FP64 pipe is ~1/64
+// of FP32, and conversions from a double state kept it 77-82 % busy.
+// One thread per element computes the volume integral, the fluxes of all its
+// faces (each face is computed by both of its owners, from the same operands
+// at one code location, so the two contributions are exact negatives), the
+// M^-1 scaling and the update, with error-free FP32 transformations for
+// u - dt*M^-1*R and the SSP combinations.  No face buffer goes through HBM.
+
+struct FF { float h, l; };
+
+__device__ __forceinline__ FF ff_two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return {s, e};
+}
+
+__device__ __forceinline__ FF ff_renorm(float s, float e)
+{
+    const float h = __fadd_rn(s, e);
+    return {h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+
+// x - (dh + dl) * r
+__device__ __forceinline__ FF ff_sub_scaled(FF x, float r, float dh, float dl)
+{
+    const float ph = __fmul_rn(dh, r);
+    float pl = __fmaf_rn(dh, r, -ph);
+    pl = __fmaf_rn(dl, r, pl);
+    const FF s = ff_two_sum(x.h, -ph);
+    const float e = __fadd_rn(s.l, __fsub_rn(x.l, pl));
+    return ff_renorm(s.h, e);
+}
+
+// (ah + al) * y + (bh + bl) * w
+__device__ __forceinline__ FF ff_comb(FF y, FF w, float ah, float al, float bh, float bl)
+{
+    const float p = __fmul_rn(ah, y.h);
+    float pe = __fmaf_rn(ah, y.h, -p);
+    pe = __fmaf_rn(ah, y.l, pe);
+    pe = __fmaf_rn(al, y.h, pe);
+    const float q = __fmul_rn(bh, w.h);
+    float qe = __fmaf_rn(bh, w.h, -q);
+    qe = __fmaf_rn(bh, w.l, qe);
+    qe = __fmaf_rn(bl, w.h, qe);
+    const FF s = ff_two_sum(p, q);
+    return ff_renorm(s.h, __fadd_rn(s.l, __fadd_rn(pe, qe)));
+}
+
+__global__ void __launch_bounds__(256) ff_from_double_kernel(const double *__restrict__ u, float *__restrict__ hi,
+                                                             float *__restrict__ lo, int64_t n)
+{
+    const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double x = u[i];
+    const float h = __double2float_rn(x);
+    hi[i] = h;
+    lo[i] = __double2float_rn(x - (double) h);
+}
+
+__global__ void __launch_bounds__(256) ff_to_double_kernel(const float *__restrict__ hi, const float *__restrict__ lo,
+                                                           double *__restrict__ u, int64_t n)
+{
+    const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    u[i] = (double) hi[i] + (double) lo[i];
+}
+
+template <int V>
+__device__ __forceinline__ void load_coef_f(const float *__restrict__ u, int64_t E, int64_t e, float c[V][kNB])
+{
+#pragma unroll
+    for (int v = 0; v < V; v++)
+#pragma unroll
+        for (int k = 0; k < kNB; k++) c[v][k] = __ldg(u + (int64_t) (v * kNB + k) * E + e);
+}
+
+// Flux of one (sub-)face along axis D from the lower and upper leaves'
+// coefficients, projected on the owner's basis and added to R.
+//   kind: 0 conforming, 1 lower leaf is the small one, 2 upper leaf is small
+//   sub : position of the small face in the big face
+//   w   : gw*gj of one point of the (small) face
+// R[v][0] += x with the rounding error kept in R0l[v] (two-sum), so that the
+// mean coefficient's residual is the element's face contributions summed
+// without loss: the two owners of a face add exact negatives, and the total
+// mass change of a stage cancels to the float-float level.
+__device__ __forceinline__ void acc0(float &hi, float &lo, float x)
+{
+    const FF s = ff_two_sum(hi, x);
+    hi = s.h;
+    lo = __fadd_rn(lo, s.l);
+}
+
+template <int NC, int FLUX, int D>
+__device__ __forceinline__ void owned_face(const float cl[4 + NC][kNB], const float cu[4 + NC][kNB], int kind, int sub,
+                                           bool own_lower, float w, float R[4 + NC][kNB], float R0l[4 + NC],
+                                           unsigned *err)
+{
+    constexpr int V = 4 + NC;
+    constexpr int s = (D == 0) ? 1 : 0, t = (D == 2) ? 1 : 2;
+    const float os = (sub & 1) ? 0.25f : -0.25f, ot = (sub & 2) ? 0.25f : -0.25f;
+    float n[3] = {0.f, 0.f, 0.f};
+    n[D] = 1.f;
+    float S0[V], Ss[V], St[V];
+#pragma unroll
+    for (int v = 0; v < V; v++) S0[v] = Ss[v] = St[v] = 0.f;
+#pragma unroll 1
+    for (int g = 0; g < 6; g++) {
+        const float ps = c_face_psf[g], pt = c_face_ptf[g];
+        float psl = ps, ptl = pt, psu = ps, ptu = pt;
+        if (kind == 2) { psl = 0.5f * ps + os; ptl = 0.5f * pt + ot; }
+        if (kind == 1) { psu = 0.5f * ps + os; ptu = 0.5f * pt + ot; }
+        float Ul[V], Uu[V];
+#pragma unroll
+        for (int v = 0; v < V; v++) {
+            Ul[v] = cl[v][0] + 0.5f * cl[v][1 + D] + psl * cl[v][1 + s] + ptl * cl[v][1 + t];
+            Uu[v] = cu[v][0] - 0.5f * cu[v][1 + D] + psu * cu[v][1 + s] + ptu * cu[v][1 + t];
+        }
+        Prim<float, NC> pl, pu;
+        cons_to_prim<float, NC>(Ul, pl);
+        cons_to_prim<float, NC>(Uu, pu);
+        float q[V];
+        num_flux<FLUX, float, NC>(pl, pu, n, q, err);
+#pragma unroll
+        for (int v = 0; v < V; v++) {
+            S0[v] += q[v];
+            Ss[v] += q[v] * ps;
+            St[v] += q[v] * pt;
+        }
+    }
+    // projection on the owner's basis (lower side gets +, upper side -)
+    const bool own_big = (own_lower && kind == 2) || (!own_lower && kind == 1);
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+        const float a0 = w * S0[v];
+        float as = w * Ss[v], at = w * St[v];
+        if (own_big) { as = 0.5f * as + os * a0; at = 0.5f * at + ot * a0; }
+        const float sg = own_lower ? 1.f : -1.f;
+        acc0(R[v][0], R0l[v], sg * a0);
+        R[v][1 + D] += 0.5f * a0;
+        R[v][1 + s] += sg * as;
+        R[v][1 + t] += sg * at;
+    }
+}
+
+template <int NC, int FLUX, int D>
+__device__ __forceinline__ void owned_boundary(const MeshDev &m, const float c[4 + NC][kNB], int j, float w,
+                                               float R[4 + NC][kNB], float R0l[4 + NC], unsigned *err)
+{
+    constexpr int V = 4 + NC;
+    constexpr int s = (D == 0) ? 1 : 0, t = (D == 2) ? 1 : 2;
+    const int f = m.bface_face[j], bid = m.bface_bnd[j];
+    const float sg = (f & 1) ? 1.f : -1.f;
+    float n[3] = {0.f, 0.f, 0.f};
+    n[D] = sg;
+    float S0[V], Ss[V], St[V];
+#pragma unroll
+    for (int v = 0; v < V; v++) S0[v] = Ss[v] = St[v] = 0.f;
+#pragma unroll 1
+    for (int g = 0; g < 6; g++) {
+        const float ps = c_face_psf[g], pt = c_face_ptf[g];
+        float U[V];
+#pragma unroll
+        for (int v = 0; v < V; v++) U[v] = c[v][0] + 0.5f * sg * c[v][1 + D] + ps * c[v][1 + s] + pt * c[v][1 + t];
+        Prim<float, NC> pin, pout;
+        cons_to_prim<float, NC>(U, pin);
+        bnd_cond<float, NC>(bid, pin, pout, n);
+        float q[V];
+        num_flux<FLUX, float, NC>(pin, pout, n, q, err);
+#pragma unroll
+        for (int v = 0; v < V; v++) {
+            S0[v] += q[v];
+            Ss[v] += q[v] * ps;
+            St[v] += q[v] * pt;
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+        const float a0 = w * S0[v];
+        acc0(R[v][0], R0l[v], a0);
+        R[v][1 + D] += 0.5f * sg * a0;
+        R[v][1 + s] += w * Ss[v];
+        R[v][1 + t] += w * St[v];
+    }
+}
+
+// The two faces of element e along axis D (lower face 2D, upper face 2D+1).
+template <int NC, int FLUX, int D>
+__device__ __forceinline__ void owned_axis(const MeshDev &m, const float *__restrict__ uh, int64_t e,
+                                           const float c[4 + NC][kNB], int lev, float R[4 + NC][kNB],
+                                           float R0l[4 + NC], unsigned *err)
+{
+    constexpr int V = 4 + NC;
+    constexpr int s = (D == 0) ? 1 : 0, t = (D == 2) ? 1 : 2;
+    const int64_t E = m.n_elem;
+#pragma unroll 1
+    for (int side = 0; side < 2; side++) {
+        const int f = 2 * D + side;
+        const int code = m.lim_kind[(int64_t) f * E + e];
+        const int idx = m.lim_idx[(int64_t) f * E + e];
+        const int kind = code & 3;
+        if (kind == 1) {   // boundary
+            const float w = level_ht<float>(m, lev, s) * level_ht<float>(m, lev, t) * (1.f / 6.f);
+            owned_boundary<NC, FLUX, D>(m, c, idx, w, R, R0l, err);
+            continue;
+        }
+        const bool own_lower = (side == 1);
+        const int nsub = (kind == 2) ? 4 : 1;
+#pragma unroll 1
+        for (int k = 0; k < nsub; k++) {
+            int nb, rec_kind, sub, small_lev;
+            if (kind == 2) {   // we are the big leaf: record idx+k holds small leaf k
+                const int64_t fi = idx + k;
+                const unsigned info = m.face_info[fi];
+                rec_kind = (info >> 2) & 3;
+                nb = (rec_kind == 1) ? m.face_elem[fi] : m.face_elem[m.n_face + fi];
+                sub = k;
+                small_lev = m.level[nb];
+            } else {
+                nb = idx;
+                sub = (code >> 4) & 3;
+                rec_kind = (kind == 0) ? 0 : (own_lower ? 1 : 2);
+                small_lev = lev;
+            }
+            float cn[V][kNB];
+            load_coef_f<V>(uh, E, nb, cn);
+            float cl[V][kNB], cu[V][kNB];
+#pragma unroll
+            for (int v = 0; v < V; v++)
+#pragma unroll
+                for (int b = 0; b < kNB; b++) {
+                    cl[v][b] = own_lower ? c[v][b] : cn[v][b];
+                    cu[v][b] = own_lower ? cn[v][b] : c[v][b];
+                }
+            const float w = level_ht<float>(m, small_lev, s) * level_ht<float>(m, small_lev, t) * (1.f / 6.f);
+            owned_face<NC, FLUX, D>(cl, cu, rec_kind, sub, own_lower, w, R, R0l, err);
+        }
+    }
+}
+
+// One stage of the mixed form:
+//   out = (ah+al) * (u - dt*M^-1*R(u)) + (bh+bl) * u0     (comb != 0)
+//   out = u - dt*M^-1*R(u)                                 (comb == 0)
+// all planes FP32 hi/lo; dt = dth + dtl (or *dt_dev when given).
+template <int NC, int FLUX>
+__global__ void __launch_bounds__(128)
+ff_stage_kernel(MeshDev m, const float *__restrict__ uh, const float *__restrict__ ul, const float *u0h,
+                const float *u0l, float *oh, float *ol, float dth, float dtl, const double *__restrict__ dt_dev,
+                float ah, float al, float bh, float bl, int comb, unsigned *err)
+{
+    constexpr int V = 4 + NC;
+    const int64_t e = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t E = m.n_elem;
+    if (e >= E) return;
+    const int lev = m.level[e];
+    const float hx = level_ht<float>(m, lev, 0), hy = level_ht<float>(m, lev, 1), hz = level_ht<float>(m, lev, 2);
+    const float vol = hx * hy * hz;
+
+    float c[V][kNB];
+    load_coef_f<V>(uh, E, e, c);
+    float R[V][kNB], R0l[V];
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+        R0l[v] = 0.f;
+#pragma unroll
+        for (int k = 0; k < kNB; k++) R[v][k] = 0.f;
+    }
+
+    // volume integral (src/models/ns/charm_model_ns_conv.c:23-89)
+    {
+        float F[V], G[V], H[V];
+#pragma unroll
+        for (int v = 0; v < V; v++) F[v] = G[v] = H[v] = 0.f;
+        const bool grav = c_cfg.has_grav != 0;
+        float gr[3][kNB];
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+            for (int k = 0; k < kNB; k++) gr[a][k] = 0.f;
+#pragma unroll 1
+        for (int g = 0; g < 8; g++) {
+            const float px = (g & 1) ? (float) kGaussPhi : -(float) kGaussPhi;
+            const float py = (g & 2) ? (float) kGaussPhi : -(float) kGaussPhi;
+            const float pz = (g & 4) ? (float) kGaussPhi : -(float) kGaussPhi;
+            float U[V];
+#pragma unroll
+            for (int v = 0; v < V; v++) U[v] = c[v][0] + px * c[v][1] + py * c[v][2] + pz * c[v][3];
+            Prim<float, NC> p;
+            cons_to_prim<float, NC>(U, p);
+            if (!(p.r > 0.f) || !(p.p > 0.f)) set_error(err, (isfinite(p.r) && isfinite(p.p)) ? kErrNegative : kErrNonFinite);
+            F[0] += U[0] * p.u + p.p; F[1] += U[0] * p.v; F[2] += U[0] * p.w; F[3] += U[0] * p.e_tot + p.p * p.u;
+            G[0] += U[1] * p.u; G[1] += U[1] * p.v + p.p; G[2] += U[1] * p.w; G[3] += U[1] * p.e_tot + p.p * p.v;
+            H[0] += U[2] * p.u; H[1] += U[2] * p.v; H[2] += U[2] * p.w + p.p; H[3] += U[2] * p.e_tot + p.p * p.w;
+#pragma unroll
+            for (int i = 0; i < NC; i++) {
+                F[4 + i] += U[0] * p.c[i];
+                G[4 + i] += U[1] * p.c[i];
+                H[4 + i] += U[2] * p.c[i];
+            }
+            if (grav) {
+                const float phi[4] = {1.f, px, py, pz};
+#pragma unroll
+                for (int a = 0; a < 3; a++)
+#pragma unroll
+                    for (int k = 0; k < kNB; k++) gr[a][k] += p.r * c_cfg.grav_f[a] * phi[k];
+            }
+        }
+        const float w8 = vol * 0.125f;
+#pragma unroll
+        for (int v = 0; v < V; v++) {
+            R[v][1] -= F[v] * (w8 / hx);
+            R[v][2] -= G[v] * (w8 / hy);
+            R[v][3] -= H[v] * (w8 / hz);
+        }
+        if (grav) {
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                acc0(R[a][0], R0l[a], -gr[a][0] * w8);
+#pragma unroll
+                for (int k = 1; k < kNB; k++) R[a][k] -= gr[a][k] * w8;
+            }
+        }
+    }
+    // faces
+    owned_axis<NC, FLUX, 0>(m, uh, e, c, lev, R, R0l, err);
+    owned_axis<NC, FLUX, 1>(m, uh, e, c, lev, R, R0l, err);
+    owned_axis<NC, FLUX, 2>(m, uh, e, c, lev, R, R0l, err);
+
+    // update with diagonal M^-1 = (1/vol, 12/vol, 12/vol, 12/vol)
+    if (dt_dev) {
+        const double d = *dt_dev;
+        dth = __double2float_rn(d);
+        dtl = __double2float_rn(d - (double) dth);
+    }
+    const float minv0 = 1.f / vol, minv1 = 12.f / vol;
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+#pragma unroll
+        for (int k = 0; k < kNB; k++) {
+            const int64_t idx = (int64_t) (v * kNB + k) * E + e;
+            FF x = {uh[idx], ul[idx]};
+            FF y;
+            if (k == 0) {   // mean coefficient: (R + R0l) * minv0 kept as float-float
+                const float rh = __fmul_rn(R[v][0], minv0);
+                const float rl = __fmaf_rn(R0l[v], minv0, __fmaf_rn(R[v][0], minv0, -rh));
+                y = ff_sub_scaled(x, rh, dth, dtl);
+                y = ff_sub_scaled(y, rl, dth, dtl);
+            } else {
+                y = ff_sub_scaled(x, R[v][k] * minv1, dth, dtl);
+            }
+            if (comb) {
+                const FF w0 = {u0h[idx], u0l[idx]};
+                y = ff_comb(y, w0, ah, al, bh, bl);
+            }
+            oh[idx] = y.h;
+            ol[idx] = y.l;
+        }
+    }
+}
+
+// Barth-Jespersen limiter of the mixed form on hi/lo planes (the same rules
+// as limit_kernel; bounds and psi in FP32, coefficients scaled in hi/lo),
+// fused with the SSP combination.
+template <int NC>
+__global__ void __launch_bounds__(128)
+ff_limit_kernel(MeshDev m, const float *__restrict__ ah_, const float *__restrict__ al_, const float *u0h,
+                const float *u0l, float *oh, float *ol, float ah, float al, float bh, float bl, int comb)
+{
+    constexpr int V = 4 + NC;
+    const int64_t e = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t E = m.n_elem;
+    if (e >= E) return;
+    float c[V][kNB];
+    load_coef_f<V>(ah_, E, e, c);
+    float umin[V], umax[V];
+#pragma unroll
+    for (int v = 0; v < V; v++) umin[v] = umax[v] = c[v][0];
+#pragma unroll 1
+    for (int f = 0; f < 6; f++) {
+        const int kind = m.lim_kind[(int64_t) f * E + e] & 3;
+        const int idx = m.lim_idx[(int64_t) f * E + e];
+        float nbv[V];
+        if (kind == 0 || kind == 3) {
+#pragma unroll
+            for (int v = 0; v < V; v++) nbv[v] = __ldg(ah_ + (int64_t) (v * kNB) * E + idx);
+        } else if (kind == 2) {
+            float svol = 0.f;
+#pragma unroll
+            for (int v = 0; v < V; v++) nbv[v] = 0.f;
+            for (int k = 0; k < 4; k++) {
+                const int64_t fi = idx + k;
+                const unsigned info = m.face_info[fi];
+                const int small = (((info >> 2) & 3) == 1) ? m.face_elem[fi] : m.face_elem[m.n_face + fi];
+                const int ls = m.level[small];
+                const float vs = level_ht<float>(m, ls, 0) * level_ht<float>(m, ls, 1) * level_ht<float>(m, ls, 2);
+                svol += vs;
+#pragma unroll
+                for (int v = 0; v < V; v++) nbv[v] += __ldg(ah_ + (int64_t) (v * kNB) * E + small) * vs;
+            }
+#pragma unroll
+            for (int v = 0; v < V; v++) nbv[v] /= svol;
+        } else {
+            const int fb = m.bface_face[idx], bid = m.bface_bnd[idx];
+            float n[3] = {0.f, 0.f, 0.f};
+            n[fb >> 1] = (fb & 1) ? 1.f : -1.f;
+            float U[V];
+#pragma unroll
+            for (int v = 0; v < V; v++) U[v] = c[v][0];
+            Prim<float, NC> pin, pout;
+            cons_to_prim<float, NC>(U, pin);
+            bnd_cond<float, NC>(bid, pin, pout, n);
+            prim_to_cons<float, NC>(pout, nbv);
+        }
+#pragma unroll
+        for (int v = 0; v < V; v++) {
+            umin[v] = fminf(umin[v], nbv[v]);
+            umax[v] = fmaxf(umax[v], nbv[v]);
+        }
+    }
+    float psi[V];
+#pragma unroll
+    for (int v = 0; v < V; v++) psi[v] = 1.f;
+#pragma unroll
+    for (int vx = 0; vx < 8; vx++) {
+        const float sx = (vx & 1) ? 0.5f : -0.5f, sy = (vx & 2) ? 0.5f : -0.5f, sz = (vx & 4) ? 0.5f : -0.5f;
+#pragma unroll
+        for (int v = 0; v < V; v++) {
+            const float df = sx * c[v][1] + sy * c[v][2] + sz * c[v][3];
+            float pt = 1.f;
+            if (fabsf(df) > (float) kEps) {
+                if (df > 0.f) pt = fminf(1.f, (umax[v] - c[v][0]) / df);
+                else pt = fminf(1.f, (umin[v] - c[v][0]) / df);
+            }
+            psi[v] = fminf(psi[v], pt);
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+#pragma unroll
+        for (int k = 0; k < kNB; k++) {
+            const int64_t idx = (int64_t) (v * kNB + k) * E + e;
+            FF y = {ah_[idx], al_[idx]};
+            if (k > 0) {   // psi * y, error-free product on the hi part
+                const float p = __fmul_rn(psi[v], y.h);
+                const float pe = __fmaf_rn(psi[v], y.l, __fmaf_rn(psi[v], y.h, -p));
+                y = ff_renorm(p, pe);
+            }
+            if (comb) {
+                const FF w0 = {u0h[idx], u0l[idx]};
+                y = ff_comb(y, w0, ah, al, bh, bl);
+            }
+            oh[idx] = y.h;
+            ol[idx] = y.l;
+        }
+    }
+}
+
+
+// ===========================================================================
+// AMR indicator: density-gradient estimate of charm_adapt
+// (src/charm_amr.c:350-573): grad = (1/vol) * sum over the element's faces
+// of 0.5*(rho_L + rho_R) * n * gw*gj at the 6 face points, n pointing out of
+// side 0 (side 0 adds, side 1 subtracts); boundary faces use the boundary
+// condition's ghost density.  FP64, one thread per element.
+// ===========================================================================
+
+template <int NC>
+__device__ __forceinline__ double point_density(const double c[4 + NC][kNB], double pd, int D, double ps, double pt)
+{
+    const int s = (D == 0) ? 1 : 0, t = (D == 2) ? 1 : 2;
+    double r = 0.0;
+#pragma unroll
+    for (int i = 0; i < NC; i++)
+        r += c[4 + i][0] + pd * c[4 + i][1 + D] + ps * c[4 + i][1 + s] + pt * c[4 + i][1 + t];
+    return r < kEps ? kEps : r;   // prim.r after eos flag 4 (src/charm_eos.c:87)
+}
+
+template <int NC>
+__global__ void __launch_bounds__(128) amr_grad_kernel(MeshDev m, const double *__restrict__ u, double *__restrict__ grad)
+{
+    constexpr int V = 4 + NC;
+    const int64_t e = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t E = m.n_elem;
+    if (e >= E) return;
+    const int lev = m.level[e];
+    double c[V][kNB];
+    load_coef<double, V>(u, E, e, c);
+    double g[3] = {0.0, 0.0, 0.0};
+#pragma unroll 1
+    for (int f = 0; f < 6; f++) {
+        const int D = f >> 1;
+        const int s = (D == 0) ? 1 : 0, t = (D == 2) ? 1 : 2;
+        const int code = m.lim_kind[(int64_t) f * E + e];
+        const int kind = code & 3, idx = m.lim_idx[(int64_t) f * E + e];
+        if (kind == 1) {   // boundary
+            const int fb = m.bface_face[idx], bid = m.bface_bnd[idx];
+            const double sg = (fb & 1) ? 1.0 : -1.0;
+            double n[3] = {0.0, 0.0, 0.0};
+            n[D] = sg;
+            const double w = level_h(m, lev, s) * level_h(m, lev, t) * (1.0 / 6.0);
+            for (int q = 0; q < 6; q++) {
+                const double ps = c_face_s[q] - 0.5, pt = c_face_t[q] - 0.5;
+                double U[V];
+#pragma unroll
+                for (int v = 0; v < V; v++) {
+                    double x = c[v][0] + 0.5 * sg * c[v][1 + D];
+                    x += ps * c[v][1 + s];
+                    x += pt * c[v][1 + t];
+                    U[v] = x;
+                }
+                Prim<double, NC> pin, pout;
+                cons_to_prim<double, NC>(U, pin);
+                bnd_cond<double, NC>(bid, pin, pout, n);
+                g[D] += 0.5 * (pin.r + pout.r) * w * sg;
+            }
+            continue;
+        }
+        const bool own_lower = (f & 1);
+        const int nsub = (kind == 2) ? 4 : 1;
+        for (int k = 0; k < nsub; k++) {
+            int nb, rec_kind, sub, plev;
+            if (kind == 2) {
+                const unsigned info = m.face_info[idx + k];
+                rec_kind = (info >> 2) & 3;
+                nb = (rec_kind == 1) ? m.face_elem[idx + k] : m.face_elem[m.n_face + idx + k];
+                sub = k;
+                plev = m.level[nb];
+            } else {
+                nb = idx;
+                sub = (code >> 4) & 3;
+                rec_kind = (kind == 0) ? 0 : (own_lower ? 1 : 2);
+                plev = lev;
+            }
+            double cn[V][kNB];
+            load_coef<double, V>(u, E, nb, cn);
+            const double os = (sub & 1) ? 0.25 : -0.25, ot = (sub & 2) ? 0.25 : -0.25;
+            const double w = level_h(m, plev, s) * level_h(m, plev, t) * (1.0 / 6.0);
+            double acc = 0.0;
+            for (int q = 0; q < 6; q++) {
+                const double ps = c_face_s[q] - 0.5, pt = c_face_t[q] - 0.5;
+                double psl = ps, ptl = pt, psu = ps, ptu = pt;
+                if (rec_kind == 2) { psl = 0.5 * ps + os; ptl = 0.5 * pt + ot; }
+                if (rec_kind == 1) { psu = 0.5 * ps + os; ptu = 0.5 * pt + ot; }
+                const double rl = own_lower ? point_density<NC>(c, 0.5, D, psl, ptl) : point_density<NC>(cn, 0.5, D, psl, ptl);
+                const double ru = own_lower ? point_density<NC>(cn, -0.5, D, psu, ptu) : point_density<NC>(c, -0.5, D, psu, ptu);
+                acc += 0.5 * (rl + ru) * w;
+            }
+            g[D] += own_lower ? acc : -acc;
+        }
+    }
+    const double vol = level_h(m, lev, 0) * level_h(m, lev, 1) * level_h(m, lev, 2);
+#pragma unroll
+    for (int k = 0; k < 3; k++) grad[(int64_t) k * E + e] = g[k] / vol;
 }
 
 }  // namespace charm

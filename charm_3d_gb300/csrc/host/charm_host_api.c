@@ -23,6 +23,7 @@
 struct charm_host_forest_s {
     charm_forest_t f;
     int8_t bnd_of_side[6];
+    double *state;          /* state projected by the last charm_host_forest_adapt_state */
     /* flattened arrays (owned) */
     double  *center;
     int8_t  *level;
@@ -62,6 +63,7 @@ int charm_host_forest_free(charm_host_forest_t h)
 {
     if (!h) return CHARM_GPU_EINVAL;
     free_flat(h);
+    free(h->state);
     charm_forest_free(&h->f);
     free(h);
     return CHARM_GPU_OK;
@@ -247,5 +249,219 @@ int charm_host_forest_flatten(charm_host_forest_t h, charm_gpu_mesh_t *mesh)
     mesh->bface_elem = h->bface_elem;
     mesh->bface_face = h->bface_face;
     mesh->bface_bnd = h->bface_bnd;
+    return CHARM_GPU_OK;
+}
+
+/* ---- adapt with the state (charm_adapt, reference src/charm_amr.c:575-610) ---- */
+
+#include <math.h>
+
+static void leaf_h(const charm_forest_t *f, int level, double h[3])
+{
+    for (int d = 0; d < 3; d++) h[d] = ldexp(f->tree_len[d], -level);
+}
+
+/* charm_error_sqr_estimate (src/charm_amr.c:12-30) */
+static double err_sqr(const double *grad, int64_t E, int64_t i, double vol)
+{
+    double diff2 = 0.;
+    for (int k = 0; k < 3; k++) diff2 += grad[k * E + i] * grad[k * E + i];
+    return diff2 * (1. / 12.) * exp(log(vol) * 5. / 3.);
+}
+
+/* p1 L2 projection parent -> child for boxes (charm_replace_quads,
+ * src/charm_amr.c:268-305): the child keeps the parent's linear function. */
+static void project_down(const double *u, int64_t E, int64_t p, double *w, int64_t En, int64_t c, int cid, int V)
+{
+    const double o[3] = {(cid & 1) ? 0.25 : -0.25, (cid & 2) ? 0.25 : -0.25, (cid & 4) ? 0.25 : -0.25};
+    for (int v = 0; v < V; v++) {
+        const double *P = u + (int64_t) v * 4 * E;
+        double *C = w + (int64_t) v * 4 * En;
+        C[c] = P[p] + o[0] * P[E + p] + o[1] * P[2 * E + p] + o[2] * P[3 * E + p];
+        for (int k = 1; k < 4; k++) C[(int64_t) k * En + c] = 0.5 * P[(int64_t) k * E + p];
+    }
+}
+
+/* p1 L2 projection of 8 children onto their parent (charm_replace_quads,
+ * src/charm_amr.c:218-266) for boxes: mean of the means, and slopes from the
+ * children's means and slopes. */
+static void project_up(const double *u, int64_t E, const int64_t ch[8], const int cid[8], double *w, int64_t En,
+                       int64_t p, int V)
+{
+    for (int v = 0; v < V; v++) {
+        const double *C = u + (int64_t) v * 4 * E;
+        double *P = w + (int64_t) v * 4 * En;
+        double m = 0., s[3] = {0., 0., 0.};
+        for (int i = 0; i < 8; i++) {
+            m += C[ch[i]];
+            for (int k = 0; k < 3; k++) {
+                const double sg = (cid[i] >> k) & 1 ? 0.375 : -0.375;
+                s[k] += sg * C[ch[i]] + C[(int64_t) (k + 1) * E + ch[i]] * (1. / 16.);
+            }
+        }
+        P[p] = m * 0.125;
+        for (int k = 0; k < 3; k++) P[(int64_t) (k + 1) * En + p] = s[k];
+    }
+}
+
+/* refine flagged leaves one level, projecting the state */
+static int refine_state(charm_forest_t *f, const int8_t *fl, int V, double **u)
+{
+    const int64_t E = f->n;
+    charm_leaf_t *old = (charm_leaf_t *) malloc(sizeof(charm_leaf_t) * (size_t) (E + 1));
+    if (!old) return CHARM_GPU_ENOMEM;
+    memcpy(old, f->leaf, sizeof(charm_leaf_t) * (size_t) E);
+    if (charm_forest_refine(f, fl, -1, NULL, NULL) < 0) { free(old); return CHARM_GPU_ENOMEM; }
+    const int64_t En = f->n;
+    double *w = (double *) malloc(sizeof(double) * (size_t) V * 4 * (size_t) En);
+    if (!w) { free(old); return CHARM_GPU_ENOMEM; }
+    int64_t k = 0;
+    for (int64_t i = 0; i < E; i++) {
+        if (fl[i] && old[i].level < CHARM_FOREST_MAXLEVEL - 1) {
+            for (int c = 0; c < 8; c++) project_down(*u, E, i, w, En, k + c, charm_leaf_child_id(&f->leaf[k + c]), V);
+            k += 8;
+        } else {
+            for (int v = 0; v < V; v++)
+                for (int b = 0; b < 4; b++) w[((int64_t) v * 4 + b) * En + k] = (*u)[((int64_t) v * 4 + b) * E + i];
+            k++;
+        }
+    }
+    free(old);
+    free(*u);
+    *u = w;
+    return CHARM_GPU_OK;
+}
+
+typedef struct {
+    const charm_forest_t *f;
+    const double *grad;        /* per current leaf, NaN for leaves new in this adapt */
+    const double *u;
+    int64_t E;
+    int nc, minlevel;
+    double err2_max;
+} coarsen_state_ctx_t;
+
+/* charm_coarsen_err_estimate (src/charm_amr.c:90-142) */
+static int coarsen_family(void *user, const charm_leaf_t *leaves, const int64_t idx[8])
+{
+    const coarsen_state_ctx_t *c = (const coarsen_state_ctx_t *) user;
+    if (leaves[idx[0]].level <= c->minlevel) return 0;
+    double h[3];
+    leaf_h(c->f, leaves[idx[0]].level, h);
+    const double vol = h[0] * h[1] * h[2];
+    double r[8], parentu = 0.;
+    for (int i = 0; i < 8; i++) {
+        double ri = 0.;   /* prim.r at the centre: sum of the partial-density means, eos flag 4 clamp */
+        for (int s = 0; s < c->nc; s++) ri += c->u[((int64_t) (4 + s) * 4) * c->E + idx[i]];
+        if (ri < 1.e-12) ri = 1.e-12;
+        r[i] = ri;
+        parentu += ri / 8;
+    }
+    double err2 = 0.;
+    for (int i = 0; i < 8; i++) {
+        const double childerr2 = err_sqr(c->grad, c->E, idx[i], vol);
+        if (childerr2 > c->err2_max * vol) return 0;
+        err2 += childerr2;
+        const double diff = (parentu - r[i]) * (parentu - r[i]);
+        err2 += diff * vol;
+    }
+    return err2 < c->err2_max * (vol * 8) ? 1 : 0;
+}
+
+int charm_host_forest_adapt_state(charm_host_forest_t h, const double *grad, double max_err, int minlevel, int maxlevel,
+                                  int n_comp, const double *u_in, int64_t *n_new)
+{
+    if (!h || !grad || !u_in || n_comp < 1 || n_comp > CHARM_GPU_MAX_COMP) return CHARM_GPU_EINVAL;
+    charm_forest_t *f = &h->f;
+    const int V = 4 + n_comp;
+    const int64_t E0 = f->n;
+    const double err2_max = max_err * max_err;
+    int ml = (maxlevel < 0 || maxlevel > CHARM_FOREST_MAXLEVEL - 1) ? CHARM_FOREST_MAXLEVEL - 1 : maxlevel;
+    double *u = (double *) malloc(sizeof(double) * (size_t) V * 4 * (size_t) E0);
+    int8_t *fl = (int8_t *) calloc((size_t) E0 + 1, 1);
+    if (!u || !fl) { free(u); free(fl); return CHARM_GPU_ENOMEM; }
+    memcpy(u, u_in, sizeof(double) * (size_t) V * 4 * (size_t) E0);
+    /* 1. refine (charm_refine_err_estimate, non-recursive, maxlevel) */
+    for (int64_t i = 0; i < E0; i++) {
+        if (f->leaf[i].level >= ml) continue;
+        double hh[3];
+        leaf_h(f, f->leaf[i].level, hh);
+        const double vol = hh[0] * hh[1] * hh[2];
+        fl[i] = err_sqr(grad, E0, i, vol) > err2_max * vol;
+    }
+    /* the gradient of the leaves after refinement: unchanged leaves keep theirs,
+     * new children get NaN, so their family is never coarsened in this adapt */
+    int64_t E1 = E0;
+    for (int64_t i = 0; i < E0; i++) E1 += fl[i] ? 7 : 0;
+    double *g1 = (double *) malloc(sizeof(double) * 3 * (size_t) E1);
+    if (!g1) { free(u); free(fl); return CHARM_GPU_ENOMEM; }
+    {
+        int64_t k = 0;
+        for (int64_t i = 0; i < E0; i++) {
+            int n = fl[i] ? 8 : 1;
+            for (int c = 0; c < n; c++)
+                for (int d = 0; d < 3; d++) g1[(int64_t) d * E1 + k + c] = fl[i] ? NAN : grad[(int64_t) d * E0 + i];
+            k += n;
+        }
+    }
+    int rc = refine_state(f, fl, V, &u);
+    free(fl);
+    if (rc) { free(u); free(g1); return rc; }
+    /* 2. coarsen complete families (charm_coarsen_err_estimate, non-recursive) */
+    {
+        const int64_t E = f->n;
+        charm_leaf_t *old = (charm_leaf_t *) malloc(sizeof(charm_leaf_t) * (size_t) (E + 1));
+        if (!old) { free(u); free(g1); return CHARM_GPU_ENOMEM; }
+        memcpy(old, f->leaf, sizeof(charm_leaf_t) * (size_t) E);
+        coarsen_state_ctx_t cc = {f, g1, u, E, n_comp, minlevel, err2_max};
+        int64_t nm = charm_forest_coarsen(f, minlevel, coarsen_family, NULL, &cc);
+        if (nm < 0) { free(old); free(u); free(g1); return CHARM_GPU_ENOMEM; }
+        if (nm > 0) {
+            const int64_t En = f->n;
+            double *w = (double *) malloc(sizeof(double) * (size_t) V * 4 * (size_t) En);
+            if (!w) { free(old); free(u); free(g1); return CHARM_GPU_ENOMEM; }
+            int64_t i = 0;
+            for (int64_t k = 0; k < En; k++) {
+                const charm_leaf_t *nl = &f->leaf[k], *ol = &old[i];
+                if (ol->level == nl->level && ol->x == nl->x && ol->y == nl->y && ol->z == nl->z && ol->tree == nl->tree) {
+                    for (int v = 0; v < V; v++)
+                        for (int b = 0; b < 4; b++) w[((int64_t) v * 4 + b) * En + k] = u[((int64_t) v * 4 + b) * E + i];
+                    i++;
+                } else {
+                    int64_t ch[8];
+                    int cid[8];
+                    for (int c = 0; c < 8; c++) { ch[c] = i + c; cid[c] = charm_leaf_child_id(&old[i + c]); }
+                    project_up(u, E, ch, cid, w, En, k, V);
+                    i += 8;
+                }
+            }
+            free(u);
+            u = w;
+        }
+        free(old);
+    }
+    free(g1);
+    /* 3. 2:1 face balance, one level per pass (p4est_balance_ext with charm_replace_quads) */
+    for (;;) {
+        int8_t *bf = (int8_t *) calloc((size_t) f->n + 1, 1);
+        if (!bf) { free(u); return CHARM_GPU_ENOMEM; }
+        int64_t marks = charm_forest_balance_marks(f, bf);
+        if (marks) rc = refine_state(f, bf, V, &u);
+        free(bf);
+        if (rc) { free(u); return rc; }
+        if (!marks) break;
+    }
+    free(h->state);
+    h->state = u;
+    free_flat(h);
+    if (n_new) *n_new = f->n;
+    return CHARM_GPU_OK;
+}
+
+int charm_host_forest_state(charm_host_forest_t h, const double **u_out)
+{
+    if (!h || !u_out) return CHARM_GPU_EINVAL;
+    if (!h->state) return CHARM_GPU_ESTATE;
+    *u_out = h->state;
     return CHARM_GPU_OK;
 }

@@ -93,6 +93,18 @@ class Forest:
                   "charm_host_forest_adapt")
         return n.value
 
+    def adapt_state(self, grad: np.ndarray, max_err: float, minlevel: int, maxlevel: int, n_comp: int,
+                    u: np.ndarray) -> np.ndarray:
+        """One adapt (refine / coarsen / balance) carrying the state along; returns the new state."""
+        g = np.ascontiguousarray(grad, dtype=np.float64)
+        uu = np.ascontiguousarray(u, dtype=np.float64)
+        n = C.c_int64()
+        abi.check(self.lib.charm_host_forest_adapt_state(self.h, g.ctypes.data, max_err, minlevel, maxlevel, n_comp,
+                                                         uu.ctypes.data, C.byref(n)), "charm_host_forest_adapt_state")
+        p = C.POINTER(C.c_double)()
+        abi.check(self.lib.charm_host_forest_state(self.h, C.byref(p)), "charm_host_forest_state")
+        return np.ctypeslib.as_array(p, (4 + n_comp, 4, n.value)).copy()
+
     def leaves(self) -> tuple[np.ndarray, np.ndarray]:
         n = len(self)
         q = np.empty((n, 4), np.int32)
@@ -175,6 +187,14 @@ class Solver:
 
     def limit(self) -> None:
         abi.check(self.lib.charm_gpu_limit(self.h), "charm_gpu_limit")
+
+    def refine_flags(self, max_err: float) -> tuple[np.ndarray, np.ndarray]:
+        """Reference refine criterion per leaf and the density-gradient estimate [3][E]."""
+        flags = np.empty(self.n_elem, np.int8)
+        grad = np.empty((3, self.n_elem))
+        abi.check(self.lib.charm_gpu_refine_flags(self.h, max_err, flags.ctypes.data, grad.ctypes.data),
+                  "charm_gpu_refine_flags")
+        return flags, grad
 
     def sync(self, timeout_s: float = 600.0) -> None:
         abi.check(self.lib.charm_gpu_sync(self.h, timeout_s), "charm_gpu_sync")

@@ -249,6 +249,20 @@ int charm_host_forest_set_bnd(charm_host_forest_t f, const int8_t bnd_of_side[6]
 int charm_host_forest_adapt(charm_host_forest_t f, const int8_t *flags, int minlevel, int maxlevel,
                             int64_t *n_new);
 
+/* One adapt of charm_adapt (reference src/charm_amr.c:575-610) with the
+ * state carried along: refine (level < maxlevel) where
+ * |grad rho|^2/12 * vol^(5/3) > max_err^2 * vol, coarsen complete families by
+ * the reference's family criterion (children's estimates plus the spread of
+ * their centre densities; level > minlevel; families refined in this same
+ * adapt are not coarsened), then 2:1 face balance.  The state is projected
+ * parent <-> children as charm_replace_quads does (:206-307; exact for p1
+ * on boxes).  grad: [3][E] from charm_gpu_refine_flags; u_in: [V][B][E]
+ * of the leaves before the adapt.  The new state ([V][B][n_new]) is returned
+ * by charm_host_forest_state and stays valid until the next adapt or free. */
+int charm_host_forest_adapt_state(charm_host_forest_t f, const double *grad, double max_err, int minlevel, int maxlevel,
+                                  int n_comp, const double *u_in, int64_t *n_new);
+int charm_host_forest_state(charm_host_forest_t f, const double **u_out);
+
 /* Flatten into a mesh view whose arrays live inside the forest object and
  * stay valid until the next adapt/flatten/free. */
 int charm_host_forest_flatten(charm_host_forest_t f, charm_gpu_mesh_t *mesh);

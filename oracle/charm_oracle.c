@@ -921,6 +921,60 @@ int oracle_run(oracle_t *o, int nsteps, double dt)
     return 0;
 }
 
+/* Density-gradient estimate of charm_adapt (src/charm_amr.c:350-573):
+ * grad[3][E] = (1/vol) * sum over faces of 0.5*(r_L + r_R) * n * gw * gj,
+ * n pointing out of side 0, side 0 adding and side 1 subtracting; on
+ * boundary faces the right state is the boundary condition's ghost. */
+int oracle_amr_grad(oracle_t *o, double *grad)
+{
+    const int64_t E = o->E;
+    memset(grad, 0, sizeof(double) * 3 * (size_t) E);
+    for (int64_t j = 0; j < o->Fb; j++) {   /* _charm_amr_par_calc_face_iter_bnd (:362-423) */
+        const int32_t e = o->bface_elem[j];
+        const int f = o->bface_face[j];
+        const elem_geom_t *g = &o->g[e];
+        double gp[NFQ][3], gwj[NFQ], n[3];
+        face_points(g, f, gp, gwj);
+        outward_normal(f, n);
+        for (int q = 0; q < NFQ; q++) {
+            double U[MAXV];
+            prim_t pr[2];
+            get_fields(o, o->u, e, g->c, g->dh, gp[q], U);
+            cons_to_prim(o, U, &pr[0]);
+            bnd_cond(o, o->bface_bnd[j], &pr[0], &pr[1], n);
+            double qr = 0.5 * (pr[0].r + pr[1].r);
+            for (int k = 0; k < 3; k++) grad[k * E + e] += qr * gwj[q] * n[k];
+        }
+    }
+    for (int64_t f = 0; f < o->F; f++) {    /* _charm_amr_par_calc_face_iter_inner (:426-549) */
+        const int32_t e[2] = {o->face_elem[f], o->face_elem[o->F + f]};
+        const int d = o->face_info[f] & 3, kind = (o->face_info[f] >> 2) & 3;
+        double c1[3];
+        side1_center(o, f, c1);
+        const double *cs[2] = {o->g[e[0]].c, c1};
+        const int hs = (kind == 2) ? 1 : 0;
+        elem_geom_t pg = o->g[e[hs]];
+        memcpy(pg.c, cs[hs], sizeof(double) * 3);
+        double gp[NFQ][3], gwj[NFQ], n[3];
+        face_points(&pg, hs ? 2 * d : 2 * d + 1, gp, gwj);
+        outward_normal(2 * d + 1, n);
+        for (int q = 0; q < NFQ; q++) {
+            prim_t pr[2];
+            for (int s = 0; s < 2; s++) {
+                double U[MAXV];
+                get_fields(o, o->u, e[s], cs[s], o->g[e[s]].dh, gp[q], U);
+                cons_to_prim(o, U, &pr[s]);
+            }
+            double qr = 0.5 * (pr[0].r + pr[1].r);
+            for (int k = 0; k < 3; k++)
+                for (int s = 0; s < 2; s++) grad[k * E + e[s]] += (s ? -1. : 1.) * gwj[q] * qr * n[k];
+        }
+    }
+    for (int64_t e = 0; e < E; e++)          /* _charm_amr_par_calc_quad_iter_fn (:564-573) */
+        for (int k = 0; k < 3; k++) grad[k * E + e] /= o->g[e].vol;
+    return 0;
+}
+
 /* Point flux on two primitive states (r u v w p each), for unit tests. */
 int oracle_point_flux(oracle_t *o, const double *prim2, const double n[3], double *q)
 {

@@ -23,6 +23,7 @@ def load() -> C.CDLL:
         lib.oracle_step.argtypes = [C.c_void_p, C.c_double]
         lib.oracle_run.argtypes = [C.c_void_p, C.c_int, C.c_double]
         lib.oracle_point_flux.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.oracle_amr_grad.argtypes = [C.c_void_p, C.c_void_p]
         _lib = lib
     return _lib
 
@@ -74,6 +75,11 @@ class Port:
 
     def run(self, nsteps: int, dt: float) -> None:
         self.lib.oracle_run(self.h, nsteps, dt)
+
+    def amr_grad(self) -> np.ndarray:
+        g = np.empty((3, self.mesh.n_elem))
+        self.lib.oracle_amr_grad(self.h, g.ctypes.data)
+        return g
 
     def point_flux(self, prim2, n) -> np.ndarray:
         p = np.ascontiguousarray(prim2, dtype=np.float64)

@@ -62,3 +62,32 @@ def hanging_forest(case: Case, frac: float = 0.2, seed: int = 3) -> tuple[Forest
     flags = (rng.uniform(size=len(f)) < frac).astype(np.int8)
     f.adapt(flags, case.level, case.level + 1)
     return f, flags
+
+
+def amr_case(kind: str = "sod", level: int = 2, max_level: int = 4, max_err: float = 0.05, flux: str = "HLLC",
+             limiter: str = "BJ") -> Case:
+    """A small AMR case: refine / coarsen by the reference's criterion every `refine_period` steps."""
+    c = small_case(kind, flux, limiter, level=level)
+    c.max_err, c.min_level, c.max_level, c.refine_period = max_err, level, max_level, 2
+    c.tau = 0.1 * (1.0 / 2 ** max_level) / 1.5
+    return c
+
+
+def amr_run_oracle(case: Case, steps: int):
+    """The AMR time loop of charm_model_ns_timestep_single (src/models/ns/charm_model.c:197-214)
+    on the oracle: adapt every refine_period steps (not at step 0), then the step."""
+    from oracle.port import Port
+    forest = Forest(case)
+    mesh = forest.flatten()
+    u = case.initial_state(mesh.center)
+    for step in range(steps):
+        if case.refine_period and step and step % case.refine_period == 0:
+            port = Port(case.config(), mesh)
+            port.set_state(u)
+            u = forest.adapt_state(port.amr_grad(), case.max_err, case.min_level, case.max_level, case.n_comp, u)
+            mesh = forest.flatten()
+        port = Port(case.config(), mesh)
+        port.set_state(u)
+        port.step(case.tau)
+        u = port.get_state()
+    return forest, mesh, u
