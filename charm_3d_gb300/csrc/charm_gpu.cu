@@ -19,6 +19,7 @@
 #include <string>
 #include <thread>
 #include <utility>
+#include <algorithm>
 #include <vector>
 
 #include "charm_gpu.h"
@@ -74,6 +75,10 @@ struct charm_gpu_handle_s {
     void *d_slots = nullptr;           // double or float [V*B][S]
     // mixed form: FP32 hi/lo planes of u, ua, ub ([V][B][E] each)
     float *d_fh[3] = {nullptr, nullptr, nullptr}, *d_fl[3] = {nullptr, nullptr, nullptr};
+    // mixed form, block-local stage: per-tile face lists and element-face slots
+    int32_t *d_tile_fptr = nullptr, *d_tile_faces = nullptr, *d_tile_slot = nullptr;
+    int64_t n_tiles = 0;
+    size_t tile_smem = 0;      // dynamic shared memory of tile_stage_kernel (0: use ff_stage_kernel)
     double *d_dt = nullptr;            // CFL step (bits as unsigned long long)
     unsigned *d_err = nullptr;
     bool mesh_ready = false;
@@ -103,6 +108,12 @@ void free_mesh(charm_gpu_handle_s *h)
         if (h->d_fl[k]) cudaFree(h->d_fl[k]);
         h->d_fh[k] = h->d_fl[k] = nullptr;
     }
+    if (h->d_tile_fptr) cudaFree(h->d_tile_fptr);
+    if (h->d_tile_faces) cudaFree(h->d_tile_faces);
+    if (h->d_tile_slot) cudaFree(h->d_tile_slot);
+    h->d_tile_fptr = h->d_tile_faces = h->d_tile_slot = nullptr;
+    h->n_tiles = 0;
+    h->tile_smem = 0;
     h->d_center = nullptr; h->d_level = nullptr; h->d_face_elem = nullptr; h->d_face_info = nullptr;
     h->d_bface_elem = nullptr; h->d_bface_face = nullptr; h->d_bface_bnd = nullptr;
     h->d_gather_ptr = nullptr; h->d_gather_slot = nullptr; h->d_lim_idx = nullptr; h->d_lim_kind = nullptr;
@@ -396,10 +407,48 @@ FFCoef ff_split(double x)
     return {hi, (float) (x - (double) hi)};
 }
 
+template <int NC, int FLUX>
+int launch_tile_stage(charm_gpu_handle_s *h, int in, int u0, int out, FFCoef dt, const double *dt_dev, FFCoef a,
+                      FFCoef b, bool comb)
+{
+    MeshDev m = mesh_view(h);
+    TileDev tl;
+    tl.fptr = h->d_tile_fptr;
+    tl.faces = h->d_tile_faces;
+    tl.slot = h->d_tile_slot;
+    // the dynamic shared memory limit is a per-device attribute of the kernel
+    static int attr_smem[64] = {0};
+    const int dev = h->device & 63;
+    if ((size_t) attr_smem[dev] < h->tile_smem) {
+        int max_optin = 0;
+        CUDA_TRY(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
+        CUDA_TRY(cudaFuncSetAttribute(tile_stage_kernel<NC, FLUX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      max_optin));
+        attr_smem[dev] = max_optin;
+    }
+    const float *u0h = (u0 >= 0) ? h->d_fh[u0] : nullptr, *u0l = (u0 >= 0) ? h->d_fl[u0] : nullptr;
+    TimedLaunch t;
+    begin_launch(h, 1, &t);
+    tile_stage_kernel<NC, FLUX><<<(unsigned) h->n_tiles, kTile, h->tile_smem, h->stream>>>(
+        m, tl, h->d_fh[in], h->d_fl[in], u0h, u0l, h->d_fh[out], h->d_fl[out], dt.h, dt.l, dt_dev, a.h, a.l, b.h, b.l,
+        comb ? 1 : 0, h->d_err);
+    end_launch(h, &t);
+    CUDA_TRY(cudaGetLastError());
+    return CHARM_GPU_OK;
+}
+
 template <int NC>
 int launch_ff_stage(charm_gpu_handle_s *h, int in, int u0, int out, FFCoef dt, const double *dt_dev, FFCoef a, FFCoef b,
                     bool comb)
 {
+    if (h->tile_smem) {
+        switch (h->cfg.flux) {
+        case CHARM_GPU_FLUX_LF: return launch_tile_stage<NC, CHARM_GPU_FLUX_LF>(h, in, u0, out, dt, dt_dev, a, b, comb);
+        case CHARM_GPU_FLUX_HLLC: return launch_tile_stage<NC, CHARM_GPU_FLUX_HLLC>(h, in, u0, out, dt, dt_dev, a, b, comb);
+        case CHARM_GPU_FLUX_CD: return launch_tile_stage<NC, CHARM_GPU_FLUX_CD>(h, in, u0, out, dt, dt_dev, a, b, comb);
+        default: return launch_tile_stage<NC, CHARM_GPU_FLUX_GODUNOV>(h, in, u0, out, dt, dt_dev, a, b, comb);
+        }
+    }
     MeshDev m = mesh_view(h);
     const int bs = 128;
     const unsigned nb = (unsigned) ((h->E + bs - 1) / bs);
@@ -679,6 +728,65 @@ int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh)
             CUDA_TRY(cudaMalloc(&h->d_fl[k], st / 2));
             CUDA_TRY(cudaMemset(h->d_fh[k], 0, st / 2));
             CUDA_TRY(cudaMemset(h->d_fl[k], 0, st / 2));
+        }
+        // tiles of kTile consecutive elements: every face touching a tile, in
+        // global face order (keeps the 4 records of a mortar consecutive),
+        // and for every element face its position in the tile's list
+        const int64_t nt = (E + kTile - 1) / kTile;
+        std::vector<int32_t> tcnt(nt + 1, 0);
+        for (int64_t i = 0; i < F; i++) {
+            const int64_t t0 = mesh->face_elem[i] / kTile, t1 = mesh->face_elem[F + i] / kTile;
+            tcnt[t0]++;
+            if (t1 != t0) tcnt[t1]++;
+        }
+        for (int64_t j = 0; j < Fb; j++) tcnt[mesh->bface_elem[j] / kTile]++;
+        std::vector<int32_t> tptr(nt + 1, 0);
+        for (int64_t t = 0; t < nt; t++) tptr[t + 1] = tptr[t] + tcnt[t];
+        std::vector<int32_t> tfaces(tptr[nt] > 0 ? tptr[nt] : 1), tslot(6 * E, -1), tfill(tptr.begin(), tptr.end() - 1);
+        int64_t max_list = 0;
+        for (int64_t t = 0; t < nt; t++) max_list = std::max<int64_t>(max_list, tcnt[t]);
+        for (int64_t i = 0; i < F; i++) {
+            const int32_t a = mesh->face_elem[i], b = mesh->face_elem[F + i];
+            const unsigned info = mesh->face_info[i];
+            const int d = info & 3, kind = (info >> 2) & 3, sub = (info >> 4) & 3;
+            const int64_t ta = a / kTile, tb = b / kTile;
+            for (int pass = 0; pass < 2; pass++) {
+                const int64_t t = pass ? tb : ta;
+                if (pass && tb == ta) break;
+                const int32_t p = tfill[t]++;
+                tfaces[p] = (int32_t) (i << 1);
+                const int32_t loc = p - tptr[t];
+                for (int side = 0; side < 2; side++) {
+                    const int32_t e = side ? b : a;
+                    if (e / kTile != t) continue;
+                    const int f = side ? 2 * d : 2 * d + 1;
+                    const bool big = (kind == 1 && side == 1) || (kind == 2 && side == 0);
+                    if (!big) tslot[(int64_t) f * E + e] = loc;
+                    else if (sub == 0) tslot[(int64_t) f * E + e] = loc;
+                }
+            }
+        }
+        for (int64_t j = 0; j < Fb; j++) {
+            const int32_t e = mesh->bface_elem[j];
+            const int64_t t = e / kTile;
+            const int32_t p = tfill[t]++;
+            tfaces[p] = (int32_t) ((j << 1) | 1);
+            tslot[(int64_t) mesh->bface_face[j] * E + e] = p - tptr[t];
+        }
+        for (int64_t k = 0; k < 6 * E; k++)
+            if (tslot[k] < 0) return fail(CHARM_GPU_EINVAL, "element face without a tile face slot");
+        const size_t smem = sizeof(float) * ((size_t) V * CHARM_GPU_BASIS * kTile + (size_t) max_list * 3 * V);
+        int max_optin = 0;
+        CUDA_TRY(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
+        if (smem <= (size_t) max_optin) {
+            CUDA_TRY(cudaMalloc(&h->d_tile_fptr, (nt + 1) * sizeof(int32_t)));
+            CUDA_TRY(cudaMalloc(&h->d_tile_faces, tfaces.size() * sizeof(int32_t)));
+            CUDA_TRY(cudaMalloc(&h->d_tile_slot, (size_t) 6 * E * sizeof(int32_t)));
+            CUDA_TRY(cudaMemcpy(h->d_tile_fptr, tptr.data(), (nt + 1) * sizeof(int32_t), cudaMemcpyHostToDevice));
+            CUDA_TRY(cudaMemcpy(h->d_tile_faces, tfaces.data(), tfaces.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+            CUDA_TRY(cudaMemcpy(h->d_tile_slot, tslot.data(), (size_t) 6 * E * sizeof(int32_t), cudaMemcpyHostToDevice));
+            h->n_tiles = nt;
+            h->tile_smem = smem;
         }
     }
     CUDA_TRY(cudaMemcpy(h->d_center, mesh->center, 3 * E * sizeof(double), cudaMemcpyHostToDevice));

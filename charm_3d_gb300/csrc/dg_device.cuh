@@ -67,6 +67,25 @@ __device__ __forceinline__ T cfgv(const double &d, const float &f)
     else return d;
 }
 
+// Quotient on the hot flux path: IEEE a/b in FP64; in the FP32 residual of
+// the mixed form the hardware reciprocal (__fdividef, within 2 ulp), whose
+// error stays far below the FP32 rounding of the residual itself.
+template <typename T>
+__device__ __forceinline__ T qdiv(T a, T b)
+{
+    if constexpr (sizeof(T) == sizeof(float)) return __fdividef(a, b);
+    else return a / b;
+}
+
+// Square root on the hot flux path: IEEE sqrt in FP64; x * rsqrt(x) from the
+// hardware reciprocal square root in FP32 (0 stays 0, negative gives NaN).
+template <typename T>
+__device__ __forceinline__ T qsqrt(T x)
+{
+    if constexpr (sizeof(T) == sizeof(float)) return (x == 0.f) ? 0.f : x * rsqrtf(x);
+    else return sqrt(x);
+}
+
 __device__ __forceinline__ void set_error(unsigned *err, unsigned bit)
 {
     if (err) atomicOr(err, bit);
@@ -194,7 +213,7 @@ __device__ __forceinline__ void cons_to_prim(const T *U, Prim<T, NC> &p)
     T r = T(0);
     for (int i = 0; i < NC; i++) r += U[4 + i];
     p.r = r;
-    T ir = T(1) / r;
+    T ir = qdiv<T>(T(1), r);
     p.u = U[0] * ir;
     p.v = U[1] * ir;
     p.w = U[2] * ir;
@@ -213,7 +232,7 @@ __device__ __forceinline__ void cons_to_prim(const T *U, Prim<T, NC> &p)
         p.cp = cfgv<T>(c_cfg.ideal_cp, c_cfg.ideal_cp_f); p.m = cfgv<T>(c_cfg.ideal_m, c_cfg.ideal_m_f);
         p.cv = cfgv<T>(c_cfg.ideal_cv, c_cfg.ideal_cv_f); p.gam = cfgv<T>(c_cfg.ideal_gam, c_cfg.ideal_gam_f);
         p.p = r * p.e * (p.gam - T(1));
-        p.cz = sqrt(p.gam * p.p * ir);
+        p.cz = qsqrt<T>(p.gam * p.p * ir);
         p.t = p.e * cfgv<T>(c_cfg.ideal_inv_cv, c_cfg.ideal_inv_cv_f);
         return;
     }
@@ -378,21 +397,43 @@ __device__ void flux_hllc(const Prim<T, NC> &pa, const Prim<T, NC> &pb, const T 
 
     T p_pvrs = T(0.5) * (pa.p + pb.p) - T(0.5) * (ub - ua) * T(0.25) * (pa.r + pb.r) * (pa.cz + pb.cz);
     T p_star = (p_pvrs > T(0)) ? p_pvrs : T(0);
-    T ql = (p_star <= pa.p) ? T(1) : sqrt(T(1) + (pa.gam + T(1)) * (p_star / pa.p - T(1)) / (T(2) * pa.gam));
-    T qr = (p_star <= pb.p) ? T(1) : sqrt(T(1) + (pb.gam + T(1)) * (p_star / pb.p - T(1)) / (T(2) * pb.gam));
+    T ql = (p_star <= pa.p) ? T(1) : qsqrt<T>(T(1) + qdiv<T>((pa.gam + T(1)) * (qdiv<T>(p_star, pa.p) - T(1)), T(2) * pa.gam));
+    T qr = (p_star <= pb.p) ? T(1) : qsqrt<T>(T(1) + qdiv<T>((pb.gam + T(1)) * (qdiv<T>(p_star, pb.p) - T(1)), T(2) * pb.gam));
     T sl = ua - pa.cz * ql;
     T sr = ub + pb.cz * qr;
     if (sl > sr) { T tmp = sl; sl = sr; sr = tmp; }
     T s_star = pb.p - pa.p;
     s_star += pa.r * ua * (sl - ua);
     s_star -= pb.r * ub * (sr - ub);
-    s_star /= (pa.r * (sl - ua) - pb.r * (sr - ub));
+    s_star = qdiv<T>(s_star, pa.r * (sl - ua) - pb.r * (sr - ub));
     if (s_star < sl) s_star = sl;
     if (s_star > sr) s_star = sr;
     if (!((sl <= s_star) && (s_star <= sr))) set_error(err, kErrHllc);
 
     T fu, fv, fw;
-    if (sl >= T(0)) {
+    if constexpr (sizeof(T) == sizeof(float)) {
+        // the same four cases as below, with the side chosen by selects: the
+        // state k and its wave speed, then the star flux or the side's flux
+        const bool ka = (sl >= T(0)) || (!(sr <= T(0)) && (s_star >= T(0)));
+        const bool star = !(sl >= T(0)) && !(sr <= T(0));
+        const T rk = ka ? pa.r : pb.r, uk = ka ? ua : ub, vk = ka ? va : vb, wk = ka ? wa : wb;
+        const T pk = ka ? pa.p : pb.p, ek = ka ? pa.e_tot : pb.e_tot, sk = ka ? sl : sr;
+        const T fu_k = rk * uk * uk + pk, fv_k = rk * vk * uk, fw_k = rk * wk * uk, fe_k = (rk * ek + pk) * uk;
+        if (star) {
+            const T inv = qdiv<T>(T(1), sk - s_star);
+            fu = f_hllc_u<T>(rk * uk, fu_k, sk, s_star, pk, rk, uk, inv);
+            fv = f_hllc_v<T>(rk * vk, rk * uk * vk, sk, s_star, inv);
+            fw = f_hllc_v<T>(rk * wk, rk * uk * wk, sk, s_star, inv);
+            q[3] = f_hllc_e<T>(rk * ek, fe_k, sk, s_star, pk, rk, uk, inv);
+            for (int i = 0; i < NC; i++) {
+                const T ck = ka ? pa.c[i] : pb.c[i];
+                q[4 + i] = f_hllc_v<T>(rk * ck, rk * ck * uk, sk, s_star, inv);
+            }
+        } else {
+            fu = fu_k; fv = fv_k; fw = fw_k; q[3] = fe_k;
+            for (int i = 0; i < NC; i++) q[4 + i] = rk * uk * (ka ? pa.c[i] : pb.c[i]);
+        }
+    } else if (sl >= T(0)) {
         fu = pa.r * ua * ua + pa.p;
         fv = pa.r * va * ua;
         fw = pa.r * wa * ua;
@@ -405,14 +446,14 @@ __device__ void flux_hllc(const Prim<T, NC> &pa, const Prim<T, NC> &pb, const T 
         q[3] = (pb.r * pb.e_tot + pb.p) * ub;
         for (int i = 0; i < NC; i++) q[4 + i] = pb.r * ub * pb.c[i];
     } else if (s_star >= T(0)) {
-        const T inv = T(1) / (sl - s_star);
+        const T inv = qdiv<T>(T(1), sl - s_star);
         fu = f_hllc_u<T>(pa.r * ua, pa.r * ua * ua + pa.p, sl, s_star, pa.p, pa.r, ua, inv);
         fv = f_hllc_v<T>(pa.r * va, pa.r * ua * va, sl, s_star, inv);
         fw = f_hllc_v<T>(pa.r * wa, pa.r * ua * wa, sl, s_star, inv);
         q[3] = f_hllc_e<T>(pa.r * pa.e_tot, (pa.r * pa.e_tot + pa.p) * ua, sl, s_star, pa.p, pa.r, ua, inv);
         for (int i = 0; i < NC; i++) q[4 + i] = f_hllc_v<T>(pa.r * pa.c[i], pa.r * pa.c[i] * ua, sl, s_star, inv);
     } else {
-        const T inv = T(1) / (sr - s_star);
+        const T inv = qdiv<T>(T(1), sr - s_star);
         fu = f_hllc_u<T>(pb.r * ub, pb.r * ub * ub + pb.p, sr, s_star, pb.p, pb.r, ub, inv);
         fv = f_hllc_v<T>(pb.r * vb, pb.r * ub * vb, sr, s_star, inv);
         fw = f_hllc_v<T>(pb.r * wb, pb.r * ub * wb, sr, s_star, inv);

@@ -1131,4 +1131,337 @@ __global__ void __launch_bounds__(128) amr_grad_kernel(MeshDev m, const double *
     for (int k = 0; k < 3; k++) grad[(int64_t) k * E + e] = g[k] / vol;
 }
 
+
+// ===========================================================================
+// Mixed form, block-local: one CTA per tile of kTile Morton-consecutive
+// elements.  The tile's states are staged in shared memory; every face that
+// touches the tile is evaluated once by the CTA (faces inside the tile once
+// in total, faces on the tile boundary once by each of the two tiles, from
+// identical operands at one code location), its projections (a0, as, at per
+// variable) kept in shared memory; then each thread gathers its element's
+// faces, adds the volume integral and updates u in float-float.
+// ===========================================================================
+constexpr int kTile = 128;
+
+struct TileDev {
+    const int32_t *fptr;    // [n_tiles + 1] into faces
+    const int32_t *faces;   // (interior face << 1) | 0, or (boundary face << 1) | 1
+    const int32_t *slot;    // [6][E]: position of the element face in its tile's face list
+};
+
+// Coefficients of element e for the tile starting at e_begin: from shared
+// memory when e is in the tile, else from the global hi plane.
+template <int V>
+__device__ __forceinline__ void tile_coef(const float *s_u, const float *__restrict__ uh, int64_t E, int64_t e_begin,
+                                          int64_t e, float c[V][kNB])
+{
+    const int64_t l = e - e_begin;
+    if (l >= 0 && l < kTile) {
+#pragma unroll
+        for (int v = 0; v < V; v++)
+#pragma unroll
+            for (int k = 0; k < kNB; k++) c[v][k] = s_u[(v * kNB + k) * kTile + l];
+    } else {
+        load_coef_f<V>(uh, E, e, c);
+    }
+}
+
+// 6-point sums of one interior (sub-)face along D: S0 = sum q, Ss = sum q*ps,
+// St = sum q*pt with the lower/upper leaves' coefficients.
+template <int NC, int FLUX, int D>
+__device__ __forceinline__ void face_sums(const float cl[4 + NC][kNB], const float cu[4 + NC][kNB], int kind, int sub,
+                                          float S0[4 + NC], float Ss[4 + NC], float St[4 + NC], unsigned *err)
+{
+    constexpr int V = 4 + NC;
+    constexpr int s = (D == 0) ? 1 : 0, t = (D == 2) ? 1 : 2;
+    const float os = (sub & 1) ? 0.25f : -0.25f, ot = (sub & 2) ? 0.25f : -0.25f;
+    float n[3] = {0.f, 0.f, 0.f};
+    n[D] = 1.f;
+#pragma unroll
+    for (int v = 0; v < V; v++) S0[v] = Ss[v] = St[v] = 0.f;
+#pragma unroll 1
+    for (int g = 0; g < 6; g++) {
+        const float ps = c_face_psf[g], pt = c_face_ptf[g];
+        float psl = ps, ptl = pt, psu = ps, ptu = pt;
+        if (kind == 2) { psl = 0.5f * ps + os; ptl = 0.5f * pt + ot; }
+        if (kind == 1) { psu = 0.5f * ps + os; ptu = 0.5f * pt + ot; }
+        float Ul[V], Uu[V];
+#pragma unroll
+        for (int v = 0; v < V; v++) {
+            Ul[v] = cl[v][0] + 0.5f * cl[v][1 + D] + psl * cl[v][1 + s] + ptl * cl[v][1 + t];
+            Uu[v] = cu[v][0] - 0.5f * cu[v][1 + D] + psu * cu[v][1 + s] + ptu * cu[v][1 + t];
+        }
+        Prim<float, NC> pl, pu;
+        cons_to_prim<float, NC>(Ul, pl);
+        cons_to_prim<float, NC>(Uu, pu);
+        float q[V];
+        num_flux<FLUX, float, NC>(pl, pu, n, q, err);
+#pragma unroll
+        for (int v = 0; v < V; v++) {
+            S0[v] += q[v];
+            Ss[v] += q[v] * ps;
+            St[v] += q[v] * pt;
+        }
+    }
+}
+
+template <int NC, int FLUX, int D>
+__device__ __forceinline__ void tile_interior(const MeshDev &m, const float *s_u, const float *__restrict__ uh,
+                                              int64_t e_begin, int64_t i, float *out, unsigned *err)
+{
+    constexpr int V = 4 + NC;
+    constexpr int s = (D == 0) ? 1 : 0, t = (D == 2) ? 1 : 2;
+    const int e0 = m.face_elem[i], e1 = m.face_elem[m.n_face + i];
+    const unsigned info = m.face_info[i];
+    const int kind = (info >> 2) & 3, sub = (info >> 4) & 3;
+    float cl[V][kNB], cu[V][kNB];
+    tile_coef<V>(s_u, uh, m.n_elem, e_begin, e0, cl);
+    tile_coef<V>(s_u, uh, m.n_elem, e_begin, e1, cu);
+    float S0[V], Ss[V], St[V];
+    face_sums<NC, FLUX, D>(cl, cu, kind, sub, S0, Ss, St, err);
+    const int lev = m.level[(kind == 2) ? e1 : e0];
+    const float w = level_ht<float>(m, lev, s) * level_ht<float>(m, lev, t) * (1.f / 6.f);
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+        out[v] = w * S0[v];
+        out[V + v] = w * Ss[v];
+        out[2 * V + v] = w * St[v];
+    }
+}
+
+template <int NC, int FLUX, int D>
+__device__ __forceinline__ void tile_boundary(const MeshDev &m, const float *s_u, const float *__restrict__ uh,
+                                              int64_t e_begin, int j, float *out, unsigned *err)
+{
+    constexpr int V = 4 + NC;
+    constexpr int s = (D == 0) ? 1 : 0, t = (D == 2) ? 1 : 2;
+    const int e = m.bface_elem[j], f = m.bface_face[j], bid = m.bface_bnd[j];
+    const float sg = (f & 1) ? 1.f : -1.f;
+    float c[V][kNB];
+    tile_coef<V>(s_u, uh, m.n_elem, e_begin, e, c);
+    float n[3] = {0.f, 0.f, 0.f};
+    n[D] = sg;
+    float S0[V], Ss[V], St[V];
+#pragma unroll
+    for (int v = 0; v < V; v++) S0[v] = Ss[v] = St[v] = 0.f;
+#pragma unroll 1
+    for (int g = 0; g < 6; g++) {
+        const float ps = c_face_psf[g], pt = c_face_ptf[g];
+        float U[V];
+#pragma unroll
+        for (int v = 0; v < V; v++) U[v] = c[v][0] + 0.5f * sg * c[v][1 + D] + ps * c[v][1 + s] + pt * c[v][1 + t];
+        Prim<float, NC> pin, pout;
+        cons_to_prim<float, NC>(U, pin);
+        bnd_cond<float, NC>(bid, pin, pout, n);
+        float q[V];
+        num_flux<FLUX, float, NC>(pin, pout, n, q, err);
+#pragma unroll
+        for (int v = 0; v < V; v++) {
+            S0[v] += q[v];
+            Ss[v] += q[v] * ps;
+            St[v] += q[v] * pt;
+        }
+    }
+    const int lev = m.level[e];
+    const float w = level_ht<float>(m, lev, s) * level_ht<float>(m, lev, t) * (1.f / 6.f);
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+        out[v] = w * S0[v];
+        out[V + v] = w * Ss[v];
+        out[2 * V + v] = w * St[v];
+    }
+}
+
+// Add the projections of element e's two faces along D to R.
+template <int NC, int D>
+__device__ __forceinline__ void tile_gather_axis(const MeshDev &m, const TileDev &tl, const float *s_f, int64_t e,
+                                                 float R[4 + NC][kNB], float R0l[4 + NC])
+{
+    constexpr int V = 4 + NC;
+    constexpr int s = (D == 0) ? 1 : 0, t = (D == 2) ? 1 : 2;
+    const int64_t E = m.n_elem;
+#pragma unroll
+    for (int side = 0; side < 2; side++) {
+        const int f = 2 * D + side;
+        const int code = m.lim_kind[(int64_t) f * E + e];
+        const int kind = code & 3;
+        const int slot = tl.slot[(int64_t) f * E + e];
+        if (kind == 1) {   // boundary: outward normal sg * e_D
+            const float sg = side ? 1.f : -1.f;
+            const float *o = s_f + (int64_t) slot * 3 * V;
+#pragma unroll
+            for (int v = 0; v < V; v++) {
+                acc0(R[v][0], R0l[v], o[v]);
+                R[v][1 + D] += 0.5f * sg * o[v];
+                R[v][1 + s] += o[V + v];
+                R[v][1 + t] += o[2 * V + v];
+            }
+            continue;
+        }
+        const float sg = side ? 1.f : -1.f;   // upper face of e: e is the lower leaf (+)
+        const int nsub = (kind == 2) ? 4 : 1;
+        for (int k = 0; k < nsub; k++) {
+            const float *o = s_f + (int64_t) (slot + k) * 3 * V;
+            const float os = (k & 1) ? 0.25f : -0.25f, ot = (k & 2) ? 0.25f : -0.25f;
+#pragma unroll
+            for (int v = 0; v < V; v++) {
+                const float a0 = o[v];
+                float as = o[V + v], at = o[2 * V + v];
+                if (kind == 2) { as = 0.5f * as + os * a0; at = 0.5f * at + ot * a0; }
+                acc0(R[v][0], R0l[v], sg * a0);
+                R[v][1 + D] += 0.5f * a0;
+                R[v][1 + s] += sg * as;
+                R[v][1 + t] += sg * at;
+            }
+        }
+    }
+}
+
+template <int NC, int FLUX>
+__global__ void __launch_bounds__(kTile, 5)
+tile_stage_kernel(MeshDev m, TileDev tl, const float *__restrict__ uh, const float *__restrict__ ul, const float *u0h,
+                  const float *u0l, float *oh, float *ol, float dth, float dtl, const double *__restrict__ dt_dev,
+                  float ah, float al, float bh, float bl, int comb, unsigned *err)
+{
+    constexpr int V = 4 + NC;
+    extern __shared__ float smem[];
+    float *s_u = smem;                       // [V*4][kTile]
+    float *s_f = smem + V * kNB * kTile;     // [faces][3V]
+    const int64_t E = m.n_elem;
+    const int64_t e_begin = (int64_t) blockIdx.x * kTile;
+    const int nloc = (int) min((int64_t) kTile, E - e_begin);
+    for (int i = threadIdx.x; i < V * kNB * kTile; i += kTile) {
+        const int plane = i / kTile, l = i % kTile;
+        s_u[i] = (l < nloc) ? __ldg(uh + (int64_t) plane * E + e_begin + l) : 0.f;
+    }
+    __syncthreads();
+    // ---- faces of the tile ----
+    const int f0 = tl.fptr[blockIdx.x], f1 = tl.fptr[blockIdx.x + 1];
+    for (int j = f0 + threadIdx.x; j < f1; j += kTile) {
+        const int code = tl.faces[j];
+        float *out = s_f + (int64_t) (j - f0) * 3 * V;
+        if (code & 1) {
+            const int jb = code >> 1;
+            switch (m.bface_face[jb] >> 1) {
+            case 0: tile_boundary<NC, FLUX, 0>(m, s_u, uh, e_begin, jb, out, err); break;
+            case 1: tile_boundary<NC, FLUX, 1>(m, s_u, uh, e_begin, jb, out, err); break;
+            default: tile_boundary<NC, FLUX, 2>(m, s_u, uh, e_begin, jb, out, err); break;
+            }
+        } else {
+            const int64_t i = code >> 1;
+            switch (m.face_info[i] & 3) {
+            case 0: tile_interior<NC, FLUX, 0>(m, s_u, uh, e_begin, i, out, err); break;
+            case 1: tile_interior<NC, FLUX, 1>(m, s_u, uh, e_begin, i, out, err); break;
+            default: tile_interior<NC, FLUX, 2>(m, s_u, uh, e_begin, i, out, err); break;
+            }
+        }
+    }
+    __syncthreads();
+    if ((int) threadIdx.x >= nloc) return;
+    // ---- element: volume integral, gather, update ----
+    const int l = threadIdx.x;
+    const int64_t e = e_begin + l;
+    const int lev = m.level[e];
+    const float hx = level_ht<float>(m, lev, 0), hy = level_ht<float>(m, lev, 1), hz = level_ht<float>(m, lev, 2);
+    const float vol = hx * hy * hz;
+    float c[V][kNB];
+#pragma unroll
+    for (int v = 0; v < V; v++)
+#pragma unroll
+        for (int k = 0; k < kNB; k++) c[v][k] = s_u[(v * kNB + k) * kTile + l];
+    float R[V][kNB], R0l[V];
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+        R0l[v] = 0.f;
+#pragma unroll
+        for (int k = 0; k < kNB; k++) R[v][k] = 0.f;
+    }
+    {
+        float F[V], G[V], H[V];
+#pragma unroll
+        for (int v = 0; v < V; v++) F[v] = G[v] = H[v] = 0.f;
+        const bool grav = c_cfg.has_grav != 0;
+        float gr[3][kNB];
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+            for (int k = 0; k < kNB; k++) gr[a][k] = 0.f;
+#pragma unroll 1
+        for (int g = 0; g < 8; g++) {
+            const float px = (g & 1) ? (float) kGaussPhi : -(float) kGaussPhi;
+            const float py = (g & 2) ? (float) kGaussPhi : -(float) kGaussPhi;
+            const float pz = (g & 4) ? (float) kGaussPhi : -(float) kGaussPhi;
+            float U[V];
+#pragma unroll
+            for (int v = 0; v < V; v++) U[v] = c[v][0] + px * c[v][1] + py * c[v][2] + pz * c[v][3];
+            Prim<float, NC> p;
+            cons_to_prim<float, NC>(U, p);
+            if (!(p.r > 0.f) || !(p.p > 0.f)) set_error(err, (isfinite(p.r) && isfinite(p.p)) ? kErrNegative : kErrNonFinite);
+            F[0] += U[0] * p.u + p.p; F[1] += U[0] * p.v; F[2] += U[0] * p.w; F[3] += U[0] * p.e_tot + p.p * p.u;
+            G[0] += U[1] * p.u; G[1] += U[1] * p.v + p.p; G[2] += U[1] * p.w; G[3] += U[1] * p.e_tot + p.p * p.v;
+            H[0] += U[2] * p.u; H[1] += U[2] * p.v; H[2] += U[2] * p.w + p.p; H[3] += U[2] * p.e_tot + p.p * p.w;
+#pragma unroll
+            for (int i = 0; i < NC; i++) {
+                F[4 + i] += U[0] * p.c[i];
+                G[4 + i] += U[1] * p.c[i];
+                H[4 + i] += U[2] * p.c[i];
+            }
+            if (grav) {
+                const float phi[4] = {1.f, px, py, pz};
+#pragma unroll
+                for (int a = 0; a < 3; a++)
+#pragma unroll
+                    for (int k = 0; k < kNB; k++) gr[a][k] += p.r * c_cfg.grav_f[a] * phi[k];
+            }
+        }
+        const float w8 = vol * 0.125f;
+#pragma unroll
+        for (int v = 0; v < V; v++) {
+            R[v][1] -= F[v] * (w8 / hx);
+            R[v][2] -= G[v] * (w8 / hy);
+            R[v][3] -= H[v] * (w8 / hz);
+        }
+        if (grav) {
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                acc0(R[a][0], R0l[a], -gr[a][0] * w8);
+#pragma unroll
+                for (int k = 1; k < kNB; k++) R[a][k] -= gr[a][k] * w8;
+            }
+        }
+    }
+    tile_gather_axis<NC, 0>(m, tl, s_f, e, R, R0l);
+    tile_gather_axis<NC, 1>(m, tl, s_f, e, R, R0l);
+    tile_gather_axis<NC, 2>(m, tl, s_f, e, R, R0l);
+    if (dt_dev) {
+        const double d = *dt_dev;
+        dth = __double2float_rn(d);
+        dtl = __double2float_rn(d - (double) dth);
+    }
+    const float minv0 = 1.f / vol, minv1 = 12.f / vol;
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+#pragma unroll
+        for (int k = 0; k < kNB; k++) {
+            const int64_t idx = (int64_t) (v * kNB + k) * E + e;
+            FF x = {uh[idx], ul[idx]};
+            FF y;
+            if (k == 0) {
+                const float rh = __fmul_rn(R[v][0], minv0);
+                const float rl = __fmaf_rn(R0l[v], minv0, __fmaf_rn(R[v][0], minv0, -rh));
+                y = ff_sub_scaled(x, rh, dth, dtl);
+                y = ff_sub_scaled(y, rl, dth, dtl);
+            } else {
+                y = ff_sub_scaled(x, R[v][k] * minv1, dth, dtl);
+            }
+            if (comb) {
+                const FF w0 = {u0h[idx], u0l[idx]};
+                y = ff_comb(y, w0, ah, al, bh, bl);
+            }
+            oh[idx] = y.h;
+            ol[idx] = y.l;
+        }
+    }
+}
+
 }  // namespace charm
