@@ -54,6 +54,18 @@ class Config(C.Structure):
                 ("use_visc", C.c_int), ("check_every", C.c_int)]
 
 
+class Objective(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("pad", C.c_int32), ("lo", C.c_double * 3), ("hi", C.c_double * 3)]
+
+
+class AdjointInfo(C.Structure):
+    _fields_ = [("J", C.c_double), ("forward_steps", C.c_int64), ("reverse_steps", C.c_int64),
+                ("snapshots", C.c_int32), ("pad", C.c_int32), ("seconds", C.c_double)]
+
+
+OBJ_PRESSURE_BOX = 1
+
+
 class Mesh(C.Structure):
     _fields_ = [("n_elem", C.c_int64), ("center", C.POINTER(C.c_double)), ("level", C.POINTER(C.c_int8)),
                 ("tree_len", C.c_double * 3), ("n_face", C.c_int64), ("face_elem", C.POINTER(C.c_int32)),
@@ -90,6 +102,9 @@ SIGNATURES = [
     ("charm_gpu_abi_sizes", C.c_int, [_I64P]),
     ("charm_gpu_residual_static", C.c_int, [C.POINTER(Config), C.POINTER(Mesh), _P, _P, _P]),
     ("charm_gpu_dims", C.c_int, [_P, _I64P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    ("charm_gpu_objective", C.c_int, [_P, C.POINTER(Objective), _DP, _P]),
+    ("charm_gpu_residual_adjoint", C.c_int, [_P, _P, _P]),
+    ("charm_gpu_adjoint", C.c_int, [_P, C.c_int, C.c_int, C.POINTER(Objective), _P, _P, C.POINTER(AdjointInfo)]),
     ("charm_host_forest_new", C.c_int, [C.POINTER(_P), _P, _P, _P, _P, C.c_int]),
     ("charm_host_forest_free", C.c_int, [_P]),
     ("charm_host_forest_count", C.c_int64, [_P]),

@@ -1,0 +1,537 @@
+// Reverse-mode (vector-Jacobian) derivatives of the pointwise arithmetic of
+// the DG residual, FP64: conserved -> primitive variables for an ideal gas
+// with constant cp, the Euler volume flux, the LF / CD / HLLC numerical
+// fluxes and the INLET / OUTLET / WALL_SLIP / WALL_NO_SLIP boundary states.
+//
+// Each *_vjp routine recomputes the forward quantities it needs from its
+// inputs (the same operations, in the same order, as the forward path:
+// charm_param_cons_to_prim src/charm_globals.c:183-208 with
+// charm_mat_eos_ideal src/charm_eos.c:98-118; charm_calc_flux_lf
+// src/charm_fluxes.c:255-315; charm_calc_flux_cd :513-559;
+// charm_calc_flux_hllc :439-510 with _charm_calc_flux_hllc_x_1 :324-437;
+// charm_bnd_cond src/charm_bnd_cond.c:21-146) and then accumulates the
+// adjoint.  Branches (upwind side, star region, clamps, max) are taken as the
+// forward evaluation takes them: the derivative is that of the active piece.
+//
+// Header-only and free of device intrinsics so that the same code is
+// compiled into the GPU kernels (__host__ __device__) and, for unit tests of
+// the derivatives, into a host library.
+#pragma once
+
+#include <math.h>
+
+#ifdef __CUDACC__
+#define ADJ_HD __host__ __device__ __forceinline__
+#else
+#define ADJ_HD inline
+#endif
+
+namespace charm {
+namespace adj {
+
+// Ideal gas with constant cp (the only EOS the adjoint supports).
+struct Gas {
+    double gam;      // cp / cv
+    double inv_cv;   // 1 / cv
+    double m;        // molar mass
+    double R;        // universal gas constant
+    double eps;      // clamp of the reference's EOS switch (1e-12)
+};
+
+template <int NC>
+struct Pr {                 // primitive state as the fluxes use it
+    double r, u, v, w, e, e_tot, p, t, cz;
+    double c[NC];
+    unsigned clamp;         // bit i: species fraction i was clamped to [0, 1]
+};
+
+template <int NC>
+struct PrBar {              // adjoint of Pr
+    double r, u, v, w, e, e_tot, p, t, cz;
+    double c[NC];
+};
+
+template <int NC>
+ADJ_HD void zero(PrBar<NC> &b)
+{
+    b.r = b.u = b.v = b.w = b.e = b.e_tot = b.p = b.t = b.cz = 0.0;
+    for (int i = 0; i < NC; i++) b.c[i] = 0.0;
+}
+
+// U = (ru, rv, rw, re, rc_0 ..) -> primitive state (eos flag 4 of an ideal
+// gas with constant cp).
+template <int NC>
+ADJ_HD void prim(const double *U, const Gas &g, Pr<NC> &p)
+{
+    double r = 0.0;
+    for (int i = 0; i < NC; i++) r += U[4 + i];
+    p.r = r;
+    const double ir = 1.0 / r;
+    p.u = U[0] * ir;
+    p.v = U[1] * ir;
+    p.w = U[2] * ir;
+    p.e_tot = U[3] * ir;
+    p.e = p.e_tot - 0.5 * (p.u * p.u + p.v * p.v + p.w * p.w);
+    p.clamp = 0;
+    for (int i = 0; i < NC; i++) {
+        double c = U[4 + i] * ir;
+        if (c < 0.0) { c = 0.0; p.clamp |= 1u << i; }
+        if (c > 1.0) { c = 1.0; p.clamp |= 1u << i; }
+        p.c[i] = c;
+    }
+    p.p = r * p.e * (g.gam - 1.0);
+    p.cz = sqrt(g.gam * p.p * ir);
+    p.t = p.e * g.inv_cv;
+}
+
+// Ub += (d prim / d U)^T b
+template <int NC>
+ADJ_HD void prim_vjp(const double *U, const Pr<NC> &p, const Gas &g, PrBar<NC> b, double *Ub)
+{
+    const double ir = 1.0 / p.r;
+    double b_ir = 0.0;
+    b.e += b.t * g.inv_cv;                                   // t = e / cv
+    if (p.cz > 0.0) {                                        // cz = sqrt(gam p ir)
+        const double d = 0.5 * g.gam / p.cz;
+        b.p += b.cz * d * ir;
+        b_ir += b.cz * d * p.p;
+    }
+    b.r += b.p * p.e * (g.gam - 1.0);                        // p = r e (gam - 1)
+    b.e += b.p * p.r * (g.gam - 1.0);
+    b.e_tot += b.e;                                          // e = e_tot - |v|^2/2
+    b.u -= b.e * p.u;
+    b.v -= b.e * p.v;
+    b.w -= b.e * p.w;
+    for (int i = 0; i < NC; i++)
+        if (!((p.clamp >> i) & 1u)) {                        // c_i = rc_i / r
+            Ub[4 + i] += b.c[i] * ir;
+            b_ir += b.c[i] * U[4 + i];
+        }
+    Ub[0] += b.u * ir;
+    Ub[1] += b.v * ir;
+    Ub[2] += b.w * ir;
+    Ub[3] += b.e_tot * ir;
+    b_ir += b.u * U[0] + b.v * U[1] + b.w * U[2] + b.e_tot * U[3];
+    b.r -= b_ir * ir * ir;                                   // ir = 1 / r
+    for (int i = 0; i < NC; i++) Ub[4 + i] += b.r;           // r = sum rc_i
+}
+
+// Euler volume fluxes F_d(U) (src/models/ns/charm_model_ns_conv.c:45-65):
+// F_d[j] = U[d] vel_j + p delta_dj, F_d[3] = U[d] e_tot + p vel_d,
+// F_d[4+i] = U[d] c_i.  Given a[d][.] = the adjoint of F_d, accumulate the
+// adjoint of the primitive state into b and of U[0..2] into Ub.
+template <int NC>
+ADJ_HD void vflux_vjp(const double *U, const Pr<NC> &p, const double a[3][4 + NC], PrBar<NC> &b, double *Ub)
+{
+    const double vel[3] = {p.u, p.v, p.w};
+    double vb[3] = {0.0, 0.0, 0.0};
+    for (int d = 0; d < 3; d++) {
+        double m = 0.0;
+        for (int j = 0; j < 3; j++) {
+            m += a[d][j] * vel[j];
+            vb[j] += a[d][j] * U[d];
+        }
+        m += a[d][3] * p.e_tot;
+        for (int i = 0; i < NC; i++) {
+            m += a[d][4 + i] * p.c[i];
+            b.c[i] += a[d][4 + i] * U[d];
+        }
+        Ub[d] += m;
+        b.p += a[d][d] + a[d][3] * vel[d];
+        vb[d] += a[d][3] * p.p;
+        b.e_tot += a[d][3] * U[d];
+    }
+    b.u += vb[0];
+    b.v += vb[1];
+    b.w += vb[2];
+}
+
+// Tangent frame of charm_calc_flux_hllc (src/charm_fluxes.c:458-488).
+ADJ_HD void frame(const double n[3], double nt[3][3])
+{
+    nt[0][0] = n[0]; nt[0][1] = n[1]; nt[0][2] = n[2];
+    double ri = sqrt(n[0] * n[0] + n[1] * n[1]);
+    if (ri > 1.e-12) {
+        nt[1][0] = -n[1] / ri; nt[1][1] = n[0] / ri; nt[1][2] = 0.0;
+    } else {
+        ri = sqrt(n[1] * n[1] + n[2] * n[2]);
+        if (ri > 1.e-12) {
+            nt[1][0] = 0.0; nt[1][1] = -n[2] / ri; nt[1][2] = n[1] / ri;
+        } else {
+            ri = sqrt(n[0] * n[0] + n[2] * n[2]);
+            nt[1][0] = -n[2] / ri; nt[1][1] = 0.0; nt[1][2] = n[0] / ri;
+        }
+    }
+    nt[2][0] = nt[0][1] * nt[1][2] - nt[0][2] * nt[1][1];
+    nt[2][1] = -nt[0][0] * nt[1][2] + nt[0][2] * nt[1][0];
+    nt[2][2] = nt[0][0] * nt[1][1] - nt[0][1] * nt[1][0];
+}
+
+// LF (central = false) or CD (central = true) flux adjoint.  q (optional)
+// receives the flux value.
+template <int NC>
+ADJ_HD void flux_lf_vjp(const Pr<NC> &a, const Pr<NC> &b, const double n[3], bool central, const double *qb,
+                        PrBar<NC> &ab, PrBar<NC> &bb, double *q)
+{
+    constexpr int V = 4 + NC;
+    const double h = 0.5;
+    const double va[3] = {a.u, a.v, a.w}, vbv[3] = {b.u, b.v, b.w};
+    const double vna = a.u * n[0] + a.v * n[1] + a.w * n[2];
+    const double vnb = b.u * n[0] + b.v * n[1] + b.w * n[2];
+    const double A = fabs(vna) + a.cz, B = fabs(vnb) + b.cz;
+    const double alpha = central ? 0.0 : fmax(A, B);
+    if (q) {
+        for (int j = 0; j < 3; j++)
+            q[j] = h * ((b.r * vnb * vbv[j] + b.p * n[j]) + (a.r * vna * va[j] + a.p * n[j]) -
+                        alpha * (b.r * vbv[j] - a.r * va[j]));
+        q[3] = h * (((b.r * b.e_tot + b.p) * vnb) + ((a.r * a.e_tot + a.p) * vna) - alpha * (b.r * b.e_tot - a.r * a.e_tot));
+        for (int i = 0; i < NC; i++)
+            q[4 + i] = h * ((b.r * vnb * b.c[i]) + (a.r * vna * a.c[i]) - alpha * (b.r * b.c[i] - a.r * a.c[i]));
+    }
+    double alb = 0.0, vnab = 0.0, vnbb = 0.0;
+    double vab[3] = {0.0, 0.0, 0.0}, vbb[3] = {0.0, 0.0, 0.0};
+    for (int j = 0; j < 3; j++) {
+        const double x = h * qb[j];
+        alb -= x * (b.r * vbv[j] - a.r * va[j]);
+        bb.r += x * (vnb * vbv[j] - alpha * vbv[j]);
+        vnbb += x * b.r * vbv[j];
+        vbb[j] += x * (b.r * vnb - alpha * b.r);
+        bb.p += x * n[j];
+        ab.r += x * (vna * va[j] + alpha * va[j]);
+        vnab += x * a.r * va[j];
+        vab[j] += x * (a.r * vna + alpha * a.r);
+        ab.p += x * n[j];
+    }
+    {
+        const double x = h * qb[3];
+        alb -= x * (b.r * b.e_tot - a.r * a.e_tot);
+        bb.r += x * (b.e_tot * vnb - alpha * b.e_tot);
+        bb.e_tot += x * (b.r * vnb - alpha * b.r);
+        bb.p += x * vnb;
+        vnbb += x * (b.r * b.e_tot + b.p);
+        ab.r += x * (a.e_tot * vna + alpha * a.e_tot);
+        ab.e_tot += x * (a.r * vna + alpha * a.r);
+        ab.p += x * vna;
+        vnab += x * (a.r * a.e_tot + a.p);
+    }
+    for (int i = 0; i < NC; i++) {
+        const double x = h * qb[4 + i];
+        alb -= x * (b.r * b.c[i] - a.r * a.c[i]);
+        bb.r += x * (vnb * b.c[i] - alpha * b.c[i]);
+        vnbb += x * b.r * b.c[i];
+        bb.c[i] += x * (b.r * vnb - alpha * b.r);
+        ab.r += x * (vna * a.c[i] + alpha * a.c[i]);
+        vnab += x * a.r * a.c[i];
+        ab.c[i] += x * (a.r * vna + alpha * a.r);
+    }
+    if (!central) {                                  // alpha = max(A, B)
+        if (A >= B) {
+            vnab += alb * ((vna > 0.0) ? 1.0 : ((vna < 0.0) ? -1.0 : 0.0));
+            ab.cz += alb;
+        } else {
+            vnbb += alb * ((vnb > 0.0) ? 1.0 : ((vnb < 0.0) ? -1.0 : 0.0));
+            bb.cz += alb;
+        }
+    }
+    ab.u += vab[0] + vnab * n[0]; ab.v += vab[1] + vnab * n[1]; ab.w += vab[2] + vnab * n[2];
+    bb.u += vbb[0] + vnbb * n[0]; bb.v += vbb[1] + vnbb * n[1]; bb.w += vbb[2] + vnbb * n[2];
+    (void) V;
+}
+
+// HLLC flux adjoint (the PVRS wave speeds of src/charm_fluxes.c:340-372, the
+// four upwind / star cases of :374-435, rotation back :505-509).
+template <int NC>
+ADJ_HD void flux_hllc_vjp(const Pr<NC> &a, const Pr<NC> &b, const double n[3], const Gas &g, const double *qb,
+                          PrBar<NC> &ab, PrBar<NC> &bb, double *q)
+{
+    double nt[3][3];
+    frame(n, nt);
+    const double ua = a.u * nt[0][0] + a.v * nt[0][1] + a.w * nt[0][2];
+    const double va = a.u * nt[1][0] + a.v * nt[1][1] + a.w * nt[1][2];
+    const double wa = a.u * nt[2][0] + a.v * nt[2][1] + a.w * nt[2][2];
+    const double ub = b.u * nt[0][0] + b.v * nt[0][1] + b.w * nt[0][2];
+    const double vb = b.u * nt[1][0] + b.v * nt[1][1] + b.w * nt[1][2];
+    const double wb = b.u * nt[2][0] + b.v * nt[2][1] + b.w * nt[2][2];
+    const double gam = g.gam;
+
+    const double p_pvrs = 0.5 * (a.p + b.p) - 0.5 * (ub - ua) * 0.25 * (a.r + b.r) * (a.cz + b.cz);
+    const double p_star = (p_pvrs > 0.0) ? p_pvrs : 0.0;
+    const double kq = (gam + 1.0) / (2.0 * gam);
+    const bool shock_a = !(p_star <= a.p), shock_b = !(p_star <= b.p);
+    const double ql = shock_a ? sqrt(1.0 + (gam + 1.0) * (p_star / a.p - 1.0) / (2.0 * gam)) : 1.0;
+    const double qr = shock_b ? sqrt(1.0 + (gam + 1.0) * (p_star / b.p - 1.0) / (2.0 * gam)) : 1.0;
+    const double sl0 = ua - a.cz * ql, sr0 = ub + b.cz * qr;
+    const bool swap = sl0 > sr0;
+    const double sl = swap ? sr0 : sl0, sr = swap ? sl0 : sr0;
+    double num = b.p - a.p;
+    num += a.r * ua * (sl - ua);
+    num -= b.r * ub * (sr - ub);
+    const double den = a.r * (sl - ua) - b.r * (sr - ub);
+    double ss = num / den;
+    int clamp = 0;
+    if (ss < sl) { ss = sl; clamp = 1; }
+    if (ss > sr) { ss = sr; clamp = 2; }
+
+    // the state k of the active case
+    const bool sup_a = (sl >= 0.0), sup_b = !sup_a && (sr <= 0.0);
+    const bool star = !sup_a && !sup_b;
+    const bool ka = sup_a || (star && ss >= 0.0);
+    const double rk = ka ? a.r : b.r, uk = ka ? ua : ub, vk = ka ? va : vb, wk = ka ? wa : wb;
+    const double pk = ka ? a.p : b.p, ek = ka ? a.e_tot : b.e_tot, sk = ka ? sl : sr;
+    const double *ck = ka ? a.c : b.c;
+
+    if (q) {
+        double fu, fv, fw;
+        if (!star) {
+            fu = rk * uk * uk + pk; fv = rk * vk * uk; fw = rk * wk * uk;
+            q[3] = (rk * ek + pk) * uk;
+            for (int i = 0; i < NC; i++) q[4 + i] = rk * uk * ck[i];
+        } else {
+            const double inv = 1.0 / (sk - ss);
+            fu = (ss * (sk * (rk * uk) - (rk * uk * uk + pk)) + sk * (pk + rk * (sk - uk) * (ss - uk))) * inv;
+            fv = (ss * (sk * (rk * vk) - rk * uk * vk)) * inv;
+            fw = (ss * (sk * (rk * wk) - rk * uk * wk)) * inv;
+            q[3] = (ss * (sk * (rk * ek) - (rk * ek + pk) * uk) + sk * (pk + rk * (sk - uk) * (ss - uk)) * ss) * inv;
+            for (int i = 0; i < NC; i++) q[4 + i] = (ss * (sk * (rk * ck[i]) - rk * ck[i] * uk)) * inv;
+        }
+        q[0] = fu * nt[0][0] + fv * nt[1][0] + fw * nt[2][0];
+        q[1] = fu * nt[0][1] + fv * nt[1][1] + fw * nt[2][1];
+        q[2] = fu * nt[0][2] + fv * nt[1][2] + fw * nt[2][2];
+    }
+
+    // ---- reverse ----
+    const double fub = qb[0] * nt[0][0] + qb[1] * nt[0][1] + qb[2] * nt[0][2];
+    const double fvb = qb[0] * nt[1][0] + qb[1] * nt[1][1] + qb[2] * nt[1][2];
+    const double fwb = qb[0] * nt[2][0] + qb[1] * nt[2][1] + qb[2] * nt[2][2];
+    const double qeb = qb[3];
+    double rkb = 0.0, ukb = 0.0, vkb = 0.0, wkb = 0.0, pkb = 0.0, ekb = 0.0, skb = 0.0, ssb = 0.0;
+    double ckb[NC];
+    for (int i = 0; i < NC; i++) ckb[i] = 0.0;
+    if (!star) {
+        rkb = fub * uk * uk + fvb * vk * uk + fwb * wk * uk + qeb * ek * uk;
+        ukb = fub * 2.0 * rk * uk + fvb * rk * vk + fwb * rk * wk + qeb * (rk * ek + pk);
+        vkb = fvb * rk * uk;
+        wkb = fwb * rk * uk;
+        pkb = fub + qeb * uk;
+        ekb = qeb * rk * uk;
+        for (int i = 0; i < NC; i++) {
+            const double x = qb[4 + i];
+            rkb += x * uk * ck[i];
+            ukb += x * rk * ck[i];
+            ckb[i] += x * rk * uk;
+        }
+    } else {
+        const double X = sk - uk, Y = ss - uk, G = 1.0 / (sk - ss), G2 = G * G;
+        // h(phi) = ss rk phi X G for phi = vk, wk, c_i
+        auto hterm = [&](double bar, double phi, double &phib) {
+            ssb += bar * rk * phi * X * sk * G2;
+            skb -= bar * ss * rk * phi * Y * G2;
+            ukb -= bar * ss * rk * phi * G;
+            rkb += bar * ss * phi * X * G;
+            phib += bar * ss * rk * X * G;
+        };
+        hterm(fvb, vk, vkb);
+        hterm(fwb, wk, wkb);
+        for (int i = 0; i < NC; i++) hterm(qb[4 + i], ck[i], ckb[i]);
+        // fu = ss rk uk X G + pk + sk rk X Y G
+        ssb += fub * (rk * uk * X * sk * G2 + sk * rk * X * X * G2);
+        skb += fub * (-ss * rk * uk * Y * G2 + rk * Y * G * (X + sk - sk * X * G));
+        ukb += fub * (ss * rk * G * (X - uk) - sk * rk * G * (X + Y));
+        rkb += fub * (ss * uk * X * G + sk * X * Y * G);
+        pkb += fub;
+        // qe = ss X G W, W = rk ek + pk + sk rk Y
+        const double W = rk * ek + pk + sk * rk * Y;
+        ssb += qeb * (X * W * sk * G2 + ss * X * G * sk * rk);
+        skb += qeb * (ss * (-W * Y * G2 + X * G * rk * Y));
+        ukb += qeb * (ss * G * (-W - X * sk * rk));
+        rkb += qeb * (ss * X * G * (ek + sk * Y));
+        ekb += qeb * (ss * X * G * rk);
+        pkb += qeb * (ss * X * G);
+    }
+    // wave speeds
+    double slb = 0.0, srb = 0.0;
+    if (ka) slb += skb; else srb += skb;
+    double uab = 0.0, ubb = 0.0;
+    if (clamp == 1) slb += ssb;
+    else if (clamp == 2) srb += ssb;
+    else {
+        const double numb = ssb / den, denb = -ssb * ss / den;
+        bb.p += numb; ab.p -= numb;
+        ab.r += numb * ua * (sl - ua); uab += numb * a.r * (sl - 2.0 * ua); slb += numb * a.r * ua;
+        bb.r -= numb * ub * (sr - ub); ubb -= numb * b.r * (sr - 2.0 * ub); srb -= numb * b.r * ub;
+        ab.r += denb * (sl - ua); slb += denb * a.r; uab -= denb * a.r;
+        bb.r -= denb * (sr - ub); srb -= denb * b.r; ubb += denb * b.r;
+    }
+    const double sl0b = swap ? srb : slb, sr0b = swap ? slb : srb;
+    uab += sl0b; ab.cz -= sl0b * ql;
+    const double qlb = -sl0b * a.cz;
+    ubb += sr0b; bb.cz += sr0b * qr;
+    const double qrb = sr0b * b.cz;
+    double pstarb = 0.0;
+    if (shock_a) {
+        const double d = 0.5 / ql * kq;
+        pstarb += qlb * d / a.p;
+        ab.p -= qlb * d * p_star / (a.p * a.p);
+    }
+    if (shock_b) {
+        const double d = 0.5 / qr * kq;
+        pstarb += qrb * d / b.p;
+        bb.p -= qrb * d * p_star / (b.p * b.p);
+    }
+    if (p_pvrs > 0.0) {
+        const double D = ub - ua, Rs = 0.25 * (a.r + b.r), Cs = a.cz + b.cz;
+        ab.p += 0.5 * pstarb; bb.p += 0.5 * pstarb;
+        const double Db = -0.5 * pstarb * Rs * Cs;
+        ubb += Db; uab -= Db;
+        const double Rsb = -0.5 * pstarb * D * Cs;
+        ab.r += 0.25 * Rsb; bb.r += 0.25 * Rsb;
+        const double Csb = -0.5 * pstarb * D * Rs;
+        ab.cz += Csb; bb.cz += Csb;
+    }
+    // the active state's adjoint
+    if (ka) {
+        ab.r += rkb; uab += ukb; ab.p += pkb; ab.e_tot += ekb;
+        for (int i = 0; i < NC; i++) ab.c[i] += ckb[i];
+    } else {
+        bb.r += rkb; ubb += ukb; bb.p += pkb; bb.e_tot += ekb;
+        for (int i = 0; i < NC; i++) bb.c[i] += ckb[i];
+    }
+    const double vab = ka ? vkb : 0.0, wab = ka ? wkb : 0.0;
+    const double vbbv = ka ? 0.0 : vkb, wbb = ka ? 0.0 : wkb;
+    // rotated velocities
+    ab.u += uab * nt[0][0] + vab * nt[1][0] + wab * nt[2][0];
+    ab.v += uab * nt[0][1] + vab * nt[1][1] + wab * nt[2][1];
+    ab.w += uab * nt[0][2] + vab * nt[1][2] + wab * nt[2][2];
+    bb.u += ubb * nt[0][0] + vbbv * nt[1][0] + wbb * nt[2][0];
+    bb.v += ubb * nt[0][1] + vbbv * nt[1][1] + wbb * nt[2][1];
+    bb.w += ubb * nt[0][2] + vbbv * nt[1][2] + wbb * nt[2][2];
+}
+
+// Boundary types (values of CHARM_GPU_BND_*).
+enum { kBndInlet = 0, kBndOutlet = 1, kBndWallSlip = 2, kBndWallNoSlip = 3, kBndMassFlow = 4 };
+
+// Ghost state of a boundary face (charm_bnd_cond, src/charm_bnd_cond.c:21-146)
+// followed by eos flag 3 ((T, p) -> r, cz, e) and e_tot.  `pressure_clamped`
+// records the p >= eps clamp of the EOS switch.
+template <int NC>
+ADJ_HD void bnd(int type, const double *par, const Pr<NC> &in, const double n[3], const Gas &g, Pr<NC> &out,
+                bool &pressure_clamped)
+{
+    out = in;
+    if (type == kBndInlet) {
+        out.u = par[0]; out.v = par[1]; out.w = par[2];
+        out.t = par[3]; out.p = par[4];
+    } else if (type == kBndWallSlip) {
+        const double svn = in.u * n[0] + in.v * n[1] + in.w * n[2];
+        const double vv0 = n[0] * svn, vv1 = n[1] * svn, vv2 = n[2] * svn;
+        out.u = (in.u - vv0) - vv0;
+        out.v = (in.v - vv1) - vv1;
+        out.w = (in.w - vv2) - vv2;
+    } else if (type == kBndWallNoSlip) {
+        const double svn = in.u * n[0] + in.v * n[1] + in.w * n[2];
+        out.u = in.u - n[0] * svn;
+        out.v = in.v - n[1] * svn;
+        out.w = in.w - n[2] * svn;
+        out.t = par[0];
+    }
+    pressure_clamped = out.p < g.eps;
+    if (pressure_clamped) out.p = g.eps;
+    out.r = out.p * g.m / (out.t * g.R);
+    out.cz = sqrt(g.gam * out.p / out.r);
+    out.e = out.p / (out.r * (g.gam - 1.0));
+    out.e_tot = out.e + 0.5 * (out.u * out.u + out.v * out.v + out.w * out.w);
+}
+
+// inb += (d out / d in)^T outb for the ghost state of bnd().
+template <int NC>
+ADJ_HD void bnd_vjp(int type, const Pr<NC> &out, bool pressure_clamped, const double n[3], const Gas &g,
+                    PrBar<NC> ob, PrBar<NC> &inb)
+{
+    // e_tot = e + |v|^2 / 2
+    ob.e += ob.e_tot;
+    ob.u += ob.e_tot * out.u; ob.v += ob.e_tot * out.v; ob.w += ob.e_tot * out.w;
+    // e = p / (r (gam - 1))
+    ob.p += ob.e / (out.r * (g.gam - 1.0));
+    ob.r -= ob.e * out.e / out.r;
+    // cz = sqrt(gam p / r)
+    if (out.cz > 0.0) {
+        ob.p += ob.cz * out.cz / (2.0 * out.p);
+        ob.r -= ob.cz * out.cz / (2.0 * out.r);
+    }
+    // r = p m / (t R)
+    ob.p += ob.r * out.r / out.p;
+    ob.t -= ob.r * out.r / out.t;
+    if (pressure_clamped) ob.p = 0.0;
+    for (int i = 0; i < NC; i++) inb.c[i] += ob.c[i];
+    if (type == kBndInlet) return;
+    inb.p += ob.p;
+    if (type != kBndWallNoSlip) inb.t += ob.t;
+    if (type == kBndWallSlip) {
+        const double s = ob.u * n[0] + ob.v * n[1] + ob.w * n[2];
+        inb.u += ob.u - 2.0 * n[0] * s; inb.v += ob.v - 2.0 * n[1] * s; inb.w += ob.w - 2.0 * n[2] * s;
+    } else if (type == kBndWallNoSlip) {
+        const double s = ob.u * n[0] + ob.v * n[1] + ob.w * n[2];
+        inb.u += ob.u - n[0] * s; inb.v += ob.v - n[1] * s; inb.w += ob.w - n[2] * s;
+    } else {
+        inb.u += ob.u; inb.v += ob.v; inb.w += ob.w;
+    }
+}
+
+// Flux selector values (CHARM_GPU_FLUX_*).
+enum { kFluxLF = 0, kFluxGodunov = 1, kFluxHLLC = 2, kFluxCD = 3 };
+
+template <int NC>
+ADJ_HD void num_flux_vjp(int flux, const Pr<NC> &a, const Pr<NC> &b, const double n[3], const Gas &g,
+                         const double *qb, PrBar<NC> &ab, PrBar<NC> &bb, double *q)
+{
+    if (flux == kFluxHLLC) flux_hllc_vjp<NC>(a, b, n, g, qb, ab, bb, q);
+    else flux_lf_vjp<NC>(a, b, n, flux == kFluxCD, qb, ab, bb, q);
+}
+
+// Interior point: (Ua, Ub) -> q; Uab/Ubb += (dq/dU)^T qb.
+template <int NC>
+ADJ_HD void point_vjp(int flux, const double *Ua, const double *Ub, const double n[3], const Gas &g,
+                      const double *qb, double *Uab, double *Ubb, double *q)
+{
+    Pr<NC> a, b;
+    prim<NC>(Ua, g, a);
+    prim<NC>(Ub, g, b);
+    PrBar<NC> ab, bb;
+    zero<NC>(ab);
+    zero<NC>(bb);
+    num_flux_vjp<NC>(flux, a, b, n, g, qb, ab, bb, q);
+    prim_vjp<NC>(Ua, a, g, ab, Uab);
+    prim_vjp<NC>(Ub, b, g, bb, Ubb);
+}
+
+// Boundary point: U -> q(U, ghost(U)); Uab += (dq/dU)^T qb.
+template <int NC>
+ADJ_HD void bpoint_vjp(int flux, int type, const double *par, const double *U, const double n[3], const Gas &g,
+                       const double *qb, double *Uab, double *q)
+{
+    Pr<NC> a, o;
+    prim<NC>(U, g, a);
+    bool pc;
+    bnd<NC>(type, par, a, n, g, o, pc);
+    PrBar<NC> ab, ob;
+    zero<NC>(ab);
+    zero<NC>(ob);
+    num_flux_vjp<NC>(flux, a, o, n, g, qb, ab, ob, q);
+    bnd_vjp<NC>(type, o, pc, n, g, ob, ab);
+    prim_vjp<NC>(U, a, g, ab, Uab);
+}
+
+// Volume point: U -> F_d(U), d = 0..2; Uab += sum_d (dF_d/dU)^T a[d].
+template <int NC>
+ADJ_HD void vpoint_vjp(const double *U, const Gas &g, const double a[3][4 + NC], double *Uab)
+{
+    Pr<NC> p;
+    prim<NC>(U, g, p);
+    PrBar<NC> b;
+    zero<NC>(b);
+    vflux_vjp<NC>(U, p, a, b, Uab);
+    prim_vjp<NC>(U, p, g, b, Uab);
+}
+
+}  // namespace adj
+}  // namespace charm

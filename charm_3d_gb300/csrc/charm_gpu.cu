@@ -24,6 +24,7 @@
 
 #include "charm_gpu.h"
 #include "dg_kernels.cuh"
+#include "dg_adjoint.cuh"
 
 using namespace charm;
 
@@ -79,6 +80,13 @@ struct charm_gpu_handle_s {
     int32_t *d_tile_fptr = nullptr, *d_tile_faces = nullptr, *d_tile_slot = nullptr;
     int64_t n_tiles = 0;
     size_t tile_smem = 0;      // dynamic shared memory of tile_stage_kernel (0: use ff_stage_kernel)
+    // discrete adjoint (allocated by the first adjoint call, sized by the mesh)
+    double *d_adj_lam = nullptr, *d_adj_s = nullptr, *d_adj_acc = nullptr;   // [V][B][E] each
+    double *d_adj_u1 = nullptr, *d_adj_u2 = nullptr, *d_adj_fin = nullptr;   // stage states, final state
+    double *d_adj_psi = nullptr;                                              // [3][V][E] limiter scalings
+    double *d_obj_part = nullptr;                                             // objective partial sums
+    std::vector<double *> d_snap;                                             // checkpoints
+    bool adj_valid = false;           // d_adj_lam holds dJ/du0 of the last adjoint run
     double *d_dt = nullptr;            // CFL step (bits as unsigned long long)
     unsigned *d_err = nullptr;
     bool mesh_ready = false;
@@ -112,6 +120,15 @@ void free_mesh(charm_gpu_handle_s *h)
     if (h->d_tile_faces) cudaFree(h->d_tile_faces);
     if (h->d_tile_slot) cudaFree(h->d_tile_slot);
     h->d_tile_fptr = h->d_tile_faces = h->d_tile_slot = nullptr;
+    double **adj[] = {&h->d_adj_lam, &h->d_adj_s, &h->d_adj_acc, &h->d_adj_u1, &h->d_adj_u2, &h->d_adj_fin,
+                      &h->d_adj_psi, &h->d_obj_part};
+    for (double **q : adj) {
+        if (*q) cudaFree(*q);
+        *q = nullptr;
+    }
+    for (double *q : h->d_snap) cudaFree(q);
+    h->d_snap.clear();
+    h->adj_valid = false;
     h->n_tiles = 0;
     h->tile_smem = 0;
     h->d_center = nullptr; h->d_level = nullptr; h->d_face_elem = nullptr; h->d_face_info = nullptr;
@@ -313,14 +330,15 @@ int launch_cell(charm_gpu_handle_s *h, const double *u, const double *u0, double
 }
 
 template <int NC>
-int launch_limit(charm_gpu_handle_s *h, const double *ua, const double *u0, double *out, double a_new, double a_old)
+int launch_limit(charm_gpu_handle_s *h, const double *ua, const double *u0, double *out, double a_new, double a_old,
+                 double *psi_out = nullptr)
 {
     MeshDev m = mesh_view(h);
     const int bs = 128;
     const int64_t nb = (h->E + bs - 1) / bs;
     TimedLaunch t;
     begin_launch(h, 2, &t);
-    limit_kernel<NC><<<(unsigned) nb, bs, 0, h->stream>>>(m, ua, u0, out, a_new, a_old);
+    limit_kernel<NC><<<(unsigned) nb, bs, 0, h->stream>>>(m, ua, u0, out, a_new, a_old, psi_out);
     end_launch(h, &t);
     CUDA_TRY(cudaGetLastError());
     return CHARM_GPU_OK;
@@ -1085,13 +1103,15 @@ int charm_gpu_probe_peak(int device, int which, double *tflops)
     return CHARM_GPU_OK;
 }
 
-int charm_gpu_abi_sizes(int64_t out[4])
+int charm_gpu_abi_sizes(int64_t out[6])
 {
     if (!out) return fail(CHARM_GPU_EINVAL, "null argument");
     out[0] = sizeof(charm_gpu_config_t);
     out[1] = sizeof(charm_gpu_mesh_t);
     out[2] = sizeof(charm_gpu_comp_t);
     out[3] = sizeof(charm_gpu_bnd_t);
+    out[4] = sizeof(charm_gpu_objective_t);
+    out[5] = sizeof(charm_gpu_adjoint_info_t);
     return CHARM_GPU_OK;
 }
 
@@ -1396,3 +1416,5 @@ extern "C" int charm_gpu_residual_static(const charm_gpu_config_t *cfg, const ch
     if (h_ctl[kCtlDeviceErr] & kErrHllc) return fail(CHARM_GPU_EHLLC, "HLLC: SL <= S* <= SR violated");
     return CHARM_GPU_OK;
 }
+
+#include "adjoint_host.cuh"

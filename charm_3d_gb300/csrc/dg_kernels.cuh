@@ -418,7 +418,7 @@ cell_kernel(MeshDev m, const double *__restrict__ u, const T *__restrict__ slots
 template <int NC>
 __global__ void __launch_bounds__(128)
 limit_kernel(MeshDev m, const double *__restrict__ ua, const double *u0, double *out,
-             double a_new, double a_old)
+             double a_new, double a_old, double *__restrict__ psi_out)
 {
     constexpr int V = 4 + NC;
     const int64_t e = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
@@ -494,6 +494,10 @@ limit_kernel(MeshDev m, const double *__restrict__ ua, const double *u0, double 
             }
             if (pt < psi[v]) psi[v] = pt;
         }
+    }
+    if (psi_out) {   // the scaling, kept for the adjoint (frozen active set)
+#pragma unroll
+        for (int v = 0; v < V; v++) psi_out[(int64_t) v * E + e] = psi[v];
     }
     const bool comb = (a_old != 0.0);
 #pragma unroll

@@ -185,6 +185,42 @@ class Solver:
         abi.check(self.lib.charm_gpu_residual(self.h, a.ctypes.data, 0), "charm_gpu_residual")
         return a
 
+    def residual_adjoint(self, rbar: np.ndarray) -> np.ndarray:
+        """(dR/du)^T rbar at the current state."""
+        rb = np.ascontiguousarray(rbar, dtype=np.float64)
+        out = np.empty(self.shape())
+        abi.check(self.lib.charm_gpu_residual_adjoint(self.h, rb.ctypes.data, out.ctypes.data),
+                  "charm_gpu_residual_adjoint")
+        return out
+
+    @staticmethod
+    def pressure_box(lo, hi) -> abi.Objective:
+        obj = abi.Objective()
+        obj.kind = abi.OBJ_PRESSURE_BOX
+        for k in range(3):
+            obj.lo[k], obj.hi[k] = float(lo[k]), float(hi[k])
+        return obj
+
+    def objective(self, obj: abi.Objective, grad: bool = False):
+        """J of the current state, and dJ/du when grad is set."""
+        J = C.c_double()
+        g = np.empty(self.shape()) if grad else None
+        abi.check(self.lib.charm_gpu_objective(self.h, C.byref(obj), C.byref(J),
+                                               g.ctypes.data if grad else None), "charm_gpu_objective")
+        return (J.value, g) if grad else J.value
+
+    def adjoint(self, n_steps: int, n_snapshots: int, obj: abi.Objective | None = None,
+                dJdu_final: np.ndarray | None = None) -> tuple[np.ndarray, abi.AdjointInfo]:
+        """dJ/du(0) through n_steps steps from the current state (which ends at step n_steps)."""
+        out = np.empty(self.shape())
+        info = abi.AdjointInfo()
+        fin = None if dJdu_final is None else np.ascontiguousarray(dJdu_final, dtype=np.float64)
+        abi.check(self.lib.charm_gpu_adjoint(self.h, int(n_steps), int(n_snapshots),
+                                             C.byref(obj) if obj is not None else None,
+                                             fin.ctypes.data if fin is not None else None, out.ctypes.data,
+                                             C.byref(info)), "charm_gpu_adjoint")
+        return out, info
+
     def limit(self) -> None:
         abi.check(self.lib.charm_gpu_limit(self.h), "charm_gpu_limit")
 

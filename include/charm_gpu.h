@@ -204,8 +204,9 @@ int charm_gpu_time_run(charm_gpu_handle_t h, int nsteps, double dt_in, double *m
 int charm_gpu_probe_peak(int device, int which, double *tflops);
 
 /* sizeof of the ABI structs as compiled into the library, for binding checks:
- * out[0] config, out[1] mesh, out[2] comp, out[3] bnd. */
-int charm_gpu_abi_sizes(int64_t out[4]);
+ * out[0] config, out[1] mesh, out[2] comp, out[3] bnd, out[4] objective,
+ * out[5] adjoint info. */
+int charm_gpu_abi_sizes(int64_t out[6]);
 
 /*
  * Residual R(u) (as charm_gpu_residual) without allocating any device
@@ -229,6 +230,54 @@ int charm_gpu_residual_static(const charm_gpu_config_t *cfg, const charm_gpu_mes
 
 /* Element count, variables and basis size of the uploaded mesh. */
 int charm_gpu_dims(charm_gpu_handle_t h, int64_t *n_elem, int *n_var, int *n_basis);
+
+/* ---- discrete adjoint ------------------------------------------------------
+ * No counterpart in the reference (it has no adjoint).  The transpose of the
+ * exact derivative of the FP64 time step as the GPU computes it: face fluxes
+ * (LF, CD, HLLC), boundary states (inlet, outlet, slip and no-slip walls),
+ * volume fluxes, gravity, the RK stages and their combinations; the BJ
+ * limiter enters with its scaling frozen at the forward value (the active
+ * set is not differentiated).  Requires an FP64 handle, an ideal gas with
+ * constant cp and a fixed step (TAU); other configurations return
+ * CHARM_GPU_ENOTSUP.  Arrays are host [V][B][E] like the state. */
+
+enum { CHARM_GPU_OBJ_PRESSURE_BOX = 1 };
+
+/* J = integral of the pressure over the elements whose centre lies in
+ * [lo, hi) (8-point Gauss rule per element). */
+typedef struct {
+    int32_t kind;       /* CHARM_GPU_OBJ_* */
+    int32_t pad;
+    double  lo[3], hi[3];
+} charm_gpu_objective_t;
+
+typedef struct {
+    double  J;               /* objective at the final state (0 when dJ/du was given) */
+    int64_t forward_steps;   /* forward time steps taken, recomputation included */
+    int64_t reverse_steps;   /* adjoint steps (= n_steps) */
+    int32_t snapshots;       /* checkpoints held at most, the initial state included */
+    int32_t pad;
+    double  seconds;         /* wall time of the call */
+} charm_gpu_adjoint_info_t;
+
+/* J and dJ/du (dJdu may be NULL) of the current state. */
+int charm_gpu_objective(charm_gpu_handle_t h, const charm_gpu_objective_t *obj, double *J, double *dJdu);
+
+/* ubar = (dR/du)^T rbar at the current state, R the residual of
+ * charm_gpu_residual. */
+int charm_gpu_residual_adjoint(charm_gpu_handle_t h, const double *rbar, double *ubar);
+
+/* Gradient of J(u(n_steps)) with respect to the current state u(0), through
+ * n_steps time steps of the handle's scheme.  J is `obj` at the final state,
+ * or, when dJdu_final is not NULL, the linear functional with that gradient.
+ * Step states are checkpointed in n_snapshots device buffers (the initial
+ * state included) and recomputed by binomial checkpointing (Griewank's
+ * revolve schedule), so any run length fits the memory given.  dJdu0 (may be
+ * NULL: the gradient stays on the device for charm_gpu_refine_flags_adjoint)
+ * receives dJ/du(0).  The handle ends at the final state, as after
+ * charm_gpu_run(h, n_steps, 0). */
+int charm_gpu_adjoint(charm_gpu_handle_t h, int n_steps, int n_snapshots, const charm_gpu_objective_t *obj,
+                      const double *dJdu_final, double *dJdu0, charm_gpu_adjoint_info_t *info);
 
 /* ---- host octree (the CPU side of the boundary) -------------------------- */
 

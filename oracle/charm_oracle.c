@@ -993,3 +993,37 @@ int oracle_point_flux(oracle_t *o, const double *prim2, const double n[3], doubl
     num_flux(o, pr, n, q);
     return 0;
 }
+
+/* Point fluxes on conserved states (U = ru rv rw re rc_i), for the
+ * derivative tests of the adjoint: interior (two states), boundary (one
+ * state and the ghost of boundary bid) and the volume fluxes F[3][V]. */
+int oracle_point_flux_cons(oracle_t *o, const double *U2, const double n[3], double *q)
+{
+    prim_t pr[2];
+    for (int s = 0; s < 2; s++) cons_to_prim(o, U2 + s * o->V, &pr[s]);
+    num_flux(o, pr, n, q);
+    return 0;
+}
+
+int oracle_point_bflux_cons(oracle_t *o, int bid, const double *U, const double n[3], double *q)
+{
+    prim_t pr[2];
+    cons_to_prim(o, U, &pr[0]);
+    bnd_cond(o, bid, &pr[0], &pr[1], n);
+    num_flux(o, pr, n, q);
+    return 0;
+}
+
+int oracle_point_vflux(oracle_t *o, const double *U, double *F)
+{   /* the volume fluxes of residual() above (src/models/ns/charm_model_ns_conv.c:45-65) */
+    const int V = o->V;
+    prim_t p;
+    cons_to_prim(o, U, &p);
+    const double vel[3] = {p.u, p.v, p.w};
+    for (int d = 0; d < 3; d++) {
+        for (int j = 0; j < 3; j++) F[d * V + j] = U[d] * vel[j] + (j == d ? p.p : 0.);
+        F[d * V + 3] = U[d] * p.e_tot + p.p * vel[d];
+        for (int i = 0; i < o->cfg.n_comp; i++) F[d * V + 4 + i] = U[d] * p.c[i];
+    }
+    return 0;
+}

@@ -23,6 +23,9 @@ def load() -> C.CDLL:
         lib.oracle_step.argtypes = [C.c_void_p, C.c_double]
         lib.oracle_run.argtypes = [C.c_void_p, C.c_int, C.c_double]
         lib.oracle_point_flux.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.oracle_point_flux_cons.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.oracle_point_bflux_cons.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.oracle_point_vflux.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         lib.oracle_amr_grad.argtypes = [C.c_void_p, C.c_void_p]
         _lib = lib
     return _lib
@@ -80,6 +83,29 @@ class Port:
         g = np.empty((3, self.mesh.n_elem))
         self.lib.oracle_amr_grad(self.h, g.ctypes.data)
         return g
+
+    def point_flux_cons(self, U2, n) -> np.ndarray:
+        """Numerical flux between two conserved states U2[2][V] along n."""
+        U = np.ascontiguousarray(U2, dtype=np.float64)
+        nn = np.ascontiguousarray(n, dtype=np.float64)
+        q = np.zeros(4 + self.cfg.n_comp)
+        self.lib.oracle_point_flux_cons(self.h, U.ctypes.data, nn.ctypes.data, q.ctypes.data)
+        return q
+
+    def point_bflux_cons(self, bid, U, n) -> np.ndarray:
+        """Boundary flux of conserved state U through boundary bid, outward normal n."""
+        Uc = np.ascontiguousarray(U, dtype=np.float64)
+        nn = np.ascontiguousarray(n, dtype=np.float64)
+        q = np.zeros(4 + self.cfg.n_comp)
+        self.lib.oracle_point_bflux_cons(self.h, int(bid), Uc.ctypes.data, nn.ctypes.data, q.ctypes.data)
+        return q
+
+    def point_vflux(self, U) -> np.ndarray:
+        """Volume fluxes F[3][V] of conserved state U."""
+        Uc = np.ascontiguousarray(U, dtype=np.float64)
+        F = np.zeros((3, 4 + self.cfg.n_comp))
+        self.lib.oracle_point_vflux(self.h, Uc.ctypes.data, F.ctypes.data)
+        return F
 
     def point_flux(self, prim2, n) -> np.ndarray:
         p = np.ascontiguousarray(prim2, dtype=np.float64)

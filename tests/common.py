@@ -91,3 +91,29 @@ def amr_run_oracle(case: Case, steps: int):
         port.step(case.tau)
         u = port.get_state()
     return forest, mesh, u
+
+
+GAUSS_PHI = 0.28867513459481288225   # 1/(2 sqrt 3): Taylor basis at the 2x2x2 Gauss points
+
+
+def pressure_box_J(case, mesh, u, lo, hi) -> float:
+    """Integral of the pressure over the elements whose centre lies in [lo, hi)
+    (8-point Gauss rule), the objective of charm_gpu_objective, in numpy."""
+    _, gam = case.gas_constants()
+    E = mesh.n_elem
+    c = mesh.center
+    inside = np.ones(E, bool)
+    for d in range(3):
+        inside &= (c[d] >= lo[d]) & (c[d] < hi[d])
+    h = np.stack([np.asarray(mesh.tree_len[d]) * 2.0 ** (-mesh.level.astype(np.float64)) for d in range(3)])
+    w8 = h[0] * h[1] * h[2] * 0.125
+    J = 0.0
+    for g in range(8):
+        phi = [GAUSS_PHI if (g >> d) & 1 else -GAUSS_PHI for d in range(3)]
+        U = u[:, 0, :] + phi[0] * u[:, 1, :] + phi[1] * u[:, 2, :] + phi[2] * u[:, 3, :]
+        r = U[4:].sum(axis=0)
+        vel = U[:3] / r
+        e = U[3] / r - 0.5 * (vel * vel).sum(axis=0)
+        p = r * e * (gam - 1.0)
+        J += float((w8 * p)[inside].sum())
+    return J

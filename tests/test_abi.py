@@ -35,12 +35,14 @@ def test_binding_covers_every_declared_symbol():
 
 def test_struct_sizes_match_binding():
     lib = abi.load()
-    out = np.zeros(4, np.int64)
+    out = np.zeros(6, np.int64)
     assert lib.charm_gpu_abi_sizes(out.ctypes.data_as(C.POINTER(C.c_int64))) == 0
     assert out[0] == C.sizeof(abi.Config)
     assert out[1] == C.sizeof(abi.Mesh)
     assert out[2] == C.sizeof(abi.Comp)
     assert out[3] == C.sizeof(abi.Bnd)
+    assert out[4] == C.sizeof(abi.Objective)
+    assert out[5] == C.sizeof(abi.AdjointInfo)
 
 
 def test_version_string():

@@ -1,0 +1,213 @@
+"""Discrete adjoint on the GPU (charm_gpu_residual_adjoint, charm_gpu_adjoint)
+against central finite differences, eps = 1e-6, through the GPU solver and
+through the oracle, and the checkpointing schedule.
+
+Bar: |<dJ/du0, d> - (J(u0 + eps d) - J(u0 - eps d)) / (2 eps)| <= 1e-6
+relative, on random directions d."""
+import math
+
+import numpy as np
+import pytest
+
+from charm_3d_gb300.solver import Forest, Solver
+from oracle.port import Port
+
+from .common import hanging_forest, pressure_box_J, small_case
+
+pytestmark = pytest.mark.gpu
+
+FD_EPS = 1e-6
+FD_TOL = 1e-6
+
+
+def _setup(case, forest=None):
+    case.precision = "FP64"
+    forest = forest or Forest(case)
+    mesh = forest.flatten()
+    gpu = Solver(case)
+    gpu.upload(mesh)
+    u0 = case.initial_state(mesh.center)
+    gpu.set_state(u0)
+    return mesh, gpu, u0
+
+
+def _direction(rng, u0, var=None):
+    """A random direction scaled like the state (or only in one variable)."""
+    scale = np.abs(u0).mean(axis=2, keepdims=True) + 1e-3
+    d = rng.normal(size=u0.shape) * scale
+    if var is not None:
+        m = np.zeros_like(d)
+        m[var] = d[var]
+        d = m
+    return d
+
+
+def _rel(a, b):
+    return abs(a - b) / max(abs(a), abs(b), 1e-300)
+
+
+RESIDUAL_CASES = [("random", "LF"), ("random", "HLLC"), ("random", "CD"), ("walls", "HLLC"), ("walls", "LF"),
+                  ("vortex", "HLLC")]
+
+
+@pytest.mark.parametrize("kind,flux", RESIDUAL_CASES)
+def test_residual_adjoint_matches_fd(kind, flux):
+    case = small_case(kind, flux, "NONE")
+    mesh, gpu, u0 = _setup(case)
+    port = Port(case.config(), mesh)
+    rng = np.random.default_rng(3)
+    rbar = rng.normal(size=u0.shape)
+    ubar = gpu.residual_adjoint(rbar)
+    for trial in range(3):
+        d = _direction(rng, u0)
+        lhs = float((ubar * d).sum())
+        Rp, Rm = [], []
+        for sgn, out in ((1, Rp), (-1, Rm)):
+            gpu.set_state(u0 + sgn * FD_EPS * d)
+            out.append(gpu.residual())
+            port.set_state(u0 + sgn * FD_EPS * d)
+            out.append(port.residual())
+        fd_gpu = float((rbar * (Rp[0] - Rm[0])).sum()) / (2 * FD_EPS)
+        fd_port = float((rbar * (Rp[1] - Rm[1])).sum()) / (2 * FD_EPS)
+        assert _rel(lhs, fd_gpu) < FD_TOL, (trial, lhs, fd_gpu)
+        assert _rel(lhs, fd_port) < FD_TOL, (trial, lhs, fd_port)
+        gpu.set_state(u0)
+
+
+def test_residual_adjoint_hanging_faces():
+    case = small_case("random", "HLLC", "NONE")
+    forest, _ = hanging_forest(case)
+    mesh, gpu, u0 = _setup(case, forest)
+    port = Port(case.config(), mesh)
+    rng = np.random.default_rng(5)
+    rbar = rng.normal(size=u0.shape)
+    ubar = gpu.residual_adjoint(rbar)
+    for trial in range(3):
+        d = _direction(rng, u0)
+        port.set_state(u0 + FD_EPS * d)
+        Rp = port.residual()
+        port.set_state(u0 - FD_EPS * d)
+        Rm = port.residual()
+        fd = float((rbar * (Rp - Rm)).sum()) / (2 * FD_EPS)
+        assert _rel(float((ubar * d).sum()), fd) < FD_TOL
+
+
+def _box(case):
+    """The middle half of the domain along each axis."""
+    lo = list(case.origin)
+    hi = [o + b * t for o, b, t in zip(case.origin, case.brick, case.tree_len)]
+    mid = [0.5 * (a + b) for a, b in zip(lo, hi)]
+    q = [0.25 * (b - a) for a, b in zip(lo, hi)]
+    return [m - x for m, x in zip(mid, q)], [m + x for m, x in zip(mid, q)]
+
+
+ADJ_CASES = [("vortex", "HLLC", "NS", 3, 8), ("random", "LF", "NS", 2, 6), ("walls", "HLLC", "NS", 2, 5),
+             ("random", "HLLC", "EULER", 2, 6)]
+
+
+@pytest.mark.parametrize("kind,flux,model,level,nsteps", ADJ_CASES)
+def test_adjoint_matches_fd_gpu_and_oracle(kind, flux, model, level, nsteps):
+    case = small_case(kind, flux, "NONE", level=level, model=model)
+    mesh, gpu, u0 = _setup(case)
+    lo, hi = _box(case)
+    obj = Solver.pressure_box(lo, hi)
+    grad, info = gpu.adjoint(nsteps, 3, obj)
+    assert np.isfinite(grad).all() and info.reverse_steps == nsteps
+    # J matches the forward run and the numpy objective on the oracle's final state
+    port = Port(case.config(), mesh)
+    port.set_state(u0)
+    port.run(nsteps, case.tau)
+    J_port = pressure_box_J(case, mesh, port.get_state(), lo, hi)
+    assert _rel(info.J, J_port) < 1e-12
+    rng = np.random.default_rng(11)
+    for trial in range(4):
+        d = _direction(rng, u0, var=4 if trial % 2 else None)
+        lhs = float((grad * d).sum())
+        Js = []
+        for sgn in (1, -1):
+            gpu.set_state(u0 + sgn * FD_EPS * d)
+            gpu.run(nsteps, case.tau)
+            Js.append(gpu.objective(obj))
+        fd = (Js[0] - Js[1]) / (2 * FD_EPS)
+        assert _rel(lhs, fd) < FD_TOL, (trial, lhs, fd)
+        if trial < 2:
+            Jp = []
+            for sgn in (1, -1):
+                port.set_state(u0 + sgn * FD_EPS * d)
+                port.run(nsteps, case.tau)
+                Jp.append(pressure_box_J(case, mesh, port.get_state(), lo, hi))
+            assert _rel(lhs, (Jp[0] - Jp[1]) / (2 * FD_EPS)) < FD_TOL
+
+
+def _revolve_cost(n, s):
+    """Forward steps of the optimal binomial schedule (recomputations of the
+    adjoint steps themselves not counted)."""
+    if n <= 1:
+        return 0
+    if s <= 1:
+        return n * (n - 1) // 2
+    t = 0
+    while math.comb(s + t, s) < n:
+        t += 1
+    return t * n - math.comb(s + 1 + t - 1, s + 1)
+
+
+@pytest.mark.parametrize("snaps", [1, 2, 3, 5, 40])
+def test_checkpointing_schedule(snaps):
+    case = small_case("vortex", "HLLC", "NONE", level=2)
+    mesh, gpu, u0 = _setup(case)
+    obj = Solver.pressure_box(*_box(case))
+    n = 17
+    ref_grad, ref_info = gpu.adjoint(n, n, obj)
+    gpu.set_state(u0)
+    grad, info = gpu.adjoint(n, snaps, obj)
+    # the same arithmetic whatever the schedule
+    assert np.array_equal(grad, ref_grad)
+    assert info.J == ref_info.J
+    s = min(snaps, n)
+    assert info.forward_steps == _revolve_cost(n, s) + n
+    assert info.snapshots <= s
+
+
+def test_adjoint_leaves_final_state():
+    case = small_case("vortex", "HLLC", "NONE", level=2)
+    mesh, gpu, u0 = _setup(case)
+    gpu.adjoint(5, 2, Solver.pressure_box(*_box(case)))
+    after = gpu.get_state()
+    gpu.set_state(u0)
+    gpu.run(5, case.tau)
+    assert np.array_equal(after, gpu.get_state())
+
+
+def test_adjoint_linear_functional():
+    """dJdu_final given: J = <g, u(N)>."""
+    case = small_case("random", "HLLC", "NONE", level=2)
+    mesh, gpu, u0 = _setup(case)
+    rng = np.random.default_rng(21)
+    g = rng.normal(size=u0.shape)
+    grad, _ = gpu.adjoint(4, 2, None, dJdu_final=g)
+    d = _direction(rng, u0)
+    Js = []
+    for sgn in (1, -1):
+        gpu.set_state(u0 + sgn * FD_EPS * d)
+        gpu.run(4, case.tau)
+        Js.append(float((g * gpu.get_state()).sum()))
+    assert _rel(float((grad * d).sum()), (Js[0] - Js[1]) / (2 * FD_EPS)) < FD_TOL
+
+
+def test_adjoint_limiter_frozen_runs():
+    """With the BJ limiter the adjoint differentiates the stages with the
+    limiter scaling held at its forward value; where no element is limited it
+    is the exact gradient."""
+    case = small_case("vortex", "LF", "BJ", level=3)
+    mesh, gpu, u0 = _setup(case)
+    grad, info = gpu.adjoint(4, 2, Solver.pressure_box(*_box(case)))
+    assert np.isfinite(grad).all()
+
+
+def test_adjoint_rejects_unsupported():
+    from charm_3d_gb300.abi import CharmGpuError
+    case = small_case("mix2", "HLLC", "NONE", level=1)
+    mesh, gpu, u0 = _setup(case)
+    with pytest.raises(CharmGpuError):
+        gpu.adjoint(2, 1, Solver.pressure_box((0, 0, 0), (1, 1, 1)))
