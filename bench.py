@@ -304,6 +304,7 @@ def finish(args, rank, world, device, case, mesh, E, V, state_bytes, t_mesh, val
                 "fp64_pipe": {"peak_tflops_measured": fp64_peak,
                               "note": "plain FP64 path is bound by the FP64 pipe, see profiles/"}}
     cpu = cpu_baseline(args.cpu_level, args.cpu_seconds, 1) if args.cpu_seconds > 0 else None
+    adjoint = run_adjoint(args, device) if args.adjoint_steps > 0 else None
     n_launch = int(launches.sum())
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -314,8 +315,77 @@ def finish(args, rank, world, device, case, mesh, E, V, state_bytes, t_mesh, val
                        "parallelism": f"replicas x{world}",
                        "l2": f"inputs larger than L2 (state {state_bytes / 1e6:.0f} MB > 129 MB)",
                        "mesh_build_s": t_mesh},
-            "e2e": e2e, "mixed": mixed, "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": n_launch,
+            "e2e": e2e, "mixed": mixed, "adjoint": adjoint, "roofline": roofline, "cpu_baseline": cpu,
+            "gpu_launches": n_launch,
             "clocks": clk.summary()}
+
+
+def run_adjoint(args, device: int) -> dict:
+    """Discrete adjoint of the vortex at level `adjoint_level`: J = integral of
+    p over [4,6]^3 after `adjoint_steps` steps, gradient with respect to the
+    initial state (checked against central differences in the density
+    perturbation), its wall time against the forward run of the same steps."""
+    from charm_3d_gb300.solver import Forest, Solver
+    case = workload(args.adjoint_level)
+    case.precision = "FP64"
+    mesh = Forest(case).flatten()
+    u0 = case.initial_state(mesh.center)
+    n = args.adjoint_steps
+    snaps = args.adjoint_snapshots if args.adjoint_snapshots > 0 else 3 * n
+    obj = Solver.pressure_box((4.0, 4.0, 4.0), (6.0, 6.0, 6.0))
+    gpu = Solver(case, device)
+    gpu.upload(mesh)
+    gpu.set_state(u0)
+    gpu.run(3, case.tau)
+    gpu.sync()
+    # forward run of the same steps (wall clock, synchronised)
+    gpu.set_state(u0)
+    gpu.sync()
+    t0 = time.perf_counter()
+    gpu.run(n, case.tau)
+    gpu.sync()
+    t_fwd = time.perf_counter() - t0
+    J_fwd = gpu.objective(obj)
+    # the first call allocates the checkpoint buffers; the second is measured
+    gpu.set_state(u0)
+    gpu.adjoint(n, snaps, obj)
+    gpu.set_state(u0)
+    gpu.sync()
+    t0 = time.perf_counter()
+    grad, info = gpu.adjoint(n, snaps, obj)
+    t_adj = time.perf_counter() - t0
+    # central differences along random density perturbations (variable rc_0, coefficient 0)
+    rng = np.random.default_rng(2024)
+    eps = 1e-6
+    # the same run with J over the whole box: no zero region of the adjoint to skip
+    gpu.set_state(u0)
+    gpu.sync()
+    t0 = time.perf_counter()
+    gpu.adjoint(n, snaps, Solver.pressure_box((0.0, 0.0, 0.0), (10.0, 10.0, 10.0)))
+    t_dense = time.perf_counter() - t0
+    errs = []
+    for _ in range(args.adjoint_fd):
+        d = np.zeros_like(u0)
+        d[4, 0] = rng.uniform(-1.0, 1.0, mesh.n_elem)
+        Js = []
+        for sgn in (1.0, -1.0):
+            gpu.set_state(u0 + sgn * eps * d)
+            gpu.run(n, case.tau)
+            Js.append(gpu.objective(obj))
+        fd = (Js[0] - Js[1]) / (2 * eps)
+        ad = float((grad * d).sum())
+        errs.append(abs(ad - fd) / max(abs(fd), 1e-300))
+    gpu.close()
+    return {"workload": f"vortex level {args.adjoint_level} ({mesh.n_elem} hex), HLLC, no limiter, FP64, "
+                        f"J = integral of p over [4,6]^3 at step {n}",
+            "n_steps": n, "n_snapshots": snaps, "J": info.J, "J_forward": J_fwd,
+            "forward_s": t_fwd, "adjoint_s": t_adj, "adjoint_over_forward": t_adj / t_fwd,
+            "adjoint_whole_domain_J_over_forward": t_dense / t_fwd,
+            "forward_steps_in_adjoint": int(info.forward_steps), "snapshots_held": int(info.snapshots),
+            "fd_check": {"directions": args.adjoint_fd, "eps": eps, "max_rel_err": max(errs) if errs else None,
+                         "median_rel_err": float(np.median(errs)) if errs else None,
+                         "direction": "uniform(-1, 1) on the density mean of every element (the seeded "
+                                      "noise's variable and coefficient)"}}
 
 
 def probe(abi, device: int, which: int) -> float | None:
@@ -371,7 +441,12 @@ def main():
     ap.add_argument("--cpu-level", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--brick", type=int, default=1, help="trees along x (profiling sizes)")
-    ap.add_argument("--only", default="both", choices=["both", "fp64", "mixed"])
+    ap.add_argument("--only", default="both", choices=["both", "fp64", "mixed", "adjoint"])
+    ap.add_argument("--adjoint-level", type=int, default=6)
+    ap.add_argument("--adjoint-steps", type=int, default=200, help="0 skips the adjoint leg")
+    ap.add_argument("--adjoint-snapshots", type=int, default=0,
+                    help="checkpoint buffers (0: every stage state of the run, 3 per step)")
+    ap.add_argument("--adjoint-fd", type=int, default=16, help="finite-difference directions")
     ap.add_argument("--skip-e2e", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -398,6 +473,10 @@ def main():
         return
 
     rank, world, local = init_dist(args)
+    if args.only == "adjoint":
+        if rank == 0:
+            print(json.dumps({"only": "adjoint", "adjoint": run_adjoint(args, local)}))
+        return
     res = run_gpu(args, rank, world, local)
     if rank == 0 and res is not None:
         print(json.dumps(res))

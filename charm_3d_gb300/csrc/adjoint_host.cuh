@@ -40,9 +40,9 @@ int adj_alloc(charm_gpu_handle_s *h, int n_snap)
     return CHARM_GPU_OK;
 }
 
-double *adj_psi(charm_gpu_handle_s *h, int stage)
+double *adj_psi(charm_gpu_handle_s *h, double *psi, int stage)
 {
-    return h->d_adj_psi + (size_t) stage * n_var(h) * h->E;
+    return psi + (size_t) stage * n_var(h) * h->E;
 }
 
 template <int NC>
@@ -100,12 +100,12 @@ int launch_adj_init(charm_gpu_handle_s *h, const double *psi, double a, double b
     return CHARM_GPU_OK;
 }
 
-// Recompute the stage states of one step from `in`: u1 -> d_adj_u1, u2 ->
-// d_adj_u2, the limiter scalings of the stages -> d_adj_psi, and the new
-// state -> out when out is not null.  The stage that only produces the new
-// state is skipped when neither it nor its limiter scaling is needed.
+// Recompute the stage states of one step from `in`: u1, u2, the limiter
+// scalings of the stages -> psi ([3][V][E]), and the new state -> out when out
+// is not null.  The stage that only produces the new state is skipped when
+// neither it nor its limiter scaling is needed.
 template <int NC>
-int adj_forward_step(charm_gpu_handle_s *h, const double *in, double *out)
+int adj_forward_step(charm_gpu_handle_s *h, const double *in, double *u1, double *u2, double *psi, double *out)
 {
     const double dt = h->cfg.tau;
     const bool lim = h->cfg.limiter == CHARM_GPU_LIM_BJ;
@@ -115,7 +115,7 @@ int adj_forward_step(charm_gpu_handle_s *h, const double *in, double *out)
         if (r) return r;
         if (lim) {
             if ((r = launch_cell<double, NC>(h, u, nullptr, h->d_ua, dt, nullptr, 1.0, 0.0, kCellUpdate))) return r;
-            return launch_limit<NC>(h, h->d_ua, u0, dst, a, b, adj_psi(h, k));
+            return launch_limit<NC>(h, h->d_ua, u0, dst, a, b, adj_psi(h, psi, k));
         }
         return launch_cell<double, NC>(h, u, u0, dst, dt, nullptr, a, b, kCellUpdate);
     };
@@ -123,35 +123,35 @@ int adj_forward_step(charm_gpu_handle_s *h, const double *in, double *out)
         if (!out && !lim) return CHARM_GPU_OK;
         return stage(in, nullptr, out ? out : h->d_ub, 1.0, 0.0, 0);
     }
-    if ((rc = stage(in, nullptr, h->d_adj_u1, 1.0, 0.0, 0))) return rc;
-    if ((rc = stage(h->d_adj_u1, in, h->d_adj_u2, 0.25, 0.75, 1))) return rc;
+    if ((rc = stage(in, nullptr, u1, 1.0, 0.0, 0))) return rc;
+    if ((rc = stage(u1, in, u2, 0.25, 0.75, 1))) return rc;
     if (!out && !lim) return CHARM_GPU_OK;
-    return stage(h->d_adj_u2, in, out ? out : h->d_ub, 2.0 / 3.0, 1.0 / 3.0, 2);
+    return stage(u2, in, out ? out : h->d_ub, 2.0 / 3.0, 1.0 / 3.0, 2);
 }
 
-// d_adj_lam: dJ/du(n+1) -> dJ/du(n), with u(n) = in and the stage states of
-// adj_forward_step.
+// d_adj_lam: dJ/du(n+1) -> dJ/du(n), with u(n) = in and the stage states
+// (u1, u2, psi) of adj_forward_step.
 template <int NC>
-int adj_reverse_step(charm_gpu_handle_s *h, const double *in)
+int adj_reverse_step(charm_gpu_handle_s *h, const double *in, const double *u1, const double *u2, double *psi)
 {
     const double dt = h->cfg.tau;
     const bool lim = h->cfg.limiter == CHARM_GPU_LIM_BJ;
     int rc;
     if (h->cfg.model == CHARM_GPU_MODEL_EULER) {
-        if ((rc = launch_adj_init(h, lim ? adj_psi(h, 0) : nullptr, 1.0, 0.0, false))) return rc;
+        if ((rc = launch_adj_init(h, lim ? adj_psi(h, psi, 0) : nullptr, 1.0, 0.0, false))) return rc;
         if ((rc = launch_adj_face<NC>(h, in, h->d_adj_s, -dt, 1))) return rc;
         return launch_adj_cell<NC>(h, in, h->d_adj_s, -dt, 1, 1.0, kAdjFinal, nullptr, 0, 0, nullptr, h->d_adj_lam);
     }
     // u3 = 2/3 L(s3) + 1/3 u0
-    if ((rc = launch_adj_init(h, lim ? adj_psi(h, 2) : nullptr, 2.0 / 3.0, 1.0 / 3.0, true))) return rc;
+    if ((rc = launch_adj_init(h, lim ? adj_psi(h, psi, 2) : nullptr, 2.0 / 3.0, 1.0 / 3.0, true))) return rc;
     // stage 3 from u2; its u2^ feeds u2 = 1/4 L(s2) + 3/4 u0
-    if ((rc = launch_adj_face<NC>(h, h->d_adj_u2, h->d_adj_s, -dt, 1))) return rc;
-    if ((rc = launch_adj_cell<NC>(h, h->d_adj_u2, h->d_adj_s, -dt, 1, 1.0, kAdjStage, lim ? adj_psi(h, 1) : nullptr,
+    if ((rc = launch_adj_face<NC>(h, u2, h->d_adj_s, -dt, 1))) return rc;
+    if ((rc = launch_adj_cell<NC>(h, u2, h->d_adj_s, -dt, 1, 1.0, kAdjStage, lim ? adj_psi(h, psi, 1) : nullptr,
                                   0.25, 0.75, h->d_adj_acc, h->d_adj_s)))
         return rc;
     // stage 2 from u1; u1 = L(s1)
-    if ((rc = launch_adj_face<NC>(h, h->d_adj_u1, h->d_adj_s, -dt, 1))) return rc;
-    if ((rc = launch_adj_cell<NC>(h, h->d_adj_u1, h->d_adj_s, -dt, 1, 1.0, kAdjStage, lim ? adj_psi(h, 0) : nullptr,
+    if ((rc = launch_adj_face<NC>(h, u1, h->d_adj_s, -dt, 1))) return rc;
+    if ((rc = launch_adj_cell<NC>(h, u1, h->d_adj_s, -dt, 1, 1.0, kAdjStage, lim ? adj_psi(h, psi, 0) : nullptr,
                                   1.0, 0.0, nullptr, h->d_adj_s)))
         return rc;
     // stage 1 from u0, plus the u0 terms of the combinations
@@ -239,7 +239,9 @@ int adj_leaf(AdjRun &r, int64_t a)
     charm_gpu_handle_s *h = r.h;
     int rc;
     const bool last = (a == r.n_steps - 1) && !r.have_final;
-    if ((rc = adj_forward_step<NC>(h, h->d_u, last ? h->d_adj_fin : nullptr))) return rc;
+    if ((rc = adj_forward_step<NC>(h, h->d_u, h->d_adj_u1, h->d_adj_u2, h->d_adj_psi,
+                                   last ? h->d_adj_fin : nullptr)))
+        return rc;
     r.forward_steps += 1;
     if (last) {
         const size_t st = (size_t) n_var(h) * CHARM_GPU_BASIS * h->E * sizeof(double);
@@ -250,7 +252,7 @@ int adj_leaf(AdjRun &r, int64_t a)
         }
         r.have_final = true;
     }
-    if ((rc = adj_reverse_step<NC>(h, h->d_u))) return rc;
+    if ((rc = adj_reverse_step<NC>(h, h->d_u, h->d_adj_u1, h->d_adj_u2, h->d_adj_psi))) return rc;
     r.reverse_steps += 1;
     if (h->cfg.check_every > 0 && r.reverse_steps % h->cfg.check_every == 0) return charm_gpu_sync(h, 600.0);
     return CHARM_GPU_OK;
@@ -285,6 +287,55 @@ int adj_revolve(AdjRun &r, int64_t a, int64_t b, int slot_a, int s)
     return adj_revolve<NC>(r, a, m, slot_a, s);
 }
 
+// Number of state buffers per step that keep every stage state of it.
+int stage_states(const charm_gpu_handle_s *h) { return h->cfg.model == CHARM_GPU_MODEL_EULER ? 1 : 3; }
+
+// Enough buffers for every stage state of the run: one forward sweep keeps
+// them all and the reverse sweep recomputes nothing.
+template <int NC>
+int adjoint_all_stages(charm_gpu_handle_s *h, int n_steps, const charm_gpu_objective_t *obj,
+                       const double *dJdu_final, AdjRun &r)
+{
+    const size_t st = (size_t) n_var(h) * CHARM_GPU_BASIS * h->E * sizeof(double);
+    const int k = stage_states(h);
+    const bool lim = h->cfg.limiter == CHARM_GPU_LIM_BJ;
+    const size_t psi_n = (size_t) 3 * n_var(h) * h->E;   // per step
+    if (lim && h->n_psi_all < (size_t) n_steps * psi_n) {
+        if (h->d_adj_psi_all) cudaFree(h->d_adj_psi_all);
+        h->n_psi_all = 0;
+        if (cudaMalloc(&h->d_adj_psi_all, (size_t) n_steps * psi_n * sizeof(double)) != cudaSuccess) {
+            h->d_adj_psi_all = nullptr;
+            return fail(CHARM_GPU_ENOMEM, "adjoint limiter scalings");
+        }
+        h->n_psi_all = (size_t) n_steps * psi_n;
+    }
+    auto psi_of = [&](int64_t n) { return lim ? h->d_adj_psi_all + (size_t) n * psi_n : h->d_adj_psi; };
+    auto u1_of = [&](int64_t n) { return k == 3 ? h->d_snap[k * n + 1] : h->d_adj_u1; };
+    auto u2_of = [&](int64_t n) { return k == 3 ? h->d_snap[k * n + 2] : h->d_adj_u2; };
+    CUDA_TRY(cudaMemcpyAsync(h->d_snap[0], h->d_u, st, cudaMemcpyDeviceToDevice, h->stream));
+    int rc;
+    for (int64_t n = 0; n < n_steps; n++) {
+        double *out = (n + 1 < n_steps) ? h->d_snap[k * (n + 1)] : h->d_adj_fin;
+        if ((rc = adj_forward_step<NC>(h, h->d_snap[k * n], u1_of(n), u2_of(n), psi_of(n), out))) return rc;
+        r.forward_steps++;
+        if (h->cfg.check_every > 0 && (n + 1) % h->cfg.check_every == 0 && (rc = charm_gpu_sync(h, 600.0))) return rc;
+    }
+    if (dJdu_final) {
+        CUDA_TRY(cudaMemcpyAsync(h->d_adj_lam, dJdu_final, st, cudaMemcpyHostToDevice, h->stream));
+    } else if ((rc = objective_eval<NC>(h, h->d_adj_fin, obj, &r.J, h->d_adj_lam))) {
+        return rc;
+    }
+    for (int64_t n = n_steps - 1; n >= 0; n--) {
+        if ((rc = adj_reverse_step<NC>(h, h->d_snap[k * n], u1_of(n), u2_of(n), psi_of(n)))) return rc;
+        r.reverse_steps++;
+        if (h->cfg.check_every > 0 && r.reverse_steps % h->cfg.check_every == 0 && (rc = charm_gpu_sync(h, 600.0)))
+            return rc;
+    }
+    r.max_slots_used = k * n_steps;
+    CUDA_TRY(cudaMemcpyAsync(h->d_u, h->d_adj_fin, st, cudaMemcpyDeviceToDevice, h->stream));
+    return CHARM_GPU_OK;
+}
+
 template <int NC>
 int adjoint_impl(charm_gpu_handle_s *h, int n_steps, int n_snap, const charm_gpu_objective_t *obj,
                  const double *dJdu_final, AdjRun &r)
@@ -294,6 +345,7 @@ int adjoint_impl(charm_gpu_handle_s *h, int n_steps, int n_snap, const charm_gpu
     r.n_steps = n_steps;
     r.obj = obj;
     r.dJdu_final = dJdu_final;
+    if (n_snap >= stage_states(h) * n_steps) return adjoint_all_stages<NC>(h, n_steps, obj, dJdu_final, r);
     for (int k = n_snap - 1; k >= 1; k--) r.free_slots.push_back(k);
     CUDA_TRY(cudaMemcpyAsync(h->d_snap[0], h->d_u, st, cudaMemcpyDeviceToDevice, h->stream));
     int rc = adj_revolve<NC>(r, 0, n_steps, 0, n_snap);
@@ -360,7 +412,8 @@ int charm_gpu_adjoint(charm_gpu_handle_t h, int n_steps, int n_snapshots, const 
     if (n_steps < 1 || n_snapshots < 1) return fail(CHARM_GPU_EINVAL, "n_steps and n_snapshots must be >= 1");
     if (!obj && !dJdu_final) return fail(CHARM_GPU_EINVAL, "adjoint: need an objective or dJ/du at the final state");
     if ((rc = adj_check(h))) return rc;
-    const int n_snap = std::min(n_snapshots, n_steps);
+    const int n_snap = (n_snapshots >= stage_states(h) * n_steps) ? stage_states(h) * n_steps
+                                                                   : std::min(n_snapshots, n_steps);
     if ((rc = adj_alloc(h, n_snap))) return rc;
     h->adj_valid = false;
     const auto t0 = std::chrono::steady_clock::now();

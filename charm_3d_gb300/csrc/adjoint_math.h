@@ -41,6 +41,7 @@ struct Gas {
 template <int NC>
 struct Pr {                 // primitive state as the fluxes use it
     double r, u, v, w, e, e_tot, p, t, cz;
+    double ir;              // 1 / r
     double c[NC];
     unsigned clamp;         // bit i: species fraction i was clamped to [0, 1]
 };
@@ -67,6 +68,7 @@ ADJ_HD void prim(const double *U, const Gas &g, Pr<NC> &p)
     for (int i = 0; i < NC; i++) r += U[4 + i];
     p.r = r;
     const double ir = 1.0 / r;
+    p.ir = ir;
     p.u = U[0] * ir;
     p.v = U[1] * ir;
     p.w = U[2] * ir;
@@ -88,7 +90,7 @@ ADJ_HD void prim(const double *U, const Gas &g, Pr<NC> &p)
 template <int NC>
 ADJ_HD void prim_vjp(const double *U, const Pr<NC> &p, const Gas &g, PrBar<NC> b, double *Ub)
 {
-    const double ir = 1.0 / p.r;
+    const double ir = p.ir;
     double b_ir = 0.0;
     b.e += b.t * g.inv_cv;                                   // t = e / cv
     if (p.cz > 0.0) {                                        // cz = sqrt(gam p ir)
@@ -167,22 +169,64 @@ ADJ_HD void frame(const double n[3], double nt[3][3])
     nt[2][2] = nt[0][0] * nt[1][1] - nt[0][1] * nt[1][0];
 }
 
+// Frame of an axis-aligned normal n = s e_AX (AX >= 0): a signed
+// permutation, applied without the products with its zero entries; AX < 0
+// uses the general frame nt.  frame_in gives the components along the rows
+// of the frame, frame_out sums rows weighted by (fu, fv, fw); each is the
+// transpose of the other.
+template <int AX>
+ADJ_HD void frame_in(const double nt[3][3], double s, double x, double y, double z, double &un, double &u1,
+                     double &u2)
+{
+    if (AX == 0) { un = s * x; u1 = s * y; u2 = z; }
+    else if (AX == 1) { un = s * y; u1 = -s * x; u2 = z; }
+    else if (AX == 2) { un = s * z; u1 = -s * y; u2 = x; }
+    else {
+        un = x * nt[0][0] + y * nt[0][1] + z * nt[0][2];
+        u1 = x * nt[1][0] + y * nt[1][1] + z * nt[1][2];
+        u2 = x * nt[2][0] + y * nt[2][1] + z * nt[2][2];
+    }
+}
+
+template <int AX>
+ADJ_HD void frame_out(const double nt[3][3], double s, double fu, double fv, double fw, double *q)
+{
+    if (AX == 0) { q[0] = s * fu; q[1] = s * fv; q[2] = fw; }
+    else if (AX == 1) { q[1] = s * fu; q[0] = -s * fv; q[2] = fw; }
+    else if (AX == 2) { q[2] = s * fu; q[1] = -s * fv; q[0] = fw; }
+    else {
+        q[0] = fu * nt[0][0] + fv * nt[1][0] + fw * nt[2][0];
+        q[1] = fu * nt[0][1] + fv * nt[1][1] + fw * nt[2][1];
+        q[2] = fu * nt[0][2] + fv * nt[1][2] + fw * nt[2][2];
+    }
+}
+
+// v.n, without the zero products for an axis-aligned n
+template <int AX>
+ADJ_HD double vdotn(const double v[3], const double n[3])
+{
+    if (AX >= 0) return v[AX] * n[AX];
+    return v[0] * n[0] + v[1] * n[1] + v[2] * n[2];
+}
+
 // LF (central = false) or CD (central = true) flux adjoint.  q (optional)
 // receives the flux value.
-template <int NC>
+template <int NC, int AX = -1>
 ADJ_HD void flux_lf_vjp(const Pr<NC> &a, const Pr<NC> &b, const double n[3], bool central, const double *qb,
                         PrBar<NC> &ab, PrBar<NC> &bb, double *q)
 {
     constexpr int V = 4 + NC;
     const double h = 0.5;
     const double va[3] = {a.u, a.v, a.w}, vbv[3] = {b.u, b.v, b.w};
-    const double vna = a.u * n[0] + a.v * n[1] + a.w * n[2];
-    const double vnb = b.u * n[0] + b.v * n[1] + b.w * n[2];
+    const double vna = vdotn<AX>(va, n);
+    const double vnb = vdotn<AX>(vbv, n);
+    // n_j, zero off the axis
+    auto nj = [&](int j) { return (AX < 0 || j == AX) ? n[j] : 0.0; };
     const double A = fabs(vna) + a.cz, B = fabs(vnb) + b.cz;
     const double alpha = central ? 0.0 : fmax(A, B);
     if (q) {
         for (int j = 0; j < 3; j++)
-            q[j] = h * ((b.r * vnb * vbv[j] + b.p * n[j]) + (a.r * vna * va[j] + a.p * n[j]) -
+            q[j] = h * ((b.r * vnb * vbv[j] + b.p * nj(j)) + (a.r * vna * va[j] + a.p * nj(j)) -
                         alpha * (b.r * vbv[j] - a.r * va[j]));
         q[3] = h * (((b.r * b.e_tot + b.p) * vnb) + ((a.r * a.e_tot + a.p) * vna) - alpha * (b.r * b.e_tot - a.r * a.e_tot));
         for (int i = 0; i < NC; i++)
@@ -196,11 +240,10 @@ ADJ_HD void flux_lf_vjp(const Pr<NC> &a, const Pr<NC> &b, const double n[3], boo
         bb.r += x * (vnb * vbv[j] - alpha * vbv[j]);
         vnbb += x * b.r * vbv[j];
         vbb[j] += x * (b.r * vnb - alpha * b.r);
-        bb.p += x * n[j];
+        if (AX < 0 || j == AX) { bb.p += x * n[j]; ab.p += x * n[j]; }
         ab.r += x * (vna * va[j] + alpha * va[j]);
         vnab += x * a.r * va[j];
         vab[j] += x * (a.r * vna + alpha * a.r);
-        ab.p += x * n[j];
     }
     {
         const double x = h * qb[3];
@@ -233,25 +276,30 @@ ADJ_HD void flux_lf_vjp(const Pr<NC> &a, const Pr<NC> &b, const double n[3], boo
             bb.cz += alb;
         }
     }
-    ab.u += vab[0] + vnab * n[0]; ab.v += vab[1] + vnab * n[1]; ab.w += vab[2] + vnab * n[2];
-    bb.u += vbb[0] + vnbb * n[0]; bb.v += vbb[1] + vnbb * n[1]; bb.w += vbb[2] + vnbb * n[2];
+    if (AX >= 0) {
+        vab[AX] += vnab * n[AX];
+        vbb[AX] += vnbb * n[AX];
+    } else {
+        for (int j = 0; j < 3; j++) { vab[j] += vnab * n[j]; vbb[j] += vnbb * n[j]; }
+    }
+    ab.u += vab[0]; ab.v += vab[1]; ab.w += vab[2];
+    bb.u += vbb[0]; bb.v += vbb[1]; bb.w += vbb[2];
     (void) V;
 }
 
 // HLLC flux adjoint (the PVRS wave speeds of src/charm_fluxes.c:340-372, the
 // four upwind / star cases of :374-435, rotation back :505-509).
-template <int NC>
+template <int NC, int AX = -1>
 ADJ_HD void flux_hllc_vjp(const Pr<NC> &a, const Pr<NC> &b, const double n[3], const Gas &g, const double *qb,
                           PrBar<NC> &ab, PrBar<NC> &bb, double *q)
 {
-    double nt[3][3];
-    frame(n, nt);
-    const double ua = a.u * nt[0][0] + a.v * nt[0][1] + a.w * nt[0][2];
-    const double va = a.u * nt[1][0] + a.v * nt[1][1] + a.w * nt[1][2];
-    const double wa = a.u * nt[2][0] + a.v * nt[2][1] + a.w * nt[2][2];
-    const double ub = b.u * nt[0][0] + b.v * nt[0][1] + b.w * nt[0][2];
-    const double vb = b.u * nt[1][0] + b.v * nt[1][1] + b.w * nt[1][2];
-    const double wb = b.u * nt[2][0] + b.v * nt[2][1] + b.w * nt[2][2];
+    double nt[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+    double sn = 1.0;
+    if (AX < 0) frame(n, nt);
+    else sn = n[AX < 0 ? 0 : AX];
+    double ua, va, wa, ub, vb, wb;
+    frame_in<AX>(nt, sn, a.u, a.v, a.w, ua, va, wa);
+    frame_in<AX>(nt, sn, b.u, b.v, b.w, ub, vb, wb);
     const double gam = g.gam;
 
     const double p_pvrs = 0.5 * (a.p + b.p) - 0.5 * (ub - ua) * 0.25 * (a.r + b.r) * (a.cz + b.cz);
@@ -294,15 +342,12 @@ ADJ_HD void flux_hllc_vjp(const Pr<NC> &a, const Pr<NC> &b, const double n[3], c
             q[3] = (ss * (sk * (rk * ek) - (rk * ek + pk) * uk) + sk * (pk + rk * (sk - uk) * (ss - uk)) * ss) * inv;
             for (int i = 0; i < NC; i++) q[4 + i] = (ss * (sk * (rk * ck[i]) - rk * ck[i] * uk)) * inv;
         }
-        q[0] = fu * nt[0][0] + fv * nt[1][0] + fw * nt[2][0];
-        q[1] = fu * nt[0][1] + fv * nt[1][1] + fw * nt[2][1];
-        q[2] = fu * nt[0][2] + fv * nt[1][2] + fw * nt[2][2];
+        frame_out<AX>(nt, sn, fu, fv, fw, q);
     }
 
     // ---- reverse ----
-    const double fub = qb[0] * nt[0][0] + qb[1] * nt[0][1] + qb[2] * nt[0][2];
-    const double fvb = qb[0] * nt[1][0] + qb[1] * nt[1][1] + qb[2] * nt[1][2];
-    const double fwb = qb[0] * nt[2][0] + qb[1] * nt[2][1] + qb[2] * nt[2][2];
+    double fub, fvb, fwb;
+    frame_in<AX>(nt, sn, qb[0], qb[1], qb[2], fub, fvb, fwb);
     const double qeb = qb[3];
     double rkb = 0.0, ukb = 0.0, vkb = 0.0, wkb = 0.0, pkb = 0.0, ekb = 0.0, skb = 0.0, ssb = 0.0;
     double ckb[NC];
@@ -322,17 +367,20 @@ ADJ_HD void flux_hllc_vjp(const Pr<NC> &a, const Pr<NC> &b, const double n[3], c
         }
     } else {
         const double X = sk - uk, Y = ss - uk, G = 1.0 / (sk - ss), G2 = G * G;
-        // h(phi) = ss rk phi X G for phi = vk, wk, c_i
-        auto hterm = [&](double bar, double phi, double &phib) {
-            ssb += bar * rk * phi * X * sk * G2;
-            skb -= bar * ss * rk * phi * Y * G2;
-            ukb -= bar * ss * rk * phi * G;
-            rkb += bar * ss * phi * X * G;
-            phib += bar * ss * rk * X * G;
-        };
-        hterm(fvb, vk, vkb);
-        hterm(fwb, wk, wkb);
-        for (int i = 0; i < NC; i++) hterm(qb[4 + i], ck[i], ckb[i]);
+        // h(phi) = ss rk phi X G for phi = vk, wk, c_i: the adjoints of ss,
+        // sk, uk, rk are linear in sum(bar * phi)
+        const double KX = ss * X * G, K = rk * KX;
+        double sc = fvb * vk + fwb * wk;
+        for (int i = 0; i < NC; i++) {
+            sc += qb[4 + i] * ck[i];
+            ckb[i] += qb[4 + i] * K;
+        }
+        vkb += fvb * K;
+        wkb += fwb * K;
+        ssb += sc * rk * X * sk * G2;
+        skb -= sc * ss * rk * Y * G2;
+        ukb -= sc * ss * rk * G;
+        rkb += sc * KX;
         // fu = ss rk uk X G + pk + sk rk X Y G
         ssb += fub * (rk * uk * X * sk * G2 + sk * rk * X * X * G2);
         skb += fub * (-ss * rk * uk * Y * G2 + rk * Y * G * (X + sk - sk * X * G));
@@ -355,7 +403,7 @@ ADJ_HD void flux_hllc_vjp(const Pr<NC> &a, const Pr<NC> &b, const double n[3], c
     if (clamp == 1) slb += ssb;
     else if (clamp == 2) srb += ssb;
     else {
-        const double numb = ssb / den, denb = -ssb * ss / den;
+        const double numb = ssb / den, denb = -numb * ss;
         bb.p += numb; ab.p -= numb;
         ab.r += numb * ua * (sl - ua); uab += numb * a.r * (sl - 2.0 * ua); slb += numb * a.r * ua;
         bb.r -= numb * ub * (sr - ub); ubb -= numb * b.r * (sr - 2.0 * ub); srb -= numb * b.r * ub;
@@ -368,15 +416,15 @@ ADJ_HD void flux_hllc_vjp(const Pr<NC> &a, const Pr<NC> &b, const double n[3], c
     ubb += sr0b; bb.cz += sr0b * qr;
     const double qrb = sr0b * b.cz;
     double pstarb = 0.0;
-    if (shock_a) {
-        const double d = 0.5 / ql * kq;
-        pstarb += qlb * d / a.p;
-        ab.p -= qlb * d * p_star / (a.p * a.p);
+    if (shock_a) {   // ql = sqrt(1 + kq (p*/pa - 1))
+        const double d = 0.5 * kq / (ql * a.p);
+        pstarb += qlb * d;
+        ab.p -= qlb * d * p_star / a.p;
     }
     if (shock_b) {
-        const double d = 0.5 / qr * kq;
-        pstarb += qrb * d / b.p;
-        bb.p -= qrb * d * p_star / (b.p * b.p);
+        const double d = 0.5 * kq / (qr * b.p);
+        pstarb += qrb * d;
+        bb.p -= qrb * d * p_star / b.p;
     }
     if (p_pvrs > 0.0) {
         const double D = ub - ua, Rs = 0.25 * (a.r + b.r), Cs = a.cz + b.cz;
@@ -399,12 +447,11 @@ ADJ_HD void flux_hllc_vjp(const Pr<NC> &a, const Pr<NC> &b, const double n[3], c
     const double vab = ka ? vkb : 0.0, wab = ka ? wkb : 0.0;
     const double vbbv = ka ? 0.0 : vkb, wbb = ka ? 0.0 : wkb;
     // rotated velocities
-    ab.u += uab * nt[0][0] + vab * nt[1][0] + wab * nt[2][0];
-    ab.v += uab * nt[0][1] + vab * nt[1][1] + wab * nt[2][1];
-    ab.w += uab * nt[0][2] + vab * nt[1][2] + wab * nt[2][2];
-    bb.u += ubb * nt[0][0] + vbbv * nt[1][0] + wbb * nt[2][0];
-    bb.v += ubb * nt[0][1] + vbbv * nt[1][1] + wbb * nt[2][1];
-    bb.w += ubb * nt[0][2] + vbbv * nt[1][2] + wbb * nt[2][2];
+    double da[3], db[3];
+    frame_out<AX>(nt, sn, uab, vab, wab, da);
+    frame_out<AX>(nt, sn, ubb, vbbv, wbb, db);
+    ab.u += da[0]; ab.v += da[1]; ab.w += da[2];
+    bb.u += db[0]; bb.v += db[1]; bb.w += db[2];
 }
 
 // Boundary types (values of CHARM_GPU_BND_*).
@@ -480,16 +527,18 @@ ADJ_HD void bnd_vjp(int type, const Pr<NC> &out, bool pressure_clamped, const do
 // Flux selector values (CHARM_GPU_FLUX_*).
 enum { kFluxLF = 0, kFluxGodunov = 1, kFluxHLLC = 2, kFluxCD = 3 };
 
-template <int NC>
+// AX >= 0: n = s e_AX (axis-aligned faces), the frame products with zeros
+// left out; AX < 0: any unit normal.
+template <int NC, int AX = -1>
 ADJ_HD void num_flux_vjp(int flux, const Pr<NC> &a, const Pr<NC> &b, const double n[3], const Gas &g,
                          const double *qb, PrBar<NC> &ab, PrBar<NC> &bb, double *q)
 {
-    if (flux == kFluxHLLC) flux_hllc_vjp<NC>(a, b, n, g, qb, ab, bb, q);
-    else flux_lf_vjp<NC>(a, b, n, flux == kFluxCD, qb, ab, bb, q);
+    if (flux == kFluxHLLC) flux_hllc_vjp<NC, AX>(a, b, n, g, qb, ab, bb, q);
+    else flux_lf_vjp<NC, AX>(a, b, n, flux == kFluxCD, qb, ab, bb, q);
 }
 
 // Interior point: (Ua, Ub) -> q; Uab/Ubb += (dq/dU)^T qb.
-template <int NC>
+template <int NC, int AX = -1>
 ADJ_HD void point_vjp(int flux, const double *Ua, const double *Ub, const double n[3], const Gas &g,
                       const double *qb, double *Uab, double *Ubb, double *q)
 {
@@ -499,13 +548,13 @@ ADJ_HD void point_vjp(int flux, const double *Ua, const double *Ub, const double
     PrBar<NC> ab, bb;
     zero<NC>(ab);
     zero<NC>(bb);
-    num_flux_vjp<NC>(flux, a, b, n, g, qb, ab, bb, q);
+    num_flux_vjp<NC, AX>(flux, a, b, n, g, qb, ab, bb, q);
     prim_vjp<NC>(Ua, a, g, ab, Uab);
     prim_vjp<NC>(Ub, b, g, bb, Ubb);
 }
 
 // Boundary point: U -> q(U, ghost(U)); Uab += (dq/dU)^T qb.
-template <int NC>
+template <int NC, int AX = -1>
 ADJ_HD void bpoint_vjp(int flux, int type, const double *par, const double *U, const double n[3], const Gas &g,
                        const double *qb, double *Uab, double *q)
 {
@@ -516,7 +565,7 @@ ADJ_HD void bpoint_vjp(int flux, int type, const double *par, const double *U, c
     PrBar<NC> ab, ob;
     zero<NC>(ab);
     zero<NC>(ob);
-    num_flux_vjp<NC>(flux, a, o, n, g, qb, ab, ob, q);
+    num_flux_vjp<NC, AX>(flux, a, o, n, g, qb, ab, ob, q);
     bnd_vjp<NC>(type, o, pc, n, g, ob, ab);
     prim_vjp<NC>(U, a, g, ab, Uab);
 }

@@ -84,6 +84,8 @@ struct charm_gpu_handle_s {
     double *d_adj_lam = nullptr, *d_adj_s = nullptr, *d_adj_acc = nullptr;   // [V][B][E] each
     double *d_adj_u1 = nullptr, *d_adj_u2 = nullptr, *d_adj_fin = nullptr;   // stage states, final state
     double *d_adj_psi = nullptr;                                              // [3][V][E] limiter scalings
+    double *d_adj_psi_all = nullptr;                                          // [steps][3][V][E]
+    size_t n_psi_all = 0;
     double *d_obj_part = nullptr;                                             // objective partial sums
     std::vector<double *> d_snap;                                             // checkpoints
     bool adj_valid = false;           // d_adj_lam holds dJ/du0 of the last adjoint run
@@ -121,7 +123,8 @@ void free_mesh(charm_gpu_handle_s *h)
     if (h->d_tile_slot) cudaFree(h->d_tile_slot);
     h->d_tile_fptr = h->d_tile_faces = h->d_tile_slot = nullptr;
     double **adj[] = {&h->d_adj_lam, &h->d_adj_s, &h->d_adj_acc, &h->d_adj_u1, &h->d_adj_u2, &h->d_adj_fin,
-                      &h->d_adj_psi, &h->d_obj_part};
+                      &h->d_adj_psi, &h->d_obj_part, &h->d_adj_psi_all};
+    h->n_psi_all = 0;
     for (double **q : adj) {
         if (*q) cudaFree(*q);
         *q = nullptr;

@@ -79,6 +79,21 @@ __device__ __forceinline__ void adj_interior(const MeshDev &m, const double *__r
             C[v] = w * (g0 * r0[v][1 + t] - g1 * r1[v][1 + t]);
         }
     }
+    const int64_t base = 2 * i;
+    {
+        // outside the support of the adjoint the trace is exactly zero, and so
+        // is the contribution (linear in q^): skip the face
+        bool live = false;
+#pragma unroll
+        for (int v = 0; v < V; v++) live |= (A[v] != 0.0) | (B[v] != 0.0) | (C[v] != 0.0);
+        if (!live) {
+#pragma unroll
+            for (int v = 0; v < V; v++)
+#pragma unroll
+                for (int k = 0; k < kNB; k++) store_pair<double>(slots, (int64_t) (v * kNB + k) * S + base, 0.0, 0.0);
+            return;
+        }
+    }
     const adj::Gas gas = adj_gas();
     double n[3] = {0.0, 0.0, 0.0};
     n[D] = 1.0;
@@ -100,14 +115,13 @@ __device__ __forceinline__ void adj_interior(const MeshDev &m, const double *__r
             qb[v] = A[v] + B[v] * ps + C[v] * pt;
             Uab[v] = Ubb[v] = 0.0;
         }
-        adj::point_vjp<NC>(FLUX, Ua, Ub, n, gas, qb, Uab, Ubb, nullptr);
+        adj::point_vjp<NC, D>(FLUX, Ua, Ub, n, gas, qb, Uab, Ubb, nullptr);
 #pragma unroll
         for (int v = 0; v < V; v++) {
             S0a[v] += Uab[v]; Ssa[v] += Uab[v] * ps; Sta[v] += Uab[v] * pt;
             S0b[v] += Ubb[v]; Ssb[v] += Ubb[v] * ps; Stb[v] += Ubb[v] * pt;
         }
     }
-    const int64_t base = 2 * i;
 #pragma unroll
     for (int v = 0; v < V; v++) {
         store_pair<double>(slots, (int64_t) (v * kNB + 0) * S + base, S0a[v], S0b[v]);
@@ -142,6 +156,19 @@ __device__ __forceinline__ void adj_boundary(const MeshDev &m, const double *__r
             C[v] = w * r[v][1 + t];
         }
     }
+    const int64_t slot = 2 * m.n_face + j;
+    {
+        bool live = false;
+#pragma unroll
+        for (int v = 0; v < V; v++) live |= (A[v] != 0.0) | (B[v] != 0.0) | (C[v] != 0.0);
+        if (!live) {
+#pragma unroll
+            for (int v = 0; v < V; v++)
+#pragma unroll
+                for (int k = 0; k < kNB; k++) slots[(int64_t) (v * kNB + k) * S + slot] = 0.0;
+            return;
+        }
+    }
     load_coef<double, V>(u, E, e, c);
     const adj::Gas gas = adj_gas();
     double n[3] = {0.0, 0.0, 0.0};
@@ -161,11 +188,10 @@ __device__ __forceinline__ void adj_boundary(const MeshDev &m, const double *__r
             qb[v] = A[v] + B[v] * ps + C[v] * pt;
             Ub[v] = 0.0;
         }
-        adj::bpoint_vjp<NC>(FLUX, type, par, U, n, gas, qb, Ub, nullptr);
+        adj::bpoint_vjp<NC, D>(FLUX, type, par, U, n, gas, qb, Ub, nullptr);
 #pragma unroll
         for (int v = 0; v < V; v++) { S0[v] += Ub[v]; Ss[v] += Ub[v] * ps; St[v] += Ub[v] * pt; }
     }
-    const int64_t slot = 2 * m.n_face + j;
 #pragma unroll
     for (int v = 0; v < V; v++) {
         slots[(int64_t) (v * kNB + 0) * S + slot] = S0[v];
@@ -244,11 +270,16 @@ adj_cell_kernel(MeshDev m, const double *__restrict__ u, const double *sh, doubl
         }
     }
     const bool grav = c_cfg.has_grav != 0;
+    bool live = false;   // r^ = 0: the volume term contributes exactly zero
+#pragma unroll
+    for (int v = 0; v < V; v++) live |= (a[0][v] != 0.0) | (a[1][v] != 0.0) | (a[2][v] != 0.0);
+#pragma unroll
+    for (int k = 0; k < kNB; k++) live |= grav && (grb[k] != 0.0);
     const adj::Gas gas = adj_gas();
     double c[V][kNB];
-    load_coef<double, V>(u, E, e, c);
+    if (live) load_coef<double, V>(u, E, e, c);
 #pragma unroll 1
-    for (int g = 0; g < 8; g++) {
+    for (int g = 0; g < (live ? 8 : 0); g++) {
         const double px = (g & 1) ? kGaussPhi : -kGaussPhi;
         const double py = (g & 2) ? kGaussPhi : -kGaussPhi;
         const double pz = (g & 4) ? kGaussPhi : -kGaussPhi;

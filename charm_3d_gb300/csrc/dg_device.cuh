@@ -315,31 +315,51 @@ __device__ void bnd_cond(int bid, const Prim<T, NC> &in, Prim<T, NC> &out, const
 // Output q = (qu, qv, qw, qe, qc_0..); flux from side 0 to side 1 along n.
 
 // charm_calc_flux_lf (:255-315).
-template <typename T, int NC>
+// Normal velocity v.n; for an axis-aligned normal n = s e_AX (AX >= 0) the
+// products with the zero components are left out (IEEE rules keep x * 0 in
+// the instruction stream otherwise).
+template <int AX, typename T>
+__device__ __forceinline__ T vdotn(T x, T y, T z, const T n[3])
+{
+    if constexpr (AX == 0) return x * n[0];
+    else if constexpr (AX == 1) return y * n[1];
+    else if constexpr (AX == 2) return z * n[2];
+    else return x * n[0] + y * n[1] + z * n[2];
+}
+
+// p n_j (the pressure term of component j of the flux)
+template <int AX, typename T>
+__device__ __forceinline__ T pn(T p, const T n[3], int j)
+{
+    if constexpr (AX >= 0) return (j == AX) ? p * n[AX] : T(0);
+    else return p * n[j];
+}
+
+template <typename T, int NC, int AX = -1>
 __device__ __forceinline__ void flux_lf(const Prim<T, NC> &a, const Prim<T, NC> &b, const T n[3], T *q)
 {
-    T vna = a.u * n[0] + a.v * n[1] + a.w * n[2];
-    T vnb = b.u * n[0] + b.v * n[1] + b.w * n[2];
+    T vna = vdotn<AX, T>(a.u, a.v, a.w, n);
+    T vnb = vdotn<AX, T>(b.u, b.v, b.w, n);
     T alpha = fmax(fabs(vna) + a.cz, fabs(vnb) + b.cz);
     T ha = T(0.5);
-    q[0] = ha * ((b.r * vnb * b.u + b.p * n[0]) + (a.r * vna * a.u + a.p * n[0]) - alpha * (b.r * b.u - a.r * a.u));
-    q[1] = ha * ((b.r * vnb * b.v + b.p * n[1]) + (a.r * vna * a.v + a.p * n[1]) - alpha * (b.r * b.v - a.r * a.v));
-    q[2] = ha * ((b.r * vnb * b.w + b.p * n[2]) + (a.r * vna * a.w + a.p * n[2]) - alpha * (b.r * b.w - a.r * a.w));
+    q[0] = ha * ((b.r * vnb * b.u + pn<AX, T>(b.p, n, 0)) + (a.r * vna * a.u + pn<AX, T>(a.p, n, 0)) - alpha * (b.r * b.u - a.r * a.u));
+    q[1] = ha * ((b.r * vnb * b.v + pn<AX, T>(b.p, n, 1)) + (a.r * vna * a.v + pn<AX, T>(a.p, n, 1)) - alpha * (b.r * b.v - a.r * a.v));
+    q[2] = ha * ((b.r * vnb * b.w + pn<AX, T>(b.p, n, 2)) + (a.r * vna * a.w + pn<AX, T>(a.p, n, 2)) - alpha * (b.r * b.w - a.r * a.w));
     q[3] = ha * (((b.r * b.e_tot + b.p) * vnb) + ((a.r * a.e_tot + a.p) * vna) - alpha * (b.r * b.e_tot - a.r * a.e_tot));
     for (int i = 0; i < NC; i++)
         q[4 + i] = ha * ((b.r * vnb * b.c[i]) + (a.r * vna * a.c[i]) - alpha * (b.r * b.c[i] - a.r * a.c[i]));
 }
 
 // charm_calc_flux_cd (:513-559).
-template <typename T, int NC>
+template <typename T, int NC, int AX = -1>
 __device__ __forceinline__ void flux_cd(const Prim<T, NC> &a, const Prim<T, NC> &b, const T n[3], T *q)
 {
-    T vna = a.u * n[0] + a.v * n[1] + a.w * n[2];
-    T vnb = b.u * n[0] + b.v * n[1] + b.w * n[2];
+    T vna = vdotn<AX, T>(a.u, a.v, a.w, n);
+    T vnb = vdotn<AX, T>(b.u, b.v, b.w, n);
     T ha = T(0.5);
-    q[0] = ha * ((b.r * vnb * b.u + b.p * n[0]) + (a.r * vna * a.u + a.p * n[0]));
-    q[1] = ha * ((b.r * vnb * b.v + b.p * n[1]) + (a.r * vna * a.v + a.p * n[1]));
-    q[2] = ha * ((b.r * vnb * b.w + b.p * n[2]) + (a.r * vna * a.w + a.p * n[2]));
+    q[0] = ha * ((b.r * vnb * b.u + pn<AX, T>(b.p, n, 0)) + (a.r * vna * a.u + pn<AX, T>(a.p, n, 0)));
+    q[1] = ha * ((b.r * vnb * b.v + pn<AX, T>(b.p, n, 1)) + (a.r * vna * a.v + pn<AX, T>(a.p, n, 1)));
+    q[2] = ha * ((b.r * vnb * b.w + pn<AX, T>(b.p, n, 2)) + (a.r * vna * a.w + pn<AX, T>(a.p, n, 2)));
     q[3] = ha * (((b.r * b.e_tot + b.p) * vnb) + ((a.r * a.e_tot + a.p) * vna));
     for (int i = 0; i < NC; i++) q[4 + i] = ha * ((b.r * b.c[i] * vnb) + (a.r * a.c[i] * vna));
 }
@@ -382,18 +402,47 @@ __device__ __forceinline__ T f_hllc_e(T uk, T fk, T sk, T ss, T pk, T rk, T vk, 
 
 // _charm_calc_flux_hllc_x_1 (:324-437) on states already in the normal frame
 // (u is the normal velocity), then rotated back (:505-509).
-template <typename T, int NC>
+// Velocities into the frame (rows nt[k]) and the flux back out of it.  For
+// n = s e_AX the frame of normal_frame is a signed permutation:
+//   AX 0: (s e0, s e1, e2);  AX 1: (s e1, -s e0, e2);  AX 2: (s e2, -s e1, e0)
+// and only the non-zero products are issued.
+template <int AX, typename T>
+__device__ __forceinline__ void frame_in(const T nt[3][3], T s, T x, T y, T z, T &un, T &u1, T &u2)
+{
+    if constexpr (AX == 0) { un = s * x; u1 = s * y; u2 = z; }
+    else if constexpr (AX == 1) { un = s * y; u1 = -s * x; u2 = z; }
+    else if constexpr (AX == 2) { un = s * z; u1 = -s * y; u2 = x; }
+    else {
+        un = x * nt[0][0] + y * nt[0][1] + z * nt[0][2];
+        u1 = x * nt[1][0] + y * nt[1][1] + z * nt[1][2];
+        u2 = x * nt[2][0] + y * nt[2][1] + z * nt[2][2];
+    }
+}
+
+template <int AX, typename T>
+__device__ __forceinline__ void frame_out(const T nt[3][3], T s, T fu, T fv, T fw, T *q)
+{
+    if constexpr (AX == 0) { q[0] = s * fu; q[1] = s * fv; q[2] = fw; }
+    else if constexpr (AX == 1) { q[1] = s * fu; q[0] = -s * fv; q[2] = fw; }
+    else if constexpr (AX == 2) { q[2] = s * fu; q[1] = -s * fv; q[0] = fw; }
+    else {
+        q[0] = fu * nt[0][0] + fv * nt[1][0] + fw * nt[2][0];
+        q[1] = fu * nt[0][1] + fv * nt[1][1] + fw * nt[2][1];
+        q[2] = fu * nt[0][2] + fv * nt[1][2] + fw * nt[2][2];
+    }
+}
+
+template <typename T, int NC, int AX = -1>
 __device__ void flux_hllc(const Prim<T, NC> &pa, const Prim<T, NC> &pb, const T n[3], T *q, unsigned *err)
 {
     T nt[3][3];
-    normal_frame<T>(n, nt);
+    T sn = T(1);
+    if constexpr (AX < 0) normal_frame<T>(n, nt);
+    else sn = n[AX];
     // velocities in the (n, t1, t2) frame
-    T ua = pa.u * nt[0][0] + pa.v * nt[0][1] + pa.w * nt[0][2];
-    T va = pa.u * nt[1][0] + pa.v * nt[1][1] + pa.w * nt[1][2];
-    T wa = pa.u * nt[2][0] + pa.v * nt[2][1] + pa.w * nt[2][2];
-    T ub = pb.u * nt[0][0] + pb.v * nt[0][1] + pb.w * nt[0][2];
-    T vb = pb.u * nt[1][0] + pb.v * nt[1][1] + pb.w * nt[1][2];
-    T wb = pb.u * nt[2][0] + pb.v * nt[2][1] + pb.w * nt[2][2];
+    T ua, va, wa, ub, vb, wb;
+    frame_in<AX, T>(nt, sn, pa.u, pa.v, pa.w, ua, va, wa);
+    frame_in<AX, T>(nt, sn, pb.u, pb.v, pb.w, ub, vb, wb);
 
     T p_pvrs = T(0.5) * (pa.p + pb.p) - T(0.5) * (ub - ua) * T(0.25) * (pa.r + pb.r) * (pa.cz + pb.cz);
     T p_star = (p_pvrs > T(0)) ? p_pvrs : T(0);
@@ -460,9 +509,7 @@ __device__ void flux_hllc(const Prim<T, NC> &pa, const Prim<T, NC> &pb, const T 
         q[3] = f_hllc_e<T>(pb.r * pb.e_tot, (pb.r * pb.e_tot + pb.p) * ub, sr, s_star, pb.p, pb.r, ub, inv);
         for (int i = 0; i < NC; i++) q[4 + i] = f_hllc_v<T>(pb.r * pb.c[i], pb.r * pb.c[i] * ub, sr, s_star, inv);
     }
-    q[0] = fu * nt[0][0] + fv * nt[1][0] + fw * nt[2][0];
-    q[1] = fu * nt[0][1] + fv * nt[1][1] + fw * nt[2][1];
-    q[2] = fu * nt[0][2] + fv * nt[1][2] + fw * nt[2][2];
+    frame_out<AX, T>(nt, sn, fu, fv, fw, q);
 }
 
 // rim_orig (:8-180): exact Riemann solver (Newton on the star pressure).
@@ -601,12 +648,12 @@ __device__ void flux_godunov(const Prim<T, NC> &pa, const Prim<T, NC> &pb, const
     for (int i = 0; i < NC; i++) q[4 + i] = qr * ((qr >= T(0)) ? pa.c[i] : pb.c[i]);
 }
 
-template <int FLUX, typename T, int NC>
+template <int FLUX, typename T, int NC, int AX = -1>
 __device__ __forceinline__ void num_flux(const Prim<T, NC> &a, const Prim<T, NC> &b, const T n[3], T *q, unsigned *err)
 {
-    if (FLUX == CHARM_GPU_FLUX_LF) flux_lf<T, NC>(a, b, n, q);
-    else if (FLUX == CHARM_GPU_FLUX_HLLC) flux_hllc<T, NC>(a, b, n, q, err);
-    else if (FLUX == CHARM_GPU_FLUX_CD) flux_cd<T, NC>(a, b, n, q);
+    if (FLUX == CHARM_GPU_FLUX_LF) flux_lf<T, NC, AX>(a, b, n, q);
+    else if (FLUX == CHARM_GPU_FLUX_HLLC) flux_hllc<T, NC, AX>(a, b, n, q, err);
+    else if (FLUX == CHARM_GPU_FLUX_CD) flux_cd<T, NC, AX>(a, b, n, q);
     else flux_godunov<T, NC>(a, b, n, q);
 }
 

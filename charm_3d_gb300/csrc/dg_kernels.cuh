@@ -171,7 +171,7 @@ __device__ __forceinline__ void interior_face(const MeshDev &m, const double *__
         cons_to_prim<T, NC>(U0, p0);
         cons_to_prim<T, NC>(U1, p1);
         T q[V];
-        num_flux<FLUX, T, NC>(p0, p1, n, q, err);
+        num_flux<FLUX, T, NC, D>(p0, p1, n, q, err);
 #pragma unroll
         for (int v = 0; v < V; v++) {
             S0[v] += q[v];
@@ -223,7 +223,7 @@ __device__ __forceinline__ void boundary_face(const MeshDev &m, const double *__
         cons_to_prim<T, NC>(U, pin);
         bnd_cond<T, NC>(bid, pin, pout, n);
         T q[V];
-        num_flux<FLUX, T, NC>(pin, pout, n, q, err);
+        num_flux<FLUX, T, NC, D>(pin, pout, n, q, err);
 #pragma unroll
         for (int v = 0; v < V; v++) {
             S0[v] += q[v];
@@ -702,7 +702,7 @@ __device__ __forceinline__ void owned_face(const float cl[4 + NC][kNB], const fl
         cons_to_prim<float, NC>(Ul, pl);
         cons_to_prim<float, NC>(Uu, pu);
         float q[V];
-        num_flux<FLUX, float, NC>(pl, pu, n, q, err);
+        num_flux<FLUX, float, NC, D>(pl, pu, n, q, err);
 #pragma unroll
         for (int v = 0; v < V; v++) {
             S0[v] += q[v];
@@ -748,7 +748,7 @@ __device__ __forceinline__ void owned_boundary(const MeshDev &m, const float c[4
         cons_to_prim<float, NC>(U, pin);
         bnd_cond<float, NC>(bid, pin, pout, n);
         float q[V];
-        num_flux<FLUX, float, NC>(pin, pout, n, q, err);
+        num_flux<FLUX, float, NC, D>(pin, pout, n, q, err);
 #pragma unroll
         for (int v = 0; v < V; v++) {
             S0[v] += q[v];
@@ -1199,7 +1199,7 @@ __device__ __forceinline__ void face_sums(const float cl[4 + NC][kNB], const flo
         cons_to_prim<float, NC>(Ul, pl);
         cons_to_prim<float, NC>(Uu, pu);
         float q[V];
-        num_flux<FLUX, float, NC>(pl, pu, n, q, err);
+        num_flux<FLUX, float, NC, D>(pl, pu, n, q, err);
 #pragma unroll
         for (int v = 0; v < V; v++) {
             S0[v] += q[v];
@@ -1258,7 +1258,7 @@ __device__ __forceinline__ void tile_boundary(const MeshDev &m, const float *s_u
         cons_to_prim<float, NC>(U, pin);
         bnd_cond<float, NC>(bid, pin, pout, n);
         float q[V];
-        num_flux<FLUX, float, NC>(pin, pout, n, q, err);
+        num_flux<FLUX, float, NC, D>(pin, pout, n, q, err);
 #pragma unroll
         for (int v = 0; v < V; v++) {
             S0[v] += q[v];

@@ -272,7 +272,9 @@ int charm_gpu_residual_adjoint(charm_gpu_handle_t h, const double *rbar, double 
  * or, when dJdu_final is not NULL, the linear functional with that gradient.
  * Step states are checkpointed in n_snapshots device buffers (the initial
  * state included) and recomputed by binomial checkpointing (Griewank's
- * revolve schedule), so any run length fits the memory given.  dJdu0 (may be
+ * revolve schedule), so any run length fits the memory given.  With
+ * n_snapshots >= 3 * n_steps (1 * n_steps for the forward-Euler model) every
+ * stage state is kept instead and nothing is recomputed (one forward sweep).  dJdu0 (may be
  * NULL: the gradient stays on the device for charm_gpu_refine_flags_adjoint)
  * receives dJ/du(0).  The handle ends at the final state, as after
  * charm_gpu_run(h, n_steps, 0). */

@@ -8,17 +8,35 @@ using namespace charm::adj;
 namespace {
 Gas gas_of(const double *g) { return Gas{g[0], g[1], g[2], g[3], g[4]}; }
 
+// the axis-aligned specialisations when n = +-e_d exactly, else the general frame
+int axis_of(const double *n)
+{
+    for (int d = 0; d < 3; d++)
+        if ((n[d] == 1.0 || n[d] == -1.0) && n[(d + 1) % 3] == 0.0 && n[(d + 2) % 3] == 0.0) return d;
+    return -1;
+}
+
 template <int NC>
 void point(int flux, const double *g, const double *Ua, const double *Ub, const double *n, const double *qb,
            double *Uab, double *Ubb, double *q)
 {
-    point_vjp<NC>(flux, Ua, Ub, n, gas_of(g), qb, Uab, Ubb, q);
+    switch (axis_of(n)) {
+    case 0: point_vjp<NC, 0>(flux, Ua, Ub, n, gas_of(g), qb, Uab, Ubb, q); break;
+    case 1: point_vjp<NC, 1>(flux, Ua, Ub, n, gas_of(g), qb, Uab, Ubb, q); break;
+    case 2: point_vjp<NC, 2>(flux, Ua, Ub, n, gas_of(g), qb, Uab, Ubb, q); break;
+    default: point_vjp<NC>(flux, Ua, Ub, n, gas_of(g), qb, Uab, Ubb, q); break;
+    }
 }
 template <int NC>
 void bpoint(int flux, int type, const double *par, const double *g, const double *U, const double *n,
             const double *qb, double *Uab, double *q)
 {
-    bpoint_vjp<NC>(flux, type, par, U, n, gas_of(g), qb, Uab, q);
+    switch (axis_of(n)) {
+    case 0: bpoint_vjp<NC, 0>(flux, type, par, U, n, gas_of(g), qb, Uab, q); break;
+    case 1: bpoint_vjp<NC, 1>(flux, type, par, U, n, gas_of(g), qb, Uab, q); break;
+    case 2: bpoint_vjp<NC, 2>(flux, type, par, U, n, gas_of(g), qb, Uab, q); break;
+    default: bpoint_vjp<NC>(flux, type, par, U, n, gas_of(g), qb, Uab, q); break;
+    }
 }
 template <int NC>
 void vpoint(const double *g, const double *U, const double *a, double *Uab)

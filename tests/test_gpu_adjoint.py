@@ -152,7 +152,7 @@ def _revolve_cost(n, s):
     return t * n - math.comb(s + 1 + t - 1, s + 1)
 
 
-@pytest.mark.parametrize("snaps", [1, 2, 3, 5, 40])
+@pytest.mark.parametrize("snaps", [1, 2, 3, 5, 40, 60])
 def test_checkpointing_schedule(snaps):
     case = small_case("vortex", "HLLC", "NONE", level=2)
     mesh, gpu, u0 = _setup(case)
@@ -164,9 +164,13 @@ def test_checkpointing_schedule(snaps):
     # the same arithmetic whatever the schedule
     assert np.array_equal(grad, ref_grad)
     assert info.J == ref_info.J
-    s = min(snaps, n)
-    assert info.forward_steps == _revolve_cost(n, s) + n
-    assert info.snapshots <= s
+    if snaps >= 3 * n:
+        # every stage state kept: one forward sweep, no recomputation
+        assert info.forward_steps == n and info.snapshots == 3 * n
+    else:
+        s = min(snaps, n)
+        assert info.forward_steps == _revolve_cost(n, s) + n
+        assert info.snapshots <= s
 
 
 def test_adjoint_leaves_final_state():
@@ -193,6 +197,21 @@ def test_adjoint_linear_functional():
         gpu.run(4, case.tau)
         Js.append(float((g * gpu.get_state()).sum()))
     assert _rel(float((grad * d).sum()), (Js[0] - Js[1]) / (2 * FD_EPS)) < FD_TOL
+
+
+@pytest.mark.parametrize("model", ["NS", "EULER"])
+def test_adjoint_limiter_schedules_agree(model):
+    """With the BJ limiter: the stored limiter scalings of the keep-everything
+    mode and the recomputed ones of the checkpointed mode give the same
+    gradient."""
+    case = small_case("vortex", "LF", "BJ", level=2, model=model)
+    mesh, gpu, u0 = _setup(case)
+    obj = Solver.pressure_box(*_box(case))
+    g1, _ = gpu.adjoint(6, 2, obj)
+    gpu.set_state(u0)
+    g2, info = gpu.adjoint(6, 18, obj)
+    assert info.forward_steps == 6
+    assert np.array_equal(g1, g2)
 
 
 def test_adjoint_limiter_frozen_runs():
