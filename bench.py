@@ -356,7 +356,7 @@ def run_adjoint(args, device: int) -> dict:
     t_adj = time.perf_counter() - t0
     # central differences along random density perturbations (variable rc_0, coefficient 0)
     rng = np.random.default_rng(2024)
-    eps = 1e-6
+    eps = args.adjoint_fd_eps
     # the same run with J over the whole box: no zero region of the adjoint to skip
     gpu.set_state(u0)
     gpu.sync()
@@ -447,6 +447,7 @@ def main():
     ap.add_argument("--adjoint-snapshots", type=int, default=0,
                     help="checkpoint buffers (0: every stage state of the run, 3 per step)")
     ap.add_argument("--adjoint-fd", type=int, default=16, help="finite-difference directions")
+    ap.add_argument("--adjoint-fd-eps", type=float, default=1e-6, help="central-difference step")
     ap.add_argument("--skip-e2e", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
