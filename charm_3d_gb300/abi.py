@@ -105,6 +105,7 @@ SIGNATURES = [
     ("charm_gpu_objective", C.c_int, [_P, C.POINTER(Objective), _DP, _P]),
     ("charm_gpu_residual_adjoint", C.c_int, [_P, _P, _P]),
     ("charm_gpu_adjoint", C.c_int, [_P, C.c_int, C.c_int, C.POINTER(Objective), _P, _P, C.POINTER(AdjointInfo)]),
+    ("charm_gpu_refine_flags_adjoint", C.c_int, [_P, C.c_double, _P, _P]),
     ("charm_host_forest_new", C.c_int, [C.POINTER(_P), _P, _P, _P, _P, C.c_int]),
     ("charm_host_forest_free", C.c_int, [_P]),
     ("charm_host_forest_count", C.c_int64, [_P]),

@@ -404,6 +404,53 @@ int charm_gpu_residual_adjoint(charm_gpu_handle_t h, const double *rbar, double 
     return charm_gpu_sync(h, 600.0);
 }
 
+int charm_gpu_refine_flags_adjoint(charm_gpu_handle_t h, double max_err, int8_t *flags, double *grad_out)
+{
+    int rc = check_ready(h);
+    if (rc) return rc;
+    if (!flags && !grad_out) return fail(CHARM_GPU_EINVAL, "null argument");
+    if (!h->adj_valid) return fail(CHARM_GPU_ESTATE, "no adjoint: call charm_gpu_adjoint first");
+    std::vector<double> grad((size_t) (3 * h->E)), w((size_t) h->E);
+    if ((rc = charm_gpu_refine_flags(h, max_err, nullptr, grad.data()))) return rc;
+    MeshDev m = mesh_view(h);
+    const int bs = 256;
+    TimedLaunch t;
+    begin_launch(h, 3, &t);
+    adj_weight_kernel<<<(unsigned) ((h->E + bs - 1) / bs), bs, 0, h->stream>>>(m, h->d_adj_lam, h->cfg.n_comp,
+                                                                               h->d_ub);
+    end_launch(h, &t);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(w.data(), h->d_ub, sizeof(double) * h->E, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    double mean = 0.0;
+    for (double x : w) mean += x;
+    mean /= (double) h->E;
+    // grad * sqrt(w / mean(w)): the reference criterion |grad|^2/12 V^(5/3) >
+    // max_err^2 V applied to this weighted gradient is the criterion scaled by
+    // the relative adjoint weight, so that charm_host_forest_adapt_state (the
+    // refine/coarsen callbacks) can take it unchanged
+    for (int64_t e = 0; e < h->E; e++) {
+        const double s = (mean > 0.0) ? sqrt(w[e] / mean) : 0.0;
+        for (int d = 0; d < 3; d++) grad[d * h->E + e] *= s;
+    }
+    if (grad_out) memcpy(grad_out, grad.data(), sizeof(double) * 3 * h->E);
+    if (flags) {
+        std::vector<int8_t> lev((size_t) h->E);
+        CUDA_TRY(cudaMemcpy(lev.data(), h->d_level, (size_t) h->E, cudaMemcpyDeviceToHost));
+        const double err2_max = max_err * max_err;
+        for (int64_t e = 0; e < h->E; e++) {
+            double hh[3];
+            for (int d = 0; d < 3; d++) hh[d] = ldexp(h->tree_len[d], -lev[e]);
+            const double vol = hh[0] * hh[1] * hh[2];
+            double diff2 = 0.0;
+            for (int d = 0; d < 3; d++) diff2 += grad[d * h->E + e] * grad[d * h->E + e];
+            const double err2 = diff2 * (1. / 12.) * exp(log(vol) * 5. / 3.);
+            flags[e] = (err2 > err2_max * vol) ? 1 : 0;
+        }
+    }
+    return CHARM_GPU_OK;
+}
+
 int charm_gpu_adjoint(charm_gpu_handle_t h, int n_steps, int n_snapshots, const charm_gpu_objective_t *obj,
                       const double *dJdu_final, double *dJdu0, charm_gpu_adjoint_info_t *info)
 {

@@ -415,4 +415,18 @@ adj_objective_kernel(MeshDev m, const double *__restrict__ u, double lo0, double
     if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
 }
 
+// Weight of the adjoint-weighted refinement indicator: |dJ/d(density mean)|
+// per unit volume, w[e] = |sum_i lam[rc_i][0][e]| / vol_e.
+__global__ void __launch_bounds__(256)
+adj_weight_kernel(MeshDev m, const double *__restrict__ lam, int n_comp, double *__restrict__ w)
+{
+    const int64_t e = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t E = m.n_elem;
+    if (e >= E) return;
+    double x = 0.0;
+    for (int i = 0; i < n_comp; i++) x += lam[(int64_t) ((4 + i) * kNB) * E + e];
+    const int lev = m.level[e];
+    w[e] = fabs(x) / (level_h(m, lev, 0) * level_h(m, lev, 1) * level_h(m, lev, 2));
+}
+
 }  // namespace charm

@@ -232,6 +232,14 @@ class Solver:
                   "charm_gpu_refine_flags")
         return flags, grad
 
+    def refine_flags_adjoint(self, max_err: float) -> tuple[np.ndarray, np.ndarray]:
+        """Adjoint-weighted refine flags and the weighted gradient [3][E] (after adjoint())."""
+        flags = np.empty(self.n_elem, np.int8)
+        grad = np.empty((3, self.n_elem))
+        abi.check(self.lib.charm_gpu_refine_flags_adjoint(self.h, max_err, flags.ctypes.data, grad.ctypes.data),
+                  "charm_gpu_refine_flags_adjoint")
+        return flags, grad
+
     def sync(self, timeout_s: float = 600.0) -> None:
         abi.check(self.lib.charm_gpu_sync(self.h, timeout_s), "charm_gpu_sync")
 

@@ -281,6 +281,17 @@ int charm_gpu_residual_adjoint(charm_gpu_handle_t h, const double *rbar, double 
 int charm_gpu_adjoint(charm_gpu_handle_t h, int n_steps, int n_snapshots, const charm_gpu_objective_t *obj,
                       const double *dJdu_final, double *dJdu0, charm_gpu_adjoint_info_t *info);
 
+/* Adjoint-weighted refinement indicator: the density-gradient estimate of
+ * charm_gpu_refine_flags scaled by sqrt(w_e / mean(w)), w_e = |dJ/d(density
+ * mean of e)| / V_e from the last charm_gpu_adjoint call, and the reference
+ * criterion applied to it (flags[e] = 1: refine).  grad_out ([3][E], may be
+ * NULL) receives the weighted gradient, which charm_host_forest_adapt_state
+ * takes in place of the plain one, so the octree's refine and coarsen
+ * callbacks follow the weighted criterion.  The gradient is that of the
+ * current state: set the state the adjoint started from to weight it at
+ * that time.  CHARM_GPU_ESTATE when no adjoint has been computed. */
+int charm_gpu_refine_flags_adjoint(charm_gpu_handle_t h, double max_err, int8_t *flags, double *grad_out);
+
 /* ---- host octree (the CPU side of the boundary) -------------------------- */
 
 typedef struct charm_host_forest_s *charm_host_forest_t;

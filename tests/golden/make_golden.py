@@ -21,7 +21,7 @@ sys.path.insert(0, ROOT)
 
 from charm_3d_gb300.solver import Forest  # noqa: E402
 from oracle.ref import RefSolver  # noqa: E402
-from tests.common import hanging_forest, small_case  # noqa: E402
+from tests.common import hanging_forest, pressure_box_J, small_case  # noqa: E402
 
 # name: (kind, flux, limiter, model, level, steps, hanging)
 FIXTURES = {
@@ -82,6 +82,36 @@ def point_fluxes() -> dict:
     return out
 
 
+ADJ_EPS = 1e-6
+ADJ_STEPS = 10
+
+
+def adjoint_fd() -> dict:
+    """Central differences of J = integral of p over the middle half of the
+    box after ADJ_STEPS steps of the reference (vortex, level 3, HLLC, no
+    limiter), along 4 seeded directions on the density mean of every element:
+    the finite-difference side of the adjoint check, through the reference."""
+    case = small_case("vortex", "HLLC", "NONE", level=3)
+    ref = RefSolver(case)
+    mesh = Forest(case).flatten()
+    u0 = case.initial_state(mesh.center)
+    lo = [o + 0.25 * b * t for o, b, t in zip(case.origin, case.brick, case.tree_len)]
+    hi = [o + 0.75 * b * t for o, b, t in zip(case.origin, case.brick, case.tree_len)]
+    rng = np.random.default_rng(77)
+    dirs = np.zeros((4,) + u0.shape)
+    dirs[:, 4, 0, :] = rng.uniform(-1.0, 1.0, (4, mesh.n_elem))
+
+    def J(u):
+        ref.set_state(u)
+        ref.run(ADJ_STEPS)
+        return pressure_box_J(case, mesh, ref.get_state(), lo, hi)
+
+    Jp = np.array([J(u0 + ADJ_EPS * d) for d in dirs])
+    Jm = np.array([J(u0 - ADJ_EPS * d) for d in dirs])
+    return {"u0": u0, "dirs": dirs, "Jp": Jp, "Jm": Jm, "J0": np.array(J(u0)), "eps": np.array(ADJ_EPS),
+            "steps": np.array(ADJ_STEPS), "lo": np.array(lo), "hi": np.array(hi)}
+
+
 def main() -> None:
     for name in FIXTURES:
         d = make(name)
@@ -89,6 +119,8 @@ def main() -> None:
         print(name, d["u0"].shape, "dt", float(d["dt"]))
     np.savez_compressed(os.path.join(HERE, "point_fluxes.npz"), **point_fluxes())
     print("point_fluxes")
+    np.savez_compressed(os.path.join(HERE, "adjoint_fd_vortex.npz"), **adjoint_fd())
+    print("adjoint_fd_vortex")
 
 
 if __name__ == "__main__":

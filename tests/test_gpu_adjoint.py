@@ -230,3 +230,54 @@ def test_adjoint_rejects_unsupported():
     mesh, gpu, u0 = _setup(case)
     with pytest.raises(CharmGpuError):
         gpu.adjoint(2, 1, Solver.pressure_box((0, 0, 0), (1, 1, 1)))
+
+
+def test_adjoint_matches_reference_fd_fixture():
+    """dJ/du0 from the GPU adjoint against central differences of the
+    reference's own solver (tests/golden/adjoint_fd_vortex.npz)."""
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "adjoint_fd_vortex.npz"))
+    case = small_case("vortex", "HLLC", "NONE", level=3)
+    mesh, gpu, u0 = _setup(case)
+    # the fixture's own initial state (libm exp may differ in the last bit across hosts)
+    assert np.allclose(u0, d["u0"], rtol=1e-13, atol=0.0)
+    u0 = d["u0"]
+    gpu.set_state(u0)
+    grad, info = gpu.adjoint(int(d["steps"]), 3 * int(d["steps"]), Solver.pressure_box(d["lo"], d["hi"]))
+    assert _rel(info.J, float(d["J0"])) < 1e-12
+    eps = float(d["eps"])
+    for k in range(d["dirs"].shape[0]):
+        fd = (d["Jp"][k] - d["Jm"][k]) / (2 * eps)
+        assert _rel(float((grad * d["dirs"][k]).sum()), fd) < FD_TOL, k
+
+
+def test_adjoint_weighted_refine_flags():
+    from charm_3d_gb300.abi import CharmGpuError
+    case = small_case("vortex", "HLLC", "NONE", level=4)
+    mesh, gpu, u0 = _setup(case)
+    with pytest.raises(CharmGpuError):
+        gpu.refine_flags_adjoint(0.01)            # no adjoint yet
+    lo, hi = (4.0, 4.0, 4.0), (6.0, 6.0, 6.0)
+    g, _ = gpu.adjoint(1, 3, Solver.pressure_box(lo, hi))
+    gpu.set_state(u0)
+    _, grad0 = gpu.refine_flags(1.0)
+    h = np.stack([np.asarray(mesh.tree_len[d]) * 2.0 ** (-mesh.level.astype(np.float64)) for d in range(3)])
+    vol = h[0] * h[1] * h[2]
+    w = np.abs(g[4:, 0, :].sum(axis=0)) / vol
+    want = grad0 * np.sqrt(w / w.mean())
+    # a threshold that flags about a fifth of the weighted leaves
+    crit = np.sqrt((want ** 2).sum(axis=0) / 12.0 * vol ** (5.0 / 3.0) / vol)
+    max_err = float(np.quantile(crit[crit > 0], 0.8))
+    flags, gw = gpu.refine_flags_adjoint(max_err)
+    assert np.allclose(gw, want, rtol=1e-13, atol=0.0)
+    err2 = (gw ** 2).sum(axis=0) / 12.0 * np.exp(np.log(vol) * 5.0 / 3.0)
+    assert np.array_equal(flags, (err2 > max_err ** 2 * vol).astype(np.int8))
+    assert flags.sum() > 0
+    assert flags[w == 0].sum() == 0 and (w == 0).any()   # outside the adjoint's support: never refined
+    # the weighted gradient drives the host octree's refine/coarsen callbacks:
+    # flagged leaves refined, families the objective does not see coarsened
+    forest = Forest(case)
+    u_new = forest.adapt_state(gw, max_err, case.level - 1, case.level + 1, case.n_comp, u0)
+    assert u_new.shape[2] == len(forest)
+    _, lv = forest.leaves()
+    assert (lv == case.level + 1).any() and (lv == case.level - 1).any()

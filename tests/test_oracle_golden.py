@@ -45,3 +45,30 @@ def test_oracle_point_fluxes_match_reference(flux):
     got = np.stack([port.point_flux(d["prim2"][i].ravel(), d["normals"][i]) for i in range(d["prim2"].shape[0])])
     want = d[flux]
     assert np.abs(got - want).max() <= 1e-13 * np.abs(want).max()
+
+
+def test_oracle_adjoint_fd_fixture():
+    """The oracle reproduces the reference's J(u0 +- eps d) of the adjoint
+    finite-difference fixture (so FD through the oracle is FD through the
+    reference)."""
+    from charm_3d_gb300.solver import Forest
+    from .common import pressure_box_J, small_case
+    d = np.load(os.path.join(GOLDEN, "adjoint_fd_vortex.npz"))
+    case = small_case("vortex", "HLLC", "NONE", level=3)
+    mesh = Forest(case).flatten()
+    assert np.allclose(case.initial_state(mesh.center), d["u0"], rtol=1e-13, atol=0.0)
+    u0 = d["u0"]
+    port = Port(case.config(), mesh)
+    n = int(d["steps"])
+
+    def J(u):
+        port.set_state(u)
+        port.run(n, case.tau)
+        return pressure_box_J(case, mesh, port.get_state(), d["lo"], d["hi"])
+
+    assert abs(J(u0) - float(d["J0"])) <= 1e-12 * abs(float(d["J0"]))
+    eps = float(d["eps"])
+    for k in range(2):
+        fd_port = (J(u0 + eps * d["dirs"][k]) - J(u0 - eps * d["dirs"][k])) / (2 * eps)
+        fd_ref = (d["Jp"][k] - d["Jm"][k]) / (2 * eps)
+        assert abs(fd_port - fd_ref) <= 1e-8 * abs(fd_ref)
