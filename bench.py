@@ -332,7 +332,8 @@ def run_adjoint(args, device: int) -> dict:
     u0 = case.initial_state(mesh.center)
     n = args.adjoint_steps
     snaps = args.adjoint_snapshots if args.adjoint_snapshots > 0 else 3 * n
-    obj = Solver.pressure_box((4.0, 4.0, 4.0), (6.0, 6.0, 6.0))
+    blo, bhi = (float(x) for x in args.adjoint_box.split(","))
+    obj = Solver.pressure_box((blo,) * 3, (bhi,) * 3)
     gpu = Solver(case, device)
     gpu.upload(mesh)
     gpu.set_state(u0)
@@ -377,7 +378,7 @@ def run_adjoint(args, device: int) -> dict:
         errs.append(abs(ad - fd) / max(abs(fd), 1e-300))
     gpu.close()
     return {"workload": f"vortex level {args.adjoint_level} ({mesh.n_elem} hex), HLLC, no limiter, FP64, "
-                        f"J = integral of p over [4,6]^3 at step {n}",
+                        f"J = integral of p over [{args.adjoint_box}]^3 at step {n}",
             "n_steps": n, "n_snapshots": snaps, "J": info.J, "J_forward": J_fwd,
             "forward_s": t_fwd, "adjoint_s": t_adj, "adjoint_over_forward": t_adj / t_fwd,
             "adjoint_whole_domain_J_over_forward": t_dense / t_fwd,
@@ -443,6 +444,7 @@ def main():
     ap.add_argument("--brick", type=int, default=1, help="trees along x (profiling sizes)")
     ap.add_argument("--only", default="both", choices=["both", "fp64", "mixed", "adjoint"])
     ap.add_argument("--adjoint-level", type=int, default=6)
+    ap.add_argument("--adjoint-box", default="4,6", help="J = integral of p over [lo,hi]^3 (lo,hi)")
     ap.add_argument("--adjoint-steps", type=int, default=200, help="0 skips the adjoint leg")
     ap.add_argument("--adjoint-snapshots", type=int, default=0,
                     help="checkpoint buffers (0: every stage state of the run, 3 per step)")
