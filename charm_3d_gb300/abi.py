@@ -46,12 +46,21 @@ class Bnd(C.Structure):
     _fields_ = [("type", C.c_int), ("params", C.c_double * (7 + MAX_COMP))]
 
 
+MAX_REACT = 8
+
+
+class Reaction(C.Structure):
+    _fields_ = [("left", C.c_int32 * 3), ("right", C.c_int32 * 3), ("a", C.c_double), ("e", C.c_double),
+                ("n", C.c_double)]
+
+
 class Config(C.Structure):
     _fields_ = [("model", C.c_int), ("flux", C.c_int), ("limiter", C.c_int), ("eos", C.c_int),
                 ("precision", C.c_int), ("dt_mode", C.c_int), ("n_comp", C.c_int),
                 ("comp", Comp * MAX_COMP), ("n_bnd", C.c_int), ("bnd", Bnd * MAX_BND),
                 ("grav", C.c_double * 3), ("tau", C.c_double), ("cfl", C.c_double), ("t_ref", C.c_double),
-                ("use_visc", C.c_int), ("check_every", C.c_int)]
+                ("use_visc", C.c_int), ("check_every", C.c_int), ("use_diff", C.c_int), ("n_react", C.c_int),
+                ("react", Reaction * MAX_REACT)]
 
 
 class Objective(C.Structure):

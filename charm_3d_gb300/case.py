@@ -45,6 +45,16 @@ class Component:
 
 
 @dc.dataclass
+class Reaction:
+    """One Arrhenius reaction, k = a T^n exp(-e / (T R)); components by index, -1 = none."""
+    left: tuple = (0, -1, -1)
+    right: tuple = (1, -1, -1)
+    a: float = 1.0e9
+    e: float = 15000.0 * GAS_R
+    n: float = 0.0
+
+
+@dc.dataclass
 class Boundary:
     name: str
     type: str = "BOUND_OUTLET"
@@ -82,6 +92,9 @@ class Case:
     steps: int = 10
     seed: int = 0
     init: str = "sod"          # initial-data generator name (see initial_state)
+    use_visc: int = 0
+    use_diff: int = 0
+    reactions: list = dc.field(default_factory=list)
     init_args: dict = dc.field(default_factory=dict)
 
     @property
@@ -119,7 +132,14 @@ class Case:
         for k in range(3):
             c.grav[k] = self.grav[k]
         c.tau, c.cfl, c.t_ref = self.tau, self.cfl, self.t_ref
-        c.use_visc = 0
+        c.use_visc = self.use_visc
+        c.use_diff = self.use_diff
+        c.n_react = len(self.reactions)
+        for i, r in enumerate(self.reactions):
+            for k in range(3):
+                c.react[i].left[k] = (list(r.left) + [-1, -1, -1])[k]
+                c.react[i].right[k] = (list(r.right) + [-1, -1, -1])[k]
+            c.react[i].a, c.react[i].e, c.react[i].n = r.a, r.e, r.n
         c.check_every = 0
         return c
 

@@ -165,6 +165,8 @@ int validate_config(const charm_gpu_config_t *c)
         if (c->bnd[b].type < 0 || c->bnd[b].type > CHARM_GPU_BND_MASS_FLOW)
             return fail(CHARM_GPU_EINVAL, "unknown boundary type");
     if (c->use_visc) return fail(CHARM_GPU_ENOTSUP, "viscous terms are not implemented on the GPU path");
+    if (c->n_react < 0 || c->n_react > CHARM_GPU_MAX_REACT) return fail(CHARM_GPU_EINVAL, "bad reaction count");
+    if (c->n_react) return fail(CHARM_GPU_ENOTSUP, "reactions are not implemented on the GPU path");
     if (c->dt_mode != CHARM_GPU_DT_TAU && c->dt_mode != CHARM_GPU_DT_CFL)
         return fail(CHARM_GPU_EINVAL, "unknown dt mode");
     return CHARM_GPU_OK;

@@ -260,6 +260,19 @@ int charm_model_gpu_config(charm_ctx_t *ctx, int precision, charm_gpu_config_t *
     cfg->cfl = ctx->CFL;
     cfg->t_ref = ctx->model.ns.t_ref;
     cfg->use_visc = ctx->model.ns.use_visc;
+    cfg->use_diff = ctx->model.ns.use_diff;
+    cfg->n_react = 0;
+    if (ctx->reactions) {   /* charm_reaction_t list of src/models/ns/charm_model_ns_init.cpp:58-77 */
+        if ((int) ctx->reactions->elem_count > CHARM_GPU_MAX_REACT) return CHARM_GPU_ENOTSUP;
+        cfg->n_react = (int) ctx->reactions->elem_count;
+        for (i = 0; i < cfg->n_react; i++) {
+            charm_reaction_t *r = (charm_reaction_t *) sc_array_index(ctx->reactions, i);
+            for (k = 0; k < 3; k++) { cfg->react[i].left[k] = r->left_comps[k]; cfg->react[i].right[k] = r->right_comps[k]; }
+            cfg->react[i].a = r->a;
+            cfg->react[i].e = r->e;
+            cfg->react[i].n = r->n;
+        }
+    }
     return CHARM_GPU_OK;
 }
 

@@ -95,6 +95,13 @@ typedef struct charm_gpu_bnd {       /* charm_bnd_t, include/charm_globals.h:441
     double params[7 + CHARM_GPU_MAX_COMP];
 } charm_gpu_bnd_t;
 
+#define CHARM_GPU_MAX_REACT  8    /* reactions (charm_ctx_t.reactions) */
+
+typedef struct charm_gpu_reaction {  /* charm_reaction_t, include/charm_globals.h:280-287 */
+    int32_t left[3], right[3];       /* component indices, -1 = none (always 3 entries) */
+    double  a, e, n;                 /* k = a * T^n * exp(-e / (T R)) */
+} charm_gpu_reaction_t;
+
 typedef struct charm_gpu_config {
     int    model, flux, limiter, eos, precision, dt_mode;
     int    n_comp;
@@ -105,8 +112,11 @@ typedef struct charm_gpu_config {
     double tau;          /* control.TAU */
     double cfl;          /* control.CFL */
     double t_ref;        /* control.MODEL.t_ref */
-    int    use_visc;     /* must be 0 on this path (viscous terms not implemented) */
+    int    use_visc;     /* MODEL.use_visc: viscous and heat-conduction terms (FP64 only) */
     int    check_every;  /* steps between device error-word checks (0 = only at sync) */
+    int    use_diff;     /* MODEL.use_diffusion: species diffusion (needs use_visc, >= 2 species) */
+    int    n_react;      /* reactions, evaluated per RK stage on cell means */
+    charm_gpu_reaction_t react[CHARM_GPU_MAX_REACT];
 } charm_gpu_config_t;
 
 /*

@@ -58,6 +58,9 @@ typedef struct oracle {
     int8_t *bface_face, *bface_bnd;
     double *u, *u_old, *res;        /* [V][B][E] */
     double *lim_nb;                 /* [E][6][V] limiter neighbour values */
+    double *vis;                    /* [E][9][NB] tau xx yy zz xy xz yz, q x y z (after A^-1) */
+    double *dif;                    /* [E][n_comp] species diffusion coefficients */
+    double *chem_rhs;               /* [E] chemical heat release of the stage */
 } oracle_t;
 
 /* ---- component laws and EOS --------------------------------------------- */
@@ -635,6 +638,10 @@ static void side1_center(const oracle_t *o, int64_t f, double c1[3])
     if (o->face_info[f] & 0x40) c1[d] = o->g[e0].c[d] + 0.5 * (o->g[e0].dh[d] + o->g[e1].dh[d]);
 }
 
+static void diffusion(oracle_t *o, const double *u);
+static void visc_grad(oracle_t *o, const double *u);
+static void visc_integrals(oracle_t *o, const double *u, double *res);
+
 /* ---- residual (src/models/ns/charm_model_ns_conv.c) ------------------------ */
 
 static void residual(oracle_t *o, const double *u, double *res)
@@ -642,6 +649,11 @@ static void residual(oracle_t *o, const double *u, double *res)
     const int64_t E = o->E;
     const int V = o->V;
     memset(res, 0, sizeof(double) * (size_t) V * NB * (size_t) E);
+    if (o->cfg.use_visc && o->cfg.model == CHARM_GPU_MODEL_NS) {   /* charm_model_ns_timestep_diff */
+        diffusion(o, u);
+        visc_grad(o, u);
+        visc_integrals(o, u, res);
+    }
     /* volume integrals (:23-89) */
     for (int64_t e = 0; e < E; e++) {
         const elem_geom_t *g = &o->g[e];
@@ -719,6 +731,422 @@ static void residual(oracle_t *o, const double *u, double *res)
                 double bfv = base_func(gp[q], k, g->c, g->dh) * gwj[q];
                 for (int v = 0; v < V; v++) res[(v * NB + k) * E + e] += qf[v] * bfv;
             }
+        }
+    }
+}
+
+/* ---- viscous terms (src/models/ns/charm_model_ns_diff*.c) ------------------ */
+
+static double comp_ml(const charm_gpu_comp_t *c, double t)
+{   /* charm_comp_calc_ml, src/charm_globals.c:651-662 */
+    if (c->ml_type == CHARM_GPU_LAW_SUTHERLAND) return c->ml0 * sqrt(pow(t / c->t0, 3)) * (c->t0 + c->ts) / (t + c->ts);
+    return c->ml0;
+}
+
+static double comp_kp(const charm_gpu_comp_t *c, double t)
+{   /* charm_comp_calc_kp, :665-676 */
+    if (c->kp_type == CHARM_GPU_LAW_SUTHERLAND) return c->kp0 * sqrt(pow(t / c->t0, 3)) * (c->t0 + c->ts) / (t + c->ts);
+    return c->kp0;
+}
+
+static double comp_h(const oracle_t *o, const charm_gpu_comp_t *c, double t)
+{   /* charm_comp_calc_enthalpy, :679-694: h0 + integral of the cp polynomial from t_ref */
+    double h = c->h0;
+    for (int i = 0; i < c->n_cp; i++) {
+        double t2 = pow(t, i + 1) / (i + 1), t1 = pow(o->cfg.t_ref, i + 1) / (i + 1);
+        h += c->cp[i] * (t2 - t1);
+    }
+    return h;
+}
+
+static double visc_mu(const oracle_t *o, const prim_t *p)
+{   /* charm_get_visc_mu, src/charm_globals.c:515-538 (molar-fraction weighted) */
+    double s = 0., mu = 0.;
+    for (int i = 0; i < o->cfg.n_comp; i++) {
+        double cm = p->c[i] / o->cfg.comp[i].m;
+        s += cm;
+        mu += cm * comp_ml(&o->cfg.comp[i], p->t);
+    }
+    return mu / s;
+}
+
+static double heat_k(const oracle_t *o, const prim_t *p)
+{   /* charm_get_heat_k, :541-558 */
+    double kt = 0.;
+    for (int i = 0; i < o->cfg.n_comp; i++) kt += p->c[i] * comp_kp(&o->cfg.comp[i], p->t);
+    return kt;
+}
+
+static void prim_at(const oracle_t *o, const double *u, int64_t e, const double c[3], const double *x, prim_t *p)
+{
+    double U[MAXV];
+    get_fields(o, u, e, c, o->g[e].dh, x, U);
+    cons_to_prim(o, U, p);
+}
+
+/* tau (6) and q (3) of element e at x from the lifted coefficients
+ * (charm_get_visc_tau / charm_get_heat_q, src/charm_base_func.c:343-373) */
+static void vis_at(const oracle_t *o, int64_t e, const double c[3], const double *x, double t[9])
+{
+    for (int f = 0; f < 9; f++) {
+        t[f] = 0.;
+        for (int k = 0; k < NB; k++) t[f] += o->vis[(e * 9 + f) * NB + k] * base_func(x, k, c, o->g[e].dh);
+    }
+}
+
+static void diffusion(oracle_t *o, const double *u)
+{   /* _charm_model_ns_timestep_diffusion_quad_iter_fn, src/models/ns/charm_model_ns_diff.c:18-71 */
+    const int nc = o->cfg.n_comp;
+    if (nc < 2) return;
+    for (int64_t e = 0; e < o->E; e++) {
+        prim_t p;
+        double x[CHARM_GPU_MAX_COMP], s = 0.;
+        prim_at(o, u, e, o->g[e].c, o->g[e].c, &p);
+        double pabs = p.p / 101325.0;
+        for (int i = 0; i < nc; i++) o->dif[e * nc + i] = 0.;
+        if (!o->cfg.use_diff) continue;
+        for (int i = 0; i < nc; i++) { x[i] = p.c[i] / o->cfg.comp[i].m; s += x[i]; }
+        for (int i = 0; i < nc; i++) x[i] /= s;
+        for (int i = 0; i < nc; i++) {
+            if (fabs(p.c[i] - 1.) <= EPS) { o->dif[e * nc + i] = 0.; continue; }
+            const charm_gpu_comp_t *ci = &o->cfg.comp[i];
+            double s_xd = 0.;
+            for (int j = 0; j < nc; j++) {
+                const charm_gpu_comp_t *cj = &o->cfg.comp[j];
+                double td = p.t / sqrt(ci->ek * cj->ek);
+                double wd = 1.06036 / pow(td, 0.1561) + 0.1930 / exp(0.47635 * td) + 1.03587 / exp(1.52996 * td) +
+                            1.76474 / exp(3.89411 * td);
+                double dij = (2.628e-7) * sqrt(0.5 * (1.0 / (1000.0 * ci->m) + 1.0 / (1000.0 * cj->m))) *
+                             sqrt(p.t * p.t * p.t) / (pabs * pow((0.5 * (ci->sig + cj->sig)), 2.0) * wd);
+                s_xd += i == j ? 0. : x[j] / dij;
+            }
+            o->dif[e * nc + i] = (1. - x[i]) / s_xd;
+        }
+    }
+}
+
+/* one face point of the lifting: the central values -> q[9] (tau xx yy zz xy
+ * xz yz, heat x y z) as in src/models/ns/charm_model_ns_diff_grad.c:150-176, 266-305 */
+static void grad_face_q(const oracle_t *o, double mu, double kt, double fr, double ft, double fu, double fv,
+                        double fw, const double *fc, const double *dm, const double n[3], double q[9])
+{
+    const double lambda = 0.;   /* charm_get_visc_lambda, src/charm_globals.c:509-512 */
+    const double lp = (lambda + 4. * mu / 3.), lm = (lambda - 2. * mu / 3.);
+    q[0] = lp * fu * n[0] + lm * fv * n[1] + lm * fw * n[2];
+    q[1] = lm * fu * n[0] + lp * fv * n[1] + lm * fw * n[2];
+    q[2] = lm * fu * n[0] + lm * fv * n[1] + lp * fw * n[2];
+    q[3] = mu * (fu * n[1] + fv * n[0]);
+    q[4] = mu * (fw * n[0] + fu * n[2]);
+    q[5] = mu * (fw * n[1] + fv * n[2]);
+    q[6] = kt * ft * n[0];
+    q[7] = kt * ft * n[1];
+    q[8] = kt * ft * n[2];
+    for (int i = 0; i < o->cfg.n_comp; i++) {
+        double h = comp_h(o, &o->cfg.comp[i], ft);
+        q[6] += h * fr * dm[i] * fc[i] * n[0];
+        q[7] += h * fr * dm[i] * fc[i] * n[1];
+        q[8] += h * fr * dm[i] * fc[i] * n[2];
+    }
+}
+
+static void grad_add(oracle_t *o, double *acc, int64_t e, const double q[9], double bfv, int k)
+{
+    for (int f = 0; f < 6; f++) acc[(e * 9 + f) * NB + k] += q[f] * bfv;
+    for (int f = 6; f < 9; f++) acc[(e * 9 + f) * NB + k] -= q[f] * bfv;
+}
+
+/* charm_model_ns_timestep_diff_grad (src/models/ns/charm_model_ns_diff_grad.c) */
+static void visc_grad(oracle_t *o, const double *u)
+{
+    const int64_t E = o->E;
+    const int nc = o->cfg.n_comp;
+    double *acc = (double *) calloc((size_t) E * 9 * NB, sizeof(double));
+    /* volume (:21-77) */
+    for (int64_t e = 0; e < E; e++) {
+        const elem_geom_t *g = &o->g[e];
+        for (int q = 0; q < NQ; q++) {
+            const double *x = g->qgp[q];
+            prim_t p;
+            prim_at(o, u, e, g->c, x, &p);
+            const double kt = heat_k(o, &p), lambda = 0., mu = visc_mu(o, &p);
+            const double lp = (lambda + 4. * mu / 3.), lm = (lambda - 2. * mu / 3.);
+            for (int k = 0; k < NB; k++) {
+                const double px = base_func_d(k, 0, g->dh) * g->qgj[q], py = base_func_d(k, 1, g->dh) * g->qgj[q],
+                             pz = base_func_d(k, 2, g->dh) * g->qgj[q];
+                double *a = &acc[e * 9 * NB];
+                a[0 * NB + k] -= (lp * p.u * px + lm * p.v * py + lm * p.w * pz);
+                a[1 * NB + k] -= (lm * p.u * px + lp * p.v * py + lm * p.w * pz);
+                a[2 * NB + k] -= (lm * p.u * px + lm * p.v * py + lp * p.w * pz);
+                a[3 * NB + k] -= mu * (p.u * py + p.v * px);
+                a[4 * NB + k] -= mu * (p.w * px + p.u * pz);
+                a[5 * NB + k] -= mu * (p.w * py + p.v * pz);
+                double tqx = kt * p.t * px, tqy = kt * p.t * py, tqz = kt * p.t * pz;
+                for (int i = 0; i < nc; i++) {
+                    double h = comp_h(o, &o->cfg.comp[i], p.t);
+                    tqx += h * p.r * o->dif[e * nc + i] * p.c[i] * px;
+                    tqy += h * p.r * o->dif[e * nc + i] * p.c[i] * py;
+                    tqz += h * p.r * o->dif[e * nc + i] * p.c[i] * pz;
+                }
+                a[6 * NB + k] += tqx;
+                a[7 * NB + k] += tqy;
+                a[8 * NB + k] += tqz;
+            }
+        }
+    }
+    /* interior faces, conforming and hanging (:194-450) */
+    for (int64_t f = 0; f < o->F; f++) {
+        const int32_t e[2] = {o->face_elem[f], o->face_elem[o->F + f]};
+        const int d = o->face_info[f] & 3, kind = (o->face_info[f] >> 2) & 3;
+        double c1[3];
+        side1_center(o, f, c1);
+        const double *cs[2] = {o->g[e[0]].c, c1};
+        const int hs = (kind == 2) ? 1 : 0;
+        elem_geom_t pg = o->g[e[hs]];
+        memcpy(pg.c, cs[hs], sizeof(double) * 3);
+        double gp[NFQ][3], gwj[NFQ], n[3];
+        face_points(&pg, hs ? 2 * d : 2 * d + 1, gp, gwj);
+        outward_normal(2 * d + 1, n);
+        for (int q = 0; q < NFQ; q++) {
+            prim_t pr[2];
+            double mu[2], kt = 0.;
+            for (int s = 0; s < 2; s++) {
+                prim_at(o, u, e[s], cs[s], gp[q], &pr[s]);
+                mu[s] = visc_mu(o, &pr[s]);
+                kt += heat_k(o, &pr[s]);
+            }
+            const double fmu = 0.5 * (mu[0] + mu[1]);
+            kt *= 0.5;
+            double fc[CHARM_GPU_MAX_COMP], dm[CHARM_GPU_MAX_COMP];
+            for (int i = 0; i < nc; i++) {
+                fc[i] = (pr[0].c[i] + pr[1].c[i]) * 0.5;
+                dm[i] = (o->dif[e[0] * nc + i] + o->dif[e[1] * nc + i]) * 0.5;
+            }
+            double qq[9];
+            grad_face_q(o, fmu, kt, (pr[0].r + pr[1].r) * 0.5, (pr[0].t + pr[1].t) * 0.5, (pr[0].u + pr[1].u) * 0.5,
+                        (pr[0].v + pr[1].v) * 0.5, (pr[0].w + pr[1].w) * 0.5, fc, dm, n, qq);
+            for (int k = 0; k < NB; k++)
+                for (int s = 0; s < 2; s++) {
+                    double bfv = (s ? -1. : 1.) * base_func(gp[q], k, cs[s], o->g[e[s]].dh) * gwj[q];
+                    grad_add(o, acc, e[s], qq, bfv, k);
+                }
+        }
+    }
+    /* boundary faces (:83-180) */
+    for (int64_t j = 0; j < o->Fb; j++) {
+        const int32_t e = o->bface_elem[j];
+        const int f = o->bface_face[j], bid = o->bface_bnd[j];
+        const elem_geom_t *g = &o->g[e];
+        double gp[NFQ][3], gwj[NFQ], n[3];
+        face_points(g, f, gp, gwj);
+        outward_normal(f, n);
+        const int noslip = o->cfg.bnd[bid].type == CHARM_GPU_BND_WALL_NO_SLIP;
+        for (int q = 0; q < NFQ; q++) {
+            prim_t pr[2];
+            prim_at(o, u, e, g->c, gp[q], &pr[0]);
+            const double mu = visc_mu(o, &pr[0]), kt = heat_k(o, &pr[0]);
+            bnd_cond(o, bid, &pr[0], &pr[1], n);
+            double fu, fv, fw, ft;
+            if (noslip) { fu = fv = fw = 0.; ft = o->cfg.bnd[bid].params[0]; }
+            else {
+                fu = (pr[0].u + pr[1].u) * 0.5; fv = (pr[0].v + pr[1].v) * 0.5;
+                fw = (pr[0].w + pr[1].w) * 0.5; ft = (pr[0].t + pr[1].t) * 0.5;
+            }
+            double fc[CHARM_GPU_MAX_COMP];
+            for (int i = 0; i < nc; i++) fc[i] = (pr[0].c[i] + pr[1].c[i]) * 0.5;
+            double qq[9];
+            grad_face_q(o, mu, kt, (pr[0].r + pr[1].r) * 0.5, ft, fu, fv, fw, fc, &o->dif[e * nc], n, qq);
+            for (int k = 0; k < NB; k++) grad_add(o, acc, e, qq, base_func(gp[q], k, g->c, g->dh) * gwj[q], k);
+        }
+    }
+    /* A^-1 (_charm_model_ns_diff_grad_update_quad_iter_fn, :462-476) */
+    for (int64_t e = 0; e < E; e++)
+        for (int f = 0; f < 9; f++)
+            for (int i = 0; i < NB; i++) {
+                double r = 0.;
+                for (int k = 0; k < NB; k++) r += o->g[e].a_inv[i][k] * acc[(e * 9 + f) * NB + k];
+                o->vis[(e * 9 + f) * NB + i] = r;
+            }
+    free(acc);
+}
+
+/* charm_model_ns_timestep_diff_integrals (src/models/ns/charm_model_ns_diff_integrals.c) */
+static void visc_integrals(oracle_t *o, const double *u, double *res)
+{
+    const int64_t E = o->E;
+    /* volume (:21-55) */
+    for (int64_t e = 0; e < E; e++) {
+        const elem_geom_t *g = &o->g[e];
+        for (int q = 0; q < NQ; q++) {
+            const double *x = g->qgp[q];
+            prim_t p;
+            double t[9];
+            prim_at(o, u, e, g->c, x, &p);
+            vis_at(o, e, g->c, x, t);
+            for (int k = 0; k < NB; k++) {
+                const double px = base_func_d(k, 0, g->dh) * g->qgj[q], py = base_func_d(k, 1, g->dh) * g->qgj[q],
+                             pz = base_func_d(k, 2, g->dh) * g->qgj[q], phi = base_func(x, k, g->c, g->dh) * g->qgj[q];
+                res[(0 * NB + k) * E + e] += (t[0] * px + t[3] * py + t[4] * pz);
+                res[(1 * NB + k) * E + e] += (t[3] * px + t[1] * py + t[5] * pz);
+                res[(2 * NB + k) * E + e] += (t[4] * px + t[5] * py + t[2] * pz);
+                double *re = &res[(3 * NB + k) * E + e];
+                *re += (t[0] * p.u + t[3] * p.v + t[4] * p.w) * px;
+                *re += (t[3] * p.u + t[1] * p.v + t[5] * p.w) * py;
+                *re += (t[4] * p.u + t[5] * p.v + t[2] * p.w) * pz;
+                *re += o->chem_rhs[e] * phi;
+            }
+        }
+    }
+    /* interior faces (:200-392) */
+    for (int64_t f = 0; f < o->F; f++) {
+        const int32_t e[2] = {o->face_elem[f], o->face_elem[o->F + f]};
+        const int d = o->face_info[f] & 3, kind = (o->face_info[f] >> 2) & 3;
+        double c1[3];
+        side1_center(o, f, c1);
+        const double *cs[2] = {o->g[e[0]].c, c1};
+        const int hs = (kind == 2) ? 1 : 0;
+        elem_geom_t pg = o->g[e[hs]];
+        memcpy(pg.c, cs[hs], sizeof(double) * 3);
+        double gp[NFQ][3], gwj[NFQ], n[3];
+        face_points(&pg, hs ? 2 * d : 2 * d + 1, gp, gwj);
+        outward_normal(2 * d + 1, n);
+        for (int q = 0; q < NFQ; q++) {
+            double ft6[6] = {0., 0., 0., 0., 0., 0.}, fu = 0., fv = 0., fw = 0., ft = 0.;
+            for (int s = 0; s < 2; s++) {
+                prim_t p;
+                double t[9];
+                prim_at(o, u, e[s], cs[s], gp[q], &p);
+                vis_at(o, e[s], cs[s], gp[q], t);
+                for (int c = 0; c < 6; c++) ft6[c] += t[c];
+                fu += p.u * t[0] + p.v * t[3] + p.w * t[4];
+                fv += p.u * t[3] + p.v * t[1] + p.w * t[5];
+                fw += p.u * t[4] + p.v * t[5] + p.w * t[2];
+                ft += t[6] * n[0] + t[7] * n[1] + t[8] * n[2];
+            }
+            for (int c = 0; c < 6; c++) ft6[c] *= 0.5;
+            fu *= 0.5; fv *= 0.5; fw *= 0.5; ft *= 0.5;
+            const double qu = ft6[0] * n[0] + ft6[3] * n[1] + ft6[4] * n[2];
+            const double qv = ft6[3] * n[0] + ft6[1] * n[1] + ft6[5] * n[2];
+            const double qw = ft6[4] * n[0] + ft6[5] * n[1] + ft6[2] * n[2];
+            const double qe = fu * n[0] + fv * n[1] + fw * n[2] - ft;
+            for (int k = 0; k < NB; k++)
+                for (int s = 0; s < 2; s++) {
+                    double bfv = (s ? -1. : 1.) * base_func(gp[q], k, cs[s], o->g[e[s]].dh) * gwj[q];
+                    res[(0 * NB + k) * E + e[s]] -= qu * bfv;
+                    res[(1 * NB + k) * E + e[s]] -= qv * bfv;
+                    res[(2 * NB + k) * E + e[s]] -= qw * bfv;
+                    res[(3 * NB + k) * E + e[s]] -= qe * bfv;
+                }
+        }
+    }
+    /* no-slip walls: one point at the face centre (:58-126) */
+    for (int64_t j = 0; j < o->Fb; j++) {
+        const int bid = o->bface_bnd[j];
+        if (o->cfg.bnd[bid].type != CHARM_GPU_BND_WALL_NO_SLIP) continue;
+        const int32_t e = o->bface_elem[j];
+        const int f = o->bface_face[j], dd = f / 2;
+        const elem_geom_t *g = &o->g[e];
+        double n[3], x[3], U[MAXV], t[9];
+        outward_normal(f, n);
+        memcpy(x, g->c, sizeof(x));
+        x[dd] += ((f & 1) ? 0.5 : -0.5) * g->dh[dd];
+        const double area = g->dh[(dd + 1) % 3] * g->dh[(dd + 2) % 3];
+        prim_t px, pr[2];
+        prim_at(o, u, e, g->c, x, &px);
+        const double mu = visc_mu(o, &px);
+        get_fields_avg(o, u, e, U);
+        cons_to_prim(o, U, &pr[0]);
+        vis_at(o, e, g->c, x, t);
+        bnd_cond(o, bid, &pr[0], &pr[1], n);
+        const double vv[3] = {pr[0].u, pr[0].v, pr[0].w};
+        const double un = vv[0] * n[0] + vv[1] * n[1] + vv[2] * n[2];
+        const double vt[3] = {vv[0] - un * n[0], vv[1] - un * n[1], vv[2] - un * n[2]};
+        const double ll = 0.5 * g->dh[dd];
+        const double qu = -mu * vt[0] / ll, qv = -mu * vt[1] / ll, qw = -mu * vt[2] / ll;
+        const double qe = -t[6] * n[0] - t[7] * n[1] - t[8] * n[2];
+        for (int k = 0; k < NB; k++) {
+            double bfv = base_func(x, k, g->c, g->dh) * 1. * area;
+            res[(0 * NB + k) * E + e] -= qu * bfv;
+            res[(1 * NB + k) * E + e] -= qv * bfv;
+            res[(2 * NB + k) * E + e] -= qw * bfv;
+            res[(3 * NB + k) * E + e] -= qe * bfv;
+        }
+    }
+}
+
+/* ---- chemistry on cell means (src/models/ns/charm_model_ns_chem.c) --------- */
+
+/* _charm_model_ns_chem_rhs (:18-63): rates at concentrations cc -> phi, psi */
+static void chem_rates(const oracle_t *o, double t, const double *cc, double *k, double *w, double *phi, double *psi)
+{
+    const int nr = o->cfg.n_react, nc = o->cfg.n_comp;
+    for (int n = 0; n < nr; n++) {
+        const charm_gpu_reaction_t *r = &o->cfg.react[n];
+        k[n] = r->a * pow(t, r->n) * exp(-r->e / t / gR);
+        w[n] = k[n];
+        for (int m = 0; m < 3; m++) { int i = r->left[m]; w[n] *= (i < 0 ? 1. : cc[i]); }
+    }
+    if (!phi) return;
+    for (int i = 0; i < nc; i++) {
+        phi[i] = 0.;
+        psi[i] = 0.;
+        for (int n = 0; n < nr; n++) {
+            const charm_gpu_reaction_t *r = &o->cfg.react[n];
+            for (int m = 0; m < 3; m++) {
+                if (i == r->left[m]) {
+                    double x = k[n];
+                    for (int j = 1; j < 3; j++) { int ic = r->left[(m + j) % 3]; x *= (ic < 0 ? 1. : cc[ic]); }
+                    phi[i] += x;
+                }
+                if (i == r->right[m]) psi[i] += w[n];
+            }
+        }
+    }
+}
+
+/* _charm_model_ns_chem_iter_fn (:111-156): two semi-implicit passes on the
+ * molar concentrations of the cell mean, dt = the configured TAU (not the
+ * stage dt, as in the reference); the species coefficients are replaced by
+ * their new means (higher moments zeroed) and chem_rhs keeps the heat release
+ * (_charm_model_ns_chem_rhs_save, :66-108, including its w -= chem_w[i]). */
+static void chemistry(oracle_t *o, double *u)
+{
+    const int nc = o->cfg.n_comp, nr = o->cfg.n_react;
+    const int64_t E = o->E;
+    const double dt = o->cfg.tau;
+    for (int64_t e = 0; e < E; e++) {
+        o->chem_rhs[e] = 0.;
+        if (!nr) continue;
+        double U[MAXV], c[CHARM_GPU_MAX_COMP], ch[CHARM_GPU_MAX_COMP], c_[CHARM_GPU_MAX_COMP];
+        double k[CHARM_GPU_MAX_REACT], w[CHARM_GPU_MAX_REACT], phi[CHARM_GPU_MAX_COMP], psi[CHARM_GPU_MAX_COMP];
+        prim_t p;
+        get_fields_avg(o, u, e, U);
+        cons_to_prim(o, U, &p);
+        for (int i = 0; i < nc; i++) { c[i] = U[4 + i] / o->cfg.comp[i].m; ch[i] = c[i]; }
+        for (int j = 0; j < 2; j++) {
+            for (int i = 0; i < nc; i++) c_[i] = (ch[i] + c[i]) * 0.5;
+            chem_rates(o, p.t, c_, k, w, phi, psi);
+            for (int i = 0; i < nc; i++) {
+                ch[i] = (c[i] + dt * psi[i] * (1. + dt * phi[i] * 0.5));
+                ch[i] /= (1. + dt * phi[i] + (dt * phi[i]) * (dt * phi[i]) * 0.5);
+            }
+        }
+        chem_rates(o, p.t, ch, k, w, NULL, NULL);
+        double rhs = 0.;
+        for (int i = 0; i < nc; i++) {
+            double ww = 0.;
+            for (int n = 0; n < nr; n++) {
+                const charm_gpu_reaction_t *r = &o->cfg.react[n];
+                for (int m = 0; m < 3; m++) {
+                    if (i == r->left[m]) ww -= w[i];   /* indexed by species, as the reference */
+                    if (i == r->right[m]) ww += w[n];
+                }
+            }
+            rhs += ww * comp_h(o, &o->cfg.comp[i], p.t);
+        }
+        o->chem_rhs[e] = rhs;
+        for (int i = 0; i < nc; i++) {
+            for (int kk = 0; kk < NB; kk++) u[((4 + i) * NB + kk) * E + e] = 0.;
+            u[((4 + i) * NB) * E + e] = ch[i] * o->cfg.comp[i].m;
         }
     }
 }
@@ -827,7 +1255,7 @@ void oracle_free(oracle_t *o)
 {
     if (!o) return;
     free(o->g); free(o->face_elem); free(o->face_info); free(o->bface_elem); free(o->bface_face); free(o->bface_bnd);
-    free(o->u); free(o->u_old); free(o->res); free(o->lim_nb);
+    free(o->u); free(o->u_old); free(o->res); free(o->lim_nb); free(o->vis); free(o->dif); free(o->chem_rhs);
     free(o);
 }
 
@@ -849,8 +1277,11 @@ oracle_t *oracle_new(const charm_gpu_config_t *cfg, const charm_gpu_mesh_t *m)
     o->u_old = (double *) calloc(1, st);
     o->res = (double *) calloc(1, st);
     o->lim_nb = (double *) calloc((size_t) o->E * 6 * (size_t) o->V, sizeof(double));
+    o->vis = (double *) calloc((size_t) o->E * 9 * NB, sizeof(double));
+    o->dif = (double *) calloc((size_t) o->E * (size_t) cfg->n_comp, sizeof(double));
+    o->chem_rhs = (double *) calloc((size_t) o->E, sizeof(double));
     if (!o->g || !o->face_elem || !o->face_info || !o->bface_elem || !o->bface_face || !o->bface_bnd || !o->u ||
-        !o->u_old || !o->res || !o->lim_nb) {
+        !o->u_old || !o->res || !o->lim_nb || !o->vis || !o->dif || !o->chem_rhs) {
         oracle_free(o);
         return NULL;
     }
@@ -881,6 +1312,7 @@ int oracle_get_state(oracle_t *o, double *u)
 
 int oracle_residual(oracle_t *o, double *res)
 {
+    memset(o->chem_rhs, 0, sizeof(double) * (size_t) o->E);   /* no chemistry outside a step */
     residual(o, o->u, res);
     return 0;
 }
@@ -904,6 +1336,7 @@ int oracle_step(oracle_t *o, double dt)
     }
     memcpy(o->u_old, o->u, sizeof(double) * n);             /* rk_0 (:119-133) */
     for (int s = 0; s < 3; s++) {
+        chemistry(o, o->u);                                   /* charm_model_ns_timestep_chem */
         residual(o, o->u, o->res);
         update(o, o->u, o->res, dt);
         if (lim) limiter(o, o->u);

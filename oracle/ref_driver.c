@@ -92,6 +92,7 @@ static void free_case(void)
     }
     if (g_ctx.mat) sc_array_destroy(g_ctx.mat);
     if (g_ctx.reg) sc_array_destroy(g_ctx.reg);
+    if (g_ctx.reactions) sc_array_destroy(g_ctx.reactions);
     free(g_ctx.msh);
     memset(&g_ctx, 0, sizeof(g_ctx));
 }
@@ -177,6 +178,16 @@ int ref_setup(const charm_gpu_config_t *cfg, const int32_t brick[3], const int32
     }
     ctx->msh = (charm_mesh_info_t *) calloc(1, sizeof(charm_mesh_info_t));
     ctx->reactions = NULL;
+    if (cfg->n_react > 0) {   /* src/models/ns/charm_model_ns_init.cpp:15-77 */
+        ctx->reactions = sc_array_new(sizeof(charm_reaction_t));
+        for (i = 0; i < cfg->n_react; i++) {
+            charm_reaction_t *r = (charm_reaction_t *) sc_array_push(ctx->reactions);
+            for (k = 0; k < 3; k++) { r->left_comps[k] = cfg->react[i].left[k]; r->right_comps[k] = cfg->react[i].right[k]; }
+            r->a = cfg->react[i].a;
+            r->e = cfg->react[i].e;
+            r->n = cfg->react[i].n;
+        }
+    }
     /* control (:352-413) */
     switch (cfg->flux) {
     case CHARM_GPU_FLUX_LF: ctx->flux_fn = charm_calc_flux_lf; break;
@@ -196,7 +207,7 @@ int ref_setup(const charm_gpu_config_t *cfg, const int32_t brick[3], const int32
     ctx->CFL = cfg->cfl;
     ctx->time = 1.0e300;
     ctx->model.ns.use_visc = cfg->use_visc;
-    ctx->model.ns.use_diff = 0;
+    ctx->model.ns.use_diff = cfg->use_diff;
     ctx->model.ns.t_ref = cfg->t_ref;
     if (cfg->model == CHARM_GPU_MODEL_EULER) {
         ctx->get_dt_fn = charm_model_euler_get_dt;
@@ -243,6 +254,11 @@ int ref_set_state(const double *u)
     for (i = 0; i < E; i++) {
         charm_data_t *d = (charm_data_t *) charm_shim_quad(g_p4est, i)->p.user_data;
         memset(&d->par.c, 0, sizeof(d->par.c));
+        /* model fields start at zero, as after the initial fill: with fewer
+         * than 2 species the diffusion coefficients are never written
+         * (src/models/ns/charm_model_ns_diff.c:74-76), and leaves made by
+         * refinement would otherwise keep whatever their memory held */
+        memset(&d->par.model.ns, 0, sizeof(d->par.model.ns));
         for (k = 0; k < B; k++) {
             d->par.c.ru[k] = u[(0 * B + k) * E + i];
             d->par.c.rv[k] = u[(1 * B + k) * E + i];
@@ -300,6 +316,8 @@ int ref_run(int nsteps, double *dt_out)
 
 /* Residual int_* of the current state (zero + volume/face integrals,
  * src/models/ns/charm_model.c:248-252). */
+void charm_model_ns_timestep_diff(p4est_t *p4est, p4est_ghost_t *ghost, charm_data_t *ghost_data);
+
 int ref_residual(double *res)
 {
     int64_t E = charm_shim_count(g_p4est), i;
@@ -313,7 +331,11 @@ int ref_residual(double *res)
         memset(d->int_rw, 0, sizeof(d->int_rw));
         memset(d->int_re, 0, sizeof(d->int_re));
         memset(d->int_rc, 0, sizeof(d->int_rc));
+        d->par.model.ns.chem_rhs = 0.;
     }
+    p4est_ghost_exchange_data(g_p4est, g_ghost, g_ghost_data);
+    /* the order of charm_model_ns_timestep_single's stage (src/models/ns/charm_model.c:248-251) */
+    charm_model_ns_timestep_diff(g_p4est, g_ghost, g_ghost_data);
     charm_model_ns_timestep_conv(g_p4est, g_ghost, g_ghost_data);
     for (i = 0; i < E; i++) {
         charm_data_t *d = (charm_data_t *) charm_shim_quad(g_p4est, i)->p.user_data;

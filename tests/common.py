@@ -3,7 +3,8 @@ from __future__ import annotations
 
 import numpy as np
 
-from charm_3d_gb300 import Boundary, Case, Component, synthetic
+from charm_3d_gb300 import Boundary, Case, Component, Reaction, synthetic
+from charm_3d_gb300.case import GAS_R
 from charm_3d_gb300.solver import Forest
 
 
@@ -43,11 +44,37 @@ def small_case(kind: str, flux: str = "LF", limiter: str = "BJ", level: int = 3,
         c.seed = 5
         c.eos = "MIX"
         c.components = [Component("A", m=0.02869409, cp=(1014.16,)), Component("B", m=0.018, cp=(1850.0,))]
+    elif kind in ("visc", "visc_walls", "visc2", "react"):
+        # viscous / reacting unit cases on dimensionless states (T ~ 3.5e-3):
+        # constant transport laws large enough to matter next to the fluxes
+        c = synthetic("sod", level=level)
+        c.init = "random"
+        c.seed = {"visc": 13, "visc_walls": 17, "visc2": 19, "react": 23}[kind]
+        c.use_visc = 1
+        if kind == "visc_walls":
+            T_in = 1.0 * 0.02869409 / (1.0 * 8.31446261815324)
+            c.boundaries = [Boundary("IN", "BOUND_INLET", (0.3, 0.0, 0.0, T_in, 1.0)),
+                            Boundary("OUT", "BOUND_OUTLET"),
+                            Boundary("SLIP", "BOUND_WALL_SLIP"),
+                            Boundary("NOSLIP", "BOUND_WALL_NO_SLIP", (T_in,))]
+            c.bnd_of_side = (0, 1, 2, 2, 3, 2)
+        if kind in ("visc2", "react"):
+            c.eos = "MIX"
+            c.components = [Component("A", m=0.02869409, cp=(1014.16,), h0=2.0e6, sig=3.62, ek=97.0),
+                            Component("B", m=0.018, cp=(1850.0,), sig=2.64, ek=809.1)]
+            c.use_diff = 1
+        if kind == "react":
+            # rates and heat release scaled to the dimensionless state
+            c.t_ref = 0.0
+            c.components[0].h0 = 1.0
+            c.reactions = [Reaction(left=(0, -1, -1), right=(1, -1, -1), a=4.0, e=2.0e-3 * GAS_R, n=0.5)]
+        for comp in c.components:
+            comp.ml0, comp.kp0 = 0.02, 0.03
     else:
         raise ValueError(kind)
     c.flux, c.limiter, c.model = flux, limiter, model
     c.steps = 3
-    if kind in ("random", "walls", "mix2"):
+    if kind in ("random", "walls", "mix2", "visc", "visc_walls", "visc2", "react"):
         # random slopes and no limiter: keep the step well inside p1 DG's CFL limit
         c.tau = 0.1 * (1.0 / 2 ** level) / 1.5
     return c
