@@ -15,6 +15,8 @@ int adj_check(charm_gpu_handle_s *h)
         if (h->cfg.bnd[b].type == CHARM_GPU_BND_MASS_FLOW)
             return fail(CHARM_GPU_ENOTSUP, "adjoint: MASS_FLOW boundary not supported");
     if (h->cfg.n_comp < 1 || h->cfg.n_comp > 2) return fail(CHARM_GPU_ENOTSUP, "species count not instantiated");
+    if (h->cfg.model == CHARM_GPU_MODEL_NS && (h->cfg.use_visc || h->cfg.n_react))
+        return fail(CHARM_GPU_ENOTSUP, "adjoint: viscous terms and reactions not supported");
     return CHARM_GPU_OK;
 }
 

@@ -25,6 +25,7 @@
 #include "charm_gpu.h"
 #include "dg_kernels.cuh"
 #include "dg_adjoint.cuh"
+#include "dg_visc.cuh"
 
 using namespace charm;
 
@@ -89,6 +90,13 @@ struct charm_gpu_handle_s {
     double *d_obj_part = nullptr;                                             // objective partial sums
     std::vector<double *> d_snap;                                             // checkpoints
     bool adj_valid = false;           // d_adj_lam holds dJ/du0 of the last adjoint run
+    // viscous terms and chemistry (NS model, FP64)
+    double *d_s9 = nullptr;            // lifting face terms [9*B][S]
+    double *d_vis = nullptr;           // lifted tau and q [9][B][E]
+    double *d_radd = nullptr;          // viscous volume terms [4][B][E]
+    double *d_dif = nullptr;           // species diffusion coefficients [n_comp][E]
+    double *d_uc = nullptr;            // stage state after chemistry [V][B][E]
+    double *d_chem_rhs = nullptr;      // heat release of the stage [E]
     double *d_dt = nullptr;            // CFL step (bits as unsigned long long)
     unsigned *d_err = nullptr;
     bool mesh_ready = false;
@@ -131,6 +139,11 @@ void free_mesh(charm_gpu_handle_s *h)
     }
     for (double *q : h->d_snap) cudaFree(q);
     h->d_snap.clear();
+    double **visc[] = {&h->d_s9, &h->d_vis, &h->d_radd, &h->d_dif, &h->d_uc, &h->d_chem_rhs};
+    for (double **q : visc) {
+        if (*q) cudaFree(*q);
+        *q = nullptr;
+    }
     h->adj_valid = false;
     h->n_tiles = 0;
     h->tile_smem = 0;
@@ -164,9 +177,14 @@ int validate_config(const charm_gpu_config_t *c)
     for (int b = 0; b < c->n_bnd; b++)
         if (c->bnd[b].type < 0 || c->bnd[b].type > CHARM_GPU_BND_MASS_FLOW)
             return fail(CHARM_GPU_EINVAL, "unknown boundary type");
-    if (c->use_visc) return fail(CHARM_GPU_ENOTSUP, "viscous terms are not implemented on the GPU path");
     if (c->n_react < 0 || c->n_react > CHARM_GPU_MAX_REACT) return fail(CHARM_GPU_EINVAL, "bad reaction count");
-    if (c->n_react) return fail(CHARM_GPU_ENOTSUP, "reactions are not implemented on the GPU path");
+    for (int r = 0; r < c->n_react; r++)
+        for (int k = 0; k < 3; k++)
+            if (c->react[r].left[k] < -1 || c->react[r].left[k] >= c->n_comp || c->react[r].right[k] < -1 ||
+                c->react[r].right[k] >= c->n_comp)
+                return fail(CHARM_GPU_EINVAL, "reaction component index out of range");
+    if ((c->use_visc || c->n_react) && c->precision != CHARM_GPU_PREC_FP64)
+        return fail(CHARM_GPU_ENOTSUP, "viscous terms and reactions: FP64 precision only");
     if (c->dt_mode != CHARM_GPU_DT_TAU && c->dt_mode != CHARM_GPU_DT_CFL)
         return fail(CHARM_GPU_EINVAL, "unknown dt mode");
     return CHARM_GPU_OK;
@@ -214,6 +232,21 @@ void build_devcfg(const charm_gpu_config_t *c, DevCfg *d)
     for (int b = 0; b < CHARM_GPU_MAX_BND; b++)
         for (int k = 0; k < 7 + CHARM_GPU_MAX_COMP; k++) d->bnd_par_f[b][k] = (float) d->bnd_par[b][k];
     for (int a = 0; a < 3; a++) d->grav_f[a] = (float) d->grav[a];
+    d->use_visc = c->use_visc;
+    d->use_diff = c->use_diff;
+    d->n_react = c->n_react;
+    d->t_ref = c->t_ref;
+    d->tau = c->tau;
+    for (int i = 0; i < c->n_comp; i++) {
+        d->comp_ml0[i] = c->comp[i].ml0; d->comp_kp0[i] = c->comp[i].kp0;
+        d->comp_t0[i] = c->comp[i].t0; d->comp_ts[i] = c->comp[i].ts;
+        d->comp_sig[i] = c->comp[i].sig; d->comp_ek[i] = c->comp[i].ek; d->comp_h0[i] = c->comp[i].h0;
+        d->comp_kp_type[i] = c->comp[i].kp_type;
+    }
+    for (int r = 0; r < c->n_react; r++) {
+        for (int k = 0; k < 3; k++) { d->react_l[r][k] = c->react[r].left[k]; d->react_r[r][k] = c->react[r].right[k]; }
+        d->react_a[r] = c->react[r].a; d->react_e[r] = c->react[r].e; d->react_n[r] = c->react[r].n;
+    }
 }
 
 int ensure_cfg(charm_gpu_handle_s *h)
@@ -320,7 +353,7 @@ int launch_face(charm_gpu_handle_s *h, const double *u)
 
 template <typename T, int NC>
 int launch_cell(charm_gpu_handle_s *h, const double *u, const double *u0, double *out, double dt,
-                const double *dt_dev, double a_new, double a_old, int mode)
+                const double *dt_dev, double a_new, double a_old, int mode, const double *radd = nullptr)
 {
     MeshDev m = mesh_view(h);
     const int bs = 128;
@@ -328,7 +361,7 @@ int launch_cell(charm_gpu_handle_s *h, const double *u, const double *u0, double
     TimedLaunch t;
     begin_launch(h, 1, &t);
     cell_kernel<T, NC><<<(unsigned) nb, bs, 0, h->stream>>>(m, u, static_cast<const T *>(h->d_slots), u0, out, dt,
-                                                            dt_dev, a_new, a_old, mode, h->d_err);
+                                                            dt_dev, a_new, a_old, mode, h->d_err, radd);
     end_launch(h, &t);
     CUDA_TRY(cudaGetLastError());
     return CHARM_GPU_OK;
@@ -366,18 +399,93 @@ int launch_cfl(charm_gpu_handle_s *h, const double *u)
 }
 
 // One stage: out = a_new*L(u - dt*M^-1*R(u)) + a_old*u0 (L = limiter or identity).
+// ---- viscous terms and chemistry (charm_model_ns_timestep_single's stage,
+//      src/models/ns/charm_model.c:242-253: chem, diff, conv, update) -------
+
+bool has_visc_chem(const charm_gpu_handle_s *h)
+{
+    return h->cfg.model == CHARM_GPU_MODEL_NS && (h->cfg.use_visc || h->cfg.n_react);
+}
+
+// chemistry of the stage state u -> h->d_uc (when there are reactions)
+template <int NC>
+int launch_chem(charm_gpu_handle_s *h, const double *u)
+{
+    MeshDev m = mesh_view(h);
+    const int bs = 128;
+    TimedLaunch t;
+    begin_launch(h, 3, &t);
+    chem_kernel<NC><<<(unsigned) ((h->E + bs - 1) / bs), bs, 0, h->stream>>>(m, u, h->d_uc, h->d_chem_rhs);
+    end_launch(h, &t);
+    CUDA_TRY(cudaGetLastError());
+    return CHARM_GPU_OK;
+}
+
+// diffusion coefficients, lifting and the viscous volume terms of u
+template <int NC>
+int launch_visc(charm_gpu_handle_s *h, const double *u, const double *chem_rhs)
+{
+    MeshDev m = mesh_view(h);
+    const int bs = 128;
+    const int64_t nbe = (h->E + bs - 1) / bs;
+    const int64_t nbi = (h->F + bs - 1) / bs, nbb = (h->Fb + bs - 1) / bs;
+    TimedLaunch t;
+    begin_launch(h, 3, &t);
+    if (h->cfg.use_diff && NC >= 2)
+        diffcoef_kernel<NC><<<(unsigned) nbe, bs, 0, h->stream>>>(m, u, h->d_dif);
+    if (nbi + nbb) vgrad_face_kernel<NC><<<(unsigned) (nbi + nbb), bs, 0, h->stream>>>(m, u, h->d_dif, h->d_s9, nbi);
+    vgrad_cell_kernel<NC><<<(unsigned) nbe, bs, 0, h->stream>>>(m, u, h->d_dif, h->d_s9, h->d_vis);
+    vvol_kernel<NC><<<(unsigned) nbe, bs, 0, h->stream>>>(m, u, h->d_vis, chem_rhs, h->d_radd);
+    end_launch(h, &t);
+    CUDA_TRY(cudaGetLastError());
+    return CHARM_GPU_OK;
+}
+
+// viscous face fluxes, added into the convective slots (after launch_face)
+template <int NC>
+int launch_vflux(charm_gpu_handle_s *h, const double *u)
+{
+    MeshDev m = mesh_view(h);
+    const int bs = 128;
+    const int64_t nbi = (h->F + bs - 1) / bs, nbb = (h->Fb + bs - 1) / bs;
+    if (nbi + nbb == 0) return CHARM_GPU_OK;
+    TimedLaunch t;
+    begin_launch(h, 0, &t);
+    vflux_face_kernel<NC><<<(unsigned) (nbi + nbb), bs, 0, h->stream>>>(m, u, h->d_vis,
+                                                                       static_cast<double *>(h->d_slots), nbi);
+    end_launch(h, &t);
+    CUDA_TRY(cudaGetLastError());
+    return CHARM_GPU_OK;
+}
+
 template <typename T, int NC>
 int stage(charm_gpu_handle_s *h, const double *u, const double *u0, double *out, double dt, const double *dt_dev,
           double a_new, double a_old)
 {
-    int rc = launch_face<T, NC>(h, u);
+    int rc;
+    const double *radd = nullptr;
+    if constexpr (sizeof(T) == sizeof(double)) {
+        if (has_visc_chem(h)) {
+            if (h->cfg.n_react) {
+                if ((rc = launch_chem<NC>(h, u))) return rc;
+                u = h->d_uc;   // the residual and the update act on the state after chemistry
+            }
+            if (h->cfg.use_visc) {
+                if ((rc = launch_visc<NC>(h, u, h->d_chem_rhs))) return rc;
+                radd = h->d_radd;
+            }
+        }
+    }
+    rc = launch_face<T, NC>(h, u);
     if (rc) return rc;
+    if constexpr (sizeof(T) == sizeof(double))
+        if (radd && (rc = launch_vflux<NC>(h, u))) return rc;
     if (h->cfg.limiter == CHARM_GPU_LIM_BJ) {
-        rc = launch_cell<T, NC>(h, u, nullptr, h->d_ua, dt, dt_dev, 1.0, 0.0, kCellUpdate);
+        rc = launch_cell<T, NC>(h, u, nullptr, h->d_ua, dt, dt_dev, 1.0, 0.0, kCellUpdate, radd);
         if (rc) return rc;
         return launch_limit<NC>(h, h->d_ua, u0, out, a_new, a_old);
     }
-    return launch_cell<T, NC>(h, u, u0, out, dt, dt_dev, a_new, a_old, kCellUpdate);
+    return launch_cell<T, NC>(h, u, u0, out, dt, dt_dev, a_new, a_old, kCellUpdate, radd);
 }
 
 template <typename T, int NC>
@@ -745,6 +853,18 @@ int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh)
     CUDA_TRY(cudaMalloc(&h->d_ua, st));
     CUDA_TRY(cudaMalloc(&h->d_ub, st));
     CUDA_TRY(cudaMalloc(&h->d_slots, sl));
+    if (h->cfg.model == CHARM_GPU_MODEL_NS && (h->cfg.use_visc || h->cfg.n_react)) {
+        CUDA_TRY(cudaMalloc(&h->d_chem_rhs, sizeof(double) * E));
+        CUDA_TRY(cudaMemset(h->d_chem_rhs, 0, sizeof(double) * E));
+        if (h->cfg.n_react) CUDA_TRY(cudaMalloc(&h->d_uc, st));
+        if (h->cfg.use_visc) {
+            CUDA_TRY(cudaMalloc(&h->d_s9, sizeof(double) * 9 * CHARM_GPU_BASIS * S));
+            CUDA_TRY(cudaMalloc(&h->d_vis, sizeof(double) * 9 * CHARM_GPU_BASIS * E));
+            CUDA_TRY(cudaMalloc(&h->d_radd, sizeof(double) * 4 * CHARM_GPU_BASIS * E));
+            CUDA_TRY(cudaMalloc(&h->d_dif, sizeof(double) * V * E));
+            CUDA_TRY(cudaMemset(h->d_dif, 0, sizeof(double) * V * E));
+        }
+    }
     if (h->cfg.precision == CHARM_GPU_PREC_MIXED) {
         for (int k = 0; k < 3; k++) {
             CUDA_TRY(cudaMalloc(&h->d_fh[k], st / 2));
@@ -921,7 +1041,21 @@ int charm_gpu_residual(charm_gpu_handle_t h, double *res, int on_device)
     if (!res) return fail(CHARM_GPU_EINVAL, "null argument");
     const bool mixed = h->cfg.precision == CHARM_GPU_PREC_MIXED;
     if (mixed && (rc = ff_convert(h, false))) return rc;   // d_u <- hi + lo
-    switch (h->cfg.n_comp * 2 + (mixed ? 1 : 0)) {
+    if (!mixed && h->cfg.model == CHARM_GPU_MODEL_NS && h->cfg.use_visc) {
+        // with the viscous terms (no chemistry outside a step: chem_rhs = 0)
+        switch (h->cfg.n_comp) {
+        case 1:
+            if (!(rc = launch_visc<1>(h, h->d_u, nullptr)) && !(rc = launch_face<double, 1>(h, h->d_u)) &&
+                !(rc = launch_vflux<1>(h, h->d_u)))
+                rc = launch_cell<double, 1>(h, h->d_u, nullptr, h->d_ua, 0, nullptr, 1, 0, kCellResidual, h->d_radd);
+            break;
+        default:
+            if (!(rc = launch_visc<2>(h, h->d_u, nullptr)) && !(rc = launch_face<double, 2>(h, h->d_u)) &&
+                !(rc = launch_vflux<2>(h, h->d_u)))
+                rc = launch_cell<double, 2>(h, h->d_u, nullptr, h->d_ua, 0, nullptr, 1, 0, kCellResidual, h->d_radd);
+            break;
+        }
+    } else switch (h->cfg.n_comp * 2 + (mixed ? 1 : 0)) {
     case 2: rc = launch_face<double, 1>(h, h->d_u); if (!rc) rc = launch_cell<double, 1>(h, h->d_u, nullptr, h->d_ua, 0, nullptr, 1, 0, kCellResidual); break;
     case 3: rc = launch_face<float, 1>(h, h->d_u); if (!rc) rc = launch_cell<float, 1>(h, h->d_u, nullptr, h->d_ua, 0, nullptr, 1, 0, kCellResidual); break;
     case 4: rc = launch_face<double, 2>(h, h->d_u); if (!rc) rc = launch_cell<double, 2>(h, h->d_u, nullptr, h->d_ua, 0, nullptr, 1, 0, kCellResidual); break;

@@ -54,6 +54,14 @@ struct DevCfg {
     float  comp_cp_f[kMaxComp][kMaxCp];
     float  bnd_par_f[kMaxBnd][7 + kMaxComp];
     float  grav_f[3];
+    // viscous terms and chemistry (FP64 path)
+    int    use_visc, use_diff, n_react;
+    double t_ref, tau;
+    double comp_ml0[kMaxComp], comp_kp0[kMaxComp], comp_t0[kMaxComp], comp_ts[kMaxComp];
+    double comp_sig[kMaxComp], comp_ek[kMaxComp], comp_h0[kMaxComp];
+    int    comp_kp_type[kMaxComp];
+    int    react_l[CHARM_GPU_MAX_REACT][3], react_r[CHARM_GPU_MAX_REACT][3];
+    double react_a[CHARM_GPU_MAX_REACT], react_e[CHARM_GPU_MAX_REACT], react_n[CHARM_GPU_MAX_REACT];
 };
 
 __constant__ DevCfg c_cfg;

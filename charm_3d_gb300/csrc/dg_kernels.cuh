@@ -286,7 +286,7 @@ template <typename T, int NC>
 __global__ void __launch_bounds__(128)
 cell_kernel(MeshDev m, const double *__restrict__ u, const T *__restrict__ slots, const double *u0,
             double *out, double dt, const double *__restrict__ dt_dev, double a_new, double a_old,
-            int mode, unsigned *err)
+            int mode, unsigned *err, const double *__restrict__ radd)
 {
     constexpr int V = 4 + NC;
     const int64_t e = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
@@ -375,6 +375,12 @@ cell_kernel(MeshDev m, const double *__restrict__ u, const T *__restrict__ slots
     for (int v = 0; v < V; v++)
 #pragma unroll
         for (int k = 0; k < kNB; k++) R[v][k] += (double) acc[v][k];
+    if (radd) {   // viscous volume terms of the momentum and energy rows
+#pragma unroll
+        for (int v = 0; v < 4; v++)
+#pragma unroll
+            for (int k = 0; k < kNB; k++) R[v][k] += __ldg(radd + (int64_t) (v * kNB + k) * E + e);
+    }
 
     if (mode == kCellResidual) {
 #pragma unroll
