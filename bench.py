@@ -305,6 +305,7 @@ def finish(args, rank, world, device, case, mesh, E, V, state_bytes, t_mesh, val
                               "note": "plain FP64 path is bound by the FP64 pipe, see profiles/"}}
     cpu = cpu_baseline(args.cpu_level, args.cpu_seconds, 1) if args.cpu_seconds > 0 else None
     adjoint = run_adjoint(args, device) if args.adjoint_steps > 0 else None
+    flame = run_flame(args, device) if args.flame_steps > 0 else None
     n_launch = int(launches.sum())
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -315,7 +316,8 @@ def finish(args, rank, world, device, case, mesh, E, V, state_bytes, t_mesh, val
                        "parallelism": f"replicas x{world}",
                        "l2": f"inputs larger than L2 (state {state_bytes / 1e6:.0f} MB > 129 MB)",
                        "mesh_build_s": t_mesh},
-            "e2e": e2e, "mixed": mixed, "adjoint": adjoint, "roofline": roofline, "cpu_baseline": cpu,
+            "e2e": e2e, "mixed": mixed, "adjoint": adjoint, "reacting_ns": flame, "roofline": roofline,
+            "cpu_baseline": cpu,
             "gpu_launches": n_launch,
             "clocks": clk.summary()}
 
@@ -389,6 +391,41 @@ def run_adjoint(args, device: int) -> dict:
                                       "noise's variable and coefficient)"}}
 
 
+def run_flame(args, device: int) -> dict:
+    """Reacting 2-species Navier-Stokes (viscous terms, species diffusion,
+    Arrhenius chemistry every stage), FP64, p1: DOF-updates/s of the step."""
+    from charm_3d_gb300 import synthetic
+    from charm_3d_gb300.solver import Forest, Solver
+    case = synthetic("flame", level=args.flame_level)
+    case.precision = "FP64"
+    mesh = Forest(case).flatten()
+    u0 = case.initial_state(mesh.center)
+    E, V = mesh.n_elem, case.n_var
+    gpu = Solver(case, device)
+    gpu.upload(mesh)
+    gpu.set_state(u0)
+    gpu.run(3, case.tau)
+    gpu.sync()
+    gpu.set_state(u0)
+    gpu.reset_stats()
+    gpu.set_timing(True)
+    ms = gpu.time_run(args.flame_steps, case.tau)
+    gpu.set_timing(False)
+    launches, kms = gpu.kernel_stats()
+    u = gpu.get_state()
+    gpu.close()
+    return {"workload": f"reacting 2-species NS, unit cube level {args.flame_level} ({E} hex), p1, HLLC, MIX EOS, "
+                        f"Sutherland mu/kappa, species diffusion, A->B Arrhenius, FP64",
+            "value": dof_per_step(E, V) * args.flame_steps / (ms * 1e-3), "unit": UNIT,
+            "ms_per_step": ms / args.flame_steps, "steps": args.flame_steps,
+            "kernel_share": {n: float(kms[i] / kms.sum()) for i, n in
+                             enumerate(["face (convective + viscous)", "cell", "limiter",
+                                        "chemistry, diffusion coefficients, lifting, viscous volume"])},
+            "finite": bool(np.isfinite(u).all()),
+            "mixed": "not built for the viscous/reacting terms (FP64 only)",
+            "basis": "p1 (the p2 basis with 27/9-point rules of this configuration is not built)"}
+
+
 def probe(abi, device: int, which: int) -> float | None:
     import ctypes as C
     lib = abi.load()
@@ -442,7 +479,9 @@ def main():
     ap.add_argument("--cpu-level", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--brick", type=int, default=1, help="trees along x (profiling sizes)")
-    ap.add_argument("--only", default="both", choices=["both", "fp64", "mixed", "adjoint"])
+    ap.add_argument("--only", default="both", choices=["both", "fp64", "mixed", "adjoint", "flame"])
+    ap.add_argument("--flame-level", type=int, default=6)
+    ap.add_argument("--flame-steps", type=int, default=5, help="0 skips the reacting-NS leg")
     ap.add_argument("--adjoint-level", type=int, default=6)
     ap.add_argument("--adjoint-box", default="4,6", help="J = integral of p over [lo,hi]^3 (lo,hi)")
     ap.add_argument("--adjoint-steps", type=int, default=200, help="0 skips the adjoint leg")
@@ -479,6 +518,10 @@ def main():
     if args.only == "adjoint":
         if rank == 0:
             print(json.dumps({"only": "adjoint", "adjoint": run_adjoint(args, local)}))
+        return
+    if args.only == "flame":
+        if rank == 0:
+            print(json.dumps({"only": "flame", "reacting_ns": run_flame(args, local)}))
         return
     res = run_gpu(args, rank, world, local)
     if rank == 0 and res is not None:

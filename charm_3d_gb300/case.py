@@ -211,6 +211,18 @@ class Case:
             p = np.where(r < a.get("radius", 0.1), a.get("p_in", 1.0e3), a.get("p_out", 0.1))
             rho = np.ones(E) * (1.0 + rng.uniform(-a.get("noise", 0.01), a.get("noise", 0.01), E))
             U = self.cons_from_prim(rho, zeros, zeros, zeros, p)
+        elif self.init == "flame":
+            r = np.sqrt((x - 0.5) ** 2 + (y - 0.5) ** 2 + (z - 0.5) ** 2)
+            hot = r < a.get("radius", 0.2)
+            T = np.where(hot, a.get("t_in", 1500.0), a.get("t_out", 300.0))
+            T = T * (1.0 + rng.uniform(-a.get("noise", 0.01), a.get("noise", 0.01), E))
+            c = np.zeros((self.n_comp, E))
+            c[0] = np.where(hot, 1.0, 0.0)
+            c[1] = 1.0 - c[0]
+            M_ = sum(c[i] / self.components[i].m for i in range(self.n_comp))
+            p = np.full(E, a.get("p", 1.0e5))
+            rho = p / (GAS_R * T * M_)
+            U = self.cons_from_prim(rho, zeros, zeros, zeros, p, c)
         elif self.init == "random":
             # smooth-ish random state for unit tests: all 4 coefficients set
             rho = 1.0 + 0.2 * rng.uniform(-1, 1, E)
@@ -269,6 +281,22 @@ def synthetic(name: str, level: int | None = None, **kw) -> Case:
                  init_args={"radius": 0.1, "p_in": 1.0e3, "p_out": 0.1, "noise": 0.01},
                  boundaries=[Boundary("ALL", "BOUND_OUTLET")])
         c.tau = 0.3 * (1.0 / 2 ** 8) / math.sqrt(1.4 * 1.0e3)
+    elif name == "flame":
+        # reacting 2-species Navier-Stokes: hot fuel kernel (T = 1500 K, Y_A = 1,
+        # r < 0.2) in 300 K air (species B), p = 1e5 Pa, unit cube; one-step
+        # A -> B, a = 1e9 1/s, Ea/R = 15000 K, heat release h0_A - h0_B = 2e6 J/kg;
+        # Sutherland viscosity, conductivity mu*cp/Pr with Pr = 0.72
+        mu0, cp = 1.716e-5, 1004.5
+        sl = dict(ml_type="SATHERLAND", kp_type="SATHERLAND", ml0=mu0, kp0=mu0 * cp / 0.72, t0=273.15, ts=110.4)
+        c = Case(name="flame", model="NS", flux="HLLC", limiter="NONE", level=6 if level is None else level,
+                 init="flame", steps=20, eos="MIX", use_visc=1, use_diff=1,
+                 components=[Component("A", m=0.02869409, cp=(cp,), h0=2.0e6, sig=3.62, ek=97.0, **sl),
+                             Component("B", m=0.02869409, cp=(cp,), h0=0.0, sig=3.62, ek=97.0, **sl)],
+                 reactions=[Reaction(left=(0, -1, -1), right=(1, -1, -1), a=1.0e9, e=15000.0 * GAS_R, n=0.0)],
+                 init_args={"radius": 0.2, "t_in": 1500.0, "t_out": 300.0, "p": 1.0e5, "noise": 0.01},
+                 boundaries=[Boundary("ALL", "BOUND_OUTLET")])
+        # acoustic limit of the hot kernel: c = sqrt(1.4 R 1500 / M) ~ 777 m/s
+        c.tau = 0.05 * (1.0 / 2 ** c.level) / 777.0
     else:
         raise ValueError(f"unknown synthetic case '{name}'")
     for k, v in kw.items():

@@ -69,3 +69,15 @@ def test_viscous_rejected_where_not_built():
     mesh, gpu, _, _ = _pair(small_case("visc", "HLLC", "NONE", level=1))
     with pytest.raises(CharmGpuError):
         gpu.adjoint(1, 3, Solver.pressure_box((0, 0, 0), (1, 1, 1)))
+
+
+def test_flame_workload_matches_oracle():
+    """The reacting workload of the bench (viscous, diffusion, chemistry) at
+    level 3, two steps, against the oracle."""
+    from charm_3d_gb300 import synthetic
+    case = synthetic("flame", level=3)
+    mesh, gpu, port, u0 = _pair(case)
+    gpu.run(2, case.tau)
+    gpu.sync()
+    port.run(2, case.tau)
+    assert rel_l2(gpu.get_state(), port.get_state()) < FP64_TOL
