@@ -242,6 +242,11 @@ void build_devcfg(const charm_gpu_config_t *c, DevCfg *d)
         d->comp_t0[i] = c->comp[i].t0; d->comp_ts[i] = c->comp[i].ts;
         d->comp_sig[i] = c->comp[i].sig; d->comp_ek[i] = c->comp[i].ek; d->comp_h0[i] = c->comp[i].h0;
         d->comp_kp_type[i] = c->comp[i].kp_type;
+        d->comp_href[i] = 0.0;
+        for (int k = 0; k < c->comp[i].n_cp; k++) {
+            d->comp_hc[i][k] = c->comp[i].cp[k] / (k + 1);
+            d->comp_href[i] += c->comp[i].cp[k] * pow(c->t_ref, k + 1) / (k + 1);
+        }
     }
     for (int r = 0; r < c->n_react; r++) {
         for (int k = 0; k < 3; k++) { d->react_l[r][k] = c->react[r].left[k]; d->react_r[r][k] = c->react[r].right[k]; }

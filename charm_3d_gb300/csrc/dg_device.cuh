@@ -60,6 +60,8 @@ struct DevCfg {
     double comp_ml0[kMaxComp], comp_kp0[kMaxComp], comp_t0[kMaxComp], comp_ts[kMaxComp];
     double comp_sig[kMaxComp], comp_ek[kMaxComp], comp_h0[kMaxComp];
     int    comp_kp_type[kMaxComp];
+    double comp_hc[kMaxComp][kMaxCp];   // cp_k / (k + 1): enthalpy polynomial
+    double comp_href[kMaxComp];         // sum cp_k t_ref^(k+1) / (k + 1)
     int    react_l[CHARM_GPU_MAX_REACT][3], react_r[CHARM_GPU_MAX_REACT][3];
     double react_a[CHARM_GPU_MAX_REACT], react_e[CHARM_GPU_MAX_REACT], react_n[CHARM_GPU_MAX_REACT];
 };

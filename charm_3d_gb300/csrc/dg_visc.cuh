@@ -26,55 +26,52 @@
 
 namespace charm {
 
-// charm_comp_calc_ml / _kp (src/charm_globals.c:651-676)
-__device__ __forceinline__ double comp_ml(int i, double t)
+// Sutherland factor sqrt((t/t0)^3) (t0 + ts) / (t + ts) of component i
+// (charm_comp_calc_ml / _kp, src/charm_globals.c:651-676; (t/t0)^1.5 as
+// x sqrt(x), without pow)
+__device__ __forceinline__ double sutherland(int i, double t)
 {
-    if (c_cfg.comp_ml_type[i] == CHARM_GPU_LAW_SUTHERLAND)
-        return c_cfg.comp_ml0[i] * sqrt(pow(t / c_cfg.comp_t0[i], 3.0)) * (c_cfg.comp_t0[i] + c_cfg.comp_ts[i]) /
-               (t + c_cfg.comp_ts[i]);
-    return c_cfg.comp_ml0[i];
+    const double x = t / c_cfg.comp_t0[i];
+    return x * sqrt(x) * (c_cfg.comp_t0[i] + c_cfg.comp_ts[i]) / (t + c_cfg.comp_ts[i]);
 }
 
-__device__ __forceinline__ double comp_kp(int i, double t)
-{
-    if (c_cfg.comp_kp_type[i] == CHARM_GPU_LAW_SUTHERLAND)
-        return c_cfg.comp_kp0[i] * sqrt(pow(t / c_cfg.comp_t0[i], 3.0)) * (c_cfg.comp_t0[i] + c_cfg.comp_ts[i]) /
-               (t + c_cfg.comp_ts[i]);
-    return c_cfg.comp_kp0[i];
-}
-
-// charm_comp_calc_enthalpy (:679-694): h0 + integral of the cp polynomial from t_ref
+// charm_comp_calc_enthalpy (:679-694): h0 + integral of the cp polynomial
+// from t_ref, here as h0 - H(t_ref) + H(t) with H(t) = sum cp_k t^(k+1)/(k+1)
+// by Horner (coefficients cp_k/(k+1) and H(t_ref) prepared on the host)
 __device__ __forceinline__ double comp_h(int i, double t)
 {
-    double h = c_cfg.comp_h0[i];
-    for (int k = 0; k < c_cfg.comp_ncp[i]; k++) {
-        const double t2 = pow(t, (double) (k + 1)) / (k + 1), t1 = pow(c_cfg.t_ref, (double) (k + 1)) / (k + 1);
-        h += c_cfg.comp_cp[i][k] * (t2 - t1);
-    }
-    return h;
+    double x = 0.0;
+    for (int k = c_cfg.comp_ncp[i] - 1; k >= 0; k--) x = x * t + c_cfg.comp_hc[i][k];
+    return c_cfg.comp_h0[i] + (x * t - c_cfg.comp_href[i]);
 }
 
-// charm_get_visc_mu / charm_get_heat_k (:515-558)
+// charm_get_visc_mu and charm_get_heat_k (:515-558) at one point, with one
+// Sutherland factor per component shared by mu and kappa (both laws use the
+// component's t0 and ts)
+template <int NC>
+__device__ __forceinline__ void transport(const Prim<double, NC> &p, double &mu, double &kt)
+{
+    double s = 0.0, m = 0.0, k = 0.0;
+#pragma unroll
+    for (int i = 0; i < NC; i++) {
+        const bool sm = c_cfg.comp_ml_type[i] == CHARM_GPU_LAW_SUTHERLAND;
+        const bool sk = c_cfg.comp_kp_type[i] == CHARM_GPU_LAW_SUTHERLAND;
+        const double f = (sm || sk) ? sutherland(i, p.t) : 1.0;
+        const double cm = p.c[i] / c_cfg.comp_m[i];
+        s += cm;
+        m += cm * (sm ? c_cfg.comp_ml0[i] * f : c_cfg.comp_ml0[i]);
+        k += p.c[i] * (sk ? c_cfg.comp_kp0[i] * f : c_cfg.comp_kp0[i]);
+    }
+    mu = m / s;
+    kt = k;
+}
+
 template <int NC>
 __device__ __forceinline__ double visc_mu(const Prim<double, NC> &p)
 {
-    double s = 0.0, mu = 0.0;
-#pragma unroll
-    for (int i = 0; i < NC; i++) {
-        const double cm = p.c[i] / c_cfg.comp_m[i];
-        s += cm;
-        mu += cm * comp_ml(i, p.t);
-    }
-    return mu / s;
-}
-
-template <int NC>
-__device__ __forceinline__ double heat_k(const Prim<double, NC> &p)
-{
-    double kt = 0.0;
-#pragma unroll
-    for (int i = 0; i < NC; i++) kt += p.c[i] * comp_kp(i, p.t);
-    return kt;
+    double mu, kt;
+    transport<NC>(p, mu, kt);
+    return mu;
 }
 
 // The 9 lifted fields' face values (diff_grad.c:150-176, 266-305): tau
@@ -290,8 +287,11 @@ __device__ __forceinline__ void vgrad_interior(const MeshDev &m, const double *_
         Prim<double, NC> pa, pb;
         cons_to_prim<double, NC>(Ua, pa);
         cons_to_prim<double, NC>(Ub, pb);
-        const double fmu = 0.5 * (visc_mu<NC>(pa) + visc_mu<NC>(pb));
-        const double kt = (heat_k<NC>(pa) + heat_k<NC>(pb)) * 0.5;
+        double mua, kta, mub, ktb;
+        transport<NC>(pa, mua, kta);
+        transport<NC>(pb, mub, ktb);
+        const double fmu = 0.5 * (mua + mub);
+        const double kt = (kta + ktb) * 0.5;
         double fc[NC];
 #pragma unroll
         for (int c = 0; c < NC; c++) fc[c] = (pa.c[c] + pb.c[c]) * 0.5;
@@ -347,7 +347,8 @@ __device__ __forceinline__ void vgrad_boundary(const MeshDev &m, const double *_
         for (int v = 0; v < V; v++) U[v] = c[v][0] + 0.5 * sg * c[v][1 + D] + ps * c[v][1 + s] + pt * c[v][1 + t];
         Prim<double, NC> pin, pout;
         cons_to_prim<double, NC>(U, pin);
-        const double mu = visc_mu<NC>(pin), kt = heat_k<NC>(pin);
+        double mu, kt;
+        transport<NC>(pin, mu, kt);
         bnd_cond<double, NC>(bid, pin, pout, n);
         double fu, fv, fw, ft;
         if (noslip) {
@@ -436,7 +437,8 @@ vgrad_cell_kernel(MeshDev m, const double *__restrict__ u, const double *__restr
         for (int v = 0; v < V; v++) U[v] = c[v][0] + px * c[v][1] + py * c[v][2] + pz * c[v][3];
         Prim<double, NC> p;
         cons_to_prim<double, NC>(U, p);
-        const double kt = heat_k<NC>(p), mu = visc_mu<NC>(p);
+        double kt, mu;
+        transport<NC>(p, mu, kt);
         const double lp = 4. * mu / 3., lm = -2. * mu / 3.;
         double hq = kt * p.t;
 #pragma unroll
