@@ -306,6 +306,7 @@ def finish(args, rank, world, device, case, mesh, E, V, state_bytes, t_mesh, val
     cpu = cpu_baseline(args.cpu_level, args.cpu_seconds, 1) if args.cpu_seconds > 0 else None
     adjoint = run_adjoint(args, device) if args.adjoint_steps > 0 else None
     flame = run_flame(args, device) if args.flame_steps > 0 else None
+    blast = run_blast(args, device) if args.blast_steps > 0 else None
     n_launch = int(launches.sum())
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -316,7 +317,8 @@ def finish(args, rank, world, device, case, mesh, E, V, state_bytes, t_mesh, val
                        "parallelism": f"replicas x{world}",
                        "l2": f"inputs larger than L2 (state {state_bytes / 1e6:.0f} MB > 129 MB)",
                        "mesh_build_s": t_mesh},
-            "e2e": e2e, "mixed": mixed, "adjoint": adjoint, "reacting_ns": flame, "roofline": roofline,
+            "e2e": e2e, "mixed": mixed, "adjoint": adjoint, "reacting_ns": flame, "blast_amr": blast,
+            "roofline": roofline,
             "cpu_baseline": cpu,
             "gpu_launches": n_launch,
             "clocks": clk.summary()}
@@ -426,6 +428,79 @@ def run_flame(args, device: int) -> dict:
             "basis": "p1 (the p2 basis with 27/9-point rules of this configuration is not built)"}
 
 
+def _blast_run(case, steps: int, device: int, precision: str):
+    """The AMR time loop of charm_model_ns_timestep_single on the GPU: the
+    reference criterion (charm_gpu_refine_flags) and the host octree's adapt
+    with projection every refine_period steps, then upload and continue."""
+    from charm_3d_gb300.solver import Forest, Solver
+    case.precision = precision
+    forest = Forest(case)
+    mesh = forest.flatten()
+    u = case.initial_state(mesh.center)
+    mass0 = None
+    gpu = Solver(case, device)
+    gpu.upload(mesh)
+    gpu.set_state(u)
+    dev_ms, dofs, t_adapt, step = 0.0, 0, 0.0, 0
+    t0 = time.perf_counter()
+    while step < steps:
+        if step and step % case.refine_period == 0:
+            ta = time.perf_counter()
+            _, grad = gpu.refine_flags(case.max_err)
+            u = forest.adapt_state(grad, case.max_err, case.min_level, case.max_level, case.n_comp, gpu.get_state())
+            mesh = forest.flatten()
+            gpu.upload(mesh)
+            gpu.set_state(u)
+            t_adapt += time.perf_counter() - ta
+        n = min(case.refine_period - step % case.refine_period, steps - step)
+        dev_ms += gpu.time_run(n, case.tau)
+        dofs += dof_per_step(mesh.n_elem, case.n_var) * n
+        step += n
+    gpu.sync()
+    wall = time.perf_counter() - t0
+    u = gpu.get_state()
+    gpu.close()
+    return forest, mesh, u, dev_ms, dofs, wall, t_adapt
+
+
+def _shock_radius(mesh, u, gam):
+    """Largest centre distance from the blast centre where p > 2 x ambient."""
+    r = np.sqrt(((mesh.center - 0.5) ** 2).sum(axis=0))
+    rho = u[4:, 0].sum(axis=0)
+    vel = u[:3, 0] / rho
+    p = (u[3, 0] - 0.5 * rho * (vel ** 2).sum(axis=0)) * (gam - 1.0)
+    hot = p > 0.2
+    return float(r[hot].max()) if hot.any() else 0.0
+
+
+def run_blast(args, device: int) -> dict:
+    """Spherical blast on AMR (base level 5, max 8, refine every 10 steps),
+    HLLC + BJ limiter: FP64 and the mixed form on the same loop."""
+    from charm_3d_gb300 import synthetic
+    out = {"workload": f"blast p=1 in r<0.1, p=0.1 outside, rho=1 +-1% noise; levels 5..8, reference refine "
+                       f"criterion every 10 steps, HLLC, BJ limiter, {args.blast_steps} steps"}
+    res = {}
+    for prec in ("FP64", "MIXED"):
+        case = synthetic("blast")
+        _, gam = case.gas_constants()
+        forest, mesh, u, dev_ms, dofs, wall, t_adapt = _blast_run(case, args.blast_steps, device, prec)
+        q, lv = forest.leaves()
+        res[prec] = (q, lv, u, mesh)
+        out[prec.lower()] = {"value": dofs / (dev_ms * 1e-3), "unit": UNIT, "device_ms": dev_ms,
+                             "e2e_dof_updates_per_s": dofs / wall, "wall_s": wall, "adapt_s": t_adapt,
+                             "final_elements": int(mesh.n_elem), "levels": [int(lv.min()), int(lv.max())],
+                             "shock_radius": _shock_radius(mesh, u, gam), "finite": bool(np.isfinite(u).all())}
+    q0, l0, u0, m0 = res["FP64"]
+    q1, l1, u1, _ = res["MIXED"]
+    same = q0.shape == q1.shape and np.array_equal(q0, q1) and np.array_equal(l0, l1)
+    out["same_mesh"] = bool(same)
+    if same:
+        rho0, rho1 = u0[4:].sum(axis=0), u1[4:].sum(axis=0)
+        out["rel_l2_density_mixed_vs_fp64"] = float(np.linalg.norm(rho1 - rho0) / np.linalg.norm(rho0))
+    out["speedup_mixed_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    return out
+
+
 def probe(abi, device: int, which: int) -> float | None:
     import ctypes as C
     lib = abi.load()
@@ -479,7 +554,8 @@ def main():
     ap.add_argument("--cpu-level", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--brick", type=int, default=1, help="trees along x (profiling sizes)")
-    ap.add_argument("--only", default="both", choices=["both", "fp64", "mixed", "adjoint", "flame"])
+    ap.add_argument("--only", default="both", choices=["both", "fp64", "mixed", "adjoint", "flame", "blast"])
+    ap.add_argument("--blast-steps", type=int, default=60, help="0 skips the AMR blast leg")
     ap.add_argument("--flame-level", type=int, default=6)
     ap.add_argument("--flame-steps", type=int, default=5, help="0 skips the reacting-NS leg")
     ap.add_argument("--adjoint-level", type=int, default=6)
@@ -518,6 +594,10 @@ def main():
     if args.only == "adjoint":
         if rank == 0:
             print(json.dumps({"only": "adjoint", "adjoint": run_adjoint(args, local)}))
+        return
+    if args.only == "blast":
+        if rank == 0:
+            print(json.dumps({"only": "blast", "blast_amr": run_blast(args, local)}))
         return
     if args.only == "flame":
         if rank == 0:
