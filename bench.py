@@ -437,7 +437,7 @@ def _blast_run(case, steps: int, device: int, precision: str):
     forest = Forest(case)
     mesh = forest.flatten()
     u = case.initial_state(mesh.center)
-    mass0 = None
+    mass0 = _mass(mesh, u)
     gpu = Solver(case, device)
     gpu.upload(mesh)
     gpu.set_state(u)
@@ -460,7 +460,13 @@ def _blast_run(case, steps: int, device: int, precision: str):
     wall = time.perf_counter() - t0
     u = gpu.get_state()
     gpu.close()
-    return forest, mesh, u, dev_ms, dofs, wall, t_adapt
+    return forest, mesh, u, dev_ms, dofs, wall, t_adapt, (_mass(mesh, u) - mass0) / mass0
+
+
+def _mass(mesh, u) -> float:
+    """Total mass: density means times leaf volumes."""
+    vol = np.prod([np.asarray(mesh.tree_len[d]) * 2.0 ** (-mesh.level.astype(np.float64)) for d in range(3)], axis=0)
+    return float((u[4:, 0].sum(axis=0) * vol).sum())
 
 
 def _shock_radius(mesh, u, gam):
@@ -483,13 +489,14 @@ def run_blast(args, device: int) -> dict:
     for prec in ("FP64", "MIXED"):
         case = synthetic("blast")
         _, gam = case.gas_constants()
-        forest, mesh, u, dev_ms, dofs, wall, t_adapt = _blast_run(case, args.blast_steps, device, prec)
+        forest, mesh, u, dev_ms, dofs, wall, t_adapt, drift = _blast_run(case, args.blast_steps, device, prec)
         q, lv = forest.leaves()
         res[prec] = (q, lv, u, mesh)
         out[prec.lower()] = {"value": dofs / (dev_ms * 1e-3), "unit": UNIT, "device_ms": dev_ms,
                              "e2e_dof_updates_per_s": dofs / wall, "wall_s": wall, "adapt_s": t_adapt,
                              "final_elements": int(mesh.n_elem), "levels": [int(lv.min()), int(lv.max())],
-                             "shock_radius": _shock_radius(mesh, u, gam), "finite": bool(np.isfinite(u).all())}
+                             "shock_radius": _shock_radius(mesh, u, gam), "mass_drift": drift,
+                             "finite": bool(np.isfinite(u).all())}
     q0, l0, u0, m0 = res["FP64"]
     q1, l1, u1, _ = res["MIXED"]
     same = q0.shape == q1.shape and np.array_equal(q0, q1) and np.array_equal(l0, l1)
