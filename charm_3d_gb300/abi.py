@@ -18,6 +18,7 @@ MAX_COMP = 8
 MAX_CP = 8
 MAX_BND = 16
 BASIS = 4
+BASIS_P2 = 10
 
 # status codes
 OK, EINVAL, ENOMEM, ECUDA, ENONFINITE, ENEGATIVE, EHLLC, ETIMEDOUT, ESTATE, ENOTSUP = range(10)
@@ -60,7 +61,7 @@ class Config(C.Structure):
                 ("comp", Comp * MAX_COMP), ("n_bnd", C.c_int), ("bnd", Bnd * MAX_BND),
                 ("grav", C.c_double * 3), ("tau", C.c_double), ("cfl", C.c_double), ("t_ref", C.c_double),
                 ("use_visc", C.c_int), ("check_every", C.c_int), ("use_diff", C.c_int), ("n_react", C.c_int),
-                ("react", Reaction * MAX_REACT)]
+                ("react", Reaction * MAX_REACT), ("p_order", C.c_int)]
 
 
 class Objective(C.Structure):

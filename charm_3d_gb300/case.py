@@ -92,6 +92,7 @@ class Case:
     steps: int = 10
     seed: int = 0
     init: str = "sod"          # initial-data generator name (see initial_state)
+    p_order: int = 1
     use_visc: int = 0
     use_diff: int = 0
     reactions: list = dc.field(default_factory=list)
@@ -104,6 +105,10 @@ class Case:
     @property
     def n_var(self) -> int:
         return 4 + self.n_comp
+
+    @property
+    def n_basis(self) -> int:
+        return 10 if self.p_order == 2 else 4
 
     def config(self) -> abi.Config:
         c = abi.Config()
@@ -141,6 +146,7 @@ class Case:
                 c.react[i].right[k] = (list(r.right) + [-1, -1, -1])[k]
             c.react[i].a, c.react[i].e, c.react[i].n = r.a, r.e, r.n
         c.check_every = 0
+        c.p_order = self.p_order
         return c
 
     # ---- thermodynamics for building initial states (reference formulas) ----
@@ -233,14 +239,16 @@ class Case:
                 c = rng.uniform(0.05, 1.0, (self.n_comp, E))
                 c /= c.sum(axis=0)
             U = self.cons_from_prim(rho, vel[0], vel[1], vel[2], p, c)
-            out = np.zeros((self.n_var, abi.BASIS, E))
+            out = np.zeros((self.n_var, self.n_basis, E))
             out[:, 0, :] = U
             slope = a.get("slope", 0.05)
-            out[:, 1:, :] = slope * rng.uniform(-1, 1, (self.n_var, 3, E)) * np.abs(U)[:, None, :]
+            out[:, 1:4, :] = slope * rng.uniform(-1, 1, (self.n_var, 3, E)) * np.abs(U)[:, None, :]
+            if self.n_basis == 10:   # second-order coefficients for p2
+                out[:, 4:, :] = 0.3 * slope * rng.uniform(-1, 1, (self.n_var, 6, E)) * np.abs(U)[:, None, :]
             return np.ascontiguousarray(out)
         else:
             raise ValueError(f"unknown initial data '{self.init}'")
-        out = np.zeros((self.n_var, abi.BASIS, E))
+        out = np.zeros((self.n_var, self.n_basis, E))
         out[:, 0, :] = U
         return np.ascontiguousarray(out)
 

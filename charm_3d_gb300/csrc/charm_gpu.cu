@@ -177,6 +177,8 @@ int validate_config(const charm_gpu_config_t *c)
     for (int b = 0; b < c->n_bnd; b++)
         if (c->bnd[b].type < 0 || c->bnd[b].type > CHARM_GPU_BND_MASS_FLOW)
             return fail(CHARM_GPU_EINVAL, "unknown boundary type");
+    if (c->p_order < 0 || c->p_order > 2) return fail(CHARM_GPU_EINVAL, "p_order must be 1 or 2");
+    if (c->p_order == 2) return fail(CHARM_GPU_ENOTSUP, "p2 basis not implemented on the GPU path");
     if (c->n_react < 0 || c->n_react > CHARM_GPU_MAX_REACT) return fail(CHARM_GPU_EINVAL, "bad reaction count");
     for (int r = 0; r < c->n_react; r++)
         for (int k = 0; k < 3; k++)

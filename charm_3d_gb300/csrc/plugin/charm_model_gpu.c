@@ -261,6 +261,7 @@ int charm_model_gpu_config(charm_ctx_t *ctx, int precision, charm_gpu_config_t *
     cfg->t_ref = ctx->model.ns.t_ref;
     cfg->use_visc = ctx->model.ns.use_visc;
     cfg->use_diff = ctx->model.ns.use_diff;
+    cfg->p_order = CHARM_BASE_FN_COUNT == 10 ? 2 : 1;   /* include/charm_def.h:177 */
     cfg->n_react = 0;
     if (ctx->reactions) {   /* charm_reaction_t list of src/models/ns/charm_model_ns_init.cpp:58-77 */
         if ((int) ctx->reactions->elem_count > CHARM_GPU_MAX_REACT) return CHARM_GPU_ENOTSUP;

@@ -122,6 +122,7 @@ class Solver:
         self.h = C.c_void_p()
         abi.check(self.lib.charm_gpu_create(C.byref(self.h), C.byref(self.cfg), device), "charm_gpu_create")
         self.n_var = 4 + self.cfg.n_comp
+        self.n_basis = abi.BASIS_P2 if self.cfg.p_order == 2 else abi.BASIS
         self.n_elem = 0
         self.mesh = None
 
@@ -143,7 +144,7 @@ class Solver:
         self.n_elem = mesh.n_elem
 
     def shape(self) -> tuple[int, int, int]:
-        return (self.n_var, abi.BASIS, self.n_elem)
+        return (self.n_var, self.n_basis, self.n_elem)
 
     def set_state(self, u) -> None:
         if isinstance(u, np.ndarray):

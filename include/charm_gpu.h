@@ -81,6 +81,7 @@ enum { CHARM_GPU_LAW_CONST = 0, CHARM_GPU_LAW_SUTHERLAND = 1 };
 #define CHARM_GPU_MAX_CP     8    /* cp polynomial coefficients */
 #define CHARM_GPU_MAX_BND   16    /* boundary-condition table entries */
 #define CHARM_GPU_BASIS      4    /* p1 Taylor basis (CHARM_BASE_FN_COUNT, charm_def.h:177) */
+#define CHARM_GPU_BASIS_P2  10    /* p2 Taylor basis (p_order = 2); state arrays are then [V][10][E] */
 
 typedef struct charm_gpu_comp {      /* charm_comp_t, include/charm_globals.h:224-240 */
     double m, ml0, kp0, t0, ts, sig, ek, h0;
@@ -117,6 +118,9 @@ typedef struct charm_gpu_config {
     int    use_diff;     /* MODEL.use_diffusion: species diffusion (needs use_visc, >= 2 species) */
     int    n_react;      /* reactions, evaluated per RK stage on cell means */
     charm_gpu_reaction_t react[CHARM_GPU_MAX_REACT];
+    int    p_order;      /* basis order: 1 (0 = 1), the reference's p1 Taylor basis with its 8/6-point
+                            rules; 2: the p2 Taylor basis (10 functions, charm_base_func) with
+                            27-point cell and 9-point face Gauss rules (uniform meshes, FP64) */
 } charm_gpu_config_t;
 
 /*

@@ -28,9 +28,17 @@
 #include <stdlib.h>
 #include <string.h>
 
-#define NB 4
-#define NQ 8
-#define NFQ 6
+/* basis size and quadrature sizes of the oracle instance `o` in scope:
+ * p1 (4 functions) with the reference's rules (8 Gauss points per cell, 6
+ * triangle points per face), or p2 (10 functions, the reference's
+ * charm_base_func with CHARM_BASE_FN_COUNT = 10) with 27-point and 9-point
+ * tensor Gauss rules (the reference's 8/6 rules under-integrate p2) */
+#define NBMAX 10
+#define NQMAX 27
+#define NFQMAX 9
+#define NB (o->nb)
+#define NQ (o->nq)
+#define NFQ (o->nfq)
 #define MAXV (4 + CHARM_GPU_MAX_COMP)
 
 static const double gR = 8.31446261815324;   /* src/charm_eos.c:8 */
@@ -43,12 +51,13 @@ typedef struct {
 
 typedef struct {
     double c[3], dh[3], vol;
-    double qgp[NQ][3], qgj[NQ];
-    double a_inv[NB][NB];
+    double qgp[NQMAX][3], qgj[NQMAX];
+    double a_inv[NBMAX][NBMAX];
 } elem_geom_t;
 
 typedef struct oracle {
     charm_gpu_config_t cfg;
+    int nb, nq, nfq;                /* basis functions, cell and face quadrature points */
     int64_t E, F, Fb;
     int V;
     elem_geom_t *g;
@@ -477,50 +486,68 @@ static void num_flux(const oracle_t *o, const prim_t pr[2], const double n[3], d
 /* ---- geometry (src/charm_geom.c) ------------------------------------------ */
 
 static double base_func(const double *x, int k, const double c[3], const double dh[3])
-{   /* charm_base_func, src/charm_base_func.c:8-35 (p1) */
+{   /* charm_base_func, src/charm_base_func.c:8-35 (p1: k < 4; p2: k < 10) */
     switch (k) {
     case 0: return 1.;
     case 1: return (x[0] - c[0]) / dh[0];
     case 2: return (x[1] - c[1]) / dh[1];
     case 3: return (x[2] - c[2]) / dh[2];
+    case 4: return (x[0] - c[0]) * (x[0] - c[0]) / (dh[0] * dh[0]);
+    case 5: return (x[1] - c[1]) * (x[1] - c[1]) / (dh[1] * dh[1]);
+    case 6: return (x[2] - c[2]) * (x[2] - c[2]) / (dh[2] * dh[2]);
+    case 7: return (x[0] - c[0]) * (x[1] - c[1]) / (dh[0] * dh[1]);
+    case 8: return (x[0] - c[0]) * (x[2] - c[2]) / (dh[0] * dh[2]);
+    case 9: return (x[1] - c[1]) * (x[2] - c[2]) / (dh[1] * dh[2]);
     default: return 0.;
     }
 }
 
-static double base_func_d(int k, int dir, const double dh[3])
-{   /* charm_base_func_dx/dy/dz, :38-125 (p1) */
-    return (k == dir + 1) ? 1. / dh[dir] : 0.;
+static double base_func_grad(const double *x, int k, const double c[3], const double dh[3], int dir)
+{   /* charm_base_func_dx/dy/dz, :38-125 */
+    if (k == 0) return 0.;
+    if (k <= 3) return (k == dir + 1) ? 1. / dh[dir] : 0.;
+    if (k <= 6) return (k == dir + 4) ? 2. * (x[dir] - c[dir]) / (dh[dir] * dh[dir]) : 0.;
+    {   /* 7: xy, 8: xz, 9: yz */
+        const int p0 = (k == 9) ? 1 : 0, p1 = (k == 7) ? 1 : 2;
+        if (dir == p0) return (x[p1] - c[p1]) / (dh[p0] * dh[p1]);
+        if (dir == p1) return (x[p0] - c[p0]) / (dh[p0] * dh[p1]);
+        return 0.;
+    }
 }
 
-static void matr_inv(double a_src[NB][NB], double am[NB][NB])
+static void matr_inv(int n, double a_src[NBMAX][NBMAX], double am[NBMAX][NBMAX])
 {   /* Gauss-Jordan with partial pivoting, src/charm_globals.c:285-394 */
-    double a[NB][NB];
-    int mask[NB], i, j, ni, nj;
+    double a[NBMAX][NBMAX];
+    int mask[NBMAX], i, j, ni, nj;
     memcpy(a, a_src, sizeof(a));
-    for (i = 0; i < NB; i++)
-        for (j = 0; j < NB; j++) am[i][j] = (i == j) ? 1.0 : 0.0;
-    for (i = 0; i < NB; i++) mask[i] = i;
-    for (i = 0; i < NB; i++) {
+    for (i = 0; i < n; i++)
+        for (j = 0; j < n; j++) am[i][j] = (i == j) ? 1.0 : 0.0;
+    for (i = 0; i < n; i++) mask[i] = i;
+    for (i = 0; i < n; i++) {
         int maxind = i;
         double fmaxval = fabs(a[i][i]);
-        for (ni = i + 1; ni < NB; ni++)
+        for (ni = i + 1; ni < n; ni++)
             if (fabs(fmaxval) <= fabs(a[ni][i])) { fmaxval = fabs(a[ni][i]); maxind = ni; }
         if (i != maxind) {
-            for (nj = 0; nj < NB; nj++) {
+            for (nj = 0; nj < n; nj++) {
                 double t = a[i][nj]; a[i][nj] = a[maxind][nj]; a[maxind][nj] = t;
                 t = am[i][nj]; am[i][nj] = am[maxind][nj]; am[maxind][nj] = t;
             }
             int ti = mask[i]; mask[i] = mask[maxind]; mask[maxind] = ti;
         }
         double aii = a[i][i];
-        for (j = 0; j < NB; j++) { a[i][j] /= aii; am[i][j] /= aii; }
-        for (ni = 0; ni < NB; ni++) {
+        for (j = 0; j < n; j++) { a[i][j] /= aii; am[i][j] /= aii; }
+        for (ni = 0; ni < n; ni++) {
             if (ni == i) continue;
             double fc = a[ni][i];
-            for (nj = 0; nj < NB; nj++) { a[ni][nj] -= fc * a[i][nj]; am[ni][nj] -= fc * am[i][nj]; }
+            for (nj = 0; nj < n; nj++) { a[ni][nj] -= fc * a[i][nj]; am[ni][nj] -= fc * am[i][nj]; }
         }
     }
 }
+
+/* 3-point Gauss-Legendre on [-1/2, 1/2] and its weights (sum 1), for the p2 rules */
+static const double GL3X[3] = {-0.38729833462074168852, 0.0, 0.38729833462074168852};   /* sqrt(3/5)/2 */
+static const double GL3W[3] = {5.0 / 18.0, 8.0 / 18.0, 5.0 / 18.0};
 
 static void trilinear(const double v[8][3], const double ref[3], double x[3])
 {   /* point of the trilinear map, src/charm_geom.c:47-66 */
@@ -547,33 +574,56 @@ static void elem_vertices(const elem_geom_t *g, double v[8][3])
     }
 }
 
-static void elem_geom(elem_geom_t *g, const double c[3], const double h[3])
+static void elem_geom(const oracle_t *o, elem_geom_t *g, const double c[3], const double h[3])
 {   /* charm_geom_quad_calc for a box (src/charm_geom.c:496-530) */
     double v[8][3];
     const double s3 = 1. / sqrt(3.);
     for (int k = 0; k < 3; k++) { g->c[k] = c[k]; g->dh[k] = h[k]; }
     elem_vertices(g, v);
     g->vol = 0.;
-    for (int i = 0; i < NQ; i++) {
-        double ref[3] = {(i & 1) ? s3 : -s3, (i & 2) ? s3 : -s3, (i & 4) ? s3 : -s3};
-        trilinear(v, ref, g->qgp[i]);
-        g->qgj[i] = (h[0] * 0.5) * (h[1] * 0.5) * (h[2] * 0.5);   /* det J of a box */
-        g->vol += g->qgj[i];
+    if (o->nb == 4) {
+        for (int i = 0; i < NQ; i++) {
+            double ref[3] = {(i & 1) ? s3 : -s3, (i & 2) ? s3 : -s3, (i & 4) ? s3 : -s3};
+            trilinear(v, ref, g->qgp[i]);
+            g->qgj[i] = (h[0] * 0.5) * (h[1] * 0.5) * (h[2] * 0.5);   /* det J of a box */
+            g->vol += g->qgj[i];
+        }
+    } else {   /* 3 x 3 x 3 Gauss, x fastest */
+        for (int i = 0; i < NQ; i++) {
+            const int ix = i % 3, iy = (i / 3) % 3, iz = i / 9;
+            g->qgp[i][0] = c[0] + GL3X[ix] * h[0];
+            g->qgp[i][1] = c[1] + GL3X[iy] * h[1];
+            g->qgp[i][2] = c[2] + GL3X[iz] * h[2];
+            g->qgj[i] = h[0] * h[1] * h[2] * GL3W[ix] * GL3W[iy] * GL3W[iz];
+            g->vol += g->qgj[i];
+        }
     }
-    double a[NB][NB];
+    double a[NBMAX][NBMAX];
     for (int i = 0; i < NB; i++)
         for (int j = 0; j < NB; j++) {
             a[i][j] = 0.;
             for (int q = 0; q < NQ; q++)
                 a[i][j] += g->qgj[q] * base_func(g->qgp[q], i, g->c, g->dh) * base_func(g->qgp[q], j, g->c, g->dh);
         }
-    matr_inv(a, g->a_inv);
+    matr_inv(NB, a, g->a_inv);
 }
 
 /* Face quadrature points of face f of a box (_charm_face_calc_gp_by_tri,
  * src/charm_geom.c:443-494) and the per-point weight gw*gj. */
-static void face_points(const elem_geom_t *g, int f, double gp[NFQ][3], double gwj[NFQ])
+static void face_points(const oracle_t *o, const elem_geom_t *g, int f, double gp[NFQMAX][3], double gwj[NFQMAX])
 {
+    if (o->nb != 4) {   /* p2: 3 x 3 Gauss on the face, lower tangential axis fastest */
+        const int d = f / 2, sa = (d == 0) ? 1 : 0, ta = (d == 2) ? 1 : 2;
+        const double area = g->dh[sa] * g->dh[ta];
+        for (int i = 0; i < 9; i++) {
+            const int is = i % 3, it = i / 3;
+            gp[i][d] = g->c[d] + ((f & 1) ? 0.5 : -0.5) * g->dh[d];
+            gp[i][sa] = g->c[sa] + GL3X[is] * g->dh[sa];
+            gp[i][ta] = g->c[ta] + GL3X[it] * g->dh[ta];
+            gwj[i] = area * GL3W[is] * GL3W[it];
+        }
+        return;
+    }
     static const int ftv[6][4] = {{0, 2, 4, 6}, {1, 3, 5, 7}, {0, 1, 4, 5}, {2, 3, 6, 7}, {0, 1, 2, 3}, {4, 5, 6, 7}};
     double v8[8][3], v[4][3];
     elem_vertices(g, v8);
@@ -672,8 +722,8 @@ static void residual(oracle_t *o, const double *u, double *res)
             }
             const double gjw = g->qgj[q];
             for (int k = 0; k < NB; k++) {
-                double px = base_func_d(k, 0, g->dh) * gjw, py = base_func_d(k, 1, g->dh) * gjw,
-                       pz = base_func_d(k, 2, g->dh) * gjw, phi = base_func(x, k, g->c, g->dh) * gjw;
+                double px = base_func_grad(x, k, g->c, g->dh, 0) * gjw, py = base_func_grad(x, k, g->c, g->dh, 1) * gjw,
+                       pz = base_func_grad(x, k, g->c, g->dh, 2) * gjw, phi = base_func(x, k, g->c, g->dh) * gjw;
                 for (int v = 0; v < V; v++) {
                     double gr = (v < 3) ? p.r * o->cfg.grav[v] * phi : 0.;
                     res[(v * NB + k) * E + e] -= (F[0][v] * px + F[1][v] * py + F[2][v] * pz) + gr;
@@ -692,8 +742,8 @@ static void residual(oracle_t *o, const double *u, double *res)
         const int hs = (kind == 2) ? 1 : 0;
         elem_geom_t pg = o->g[e[hs]];
         memcpy(pg.c, cs[hs], sizeof(double) * 3);
-        double gp[NFQ][3], gwj[NFQ], n[3];
-        face_points(&pg, hs ? 2 * d : 2 * d + 1, gp, gwj);
+        double gp[NFQMAX][3], gwj[NFQMAX], n[3];
+        face_points(o, &pg, hs ? 2 * d : 2 * d + 1, gp, gwj);
         outward_normal(2 * d + 1, n);
         for (int q = 0; q < NFQ; q++) {
             prim_t pr[2];
@@ -716,8 +766,8 @@ static void residual(oracle_t *o, const double *u, double *res)
         const int32_t e = o->bface_elem[j];
         const int f = o->bface_face[j], bid = o->bface_bnd[j];
         const elem_geom_t *g = &o->g[e];
-        double gp[NFQ][3], gwj[NFQ], n[3];
-        face_points(g, f, gp, gwj);
+        double gp[NFQMAX][3], gwj[NFQMAX], n[3];
+        face_points(o, g, f, gp, gwj);
         outward_normal(f, n);
         for (int q = 0; q < NFQ; q++) {
             double U[MAXV];
@@ -871,8 +921,9 @@ static void visc_grad(oracle_t *o, const double *u)
             const double kt = heat_k(o, &p), lambda = 0., mu = visc_mu(o, &p);
             const double lp = (lambda + 4. * mu / 3.), lm = (lambda - 2. * mu / 3.);
             for (int k = 0; k < NB; k++) {
-                const double px = base_func_d(k, 0, g->dh) * g->qgj[q], py = base_func_d(k, 1, g->dh) * g->qgj[q],
-                             pz = base_func_d(k, 2, g->dh) * g->qgj[q];
+                const double px = base_func_grad(x, k, g->c, g->dh, 0) * g->qgj[q],
+                             py = base_func_grad(x, k, g->c, g->dh, 1) * g->qgj[q],
+                             pz = base_func_grad(x, k, g->c, g->dh, 2) * g->qgj[q];
                 double *a = &acc[e * 9 * NB];
                 a[0 * NB + k] -= (lp * p.u * px + lm * p.v * py + lm * p.w * pz);
                 a[1 * NB + k] -= (lm * p.u * px + lp * p.v * py + lm * p.w * pz);
@@ -903,8 +954,8 @@ static void visc_grad(oracle_t *o, const double *u)
         const int hs = (kind == 2) ? 1 : 0;
         elem_geom_t pg = o->g[e[hs]];
         memcpy(pg.c, cs[hs], sizeof(double) * 3);
-        double gp[NFQ][3], gwj[NFQ], n[3];
-        face_points(&pg, hs ? 2 * d : 2 * d + 1, gp, gwj);
+        double gp[NFQMAX][3], gwj[NFQMAX], n[3];
+        face_points(o, &pg, hs ? 2 * d : 2 * d + 1, gp, gwj);
         outward_normal(2 * d + 1, n);
         for (int q = 0; q < NFQ; q++) {
             prim_t pr[2];
@@ -936,8 +987,8 @@ static void visc_grad(oracle_t *o, const double *u)
         const int32_t e = o->bface_elem[j];
         const int f = o->bface_face[j], bid = o->bface_bnd[j];
         const elem_geom_t *g = &o->g[e];
-        double gp[NFQ][3], gwj[NFQ], n[3];
-        face_points(g, f, gp, gwj);
+        double gp[NFQMAX][3], gwj[NFQMAX], n[3];
+        face_points(o, g, f, gp, gwj);
         outward_normal(f, n);
         const int noslip = o->cfg.bnd[bid].type == CHARM_GPU_BND_WALL_NO_SLIP;
         for (int q = 0; q < NFQ; q++) {
@@ -983,8 +1034,9 @@ static void visc_integrals(oracle_t *o, const double *u, double *res)
             prim_at(o, u, e, g->c, x, &p);
             vis_at(o, e, g->c, x, t);
             for (int k = 0; k < NB; k++) {
-                const double px = base_func_d(k, 0, g->dh) * g->qgj[q], py = base_func_d(k, 1, g->dh) * g->qgj[q],
-                             pz = base_func_d(k, 2, g->dh) * g->qgj[q], phi = base_func(x, k, g->c, g->dh) * g->qgj[q];
+                const double px = base_func_grad(x, k, g->c, g->dh, 0) * g->qgj[q],
+                             py = base_func_grad(x, k, g->c, g->dh, 1) * g->qgj[q],
+                             pz = base_func_grad(x, k, g->c, g->dh, 2) * g->qgj[q], phi = base_func(x, k, g->c, g->dh) * g->qgj[q];
                 res[(0 * NB + k) * E + e] += (t[0] * px + t[3] * py + t[4] * pz);
                 res[(1 * NB + k) * E + e] += (t[3] * px + t[1] * py + t[5] * pz);
                 res[(2 * NB + k) * E + e] += (t[4] * px + t[5] * py + t[2] * pz);
@@ -1006,8 +1058,8 @@ static void visc_integrals(oracle_t *o, const double *u, double *res)
         const int hs = (kind == 2) ? 1 : 0;
         elem_geom_t pg = o->g[e[hs]];
         memcpy(pg.c, cs[hs], sizeof(double) * 3);
-        double gp[NFQ][3], gwj[NFQ], n[3];
-        face_points(&pg, hs ? 2 * d : 2 * d + 1, gp, gwj);
+        double gp[NFQMAX][3], gwj[NFQMAX], n[3];
+        face_points(o, &pg, hs ? 2 * d : 2 * d + 1, gp, gwj);
         outward_normal(2 * d + 1, n);
         for (int q = 0; q < NFQ; q++) {
             double ft6[6] = {0., 0., 0., 0., 0., 0.}, fu = 0., fv = 0., fw = 0., ft = 0.;
@@ -1156,7 +1208,7 @@ static void update(oracle_t *o, double *u, const double *res, double dt)
 {
     for (int64_t e = 0; e < o->E; e++)
         for (int v = 0; v < o->V; v++) {
-            double rhs[NB];
+            double rhs[NBMAX];
             for (int i = 0; i < NB; i++) {
                 rhs[i] = 0.;
                 for (int j = 0; j < NB; j++) rhs[i] += o->g[e].a_inv[i][j] * res[(v * NB + j) * o->E + e];
@@ -1264,6 +1316,9 @@ oracle_t *oracle_new(const charm_gpu_config_t *cfg, const charm_gpu_mesh_t *m)
     oracle_t *o = (oracle_t *) calloc(1, sizeof(oracle_t));
     if (!o) return NULL;
     o->cfg = *cfg;
+    o->nb = (cfg->p_order == 2) ? 10 : 4;
+    o->nq = (cfg->p_order == 2) ? 27 : 8;
+    o->nfq = (cfg->p_order == 2) ? 9 : 6;
     o->E = m->n_elem; o->F = m->n_face; o->Fb = m->n_bface;
     o->V = 4 + cfg->n_comp;
     const size_t st = sizeof(double) * (size_t) o->V * NB * (size_t) o->E;
@@ -1288,7 +1343,7 @@ oracle_t *oracle_new(const charm_gpu_config_t *cfg, const charm_gpu_mesh_t *m)
     for (int64_t e = 0; e < o->E; e++) {
         double c[3] = {m->center[e], m->center[o->E + e], m->center[2 * o->E + e]}, h[3];
         for (int d = 0; d < 3; d++) h[d] = ldexp(m->tree_len[d], -m->level[e]);
-        elem_geom(&o->g[e], c, h);
+        elem_geom(o, &o->g[e], c, h);
     }
     memcpy(o->face_elem, m->face_elem, sizeof(int32_t) * 2 * (size_t) o->F);
     memcpy(o->face_info, m->face_info, (size_t) o->F);
@@ -1366,8 +1421,8 @@ int oracle_amr_grad(oracle_t *o, double *grad)
         const int32_t e = o->bface_elem[j];
         const int f = o->bface_face[j];
         const elem_geom_t *g = &o->g[e];
-        double gp[NFQ][3], gwj[NFQ], n[3];
-        face_points(g, f, gp, gwj);
+        double gp[NFQMAX][3], gwj[NFQMAX], n[3];
+        face_points(o, g, f, gp, gwj);
         outward_normal(f, n);
         for (int q = 0; q < NFQ; q++) {
             double U[MAXV];
@@ -1388,8 +1443,8 @@ int oracle_amr_grad(oracle_t *o, double *grad)
         const int hs = (kind == 2) ? 1 : 0;
         elem_geom_t pg = o->g[e[hs]];
         memcpy(pg.c, cs[hs], sizeof(double) * 3);
-        double gp[NFQ][3], gwj[NFQ], n[3];
-        face_points(&pg, hs ? 2 * d : 2 * d + 1, gp, gwj);
+        double gp[NFQMAX][3], gwj[NFQMAX], n[3];
+        face_points(o, &pg, hs ? 2 * d : 2 * d + 1, gp, gwj);
         outward_normal(2 * d + 1, n);
         for (int q = 0; q < NFQ; q++) {
             prim_t pr[2];

@@ -42,7 +42,7 @@ class Port:
         self.h = self.lib.oracle_new(C.addressof(cfg), C.addressof(self._m))
         if not self.h:
             raise MemoryError("oracle_new failed")
-        self.shape = (4 + cfg.n_comp, 4, mesh.n_elem)
+        self.shape = (4 + cfg.n_comp, 10 if cfg.p_order == 2 else 4, mesh.n_elem)
 
     def close(self):
         if self.h:
