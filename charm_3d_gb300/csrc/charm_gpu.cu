@@ -26,6 +26,7 @@
 #include "dg_kernels.cuh"
 #include "dg_adjoint.cuh"
 #include "dg_visc.cuh"
+#include "dg_p2.cuh"
 
 using namespace charm;
 
@@ -57,6 +58,7 @@ struct TimedLaunch {
 struct charm_gpu_handle_s {
     charm_gpu_config_t cfg;
     DevCfg dcfg;
+    int nb = CHARM_GPU_BASIS;          // basis functions: 4 (p1) or 10 (p2)
     int device = 0;
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
@@ -178,7 +180,11 @@ int validate_config(const charm_gpu_config_t *c)
         if (c->bnd[b].type < 0 || c->bnd[b].type > CHARM_GPU_BND_MASS_FLOW)
             return fail(CHARM_GPU_EINVAL, "unknown boundary type");
     if (c->p_order < 0 || c->p_order > 2) return fail(CHARM_GPU_EINVAL, "p_order must be 1 or 2");
-    if (c->p_order == 2) return fail(CHARM_GPU_ENOTSUP, "p2 basis not implemented on the GPU path");
+    if (c->p_order == 2) {
+        if (c->precision != CHARM_GPU_PREC_FP64) return fail(CHARM_GPU_ENOTSUP, "p2: FP64 precision only");
+        if (c->limiter != CHARM_GPU_LIM_NONE) return fail(CHARM_GPU_ENOTSUP, "p2: limiter not supported");
+        if (c->dt_mode != CHARM_GPU_DT_TAU) return fail(CHARM_GPU_ENOTSUP, "p2: fixed time step (TAU) only");
+    }
     if (c->n_react < 0 || c->n_react > CHARM_GPU_MAX_REACT) return fail(CHARM_GPU_EINVAL, "bad reaction count");
     for (int r = 0; r < c->n_react; r++)
         for (int k = 0; k < 3; k++)
@@ -406,6 +412,153 @@ int launch_cfl(charm_gpu_handle_s *h, const double *u)
 }
 
 // One stage: out = a_new*L(u - dt*M^-1*R(u)) + a_old*u0 (L = limiter or identity).
+// ---- p2 basis -------------------------------------------------------------------
+
+// Rule tables and the inverse mass matrix of the reference box for the p2
+// kernels (3-point Gauss-Legendre per axis; the mass matrix by the 27-point
+// rule, exact for the quadratic basis, inverted by Gauss-Jordan).
+int upload_p2_tables(charm_gpu_handle_s *h)
+{
+    P2Tab t;
+    memset(&t, 0, sizeof(t));
+    const double gx[3] = {-0.5 * sqrt(0.6), 0.0, 0.5 * sqrt(0.6)};
+    const double gw[3] = {5.0 / 18.0, 8.0 / 18.0, 5.0 / 18.0};
+    for (int i = 0; i < 27; i++) {
+        const int ix = i % 3, iy = (i / 3) % 3, iz = i / 9;
+        t.cxi[i][0] = gx[ix]; t.cxi[i][1] = gx[iy]; t.cxi[i][2] = gx[iz];
+        t.cw[i] = gw[ix] * gw[iy] * gw[iz];
+    }
+    for (int i = 0; i < 9; i++) {
+        t.fxi[i][0] = gx[i % 3]; t.fxi[i][1] = gx[i / 3];
+        t.fw[i] = gw[i % 3] * gw[i / 3];
+    }
+    double a[kNB2][2 * kNB2];
+    memset(a, 0, sizeof(a));
+    for (int q = 0; q < 27; q++) {
+        const double x = t.cxi[q][0], y = t.cxi[q][1], z = t.cxi[q][2];
+        const double ph[kNB2] = {1.0, x, y, z, x * x, y * y, z * z, x * y, x * z, y * z};
+        for (int i = 0; i < kNB2; i++) {
+            t.mean[i] += t.cw[q] * ph[i];
+            for (int j = 0; j < kNB2; j++) a[i][j] += t.cw[q] * ph[i] * ph[j];
+        }
+    }
+    for (int i = 0; i < kNB2; i++) a[i][kNB2 + i] = 1.0;
+    for (int c = 0; c < kNB2; c++) {   // Gauss-Jordan, partial pivoting
+        int piv = c;
+        for (int r = c + 1; r < kNB2; r++)
+            if (fabs(a[r][c]) > fabs(a[piv][c])) piv = r;
+        if (piv != c)
+            for (int k = 0; k < 2 * kNB2; k++) std::swap(a[c][k], a[piv][k]);
+        const double d = a[c][c];
+        for (int k = 0; k < 2 * kNB2; k++) a[c][k] /= d;
+        for (int r = 0; r < kNB2; r++) {
+            if (r == c) continue;
+            const double f = a[r][c];
+            for (int k = 0; k < 2 * kNB2; k++) a[r][k] -= f * a[c][k];
+        }
+    }
+    for (int i = 0; i < kNB2; i++)
+        for (int j = 0; j < kNB2; j++) t.minv[i][j] = a[i][kNB2 + j];
+    CUDA_TRY(cudaMemcpyToSymbol(c_p2, &t, sizeof(t)));
+    return CHARM_GPU_OK;
+}
+
+template <int NC>
+int launch_p2_face(charm_gpu_handle_s *h, const double *u)
+{
+    MeshDev m = mesh_view(h);
+    const int bs = 128;
+    const int64_t nbi = (h->F + bs - 1) / bs, nbb = (h->Fb + bs - 1) / bs;
+    if (nbi + nbb == 0) return CHARM_GPU_OK;
+    double *slots = static_cast<double *>(h->d_slots);
+    const unsigned nb = (unsigned) (nbi + nbb);
+    TimedLaunch t;
+    begin_launch(h, 0, &t);
+    switch (h->cfg.flux) {
+    case CHARM_GPU_FLUX_LF: p2_face_kernel<NC, CHARM_GPU_FLUX_LF><<<nb, bs, 0, h->stream>>>(m, u, slots, nbi, h->d_err); break;
+    case CHARM_GPU_FLUX_HLLC: p2_face_kernel<NC, CHARM_GPU_FLUX_HLLC><<<nb, bs, 0, h->stream>>>(m, u, slots, nbi, h->d_err); break;
+    case CHARM_GPU_FLUX_CD: p2_face_kernel<NC, CHARM_GPU_FLUX_CD><<<nb, bs, 0, h->stream>>>(m, u, slots, nbi, h->d_err); break;
+    default: p2_face_kernel<NC, CHARM_GPU_FLUX_GODUNOV><<<nb, bs, 0, h->stream>>>(m, u, slots, nbi, h->d_err); break;
+    }
+    end_launch(h, &t);
+    CUDA_TRY(cudaGetLastError());
+    return CHARM_GPU_OK;
+}
+
+template <int NC>
+int launch_p2_cell(charm_gpu_handle_s *h, const double *u, const double *u0, double *out, double dt,
+                   const double *dt_dev, double a_new, double a_old, int mode, const double *radd)
+{
+    MeshDev m = mesh_view(h);
+    const int bs = 128;
+    TimedLaunch t;
+    begin_launch(h, 1, &t);
+    p2_cell_kernel<NC><<<(unsigned) ((h->E + bs - 1) / bs), bs, 0, h->stream>>>(
+        m, u, static_cast<const double *>(h->d_slots), u0, out, dt, dt_dev, a_new, a_old, mode, h->d_err, radd);
+    end_launch(h, &t);
+    CUDA_TRY(cudaGetLastError());
+    return CHARM_GPU_OK;
+}
+
+// chemistry, lifting and viscous volume terms of the p2 stage state
+template <int NC>
+int launch_p2_visc_chem(charm_gpu_handle_s *h, const double **u, const double **radd, bool chem)
+{
+    MeshDev m = mesh_view(h);
+    const int bs = 128;
+    const int64_t nbe = (h->E + bs - 1) / bs;
+    const int64_t nbi = (h->F + bs - 1) / bs, nbb = (h->Fb + bs - 1) / bs;
+    TimedLaunch t;
+    begin_launch(h, 3, &t);
+    if (chem && h->cfg.n_react) {
+        p2_chem_kernel<NC><<<(unsigned) nbe, bs, 0, h->stream>>>(m, *u, h->d_uc, h->d_chem_rhs);
+        *u = h->d_uc;
+    }
+    if (h->cfg.use_visc) {
+        if (h->cfg.use_diff && NC >= 2)
+            diffcoef_kernel<NC, kNB2><<<(unsigned) nbe, bs, 0, h->stream>>>(m, *u, h->d_dif);
+        if (nbi + nbb)
+            p2_vgrad_face_kernel<NC><<<(unsigned) (nbi + nbb), bs, 0, h->stream>>>(m, *u, h->d_dif, h->d_s9, nbi);
+        p2_vgrad_cell_kernel<NC><<<(unsigned) nbe, bs, 0, h->stream>>>(m, *u, h->d_dif, h->d_s9, h->d_vis);
+        p2_vvol_kernel<NC><<<(unsigned) nbe, bs, 0, h->stream>>>(m, *u, h->d_vis, chem ? h->d_chem_rhs : nullptr,
+                                                                  h->d_radd);
+        *radd = h->d_radd;
+    }
+    end_launch(h, &t);
+    CUDA_TRY(cudaGetLastError());
+    return CHARM_GPU_OK;
+}
+
+template <int NC>
+int launch_p2_vflux(charm_gpu_handle_s *h, const double *u)
+{
+    MeshDev m = mesh_view(h);
+    const int bs = 128;
+    const int64_t nbi = (h->F + bs - 1) / bs, nbb = (h->Fb + bs - 1) / bs;
+    if (nbi + nbb == 0) return CHARM_GPU_OK;
+    TimedLaunch t;
+    begin_launch(h, 0, &t);
+    p2_vflux_face_kernel<NC><<<(unsigned) (nbi + nbb), bs, 0, h->stream>>>(m, u, h->d_vis,
+                                                                          static_cast<double *>(h->d_slots), nbi);
+    end_launch(h, &t);
+    CUDA_TRY(cudaGetLastError());
+    return CHARM_GPU_OK;
+}
+
+// one p2 stage (or, with mode kCellResidual and no chemistry, the residual)
+template <int NC>
+int p2_stage(charm_gpu_handle_s *h, const double *u, const double *u0, double *out, double dt, const double *dt_dev,
+             double a_new, double a_old, int mode)
+{
+    int rc;
+    const double *radd = nullptr;
+    const bool model_ns = h->cfg.model == CHARM_GPU_MODEL_NS;
+    if (model_ns && (rc = launch_p2_visc_chem<NC>(h, &u, &radd, mode == kCellUpdate))) return rc;
+    if ((rc = launch_p2_face<NC>(h, u))) return rc;
+    if (radd && (rc = launch_p2_vflux<NC>(h, u))) return rc;
+    return launch_p2_cell<NC>(h, u, u0, out, dt, dt_dev, a_new, a_old, mode, radd);
+}
+
 // ---- viscous terms and chemistry (charm_model_ns_timestep_single's stage,
 //      src/models/ns/charm_model.c:242-253: chem, diff, conv, update) -------
 
@@ -471,6 +624,8 @@ int stage(charm_gpu_handle_s *h, const double *u, const double *u0, double *out,
 {
     int rc;
     const double *radd = nullptr;
+    if constexpr (sizeof(T) == sizeof(double))
+        if (h->nb == kNB2) return p2_stage<NC>(h, u, u0, out, dt, dt_dev, a_new, a_old, kCellUpdate);
     if constexpr (sizeof(T) == sizeof(double)) {
         if (has_visc_chem(h)) {
             if (h->cfg.n_react) {
@@ -520,7 +675,7 @@ int step_impl(charm_gpu_handle_s *h, double dt, const double *dt_dev)
 
 // ---- mixed form on FP32 hi/lo planes ---------------------------------------
 
-int64_t n_state(const charm_gpu_handle_s *h) { return (int64_t) n_var(h) * CHARM_GPU_BASIS * h->E; }
+int64_t n_state(const charm_gpu_handle_s *h) { return (int64_t) n_var(h) * h->nb * h->E; }
 
 // hi/lo <- d_u (to_ff) or d_u <- hi/lo of buffer 0
 int ff_convert(charm_gpu_handle_s *h, bool to_ff)
@@ -741,7 +896,12 @@ int charm_gpu_create(charm_gpu_handle_t *out, const charm_gpu_config_t *cfg, int
     auto *h = new charm_gpu_handle_s();
     h->cfg = *cfg;
     h->device = device;
+    h->nb = (cfg->p_order == 2) ? kNB2 : CHARM_GPU_BASIS;
     build_devcfg(cfg, &h->dcfg);
+    if (h->nb == kNB2 && upload_p2_tables(h) != CHARM_GPU_OK) {
+        delete h;
+        return CHARM_GPU_ECUDA;
+    }
     if (cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete h;
         return fail(CHARM_GPU_ECUDA, "cudaStreamCreate failed");
@@ -793,6 +953,7 @@ int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh)
         const int d = info & 3, kind = (info >> 2) & 3;
         if (a < 0 || a >= E || b < 0 || b >= E || d > 2 || kind > 2)
             return fail(CHARM_GPU_EINVAL, "face record out of range");
+        if (kind && h->nb != CHARM_GPU_BASIS) return fail(CHARM_GPU_ENOTSUP, "p2: conforming meshes only");
         cnt[a]++; cnt[b]++;
         const int fa = 2 * d + 1, fb = 2 * d;   // face ids on side 0 / side 1
         if (kind == 0) {
@@ -842,8 +1003,8 @@ int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh)
     cudaStreamSynchronize(h->stream);
     free_mesh(h);
     const int V = n_var(h);
-    const size_t st = (size_t) V * CHARM_GPU_BASIS * E * sizeof(double);
-    const size_t sl = (size_t) V * CHARM_GPU_BASIS * (S > 0 ? S : 2) *
+    const size_t st = (size_t) V * h->nb * E * sizeof(double);
+    const size_t sl = (size_t) V * h->nb * (S > 0 ? S : 2) *
                       (h->cfg.precision == CHARM_GPU_PREC_MIXED ? sizeof(float) : sizeof(double));
     CUDA_TRY(cudaMalloc(&h->d_center, 3 * E * sizeof(double)));
     CUDA_TRY(cudaMalloc(&h->d_level, E));
@@ -865,9 +1026,9 @@ int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh)
         CUDA_TRY(cudaMemset(h->d_chem_rhs, 0, sizeof(double) * E));
         if (h->cfg.n_react) CUDA_TRY(cudaMalloc(&h->d_uc, st));
         if (h->cfg.use_visc) {
-            CUDA_TRY(cudaMalloc(&h->d_s9, sizeof(double) * 9 * CHARM_GPU_BASIS * S));
-            CUDA_TRY(cudaMalloc(&h->d_vis, sizeof(double) * 9 * CHARM_GPU_BASIS * E));
-            CUDA_TRY(cudaMalloc(&h->d_radd, sizeof(double) * 4 * CHARM_GPU_BASIS * E));
+            CUDA_TRY(cudaMalloc(&h->d_s9, sizeof(double) * 9 * h->nb * S));
+            CUDA_TRY(cudaMalloc(&h->d_vis, sizeof(double) * 9 * h->nb * E));
+            CUDA_TRY(cudaMalloc(&h->d_radd, sizeof(double) * 4 * h->nb * E));
             CUDA_TRY(cudaMalloc(&h->d_dif, sizeof(double) * V * E));
             CUDA_TRY(cudaMemset(h->d_dif, 0, sizeof(double) * V * E));
         }
@@ -969,7 +1130,7 @@ int charm_gpu_set_state(charm_gpu_handle_t h, const double *u, int on_device)
     if (!h || !u) return fail(CHARM_GPU_EINVAL, "null argument");
     if (!h->mesh_ready) return fail(CHARM_GPU_ESTATE, "no mesh uploaded");
     CUDA_TRY(cudaSetDevice(h->device));
-    const size_t st = (size_t) n_var(h) * CHARM_GPU_BASIS * h->E * sizeof(double);
+    const size_t st = (size_t) n_var(h) * h->nb * h->E * sizeof(double);
     CUDA_TRY(cudaMemcpyAsync(h->d_u, u, st, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
     if (h->cfg.precision == CHARM_GPU_PREC_MIXED) {
         int rc = ff_convert(h, true);
@@ -984,7 +1145,7 @@ int charm_gpu_get_state(charm_gpu_handle_t h, double *u, int on_device)
     if (!h || !u) return fail(CHARM_GPU_EINVAL, "null argument");
     if (!h->mesh_ready) return fail(CHARM_GPU_ESTATE, "no mesh uploaded");
     CUDA_TRY(cudaSetDevice(h->device));
-    const size_t st = (size_t) n_var(h) * CHARM_GPU_BASIS * h->E * sizeof(double);
+    const size_t st = (size_t) n_var(h) * h->nb * h->E * sizeof(double);
     if (h->cfg.precision == CHARM_GPU_PREC_MIXED) {
         int rc = ff_convert(h, false);
         if (rc) return rc;
@@ -1048,7 +1209,12 @@ int charm_gpu_residual(charm_gpu_handle_t h, double *res, int on_device)
     if (!res) return fail(CHARM_GPU_EINVAL, "null argument");
     const bool mixed = h->cfg.precision == CHARM_GPU_PREC_MIXED;
     if (mixed && (rc = ff_convert(h, false))) return rc;   // d_u <- hi + lo
-    if (!mixed && h->cfg.model == CHARM_GPU_MODEL_NS && h->cfg.use_visc) {
+    if (h->nb == kNB2) {
+        switch (h->cfg.n_comp) {
+        case 1: rc = p2_stage<1>(h, h->d_u, nullptr, h->d_ua, 0, nullptr, 1, 0, kCellResidual); break;
+        default: rc = p2_stage<2>(h, h->d_u, nullptr, h->d_ua, 0, nullptr, 1, 0, kCellResidual); break;
+        }
+    } else if (!mixed && h->cfg.model == CHARM_GPU_MODEL_NS && h->cfg.use_visc) {
         // with the viscous terms (no chemistry outside a step: chem_rhs = 0)
         switch (h->cfg.n_comp) {
         case 1:
@@ -1070,7 +1236,7 @@ int charm_gpu_residual(charm_gpu_handle_t h, double *res, int on_device)
     default: return fail(CHARM_GPU_ENOTSUP, "species count not instantiated");
     }
     if (rc) return rc;
-    const size_t st = (size_t) n_var(h) * CHARM_GPU_BASIS * h->E * sizeof(double);
+    const size_t st = (size_t) n_var(h) * h->nb * h->E * sizeof(double);
     CUDA_TRY(cudaMemcpyAsync(res, h->d_ua, st, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     return CHARM_GPU_OK;
@@ -1081,7 +1247,7 @@ int charm_gpu_limit(charm_gpu_handle_t h)
     int rc = check_ready(h);
     if (rc) return rc;
     if (h->cfg.limiter != CHARM_GPU_LIM_BJ) return CHARM_GPU_OK;
-    const size_t st = (size_t) n_var(h) * CHARM_GPU_BASIS * h->E * sizeof(double);
+    const size_t st = (size_t) n_var(h) * h->nb * h->E * sizeof(double);
     const bool mixed = h->cfg.precision == CHARM_GPU_PREC_MIXED;
     if (mixed && (rc = ff_convert(h, false))) return rc;   // d_u <- hi + lo
     CUDA_TRY(cudaMemcpyAsync(h->d_ua, h->d_u, st, cudaMemcpyDeviceToDevice, h->stream));
@@ -1098,6 +1264,7 @@ int charm_gpu_refine_flags(charm_gpu_handle_t h, double max_err, int8_t *flags, 
 {
     int rc = check_ready(h);
     if (rc) return rc;
+    if (h->nb != CHARM_GPU_BASIS) return fail(CHARM_GPU_ENOTSUP, "refine flags: p1 only");
     if (!flags && !grad_out) return fail(CHARM_GPU_EINVAL, "null argument");
     if (h->cfg.precision == CHARM_GPU_PREC_MIXED && (rc = ff_convert(h, false))) return rc;   // d_u <- hi + lo
     // the gradient goes through the (idle) slot buffer: 3*E doubles fit in it
@@ -1266,7 +1433,7 @@ int charm_gpu_dims(charm_gpu_handle_t h, int64_t *n_elem, int *nv, int *nb)
     if (!h) return fail(CHARM_GPU_EINVAL, "null handle");
     if (n_elem) *n_elem = h->E;
     if (nv) *nv = n_var(h);
-    if (nb) *nb = CHARM_GPU_BASIS;
+    if (nb) *nb = h->nb;
     return CHARM_GPU_OK;
 }
 
@@ -1477,7 +1644,7 @@ extern "C" int charm_gpu_residual_static(const charm_gpu_config_t *cfg, const ch
 {
     if (!cfg || !mesh || !u || !res) return fail(CHARM_GPU_EINVAL, "null argument");
     if (cfg->n_comp < 1 || cfg->n_comp > 2) return fail(CHARM_GPU_ENOTSUP, "1 or 2 species only");
-    if (cfg->flux < 0 || cfg->flux > 3 || cfg->n_bnd < 0 || cfg->n_bnd > CHARM_GPU_MAX_BND || cfg->use_visc ||
+    if (cfg->flux < 0 || cfg->flux > 3 || cfg->n_bnd < 0 || cfg->n_bnd > CHARM_GPU_MAX_BND || cfg->use_visc || cfg->p_order == 2 ||
         (cfg->precision != CHARM_GPU_PREC_FP64 && cfg->precision != CHARM_GPU_PREC_MIXED) ||
         (cfg->eos != CHARM_GPU_EOS_IDEAL && cfg->eos != CHARM_GPU_EOS_MIX))
         return fail(CHARM_GPU_EINVAL, "invalid configuration");

@@ -200,7 +200,8 @@ chem_kernel(MeshDev m, const double *__restrict__ u, double *__restrict__ out, d
 // ---------------------------------------------------------------------------
 // species diffusion coefficients (charm_model_ns_diff.c:18-71)
 // ---------------------------------------------------------------------------
-template <int NC>
+// NBK: basis functions per variable (4 or 10); the centre value is c_0 for both
+template <int NC, int NBK = kNB>
 __global__ void __launch_bounds__(128) diffcoef_kernel(MeshDev m, const double *__restrict__ u, double *__restrict__ dif)
 {
     constexpr int V = 4 + NC;
@@ -209,7 +210,7 @@ __global__ void __launch_bounds__(128) diffcoef_kernel(MeshDev m, const double *
     if (e >= E) return;
     double U[V];
 #pragma unroll
-    for (int v = 0; v < V; v++) U[v] = __ldg(u + (int64_t) (v * kNB) * E + e);   // centre value = c_0
+    for (int v = 0; v < V; v++) U[v] = __ldg(u + (int64_t) (v * NBK) * E + e);   // centre value = c_0
     Prim<double, NC> p;
     cons_to_prim<double, NC>(U, p);
     const double pabs = p.p / 101325.0;
