@@ -393,16 +393,11 @@ def run_adjoint(args, device: int) -> dict:
                                       "noise's variable and coefficient)"}}
 
 
-def run_flame(args, device: int) -> dict:
-    """Reacting 2-species Navier-Stokes (viscous terms, species diffusion,
-    Arrhenius chemistry every stage), FP64, p1: DOF-updates/s of the step."""
-    from charm_3d_gb300 import synthetic
-    from charm_3d_gb300.solver import Forest, Solver
-    case = synthetic("flame", level=args.flame_level, p_order=args.flame_order)
-    case.precision = "FP64"
-    mesh = Forest(case).flatten()
-    u0 = case.initial_state(mesh.center)
-    E, V = mesh.n_elem, case.n_var
+def _flame_run(case, mesh, u0, steps: int, device: int, precision: str):
+    """Warm-up, then `steps` timed steps (CUDA events on the solver's stream)
+    from u0; returns (ms, per-class kernel ms, final state)."""
+    from charm_3d_gb300.solver import Solver
+    case.precision = precision
     gpu = Solver(case, device)
     gpu.upload(mesh)
     gpu.set_state(u0)
@@ -411,22 +406,68 @@ def run_flame(args, device: int) -> dict:
     gpu.set_state(u0)
     gpu.reset_stats()
     gpu.set_timing(True)
-    ms = gpu.time_run(args.flame_steps, case.tau)
+    ms = gpu.time_run(steps, case.tau)
     gpu.set_timing(False)
-    launches, kms = gpu.kernel_stats()
+    _, kms = gpu.kernel_stats()
     u = gpu.get_state()
     gpu.close()
-    B = case.n_basis
-    return {"workload": f"reacting 2-species NS, unit cube level {args.flame_level} ({E} hex), p{args.flame_order} "
-                        f"({B} basis functions, {'27/9' if B == 10 else '8/6'}-point rules), HLLC, MIX EOS, "
-                        f"Sutherland mu/kappa, species diffusion, A->B Arrhenius, FP64",
-            "value": E * V * B * STAGES * args.flame_steps / (ms * 1e-3), "unit": UNIT,
-            "ms_per_step": ms / args.flame_steps, "steps": args.flame_steps,
-            "kernel_share": {n: float(kms[i] / kms.sum()) for i, n in
-                             enumerate(["face (convective + viscous)", "cell", "limiter",
-                                        "chemistry, diffusion coefficients, lifting, viscous volume"])},
-            "finite": bool(np.isfinite(u).all()),
-            "mixed": "not built for the viscous/reacting terms (FP64 only)"}
+    return ms, kms, u
+
+
+def run_flame(args, device: int) -> dict:
+    """Reacting 2-species Navier-Stokes (viscous terms, species diffusion,
+    Arrhenius chemistry every stage): DOF-updates/s of the FP64 step and of
+    the mixed form (p2 only), the mixed form's error against FP64."""
+    from charm_3d_gb300 import synthetic
+    from charm_3d_gb300.solver import Forest
+    case = synthetic("flame", level=args.flame_level, p_order=args.flame_order)
+    mesh = Forest(case).flatten()
+    u0 = case.initial_state(mesh.center)
+    E, V, B = mesh.n_elem, case.n_var, case.n_basis
+    dofs = E * V * B * STAGES * args.flame_steps
+    ms, kms, u = _flame_run(case, mesh, u0, args.flame_steps, device, "FP64")
+    names = ["face (convective + viscous)", "cell", "limiter", "chemistry, diffusion coefficients, lifting, viscous volume"]
+    out = {"workload": f"reacting 2-species NS, unit cube level {args.flame_level} ({E} hex), p{args.flame_order} "
+                       f"({B} basis functions, {'27/9' if B == 10 else '8/6'}-point rules), HLLC, MIX EOS, "
+                       f"Sutherland mu/kappa, species diffusion, A->B Arrhenius",
+           "value": dofs / (ms * 1e-3), "unit": UNIT, "dtype": "f64",
+           "ms_per_step": ms / args.flame_steps, "steps": args.flame_steps,
+           "kernel_share": {n: float(kms[i] / kms.sum()) for i, n in enumerate(names)},
+           "finite": bool(np.isfinite(u).all())}
+    if B != 10:
+        out["mixed"] = "not built for the viscous/reacting terms at p1 (FP64 only)"
+        return out
+    ms32, kms32, u32 = _flame_run(case, mesh, u0, args.flame_steps, device, "MIXED")
+    rho = lambda x: x[4:V].sum(axis=0)
+    # reference-box mass matrix of the 10 Taylor functions (3-point Gauss per
+    # axis): the L2 norm of a p2 field on the uniform mesh is sqrt(sum c^T M c)
+    gx, gw = np.array([-0.5 * np.sqrt(0.6), 0.0, 0.5 * np.sqrt(0.6)]), np.array([5.0, 8.0, 5.0]) / 18.0
+    X, Y, Z = [a.ravel() for a in np.meshgrid(gx, gx, gx, indexing="ij")]
+    W = (gw[:, None, None] * gw[None, :, None] * gw[None, None, :]).ravel()
+    P = np.stack([np.ones_like(X), X, Y, Z, X * X, Y * Y, Z * Z, X * Y, X * Z, Y * Z])
+    M = (P * W) @ P.T
+
+    def field_l2(a, b):
+        d, r = (a - b).reshape(-1, B, E), b.reshape(-1, B, E)
+        return float(np.sqrt(np.einsum("vke,kl,vle->", d, M, d) / np.einsum("vke,kl,vle->", r, M, r)))
+
+    def mass(x):   # cell mean of a p2 field on a box: c0 + (c4 + c5 + c6) / 12
+        vol = np.prod([mesh.tree_len[d] * 2.0 ** (-mesh.level.astype(np.float64)) for d in range(3)], axis=0)
+        r = rho(x)
+        return float((vol * (r[0] + (r[4] + r[5] + r[6]) / 12.0)).sum())
+
+    out["mixed"] = {"dtype": "f32 residual, f32 hi/lo state, f64 chemistry",
+                    "value": dofs / (ms32 * 1e-3), "ms_per_step": ms32 / args.flame_steps,
+                    "speedup_vs_fp64": ms / ms32,
+                    "kernel_share": {n: float(kms32[i] / kms32.sum()) for i, n in enumerate(names)},
+                    "rel_l2_density_vs_fp64": field_l2(rho(u32), rho(u)),
+                    "rel_l2_state_vs_fp64": field_l2(u32, u),
+                    "norm": "L2 of the fields over the domain (coefficients weighted by the mass matrix)",
+                    "rel_l2_density_coefficients_vs_fp64": float(np.linalg.norm(rho(u32) - rho(u)) /
+                                                                 np.linalg.norm(rho(u))),
+                    "total_mass_vs_fp64": abs(mass(u32) - mass(u)) / mass(u),
+                    "finite": bool(np.isfinite(u32).all())}
+    return out
 
 
 def _blast_run(case, steps: int, device: int, precision: str):

@@ -26,7 +26,7 @@
 #include "dg_kernels.cuh"
 #include "dg_adjoint.cuh"
 #include "dg_visc.cuh"
-#include "dg_p2.cuh"
+#include "dg_launch.h"
 
 using namespace charm;
 
@@ -181,7 +181,6 @@ int validate_config(const charm_gpu_config_t *c)
             return fail(CHARM_GPU_EINVAL, "unknown boundary type");
     if (c->p_order < 0 || c->p_order > 2) return fail(CHARM_GPU_EINVAL, "p_order must be 1 or 2");
     if (c->p_order == 2) {
-        if (c->precision != CHARM_GPU_PREC_FP64) return fail(CHARM_GPU_ENOTSUP, "p2: FP64 precision only");
         if (c->limiter != CHARM_GPU_LIM_NONE) return fail(CHARM_GPU_ENOTSUP, "p2: limiter not supported");
         if (c->dt_mode != CHARM_GPU_DT_TAU) return fail(CHARM_GPU_ENOTSUP, "p2: fixed time step (TAU) only");
     }
@@ -191,8 +190,8 @@ int validate_config(const charm_gpu_config_t *c)
             if (c->react[r].left[k] < -1 || c->react[r].left[k] >= c->n_comp || c->react[r].right[k] < -1 ||
                 c->react[r].right[k] >= c->n_comp)
                 return fail(CHARM_GPU_EINVAL, "reaction component index out of range");
-    if ((c->use_visc || c->n_react) && c->precision != CHARM_GPU_PREC_FP64)
-        return fail(CHARM_GPU_ENOTSUP, "viscous terms and reactions: FP64 precision only");
+    if ((c->use_visc || c->n_react) && c->precision != CHARM_GPU_PREC_FP64 && c->p_order != 2)
+        return fail(CHARM_GPU_ENOTSUP, "viscous terms and reactions in the mixed form: p2 basis only");
     if (c->dt_mode != CHARM_GPU_DT_TAU && c->dt_mode != CHARM_GPU_DT_CFL)
         return fail(CHARM_GPU_EINVAL, "unknown dt mode");
     return CHARM_GPU_OK;
@@ -255,6 +254,10 @@ void build_devcfg(const charm_gpu_config_t *c, DevCfg *d)
             d->comp_hc[i][k] = c->comp[i].cp[k] / (k + 1);
             d->comp_href[i] += c->comp[i].cp[k] * pow(c->t_ref, k + 1) / (k + 1);
         }
+        d->comp_ml0_f[i] = (float) d->comp_ml0[i]; d->comp_kp0_f[i] = (float) d->comp_kp0[i];
+        d->comp_t0_f[i] = (float) d->comp_t0[i]; d->comp_ts_f[i] = (float) d->comp_ts[i];
+        for (int k = 0; k < CHARM_GPU_MAX_CP; k++) d->comp_hc_f[i][k] = (float) d->comp_hc[i][k];
+        d->comp_hoff_f[i] = (float) (d->comp_h0[i] - d->comp_href[i]);
     }
     for (int r = 0; r < c->n_react; r++) {
         for (int k = 0; k < 3; k++) { d->react_l[r][k] = c->react[r].left[k]; d->react_r[r][k] = c->react[r].right[k]; }
@@ -266,6 +269,7 @@ int ensure_cfg(charm_gpu_handle_s *h)
 {
     if (g_cfg_owner == h) return CHARM_GPU_OK;
     CUDA_TRY(cudaMemcpyToSymbolAsync(c_cfg, &h->dcfg, sizeof(DevCfg), 0, cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(p2_upload_cfg(&h->dcfg, h->stream));
     g_cfg_owner = h;
     return CHARM_GPU_OK;
 }
@@ -419,7 +423,7 @@ int launch_cfl(charm_gpu_handle_s *h, const double *u)
 // rule, exact for the quadratic basis, inverted by Gauss-Jordan).
 int upload_p2_tables(charm_gpu_handle_s *h)
 {
-    P2Tab t;
+    P2TabT<double> t;
     memset(&t, 0, sizeof(t));
     const double gx[3] = {-0.5 * sqrt(0.6), 0.0, 0.5 * sqrt(0.6)};
     const double gw[3] = {5.0 / 18.0, 8.0 / 18.0, 5.0 / 18.0};
@@ -442,6 +446,15 @@ int upload_p2_tables(charm_gpu_handle_s *h)
             for (int j = 0; j < kNB2; j++) a[i][j] += t.cw[q] * ph[i] * ph[j];
         }
     }
+    // odd moments vanish on the symmetric rule: keep them exact zeros, so that
+    // M^-1 is exactly block-structured ({0, 4, 5, 6} coupled, the rest diagonal)
+    auto coupled = [](int i, int j) {
+        const bool bi = (i == 0 || (i >= 4 && i <= 6)), bj = (j == 0 || (j >= 4 && j <= 6));
+        return i == j || (bi && bj);
+    };
+    for (int i = 0; i < kNB2; i++)
+        for (int j = 0; j < kNB2; j++)
+            if (!coupled(i, j)) a[i][j] = 0.0;
     for (int i = 0; i < kNB2; i++) a[i][kNB2 + i] = 1.0;
     for (int c = 0; c < kNB2; c++) {   // Gauss-Jordan, partial pivoting
         int piv = c;
@@ -458,105 +471,120 @@ int upload_p2_tables(charm_gpu_handle_s *h)
         }
     }
     for (int i = 0; i < kNB2; i++)
-        for (int j = 0; j < kNB2; j++) t.minv[i][j] = a[i][kNB2 + j];
-    CUDA_TRY(cudaMemcpyToSymbol(c_p2, &t, sizeof(t)));
+        for (int j = 0; j < kNB2; j++) t.minv[i][j] = coupled(i, j) ? a[i][kNB2 + j] : 0.0;
+    P2TabT<float> tf;
+    for (int i = 0; i < 27; i++) {
+        for (int k = 0; k < 3; k++) tf.cxi[i][k] = (float) t.cxi[i][k];
+        tf.cw[i] = (float) t.cw[i];
+    }
+    for (int i = 0; i < 9; i++) {
+        for (int k = 0; k < 2; k++) tf.fxi[i][k] = (float) t.fxi[i][k];
+        tf.fw[i] = (float) t.fw[i];
+    }
+    for (int i = 0; i < kNB2; i++) {
+        for (int j = 0; j < kNB2; j++) tf.minv[i][j] = (float) t.minv[i][j];
+        tf.mean[i] = (float) t.mean[i];
+    }
+    CUDA_TRY(p2_upload_tables(t, tf));
     return CHARM_GPU_OK;
 }
 
-template <int NC>
-int launch_p2_face(charm_gpu_handle_s *h, const double *u)
+// p2 launchers, for T = double (FP64 form) and T = float (mixed form: u is
+// the hi plane; the slot, lifting and volume-term buffers hold T).  The
+// kernels are in charm_p2.cu.
+template <typename T, int NC>
+int launch_p2_face(charm_gpu_handle_s *h, const T *u)
 {
-    MeshDev m = mesh_view(h);
     const int bs = 128;
     const int64_t nbi = (h->F + bs - 1) / bs, nbb = (h->Fb + bs - 1) / bs;
     if (nbi + nbb == 0) return CHARM_GPU_OK;
-    double *slots = static_cast<double *>(h->d_slots);
-    const unsigned nb = (unsigned) (nbi + nbb);
     TimedLaunch t;
     begin_launch(h, 0, &t);
-    switch (h->cfg.flux) {
-    case CHARM_GPU_FLUX_LF: p2_face_kernel<NC, CHARM_GPU_FLUX_LF><<<nb, bs, 0, h->stream>>>(m, u, slots, nbi, h->d_err); break;
-    case CHARM_GPU_FLUX_HLLC: p2_face_kernel<NC, CHARM_GPU_FLUX_HLLC><<<nb, bs, 0, h->stream>>>(m, u, slots, nbi, h->d_err); break;
-    case CHARM_GPU_FLUX_CD: p2_face_kernel<NC, CHARM_GPU_FLUX_CD><<<nb, bs, 0, h->stream>>>(m, u, slots, nbi, h->d_err); break;
-    default: p2_face_kernel<NC, CHARM_GPU_FLUX_GODUNOV><<<nb, bs, 0, h->stream>>>(m, u, slots, nbi, h->d_err); break;
-    }
+    p2_launch_face<T, NC>(h->cfg.flux, mesh_view(h), u, static_cast<T *>(h->d_slots), nbi, (unsigned) (nbi + nbb),
+                          h->d_err, h->stream);
     end_launch(h, &t);
     CUDA_TRY(cudaGetLastError());
     return CHARM_GPU_OK;
 }
 
-template <int NC>
-int launch_p2_cell(charm_gpu_handle_s *h, const double *u, const double *u0, double *out, double dt,
-                   const double *dt_dev, double a_new, double a_old, int mode, const double *radd)
+template <typename T, int NC>
+int launch_p2_cell(charm_gpu_handle_s *h, const T *u, const T *u0, T *out, const P2Upd &up, const T *radd)
 {
-    MeshDev m = mesh_view(h);
-    const int bs = 128;
     TimedLaunch t;
     begin_launch(h, 1, &t);
-    p2_cell_kernel<NC><<<(unsigned) ((h->E + bs - 1) / bs), bs, 0, h->stream>>>(
-        m, u, static_cast<const double *>(h->d_slots), u0, out, dt, dt_dev, a_new, a_old, mode, h->d_err, radd);
+    p2_launch_cell<T, NC>(mesh_view(h), u, static_cast<const T *>(h->d_slots), u0, out, up, h->d_err, radd, h->stream);
     end_launch(h, &t);
     CUDA_TRY(cudaGetLastError());
     return CHARM_GPU_OK;
 }
 
-// chemistry, lifting and viscous volume terms of the p2 stage state
-template <int NC>
-int launch_p2_visc_chem(charm_gpu_handle_s *h, const double **u, const double **radd, bool chem)
+// chemistry of the stage state (FP64 from the state S) -> h->d_uc, chem_rhs
+template <typename S, int NC>
+int launch_p2_chem(charm_gpu_handle_s *h, StIn<S> in, StOut<S> out)
 {
-    MeshDev m = mesh_view(h);
+    TimedLaunch t;
+    begin_launch(h, 3, &t);
+    p2_launch_chem<S, NC>(mesh_view(h), in, out, h->d_chem_rhs, h->stream);
+    end_launch(h, &t);
+    CUDA_TRY(cudaGetLastError());
+    return CHARM_GPU_OK;
+}
+
+// diffusion coefficients, lifting and the viscous volume terms -> h->d_radd
+// (u_lo: the lo plane in the mixed form, for the FP64 diffusion coefficients)
+template <typename T, int NC>
+int launch_p2_visc(charm_gpu_handle_s *h, const T *u, const float *u_lo, const double *chem_rhs)
+{
     const int bs = 128;
-    const int64_t nbe = (h->E + bs - 1) / bs;
     const int64_t nbi = (h->F + bs - 1) / bs, nbb = (h->Fb + bs - 1) / bs;
     TimedLaunch t;
     begin_launch(h, 3, &t);
-    if (chem && h->cfg.n_react) {
-        p2_chem_kernel<NC><<<(unsigned) nbe, bs, 0, h->stream>>>(m, *u, h->d_uc, h->d_chem_rhs);
-        *u = h->d_uc;
-    }
-    if (h->cfg.use_visc) {
-        if (h->cfg.use_diff && NC >= 2)
-            diffcoef_kernel<NC, kNB2><<<(unsigned) nbe, bs, 0, h->stream>>>(m, *u, h->d_dif);
-        if (nbi + nbb)
-            p2_vgrad_face_kernel<NC><<<(unsigned) (nbi + nbb), bs, 0, h->stream>>>(m, *u, h->d_dif, h->d_s9, nbi);
-        p2_vgrad_cell_kernel<NC><<<(unsigned) nbe, bs, 0, h->stream>>>(m, *u, h->d_dif, h->d_s9, h->d_vis);
-        p2_vvol_kernel<NC><<<(unsigned) nbe, bs, 0, h->stream>>>(m, *u, h->d_vis, chem ? h->d_chem_rhs : nullptr,
-                                                                  h->d_radd);
-        *radd = h->d_radd;
-    }
+    p2_launch_visc<T, NC>(mesh_view(h), h->cfg.use_diff != 0, u, u_lo, reinterpret_cast<T *>(h->d_dif),
+                          reinterpret_cast<T *>(h->d_s9), reinterpret_cast<T *>(h->d_vis), chem_rhs,
+                          reinterpret_cast<T *>(h->d_radd), nbi, (unsigned) (nbi + nbb), h->stream);
     end_launch(h, &t);
     CUDA_TRY(cudaGetLastError());
     return CHARM_GPU_OK;
 }
 
-template <int NC>
-int launch_p2_vflux(charm_gpu_handle_s *h, const double *u)
+template <typename T, int NC>
+int launch_p2_vflux(charm_gpu_handle_s *h, const T *u)
 {
-    MeshDev m = mesh_view(h);
     const int bs = 128;
     const int64_t nbi = (h->F + bs - 1) / bs, nbb = (h->Fb + bs - 1) / bs;
     if (nbi + nbb == 0) return CHARM_GPU_OK;
     TimedLaunch t;
     begin_launch(h, 0, &t);
-    p2_vflux_face_kernel<NC><<<(unsigned) (nbi + nbb), bs, 0, h->stream>>>(m, u, h->d_vis,
-                                                                          static_cast<double *>(h->d_slots), nbi);
+    p2_launch_vflux<T, NC>(mesh_view(h), u, reinterpret_cast<const T *>(h->d_vis), static_cast<T *>(h->d_slots), nbi,
+                           (unsigned) (nbi + nbb), h->stream);
     end_launch(h, &t);
     CUDA_TRY(cudaGetLastError());
     return CHARM_GPU_OK;
 }
 
-// one p2 stage (or, with mode kCellResidual and no chemistry, the residual)
+// one FP64 p2 stage (or, with mode kCellResidual, the residual without chemistry)
 template <int NC>
 int p2_stage(charm_gpu_handle_s *h, const double *u, const double *u0, double *out, double dt, const double *dt_dev,
              double a_new, double a_old, int mode)
 {
     int rc;
     const double *radd = nullptr;
-    const bool model_ns = h->cfg.model == CHARM_GPU_MODEL_NS;
-    if (model_ns && (rc = launch_p2_visc_chem<NC>(h, &u, &radd, mode == kCellUpdate))) return rc;
-    if ((rc = launch_p2_face<NC>(h, u))) return rc;
-    if (radd && (rc = launch_p2_vflux<NC>(h, u))) return rc;
-    return launch_p2_cell<NC>(h, u, u0, out, dt, dt_dev, a_new, a_old, mode, radd);
+    const bool upd = mode == kCellUpdate;
+    if (h->cfg.model == CHARM_GPU_MODEL_NS) {
+        if (upd && h->cfg.n_react) {
+            if ((rc = launch_p2_chem<double, NC>(h, StIn<double>{u}, StOut<double>{h->d_uc}))) return rc;
+            u = h->d_uc;   // the residual and the update act on the state after chemistry
+        }
+        if (h->cfg.use_visc) {
+            if ((rc = launch_p2_visc<double, NC>(h, u, nullptr, upd ? h->d_chem_rhs : nullptr))) return rc;
+            radd = h->d_radd;
+        }
+    }
+    if ((rc = launch_p2_face<double, NC>(h, u))) return rc;
+    if (radd && (rc = launch_p2_vflux<double, NC>(h, u))) return rc;
+    P2Upd up{};
+    up.dt = dt; up.a_new = a_new; up.a_old = a_old; up.dt_dev = dt_dev; up.mode = mode;
+    return launch_p2_cell<double, NC>(h, u, u0, out, up, radd);
 }
 
 // ---- viscous terms and chemistry (charm_model_ns_timestep_single's stage,
@@ -592,7 +620,7 @@ int launch_visc(charm_gpu_handle_s *h, const double *u, const double *chem_rhs)
     TimedLaunch t;
     begin_launch(h, 3, &t);
     if (h->cfg.use_diff && NC >= 2)
-        diffcoef_kernel<NC><<<(unsigned) nbe, bs, 0, h->stream>>>(m, u, h->d_dif);
+        diffcoef_kernel<NC, kNB, double, double><<<(unsigned) nbe, bs, 0, h->stream>>>(m, StIn<double>{u}, h->d_dif);
     if (nbi + nbb) vgrad_face_kernel<NC><<<(unsigned) (nbi + nbb), bs, 0, h->stream>>>(m, u, h->d_dif, h->d_s9, nbi);
     vgrad_cell_kernel<NC><<<(unsigned) nbe, bs, 0, h->stream>>>(m, u, h->d_dif, h->d_s9, h->d_vis);
     vvol_kernel<NC><<<(unsigned) nbe, bs, 0, h->stream>>>(m, u, h->d_vis, chem_rhs, h->d_radd);
@@ -700,6 +728,40 @@ FFCoef ff_split(double x)
     return {hi, (float) (x - (double) hi)};
 }
 
+// One p2 stage of the mixed form on hi/lo buffers: out = a*(in - dt*M^-1*R) +
+// b*u0 (u0 < 0: no combination), FP32 residual; chemistry in FP64 on hi + lo
+// into d_uc (hi plane, then lo plane).  mode kCellResidual writes R (FP32)
+// into the hi plane of out.
+template <int NC>
+int p2_ff_stage(charm_gpu_handle_s *h, int in, int u0, int out, FFCoef dt, FFCoef a, FFCoef b, int mode)
+{
+    int rc;
+    const float *uh = h->d_fh[in], *ul = h->d_fl[in];
+    const float *radd = nullptr;
+    const bool upd = mode == kCellUpdate;
+    if (h->cfg.model == CHARM_GPU_MODEL_NS) {
+        if (upd && h->cfg.n_react) {
+            float *ch = reinterpret_cast<float *>(h->d_uc), *cl = ch + n_state(h);
+            if ((rc = launch_p2_chem<float, NC>(h, StIn<float>{uh, ul}, StOut<float>{ch, cl}))) return rc;
+            uh = ch;
+            ul = cl;
+        }
+        if (h->cfg.use_visc) {
+            if ((rc = launch_p2_visc<float, NC>(h, uh, ul, upd ? h->d_chem_rhs : nullptr))) return rc;
+            radd = reinterpret_cast<const float *>(h->d_radd);
+        }
+    }
+    if ((rc = launch_p2_face<float, NC>(h, uh))) return rc;
+    if (radd && (rc = launch_p2_vflux<float, NC>(h, uh))) return rc;
+    P2Upd up{};
+    up.mode = mode;
+    up.u_lo = ul;
+    up.u0_lo = (u0 >= 0) ? h->d_fl[u0] : nullptr;
+    up.out_lo = h->d_fl[out];
+    up.dt_h = dt.h; up.dt_l = dt.l; up.a_h = a.h; up.a_l = a.l; up.b_h = b.h; up.b_l = b.l;
+    return launch_p2_cell<float, NC>(h, uh, (u0 >= 0) ? h->d_fh[u0] : nullptr, h->d_fh[out], up, radd);
+}
+
 template <int NC, int FLUX>
 int launch_tile_stage(charm_gpu_handle_s *h, int in, int u0, int out, FFCoef dt, const double *dt_dev, FFCoef a,
                       FFCoef b, bool comb)
@@ -784,6 +846,7 @@ int ff_stage(charm_gpu_handle_s *h, int in, int u0, int out, FFCoef dt, const do
 {
     const FFCoef one = {1.f, 0.f}, zero = {0.f, 0.f};
     int rc;
+    if (h->nb == kNB2) return p2_ff_stage<NC>(h, in, comb ? u0 : -1, out, dt, a, b, kCellUpdate);   // fixed dt only
     if (h->cfg.limiter == CHARM_GPU_LIM_BJ) {
         // ua (1) holds the updated stage value before the limiter
         if ((rc = launch_ff_stage<NC>(h, in, -1, 1, dt, dt_dev, one, zero, false))) return rc;
@@ -1209,7 +1272,17 @@ int charm_gpu_residual(charm_gpu_handle_t h, double *res, int on_device)
     if (!res) return fail(CHARM_GPU_EINVAL, "null argument");
     const bool mixed = h->cfg.precision == CHARM_GPU_PREC_MIXED;
     if (mixed && (rc = ff_convert(h, false))) return rc;   // d_u <- hi + lo
-    if (h->nb == kNB2) {
+    if (h->nb == kNB2 && mixed) {
+        // FP32 residual into the hi plane of buffer 1, widened into d_ua
+        const FFCoef z = {0.f, 0.f}, one = {1.f, 0.f};
+        rc = (h->cfg.n_comp == 1) ? p2_ff_stage<1>(h, 0, -1, 1, z, one, z, kCellResidual)
+                                  : p2_ff_stage<2>(h, 0, -1, 1, z, one, z, kCellResidual);
+        if (rc) return rc;
+        const int64_t n = n_state(h);
+        CUDA_TRY(cudaMemsetAsync(h->d_fl[1], 0, n * sizeof(float), h->stream));
+        ff_to_double_kernel<<<(unsigned) ((n + 255) / 256), 256, 0, h->stream>>>(h->d_fh[1], h->d_fl[1], h->d_ua, n);
+        CUDA_TRY(cudaGetLastError());
+    } else if (h->nb == kNB2) {
         switch (h->cfg.n_comp) {
         case 1: rc = p2_stage<1>(h, h->d_u, nullptr, h->d_ua, 0, nullptr, 1, 0, kCellResidual); break;
         default: rc = p2_stage<2>(h, h->d_u, nullptr, h->d_ua, 0, nullptr, 1, 0, kCellResidual); break;

@@ -28,8 +28,10 @@ constexpr double kEps = 1.e-12;
 enum : unsigned { kErrNonFinite = 1u, kErrNegative = 2u, kErrHllc = 4u };
 
 // Configuration in constant memory (one solver configuration per process at
-// a time; the host re-uploads it when it launches for another handle).  All
-// device code lives in one translation unit, which defines c_cfg here.
+// a time; the host re-uploads it when it launches for another handle).  The
+// kernels are compiled in several translation units; each holds its own copy
+// of c_cfg (static), which the host uploads through that unit's upload
+// function (charm_gpu.cu: ensure_cfg).
 struct DevCfg {
     int    n_comp;
     int    eos;            // CHARM_GPU_EOS_*
@@ -64,9 +66,13 @@ struct DevCfg {
     double comp_href[kMaxComp];         // sum cp_k t_ref^(k+1) / (k + 1)
     int    react_l[CHARM_GPU_MAX_REACT][3], react_r[CHARM_GPU_MAX_REACT][3];
     double react_a[CHARM_GPU_MAX_REACT], react_e[CHARM_GPU_MAX_REACT], react_n[CHARM_GPU_MAX_REACT];
+    // FP32 mirrors of the viscous constants (mixed form of the p2 kernels);
+    // comp_hoff_f = h0 - H(t_ref) rounded once
+    float  comp_ml0_f[kMaxComp], comp_kp0_f[kMaxComp], comp_t0_f[kMaxComp], comp_ts_f[kMaxComp];
+    float  comp_hc_f[kMaxComp][kMaxCp], comp_hoff_f[kMaxComp];
 };
 
-__constant__ DevCfg c_cfg;
+static __constant__ DevCfg c_cfg;
 
 // Constant of the configuration in the arithmetic type T: the double for
 // T = double, its float mirror for T = float.

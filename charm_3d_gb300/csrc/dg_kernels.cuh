@@ -33,12 +33,12 @@ namespace charm {
 // Face quadrature: two triangles x 3 points, weights 1/6, jacobian
 // 2*area(triangle) (reference src/charm_geom.c:443-494).  In face-local
 // coordinates (s, t) on [0,1]^2, s = the lower tangential axis:
-__constant__ double c_face_s[6] = {1.0 / 6.0, 2.0 / 3.0, 1.0 / 6.0, 5.0 / 6.0, 1.0 / 3.0, 5.0 / 6.0};
-__constant__ double c_face_t[6] = {1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0, 1.0 / 3.0, 5.0 / 6.0, 5.0 / 6.0};
+static __constant__ double c_face_s[6] = {1.0 / 6.0, 2.0 / 3.0, 1.0 / 6.0, 5.0 / 6.0, 1.0 / 3.0, 5.0 / 6.0};
+static __constant__ double c_face_t[6] = {1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0, 1.0 / 3.0, 5.0 / 6.0, 5.0 / 6.0};
 // the same points as float basis values s - 1/2, t - 1/2 (FP32 paths)
-__constant__ float c_face_psf[6] = {(float) (1.0 / 6.0 - 0.5), (float) (2.0 / 3.0 - 0.5), (float) (1.0 / 6.0 - 0.5),
+static __constant__ float c_face_psf[6] = {(float) (1.0 / 6.0 - 0.5), (float) (2.0 / 3.0 - 0.5), (float) (1.0 / 6.0 - 0.5),
                                     (float) (5.0 / 6.0 - 0.5), (float) (1.0 / 3.0 - 0.5), (float) (5.0 / 6.0 - 0.5)};
-__constant__ float c_face_ptf[6] = {(float) (1.0 / 6.0 - 0.5), (float) (1.0 / 6.0 - 0.5), (float) (2.0 / 3.0 - 0.5),
+static __constant__ float c_face_ptf[6] = {(float) (1.0 / 6.0 - 0.5), (float) (1.0 / 6.0 - 0.5), (float) (2.0 / 3.0 - 0.5),
                                     (float) (1.0 / 3.0 - 0.5), (float) (5.0 / 6.0 - 0.5), (float) (5.0 / 6.0 - 0.5)};
 
 template <typename T>
@@ -635,7 +635,7 @@ __device__ __forceinline__ FF ff_comb(FF y, FF w, float ah, float al, float bh, 
     return ff_renorm(s.h, __fadd_rn(s.l, __fadd_rn(pe, qe)));
 }
 
-__global__ void __launch_bounds__(256) ff_from_double_kernel(const double *__restrict__ u, float *__restrict__ hi,
+static __global__ void __launch_bounds__(256) ff_from_double_kernel(const double *__restrict__ u, float *__restrict__ hi,
                                                              float *__restrict__ lo, int64_t n)
 {
     const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
@@ -646,7 +646,7 @@ __global__ void __launch_bounds__(256) ff_from_double_kernel(const double *__res
     lo[i] = __double2float_rn(x - (double) h);
 }
 
-__global__ void __launch_bounds__(256) ff_to_double_kernel(const float *__restrict__ hi, const float *__restrict__ lo,
+static __global__ void __launch_bounds__(256) ff_to_double_kernel(const float *__restrict__ hi, const float *__restrict__ lo,
                                                            double *__restrict__ u, int64_t n)
 {
     const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;

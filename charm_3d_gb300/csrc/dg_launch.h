@@ -1,0 +1,65 @@
+// Launchers of the kernel families compiled in their own translation units
+// (several units compile in parallel; the host code in charm_gpu.cu calls
+// these).  Each unit holds its own constant-memory configuration, uploaded
+// by its *_upload_cfg.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "dg_kernels.cuh"
+#include "dg_visc.cuh"
+
+namespace charm {
+
+// ---- p2 basis (charm_p2.cu) ------------------------------------------------
+
+constexpr int kNB2 = 10;
+
+// Rule tables and the inverse mass matrix of the reference box.
+template <typename T>
+struct P2TabT {
+    T cxi[27][3];        // cell points in reference coordinates, [-1/2, 1/2]^3, x fastest
+    T cw[27];            // cell weights, sum 1
+    T fxi[9][2];         // face points (lower, upper tangential axis), [-1/2, 1/2]^2
+    T fw[9];             // face weights, sum 1
+    T minv[kNB2][kNB2];  // inverse mass matrix of the reference box (volume 1)
+    T mean[kNB2];        // cell mean of each basis function
+};
+
+// Update arguments of the p2 cell kernel.  FP64 form: out = a_new*(u -
+// dt*M^-1*(R + radd)) + a_old*u0 with the doubles.  Mixed form: the state
+// pointers are the hi planes, the lo planes and the float-float splits of
+// dt, a_new and a_old come here, and u0 == nullptr means no combination.
+struct P2Upd {
+    double dt, a_new, a_old;
+    const double *dt_dev;
+    int mode;   // kCellUpdate, or kCellResidual: out = R + radd
+    const float *u_lo, *u0_lo;
+    float *out_lo;
+    float dt_h, dt_l, a_h, a_l, b_h, b_l;
+};
+
+cudaError_t p2_upload_cfg(const DevCfg *cfg, cudaStream_t st);
+cudaError_t p2_upload_tables(const P2TabT<double> &t, const P2TabT<float> &tf);
+
+// T = double (FP64 form) or float (mixed form; u is the hi plane).  nbi:
+// blocks of 128 over the interior faces, nb: all blocks (interior, boundary).
+template <typename T, int NC>
+void p2_launch_face(int flux, const MeshDev &m, const T *u, T *slots, int64_t nbi, unsigned nb, unsigned *err,
+                    cudaStream_t st);
+template <typename T, int NC>
+void p2_launch_cell(const MeshDev &m, const T *u, const T *slots, const T *u0, T *out, const P2Upd &up,
+                    unsigned *err, const T *radd, cudaStream_t st);
+template <typename S, int NC>
+void p2_launch_chem(const MeshDev &m, StIn<S> in, StOut<S> out, double *chem_rhs, cudaStream_t st);
+// diffusion coefficients (FP64 from the state; u_lo: the lo plane of the
+// mixed form), lifting and the viscous volume terms
+template <typename T, int NC>
+void p2_launch_visc(const MeshDev &m, bool diff, const T *u, const float *u_lo, T *dif, T *s9, T *vis,
+                    const double *chem_rhs, T *radd, int64_t nbi, unsigned nbf, cudaStream_t st);
+template <typename T, int NC>
+void p2_launch_vflux(const MeshDev &m, const T *u, const T *vis, T *slots, int64_t nbi, unsigned nb,
+                     cudaStream_t st);
+
+}  // namespace charm

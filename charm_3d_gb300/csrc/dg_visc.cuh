@@ -28,41 +28,47 @@ namespace charm {
 
 // Sutherland factor sqrt((t/t0)^3) (t0 + ts) / (t + ts) of component i
 // (charm_comp_calc_ml / _kp, src/charm_globals.c:651-676; (t/t0)^1.5 as
-// x sqrt(x), without pow)
-__device__ __forceinline__ double sutherland(int i, double t)
+// x sqrt(x), without pow).  T = float reads the FP32 mirrors.
+template <typename T>
+__device__ __forceinline__ T sutherland(int i, T t)
 {
-    const double x = t / c_cfg.comp_t0[i];
-    return x * sqrt(x) * (c_cfg.comp_t0[i] + c_cfg.comp_ts[i]) / (t + c_cfg.comp_ts[i]);
+    const T t0 = cfgv<T>(c_cfg.comp_t0[i], c_cfg.comp_t0_f[i]), ts = cfgv<T>(c_cfg.comp_ts[i], c_cfg.comp_ts_f[i]);
+    const T x = qdiv<T>(t, t0);
+    return qdiv<T>(x * qsqrt<T>(x) * (t0 + ts), t + ts);
 }
 
 // charm_comp_calc_enthalpy (:679-694): h0 + integral of the cp polynomial
 // from t_ref, here as h0 - H(t_ref) + H(t) with H(t) = sum cp_k t^(k+1)/(k+1)
-// by Horner (coefficients cp_k/(k+1) and H(t_ref) prepared on the host)
-__device__ __forceinline__ double comp_h(int i, double t)
+// by Horner (coefficients cp_k/(k+1) and H(t_ref) prepared on the host;
+// in FP32 h0 - H(t_ref) is one constant)
+template <typename T>
+__device__ __forceinline__ T comp_h(int i, T t)
 {
-    double x = 0.0;
-    for (int k = c_cfg.comp_ncp[i] - 1; k >= 0; k--) x = x * t + c_cfg.comp_hc[i][k];
-    return c_cfg.comp_h0[i] + (x * t - c_cfg.comp_href[i]);
+    T x = T(0);
+    for (int k = c_cfg.comp_ncp[i] - 1; k >= 0; k--) x = x * t + cfgv<T>(c_cfg.comp_hc[i][k], c_cfg.comp_hc_f[i][k]);
+    if constexpr (sizeof(T) == sizeof(float)) return c_cfg.comp_hoff_f[i] + x * t;
+    else return c_cfg.comp_h0[i] + (x * t - c_cfg.comp_href[i]);
 }
 
 // charm_get_visc_mu and charm_get_heat_k (:515-558) at one point, with one
 // Sutherland factor per component shared by mu and kappa (both laws use the
 // component's t0 and ts)
-template <int NC>
-__device__ __forceinline__ void transport(const Prim<double, NC> &p, double &mu, double &kt)
+template <int NC, typename T>
+__device__ __forceinline__ void transport(const Prim<T, NC> &p, T &mu, T &kt)
 {
-    double s = 0.0, m = 0.0, k = 0.0;
+    T s = T(0), m = T(0), k = T(0);
 #pragma unroll
     for (int i = 0; i < NC; i++) {
         const bool sm = c_cfg.comp_ml_type[i] == CHARM_GPU_LAW_SUTHERLAND;
         const bool sk = c_cfg.comp_kp_type[i] == CHARM_GPU_LAW_SUTHERLAND;
-        const double f = (sm || sk) ? sutherland(i, p.t) : 1.0;
-        const double cm = p.c[i] / c_cfg.comp_m[i];
+        const T f = (sm || sk) ? sutherland<T>(i, p.t) : T(1);
+        const T ml0 = cfgv<T>(c_cfg.comp_ml0[i], c_cfg.comp_ml0_f[i]), kp0 = cfgv<T>(c_cfg.comp_kp0[i], c_cfg.comp_kp0_f[i]);
+        const T cm = qdiv<T>(p.c[i], cfgv<T>(c_cfg.comp_m[i], c_cfg.comp_m_f[i]));
         s += cm;
-        m += cm * (sm ? c_cfg.comp_ml0[i] * f : c_cfg.comp_ml0[i]);
-        k += p.c[i] * (sk ? c_cfg.comp_kp0[i] * f : c_cfg.comp_kp0[i]);
+        m += cm * (sm ? ml0 * f : ml0);
+        k += p.c[i] * (sk ? kp0 * f : kp0);
     }
-    mu = m / s;
+    mu = qdiv<T>(m, s);
     kt = k;
 }
 
@@ -77,12 +83,12 @@ __device__ __forceinline__ double visc_mu(const Prim<double, NC> &p)
 // The 9 lifted fields' face values (diff_grad.c:150-176, 266-305): tau
 // rows xx yy zz xy xz yz from the central velocity, heat flux from the
 // central temperature and the species enthalpy-diffusion term.
-template <int NC>
-__device__ __forceinline__ void vgrad_q(double mu, double kt, double fr, double ft, double fu, double fv, double fw,
-                                        const double *fc, const double *dm, const double n[3], double q[9])
+template <int NC, typename T>
+__device__ __forceinline__ void vgrad_q(T mu, T kt, T fr, T ft, T fu, T fv, T fw, const T *fc, const T *dm,
+                                        const T n[3], T q[9])
 {
-    const double lambda = 0.0;   // charm_get_visc_lambda (src/charm_globals.c:509-512)
-    const double lp = (lambda + 4. * mu / 3.), lm = (lambda - 2. * mu / 3.);
+    const T lambda = T(0);   // charm_get_visc_lambda (src/charm_globals.c:509-512)
+    const T lp = (lambda + T(4) * mu / T(3)), lm = (lambda - T(2) * mu / T(3));
     q[0] = lp * fu * n[0] + lm * fv * n[1] + lm * fw * n[2];
     q[1] = lm * fu * n[0] + lp * fv * n[1] + lm * fw * n[2];
     q[2] = lm * fu * n[0] + lm * fv * n[1] + lp * fw * n[2];
@@ -94,7 +100,7 @@ __device__ __forceinline__ void vgrad_q(double mu, double kt, double fr, double 
     q[8] = kt * ft * n[2];
 #pragma unroll
     for (int i = 0; i < NC; i++) {
-        const double h = comp_h(i, ft);
+        const T h = comp_h<T>(i, ft);
         q[6] += h * fr * dm[i] * fc[i] * n[0];
         q[7] += h * fr * dm[i] * fc[i] * n[1];
         q[8] += h * fr * dm[i] * fc[i] * n[2];
@@ -198,11 +204,50 @@ chem_kernel(MeshDev m, const double *__restrict__ u, double *__restrict__ out, d
 }
 
 // ---------------------------------------------------------------------------
+// state access in FP64 for the per-element kernels that stay FP64 in the
+// mixed form (chemistry, diffusion coefficients): a double plane, or the
+// FP32 hi/lo planes of the mixed form (hi + lo is exact in double)
+// ---------------------------------------------------------------------------
+
+template <typename S> struct StIn;
+template <> struct StIn<double> {
+    const double *u;
+    __device__ __forceinline__ double at(int64_t i) const { return __ldg(u + i); }
+};
+template <> struct StIn<float> {
+    const float *h, *l;
+    __device__ __forceinline__ double at(int64_t i) const { return (double) __ldg(h + i) + (double) __ldg(l + i); }
+};
+
+template <typename S> struct StOut;
+template <> struct StOut<double> {
+    double *u;
+    __device__ __forceinline__ void put(int64_t i, double x) const { u[i] = x; }
+    __device__ __forceinline__ void copy(int64_t i, const StIn<double> &in) const { u[i] = __ldg(in.u + i); }
+};
+template <> struct StOut<float> {
+    float *h, *l;
+    __device__ __forceinline__ void put(int64_t i, double x) const
+    {
+        const float a = __double2float_rn(x);
+        h[i] = a;
+        l[i] = __double2float_rn(x - (double) a);
+    }
+    __device__ __forceinline__ void copy(int64_t i, const StIn<float> &in) const
+    {
+        h[i] = __ldg(in.h + i);
+        l[i] = __ldg(in.l + i);
+    }
+};
+
+// ---------------------------------------------------------------------------
 // species diffusion coefficients (charm_model_ns_diff.c:18-71)
 // ---------------------------------------------------------------------------
-// NBK: basis functions per variable (4 or 10); the centre value is c_0 for both
-template <int NC, int NBK = kNB>
-__global__ void __launch_bounds__(128) diffcoef_kernel(MeshDev m, const double *__restrict__ u, double *__restrict__ dif)
+// NBK: basis functions per variable (4 or 10); the centre value is c_0 for
+// both.  Computed in FP64 from the state S; stored as TD (the arithmetic type
+// of the kernels that read them).
+template <int NC, int NBK, typename S, typename TD>
+__global__ void __launch_bounds__(128) diffcoef_kernel(MeshDev m, StIn<S> u, TD *__restrict__ dif)
 {
     constexpr int V = 4 + NC;
     const int64_t e = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
@@ -210,7 +255,7 @@ __global__ void __launch_bounds__(128) diffcoef_kernel(MeshDev m, const double *
     if (e >= E) return;
     double U[V];
 #pragma unroll
-    for (int v = 0; v < V; v++) U[v] = __ldg(u + (int64_t) (v * NBK) * E + e);   // centre value = c_0
+    for (int v = 0; v < V; v++) U[v] = u.at((int64_t) (v * NBK) * E + e);   // centre value = c_0
     Prim<double, NC> p;
     cons_to_prim<double, NC>(U, p);
     const double pabs = p.p / 101325.0;
@@ -240,7 +285,7 @@ __global__ void __launch_bounds__(128) diffcoef_kernel(MeshDev m, const double *
             }
             d = (1. - x[i]) / s_xd;
         }
-        dif[(int64_t) i * E + e] = d;
+        dif[(int64_t) i * E + e] = TD(d);
     }
 }
 

@@ -16,6 +16,33 @@ def rel_max(a: np.ndarray, b: np.ndarray) -> float:
     return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
 
 
+def ref_mass_matrix(nb: int) -> np.ndarray:
+    """Mass matrix of the Taylor basis (4 or 10 functions) on the reference
+    box [-1/2, 1/2]^3 of volume 1 (3-point Gauss per axis, exact)."""
+    g = np.array([-0.5 * np.sqrt(0.6), 0.0, 0.5 * np.sqrt(0.6)])
+    w = np.array([5.0, 8.0, 5.0]) / 18.0
+    x, y, z = np.meshgrid(g, g, g, indexing="ij")
+    wt = (w[:, None, None] * w[None, :, None] * w[None, None, :]).ravel()
+    x, y, z = x.ravel(), y.ravel(), z.ravel()
+    phi = [np.ones_like(x), x, y, z] + ([x * x, y * y, z * z, x * y, x * z, y * z] if nb == 10 else [])
+    P = np.stack(phi)
+    return (P * wt) @ P.T
+
+
+def rel_l2_field(a: np.ndarray, b: np.ndarray) -> float:
+    """Relative L2 norm over the domain of the difference of two DG fields
+    (arrays [..., B, E] on a uniform mesh): sqrt(sum c^T M c) with the
+    reference mass matrix, so that every basis function counts with its
+    contribution to the field."""
+    nb = a.shape[-2]
+    M = ref_mass_matrix(nb)
+    d = (a - b).reshape(-1, nb, a.shape[-1])
+    r = b.reshape(-1, nb, b.shape[-1])
+    num = np.einsum("vke,kl,vle->", d, M, d)
+    den = np.einsum("vke,kl,vle->", r, M, r)
+    return float(np.sqrt(num / max(den, 1e-300)))
+
+
 def small_case(kind: str, flux: str = "LF", limiter: str = "BJ", level: int = 3, model: str = "NS") -> Case:
     """Small parity cases."""
     if kind == "sod":

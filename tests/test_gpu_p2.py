@@ -76,10 +76,6 @@ def test_p2_rejected_where_not_built():
     case.limiter = "BJ"
     with pytest.raises(CharmGpuError):
         Solver(case)
-    case = _p2("random", "HLLC", level=1)
-    case.precision = "MIXED"
-    with pytest.raises(CharmGpuError):
-        Solver(case)
     case = _p2("random", "HLLC", level=2)
     forest, _ = hanging_forest(case)
     gpu = Solver(case)
