@@ -511,17 +511,18 @@ p2_chem_kernel(MeshDev m, StIn<S> u, StOut<S> out, double *__restrict__ chem_rhs
         c[i] = U[4 + i] / c_cfg.comp_m[i];
         ch[i] = c[i];
     }
+    rate_consts(p.t, k);
     for (int j = 0; j < 2; j++) {
 #pragma unroll
         for (int i = 0; i < NC; i++) c_[i] = (ch[i] + c[i]) * 0.5;
-        chem_rates<NC>(p.t, c_, k, w, phi, psi);
+        chem_rates<NC>(k, c_, w, phi, psi);
 #pragma unroll
         for (int i = 0; i < NC; i++) {
             ch[i] = (c[i] + dt * psi[i] * (1. + dt * phi[i] * 0.5));
             ch[i] /= (1. + dt * phi[i] + (dt * phi[i]) * (dt * phi[i]) * 0.5);
         }
     }
-    chem_rates<NC>(p.t, ch, k, w, nullptr, nullptr);
+    chem_rates<NC>(k, ch, w, nullptr, nullptr);
     double rhs = 0.;
 #pragma unroll
     for (int i = 0; i < NC; i++) {

@@ -111,12 +111,24 @@ __device__ __forceinline__ void vgrad_q(T mu, T kt, T fr, T ft, T fu, T fv, T fw
 // chemistry on cell means
 // ---------------------------------------------------------------------------
 
+// Arrhenius rate constants k_n = A t^n exp(-E / (t R)).  The reference
+// recomputes them on every call of its rate function at the same cell
+// temperature; here they are computed once per cell (same values).  t^0 is 1.
+__device__ __forceinline__ void rate_consts(double t, double *k)
+{
+    for (int n = 0; n < c_cfg.n_react; n++) {
+        const double tn = (c_cfg.react_n[n] == 0.0) ? 1.0 : pow(t, c_cfg.react_n[n]);
+        k[n] = c_cfg.react_a[n] * tn * exp(-c_cfg.react_e[n] / t / kGasR);
+    }
+}
+
+// rates w and, when phi != nullptr, the semi-implicit split phi, psi at the
+// molar concentrations cc, from the rate constants k
 template <int NC>
-__device__ __forceinline__ void chem_rates(double t, const double *cc, double *k, double *w, double *phi, double *psi)
+__device__ __forceinline__ void chem_rates(const double *k, const double *cc, double *w, double *phi, double *psi)
 {   // _charm_model_ns_chem_rhs (charm_model_ns_chem.c:18-63)
     const int nr = c_cfg.n_react;
     for (int n = 0; n < nr; n++) {
-        k[n] = c_cfg.react_a[n] * pow(t, c_cfg.react_n[n]) * exp(-c_cfg.react_e[n] / t / kGasR);
         w[n] = k[n];
         for (int m = 0; m < 3; m++) {
             const int i = c_cfg.react_l[n][m];
@@ -168,17 +180,18 @@ chem_kernel(MeshDev m, const double *__restrict__ u, double *__restrict__ out, d
         c[i] = U[4 + i] / c_cfg.comp_m[i];
         ch[i] = c[i];
     }
+    rate_consts(p.t, k);
     for (int j = 0; j < 2; j++) {
 #pragma unroll
         for (int i = 0; i < NC; i++) c_[i] = (ch[i] + c[i]) * 0.5;
-        chem_rates<NC>(p.t, c_, k, w, phi, psi);
+        chem_rates<NC>(k, c_, w, phi, psi);
 #pragma unroll
         for (int i = 0; i < NC; i++) {
             ch[i] = (c[i] + dt * psi[i] * (1. + dt * phi[i] * 0.5));
             ch[i] /= (1. + dt * phi[i] + (dt * phi[i]) * (dt * phi[i]) * 0.5);
         }
     }
-    chem_rates<NC>(p.t, ch, k, w, nullptr, nullptr);
+    chem_rates<NC>(k, ch, w, nullptr, nullptr);
     double rhs = 0.;
 #pragma unroll
     for (int i = 0; i < NC; i++) {
@@ -244,8 +257,11 @@ template <> struct StOut<float> {
 // species diffusion coefficients (charm_model_ns_diff.c:18-71)
 // ---------------------------------------------------------------------------
 // NBK: basis functions per variable (4 or 10); the centre value is c_0 for
-// both.  Computed in FP64 from the state S; stored as TD (the arithmetic type
-// of the kernels that read them).
+// both.  The state, mass and mole fractions and the pure-species test are
+// FP64 (a fraction within 1e-12 of 1 is not resolvable in FP32); the
+// collision integrals and the binary coefficients are computed and stored
+// in TD: double for the FP64 form, float for the mixed form (whose kernels
+// read them as float; the transport coefficients there are FP32 too).
 template <int NC, int NBK, typename S, typename TD>
 __global__ void __launch_bounds__(128) diffcoef_kernel(MeshDev m, StIn<S> u, TD *__restrict__ dif)
 {
@@ -258,7 +274,7 @@ __global__ void __launch_bounds__(128) diffcoef_kernel(MeshDev m, StIn<S> u, TD 
     for (int v = 0; v < V; v++) U[v] = u.at((int64_t) (v * NBK) * E + e);   // centre value = c_0
     Prim<double, NC> p;
     cons_to_prim<double, NC>(U, p);
-    const double pabs = p.p / 101325.0;
+    const TD pabs = TD(p.p / 101325.0), t = TD(p.t);
     double x[NC], s = 0.;
 #pragma unroll
     for (int i = 0; i < NC; i++) {
@@ -269,23 +285,24 @@ __global__ void __launch_bounds__(128) diffcoef_kernel(MeshDev m, StIn<S> u, TD 
     for (int i = 0; i < NC; i++) x[i] /= s;
 #pragma unroll
     for (int i = 0; i < NC; i++) {
-        double d = 0.;
+        TD d = TD(0);
         if (!(fabs(p.c[i] - 1.) <= kEps)) {
-            double s_xd = 0.;
+            TD s_xd = TD(0);
 #pragma unroll
             for (int j = 0; j < NC; j++) {
-                const double td = p.t / sqrt(c_cfg.comp_ek[i] * c_cfg.comp_ek[j]);
-                const double wd = 1.06036 / pow(td, 0.1561) + 0.1930 / exp(0.47635 * td) + 1.03587 / exp(1.52996 * td) +
-                                  1.76474 / exp(3.89411 * td);
-                const double sg = 0.5 * (c_cfg.comp_sig[i] + c_cfg.comp_sig[j]);
-                const double dij = (2.628e-7) *
-                                   sqrt(0.5 * (1.0 / (1000.0 * c_cfg.comp_m[i]) + 1.0 / (1000.0 * c_cfg.comp_m[j]))) *
-                                   sqrt(p.t * p.t * p.t) / (pabs * (sg * sg) * wd);
-                s_xd += i == j ? 0. : x[j] / dij;
+                const TD td = t / TD(sqrt(c_cfg.comp_ek[i] * c_cfg.comp_ek[j]));
+                const TD wd = TD(1.06036) / pow(td, TD(0.1561)) + TD(0.1930) / exp(TD(0.47635) * td) +
+                              TD(1.03587) / exp(TD(1.52996) * td) + TD(1.76474) / exp(TD(3.89411) * td);
+                const TD sg = TD(0.5 * (c_cfg.comp_sig[i] + c_cfg.comp_sig[j]));
+                const TD dij = TD(2.628e-7) *
+                               TD(sqrt(0.5 * (1.0 / (1000.0 * c_cfg.comp_m[i]) + 1.0 / (1000.0 * c_cfg.comp_m[j])))) *
+                               sqrt(t * t * t) / (pabs * (sg * sg) * wd);
+                s_xd += i == j ? TD(0) : TD(x[j]) / dij;
             }
-            d = (1. - x[i]) / s_xd;
+            if constexpr (sizeof(TD) == sizeof(float)) d = (s_xd > 0.f) ? TD(1. - x[i]) / s_xd : 0.f;   // FP32 underflow
+            else d = (1. - x[i]) / s_xd;
         }
-        dif[(int64_t) i * E + e] = TD(d);
+        dif[(int64_t) i * E + e] = d;
     }
 }
 
