@@ -221,6 +221,7 @@ void build_devcfg(const charm_gpu_config_t *c, DevCfg *d)
         d->ideal_cv = d->ideal_cp - kGasR / d->ideal_m;
         d->ideal_gam = d->ideal_cp / d->ideal_cv;
         d->ideal_inv_cv = 1.0 / d->ideal_cv;
+        d->ideal_qg = (d->ideal_gam + 1.0) / (2.0 * d->ideal_gam);
     }
     d->n_bnd = c->n_bnd;
     for (int b = 0; b < c->n_bnd; b++) {
@@ -232,6 +233,7 @@ void build_devcfg(const charm_gpu_config_t *c, DevCfg *d)
     // float mirrors for the FP32 instantiations
     d->ideal_cp_f = (float) d->ideal_cp; d->ideal_m_f = (float) d->ideal_m; d->ideal_cv_f = (float) d->ideal_cv;
     d->ideal_gam_f = (float) d->ideal_gam; d->ideal_inv_cv_f = (float) d->ideal_inv_cv;
+    d->ideal_qg_f = (float) d->ideal_qg;
     for (int i = 0; i < CHARM_GPU_MAX_COMP; i++) {
         d->comp_m_f[i] = (float) d->comp_m[i];
         for (int k = 0; k < CHARM_GPU_MAX_CP; k++) d->comp_cp_f[i][k] = (float) d->comp_cp[i][k];

@@ -38,6 +38,7 @@ struct DevCfg {
     int    ideal_fast;     // IDEAL EOS with constant cp: cp, m, cv, gam precomputed
     int    newton_t;       // comp[0] has a cp polynomial: T by Newton (src/charm_eos.c:105,129)
     double ideal_cp, ideal_m, ideal_cv, ideal_gam, ideal_inv_cv;
+    double ideal_qg;       // (gam + 1) / (2 gam) of the HLLC wave-speed factor
     double comp_m[kMaxComp];
     double comp_cp[kMaxComp][kMaxCp];
     int    comp_ncp[kMaxComp];
@@ -51,7 +52,7 @@ struct DevCfg {
     // FP32 mirrors (each the float rounding of the double above), read by the
     // float instantiations so that they issue no double->float conversions:
     // on GB300 those run on the narrow FP64 pipe.
-    float  ideal_cp_f, ideal_m_f, ideal_cv_f, ideal_gam_f, ideal_inv_cv_f;
+    float  ideal_cp_f, ideal_m_f, ideal_cv_f, ideal_gam_f, ideal_inv_cv_f, ideal_qg_f;
     float  comp_m_f[kMaxComp];
     float  comp_cp_f[kMaxComp][kMaxCp];
     float  bnd_par_f[kMaxBnd][7 + kMaxComp];
@@ -462,8 +463,17 @@ __device__ void flux_hllc(const Prim<T, NC> &pa, const Prim<T, NC> &pb, const T 
 
     T p_pvrs = T(0.5) * (pa.p + pb.p) - T(0.5) * (ub - ua) * T(0.25) * (pa.r + pb.r) * (pa.cz + pb.cz);
     T p_star = (p_pvrs > T(0)) ? p_pvrs : T(0);
-    T ql = (p_star <= pa.p) ? T(1) : qsqrt<T>(T(1) + qdiv<T>((pa.gam + T(1)) * (qdiv<T>(p_star, pa.p) - T(1)), T(2) * pa.gam));
-    T qr = (p_star <= pb.p) ? T(1) : qsqrt<T>(T(1) + qdiv<T>((pb.gam + T(1)) * (qdiv<T>(p_star, pb.p) - T(1)), T(2) * pb.gam));
+    // shock factor sqrt(1 + (gam+1)/(2 gam) (p*/p - 1)); (gam+1)/(2 gam) is a
+    // constant of the ideal gas with constant cp
+    T ql = T(1), qr = T(1);
+    if (c_cfg.ideal_fast) {
+        const T qg = cfgv<T>(c_cfg.ideal_qg, c_cfg.ideal_qg_f);
+        if (p_star > pa.p) ql = qsqrt<T>(T(1) + qg * (qdiv<T>(p_star, pa.p) - T(1)));
+        if (p_star > pb.p) qr = qsqrt<T>(T(1) + qg * (qdiv<T>(p_star, pb.p) - T(1)));
+    } else {
+        if (p_star > pa.p) ql = qsqrt<T>(T(1) + qdiv<T>((pa.gam + T(1)) * (qdiv<T>(p_star, pa.p) - T(1)), T(2) * pa.gam));
+        if (p_star > pb.p) qr = qsqrt<T>(T(1) + qdiv<T>((pb.gam + T(1)) * (qdiv<T>(p_star, pb.p) - T(1)), T(2) * pb.gam));
+    }
     T sl = ua - pa.cz * ql;
     T sr = ub + pb.cz * qr;
     if (sl > sr) { T tmp = sl; sl = sr; sr = tmp; }
@@ -475,55 +485,29 @@ __device__ void flux_hllc(const Prim<T, NC> &pa, const Prim<T, NC> &pb, const T 
     if (s_star > sr) s_star = sr;
     if (!((sl <= s_star) && (s_star <= sr))) set_error(err, kErrHllc);
 
+    // The four cases (:405-436) with the side chosen by selects: the state k
+    // and its wave speed, then the star flux or the side's own flux.  The
+    // arithmetic of each case is the reference's; a warp whose lanes fall in
+    // different cases issues one star-state evaluation instead of two.
     T fu, fv, fw;
-    if constexpr (sizeof(T) == sizeof(float)) {
-        // the same four cases as below, with the side chosen by selects: the
-        // state k and its wave speed, then the star flux or the side's flux
-        const bool ka = (sl >= T(0)) || (!(sr <= T(0)) && (s_star >= T(0)));
-        const bool star = !(sl >= T(0)) && !(sr <= T(0));
-        const T rk = ka ? pa.r : pb.r, uk = ka ? ua : ub, vk = ka ? va : vb, wk = ka ? wa : wb;
-        const T pk = ka ? pa.p : pb.p, ek = ka ? pa.e_tot : pb.e_tot, sk = ka ? sl : sr;
-        const T fu_k = rk * uk * uk + pk, fv_k = rk * vk * uk, fw_k = rk * wk * uk, fe_k = (rk * ek + pk) * uk;
-        if (star) {
-            const T inv = qdiv<T>(T(1), sk - s_star);
-            fu = f_hllc_u<T>(rk * uk, fu_k, sk, s_star, pk, rk, uk, inv);
-            fv = f_hllc_v<T>(rk * vk, rk * uk * vk, sk, s_star, inv);
-            fw = f_hllc_v<T>(rk * wk, rk * uk * wk, sk, s_star, inv);
-            q[3] = f_hllc_e<T>(rk * ek, fe_k, sk, s_star, pk, rk, uk, inv);
-            for (int i = 0; i < NC; i++) {
-                const T ck = ka ? pa.c[i] : pb.c[i];
-                q[4 + i] = f_hllc_v<T>(rk * ck, rk * ck * uk, sk, s_star, inv);
-            }
-        } else {
-            fu = fu_k; fv = fv_k; fw = fw_k; q[3] = fe_k;
-            for (int i = 0; i < NC; i++) q[4 + i] = rk * uk * (ka ? pa.c[i] : pb.c[i]);
+    const bool ka = (sl >= T(0)) || (!(sr <= T(0)) && (s_star >= T(0)));
+    const bool star = !(sl >= T(0)) && !(sr <= T(0));
+    const T rk = ka ? pa.r : pb.r, uk = ka ? ua : ub, vk = ka ? va : vb, wk = ka ? wa : wb;
+    const T pk = ka ? pa.p : pb.p, ek = ka ? pa.e_tot : pb.e_tot, sk = ka ? sl : sr;
+    const T fu_k = rk * uk * uk + pk, fv_k = rk * vk * uk, fw_k = rk * wk * uk, fe_k = (rk * ek + pk) * uk;
+    if (star) {
+        const T inv = qdiv<T>(T(1), sk - s_star);
+        fu = f_hllc_u<T>(rk * uk, fu_k, sk, s_star, pk, rk, uk, inv);
+        fv = f_hllc_v<T>(rk * vk, rk * uk * vk, sk, s_star, inv);
+        fw = f_hllc_v<T>(rk * wk, rk * uk * wk, sk, s_star, inv);
+        q[3] = f_hllc_e<T>(rk * ek, fe_k, sk, s_star, pk, rk, uk, inv);
+        for (int i = 0; i < NC; i++) {
+            const T ck = ka ? pa.c[i] : pb.c[i];
+            q[4 + i] = f_hllc_v<T>(rk * ck, rk * ck * uk, sk, s_star, inv);
         }
-    } else if (sl >= T(0)) {
-        fu = pa.r * ua * ua + pa.p;
-        fv = pa.r * va * ua;
-        fw = pa.r * wa * ua;
-        q[3] = (pa.r * pa.e_tot + pa.p) * ua;
-        for (int i = 0; i < NC; i++) q[4 + i] = pa.r * ua * pa.c[i];
-    } else if (sr <= T(0)) {
-        fu = pb.r * ub * ub + pb.p;
-        fv = pb.r * vb * ub;
-        fw = pb.r * wb * ub;
-        q[3] = (pb.r * pb.e_tot + pb.p) * ub;
-        for (int i = 0; i < NC; i++) q[4 + i] = pb.r * ub * pb.c[i];
-    } else if (s_star >= T(0)) {
-        const T inv = qdiv<T>(T(1), sl - s_star);
-        fu = f_hllc_u<T>(pa.r * ua, pa.r * ua * ua + pa.p, sl, s_star, pa.p, pa.r, ua, inv);
-        fv = f_hllc_v<T>(pa.r * va, pa.r * ua * va, sl, s_star, inv);
-        fw = f_hllc_v<T>(pa.r * wa, pa.r * ua * wa, sl, s_star, inv);
-        q[3] = f_hllc_e<T>(pa.r * pa.e_tot, (pa.r * pa.e_tot + pa.p) * ua, sl, s_star, pa.p, pa.r, ua, inv);
-        for (int i = 0; i < NC; i++) q[4 + i] = f_hllc_v<T>(pa.r * pa.c[i], pa.r * pa.c[i] * ua, sl, s_star, inv);
     } else {
-        const T inv = qdiv<T>(T(1), sr - s_star);
-        fu = f_hllc_u<T>(pb.r * ub, pb.r * ub * ub + pb.p, sr, s_star, pb.p, pb.r, ub, inv);
-        fv = f_hllc_v<T>(pb.r * vb, pb.r * ub * vb, sr, s_star, inv);
-        fw = f_hllc_v<T>(pb.r * wb, pb.r * ub * wb, sr, s_star, inv);
-        q[3] = f_hllc_e<T>(pb.r * pb.e_tot, (pb.r * pb.e_tot + pb.p) * ub, sr, s_star, pb.p, pb.r, ub, inv);
-        for (int i = 0; i < NC; i++) q[4 + i] = f_hllc_v<T>(pb.r * pb.c[i], pb.r * pb.c[i] * ub, sr, s_star, inv);
+        fu = fu_k; fv = fv_k; fw = fw_k; q[3] = fe_k;
+        for (int i = 0; i < NC; i++) q[4 + i] = rk * uk * (ka ? pa.c[i] : pb.c[i]);
     }
     frame_out<AX, T>(nt, sn, fu, fv, fw, q);
 }
