@@ -29,6 +29,19 @@
 namespace charm {
 namespace adj {
 
+// 1 / sqrt(x) for x > 0: the device's reciprocal square root (one rounding
+// step from the correctly rounded value), the plain quotient on the host.
+// Where a routine needs both sqrt(x) and its reciprocal it takes
+// x * rsqrt(x) and rsqrt(x), which saves a division per use.
+ADJ_HD double rsq(double x)
+{
+#ifdef __CUDA_ARCH__
+    return rsqrt(x);
+#else
+    return 1.0 / sqrt(x);
+#endif
+}
+
 // Ideal gas with constant cp (the only EOS the adjoint supports).
 struct Gas {
     double gam;      // cp / cv
@@ -42,6 +55,7 @@ template <int NC>
 struct Pr {                 // primitive state as the fluxes use it
     double r, u, v, w, e, e_tot, p, t, cz;
     double ir;              // 1 / r
+    double icz;             // 1 / cz (set by prim; 0 where cz = 0)
     double c[NC];
     unsigned clamp;         // bit i: species fraction i was clamped to [0, 1]
 };
@@ -82,7 +96,9 @@ ADJ_HD void prim(const double *U, const Gas &g, Pr<NC> &p)
         p.c[i] = c;
     }
     p.p = r * p.e * (g.gam - 1.0);
-    p.cz = sqrt(g.gam * p.p * ir);
+    const double x = g.gam * p.p * ir;
+    p.icz = (x > 0.0) ? rsq(x) : 0.0;
+    p.cz = (x > 0.0) ? x * p.icz : sqrt(x);
     p.t = p.e * g.inv_cv;
 }
 
@@ -94,7 +110,7 @@ ADJ_HD void prim_vjp(const double *U, const Pr<NC> &p, const Gas &g, PrBar<NC> b
     double b_ir = 0.0;
     b.e += b.t * g.inv_cv;                                   // t = e / cv
     if (p.cz > 0.0) {                                        // cz = sqrt(gam p ir)
-        const double d = 0.5 * g.gam / p.cz;
+        const double d = 0.5 * g.gam * p.icz;
         b.p += b.cz * d * ir;
         b_ir += b.cz * d * p.p;
     }
@@ -304,10 +320,15 @@ ADJ_HD void flux_hllc_vjp(const Pr<NC> &a, const Pr<NC> &b, const double n[3], c
 
     const double p_pvrs = 0.5 * (a.p + b.p) - 0.5 * (ub - ua) * 0.25 * (a.r + b.r) * (a.cz + b.cz);
     const double p_star = (p_pvrs > 0.0) ? p_pvrs : 0.0;
-    const double kq = (gam + 1.0) / (2.0 * gam);
+    const double kq = (gam + 1.0) / (2.0 * gam);   // loop-invariant: hoisted by the compiler
     const bool shock_a = !(p_star <= a.p), shock_b = !(p_star <= b.p);
-    const double ql = shock_a ? sqrt(1.0 + (gam + 1.0) * (p_star / a.p - 1.0) / (2.0 * gam)) : 1.0;
-    const double qr = shock_b ? sqrt(1.0 + (gam + 1.0) * (p_star / b.p - 1.0) / (2.0 * gam)) : 1.0;
+    // ql = sqrt(1 + kq (p*/pa - 1)) and its reverse need 1/pa and 1/ql
+    const double ipa = shock_a ? 1.0 / a.p : 0.0, ipb = shock_b ? 1.0 / b.p : 0.0;
+    const double ra = shock_a ? p_star * ipa : 1.0, rb = shock_b ? p_star * ipb : 1.0;
+    const double xa = 1.0 + kq * (ra - 1.0), xb = 1.0 + kq * (rb - 1.0);
+    const double iqa = shock_a ? rsq(xa) : 1.0, iqb = shock_b ? rsq(xb) : 1.0;
+    const double ql = shock_a ? xa * iqa : 1.0;
+    const double qr = shock_b ? xb * iqb : 1.0;
     const double sl0 = ua - a.cz * ql, sr0 = ub + b.cz * qr;
     const bool swap = sl0 > sr0;
     const double sl = swap ? sr0 : sl0, sr = swap ? sl0 : sr0;
@@ -315,7 +336,8 @@ ADJ_HD void flux_hllc_vjp(const Pr<NC> &a, const Pr<NC> &b, const double n[3], c
     num += a.r * ua * (sl - ua);
     num -= b.r * ub * (sr - ub);
     const double den = a.r * (sl - ua) - b.r * (sr - ub);
-    double ss = num / den;
+    const double iden = 1.0 / den;
+    double ss = num * iden;
     int clamp = 0;
     if (ss < sl) { ss = sl; clamp = 1; }
     if (ss > sr) { ss = sr; clamp = 2; }
@@ -403,7 +425,7 @@ ADJ_HD void flux_hllc_vjp(const Pr<NC> &a, const Pr<NC> &b, const double n[3], c
     if (clamp == 1) slb += ssb;
     else if (clamp == 2) srb += ssb;
     else {
-        const double numb = ssb / den, denb = -numb * ss;
+        const double numb = ssb * iden, denb = -numb * ss;
         bb.p += numb; ab.p -= numb;
         ab.r += numb * ua * (sl - ua); uab += numb * a.r * (sl - 2.0 * ua); slb += numb * a.r * ua;
         bb.r -= numb * ub * (sr - ub); ubb -= numb * b.r * (sr - 2.0 * ub); srb -= numb * b.r * ub;
@@ -416,15 +438,15 @@ ADJ_HD void flux_hllc_vjp(const Pr<NC> &a, const Pr<NC> &b, const double n[3], c
     ubb += sr0b; bb.cz += sr0b * qr;
     const double qrb = sr0b * b.cz;
     double pstarb = 0.0;
-    if (shock_a) {   // ql = sqrt(1 + kq (p*/pa - 1))
-        const double d = 0.5 * kq / (ql * a.p);
+    if (shock_a) {   // ql = sqrt(1 + kq (p*/pa - 1)): d ql / d p* = kq / (2 ql pa)
+        const double d = 0.5 * kq * iqa * ipa;
         pstarb += qlb * d;
-        ab.p -= qlb * d * p_star / a.p;
+        ab.p -= qlb * d * ra;
     }
     if (shock_b) {
-        const double d = 0.5 * kq / (qr * b.p);
+        const double d = 0.5 * kq * iqb * ipb;
         pstarb += qrb * d;
-        bb.p -= qrb * d * p_star / b.p;
+        bb.p -= qrb * d * rb;
     }
     if (p_pvrs > 0.0) {
         const double D = ub - ua, Rs = 0.25 * (a.r + b.r), Cs = a.cz + b.cz;

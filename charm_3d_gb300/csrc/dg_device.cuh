@@ -465,15 +465,10 @@ __device__ void flux_hllc(const Prim<T, NC> &pa, const Prim<T, NC> &pb, const T 
     T p_star = (p_pvrs > T(0)) ? p_pvrs : T(0);
     // shock factor sqrt(1 + (gam+1)/(2 gam) (p*/p - 1)); (gam+1)/(2 gam) is a
     // constant of the ideal gas with constant cp
-    T ql = T(1), qr = T(1);
-    if (c_cfg.ideal_fast) {
-        const T qg = cfgv<T>(c_cfg.ideal_qg, c_cfg.ideal_qg_f);
-        if (p_star > pa.p) ql = qsqrt<T>(T(1) + qg * (qdiv<T>(p_star, pa.p) - T(1)));
-        if (p_star > pb.p) qr = qsqrt<T>(T(1) + qg * (qdiv<T>(p_star, pb.p) - T(1)));
-    } else {
-        if (p_star > pa.p) ql = qsqrt<T>(T(1) + qdiv<T>((pa.gam + T(1)) * (qdiv<T>(p_star, pa.p) - T(1)), T(2) * pa.gam));
-        if (p_star > pb.p) qr = qsqrt<T>(T(1) + qdiv<T>((pb.gam + T(1)) * (qdiv<T>(p_star, pb.p) - T(1)), T(2) * pb.gam));
-    }
+    const T qga = c_cfg.ideal_fast ? cfgv<T>(c_cfg.ideal_qg, c_cfg.ideal_qg_f) : qdiv<T>(pa.gam + T(1), T(2) * pa.gam);
+    const T qgb = c_cfg.ideal_fast ? cfgv<T>(c_cfg.ideal_qg, c_cfg.ideal_qg_f) : qdiv<T>(pb.gam + T(1), T(2) * pb.gam);
+    const T ql = (p_star <= pa.p) ? T(1) : qsqrt<T>(T(1) + qga * (qdiv<T>(p_star, pa.p) - T(1)));
+    const T qr = (p_star <= pb.p) ? T(1) : qsqrt<T>(T(1) + qgb * (qdiv<T>(p_star, pb.p) - T(1)));
     T sl = ua - pa.cz * ql;
     T sr = ub + pb.cz * qr;
     if (sl > sr) { T tmp = sl; sl = sr; sr = tmp; }
