@@ -117,7 +117,13 @@ int charm_forest_copy(charm_forest_t *dst, const charm_forest_t *src)
 
 /* ---- queries ------------------------------------------------------------ */
 
-int64_t charm_forest_find(const charm_forest_t *f, int32_t t, int32_t x, int32_t y, int32_t z)
+void charm_forest_keys(const charm_forest_t *f, uint64_t *key)
+{
+    for (int64_t i = 0; i < f->n; i++) key[i] = morton(f->leaf[i].x, f->leaf[i].y, f->leaf[i].z);
+}
+
+int64_t charm_forest_find_k(const charm_forest_t *f, const uint64_t *keys, int32_t t, int32_t x, int32_t y,
+                            int32_t z)
 {
     if (x < 0 || y < 0 || z < 0 || x >= CHARM_FOREST_ROOT_LEN || y >= CHARM_FOREST_ROOT_LEN ||
         z >= CHARM_FOREST_ROOT_LEN)
@@ -127,7 +133,8 @@ int64_t charm_forest_find(const charm_forest_t *f, int32_t t, int32_t x, int32_t
     while (lo <= hi) {       /* last leaf with (tree,key) <= (t,key) */
         int64_t mid = lo + (hi - lo) / 2;
         const charm_leaf_t *q = &f->leaf[mid];
-        int le = (q->tree < t) || (q->tree == t && morton(q->x, q->y, q->z) <= key);
+        const uint64_t kq = keys ? keys[mid] : morton(q->x, q->y, q->z);
+        int le = (q->tree < t) || (q->tree == t && kq <= key);
         if (le) { best = mid; lo = mid + 1; } else hi = mid - 1;
     }
     if (best < 0) return -1;
@@ -136,6 +143,11 @@ int64_t charm_forest_find(const charm_forest_t *f, int32_t t, int32_t x, int32_t
     int32_t len = CHARM_FOREST_QLEN(q->level);
     if (x < q->x || x >= q->x + len || y < q->y || y >= q->y + len || z < q->z || z >= q->z + len) return -1;
     return best;
+}
+
+int64_t charm_forest_find(const charm_forest_t *f, int32_t t, int32_t x, int32_t y, int32_t z)
+{
+    return charm_forest_find_k(f, NULL, t, x, y, z);
 }
 
 /* Map tree-local point p (possibly one root length outside along axis d) to
@@ -170,6 +182,12 @@ static int32_t locate_tree(const charm_forest_t *f, int32_t t, int d, int32_t p[
 
 void charm_forest_face_neighbor(const charm_forest_t *f, int64_t i, int face, charm_face_nb_t *nb)
 {
+    charm_forest_face_neighbor_k(f, NULL, i, face, nb);
+}
+
+void charm_forest_face_neighbor_k(const charm_forest_t *f, const uint64_t *keys, int64_t i, int face,
+                                  charm_face_nb_t *nb)
+{
     const charm_leaf_t *q = &f->leaf[i];
     int d = face / 2, up = face & 1;
     int32_t len = CHARM_FOREST_QLEN(q->level);
@@ -180,7 +198,7 @@ void charm_forest_face_neighbor(const charm_forest_t *f, int64_t i, int face, ch
     nb->wrap = wrap;
     nb->idx[0] = nb->idx[1] = nb->idx[2] = nb->idx[3] = -1;
     if (nt < 0) { nb->kind = CHARM_NB_BOUNDARY; return; }
-    int64_t j = charm_forest_find(f, nt, p[0], p[1], p[2]);
+    int64_t j = charm_forest_find_k(f, keys, nt, p[0], p[1], p[2]);
     const charm_leaf_t *r = &f->leaf[j];
     if (r->level == q->level) { nb->kind = CHARM_NB_SAME; nb->idx[0] = j; return; }
     if (r->level < q->level) {
@@ -197,7 +215,7 @@ void charm_forest_face_neighbor(const charm_forest_t *f, int64_t i, int face, ch
         if (!up) c[d] += h;          /* the half of the region touching our face */
         c[s] += (k & 1) ? h : 0;
         c[tt] += (k & 2) ? h : 0;
-        int64_t m = charm_forest_find(f, nt, c[0], c[1], c[2]);
+        int64_t m = charm_forest_find_k(f, keys, nt, c[0], c[1], c[2]);
         nb->idx[k] = m;
         if (f->leaf[m].level != q->level + 1) nb->kind = CHARM_NB_UNBALANCED;
     }
@@ -338,11 +356,11 @@ int64_t charm_forest_coarsen(charm_forest_t *f, int minlevel, charm_forest_coars
 /* A leaf must be refined when some leaf two or more levels finer touches one
  * of its faces: the same-size neighbour region is split and at least one of
  * its four children next to our face is split again. */
-static int needs_split(const charm_forest_t *f, int64_t i)
+static int needs_split(const charm_forest_t *f, const uint64_t *keys, int64_t i)
 {
     charm_face_nb_t nb;
     for (int face = 0; face < 6; face++) {
-        charm_forest_face_neighbor(f, i, face, &nb);
+        charm_forest_face_neighbor_k(f, keys, i, face, &nb);
         if (nb.kind == CHARM_NB_UNBALANCED) {
             /* UNBALANCED is reported from both sides; only the coarse side splits */
             const charm_leaf_t *q = &f->leaf[i];
@@ -356,10 +374,13 @@ static int needs_split(const charm_forest_t *f, int64_t i)
 int64_t charm_forest_balance_marks(const charm_forest_t *f, int8_t *flag)
 {
     int64_t marks = 0;
+    uint64_t *keys = (uint64_t *) malloc(sizeof(uint64_t) * (size_t) (f->n > 0 ? f->n : 1));
+    if (keys) charm_forest_keys(f, keys);
     for (int64_t i = 0; i < f->n; i++) {
-        flag[i] = (int8_t) needs_split(f, i);
+        flag[i] = (int8_t) needs_split(f, keys, i);
         marks += flag[i];
     }
+    free(keys);
     return marks;
 }
 
@@ -368,11 +389,14 @@ int64_t charm_forest_balance(charm_forest_t *f, charm_forest_replace_fn replace,
     int64_t total = 0;
     for (;;) {
         int8_t *flag = (int8_t *) calloc((size_t) f->n, 1);
-        if (!flag) return -1;
+        uint64_t *keys = (uint64_t *) malloc(sizeof(uint64_t) * (size_t) (f->n > 0 ? f->n : 1));
+        if (!flag || !keys) { free(flag); free(keys); return -1; }
+        charm_forest_keys(f, keys);
         int64_t marks = 0;
         for (int64_t i = 0; i < f->n; i++) {
-            if (needs_split(f, i)) { flag[i] = 1; marks++; }
+            if (needs_split(f, keys, i)) { flag[i] = 1; marks++; }
         }
+        free(keys);
         if (marks == 0) { free(flag); break; }
         int64_t r = charm_forest_refine(f, flag, -1, replace, user);
         free(flag);
@@ -385,12 +409,16 @@ int64_t charm_forest_balance(charm_forest_t *f, charm_forest_replace_fn replace,
 int charm_forest_is_balanced(const charm_forest_t *f)
 {
     charm_face_nb_t nb;
-    for (int64_t i = 0; i < f->n; i++)
+    uint64_t *keys = (uint64_t *) malloc(sizeof(uint64_t) * (size_t) (f->n > 0 ? f->n : 1));
+    if (keys) charm_forest_keys(f, keys);
+    int ok = 1;
+    for (int64_t i = 0; i < f->n && ok; i++)
         for (int face = 0; face < 6; face++) {
-            charm_forest_face_neighbor(f, i, face, &nb);
-            if (nb.kind == CHARM_NB_UNBALANCED) return 0;
+            charm_forest_face_neighbor_k(f, keys, i, face, &nb);
+            if (nb.kind == CHARM_NB_UNBALANCED) { ok = 0; break; }
         }
-    return 1;
+    free(keys);
+    return ok;
 }
 
 /* keep leaf_cmp referenced for debug builds that validate ordering */

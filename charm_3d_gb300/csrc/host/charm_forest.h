@@ -86,6 +86,16 @@ int64_t charm_forest_find(const charm_forest_t *f, int32_t t, int32_t x, int32_t
 /* Neighbour relation across face `face` (0..5, p4est numbering: -x,+x,-y,+y,-z,+z). */
 void charm_forest_face_neighbor(const charm_forest_t *f, int64_t i, int face, charm_face_nb_t *nb);
 
+/* Morton keys of the lower corners, key[i] for leaf i (n entries): with them
+ * the *_k queries compare stored keys in their binary search instead of
+ * recomputing one per step.  Valid until the forest changes; NULL keys make
+ * the *_k queries compute them on the fly. */
+void charm_forest_keys(const charm_forest_t *f, uint64_t *key);
+int64_t charm_forest_find_k(const charm_forest_t *f, const uint64_t *key, int32_t t, int32_t x, int32_t y,
+                            int32_t z);
+void charm_forest_face_neighbor_k(const charm_forest_t *f, const uint64_t *key, int64_t i, int face,
+                                  charm_face_nb_t *nb);
+
 /* Physical centre and edge lengths of leaf i. */
 void charm_forest_leaf_geom(const charm_forest_t *f, int64_t i, double c[3], double h[3]);
 

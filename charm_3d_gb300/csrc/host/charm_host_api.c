@@ -161,18 +161,27 @@ int charm_host_forest_flatten(charm_host_forest_t h, charm_gpu_mesh_t *mesh)
     const charm_forest_t *f = &h->f;
     const int64_t E = f->n;
     free_flat(h);
+    /* every leaf's six face-neighbour relations, found once (binary searches
+     * on precomputed Morton keys) and read by the three passes below */
+    uint64_t *keys = (uint64_t *) malloc(sizeof(uint64_t) * (size_t) (E > 0 ? E : 1));
+    charm_face_nb_t *nbs = (charm_face_nb_t *) malloc(sizeof(charm_face_nb_t) * (size_t) (6 * (E > 0 ? E : 1)));
+    if (!keys || !nbs) { free(keys); free(nbs); return CHARM_GPU_ENOMEM; }
+    charm_forest_keys(f, keys);
+    for (int64_t i = 0; i < E; i++)
+        for (int face = 0; face < 6; face++) charm_forest_face_neighbor_k(f, keys, i, face, &nbs[6 * i + face]);
+    free(keys);
     /* count */
     int64_t nf = 0, nb = 0;
     charm_face_nb_t nbr;
     for (int64_t i = 0; i < E; i++) {
         for (int face = 0; face < 6; face++) {
-            charm_forest_face_neighbor(f, i, face, &nbr);
+            nbr = nbs[6 * i + face];
             switch (nbr.kind) {
             case CHARM_NB_BOUNDARY: nb++; break;
             case CHARM_NB_SAME: if (face & 1) nf++; break;
             case CHARM_NB_SMALLER: nf += 4; break;
             case CHARM_NB_BIGGER: break;
-            default: return CHARM_GPU_EINVAL;   /* not 2:1 balanced */
+            default: free(nbs); return CHARM_GPU_EINVAL;   /* not 2:1 balanced */
             }
         }
     }
@@ -186,6 +195,7 @@ int charm_host_forest_flatten(charm_host_forest_t h, charm_gpu_mesh_t *mesh)
     if (!h->center || !h->level || !h->face_elem || !h->face_info || !h->bface_elem || !h->bface_face ||
         !h->bface_bnd) {
         free_flat(h);
+        free(nbs);
         return CHARM_GPU_ENOMEM;
     }
     for (int64_t i = 0; i < E; i++) {
@@ -200,7 +210,7 @@ int charm_host_forest_flatten(charm_host_forest_t h, charm_gpu_mesh_t *mesh)
         for (int64_t i = 0; i < E; i++) {
             for (int up = 0; up < 2; up++) {
                 int face = 2 * d + up;
-                charm_forest_face_neighbor(f, i, face, &nbr);
+                nbr = nbs[6 * i + face];
                 uint8_t wrap = nbr.wrap ? 0x40 : 0;
                 if (nbr.kind == CHARM_NB_SAME && up) {
                     h->face_elem[k] = (int32_t) i;
@@ -227,7 +237,7 @@ int charm_host_forest_flatten(charm_host_forest_t h, charm_gpu_mesh_t *mesh)
     int64_t kb = 0;
     for (int64_t i = 0; i < E; i++) {
         for (int face = 0; face < 6; face++) {
-            charm_forest_face_neighbor(f, i, face, &nbr);
+            nbr = nbs[6 * i + face];
             if (nbr.kind == CHARM_NB_BOUNDARY) {
                 h->bface_elem[kb] = (int32_t) i;
                 h->bface_face[kb] = (int8_t) face;
@@ -236,6 +246,7 @@ int charm_host_forest_flatten(charm_host_forest_t h, charm_gpu_mesh_t *mesh)
             }
         }
     }
+    free(nbs);
     h->n_face = nf;
     h->n_bface = nb;
     mesh->n_elem = E;
