@@ -20,6 +20,7 @@
 #include <thread>
 #include <utility>
 #include <algorithm>
+#include <unordered_map>
 #include <vector>
 
 #include "charm_gpu.h"
@@ -108,6 +109,10 @@ struct charm_gpu_handle_s {
     bool timing = false;
     std::vector<TimedLaunch> pending;
     std::vector<cudaEvent_t> event_pool;
+    // capacity in bytes of the mesh-sized device buffers, by the address of
+    // the handle member that holds each one: an upload after an adapt keeps
+    // every buffer that is still large enough
+    std::unordered_map<const void *, size_t> dcap;
 };
 
 namespace {
@@ -115,6 +120,44 @@ namespace {
 const charm_gpu_handle_s *g_cfg_owner = nullptr;
 
 int n_var(const charm_gpu_handle_s *h) { return 4 + h->cfg.n_comp; }
+
+// Device buffer *p of at least `bytes` bytes: kept when the current one is
+// large enough, else replaced (contents are not preserved).
+template <typename P>
+int ensure_buf(charm_gpu_handle_s *h, P **p, size_t bytes)
+{
+    size_t &cap = h->dcap[static_cast<const void *>(p)];
+    if (*p && cap >= bytes) return CHARM_GPU_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    cap = 0;
+    if (cudaMalloc(reinterpret_cast<void **>(p), bytes) != cudaSuccess) {
+        *p = nullptr;
+        return fail(CHARM_GPU_ENOMEM, "cudaMalloc of a mesh buffer failed");
+    }
+    cap = bytes;
+    return CHARM_GPU_OK;
+}
+
+// Drop what belongs to the previous mesh but is not a reusable buffer: the
+// adjoint's buffers and checkpoints (sized by the run), the flags.
+void reset_mesh(charm_gpu_handle_s *h)
+{
+    double **adj[] = {&h->d_adj_lam, &h->d_adj_s, &h->d_adj_acc, &h->d_adj_u1, &h->d_adj_u2, &h->d_adj_fin,
+                      &h->d_adj_psi, &h->d_obj_part, &h->d_adj_psi_all};
+    for (double **q : adj) {
+        if (*q) cudaFree(*q);
+        *q = nullptr;
+    }
+    h->n_psi_all = 0;
+    for (double *q : h->d_snap) cudaFree(q);
+    h->d_snap.clear();
+    h->adj_valid = false;
+    h->n_tiles = 0;
+    h->tile_smem = 0;
+    h->mesh_ready = false;
+    h->E = h->F = h->Fb = h->S = 0;
+}
 
 void free_mesh(charm_gpu_handle_s *h)
 {
@@ -147,6 +190,7 @@ void free_mesh(charm_gpu_handle_s *h)
         *q = nullptr;
     }
     h->adj_valid = false;
+    h->dcap.clear();
     h->n_tiles = 0;
     h->tile_smem = 0;
     h->d_center = nullptr; h->d_level = nullptr; h->d_face_elem = nullptr; h->d_face_info = nullptr;
@@ -1066,42 +1110,43 @@ int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh)
 
     CUDA_TRY(cudaSetDevice(h->device));
     cudaStreamSynchronize(h->stream);
-    free_mesh(h);
+    reset_mesh(h);
+    int arc;
     const int V = n_var(h);
     const size_t st = (size_t) V * h->nb * E * sizeof(double);
     const size_t sl = (size_t) V * h->nb * (S > 0 ? S : 2) *
                       (h->cfg.precision == CHARM_GPU_PREC_MIXED ? sizeof(float) : sizeof(double));
-    CUDA_TRY(cudaMalloc(&h->d_center, 3 * E * sizeof(double)));
-    CUDA_TRY(cudaMalloc(&h->d_level, E));
-    CUDA_TRY(cudaMalloc(&h->d_face_elem, 2 * (F ? F : 1) * sizeof(int32_t)));
-    CUDA_TRY(cudaMalloc(&h->d_face_info, F ? F : 1));
-    CUDA_TRY(cudaMalloc(&h->d_bface_elem, (Fb ? Fb : 1) * sizeof(int32_t)));
-    CUDA_TRY(cudaMalloc(&h->d_bface_face, Fb ? Fb : 1));
-    CUDA_TRY(cudaMalloc(&h->d_bface_bnd, Fb ? Fb : 1));
-    CUDA_TRY(cudaMalloc(&h->d_gather_ptr, (E + 1) * sizeof(int32_t)));
-    CUDA_TRY(cudaMalloc(&h->d_gather_slot, (ptr[E] ? ptr[E] : 1) * sizeof(int32_t)));
-    CUDA_TRY(cudaMalloc(&h->d_lim_idx, 6 * E * sizeof(int32_t)));
-    CUDA_TRY(cudaMalloc(&h->d_lim_kind, 6 * E));
-    CUDA_TRY(cudaMalloc(&h->d_u, st));
-    CUDA_TRY(cudaMalloc(&h->d_ua, st));
-    CUDA_TRY(cudaMalloc(&h->d_ub, st));
-    CUDA_TRY(cudaMalloc(&h->d_slots, sl));
+    if ((arc = ensure_buf(h, &h->d_center, 3 * E * sizeof(double)))) return arc;
+    if ((arc = ensure_buf(h, &h->d_level, E))) return arc;
+    if ((arc = ensure_buf(h, &h->d_face_elem, 2 * (F ? F : 1) * sizeof(int32_t)))) return arc;
+    if ((arc = ensure_buf(h, &h->d_face_info, F ? F : 1))) return arc;
+    if ((arc = ensure_buf(h, &h->d_bface_elem, (Fb ? Fb : 1) * sizeof(int32_t)))) return arc;
+    if ((arc = ensure_buf(h, &h->d_bface_face, Fb ? Fb : 1))) return arc;
+    if ((arc = ensure_buf(h, &h->d_bface_bnd, Fb ? Fb : 1))) return arc;
+    if ((arc = ensure_buf(h, &h->d_gather_ptr, (E + 1) * sizeof(int32_t)))) return arc;
+    if ((arc = ensure_buf(h, &h->d_gather_slot, (ptr[E] ? ptr[E] : 1) * sizeof(int32_t)))) return arc;
+    if ((arc = ensure_buf(h, &h->d_lim_idx, 6 * E * sizeof(int32_t)))) return arc;
+    if ((arc = ensure_buf(h, &h->d_lim_kind, 6 * E))) return arc;
+    if ((arc = ensure_buf(h, &h->d_u, st))) return arc;
+    if ((arc = ensure_buf(h, &h->d_ua, st))) return arc;
+    if ((arc = ensure_buf(h, &h->d_ub, st))) return arc;
+    if ((arc = ensure_buf(h, &h->d_slots, sl))) return arc;
     if (h->cfg.model == CHARM_GPU_MODEL_NS && (h->cfg.use_visc || h->cfg.n_react)) {
-        CUDA_TRY(cudaMalloc(&h->d_chem_rhs, sizeof(double) * E));
+        if ((arc = ensure_buf(h, &h->d_chem_rhs, sizeof(double) * E))) return arc;
         CUDA_TRY(cudaMemset(h->d_chem_rhs, 0, sizeof(double) * E));
-        if (h->cfg.n_react) CUDA_TRY(cudaMalloc(&h->d_uc, st));
+        if (h->cfg.n_react) if ((arc = ensure_buf(h, &h->d_uc, st))) return arc;
         if (h->cfg.use_visc) {
-            CUDA_TRY(cudaMalloc(&h->d_s9, sizeof(double) * 9 * h->nb * S));
-            CUDA_TRY(cudaMalloc(&h->d_vis, sizeof(double) * 9 * h->nb * E));
-            CUDA_TRY(cudaMalloc(&h->d_radd, sizeof(double) * 4 * h->nb * E));
-            CUDA_TRY(cudaMalloc(&h->d_dif, sizeof(double) * V * E));
+            if ((arc = ensure_buf(h, &h->d_s9, sizeof(double) * 9 * h->nb * S))) return arc;
+            if ((arc = ensure_buf(h, &h->d_vis, sizeof(double) * 9 * h->nb * E))) return arc;
+            if ((arc = ensure_buf(h, &h->d_radd, sizeof(double) * 4 * h->nb * E))) return arc;
+            if ((arc = ensure_buf(h, &h->d_dif, sizeof(double) * V * E))) return arc;
             CUDA_TRY(cudaMemset(h->d_dif, 0, sizeof(double) * V * E));
         }
     }
     if (h->cfg.precision == CHARM_GPU_PREC_MIXED) {
         for (int k = 0; k < 3; k++) {
-            CUDA_TRY(cudaMalloc(&h->d_fh[k], st / 2));
-            CUDA_TRY(cudaMalloc(&h->d_fl[k], st / 2));
+            if ((arc = ensure_buf(h, &h->d_fh[k], st / 2))) return arc;
+            if ((arc = ensure_buf(h, &h->d_fl[k], st / 2))) return arc;
             CUDA_TRY(cudaMemset(h->d_fh[k], 0, st / 2));
             CUDA_TRY(cudaMemset(h->d_fl[k], 0, st / 2));
         }
@@ -1155,9 +1200,9 @@ int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh)
         int max_optin = 0;
         CUDA_TRY(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
         if (smem <= (size_t) max_optin) {
-            CUDA_TRY(cudaMalloc(&h->d_tile_fptr, (nt + 1) * sizeof(int32_t)));
-            CUDA_TRY(cudaMalloc(&h->d_tile_faces, tfaces.size() * sizeof(int32_t)));
-            CUDA_TRY(cudaMalloc(&h->d_tile_slot, (size_t) 6 * E * sizeof(int32_t)));
+            if ((arc = ensure_buf(h, &h->d_tile_fptr, (nt + 1) * sizeof(int32_t)))) return arc;
+            if ((arc = ensure_buf(h, &h->d_tile_faces, tfaces.size() * sizeof(int32_t)))) return arc;
+            if ((arc = ensure_buf(h, &h->d_tile_slot, (size_t) 6 * E * sizeof(int32_t)))) return arc;
             CUDA_TRY(cudaMemcpy(h->d_tile_fptr, tptr.data(), (nt + 1) * sizeof(int32_t), cudaMemcpyHostToDevice));
             CUDA_TRY(cudaMemcpy(h->d_tile_faces, tfaces.data(), tfaces.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
             CUDA_TRY(cudaMemcpy(h->d_tile_slot, tslot.data(), (size_t) 6 * E * sizeof(int32_t), cudaMemcpyHostToDevice));
