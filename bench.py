@@ -604,7 +604,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--brick", type=int, default=1, help="trees along x (profiling sizes)")
     ap.add_argument("--only", default="both", choices=["both", "fp64", "mixed", "adjoint", "flame", "blast"])
-    ap.add_argument("--blast-steps", type=int, default=60, help="0 skips the AMR blast leg")
+    ap.add_argument("--blast-steps", type=int, default=200, help="0 skips the AMR blast leg")
     ap.add_argument("--flame-level", type=int, default=6)
     ap.add_argument("--flame-order", type=int, default=2, choices=[1, 2], help="basis order of the reacting leg")
     ap.add_argument("--flame-steps", type=int, default=5, help="0 skips the reacting-NS leg")

@@ -52,7 +52,7 @@ def _objects(verbose_ptxas: bool) -> list[tuple[list[str], str]]:
         jobs.append((cmd, obj))
     for src in C_SOURCES:
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-        cmd = ["gcc", "-O2", "-std=c99", "-fPIC", "-Wall", "-ffp-contract=off", "-c",
+        cmd = ["gcc", "-O2", "-std=c99", "-fPIC", "-Wall", "-ffp-contract=off", "-pthread", "-c",
                os.path.join(CSRC, src), "-o", obj] + inc
         jobs.append((cmd, obj))
     return jobs
@@ -75,7 +75,7 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
         sys.stderr.write("".join(logs))
     objs = [o for _, o in jobs]
     tmp = LIB + ".tmp"
-    _run([_nvcc(), GENCODE, "-shared", "-o", tmp] + objs + ["-lcudart"])
+    _run([_nvcc(), GENCODE, "-shared", "-o", tmp] + objs + ["-lcudart", "-lpthread"])
     os.replace(tmp, LIB)
     return LIB
 

@@ -9,8 +9,11 @@
  *     p4est_balance_ext(CHARM_CONNECT_FACE) with a replace callback
  *     (src/charm_amr.c:601-608).
  */
+#define _POSIX_C_SOURCE 200809L
 #include "charm_forest.h"
 
+#include <pthread.h>
+#include <unistd.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -115,11 +118,67 @@ int charm_forest_copy(charm_forest_t *dst, const charm_forest_t *src)
     return 0;
 }
 
+/* ---- parallel loops over leaves ------------------------------------------ */
+
+typedef struct {
+    charm_forest_range_fn fn;
+    void *ctx;
+    int64_t lo, hi;
+} range_job_t;
+
+static void *run_range_job(void *arg)
+{
+    const range_job_t *j = (const range_job_t *) arg;
+    j->fn(j->ctx, j->lo, j->hi);
+    return NULL;
+}
+
+/* Run fn(ctx, lo, hi) over [0, n) in contiguous chunks on up to the online
+ * CPU count of threads (the calling thread takes the first chunk).  Loops
+ * below 16384 iterations run serially, and a chunk whose thread cannot be
+ * started runs on the calling thread. */
+void charm_forest_parallel_for(int64_t n, charm_forest_range_fn fn, void *ctx)
+{
+    enum { kMaxThreads = 64 };
+    const long cpus = sysconf(_SC_NPROCESSORS_ONLN);
+    int nt = (cpus > 1) ? (int) (cpus < kMaxThreads ? cpus : kMaxThreads) : 1;
+    if ((int64_t) nt > n / 4096) nt = (int) (n / 4096);
+    if (n < 16384 || nt <= 1) {
+        fn(ctx, 0, n);
+        return;
+    }
+    range_job_t jobs[kMaxThreads];
+    pthread_t th[kMaxThreads];
+    int started[kMaxThreads];
+    for (int k = 0; k < nt; k++) {
+        jobs[k].fn = fn;
+        jobs[k].ctx = ctx;
+        jobs[k].lo = n * k / nt;
+        jobs[k].hi = n * (k + 1) / nt;
+        started[k] = 0;
+    }
+    for (int k = 1; k < nt; k++) started[k] = pthread_create(&th[k], NULL, run_range_job, &jobs[k]) == 0;
+    fn(ctx, jobs[0].lo, jobs[0].hi);
+    for (int k = 1; k < nt; k++) {
+        if (started[k]) pthread_join(th[k], NULL);
+        else fn(ctx, jobs[k].lo, jobs[k].hi);
+    }
+}
+
 /* ---- queries ------------------------------------------------------------ */
+
+typedef struct { const charm_forest_t *f; uint64_t *key; } keys_ctx_t;
+
+static void keys_range(void *c, int64_t lo, int64_t hi)
+{
+    const keys_ctx_t *k = (const keys_ctx_t *) c;
+    for (int64_t i = lo; i < hi; i++) k->key[i] = morton(k->f->leaf[i].x, k->f->leaf[i].y, k->f->leaf[i].z);
+}
 
 void charm_forest_keys(const charm_forest_t *f, uint64_t *key)
 {
-    for (int64_t i = 0; i < f->n; i++) key[i] = morton(f->leaf[i].x, f->leaf[i].y, f->leaf[i].z);
+    keys_ctx_t c = {f, key};
+    charm_forest_parallel_for(f->n, keys_range, &c);
 }
 
 int64_t charm_forest_find_k(const charm_forest_t *f, const uint64_t *keys, int32_t t, int32_t x, int32_t y,
@@ -371,15 +430,22 @@ static int needs_split(const charm_forest_t *f, const uint64_t *keys, int64_t i)
     return 0;
 }
 
+typedef struct { const charm_forest_t *f; const uint64_t *keys; int8_t *flag; } marks_ctx_t;
+
+static void marks_range(void *c, int64_t lo, int64_t hi)
+{
+    const marks_ctx_t *m = (const marks_ctx_t *) c;
+    for (int64_t i = lo; i < hi; i++) m->flag[i] = (int8_t) needs_split(m->f, m->keys, i);
+}
+
 int64_t charm_forest_balance_marks(const charm_forest_t *f, int8_t *flag)
 {
     int64_t marks = 0;
     uint64_t *keys = (uint64_t *) malloc(sizeof(uint64_t) * (size_t) (f->n > 0 ? f->n : 1));
     if (keys) charm_forest_keys(f, keys);
-    for (int64_t i = 0; i < f->n; i++) {
-        flag[i] = (int8_t) needs_split(f, keys, i);
-        marks += flag[i];
-    }
+    marks_ctx_t c = {f, keys, flag};
+    charm_forest_parallel_for(f->n, marks_range, &c);
+    for (int64_t i = 0; i < f->n; i++) marks += flag[i];
     free(keys);
     return marks;
 }
@@ -392,10 +458,10 @@ int64_t charm_forest_balance(charm_forest_t *f, charm_forest_replace_fn replace,
         uint64_t *keys = (uint64_t *) malloc(sizeof(uint64_t) * (size_t) (f->n > 0 ? f->n : 1));
         if (!flag || !keys) { free(flag); free(keys); return -1; }
         charm_forest_keys(f, keys);
+        marks_ctx_t c = {f, keys, flag};
+        charm_forest_parallel_for(f->n, marks_range, &c);
         int64_t marks = 0;
-        for (int64_t i = 0; i < f->n; i++) {
-            if (needs_split(f, keys, i)) { flag[i] = 1; marks++; }
-        }
+        for (int64_t i = 0; i < f->n; i++) marks += flag[i];
         free(keys);
         if (marks == 0) { free(flag); break; }
         int64_t r = charm_forest_refine(f, flag, -1, replace, user);

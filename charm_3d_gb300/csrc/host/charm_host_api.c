@@ -155,6 +155,15 @@ int charm_host_forest_adapt(charm_host_forest_t h, const int8_t *flags, int minl
 
 /* ---- flatten ------------------------------------------------------------- */
 
+typedef struct { const charm_forest_t *f; const uint64_t *keys; charm_face_nb_t *nbs; } nbs_ctx_t;
+
+static void nbs_range(void *c, int64_t lo, int64_t hi)
+{
+    const nbs_ctx_t *n = (const nbs_ctx_t *) c;
+    for (int64_t i = lo; i < hi; i++)
+        for (int face = 0; face < 6; face++) charm_forest_face_neighbor_k(n->f, n->keys, i, face, &n->nbs[6 * i + face]);
+}
+
 int charm_host_forest_flatten(charm_host_forest_t h, charm_gpu_mesh_t *mesh)
 {
     if (!h || !mesh) return CHARM_GPU_EINVAL;
@@ -167,8 +176,8 @@ int charm_host_forest_flatten(charm_host_forest_t h, charm_gpu_mesh_t *mesh)
     charm_face_nb_t *nbs = (charm_face_nb_t *) malloc(sizeof(charm_face_nb_t) * (size_t) (6 * (E > 0 ? E : 1)));
     if (!keys || !nbs) { free(keys); free(nbs); return CHARM_GPU_ENOMEM; }
     charm_forest_keys(f, keys);
-    for (int64_t i = 0; i < E; i++)
-        for (int face = 0; face < 6; face++) charm_forest_face_neighbor_k(f, keys, i, face, &nbs[6 * i + face]);
+    nbs_ctx_t nc = {f, keys, nbs};
+    charm_forest_parallel_for(E, nbs_range, &nc);
     free(keys);
     /* count */
     int64_t nf = 0, nb = 0;
@@ -272,12 +281,24 @@ static void leaf_h(const charm_forest_t *f, int level, double h[3])
     for (int d = 0; d < 3; d++) h[d] = ldexp(f->tree_len[d], -level);
 }
 
-/* charm_error_sqr_estimate (src/charm_amr.c:12-30) */
-static double err_sqr(const double *grad, int64_t E, int64_t i, double vol)
+/* vol^(5/3) as charm_error_sqr_estimate computes it, exp(log(vol) * 5 / 3),
+ * for the box volume of every level (the same value for all leaves of a
+ * level, so computed once per level instead of once per leaf) */
+static void level_vpow(const charm_forest_t *f, double vpow[CHARM_FOREST_MAXLEVEL + 1])
+{
+    for (int l = 0; l <= CHARM_FOREST_MAXLEVEL; l++) {
+        double h[3];
+        leaf_h(f, l, h);
+        vpow[l] = exp(log(h[0] * h[1] * h[2]) * 5. / 3.);
+    }
+}
+
+/* charm_error_sqr_estimate (src/charm_amr.c:12-30); vpow = vol^(5/3) */
+static double err_sqr(const double *grad, int64_t E, int64_t i, double vpow)
 {
     double diff2 = 0.;
     for (int k = 0; k < 3; k++) diff2 += grad[k * E + i] * grad[k * E + i];
-    return diff2 * (1. / 12.) * exp(log(vol) * 5. / 3.);
+    return diff2 * (1. / 12.) * vpow;
 }
 
 /* p1 L2 projection parent -> child for boxes (charm_replace_quads,
@@ -350,6 +371,7 @@ typedef struct {
     int64_t E;
     int nc, minlevel;
     double err2_max;
+    const double *vpow;        /* vol^(5/3) per level */
 } coarsen_state_ctx_t;
 
 /* charm_coarsen_err_estimate (src/charm_amr.c:90-142) */
@@ -370,7 +392,7 @@ static int coarsen_family(void *user, const charm_leaf_t *leaves, const int64_t 
     }
     double err2 = 0.;
     for (int i = 0; i < 8; i++) {
-        const double childerr2 = err_sqr(c->grad, c->E, idx[i], vol);
+        const double childerr2 = err_sqr(c->grad, c->E, idx[i], c->vpow[leaves[idx[0]].level]);
         if (childerr2 > c->err2_max * vol) return 0;
         err2 += childerr2;
         const double diff = (parentu - r[i]) * (parentu - r[i]);
@@ -392,13 +414,15 @@ int charm_host_forest_adapt_state(charm_host_forest_t h, const double *grad, dou
     int8_t *fl = (int8_t *) calloc((size_t) E0 + 1, 1);
     if (!u || !fl) { free(u); free(fl); return CHARM_GPU_ENOMEM; }
     memcpy(u, u_in, sizeof(double) * (size_t) V * 4 * (size_t) E0);
+    double vpow[CHARM_FOREST_MAXLEVEL + 1];
+    level_vpow(f, vpow);
     /* 1. refine (charm_refine_err_estimate, non-recursive, maxlevel) */
     for (int64_t i = 0; i < E0; i++) {
         if (f->leaf[i].level >= ml) continue;
         double hh[3];
         leaf_h(f, f->leaf[i].level, hh);
         const double vol = hh[0] * hh[1] * hh[2];
-        fl[i] = err_sqr(grad, E0, i, vol) > err2_max * vol;
+        fl[i] = err_sqr(grad, E0, i, vpow[f->leaf[i].level]) > err2_max * vol;
     }
     /* the gradient of the leaves after refinement: unchanged leaves keep theirs,
      * new children get NaN, so their family is never coarsened in this adapt */
@@ -424,7 +448,7 @@ int charm_host_forest_adapt_state(charm_host_forest_t h, const double *grad, dou
         charm_leaf_t *old = (charm_leaf_t *) malloc(sizeof(charm_leaf_t) * (size_t) (E + 1));
         if (!old) { free(u); free(g1); return CHARM_GPU_ENOMEM; }
         memcpy(old, f->leaf, sizeof(charm_leaf_t) * (size_t) E);
-        coarsen_state_ctx_t cc = {f, g1, u, E, n_comp, minlevel, err2_max};
+        coarsen_state_ctx_t cc = {f, g1, u, E, n_comp, minlevel, err2_max, vpow};
         int64_t nm = charm_forest_coarsen(f, minlevel, coarsen_family, NULL, &cc);
         if (nm < 0) { free(old); free(u); free(g1); return CHARM_GPU_ENOMEM; }
         if (nm > 0) {
