@@ -492,12 +492,13 @@ def _blast_run(case, steps: int, device: int, precision: str):
     t0 = time.perf_counter()
     while step < steps:
         if step and step % case.refine_period == 0:
+            # the state stays on the device: the host plans the adapt from the
+            # gradient estimate and the densities, the device projects
             ta = time.perf_counter()
             _, grad = gpu.refine_flags(case.max_err)
-            u = forest.adapt_state(grad, case.max_err, case.min_level, case.max_level, case.n_comp, gpu.get_state())
+            _, plan = forest.adapt_plan(grad, gpu.density_means(), case.max_err, case.min_level, case.max_level)
             mesh = forest.flatten()
-            gpu.upload(mesh)
-            gpu.set_state(u)
+            gpu.adapt_upload(plan, mesh)
             t_adapt += time.perf_counter() - ta
         n = min(case.refine_period - step % case.refine_period, steps - step)
         dev_ms += gpu.time_run(n, case.tau)

@@ -84,6 +84,12 @@ class Mesh(C.Structure):
                 ("bface_bnd", C.POINTER(C.c_int8))]
 
 
+class AdaptPlan(C.Structure):
+    """charm_gpu_adapt_plan_t: the projection passes of one adapt."""
+    _fields_ = [("n_pass", C.c_int32), ("pad", C.c_int32), ("n_in", C.c_int64),
+                ("n_out", C.POINTER(C.c_int64)), ("map", C.POINTER(C.POINTER(C.c_int32)))]
+
+
 # Every entry point declared in include/charm_gpu.h: (name, restype, argtypes).
 _P = C.c_void_p
 _I64P = C.POINTER(C.c_int64)
@@ -116,6 +122,8 @@ SIGNATURES = [
     ("charm_gpu_residual_adjoint", C.c_int, [_P, _P, _P]),
     ("charm_gpu_adjoint", C.c_int, [_P, C.c_int, C.c_int, C.POINTER(Objective), _P, _P, C.POINTER(AdjointInfo)]),
     ("charm_gpu_refine_flags_adjoint", C.c_int, [_P, C.c_double, _P, _P]),
+    ("charm_gpu_density_means", C.c_int, [_P, _P]),
+    ("charm_gpu_adapt_upload", C.c_int, [_P, C.POINTER(AdaptPlan), C.POINTER(Mesh)]),
     ("charm_host_forest_new", C.c_int, [C.POINTER(_P), _P, _P, _P, _P, C.c_int]),
     ("charm_host_forest_free", C.c_int, [_P]),
     ("charm_host_forest_count", C.c_int64, [_P]),
@@ -123,6 +131,8 @@ SIGNATURES = [
     ("charm_host_forest_adapt", C.c_int, [_P, _P, C.c_int, C.c_int, _I64P]),
     ("charm_host_forest_adapt_state", C.c_int, [_P, _P, C.c_double, C.c_int, C.c_int, C.c_int, _P, _I64P]),
     ("charm_host_forest_state", C.c_int, [_P, C.POINTER(_DP)]),
+    ("charm_host_forest_adapt_plan", C.c_int, [_P, _P, _P, C.c_double, C.c_int, C.c_int, _I64P,
+                                               C.POINTER(AdaptPlan)]),
     ("charm_host_forest_flatten", C.c_int, [_P, C.POINTER(Mesh)]),
     ("charm_host_forest_leaves", C.c_int, [_P, _P, _P]),
 ]

@@ -101,6 +101,8 @@ struct charm_gpu_handle_s {
     double *d_uc = nullptr;            // stage state after chemistry [V][B][E]
     double *d_chem_rhs = nullptr;      // heat release of the stage [E]
     double *d_dt = nullptr;            // CFL step (bits as unsigned long long)
+    double *d_proj[2] = {nullptr, nullptr};   // adapt projection ping-pong states
+    int32_t *d_pmap = nullptr;         // one pass of an adapt plan
     unsigned *d_err = nullptr;
     bool mesh_ready = false;
     // accounting
@@ -184,7 +186,10 @@ void free_mesh(charm_gpu_handle_s *h)
     }
     for (double *q : h->d_snap) cudaFree(q);
     h->d_snap.clear();
-    double **visc[] = {&h->d_s9, &h->d_vis, &h->d_radd, &h->d_dif, &h->d_uc, &h->d_chem_rhs};
+    double **visc[] = {&h->d_s9, &h->d_vis, &h->d_radd, &h->d_dif, &h->d_uc, &h->d_chem_rhs, &h->d_proj[0],
+                       &h->d_proj[1]};
+    if (h->d_pmap) cudaFree(h->d_pmap);
+    h->d_pmap = nullptr;
     for (double **q : visc) {
         if (*q) cudaFree(*q);
         *q = nullptr;
@@ -1232,6 +1237,130 @@ int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh)
     h->E = E; h->F = F; h->Fb = Fb; h->S = S;
     for (int d = 0; d < 3; d++) h->tree_len[d] = mesh->tree_len[d];
     h->mesh_ready = true;
+    return CHARM_GPU_OK;
+}
+
+// ---- adapt with the state on the device ------------------------------------
+
+// rho[e] = sum of the species' coefficient-0 planes (0 + s_0 + s_1 ..., the
+// host criterion's order)
+__global__ void __launch_bounds__(256) density_means_kernel(const double *__restrict__ u, int64_t E, int nb, int nc,
+                                                            double *__restrict__ rho)
+{
+    const int64_t e = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    double r = 0.0;
+    for (int s = 0; s < nc; s++) r += u[(int64_t) ((4 + s) * nb) * E + e];
+    rho[e] = r;
+}
+
+// One pass of an adapt plan (charm_gpu_adapt_plan_t): output leaf k of the
+// state [V][4][Eo] from the input state [V][4][Ei].  The parent <-> child
+// projections of charm_replace_quads (src/charm_amr.c:206-307) with the
+// operations, and their order, of the host octree's project_down /
+// project_up, rounded one by one (no contraction into FMA): the result is
+// the host's, bit for bit.
+__global__ void __launch_bounds__(256) adapt_project_kernel(const double *__restrict__ src, int64_t Ei,
+                                                            double *__restrict__ dst, int64_t Eo,
+                                                            const int32_t *__restrict__ map, int V)
+{
+    const int64_t k = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= Eo) return;
+    const int64_t s = map[2 * k];
+    const int op = map[2 * k + 1];
+    for (int v = 0; v < V; v++) {
+        const double *P = src + (int64_t) v * 4 * Ei;
+        double *Cn = dst + (int64_t) v * 4 * Eo;
+        if (op < 0) {
+            for (int b = 0; b < 4; b++) Cn[(int64_t) b * Eo + k] = P[(int64_t) b * Ei + s];
+        } else if (op < 8) {
+            const double o0 = (op & 1) ? 0.25 : -0.25, o1 = (op & 2) ? 0.25 : -0.25, o2 = (op & 4) ? 0.25 : -0.25;
+            double x = __dadd_rn(P[s], __dmul_rn(o0, P[Ei + s]));
+            x = __dadd_rn(x, __dmul_rn(o1, P[2 * Ei + s]));
+            x = __dadd_rn(x, __dmul_rn(o2, P[3 * Ei + s]));
+            Cn[k] = x;
+            for (int b = 1; b < 4; b++) Cn[(int64_t) b * Eo + k] = __dmul_rn(0.5, P[(int64_t) b * Ei + s]);
+        } else {
+            double m = 0.0, sk[3] = {0.0, 0.0, 0.0};
+            for (int i = 0; i < 8; i++) {
+                const double c0 = P[s + i];
+                m = __dadd_rn(m, c0);
+                for (int d = 0; d < 3; d++) {
+                    const double sg = ((i >> d) & 1) ? 0.375 : -0.375;
+                    sk[d] = __dadd_rn(sk[d], __dadd_rn(__dmul_rn(sg, c0),
+                                                       __dmul_rn(P[(int64_t) (d + 1) * Ei + s + i], 1. / 16.)));
+                }
+            }
+            Cn[k] = __dmul_rn(m, 0.125);
+            for (int d = 0; d < 3; d++) Cn[(int64_t) (d + 1) * Eo + k] = sk[d];
+        }
+    }
+}
+
+int charm_gpu_density_means(charm_gpu_handle_t h, double *rho)
+{
+    int rc = check_ready(h);
+    if (rc) return rc;
+    if (!rho) return fail(CHARM_GPU_EINVAL, "null argument");
+    if (h->cfg.precision == CHARM_GPU_PREC_MIXED && (rc = ff_convert(h, false))) return rc;   // d_u <- hi + lo
+    if ((rc = ensure_buf(h, &h->d_proj[0], sizeof(double) * (size_t) h->E))) return rc;
+    density_means_kernel<<<(unsigned) ((h->E + 255) / 256), 256, 0, h->stream>>>(h->d_u, h->E, h->nb, h->cfg.n_comp,
+                                                                                  h->d_proj[0]);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(rho, h->d_proj[0], sizeof(double) * (size_t) h->E, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return CHARM_GPU_OK;
+}
+
+int charm_gpu_adapt_upload(charm_gpu_handle_t h, const charm_gpu_adapt_plan_t *plan, const charm_gpu_mesh_t *mesh)
+{
+    int rc = check_ready(h);
+    if (rc) return rc;
+    if (!plan || !mesh || (plan->n_pass > 0 && (!plan->n_out || !plan->map))) return fail(CHARM_GPU_EINVAL, "null argument");
+    if (h->nb != CHARM_GPU_BASIS) return fail(CHARM_GPU_ENOTSUP, "adapt projection: p1 only");
+    if (plan->n_in != h->E) return fail(CHARM_GPU_EINVAL, "adapt plan: input leaves differ from the uploaded mesh");
+    const int64_t n_last = plan->n_pass ? plan->n_out[plan->n_pass - 1] : plan->n_in;
+    if (n_last != mesh->n_elem) return fail(CHARM_GPU_EINVAL, "adapt plan: output leaves differ from the mesh");
+    const bool mixed = h->cfg.precision == CHARM_GPU_PREC_MIXED;
+    if (mixed && (rc = ff_convert(h, false))) return rc;   // d_u <- hi + lo
+    const int V = n_var(h);
+    int64_t nmax = plan->n_in;
+    for (int p = 0; p < plan->n_pass; p++) {
+        if (plan->n_out[p] < 1 || plan->n_out[p] > INT32_MAX) return fail(CHARM_GPU_EINVAL, "adapt plan: bad pass size");
+        nmax = std::max(nmax, plan->n_out[p]);
+    }
+    const size_t sb = sizeof(double) * (size_t) V * 4 * (size_t) nmax;
+    if ((rc = ensure_buf(h, &h->d_proj[0], sb)) || (rc = ensure_buf(h, &h->d_proj[1], sb)) ||
+        (rc = ensure_buf(h, &h->d_pmap, sizeof(int32_t) * 2 * (size_t) nmax)))
+        return rc;
+    const double *src = h->d_u;
+    int64_t Ei = plan->n_in;
+    double *dst = h->d_proj[0];
+    if (plan->n_pass == 0)
+        CUDA_TRY(cudaMemcpyAsync(dst, src, sizeof(double) * (size_t) V * 4 * (size_t) Ei, cudaMemcpyDeviceToDevice,
+                                 h->stream));
+    for (int p = 0; p < plan->n_pass; p++) {
+        const int64_t Eo = plan->n_out[p];
+        // the map's sources must lie in the pass's input (a bad plan must not
+        // send the kernel out of bounds)
+        const int32_t *mp = plan->map[p];
+        for (int64_t k = 0; k < Eo; k++) {
+            const int32_t sidx = mp[2 * k], op = mp[2 * k + 1];
+            if (op < -1 || op > 8 || sidx < 0 || (int64_t) sidx + (op == 8 ? 8 : 1) > Ei)
+                return fail(CHARM_GPU_EINVAL, "adapt plan: map entry out of range");
+        }
+        dst = h->d_proj[p & 1];
+        CUDA_TRY(cudaMemcpyAsync(h->d_pmap, mp, sizeof(int32_t) * 2 * (size_t) Eo, cudaMemcpyHostToDevice, h->stream));
+        adapt_project_kernel<<<(unsigned) ((Eo + 255) / 256), 256, 0, h->stream>>>(src, Ei, dst, Eo, h->d_pmap, V);
+        CUDA_TRY(cudaGetLastError());
+        src = dst;
+        Ei = Eo;
+    }
+    if ((rc = charm_gpu_upload_mesh(h, mesh))) return rc;
+    CUDA_TRY(cudaMemcpyAsync(h->d_u, dst, sizeof(double) * (size_t) V * 4 * (size_t) h->E, cudaMemcpyDeviceToDevice,
+                             h->stream));
+    if (mixed && (rc = ff_convert(h, true))) return rc;
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
     return CHARM_GPU_OK;
 }
 

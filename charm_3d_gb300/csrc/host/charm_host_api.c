@@ -24,6 +24,11 @@ struct charm_host_forest_s {
     charm_forest_t f;
     int8_t bnd_of_side[6];
     double *state;          /* state projected by the last charm_host_forest_adapt_state */
+    /* projection plan of the last charm_host_forest_adapt_plan */
+    int plan_n, plan_cap;
+    int64_t plan_n_in;
+    int64_t *plan_nout;
+    int32_t **plan_map;
     /* flattened arrays (owned) */
     double  *center;
     int8_t  *level;
@@ -59,10 +64,19 @@ int charm_host_forest_new(charm_host_forest_t *out, const int32_t ntree[3], cons
     return CHARM_GPU_OK;
 }
 
+static void free_plan(struct charm_host_forest_s *h)
+{
+    for (int p = 0; p < h->plan_n; p++) free(h->plan_map[p]);
+    h->plan_n = 0;
+}
+
 int charm_host_forest_free(charm_host_forest_t h)
 {
     if (!h) return CHARM_GPU_EINVAL;
     free_flat(h);
+    free_plan(h);
+    free(h->plan_map);
+    free(h->plan_nout);
     free(h->state);
     charm_forest_free(&h->f);
     free(h);
@@ -364,9 +378,69 @@ static int refine_state(charm_forest_t *f, const int8_t *fl, int V, double **u)
     return CHARM_GPU_OK;
 }
 
+/* Append a pass to the plan (takes ownership of map). */
+static int plan_push(struct charm_host_forest_s *h, int64_t n_out, int32_t *map)
+{
+    if (h->plan_n == h->plan_cap) {
+        const int cap = h->plan_cap ? 2 * h->plan_cap : 8;
+        int64_t *no = (int64_t *) realloc(h->plan_nout, sizeof(int64_t) * (size_t) cap);
+        if (!no) return CHARM_GPU_ENOMEM;
+        h->plan_nout = no;
+        int32_t **nm = (int32_t **) realloc(h->plan_map, sizeof(int32_t *) * (size_t) cap);
+        if (!nm) return CHARM_GPU_ENOMEM;
+        h->plan_map = nm;
+        h->plan_cap = cap;
+    }
+    h->plan_nout[h->plan_n] = n_out;
+    h->plan_map[h->plan_n] = map;
+    h->plan_n++;
+    return CHARM_GPU_OK;
+}
+
+/* refine flagged leaves one level and record the pass: output leaf k is a
+ * copy of old leaf i (op -1) or child cid of old leaf i (op cid); the
+ * centre densities *rho follow (children: NaN, never read: families made in
+ * this adapt are not coarsened) */
+static int refine_plan(struct charm_host_forest_s *h, const int8_t *fl, double **rho)
+{
+    charm_forest_t *f = &h->f;
+    const int64_t E = f->n;
+    charm_leaf_t *old = (charm_leaf_t *) malloc(sizeof(charm_leaf_t) * (size_t) (E + 1));
+    if (!old) return CHARM_GPU_ENOMEM;
+    memcpy(old, f->leaf, sizeof(charm_leaf_t) * (size_t) E);
+    if (charm_forest_refine(f, fl, -1, NULL, NULL) < 0) { free(old); return CHARM_GPU_ENOMEM; }
+    const int64_t En = f->n;
+    int32_t *map = (int32_t *) malloc(sizeof(int32_t) * 2 * (size_t) (En > 0 ? En : 1));
+    double *r = (double *) malloc(sizeof(double) * (size_t) (En > 0 ? En : 1));
+    if (!map || !r) { free(old); free(map); free(r); return CHARM_GPU_ENOMEM; }
+    int64_t k = 0;
+    for (int64_t i = 0; i < E; i++) {
+        if (fl[i] && old[i].level < CHARM_FOREST_MAXLEVEL - 1) {
+            for (int c = 0; c < 8; c++) {
+                map[2 * (k + c)] = (int32_t) i;
+                map[2 * (k + c) + 1] = charm_leaf_child_id(&f->leaf[k + c]);
+                r[k + c] = NAN;
+            }
+            k += 8;
+        } else {
+            map[2 * k] = (int32_t) i;
+            map[2 * k + 1] = -1;
+            r[k] = (*rho)[i];
+            k++;
+        }
+    }
+    free(old);
+    free(*rho);
+    *rho = r;
+    int rc = plan_push(h, En, map);
+    if (rc) free(map);
+    return rc;
+}
+
 typedef struct {
     const charm_forest_t *f;
     const double *grad;        /* per current leaf, NaN for leaves new in this adapt */
+    const double *rho;         /* centre densities per current leaf (plan mode), else NULL */
     const double *u;
     int64_t E;
     int nc, minlevel;
@@ -385,7 +459,9 @@ static int coarsen_family(void *user, const charm_leaf_t *leaves, const int64_t 
     double r[8], parentu = 0.;
     for (int i = 0; i < 8; i++) {
         double ri = 0.;   /* prim.r at the centre: sum of the partial-density means, eos flag 4 clamp */
-        for (int s = 0; s < c->nc; s++) ri += c->u[((int64_t) (4 + s) * 4) * c->E + idx[i]];
+        if (c->rho) ri = c->rho[idx[i]];
+        else
+            for (int s = 0; s < c->nc; s++) ri += c->u[((int64_t) (4 + s) * 4) * c->E + idx[i]];
         if (ri < 1.e-12) ri = 1.e-12;
         r[i] = ri;
         parentu += ri / 8;
@@ -401,19 +477,33 @@ static int coarsen_family(void *user, const charm_leaf_t *leaves, const int64_t 
     return err2 < c->err2_max * (vol * 8) ? 1 : 0;
 }
 
-int charm_host_forest_adapt_state(charm_host_forest_t h, const double *grad, double max_err, int minlevel, int maxlevel,
-                                  int n_comp, const double *u_in, int64_t *n_new)
+/* The adapt of charm_adapt.  State mode (u_in): the state [V][4][E] is
+ * projected along, into h->state.  Plan mode (rho_in): only the centre
+ * densities [E] that the coarsening criterion reads are carried, and every
+ * projection is recorded as a pass of h's plan instead. */
+static int adapt_core(struct charm_host_forest_s *h, const double *grad, double max_err, int minlevel, int maxlevel,
+                      int n_comp, const double *u_in, const double *rho_in, int64_t *n_new)
 {
-    if (!h || !grad || !u_in || n_comp < 1 || n_comp > CHARM_GPU_MAX_COMP) return CHARM_GPU_EINVAL;
     charm_forest_t *f = &h->f;
     const int V = 4 + n_comp;
     const int64_t E0 = f->n;
     const double err2_max = max_err * max_err;
-    int ml = (maxlevel < 0 || maxlevel > CHARM_FOREST_MAXLEVEL - 1) ? CHARM_FOREST_MAXLEVEL - 1 : maxlevel;
-    double *u = (double *) malloc(sizeof(double) * (size_t) V * 4 * (size_t) E0);
+    const int ml = (maxlevel < 0 || maxlevel > CHARM_FOREST_MAXLEVEL - 1) ? CHARM_FOREST_MAXLEVEL - 1 : maxlevel;
+    const int plan = (u_in == NULL);
+    double *u = NULL, *rho = NULL;
+    if (plan) {
+        free_plan(h);
+        h->plan_n_in = E0;
+        rho = (double *) malloc(sizeof(double) * (size_t) (E0 > 0 ? E0 : 1));
+        if (!rho) return CHARM_GPU_ENOMEM;
+        memcpy(rho, rho_in, sizeof(double) * (size_t) E0);
+    } else {
+        u = (double *) malloc(sizeof(double) * (size_t) V * 4 * (size_t) E0);
+        if (!u) return CHARM_GPU_ENOMEM;
+        memcpy(u, u_in, sizeof(double) * (size_t) V * 4 * (size_t) E0);
+    }
     int8_t *fl = (int8_t *) calloc((size_t) E0 + 1, 1);
-    if (!u || !fl) { free(u); free(fl); return CHARM_GPU_ENOMEM; }
-    memcpy(u, u_in, sizeof(double) * (size_t) V * 4 * (size_t) E0);
+    if (!fl) { free(u); free(rho); return CHARM_GPU_ENOMEM; }
     double vpow[CHARM_FOREST_MAXLEVEL + 1];
     level_vpow(f, vpow);
     /* 1. refine (charm_refine_err_estimate, non-recursive, maxlevel) */
@@ -429,7 +519,7 @@ int charm_host_forest_adapt_state(charm_host_forest_t h, const double *grad, dou
     int64_t E1 = E0;
     for (int64_t i = 0; i < E0; i++) E1 += fl[i] ? 7 : 0;
     double *g1 = (double *) malloc(sizeof(double) * 3 * (size_t) E1);
-    if (!g1) { free(u); free(fl); return CHARM_GPU_ENOMEM; }
+    if (!g1) { free(u); free(rho); free(fl); return CHARM_GPU_ENOMEM; }
     {
         int64_t k = 0;
         for (int64_t i = 0; i < E0; i++) {
@@ -439,57 +529,110 @@ int charm_host_forest_adapt_state(charm_host_forest_t h, const double *grad, dou
             k += n;
         }
     }
-    int rc = refine_state(f, fl, V, &u);
+    int rc = plan ? refine_plan(h, fl, &rho) : refine_state(f, fl, V, &u);
     free(fl);
-    if (rc) { free(u); free(g1); return rc; }
+    if (rc) { free(u); free(rho); free(g1); return rc; }
     /* 2. coarsen complete families (charm_coarsen_err_estimate, non-recursive) */
     {
         const int64_t E = f->n;
         charm_leaf_t *old = (charm_leaf_t *) malloc(sizeof(charm_leaf_t) * (size_t) (E + 1));
-        if (!old) { free(u); free(g1); return CHARM_GPU_ENOMEM; }
+        if (!old) { free(u); free(rho); free(g1); return CHARM_GPU_ENOMEM; }
         memcpy(old, f->leaf, sizeof(charm_leaf_t) * (size_t) E);
-        coarsen_state_ctx_t cc = {f, g1, u, E, n_comp, minlevel, err2_max, vpow};
+        coarsen_state_ctx_t cc = {f, g1, rho, u, E, n_comp, minlevel, err2_max, vpow};
         int64_t nm = charm_forest_coarsen(f, minlevel, coarsen_family, NULL, &cc);
-        if (nm < 0) { free(old); free(u); free(g1); return CHARM_GPU_ENOMEM; }
+        if (nm < 0) { free(old); free(u); free(rho); free(g1); return CHARM_GPU_ENOMEM; }
         if (nm > 0) {
             const int64_t En = f->n;
-            double *w = (double *) malloc(sizeof(double) * (size_t) V * 4 * (size_t) En);
-            if (!w) { free(old); free(u); free(g1); return CHARM_GPU_ENOMEM; }
+            double *w = plan ? NULL : (double *) malloc(sizeof(double) * (size_t) V * 4 * (size_t) En);
+            int32_t *map = plan ? (int32_t *) malloc(sizeof(int32_t) * 2 * (size_t) En) : NULL;
+            if (plan ? !map : !w) { free(old); free(u); free(rho); free(g1); return CHARM_GPU_ENOMEM; }
             int64_t i = 0;
             for (int64_t k = 0; k < En; k++) {
                 const charm_leaf_t *nl = &f->leaf[k], *ol = &old[i];
                 if (ol->level == nl->level && ol->x == nl->x && ol->y == nl->y && ol->z == nl->z && ol->tree == nl->tree) {
-                    for (int v = 0; v < V; v++)
-                        for (int b = 0; b < 4; b++) w[((int64_t) v * 4 + b) * En + k] = u[((int64_t) v * 4 + b) * E + i];
+                    if (plan) {
+                        map[2 * k] = (int32_t) i;
+                        map[2 * k + 1] = -1;
+                    } else {
+                        for (int v = 0; v < V; v++)
+                            for (int b = 0; b < 4; b++)
+                                w[((int64_t) v * 4 + b) * En + k] = u[((int64_t) v * 4 + b) * E + i];
+                    }
                     i++;
                 } else {
                     int64_t ch[8];
                     int cid[8];
                     for (int c = 0; c < 8; c++) { ch[c] = i + c; cid[c] = charm_leaf_child_id(&old[i + c]); }
-                    project_up(u, E, ch, cid, w, En, k, V);
+                    if (plan) {
+                        /* a family in Morton order: child ids 0..7 in turn */
+                        for (int c = 0; c < 8; c++)
+                            if (cid[c] != c) { free(map); free(old); free(rho); free(g1); return CHARM_GPU_EINVAL; }
+                        map[2 * k] = (int32_t) i;
+                        map[2 * k + 1] = 8;
+                    } else {
+                        project_up(u, E, ch, cid, w, En, k, V);
+                    }
                     i += 8;
                 }
             }
-            free(u);
-            u = w;
+            if (plan) {
+                if ((rc = plan_push(h, En, map))) { free(map); free(old); free(rho); free(g1); return rc; }
+            } else {
+                free(u);
+                u = w;
+            }
         }
         free(old);
     }
     free(g1);
+    free(rho);   /* the balance passes do not read densities */
+    rho = NULL;
     /* 3. 2:1 face balance, one level per pass (p4est_balance_ext with charm_replace_quads) */
     for (;;) {
         int8_t *bf = (int8_t *) calloc((size_t) f->n + 1, 1);
         if (!bf) { free(u); return CHARM_GPU_ENOMEM; }
         int64_t marks = charm_forest_balance_marks(f, bf);
-        if (marks) rc = refine_state(f, bf, V, &u);
+        if (marks) {
+            if (plan) {
+                double *dummy = (double *) calloc((size_t) f->n + 1, sizeof(double));
+                rc = dummy ? refine_plan(h, bf, &dummy) : CHARM_GPU_ENOMEM;
+                free(dummy);
+            } else {
+                rc = refine_state(f, bf, V, &u);
+            }
+        }
         free(bf);
         if (rc) { free(u); return rc; }
         if (!marks) break;
     }
-    free(h->state);
-    h->state = u;
+    if (!plan) {
+        free(h->state);
+        h->state = u;
+    }
     free_flat(h);
     if (n_new) *n_new = f->n;
+    return CHARM_GPU_OK;
+}
+
+int charm_host_forest_adapt_state(charm_host_forest_t h, const double *grad, double max_err, int minlevel, int maxlevel,
+                                  int n_comp, const double *u_in, int64_t *n_new)
+{
+    if (!h || !grad || !u_in || n_comp < 1 || n_comp > CHARM_GPU_MAX_COMP) return CHARM_GPU_EINVAL;
+    return adapt_core(h, grad, max_err, minlevel, maxlevel, n_comp, u_in, NULL, n_new);
+}
+
+int charm_host_forest_adapt_plan(charm_host_forest_t h, const double *grad, const double *rho, double max_err,
+                                 int minlevel, int maxlevel, int64_t *n_new, charm_gpu_adapt_plan_t *plan)
+{
+    if (!h || !grad || !rho) return CHARM_GPU_EINVAL;
+    int rc = adapt_core(h, grad, max_err, minlevel, maxlevel, 1, NULL, rho, n_new);
+    if (rc) return rc;
+    if (plan) {
+        plan->n_pass = h->plan_n;
+        plan->n_in = h->plan_n_in;
+        plan->n_out = h->plan_nout;
+        plan->map = (const int32_t *const *) h->plan_map;
+    }
     return CHARM_GPU_OK;
 }
 

@@ -105,6 +105,21 @@ class Forest:
         abi.check(self.lib.charm_host_forest_state(self.h, C.byref(p)), "charm_host_forest_state")
         return np.ctypeslib.as_array(p, (4 + n_comp, 4, n.value)).copy()
 
+    def adapt_plan(self, grad: np.ndarray, rho: np.ndarray, max_err: float, minlevel: int,
+                   maxlevel: int) -> tuple[int, abi.AdaptPlan]:
+        """The adapt of adapt_state without the state: the coarsening criterion
+        reads the centre densities rho [E] (Solver.density_means) and the
+        projections come back as a plan for Solver.adapt_upload (valid until
+        the next adapt of this forest)."""
+        g = np.ascontiguousarray(grad, dtype=np.float64)
+        r = np.ascontiguousarray(rho, dtype=np.float64)
+        n = C.c_int64()
+        plan = abi.AdaptPlan()
+        abi.check(self.lib.charm_host_forest_adapt_plan(self.h, g.ctypes.data, r.ctypes.data, max_err, minlevel,
+                                                        maxlevel, C.byref(n), C.byref(plan)),
+                  "charm_host_forest_adapt_plan")
+        return n.value, plan
+
     def leaves(self) -> tuple[np.ndarray, np.ndarray]:
         n = len(self)
         q = np.empty((n, 4), np.int32)
@@ -232,6 +247,19 @@ class Solver:
         abi.check(self.lib.charm_gpu_refine_flags(self.h, max_err, flags.ctypes.data, grad.ctypes.data),
                   "charm_gpu_refine_flags")
         return flags, grad
+
+    def density_means(self) -> np.ndarray:
+        """Sum of the species' mean coefficients per leaf (the coarsening criterion's densities)."""
+        rho = np.empty(self.n_elem)
+        abi.check(self.lib.charm_gpu_density_means(self.h, rho.ctypes.data), "charm_gpu_density_means")
+        return rho
+
+    def adapt_upload(self, plan: abi.AdaptPlan, mesh: MeshArrays) -> None:
+        """Carry the device state through an adapt plan and upload the adapted mesh."""
+        abi.check(self.lib.charm_gpu_adapt_upload(self.h, C.byref(plan), C.byref(mesh.struct())),
+                  "charm_gpu_adapt_upload")
+        self.n_elem = mesh.n_elem
+        self.mesh = mesh
 
     def refine_flags_adjoint(self, max_err: float) -> tuple[np.ndarray, np.ndarray]:
         """Adjoint-weighted refine flags and the weighted gradient [3][E] (after adjoint())."""

@@ -306,6 +306,32 @@ int charm_gpu_adjoint(charm_gpu_handle_t h, int n_steps, int n_snapshots, const 
  * that time.  CHARM_GPU_ESTATE when no adjoint has been computed. */
 int charm_gpu_refine_flags_adjoint(charm_gpu_handle_t h, double max_err, int8_t *flags, double *grad_out);
 
+/* Projection plan of an adapt, for carrying a device-resident state through
+ * it (charm_gpu_adapt_upload).  Pass p maps the leaves before it to its
+ * n_out[p] output leaves; for output leaf k, map[p][2k] is a leaf of the
+ * pass's input and map[p][2k+1] the operation: -1 copy; 0..7 the child with
+ * that Morton child id of that leaf (charm_replace_quads' parent -> child
+ * projection); 8 the parent of the family of 8 consecutive input leaves
+ * starting there (children -> parent).  The passes are refine, coarsen (when
+ * some family merged) and one per 2:1 balance ripple, in order. */
+typedef struct {
+    int32_t n_pass, pad;
+    int64_t n_in;                 /* leaves before the adapt */
+    const int64_t *n_out;         /* [n_pass] */
+    const int32_t *const *map;    /* [n_pass] -> int32 [2 * n_out[p]] */
+} charm_gpu_adapt_plan_t;
+
+/* rho[e] = sum over the species of their mean coefficient in the current
+ * state: the centre density that the reference's coarsening criterion reads
+ * (before its clamp). */
+int charm_gpu_density_means(charm_gpu_handle_t h, double *rho);
+
+/* Carry the device state through `plan` (p1 projections of
+ * charm_replace_quads, src/charm_amr.c:206-307, the arithmetic of
+ * charm_host_forest_adapt_state) and upload `mesh`, the flattened forest
+ * after that adapt: the state stays on the device across the adapt. */
+int charm_gpu_adapt_upload(charm_gpu_handle_t h, const charm_gpu_adapt_plan_t *plan, const charm_gpu_mesh_t *mesh);
+
 /* ---- host octree (the CPU side of the boundary) -------------------------- */
 
 typedef struct charm_host_forest_s *charm_host_forest_t;
@@ -338,6 +364,14 @@ int charm_host_forest_adapt(charm_host_forest_t f, const int8_t *flags, int minl
 int charm_host_forest_adapt_state(charm_host_forest_t f, const double *grad, double max_err, int minlevel, int maxlevel,
                                   int n_comp, const double *u_in, int64_t *n_new);
 int charm_host_forest_state(charm_host_forest_t f, const double **u_out);
+
+/* The adapt of charm_host_forest_adapt_state without the state: the family
+ * coarsening criterion reads the centre densities rho ([E], the sum of the
+ * species' mean coefficients: charm_gpu_density_means) in place of the
+ * state, and the projections are recorded in *plan (valid until the next
+ * adapt or free of f).  Same forest as charm_host_forest_adapt_state. */
+int charm_host_forest_adapt_plan(charm_host_forest_t f, const double *grad, const double *rho, double max_err,
+                                 int minlevel, int maxlevel, int64_t *n_new, charm_gpu_adapt_plan_t *plan);
 
 /* Flatten into a mesh view whose arrays live inside the forest object and
  * stay valid until the next adapt/flatten/free. */

@@ -1,0 +1,104 @@
+"""The adapt without the state (charm_host_forest_adapt_plan): the same
+forest as charm_host_forest_adapt_state, and its projection plan, applied
+with the host's arithmetic (numpy, one rounding per operation as the host
+C code without FMA contraction), gives the state adapt_state projects, bit
+for bit.  Cases that refine, coarsen and need balance ripples.  CPU only
+(the device applies the same plan: tests/test_gpu_adapt_plan.py)."""
+import numpy as np
+import pytest
+
+from charm_3d_gb300.solver import Forest
+from oracle.port import Port
+
+from .common import small_case
+
+
+def apply_plan(plan, u: np.ndarray) -> np.ndarray:
+    """The passes of an AdaptPlan on a state [V][4][E] (the host octree's
+    project_down / project_up, in the same order of operations)."""
+    for p in range(plan.n_pass):
+        Eo = plan.n_out[p]
+        m = np.ctypeslib.as_array(plan.map[p], (2 * Eo,)).reshape(Eo, 2)
+        src, op = m[:, 0].astype(np.int64), m[:, 1]
+        V = u.shape[0]
+        out = np.empty((V, 4, Eo))
+        cp, dn, up = op < 0, (op >= 0) & (op < 8), op == 8
+        out[:, :, cp] = u[:, :, src[cp]]
+        if dn.any():
+            s, c = src[dn], op[dn]
+            o = [np.where((c >> d) & 1, 0.25, -0.25) for d in range(3)]
+            x = u[:, 0, s] + o[0] * u[:, 1, s]
+            x = x + o[1] * u[:, 2, s]
+            x = x + o[2] * u[:, 3, s]
+            out[:, 0, dn] = x
+            out[:, 1:, dn] = 0.5 * u[:, 1:, s]
+        if up.any():
+            s = src[up]
+            mm = np.zeros((V, s.size))
+            sk = np.zeros((V, 3, s.size))
+            for i in range(8):
+                c0 = u[:, 0, s + i]
+                mm = mm + c0
+                for d in range(3):
+                    sg = 0.375 if (i >> d) & 1 else -0.375
+                    sk[:, d] = sk[:, d] + (sg * c0 + u[:, d + 1, s + i] * (1.0 / 16.0))
+            out[:, 0, up] = mm * 0.125
+            out[:, 1:, up] = sk
+        u = out
+    return u
+
+
+@pytest.mark.parametrize("kind,max_err,minl,level,rounds", [("sod", 0.05, 1, 2, 3), ("random", 0.3, 1, 2, 3),
+                                                             ("random", 0.6, 1, 3, 2), ("mix2", 0.3, 1, 2, 3)])
+def test_adapt_plan_matches_adapt_state(kind, max_err, minl, level, rounds):
+    case = small_case(kind, "HLLC", "BJ", level=level)
+    fa, fb = Forest(case), Forest(case)
+    mesh = fa.flatten()
+    u = case.initial_state(mesh.center)
+    V = case.n_var
+    for r in range(rounds):
+        port = Port(case.config(), mesh)
+        port.set_state(u)
+        grad = port.amr_grad()
+        port.close()
+        rho = u[4:V, 0].sum(axis=0) if V > 5 else u[4, 0].copy()
+        n_a = len(fa)
+        ua = fa.adapt_state(grad, max_err, minl, level + 2, case.n_comp, u)
+        n_b, plan = fb.adapt_plan(grad, rho, max_err, minl, level + 2)
+        assert plan.n_in == n_a
+        qa, la = fa.leaves()
+        qb, lb = fb.leaves()
+        assert n_b == len(fa) and (qa == qb).all() and (la == lb).all()
+        ub = apply_plan(plan, u)
+        assert ub.shape == ua.shape
+        assert np.array_equal(ub, ua), f"round {r}"
+        mesh = fa.flatten()
+        u = ua
+
+
+def test_adapt_plan_balance_ripples():
+    """A point refined three times in a row: the second and third adapts need
+    2:1 balance ripples (passes after the refine pass)."""
+    case = small_case("random", "HLLC", "BJ", level=2)
+    fa, fb = Forest(case), Forest(case)
+    mesh = fa.flatten()
+    u = case.initial_state(mesh.center)
+    V = case.n_var
+    ripple = 0
+    for r in range(3):
+        # refine the leaf holding the point (0.30, 0.30, 0.30)
+        d = np.abs(mesh.center - 0.30).max(axis=0)
+        grad = np.zeros((3, mesh.n_elem))
+        grad[0, int(np.argmin(d))] = 1.0e6
+        rho = u[4:V, 0].sum(axis=0)
+        ua = fa.adapt_state(grad, 0.01, 1, 6, case.n_comp, u)
+        n_b, plan = fb.adapt_plan(grad, rho, 0.01, 1, 6)
+        qa, la = fa.leaves()
+        qb, lb = fb.leaves()
+        assert n_b == len(fa) and (qa == qb).all() and (la == lb).all()
+        ub = apply_plan(plan, u)
+        assert np.array_equal(ub, ua), f"round {r}"
+        ripple += max(0, plan.n_pass - 1)
+        mesh = fa.flatten()
+        u = ua
+    assert ripple > 0
