@@ -166,3 +166,56 @@ def test_adapt_coarsens_complete_families_only():
     flags[:3] = 0          # first family keeps three non-coarsening members
     n = f.adapt(flags, 0, 5)
     assert n == 8 + 7      # first family stays, the other 7 merge
+
+
+def vectorized_face_check(forest, case, mesh):
+    """Geometric checks of every face record in O(E) (for meshes where the
+    brute-force matcher is too slow): conforming sides are same-size boxes
+    touching across the face with equal tangential extent, mortar sub-faces
+    a half-size box inside the big side's face at its sub position, boundary
+    faces on the domain boundary; the records' areas close every element."""
+    lo, ln, lv = boxes(forest, case)
+    ext = np.array(case.brick, np.int64) * (1 << 19)
+    fe, info = mesh.face_elem.astype(np.int64), mesh.face_info.astype(np.int64)
+    a, b, d = fe[0], fe[1], info & 3
+    kind, sub, wrap = (info >> 2) & 3, (info >> 4) & 3, (info >> 6) & 1
+    k = np.arange(mesh.n_face)
+    s_ax = np.where(d == 0, 1, 0)
+    t_ax = np.where(d == 2, 1, 2)
+    # side 0's upper face coordinate meets side 1's lower face (mod period)
+    top_a = (lo[a, d] + ln[a]) % ext[d]
+    assert (top_a == lo[b, d]).all()
+    assert ((lo[a, d] + ln[a] == ext[d]) == (wrap == 1)).all()
+    small = np.where(kind == 2, b, a)
+    big = np.where(kind == 2, a, b)
+    conf = kind == 0
+    assert (ln[a[conf]] == ln[b[conf]]).all()
+    assert (lo[a[conf], s_ax[conf]] == lo[b[conf], s_ax[conf]]).all()
+    assert (lo[a[conf], t_ax[conf]] == lo[b[conf], t_ax[conf]]).all()
+    hang = ~conf
+    sm, bg, kk = small[hang], big[hang], k[hang]
+    assert (2 * ln[sm] == ln[bg]).all()
+    off_s = lo[sm, s_ax[kk]] - lo[bg, s_ax[kk]]
+    off_t = lo[sm, t_ax[kk]] - lo[bg, t_ax[kk]]
+    assert (off_s == (sub[kk] & 1) * ln[sm]).all() and (off_t == ((sub[kk] >> 1) & 1) * ln[sm]).all()
+    # boundary records lie on the domain boundary
+    be, bf = mesh.bface_elem.astype(np.int64), mesh.bface_face.astype(np.int64)
+    bd, up = bf // 2, bf % 2
+    x = np.where(up == 1, lo[be, bd] + ln[be], lo[be, bd])
+    assert (np.where(up == 1, x == ext[bd], x == 0)).all()
+    # closed surfaces: 6 faces of area ln^2 per element (in units of the small side)
+    area = np.zeros(len(ln))
+    ar = ln[small].astype(np.float64) ** 2
+    np.add.at(area, a, ar)
+    np.add.at(area, b, ar)
+    np.add.at(area, be, ln[be].astype(np.float64) ** 2)
+    assert np.array_equal(area, 6.0 * ln.astype(np.float64) ** 2)
+
+
+@pytest.mark.parametrize("case", [Case(level=5), Case(level=5, brick=(2, 1, 1), periodic=(1, 0, 1))])
+def test_flatten_large_meshes(case):
+    """Meshes above the size where flatten and balance run their neighbour
+    queries on several threads (16384 leaves), refined with hanging faces."""
+    forest = hanging_forest(case, frac=0.05, seed=21)[0]
+    assert len(forest) > 16384
+    vectorized_face_check(forest, case, forest.flatten())
