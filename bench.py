@@ -296,9 +296,9 @@ def finish(args, rank, world, device, case, mesh, E, V, state_bytes, t_mesh, val
            "other": E * V * 8}
     achieved = alg[names[dom]] / (per_launch_ms * 1e-3) / 1e9
     # DRAM bytes (read + write) of one face_kernel<double> launch on the
-    # level-7 vortex (2,097,152 hex), from one ncu capture of the same bench
-    # command (profiles/face_kernel_fp64_vortex_262k.md): 1.111 GB read, 1.961
-    # GB written (the slot buffer: 2 sides x V x 4 coefficients x 8 B per face)
+    # level-7 vortex (2,097,152 hex), from one ncu capture (dram__bytes_read /
+    # _write, 1 pass) of this bench command: 1.111 GB read, 1.961 GB written
+    # (the slot buffer: 2 sides x V x 4 coefficients x 8 B per face)
     traffic = 1111392000 + 1960973056 if (names[dom] == "face" and E == 2 ** 21 and V == 5) else None
     fp64_peak = probe(abi, device, 0)
     roofline = {"bound": "hbm", "kernel": names[dom] + "_kernel<double>", "achieved": achieved,
