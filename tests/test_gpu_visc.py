@@ -1,4 +1,5 @@
-"""Viscous terms and chemistry (a21) on the GPU against the
+"""Viscous terms (src/models/ns/charm_model_ns_diff*.c) and chemistry
+(src/models/ns/charm_model_ns_chem.c) on the GPU against the
 oracle (itself pinned to the reference's code in tests/test_visc_oracle.py),
 FP64: residual with the viscous terms, its viscous part alone, and time
 steps with viscosity, species diffusion and reactions, on uniform, hanging

@@ -1,4 +1,5 @@
-"""Viscous terms and chemistry (a21) of the oracle against the
+"""Viscous terms (src/models/ns/charm_model_ns_diff*.c) and chemistry
+(src/models/ns/charm_model_ns_chem.c) of the oracle against the
 reference's own code (oracle/_ref): charm_model_ns_timestep_diff (diffusion
 coefficients, lifted stress and heat flux, viscous integrals) and
 charm_model_ns_timestep_chem, on the same meshes and seeded states.
