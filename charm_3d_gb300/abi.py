@@ -123,6 +123,7 @@ SIGNATURES = [
     ("charm_gpu_adjoint", C.c_int, [_P, C.c_int, C.c_int, C.POINTER(Objective), _P, _P, C.POINTER(AdjointInfo)]),
     ("charm_gpu_refine_flags_adjoint", C.c_int, [_P, C.c_double, _P, _P]),
     ("charm_gpu_density_means", C.c_int, [_P, _P]),
+    ("charm_gpu_cell_fields", C.c_int, [_P, _P]),
     ("charm_gpu_adapt_upload", C.c_int, [_P, C.POINTER(AdaptPlan), C.POINTER(Mesh)]),
     ("charm_host_forest_new", C.c_int, [C.POINTER(_P), _P, _P, _P, _P, C.c_int]),
     ("charm_host_forest_free", C.c_int, [_P]),
@@ -135,6 +136,7 @@ SIGNATURES = [
                                                C.POINTER(AdaptPlan)]),
     ("charm_host_forest_flatten", C.c_int, [_P, C.POINTER(Mesh)]),
     ("charm_host_forest_leaves", C.c_int, [_P, _P, _P]),
+    ("charm_host_forest_write_vtu", C.c_int, [_P, C.c_char_p, C.c_int, C.POINTER(C.c_char_p), _P]),
 ]
 
 _lib = None

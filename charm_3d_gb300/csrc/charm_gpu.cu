@@ -1297,6 +1297,24 @@ __global__ void __launch_bounds__(256) adapt_project_kernel(const double *__rest
     }
 }
 
+int charm_gpu_cell_fields(charm_gpu_handle_t h, double *out)
+{
+    int rc = check_ready(h);
+    if (rc) return rc;
+    if (!out) return fail(CHARM_GPU_EINVAL, "null argument");
+    if (h->cfg.precision == CHARM_GPU_PREC_MIXED && (rc = ff_convert(h, false))) return rc;   // d_u <- hi + lo
+    const int nf = 8 + h->cfg.n_comp;
+    if ((rc = ensure_buf(h, &h->d_proj[1], sizeof(double) * (size_t) nf * h->E))) return rc;
+    const unsigned nb = (unsigned) ((h->E + 255) / 256);
+    if (h->cfg.n_comp == 1) cell_fields_kernel<1><<<nb, 256, 0, h->stream>>>(h->d_u, h->E, h->nb, h->d_proj[1]);
+    else cell_fields_kernel<2><<<nb, 256, 0, h->stream>>>(h->d_u, h->E, h->nb, h->d_proj[1]);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(out, h->d_proj[1], sizeof(double) * (size_t) nf * h->E, cudaMemcpyDeviceToHost,
+                             h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return CHARM_GPU_OK;
+}
+
 int charm_gpu_density_means(charm_gpu_handle_t h, double *rho)
 {
     int rc = check_ready(h);

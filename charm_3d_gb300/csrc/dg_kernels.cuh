@@ -1474,4 +1474,27 @@ tile_stage_kernel(MeshDev m, TileDev tl, const float *__restrict__ uh, const flo
     }
 }
 
+// ---------------------------------------------------------------------------
+// output
+// ---------------------------------------------------------------------------
+
+// cell-centre primitive fields (the Taylor basis is 1, 0, 0, ... at the
+// centre: the conserved values are the coefficient-0 planes)
+template <int NC>
+__global__ void __launch_bounds__(256) cell_fields_kernel(const double *__restrict__ u, int64_t E, int nb,
+                                                          double *__restrict__ out)
+{
+    constexpr int V = 4 + NC;
+    const int64_t e = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    double U[V];
+    for (int v = 0; v < V; v++) U[v] = u[(int64_t) (v * nb) * E + e];
+    Prim<double, NC> p;
+    cons_to_prim<double, NC>(U, p);
+    const double f[8] = {p.r, p.p, p.e, p.e_tot, p.u, p.v, p.w, p.t};
+    for (int k = 0; k < 8; k++) out[(int64_t) k * E + e] = f[k];
+    for (int i = 0; i < NC; i++) out[(int64_t) (8 + i) * E + e] = p.c[i];
+}
+
+
 }  // namespace charm

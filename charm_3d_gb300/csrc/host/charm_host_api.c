@@ -17,6 +17,7 @@
 #include "charm_gpu.h"
 #include "charm_forest.h"
 
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -89,6 +90,59 @@ int charm_host_forest_set_bnd(charm_host_forest_t h, const int8_t bnd_of_side[6]
 {
     if (!h || !bnd_of_side) return CHARM_GPU_EINVAL;
     memcpy(h->bnd_of_side, bnd_of_side, 6);
+    return CHARM_GPU_OK;
+}
+
+/* ---- output (charm_write_solution, reference src/charm_output.c:55-120,
+ * through p4est's VTK writer: cell-centre fields, level and rank per cell) -- */
+
+int charm_host_forest_write_vtu(charm_host_forest_t h, const char *path, int n_fields, const char *const *names,
+                                const double *fields)
+{
+    if (!h || !path || n_fields < 0 || (n_fields > 0 && (!names || !fields))) return CHARM_GPU_EINVAL;
+    const charm_forest_t *f = &h->f;
+    const int64_t E = f->n;
+    FILE *fp = fopen(path, "w");
+    if (!fp) return CHARM_GPU_EINVAL;
+    fprintf(fp, "<?xml version=\"1.0\"?>\n<VTKFile type=\"UnstructuredGrid\" version=\"0.1\" "
+                "byte_order=\"LittleEndian\">\n<UnstructuredGrid>\n"
+                "<Piece NumberOfPoints=\"%lld\" NumberOfCells=\"%lld\">\n",
+            (long long) (8 * E), (long long) E);
+    /* the 8 corners of every leaf, in VTK_HEXAHEDRON order (bottom face
+     * counter-clockwise, then the top face) */
+    static const int corner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                     {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+    fprintf(fp, "<Points>\n<DataArray type=\"Float64\" NumberOfComponents=\"3\" format=\"ascii\">\n");
+    for (int64_t i = 0; i < E; i++) {
+        double c[3], hh[3];
+        charm_forest_leaf_geom(f, i, c, hh);
+        for (int k = 0; k < 8; k++)
+            fprintf(fp, "%.17g %.17g %.17g\n", c[0] + (corner[k][0] - 0.5) * hh[0], c[1] + (corner[k][1] - 0.5) * hh[1],
+                    c[2] + (corner[k][2] - 0.5) * hh[2]);
+    }
+    fprintf(fp, "</DataArray>\n</Points>\n<Cells>\n<DataArray type=\"Int64\" Name=\"connectivity\" format=\"ascii\">\n");
+    for (int64_t i = 0; i < E; i++)
+        fprintf(fp, "%lld %lld %lld %lld %lld %lld %lld %lld\n", (long long) (8 * i), (long long) (8 * i + 1),
+                (long long) (8 * i + 2), (long long) (8 * i + 3), (long long) (8 * i + 4), (long long) (8 * i + 5),
+                (long long) (8 * i + 6), (long long) (8 * i + 7));
+    fprintf(fp, "</DataArray>\n<DataArray type=\"Int64\" Name=\"offsets\" format=\"ascii\">\n");
+    for (int64_t i = 0; i < E; i++) fprintf(fp, "%lld\n", (long long) (8 * (i + 1)));
+    fprintf(fp, "</DataArray>\n<DataArray type=\"UInt8\" Name=\"types\" format=\"ascii\">\n");
+    for (int64_t i = 0; i < E; i++) fprintf(fp, "12\n");
+    fprintf(fp, "</DataArray>\n</Cells>\n<CellData Scalars=\"level\">\n"
+                "<DataArray type=\"Int32\" Name=\"level\" format=\"ascii\">\n");
+    for (int64_t i = 0; i < E; i++) fprintf(fp, "%d\n", (int) f->leaf[i].level);
+    fprintf(fp, "</DataArray>\n<DataArray type=\"Int32\" Name=\"mpirank\" format=\"ascii\">\n");
+    for (int64_t i = 0; i < E; i++) fprintf(fp, "0\n");
+    fprintf(fp, "</DataArray>\n");
+    for (int k = 0; k < n_fields; k++) {
+        fprintf(fp, "<DataArray type=\"Float64\" Name=\"%s\" format=\"ascii\">\n", names[k]);
+        for (int64_t i = 0; i < E; i++) fprintf(fp, "%.17g\n", fields[(int64_t) k * E + i]);
+        fprintf(fp, "</DataArray>\n");
+    }
+    fprintf(fp, "</CellData>\n</Piece>\n</UnstructuredGrid>\n</VTKFile>\n");
+    const int bad = ferror(fp);
+    if (fclose(fp) != 0 || bad) return CHARM_GPU_EINVAL;
     return CHARM_GPU_OK;
 }
 

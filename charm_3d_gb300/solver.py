@@ -120,6 +120,13 @@ class Forest:
                   "charm_host_forest_adapt_plan")
         return n.value, plan
 
+    def write_vtu(self, path: str, fields: np.ndarray, names: list[str]) -> None:
+        """Leaves as a VTK XML unstructured grid with cell data `fields` [n][E] named `names`."""
+        f = np.ascontiguousarray(fields, dtype=np.float64)
+        arr = (C.c_char_p * len(names))(*[n.encode() for n in names])
+        abi.check(self.lib.charm_host_forest_write_vtu(self.h, path.encode(), len(names), arr, f.ctypes.data),
+                  "charm_host_forest_write_vtu")
+
     def leaves(self) -> tuple[np.ndarray, np.ndarray]:
         n = len(self)
         q = np.empty((n, 4), np.int32)
@@ -247,6 +254,12 @@ class Solver:
         abi.check(self.lib.charm_gpu_refine_flags(self.h, max_err, flags.ctypes.data, grad.ctypes.data),
                   "charm_gpu_refine_flags")
         return flags, grad
+
+    def cell_fields(self) -> np.ndarray:
+        """Cell-centre R, P, E, E_TOT, U, V, W, T and the mass fractions [8 + n_comp][E]."""
+        out = np.empty((8 + self.cfg.n_comp, self.n_elem))
+        abi.check(self.lib.charm_gpu_cell_fields(self.h, out.ctypes.data), "charm_gpu_cell_fields")
+        return out
 
     def density_means(self) -> np.ndarray:
         """Sum of the species' mean coefficients per leaf (the coarsening criterion's densities)."""

@@ -332,6 +332,13 @@ int charm_gpu_density_means(charm_gpu_handle_t h, double *rho);
  * after that adapt: the state stays on the device across the adapt. */
 int charm_gpu_adapt_upload(charm_gpu_handle_t h, const charm_gpu_adapt_plan_t *plan, const charm_gpu_mesh_t *mesh);
 
+/* Cell-centre primitive fields of the current state: the values the
+ * reference's output writes per cell (charm_write_solution,
+ * src/charm_output.c:10-52: charm_get_fields at the centre, then
+ * charm_param_cons_to_prim).  out[f * E + e] for f = 0..7: R, P, E, E_TOT,
+ * U, V, W, T, then f = 8 + i: the mass fraction C_i of species i. */
+int charm_gpu_cell_fields(charm_gpu_handle_t h, double *out);
+
 /* ---- host octree (the CPU side of the boundary) -------------------------- */
 
 typedef struct charm_host_forest_s *charm_host_forest_t;
@@ -376,6 +383,14 @@ int charm_host_forest_adapt_plan(charm_host_forest_t f, const double *grad, cons
 /* Flatten into a mesh view whose arrays live inside the forest object and
  * stay valid until the next adapt/flatten/free. */
 int charm_host_forest_flatten(charm_host_forest_t f, charm_gpu_mesh_t *mesh);
+
+/* Write the leaves as a VTK XML unstructured grid (ASCII .vtu): one
+ * hexahedron per leaf, cell data "level", "mpirank" (0) and the n_fields
+ * arrays fields[f * E + e] under names[f] (the layout of
+ * charm_gpu_cell_fields with the reference's names R, P, E, E_TOT, U, V, W,
+ * T, C_<component>). */
+int charm_host_forest_write_vtu(charm_host_forest_t f, const char *path, int n_fields, const char *const *names,
+                                const double *fields);
 
 /* Leaf coordinates: qcoord[4*i..] = x, y, z, tree; level[i]. */
 int charm_host_forest_leaves(charm_host_forest_t f, int32_t *qcoord, int8_t *level);

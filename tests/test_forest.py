@@ -219,3 +219,27 @@ def test_flatten_large_meshes(case):
     forest = hanging_forest(case, frac=0.05, seed=21)[0]
     assert len(forest) > 16384
     vectorized_face_check(forest, case, forest.flatten())
+
+
+def test_write_vtu_round_trip(tmp_path):
+    """The VTK XML writer: one hexahedron per leaf with the leaf's corners,
+    level and field arrays as written."""
+    import xml.etree.ElementTree as ET
+    case = Case(level=1, tree_len=(1.0, 2.0, 0.5))
+    forest = hanging_forest(case, frac=0.3, seed=2)[0]
+    mesh = forest.flatten()
+    E = mesh.n_elem
+    fields = np.stack([np.arange(E, dtype=np.float64) * 0.5, -np.linspace(0.0, 1.0, E)])
+    path = str(tmp_path / "out.vtu")
+    forest.write_vtu(path, fields, ["R", "C_AIR"])
+    piece = ET.parse(path).getroot().find("UnstructuredGrid/Piece")
+    assert int(piece.get("NumberOfCells")) == E and int(piece.get("NumberOfPoints")) == 8 * E
+    arrays = {a.get("Name"): np.array(a.text.split(), dtype=np.float64) for a in piece.iter("DataArray")}
+    assert np.array_equal(arrays["level"], mesh.level.astype(np.float64))
+    assert np.array_equal(arrays["R"], fields[0]) and np.array_equal(arrays["C_AIR"], fields[1])
+    assert (arrays["types"] == 12).all()
+    pts = piece.find("Points/DataArray")
+    xyz = np.array(pts.text.split(), dtype=np.float64).reshape(E, 8, 3)
+    h = np.array(case.tree_len)[None, :] / (2.0 ** mesh.level[:, None])
+    assert np.allclose(xyz.mean(axis=1), mesh.center.T, rtol=0, atol=1e-15)
+    assert np.allclose(xyz.max(axis=1) - xyz.min(axis=1), h, rtol=1e-15)
