@@ -578,8 +578,10 @@ def init_dist(args):
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl" if args.impl != "reference" else "gloo")
+        gpu = torch.cuda.is_available() and args.impl != "reference"
+        if gpu:
+            torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if gpu else "gloo")
         _DIST["on"] = True
     return rank, world, local
 
@@ -594,7 +596,8 @@ def max_over_ranks(x: float, world: int) -> float:
     if world > 1 and _DIST["on"]:
         import torch
         import torch.distributed as dist
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
     return x
