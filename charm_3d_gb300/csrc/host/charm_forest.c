@@ -450,6 +450,55 @@ int64_t charm_forest_balance_marks(const charm_forest_t *f, int8_t *flag)
     return marks;
 }
 
+typedef struct {
+    const charm_forest_t *f;
+    const uint64_t *keys;
+    const int64_t *cand;
+    int8_t *flag;
+} marks_at_ctx_t;
+
+static void marks_at_range(void *c, int64_t lo, int64_t hi)
+{
+    const marks_at_ctx_t *m = (const marks_at_ctx_t *) c;
+    for (int64_t j = lo; j < hi; j++) m->flag[m->cand[j]] = (int8_t) needs_split(m->f, m->keys, m->cand[j]);
+}
+
+int64_t charm_forest_balance_marks_at(const charm_forest_t *f, const int64_t *cand, int64_t n_cand, int8_t *flag)
+{
+    uint64_t *keys = (uint64_t *) malloc(sizeof(uint64_t) * (size_t) (f->n > 0 ? f->n : 1));
+    if (keys) charm_forest_keys(f, keys);
+    marks_at_ctx_t c = {f, keys, cand, flag};
+    charm_forest_parallel_for(n_cand, marks_at_range, &c);
+    free(keys);
+    int64_t marks = 0;
+    for (int64_t j = 0; j < n_cand; j++) marks += flag[cand[j]];
+    return marks;
+}
+
+int64_t charm_forest_fresh_neighbourhood(const charm_forest_t *f, const int64_t *fresh, int64_t n_fresh, int64_t *out)
+{
+    int8_t *mark = (int8_t *) calloc((size_t) f->n + 1, 1);
+    uint64_t *keys = (uint64_t *) malloc(sizeof(uint64_t) * (size_t) (f->n > 0 ? f->n : 1));
+    if (!mark || !keys) { free(mark); free(keys); return -1; }
+    charm_forest_keys(f, keys);
+    for (int64_t j = 0; j < n_fresh; j++) {
+        const int64_t c = fresh[j];
+        mark[c] = 1;
+        for (int face = 0; face < 6; face++) {
+            charm_face_nb_t nb;
+            charm_forest_face_neighbor_k(f, keys, c, face, &nb);
+            for (int k = 0; k < 4; k++)
+                if (nb.idx[k] >= 0) mark[nb.idx[k]] = 1;
+        }
+    }
+    int64_t n = 0;
+    for (int64_t i = 0; i < f->n; i++)
+        if (mark[i]) out[n++] = i;
+    free(mark);
+    free(keys);
+    return n;
+}
+
 int64_t charm_forest_balance(charm_forest_t *f, charm_forest_replace_fn replace, void *user)
 {
     int64_t total = 0;

@@ -122,6 +122,17 @@ int64_t charm_forest_balance(charm_forest_t *f, charm_forest_replace_fn replace,
  * split now.  Returns the number of flags set. */
 int64_t charm_forest_balance_marks(const charm_forest_t *f, int8_t *flag);
 
+/* The same pass on the listed leaves only (cand, n_cand entries): flag[i]
+ * is set for i in cand and left as it is elsewhere.  Returns the flags set. */
+int64_t charm_forest_balance_marks_at(const charm_forest_t *f, const int64_t *cand, int64_t n_cand, int8_t *flag);
+
+/* The leaves that a ripple pass after a refine must re-check: the new
+ * leaves `fresh` and every leaf across one of their faces (a leaf that was
+ * balanced before the refine can only become unbalanced next to a new
+ * leaf).  Writes the sorted indices into out (room for f->n), returns the
+ * count, or -1 on allocation failure. */
+int64_t charm_forest_fresh_neighbourhood(const charm_forest_t *f, const int64_t *fresh, int64_t n_fresh, int64_t *out);
+
 /* 1 if every face neighbour relation is at most one level apart. */
 int charm_forest_is_balanced(const charm_forest_t *f);
 

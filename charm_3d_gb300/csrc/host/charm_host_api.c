@@ -641,24 +641,57 @@ static int adapt_core(struct charm_host_forest_s *h, const double *grad, double 
     free(g1);
     free(rho);   /* the balance passes do not read densities */
     rho = NULL;
-    /* 3. 2:1 face balance, one level per pass (p4est_balance_ext with charm_replace_quads) */
+    /* 3. 2:1 face balance, one level per pass (p4est_balance_ext with
+     * charm_replace_quads).  The first pass checks every leaf; a later pass
+     * only the leaves made by the previous one and their face neighbours
+     * (the others were balanced and kept their neighbours). */
+    int64_t *cand = NULL, n_cand = -1;
     for (;;) {
-        int8_t *bf = (int8_t *) calloc((size_t) f->n + 1, 1);
-        if (!bf) { free(u); return CHARM_GPU_ENOMEM; }
-        int64_t marks = charm_forest_balance_marks(f, bf);
+        const int64_t nold = f->n;
+        int8_t *bf = (int8_t *) calloc((size_t) nold + 1, 1);
+        int8_t *lv = (int8_t *) malloc((size_t) nold + 1);
+        if (!bf || !lv) { free(bf); free(lv); free(cand); free(u); return CHARM_GPU_ENOMEM; }
+        for (int64_t i = 0; i < nold; i++) lv[i] = f->leaf[i].level;
+        const int64_t marks = (n_cand < 0) ? charm_forest_balance_marks(f, bf)
+                                           : charm_forest_balance_marks_at(f, cand, n_cand, bf);
+        free(cand);
+        cand = NULL;
         if (marks) {
             if (plan) {
-                double *dummy = (double *) calloc((size_t) f->n + 1, sizeof(double));
+                double *dummy = (double *) calloc((size_t) nold + 1, sizeof(double));
                 rc = dummy ? refine_plan(h, bf, &dummy) : CHARM_GPU_ENOMEM;
                 free(dummy);
             } else {
                 rc = refine_state(f, bf, V, &u);
             }
+            if (!rc) {
+                /* the children made by this pass, at their new indices */
+                int64_t *fresh = (int64_t *) malloc(sizeof(int64_t) * (size_t) (8 * marks + 1));
+                cand = (int64_t *) malloc(sizeof(int64_t) * (size_t) (f->n + 1));
+                if (!fresh || !cand) {
+                    rc = CHARM_GPU_ENOMEM;
+                } else {
+                    int64_t nf = 0, k = 0;
+                    for (int64_t i = 0; i < nold; i++) {
+                        if (bf[i] && lv[i] < CHARM_FOREST_MAXLEVEL - 1) {
+                            for (int c = 0; c < 8; c++) fresh[nf++] = k + c;
+                            k += 8;
+                        } else {
+                            k++;
+                        }
+                    }
+                    n_cand = charm_forest_fresh_neighbourhood(f, fresh, nf, cand);
+                    if (n_cand < 0) rc = CHARM_GPU_ENOMEM;
+                }
+                free(fresh);
+            }
         }
         free(bf);
-        if (rc) { free(u); return rc; }
+        free(lv);
+        if (rc) { free(cand); free(u); return rc; }
         if (!marks) break;
     }
+    free(cand);
     if (!plan) {
         free(h->state);
         h->state = u;

@@ -102,3 +102,27 @@ def test_adapt_plan_balance_ripples():
         mesh = fa.flatten()
         u = ua
     assert ripple > 0
+
+
+def test_restricted_ripples_equal_full_balance():
+    """adapt_state's balance passes after the first check only the new
+    leaves and their face neighbours; the forest must be the one the full
+    ripple (charm_forest_balance, every leaf every pass) gives: refine the
+    leaf at a point four times in a row (ripples of several passes)."""
+    case = small_case("sod", "HLLC", "BJ", level=2)
+    fa, fb = Forest(case), Forest(case)
+    for r in range(4):
+        mesh = fa.flatten()
+        d = np.abs(mesh.center - 0.37).max(axis=0)
+        i = int(np.argmin(d))
+        grad = np.zeros((3, mesh.n_elem))
+        grad[0, i] = 1.0e9
+        u = np.ones((case.n_var, 4, mesh.n_elem))
+        fa.adapt_state(grad, 0.01, 9, 9, case.n_comp, u)   # minlevel 9: nothing coarsens
+        flags = np.zeros(mesh.n_elem, np.int8)
+        flags[i] = 1
+        fb.adapt(flags, 9, 9)
+        qa, la = fa.leaves()
+        qb, lb = fb.leaves()
+        assert len(fa) == len(fb) and (qa == qb).all() and (la == lb).all(), f"round {r}"
+    assert int(la.max()) - int(la.min()) >= 4
