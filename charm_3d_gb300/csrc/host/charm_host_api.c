@@ -232,6 +232,85 @@ static void nbs_range(void *c, int64_t lo, int64_t hi)
         for (int face = 0; face < 6; face++) charm_forest_face_neighbor_k(n->f, n->keys, i, face, &n->nbs[6 * i + face]);
 }
 
+/* flatten, per-leaf passes (run on several threads; every leaf writes only
+ * its own records, at offsets from prefix sums, so the records come out in
+ * the serial order: interior faces grouped by direction, then by leaf, then
+ * lower/upper face; boundary faces by leaf, then face) */
+typedef struct {
+    struct charm_host_forest_s *h;
+    const charm_face_nb_t *nbs;
+    int64_t E, nf;
+    int64_t *cnt;        /* [4][E]: records per direction, boundary records; then offsets */
+} flat_ctx_t;
+
+static void flat_count_range(void *c, int64_t lo, int64_t hi)
+{
+    const flat_ctx_t *x = (const flat_ctx_t *) c;
+    for (int64_t i = lo; i < hi; i++) {
+        int64_t n[4] = {0, 0, 0, 0};
+        for (int face = 0; face < 6; face++) {
+            const charm_face_nb_t *nbr = &x->nbs[6 * i + face];
+            switch (nbr->kind) {
+            case CHARM_NB_BOUNDARY: n[3]++; break;
+            case CHARM_NB_SAME: if (face & 1) n[face / 2]++; break;
+            case CHARM_NB_SMALLER: n[face / 2] += 4; break;
+            case CHARM_NB_BIGGER: break;
+            default: n[3] = -1000000; break;   /* not 2:1 balanced */
+            }
+        }
+        for (int d = 0; d < 4; d++) x->cnt[(int64_t) d * x->E + i] = n[d];
+    }
+}
+
+static void flat_emit_range(void *c, int64_t lo, int64_t hi)
+{
+    const flat_ctx_t *x = (const flat_ctx_t *) c;
+    struct charm_host_forest_s *h = x->h;
+    const int64_t E = x->E, nf = x->nf;
+    for (int64_t i = lo; i < hi; i++) {
+        double cc[3], hh[3];
+        charm_forest_leaf_geom(&h->f, i, cc, hh);
+        h->center[i] = cc[0]; h->center[E + i] = cc[1]; h->center[2 * E + i] = cc[2];
+        h->level[i] = h->f.leaf[i].level;
+        for (int d = 0; d < 3; d++) {
+            int64_t k = x->cnt[(int64_t) d * E + i];
+            for (int up = 0; up < 2; up++) {
+                const int face = 2 * d + up;
+                const charm_face_nb_t *nbr = &x->nbs[6 * i + face];
+                const uint8_t wrap = nbr->wrap ? 0x40 : 0;
+                if (nbr->kind == CHARM_NB_SAME && up) {
+                    h->face_elem[k] = (int32_t) i;
+                    h->face_elem[nf + k] = (int32_t) nbr->idx[0];
+                    h->face_info[k] = (uint8_t) (d | wrap);
+                    k++;
+                } else if (nbr->kind == CHARM_NB_SMALLER) {
+                    for (int j = 0; j < 4; j++) {
+                        if (up) {   /* big leaf is the lower side */
+                            h->face_elem[k] = (int32_t) i;
+                            h->face_elem[nf + k] = (int32_t) nbr->idx[j];
+                            h->face_info[k] = (uint8_t) (d | (2 << 2) | (j << 4) | wrap);
+                        } else {    /* small leaves are the lower side */
+                            h->face_elem[k] = (int32_t) nbr->idx[j];
+                            h->face_elem[nf + k] = (int32_t) i;
+                            h->face_info[k] = (uint8_t) (d | (1 << 2) | (j << 4) | wrap);
+                        }
+                        k++;
+                    }
+                }
+            }
+        }
+        int64_t kb = x->cnt[3 * E + i];
+        for (int face = 0; face < 6; face++) {
+            if (x->nbs[6 * i + face].kind == CHARM_NB_BOUNDARY) {
+                h->bface_elem[kb] = (int32_t) i;
+                h->bface_face[kb] = (int8_t) face;
+                h->bface_bnd[kb] = h->bnd_of_side[face];
+                kb++;
+            }
+        }
+    }
+}
+
 int charm_host_forest_flatten(charm_host_forest_t h, charm_gpu_mesh_t *mesh)
 {
     if (!h || !mesh) return CHARM_GPU_EINVAL;
@@ -239,31 +318,33 @@ int charm_host_forest_flatten(charm_host_forest_t h, charm_gpu_mesh_t *mesh)
     const int64_t E = f->n;
     free_flat(h);
     /* every leaf's six face-neighbour relations, found once (binary searches
-     * on precomputed Morton keys) and read by the three passes below */
+     * on precomputed Morton keys) and read by the passes below */
     uint64_t *keys = (uint64_t *) malloc(sizeof(uint64_t) * (size_t) (E > 0 ? E : 1));
     charm_face_nb_t *nbs = (charm_face_nb_t *) malloc(sizeof(charm_face_nb_t) * (size_t) (6 * (E > 0 ? E : 1)));
-    if (!keys || !nbs) { free(keys); free(nbs); return CHARM_GPU_ENOMEM; }
+    int64_t *cnt = (int64_t *) malloc(sizeof(int64_t) * (size_t) (4 * (E > 0 ? E : 1)));
+    if (!keys || !nbs || !cnt) { free(keys); free(nbs); free(cnt); return CHARM_GPU_ENOMEM; }
     charm_forest_keys(f, keys);
     nbs_ctx_t nc = {f, keys, nbs};
     charm_forest_parallel_for(E, nbs_range, &nc);
     free(keys);
-    /* count */
+    /* count, then turn the counts into offsets */
+    flat_ctx_t fc = {h, nbs, E, 0, cnt};
+    charm_forest_parallel_for(E, flat_count_range, &fc);
     int64_t nf = 0, nb = 0;
-    charm_face_nb_t nbr;
-    for (int64_t i = 0; i < E; i++) {
-        for (int face = 0; face < 6; face++) {
-            nbr = nbs[6 * i + face];
-            switch (nbr.kind) {
-            case CHARM_NB_BOUNDARY: nb++; break;
-            case CHARM_NB_SAME: if (face & 1) nf++; break;
-            case CHARM_NB_SMALLER: nf += 4; break;
-            case CHARM_NB_BIGGER: break;
-            default: free(nbs); return CHARM_GPU_EINVAL;   /* not 2:1 balanced */
-            }
+    for (int d = 0; d < 3; d++)
+        for (int64_t i = 0; i < E; i++) {
+            const int64_t n = cnt[(int64_t) d * E + i];
+            cnt[(int64_t) d * E + i] = nf;
+            nf += n;
         }
+    for (int64_t i = 0; i < E; i++) {
+        const int64_t n = cnt[3 * E + i];
+        if (n < 0) { free(nbs); free(cnt); return CHARM_GPU_EINVAL; }   /* not 2:1 balanced */
+        cnt[3 * E + i] = nb;
+        nb += n;
     }
-    h->center = (double *) malloc((size_t) (3 * E) * sizeof(double));
-    h->level = (int8_t *) malloc((size_t) E);
+    h->center = (double *) malloc((size_t) (3 * (E > 0 ? E : 1)) * sizeof(double));
+    h->level = (int8_t *) malloc((size_t) (E > 0 ? E : 1));
     h->face_elem = (int32_t *) malloc((size_t) (2 * (nf > 0 ? nf : 1)) * sizeof(int32_t));
     h->face_info = (uint8_t *) malloc((size_t) (nf > 0 ? nf : 1));
     h->bface_elem = (int32_t *) malloc((size_t) (nb > 0 ? nb : 1) * sizeof(int32_t));
@@ -273,57 +354,13 @@ int charm_host_forest_flatten(charm_host_forest_t h, charm_gpu_mesh_t *mesh)
         !h->bface_bnd) {
         free_flat(h);
         free(nbs);
+        free(cnt);
         return CHARM_GPU_ENOMEM;
     }
-    for (int64_t i = 0; i < E; i++) {
-        double c[3], hh[3];
-        charm_forest_leaf_geom(f, i, c, hh);
-        h->center[i] = c[0]; h->center[E + i] = c[1]; h->center[2 * E + i] = c[2];
-        h->level[i] = f->leaf[i].level;
-    }
-    /* interior faces grouped by direction, then by leaf order */
-    int64_t k = 0;
-    for (int d = 0; d < 3; d++) {
-        for (int64_t i = 0; i < E; i++) {
-            for (int up = 0; up < 2; up++) {
-                int face = 2 * d + up;
-                nbr = nbs[6 * i + face];
-                uint8_t wrap = nbr.wrap ? 0x40 : 0;
-                if (nbr.kind == CHARM_NB_SAME && up) {
-                    h->face_elem[k] = (int32_t) i;
-                    h->face_elem[nf + k] = (int32_t) nbr.idx[0];
-                    h->face_info[k] = (uint8_t) (d | wrap);
-                    k++;
-                } else if (nbr.kind == CHARM_NB_SMALLER) {
-                    for (int j = 0; j < 4; j++) {
-                        if (up) {   /* big leaf is the lower side */
-                            h->face_elem[k] = (int32_t) i;
-                            h->face_elem[nf + k] = (int32_t) nbr.idx[j];
-                            h->face_info[k] = (uint8_t) (d | (2 << 2) | (j << 4) | wrap);
-                        } else {    /* small leaves are the lower side */
-                            h->face_elem[k] = (int32_t) nbr.idx[j];
-                            h->face_elem[nf + k] = (int32_t) i;
-                            h->face_info[k] = (uint8_t) (d | (1 << 2) | (j << 4) | wrap);
-                        }
-                        k++;
-                    }
-                }
-            }
-        }
-    }
-    int64_t kb = 0;
-    for (int64_t i = 0; i < E; i++) {
-        for (int face = 0; face < 6; face++) {
-            nbr = nbs[6 * i + face];
-            if (nbr.kind == CHARM_NB_BOUNDARY) {
-                h->bface_elem[kb] = (int32_t) i;
-                h->bface_face[kb] = (int8_t) face;
-                h->bface_bnd[kb] = h->bnd_of_side[face];
-                kb++;
-            }
-        }
-    }
+    fc.nf = nf;
+    charm_forest_parallel_for(E, flat_emit_range, &fc);
     free(nbs);
+    free(cnt);
     h->n_face = nf;
     h->n_bface = nb;
     mesh->n_elem = E;
