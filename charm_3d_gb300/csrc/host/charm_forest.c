@@ -13,6 +13,8 @@
 #include "charm_forest.h"
 
 #include <pthread.h>
+#include <stdint.h>
+#include <sys/types.h>
 #include <unistd.h>
 #include <stdlib.h>
 #include <string.h>
@@ -120,49 +122,122 @@ int charm_forest_copy(charm_forest_t *dst, const charm_forest_t *src)
 
 /* ---- parallel loops over leaves ------------------------------------------ */
 
+/* A pool of worker threads, started on the first parallel loop of the
+ * process (and again in a forked child, which has none of them) and kept:
+ * an adapt and a flatten run a dozen loops each, and starting threads for
+ * every loop costs more than the short loops themselves. */
+enum { kMaxThreads = 64 };
+
 typedef struct {
+    pthread_mutex_t mu;
+    pthread_cond_t go, done;
+    int nworkers;                /* threads started (chunks 1..nworkers) */
+    uint64_t gen;                /* loop generation: bumped per loop */
+    int pending;                 /* chunks of the current loop not finished */
     charm_forest_range_fn fn;
     void *ctx;
-    int64_t lo, hi;
-} range_job_t;
+    int64_t n;
+    int nt;                      /* chunks of the current loop */
+    pid_t pid;                   /* process that started the workers */
+} pool_t;
 
-static void *run_range_job(void *arg)
+static pool_t g_pool;
+/* one loop at a time uses the pool; a loop that finds it busy (a loop in
+ * another thread, or one nested in a chunk) runs serially */
+static pthread_mutex_t g_dispatch = PTHREAD_MUTEX_INITIALIZER;
+
+static void *pool_worker(void *arg)
 {
-    const range_job_t *j = (const range_job_t *) arg;
-    j->fn(j->ctx, j->lo, j->hi);
+    const int k = (int) (intptr_t) arg;
+    pool_t *p = &g_pool;
+    uint64_t seen = 0;           /* workers start before the first loop */
+    pthread_mutex_lock(&p->mu);
+    for (;;) {
+        while (p->gen == seen) pthread_cond_wait(&p->go, &p->mu);
+        seen = p->gen;
+        if (k < p->nt) {
+            const charm_forest_range_fn fn = p->fn;
+            void *ctx = p->ctx;
+            const int64_t lo = p->n * k / p->nt, hi = p->n * (k + 1) / p->nt;
+            pthread_mutex_unlock(&p->mu);
+            fn(ctx, lo, hi);
+            pthread_mutex_lock(&p->mu);
+            if (--p->pending == 0) pthread_cond_signal(&p->done);
+        }
+    }
     return NULL;
 }
 
-/* Run fn(ctx, lo, hi) over [0, n) in contiguous chunks on up to the online
- * CPU count of threads (the calling thread takes the first chunk).  Loops
- * below 16384 iterations run serially, and a chunk whose thread cannot be
- * started runs on the calling thread. */
-void charm_forest_parallel_for(int64_t n, charm_forest_range_fn fn, void *ctx)
+/* With g_dispatch held: start the workers if this process has none. */
+static void pool_start(int want)
 {
-    enum { kMaxThreads = 64 };
+    pool_t *p = &g_pool;
+    if (p->pid == getpid()) return;
+    pthread_mutex_init(&p->mu, NULL);
+    pthread_cond_init(&p->go, NULL);
+    pthread_cond_init(&p->done, NULL);
+    p->gen = 0;
+    p->pending = 0;
+    p->nworkers = 0;
+    p->pid = getpid();
+    pthread_attr_t at;
+    pthread_attr_init(&at);
+    pthread_attr_setdetachstate(&at, PTHREAD_CREATE_DETACHED);
+    for (int k = 1; k < want; k++) {
+        pthread_t t;
+        if (pthread_create(&t, &at, pool_worker, (void *) (intptr_t) k) != 0) break;
+        p->nworkers = k;
+    }
+    pthread_attr_destroy(&at);
+}
+
+/* Run fn(ctx, lo, hi) over [0, n) in contiguous chunks of at least
+ * min_chunk iterations on up to the online CPU count of threads (the calling
+ * thread takes the first chunk).  A loop with one chunk, or one that finds
+ * the pool busy, runs serially on the calling thread. */
+void charm_forest_parallel_for_min(int64_t n, int64_t min_chunk, charm_forest_range_fn fn, void *ctx)
+{
     const long cpus = sysconf(_SC_NPROCESSORS_ONLN);
-    int nt = (cpus > 1) ? (int) (cpus < kMaxThreads ? cpus : kMaxThreads) : 1;
-    if ((int64_t) nt > n / 4096) nt = (int) (n / 4096);
-    if (n < 16384 || nt <= 1) {
+    const int ncpu = (cpus > 1) ? (int) (cpus < kMaxThreads ? cpus : kMaxThreads) : 1;
+    int nt = ncpu;
+    if (min_chunk < 1) min_chunk = 1;
+    if ((int64_t) nt > n / min_chunk) nt = (int) (n / min_chunk);
+    if (nt <= 1 || pthread_mutex_trylock(&g_dispatch) != 0) {
         fn(ctx, 0, n);
         return;
     }
-    range_job_t jobs[kMaxThreads];
-    pthread_t th[kMaxThreads];
-    int started[kMaxThreads];
-    for (int k = 0; k < nt; k++) {
-        jobs[k].fn = fn;
-        jobs[k].ctx = ctx;
-        jobs[k].lo = n * k / nt;
-        jobs[k].hi = n * (k + 1) / nt;
-        started[k] = 0;
+    pool_t *p = &g_pool;
+    pool_start(ncpu);
+    if (nt > p->nworkers + 1) nt = p->nworkers + 1;
+    if (nt <= 1) {
+        pthread_mutex_unlock(&g_dispatch);
+        fn(ctx, 0, n);
+        return;
     }
-    for (int k = 1; k < nt; k++) started[k] = pthread_create(&th[k], NULL, run_range_job, &jobs[k]) == 0;
-    fn(ctx, jobs[0].lo, jobs[0].hi);
-    for (int k = 1; k < nt; k++) {
-        if (started[k]) pthread_join(th[k], NULL);
-        else fn(ctx, jobs[k].lo, jobs[k].hi);
+    pthread_mutex_lock(&p->mu);
+    p->fn = fn;
+    p->ctx = ctx;
+    p->n = n;
+    p->nt = nt;
+    p->pending = nt - 1;
+    p->gen++;
+    pthread_cond_broadcast(&p->go);
+    pthread_mutex_unlock(&p->mu);
+    fn(ctx, 0, n / nt);
+    pthread_mutex_lock(&p->mu);
+    while (p->pending > 0) pthread_cond_wait(&p->done, &p->mu);
+    pthread_mutex_unlock(&p->mu);
+    pthread_mutex_unlock(&g_dispatch);
+}
+
+/* Light loops: serial below 16384 iterations, chunks of 4096 or more. */
+void charm_forest_parallel_for(int64_t n, charm_forest_range_fn fn, void *ctx)
+{
+    if (n < 16384) {
+        fn(ctx, 0, n);
+        return;
     }
+    charm_forest_parallel_for_min(n, 4096, fn, ctx);
 }
 
 /* ---- queries ------------------------------------------------------------ */
@@ -444,7 +519,7 @@ int64_t charm_forest_balance_marks(const charm_forest_t *f, int8_t *flag)
     uint64_t *keys = (uint64_t *) malloc(sizeof(uint64_t) * (size_t) (f->n > 0 ? f->n : 1));
     if (keys) charm_forest_keys(f, keys);
     marks_ctx_t c = {f, keys, flag};
-    charm_forest_parallel_for(f->n, marks_range, &c);
+    charm_forest_parallel_for_min(f->n, 256, marks_range, &c);
     for (int64_t i = 0; i < f->n; i++) marks += flag[i];
     free(keys);
     return marks;
@@ -468,27 +543,49 @@ int64_t charm_forest_balance_marks_at(const charm_forest_t *f, const int64_t *ca
     uint64_t *keys = (uint64_t *) malloc(sizeof(uint64_t) * (size_t) (f->n > 0 ? f->n : 1));
     if (keys) charm_forest_keys(f, keys);
     marks_at_ctx_t c = {f, keys, cand, flag};
-    charm_forest_parallel_for(n_cand, marks_at_range, &c);
+    charm_forest_parallel_for_min(n_cand, 256, marks_at_range, &c);
     free(keys);
     int64_t marks = 0;
     for (int64_t j = 0; j < n_cand; j++) marks += flag[cand[j]];
     return marks;
 }
 
-int64_t charm_forest_fresh_neighbourhood(const charm_forest_t *f, const int64_t *fresh, int64_t n_fresh, int64_t *out)
+typedef struct {
+    const charm_forest_t *f;
+    const uint64_t *keys;
+    const int64_t *fresh;
+    int32_t *nb;         /* [chunk][24] face-neighbour indices, -1 where none */
+} hood_ctx_t;
+
+static void hood_range(void *c, int64_t lo, int64_t hi)
 {
-    int8_t *mark = (int8_t *) calloc((size_t) f->n + 1, 1);
-    uint64_t *keys = (uint64_t *) malloc(sizeof(uint64_t) * (size_t) (f->n > 0 ? f->n : 1));
-    if (!mark || !keys) { free(mark); free(keys); return -1; }
-    charm_forest_keys(f, keys);
-    for (int64_t j = 0; j < n_fresh; j++) {
-        const int64_t c = fresh[j];
-        mark[c] = 1;
+    const hood_ctx_t *x = (const hood_ctx_t *) c;
+    for (int64_t j = lo; j < hi; j++)
         for (int face = 0; face < 6; face++) {
             charm_face_nb_t nb;
-            charm_forest_face_neighbor_k(f, keys, c, face, &nb);
-            for (int k = 0; k < 4; k++)
-                if (nb.idx[k] >= 0) mark[nb.idx[k]] = 1;
+            charm_forest_face_neighbor_k(x->f, x->keys, x->fresh[j], face, &nb);
+            for (int k = 0; k < 4; k++) x->nb[24 * j + 4 * face + k] = (int32_t) nb.idx[k];
+        }
+}
+
+int64_t charm_forest_fresh_neighbourhood(const charm_forest_t *f, const int64_t *fresh, int64_t n_fresh, int64_t *out)
+{
+    /* the face-neighbour searches run on several threads, a chunk of leaves
+     * at a time, into a buffer; the marks are set on the calling thread */
+    enum { kChunk = 1 << 16 };
+    int8_t *mark = (int8_t *) calloc((size_t) f->n + 1, 1);
+    uint64_t *keys = (uint64_t *) malloc(sizeof(uint64_t) * (size_t) (f->n > 0 ? f->n : 1));
+    int32_t *nb = (int32_t *) malloc(sizeof(int32_t) * 24 * (size_t) (n_fresh < kChunk ? (n_fresh > 0 ? n_fresh : 1) : kChunk));
+    if (!mark || !keys || !nb) { free(mark); free(keys); free(nb); return -1; }
+    charm_forest_keys(f, keys);
+    for (int64_t j0 = 0; j0 < n_fresh; j0 += kChunk) {
+        const int64_t m = (n_fresh - j0 < kChunk) ? n_fresh - j0 : kChunk;
+        hood_ctx_t c = {f, keys, fresh + j0, nb};
+        charm_forest_parallel_for_min(m, 256, hood_range, &c);
+        for (int64_t j = 0; j < m; j++) {
+            mark[fresh[j0 + j]] = 1;
+            for (int k = 0; k < 24; k++)
+                if (nb[24 * j + k] >= 0) mark[nb[24 * j + k]] = 1;
         }
     }
     int64_t n = 0;
@@ -496,6 +593,7 @@ int64_t charm_forest_fresh_neighbourhood(const charm_forest_t *f, const int64_t 
         if (mark[i]) out[n++] = i;
     free(mark);
     free(keys);
+    free(nb);
     return n;
 }
 
@@ -508,7 +606,7 @@ int64_t charm_forest_balance(charm_forest_t *f, charm_forest_replace_fn replace,
         if (!flag || !keys) { free(flag); free(keys); return -1; }
         charm_forest_keys(f, keys);
         marks_ctx_t c = {f, keys, flag};
-        charm_forest_parallel_for(f->n, marks_range, &c);
+        charm_forest_parallel_for_min(f->n, 256, marks_range, &c);
         int64_t marks = 0;
         for (int64_t i = 0; i < f->n; i++) marks += flag[i];
         free(keys);

@@ -96,11 +96,14 @@ int64_t charm_forest_find_k(const charm_forest_t *f, const uint64_t *key, int32_
 void charm_forest_face_neighbor_k(const charm_forest_t *f, const uint64_t *key, int64_t i, int face,
                                   charm_face_nb_t *nb);
 
-/* fn(ctx, lo, hi) over [0, n) split across threads (pthreads, up to the
- * online CPU count; serial below 16384 iterations).  fn must only write
- * locations owned by its range. */
+/* fn(ctx, lo, hi) over [0, n) split across threads (a pool of pthreads
+ * started once per process, up to the online CPU count; serial below 16384
+ * iterations).  fn must only write locations owned by its range.  The _min
+ * form takes the smallest chunk worth a thread (small for loops whose
+ * iterations search the forest). */
 typedef void (*charm_forest_range_fn)(void *ctx, int64_t lo, int64_t hi);
 void charm_forest_parallel_for(int64_t n, charm_forest_range_fn fn, void *ctx);
+void charm_forest_parallel_for_min(int64_t n, int64_t min_chunk, charm_forest_range_fn fn, void *ctx);
 
 /* Physical centre and edge lengths of leaf i. */
 void charm_forest_leaf_geom(const charm_forest_t *f, int64_t i, double c[3], double h[3]);

@@ -325,7 +325,7 @@ int charm_host_forest_flatten(charm_host_forest_t h, charm_gpu_mesh_t *mesh)
     if (!keys || !nbs || !cnt) { free(keys); free(nbs); free(cnt); return CHARM_GPU_ENOMEM; }
     charm_forest_keys(f, keys);
     nbs_ctx_t nc = {f, keys, nbs};
-    charm_forest_parallel_for(E, nbs_range, &nc);
+    charm_forest_parallel_for_min(E, 256, nbs_range, &nc);
     free(keys);
     /* count, then turn the counts into offsets */
     flat_ctx_t fc = {h, nbs, E, 0, cnt};
@@ -610,37 +610,43 @@ static int adapt_core(struct charm_host_forest_s *h, const double *grad, double 
     int64_t E1 = E0;
     for (int64_t i = 0; i < E0; i++) E1 += fl[i] ? 7 : 0;
     double *g1 = (double *) malloc(sizeof(double) * 3 * (size_t) E1);
-    if (!g1) { free(u); free(rho); free(fl); return CHARM_GPU_ENOMEM; }
+    /* leaves that did not exist before this adapt (children made by the
+     * refine, parents made by the coarsen), in the current numbering */
+    int8_t *isnew = (int8_t *) malloc((size_t) E1 + 1);
+    if (!g1 || !isnew) { free(u); free(rho); free(fl); free(g1); free(isnew); return CHARM_GPU_ENOMEM; }
     {
         int64_t k = 0;
         for (int64_t i = 0; i < E0; i++) {
             int n = fl[i] ? 8 : 1;
-            for (int c = 0; c < n; c++)
+            for (int c = 0; c < n; c++) {
                 for (int d = 0; d < 3; d++) g1[(int64_t) d * E1 + k + c] = fl[i] ? NAN : grad[(int64_t) d * E0 + i];
+                isnew[k + c] = fl[i];
+            }
             k += n;
         }
     }
     int rc = plan ? refine_plan(h, fl, &rho) : refine_state(f, fl, V, &u);
     free(fl);
-    if (rc) { free(u); free(rho); free(g1); return rc; }
+    if (rc) { free(u); free(rho); free(g1); free(isnew); return rc; }
     /* 2. coarsen complete families (charm_coarsen_err_estimate, non-recursive) */
     {
         const int64_t E = f->n;
         charm_leaf_t *old = (charm_leaf_t *) malloc(sizeof(charm_leaf_t) * (size_t) (E + 1));
-        if (!old) { free(u); free(rho); free(g1); return CHARM_GPU_ENOMEM; }
+        if (!old) { free(u); free(rho); free(g1); free(isnew); return CHARM_GPU_ENOMEM; }
         memcpy(old, f->leaf, sizeof(charm_leaf_t) * (size_t) E);
         coarsen_state_ctx_t cc = {f, g1, rho, u, E, n_comp, minlevel, err2_max, vpow};
         int64_t nm = charm_forest_coarsen(f, minlevel, coarsen_family, NULL, &cc);
-        if (nm < 0) { free(old); free(u); free(rho); free(g1); return CHARM_GPU_ENOMEM; }
+        if (nm < 0) { free(old); free(u); free(rho); free(g1); free(isnew); return CHARM_GPU_ENOMEM; }
         if (nm > 0) {
             const int64_t En = f->n;
             double *w = plan ? NULL : (double *) malloc(sizeof(double) * (size_t) V * 4 * (size_t) En);
             int32_t *map = plan ? (int32_t *) malloc(sizeof(int32_t) * 2 * (size_t) En) : NULL;
-            if (plan ? !map : !w) { free(old); free(u); free(rho); free(g1); return CHARM_GPU_ENOMEM; }
+            if (plan ? !map : !w) { free(old); free(u); free(rho); free(g1); free(isnew); return CHARM_GPU_ENOMEM; }
             int64_t i = 0;
             for (int64_t k = 0; k < En; k++) {
                 const charm_leaf_t *nl = &f->leaf[k], *ol = &old[i];
                 if (ol->level == nl->level && ol->x == nl->x && ol->y == nl->y && ol->z == nl->z && ol->tree == nl->tree) {
+                    isnew[k] = isnew[i];   /* k <= i: in place */
                     if (plan) {
                         map[2 * k] = (int32_t) i;
                         map[2 * k + 1] = -1;
@@ -654,10 +660,11 @@ static int adapt_core(struct charm_host_forest_s *h, const double *grad, double 
                     int64_t ch[8];
                     int cid[8];
                     for (int c = 0; c < 8; c++) { ch[c] = i + c; cid[c] = charm_leaf_child_id(&old[i + c]); }
+                    isnew[k] = 1;
                     if (plan) {
                         /* a family in Morton order: child ids 0..7 in turn */
                         for (int c = 0; c < 8; c++)
-                            if (cid[c] != c) { free(map); free(old); free(rho); free(g1); return CHARM_GPU_EINVAL; }
+                            if (cid[c] != c) { free(map); free(old); free(rho); free(g1); free(isnew); return CHARM_GPU_EINVAL; }
                         map[2 * k] = (int32_t) i;
                         map[2 * k + 1] = 8;
                     } else {
@@ -667,7 +674,7 @@ static int adapt_core(struct charm_host_forest_s *h, const double *grad, double 
                 }
             }
             if (plan) {
-                if ((rc = plan_push(h, En, map))) { free(map); free(old); free(rho); free(g1); return rc; }
+                if ((rc = plan_push(h, En, map))) { free(map); free(old); free(rho); free(g1); free(isnew); return rc; }
             } else {
                 free(u);
                 u = w;
@@ -679,10 +686,28 @@ static int adapt_core(struct charm_host_forest_s *h, const double *grad, double 
     free(rho);   /* the balance passes do not read densities */
     rho = NULL;
     /* 3. 2:1 face balance, one level per pass (p4est_balance_ext with
-     * charm_replace_quads).  The first pass checks every leaf; a later pass
-     * only the leaves made by the previous one and their face neighbours
-     * (the others were balanced and kept their neighbours). */
-    int64_t *cand = NULL, n_cand = -1;
+     * charm_replace_quads).  The forest was balanced before this adapt (every
+     * call that changes it ends balanced), and a pair of leaves that both
+     * existed before keeps its face relation; so a pass only checks the
+     * leaves made since the last balanced forest (by the refine and coarsen
+     * above, then by the previous pass) and their face neighbours. */
+    int64_t *cand = NULL, n_cand = -1;   /* -1: every leaf */
+    {
+        int64_t nfr = 0;
+        for (int64_t k = 0; k < f->n; k++) nfr += isnew[k];
+        if (4 * nfr <= f->n) {           /* else most leaves are new: check them all */
+            int64_t *list = (int64_t *) malloc(sizeof(int64_t) * (size_t) (nfr + 1));
+            cand = (int64_t *) malloc(sizeof(int64_t) * (size_t) (f->n + 1));
+            if (!list || !cand) { free(list); free(cand); free(isnew); free(u); return CHARM_GPU_ENOMEM; }
+            nfr = 0;
+            for (int64_t k = 0; k < f->n; k++)
+                if (isnew[k]) list[nfr++] = k;
+            n_cand = charm_forest_fresh_neighbourhood(f, list, nfr, cand);
+            free(list);
+            if (n_cand < 0) { free(cand); free(isnew); free(u); return CHARM_GPU_ENOMEM; }
+        }
+        free(isnew);
+    }
     for (;;) {
         const int64_t nold = f->n;
         int8_t *bf = (int8_t *) calloc((size_t) nold + 1, 1);

@@ -243,3 +243,64 @@ def test_write_vtu_round_trip(tmp_path):
     h = np.array(case.tree_len)[None, :] / (2.0 ** mesh.level[:, None])
     assert np.allclose(xyz.mean(axis=1), mesh.center.T, rtol=0, atol=1e-15)
     assert np.allclose(xyz.max(axis=1) - xyz.min(axis=1), h, rtol=1e-15)
+
+
+def _records(mesh):
+    return (mesh.center.copy(), mesh.level.copy(), mesh.face_elem.copy(), mesh.face_info.copy(),
+            mesh.bface_elem.copy(), mesh.bface_face.copy(), mesh.bface_bnd.copy())
+
+
+def test_parallel_loops_from_two_threads():
+    """The host octree's worker pool serves one loop at a time; a loop that
+    finds it busy (another thread's flatten) runs on its own thread.  Both
+    give the records a lone flatten gives."""
+    import threading
+    case = Case(level=5, brick=(2, 1, 1), periodic=(1, 0, 1))
+    forests = [hanging_forest(case, frac=0.05, seed=21)[0] for _ in range(2)]
+    want = _records(forests[0].flatten())
+    got = [None, None]
+
+    def run(k):
+        for _ in range(3):
+            got[k] = _records(forests[k].flatten())
+
+    th = [threading.Thread(target=run, args=(k,)) for k in range(2)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join(timeout=120)
+    assert not any(t.is_alive() for t in th)
+    for g in got:
+        assert all(np.array_equal(a, b) for a, b in zip(g, want))
+
+
+@pytest.mark.filterwarnings("ignore:This process .* is multi-threaded:DeprecationWarning")
+def test_parallel_loops_in_forked_child():
+    """A child forked after the worker pool started has none of its threads:
+    its first parallel loop starts a pool of its own (no wait on a thread
+    that does not exist), and its records match the parent's."""
+    import os
+    import time
+    case = Case(level=5)
+    forest = hanging_forest(case, frac=0.05, seed=21)[0]
+    want = _records(forest.flatten())           # the pool is running now
+    pid = os.fork()
+    if pid == 0:                                # child: report by exit code only
+        code = 1
+        try:
+            got = _records(forest.flatten())
+            code = 0 if all(np.array_equal(a, b) for a, b in zip(got, want)) else 2
+        finally:
+            os._exit(code)
+    deadline = time.time() + 120
+    status = None
+    while time.time() < deadline:
+        done, status = os.waitpid(pid, os.WNOHANG)
+        if done:
+            break
+        time.sleep(0.05)
+    else:
+        os.kill(pid, 9)
+        os.waitpid(pid, 0)
+        pytest.fail("forked child did not finish its flatten")
+    assert os.WIFEXITED(status) and os.WEXITSTATUS(status) == 0
