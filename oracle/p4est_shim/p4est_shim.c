@@ -128,7 +128,7 @@ struct charm_shim_state {
     p4est_quadrant_t *q;   /* one per leaf, in leaf order */
 };
 
-/* Hook set by the driver: shift the geometry of a ghost copy by `shift`. */
+/* Hook set by ref_driver.c: shift the geometry of a ghost copy by `shift`. */
 void (*charm_shim_ghost_shift)(void *data, const double shift[3]) = NULL;
 
 static void *new_data(p4est_t *p, int nan_fill)

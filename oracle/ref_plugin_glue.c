@@ -1,7 +1,7 @@
 /*
  * Test glue for the GPU model plugin (charm_3d_gb300/csrc/plugin/charm_model_gpu.c)
- * inside the reference build: flatten the driver's current forest through the
- * plugin and build the plugin's configuration from the driver's context.
+ * inside the reference build: flatten ref_driver.c's current forest through the
+ * plugin and build the plugin's configuration from ref_driver.c's context.
  * Oracle-side test infrastructure; no GPU calls.
  */
 #include "charm_globals.h"
