@@ -1,6 +1,6 @@
 """Generate tests/golden/*.npz from the reference's own code (oracle/_ref).
 
-Run where the reference checkout exists:  python tests/golden/make_golden.py
+Run where the reference checkout exists:  python tests/golden/make_golden.py [name ...]
 Each fixture holds the initial state, the reference's residual int_* of it,
 and the reference's state after `steps` calls of timestep_single_fn, on a
 small brick mesh built by the host octree (identical leaves on both sides;
@@ -34,6 +34,13 @@ FIXTURES = {
     "mix2_hllc_bj": ("mix2", "HLLC", "BJ", "NS", 2, 2, False),
     "hanging_hllc_bj": ("random", "HLLC", "BJ", "NS", 2, 2, True),
     "hanging_lf": ("random", "LF", "NONE", "NS", 2, 2, True),
+    # viscous terms, species diffusion and Arrhenius chemistry
+    # (src/models/ns/charm_model_ns_diff*.c, charm_model_ns_chem.c)
+    "visc_hllc_bj": ("visc", "HLLC", "BJ", "NS", 2, 3, False),
+    "visc_walls_lf": ("visc_walls", "LF", "NONE", "NS", 2, 3, False),
+    "visc2_hllc_hanging": ("visc2", "HLLC", "NONE", "NS", 2, 2, True),
+    "react_hllc": ("react", "HLLC", "NONE", "NS", 2, 3, False),
+    "react_lf_bj": ("react", "LF", "BJ", "NS", 2, 3, False),
 }
 
 
@@ -112,16 +119,21 @@ def adjoint_fd() -> dict:
             "steps": np.array(ADJ_STEPS), "lo": np.array(lo), "hi": np.array(hi)}
 
 
-def main() -> None:
+def main(names: list[str]) -> None:
+    """All fixtures, or only the ones named on the command line."""
     for name in FIXTURES:
+        if names and name not in names:
+            continue
         d = make(name)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
         print(name, d["u0"].shape, "dt", float(d["dt"]))
-    np.savez_compressed(os.path.join(HERE, "point_fluxes.npz"), **point_fluxes())
-    print("point_fluxes")
-    np.savez_compressed(os.path.join(HERE, "adjoint_fd_vortex.npz"), **adjoint_fd())
-    print("adjoint_fd_vortex")
+    if not names or "point_fluxes" in names:
+        np.savez_compressed(os.path.join(HERE, "point_fluxes.npz"), **point_fluxes())
+        print("point_fluxes")
+    if not names or "adjoint_fd_vortex" in names:
+        np.savez_compressed(os.path.join(HERE, "adjoint_fd_vortex.npz"), **adjoint_fd())
+        print("adjoint_fd_vortex")
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

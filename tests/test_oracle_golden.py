@@ -1,7 +1,9 @@
 """The CPU oracle (oracle/charm_oracle.c) against fixtures made by the reference's own code.
 
 The fixtures in tests/golden/ were produced by tests/golden/make_golden.py
-from the reference sources compiled in oracle/_ref.  Bar: 1e-12 relative.
+from the reference sources compiled in oracle/_ref: Euler / Navier-Stokes
+convective cases, and viscous, multi-species diffusion and Arrhenius
+reacting cases (VISC_NAMES).  Bar: 1e-12 relative.
 """
 import os
 
@@ -11,12 +13,12 @@ import pytest
 from oracle.port import Port
 
 from .common import rel_l2, rel_max
-from .golden_cases import GOLDEN, NAMES, load
+from .golden_cases import GOLDEN, NAMES, VISC_NAMES, load
 
 TOL = 1e-12
 
 
-@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("name", NAMES + VISC_NAMES)
 def test_oracle_residual_matches_reference_fixture(name):
     case, _, mesh, d, _ = load(name)
     port = Port(case.config(), mesh)
@@ -25,7 +27,7 @@ def test_oracle_residual_matches_reference_fixture(name):
     assert rel_max(port.residual(), d["residual"]) < TOL
 
 
-@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("name", NAMES + VISC_NAMES)
 def test_oracle_steps_match_reference_fixture(name):
     case, _, mesh, d, meta = load(name)
     port = Port(case.config(), mesh)
