@@ -21,7 +21,7 @@ sys.path.insert(0, ROOT)
 
 from charm_3d_gb300.solver import Forest  # noqa: E402
 from oracle.ref import RefSolver  # noqa: E402
-from tests.common import hanging_forest, pressure_box_J, small_case  # noqa: E402
+from tests.common import amr_case, hanging_forest, pressure_box_J, small_case  # noqa: E402
 
 # name: (kind, flux, limiter, model, level, steps, hanging)
 FIXTURES = {
@@ -119,6 +119,45 @@ def adjoint_fd() -> dict:
             "steps": np.array(ADJ_STEPS), "lo": np.array(lo), "hi": np.array(hi)}
 
 
+# name: (kind, max_err, minlevel, level): one charm_adapt of the seeded state
+AMR_ADAPT = {
+    "amr_adapt_sod": ("sod", 0.05, 1, 2),
+    "amr_adapt_random": ("random", 0.3, 1, 2),
+    "amr_adapt_walls": ("walls", 0.2, 1, 2),
+}
+AMR_LOOP_STEPS = 7
+
+
+def amr_adapt(name: str) -> dict:
+    """The reference's charm_adapt (src/charm_amr.c:575-610; refine and
+    coarsen by the gradient estimate, 2:1 balance, projections; patched
+    limiter variant for the hanging faces) on a seeded state: its leaves
+    (tree, x, y, z, level) and the projected state."""
+    kind, max_err, minl, level = AMR_ADAPT[name]
+    case = small_case(kind, "HLLC", "BJ", level=level)
+    case.max_err, case.min_level, case.max_level = max_err, minl, level + 2
+    ref = RefSolver(case, "patched")
+    mesh = Forest(case).flatten()
+    u0 = case.initial_state(mesh.center)
+    ref.set_state(u0)
+    ref.adapt()
+    return {"u0": u0, "leaves": ref.leaves(), "state": ref.get_state(),
+            "meta": np.array(json.dumps({"kind": kind, "max_err": max_err, "min_level": minl, "level": level}))}
+
+
+def amr_loop() -> dict:
+    """AMR_LOOP_STEPS steps of the reference's time loop with an adapt every
+    2 steps (charm_model_ns_timestep_single, src/models/ns/charm_model.c:197-214)
+    on the small Sod AMR case: final leaves and state."""
+    case = amr_case("sod", level=2, max_level=4, max_err=0.05)
+    ref = RefSolver(case, "patched")
+    m0 = Forest(case).flatten()
+    u0 = case.initial_state(m0.center)
+    ref.set_state(u0)
+    ref.run(AMR_LOOP_STEPS)
+    return {"u0": u0, "leaves": ref.leaves(), "state": ref.get_state(), "steps": np.array(AMR_LOOP_STEPS)}
+
+
 def main(names: list[str]) -> None:
     """All fixtures, or only the ones named on the command line."""
     for name in FIXTURES:
@@ -130,6 +169,13 @@ def main(names: list[str]) -> None:
     if not names or "point_fluxes" in names:
         np.savez_compressed(os.path.join(HERE, "point_fluxes.npz"), **point_fluxes())
         print("point_fluxes")
+    for name in AMR_ADAPT:
+        if not names or name in names:
+            np.savez_compressed(os.path.join(HERE, name + ".npz"), **amr_adapt(name))
+            print(name)
+    if not names or "amr_loop_sod" in names:
+        np.savez_compressed(os.path.join(HERE, "amr_loop_sod.npz"), **amr_loop())
+        print("amr_loop_sod")
     if not names or "adjoint_fd_vortex" in names:
         np.savez_compressed(os.path.join(HERE, "adjoint_fd_vortex.npz"), **adjoint_fd())
         print("adjoint_fd_vortex")
