@@ -171,3 +171,41 @@ def pressure_box_J(case, mesh, u, lo, hi) -> float:
         p = r * e * (gam - 1.0)
         J += float((w8 * p)[inside].sum())
     return J
+
+
+def face_sets_of_reference(faces):
+    """Conforming (lower, upper, axis), hanging (lower, upper, axis, sub) and
+    boundary (element, face) records of the reference's face iteration
+    (p4est_iterate's face callback sides, one row per face)."""
+    conf, hang_set, bnd = set(), set(), set()
+    for r in faces:
+        ns = r[0]
+        if ns == 1:
+            bnd.add((int(r[3]), int(r[1])))
+            continue
+        f0, h0, f1, h1 = r[1], r[2], r[7], r[8]
+        assert f0 % 2 == 1 and f1 == f0 - 1, "side 0 must be the lower leaf"
+        if not h0 and not h1:
+            conf.add((int(r[3]), int(r[9]), int(f0 // 2)))
+        elif h1:
+            for k in range(4):
+                hang_set.add((int(r[3]), int(r[9 + k]), int(f0 // 2), k))
+        else:
+            for k in range(4):
+                hang_set.add((int(r[3 + k]), int(r[9]), int(f0 // 2), k))
+    return conf, hang_set, bnd
+
+
+def face_sets_of_mesh(mesh):
+    """The same records from the flattened mesh."""
+    got_c, got_h = set(), set()
+    for k in range(mesh.n_face):
+        a, b = (int(x) for x in mesh.face_elem[:, k])
+        info = int(mesh.face_info[k])
+        d, kind, sub = info & 3, (info >> 2) & 3, (info >> 4) & 3
+        if kind == 0:
+            got_c.add((a, b, d))
+        else:
+            got_h.add((a, b, d, sub))
+    got_b = {(int(e), int(f)) for e, f in zip(mesh.bface_elem, mesh.bface_face)}
+    return got_c, got_h, got_b

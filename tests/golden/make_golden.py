@@ -158,6 +158,17 @@ def amr_loop() -> dict:
     return {"u0": u0, "leaves": ref.leaves(), "state": ref.get_state(), "steps": np.array(AMR_LOOP_STEPS)}
 
 
+def mesh_faces() -> dict:
+    """The reference's face iteration (p4est_iterate face callback sides) on
+    the level-2 brick, uniform and with the seeded hanging refinement."""
+    case = small_case("random", "LF", "NONE", level=2)
+    uniform = RefSolver(case).faces()
+    forest, flags = hanging_forest(case)
+    ref = RefSolver(case, "patched")
+    assert ref.refine_flags(flags, case.level + 1) == len(forest)
+    return {"faces_uniform": uniform, "faces_hanging": ref.faces()}
+
+
 def main(names: list[str]) -> None:
     """All fixtures, or only the ones named on the command line."""
     for name in FIXTURES:
@@ -173,6 +184,9 @@ def main(names: list[str]) -> None:
         if not names or name in names:
             np.savez_compressed(os.path.join(HERE, name + ".npz"), **amr_adapt(name))
             print(name)
+    if not names or "mesh_faces" in names:
+        np.savez_compressed(os.path.join(HERE, "mesh_faces.npz"), **mesh_faces())
+        print("mesh_faces")
     if not names or "amr_loop_sod" in names:
         np.savez_compressed(os.path.join(HERE, "amr_loop_sod.npz"), **amr_loop())
         print("amr_loop_sod")

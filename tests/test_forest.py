@@ -304,3 +304,20 @@ def test_parallel_loops_in_forked_child():
         os.waitpid(pid, 0)
         pytest.fail("forked child did not finish its flatten")
     assert os.WIFEXITED(status) and os.WEXITSTATUS(status) == 0
+
+
+@pytest.mark.parametrize("hang", [False, True])
+def test_flatten_matches_reference_face_fixture(hang):
+    """Face and boundary records of flatten against the reference's own face
+    iteration recorded in tests/golden/mesh_faces.npz (conforming,
+    hanging 1-to-4 and boundary faces; same element indices)."""
+    import os
+    from .common import face_sets_of_mesh, face_sets_of_reference, small_case
+    from .golden_cases import GOLDEN
+    d = np.load(os.path.join(GOLDEN, "mesh_faces.npz"))
+    case = small_case("random", "LF", "NONE", level=2)
+    forest = hanging_forest(case)[0] if hang else Forest(case)
+    want = face_sets_of_reference(d["faces_hanging" if hang else "faces_uniform"])
+    assert face_sets_of_mesh(forest.flatten()) == want
+    if hang:
+        assert len(want[1]) > 0

@@ -10,7 +10,7 @@ from charm_3d_gb300 import Case
 from charm_3d_gb300.solver import Forest
 from oracle.ref import RefSolver
 
-from .common import hanging_forest, small_case
+from .common import face_sets_of_mesh, face_sets_of_reference, hanging_forest, small_case
 
 pytestmark = pytest.mark.reference
 
@@ -26,34 +26,7 @@ def test_reference_face_iteration_matches_flattened_mesh(hang):
         forest = Forest(case)
         ref = RefSolver(case)
     mesh = forest.flatten()
-    faces = ref.faces()
-    conf, hang_set, bnd = set(), set(), set()
-    for r in faces:
-        ns = r[0]
-        if ns == 1:
-            bnd.add((int(r[3]), int(r[1])))
-            continue
-        f0, h0, f1, h1 = r[1], r[2], r[7], r[8]
-        assert f0 % 2 == 1 and f1 == f0 - 1, "side 0 must be the lower leaf"
-        if not h0 and not h1:
-            conf.add((int(r[3]), int(r[9]), int(f0 // 2)))
-        elif h1:
-            for k in range(4):
-                hang_set.add((int(r[3]), int(r[9 + k]), int(f0 // 2), k))
-        else:
-            for k in range(4):
-                hang_set.add((int(r[3 + k]), int(r[9]), int(f0 // 2), k))
-    got_c, got_h = set(), set()
-    for k in range(mesh.n_face):
-        a, b = (int(x) for x in mesh.face_elem[:, k])
-        info = int(mesh.face_info[k])
-        d, kind, sub = info & 3, (info >> 2) & 3, (info >> 4) & 3
-        if kind == 0:
-            got_c.add((a, b, d))
-        else:
-            got_h.add((a, b, d, sub))
-    got_b = {(int(e), int(f)) for e, f in zip(mesh.bface_elem, mesh.bface_face)}
-    assert got_c == conf and got_h == hang_set and got_b == bnd
+    assert face_sets_of_mesh(mesh) == face_sets_of_reference(ref.faces())
 
 
 def test_reference_geometry_matches_box_formulas():
