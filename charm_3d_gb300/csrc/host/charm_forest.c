@@ -168,11 +168,14 @@ static void *pool_worker(void *arg)
     return NULL;
 }
 
-/* With g_dispatch held: start the workers if this process has none. */
-static void pool_start(int want)
+/* With g_dispatch held: start the workers (one per online CPU but the
+ * caller's) if this process has none. */
+static void pool_start(void)
 {
     pool_t *p = &g_pool;
     if (p->pid == getpid()) return;
+    const long cpus = sysconf(_SC_NPROCESSORS_ONLN);
+    const int want = (cpus > 1) ? (int) (cpus < kMaxThreads ? cpus : kMaxThreads) : 1;
     pthread_mutex_init(&p->mu, NULL);
     pthread_cond_init(&p->go, NULL);
     pthread_cond_init(&p->done, NULL);
@@ -197,18 +200,16 @@ static void pool_start(int want)
  * the pool busy, runs serially on the calling thread. */
 void charm_forest_parallel_for_min(int64_t n, int64_t min_chunk, charm_forest_range_fn fn, void *ctx)
 {
-    const long cpus = sysconf(_SC_NPROCESSORS_ONLN);
-    const int ncpu = (cpus > 1) ? (int) (cpus < kMaxThreads ? cpus : kMaxThreads) : 1;
-    int nt = ncpu;
     if (min_chunk < 1) min_chunk = 1;
-    if ((int64_t) nt > n / min_chunk) nt = (int) (n / min_chunk);
-    if (nt <= 1 || pthread_mutex_trylock(&g_dispatch) != 0) {
+    const int64_t most = n / min_chunk;   /* chunks worth a thread */
+    if (most <= 1 || pthread_mutex_trylock(&g_dispatch) != 0) {
         fn(ctx, 0, n);
         return;
     }
     pool_t *p = &g_pool;
-    pool_start(ncpu);
-    if (nt > p->nworkers + 1) nt = p->nworkers + 1;
+    pool_start();
+    int nt = p->nworkers + 1;
+    if ((int64_t) nt > most) nt = (int) most;
     if (nt <= 1) {
         pthread_mutex_unlock(&g_dispatch);
         fn(ctx, 0, n);
