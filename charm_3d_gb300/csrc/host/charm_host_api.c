@@ -568,6 +568,28 @@ static int coarsen_family(void *user, const charm_leaf_t *leaves, const int64_t 
     return err2 < c->err2_max * (vol * 8) ? 1 : 0;
 }
 
+typedef struct {
+    const charm_forest_t *f;
+    const double *grad;
+    int64_t E;
+    int ml;
+    double err2_max;
+    const double *vpow;
+    double vol[CHARM_FOREST_MAXLEVEL + 1];   /* box volume per level */
+    int8_t *fl;
+} refine_flags_ctx_t;
+
+/* charm_refine_err_estimate's test per leaf (src/charm_amr.c:32-47) */
+static void refine_flags_range(void *c, int64_t lo, int64_t hi)
+{
+    const refine_flags_ctx_t *x = (const refine_flags_ctx_t *) c;
+    for (int64_t i = lo; i < hi; i++) {
+        const int l = x->f->leaf[i].level;
+        if (l >= x->ml) continue;
+        x->fl[i] = err_sqr(x->grad, x->E, i, x->vpow[l]) > x->err2_max * x->vol[l];
+    }
+}
+
 /* The adapt of charm_adapt.  State mode (u_in): the state [V][4][E] is
  * projected along, into h->state.  Plan mode (rho_in): only the centre
  * densities [E] that the coarsening criterion reads are carried, and every
@@ -598,12 +620,14 @@ static int adapt_core(struct charm_host_forest_s *h, const double *grad, double 
     double vpow[CHARM_FOREST_MAXLEVEL + 1];
     level_vpow(f, vpow);
     /* 1. refine (charm_refine_err_estimate, non-recursive, maxlevel) */
-    for (int64_t i = 0; i < E0; i++) {
-        if (f->leaf[i].level >= ml) continue;
-        double hh[3];
-        leaf_h(f, f->leaf[i].level, hh);
-        const double vol = hh[0] * hh[1] * hh[2];
-        fl[i] = err_sqr(grad, E0, i, vpow[f->leaf[i].level]) > err2_max * vol;
+    {
+        refine_flags_ctx_t rc1 = {f, grad, E0, ml, err2_max, vpow, {0}, fl};
+        for (int l = 0; l <= CHARM_FOREST_MAXLEVEL; l++) {
+            double hh[3];
+            leaf_h(f, l, hh);
+            rc1.vol[l] = hh[0] * hh[1] * hh[2];
+        }
+        charm_forest_parallel_for(E0, refine_flags_range, &rc1);
     }
     /* the gradient of the leaves after refinement: unchanged leaves keep theirs,
      * new children get NaN, so their family is never coarsened in this adapt */
