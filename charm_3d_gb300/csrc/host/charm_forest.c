@@ -384,27 +384,71 @@ static void child_of(const charm_leaf_t *p, int c, charm_leaf_t *out)
     out->level = (int8_t) (p->level + 1);
 }
 
-int64_t charm_forest_refine(charm_forest_t *f, const int8_t *flag, int maxlevel,
-                            charm_forest_replace_fn replace, void *user)
+/* refine in blocks of leaves: per block the refined count, then (after a
+ * prefix sum) each block writes its leaves from its own output offset */
+enum { kRefineBlk = 4096 };
+
+typedef struct {
+    const charm_forest_t *f;
+    const int8_t *flag;
+    int maxlevel;
+    int64_t *off;        /* per block: refined leaves, then the first output index */
+    charm_leaf_t *nl;
+    int64_t *map;        /* old leaf -> first new index */
+} refine_ctx_t;
+
+static void refine_count_range(void *c, int64_t lo, int64_t hi)
 {
-    if (maxlevel < 0 || maxlevel > CHARM_FOREST_MAXLEVEL - 1) maxlevel = CHARM_FOREST_MAXLEVEL - 1;
-    int64_t nref = 0;
-    for (int64_t i = 0; i < f->n; i++)
-        if (flag[i] && f->leaf[i].level < maxlevel) nref++;
-    if (nref == 0) return 0;
-    int64_t nn = f->n + 7 * nref;
-    charm_leaf_t *nl = (charm_leaf_t *) malloc((size_t) nn * sizeof(charm_leaf_t));
-    int64_t *map = (int64_t *) malloc((size_t) f->n * sizeof(int64_t));
-    if (!nl || !map) { free(nl); free(map); return -1; }
-    int64_t k = 0;
-    for (int64_t i = 0; i < f->n; i++) {
-        map[i] = k;
-        if (flag[i] && f->leaf[i].level < maxlevel) {
-            for (int c = 0; c < 8; c++) child_of(&f->leaf[i], c, &nl[k++]);
-        } else {
-            nl[k++] = f->leaf[i];
+    const refine_ctx_t *x = (const refine_ctx_t *) c;
+    for (int64_t b = lo; b < hi; b++) {
+        const int64_t i0 = b * kRefineBlk, i1 = (i0 + kRefineBlk < x->f->n) ? i0 + kRefineBlk : x->f->n;
+        int64_t r = 0;
+        for (int64_t i = i0; i < i1; i++) r += (x->flag[i] && x->f->leaf[i].level < x->maxlevel);
+        x->off[b] = r;
+    }
+}
+
+static void refine_emit_range(void *c, int64_t lo, int64_t hi)
+{
+    const refine_ctx_t *x = (const refine_ctx_t *) c;
+    for (int64_t b = lo; b < hi; b++) {
+        const int64_t i0 = b * kRefineBlk, i1 = (i0 + kRefineBlk < x->f->n) ? i0 + kRefineBlk : x->f->n;
+        int64_t k = x->off[b];
+        for (int64_t i = i0; i < i1; i++) {
+            x->map[i] = k;
+            if (x->flag[i] && x->f->leaf[i].level < x->maxlevel) {
+                for (int ch = 0; ch < 8; ch++) child_of(&x->f->leaf[i], ch, &x->nl[k++]);
+            } else {
+                x->nl[k++] = x->f->leaf[i];
+            }
         }
     }
+}
+
+int64_t charm_forest_refine_map(charm_forest_t *f, const int8_t *flag, int maxlevel,
+                                charm_forest_replace_fn replace, void *user, int64_t *old_to_new)
+{
+    if (maxlevel < 0 || maxlevel > CHARM_FOREST_MAXLEVEL - 1) maxlevel = CHARM_FOREST_MAXLEVEL - 1;
+    const int64_t nblk = (f->n + kRefineBlk - 1) / kRefineBlk;
+    int64_t *off = (int64_t *) malloc(sizeof(int64_t) * (size_t) (nblk + 1));
+    if (!off) return -1;
+    refine_ctx_t x = {f, flag, maxlevel, off, NULL, NULL};
+    charm_forest_parallel_for_min(nblk, 2, refine_count_range, &x);
+    int64_t nref = 0;
+    for (int64_t b = 0; b < nblk; b++) {
+        const int64_t r = off[b];
+        off[b] = b * kRefineBlk + 7 * nref;
+        nref += r;
+    }
+    if (nref == 0) { free(off); return 0; }
+    const int64_t nn = f->n + 7 * nref;
+    charm_leaf_t *nl = (charm_leaf_t *) malloc((size_t) nn * sizeof(charm_leaf_t));
+    int64_t *map = old_to_new ? old_to_new : (int64_t *) malloc((size_t) f->n * sizeof(int64_t));
+    if (!nl || !map) { free(nl); if (map != old_to_new) free(map); free(off); return -1; }
+    x.nl = nl;
+    x.map = map;
+    charm_forest_parallel_for_min(nblk, 2, refine_emit_range, &x);
+    free(off);
     if (replace) {
         for (int64_t i = 0; i < f->n; i++) {
             if (flag[i] && f->leaf[i].level < maxlevel) {
@@ -414,12 +458,18 @@ int64_t charm_forest_refine(charm_forest_t *f, const int8_t *flag, int maxlevel,
             }
         }
     }
-    free(map);
+    if (map != old_to_new) free(map);
     free(f->leaf);
     f->leaf = nl;
     f->n = nn;
     f->cap = nn;
     return nref;
+}
+
+int64_t charm_forest_refine(charm_forest_t *f, const int8_t *flag, int maxlevel,
+                            charm_forest_replace_fn replace, void *user)
+{
+    return charm_forest_refine_map(f, flag, maxlevel, replace, user, NULL);
 }
 
 static int is_family(const charm_forest_t *f, int64_t i)

@@ -112,6 +112,11 @@ void charm_forest_leaf_geom(const charm_forest_t *f, int64_t i, double c[3], dou
  * Returns the number of refined leaves, or -1 on allocation failure. */
 int64_t charm_forest_refine(charm_forest_t *f, const int8_t *flag, int maxlevel,
                             charm_forest_replace_fn replace, void *user);
+/* The same; when old_to_new is not NULL (room for the old leaf count) it
+ * receives each old leaf's first index in the refined forest (its own, or
+ * its first child's); it is left untouched when nothing is refined. */
+int64_t charm_forest_refine_map(charm_forest_t *f, const int8_t *flag, int maxlevel,
+                                charm_forest_replace_fn replace, void *user, int64_t *old_to_new);
 
 /* One non-recursive pass over complete sibling families; merges those for which
  * pred() returns non-zero and whose level > minlevel.  Returns merges or -1. */

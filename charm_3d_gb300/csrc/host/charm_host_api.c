@@ -441,29 +441,61 @@ static void project_up(const double *u, int64_t E, const int64_t ch[8], const in
     }
 }
 
+/* refine flagged leaves one level (charm_forest_refine_map); o2n[E] gets
+ * each old leaf's first new index (the identity when nothing is refined) */
+static int refine_o2n(charm_forest_t *f, const int8_t *fl, int64_t **o2n)
+{
+    const int64_t E = f->n;
+    int64_t *m = (int64_t *) malloc(sizeof(int64_t) * (size_t) (E + 1));
+    if (!m) return CHARM_GPU_ENOMEM;
+    const int64_t r = charm_forest_refine_map(f, fl, -1, NULL, NULL, m);
+    if (r < 0) { free(m); return CHARM_GPU_ENOMEM; }
+    if (r == 0)
+        for (int64_t i = 0; i < E; i++) m[i] = i;
+    m[E] = f->n;   /* end of the last old leaf's outputs */
+    *o2n = m;
+    return CHARM_GPU_OK;
+}
+
+typedef struct {
+    const charm_forest_t *f;   /* refined */
+    const int64_t *o2n;        /* [E + 1] */
+    int64_t E, En;
+    int V;
+    const double *u;           /* state (refine_state) or densities (refine_plan) before */
+    double *w;                 /* after */
+    int32_t *map;              /* plan pass (refine_plan) */
+} refine_pass_ctx_t;
+
+static void refine_state_range(void *c, int64_t lo, int64_t hi)
+{
+    const refine_pass_ctx_t *x = (const refine_pass_ctx_t *) c;
+    for (int64_t i = lo; i < hi; i++) {
+        const int64_t k = x->o2n[i];
+        if (x->o2n[i + 1] - k == 8) {
+            for (int ch = 0; ch < 8; ch++)
+                project_down(x->u, x->E, i, x->w, x->En, k + ch, charm_leaf_child_id(&x->f->leaf[k + ch]), x->V);
+        } else {
+            for (int v = 0; v < x->V; v++)
+                for (int b = 0; b < 4; b++)
+                    x->w[((int64_t) v * 4 + b) * x->En + k] = x->u[((int64_t) v * 4 + b) * x->E + i];
+        }
+    }
+}
+
 /* refine flagged leaves one level, projecting the state */
 static int refine_state(charm_forest_t *f, const int8_t *fl, int V, double **u)
 {
     const int64_t E = f->n;
-    charm_leaf_t *old = (charm_leaf_t *) malloc(sizeof(charm_leaf_t) * (size_t) (E + 1));
-    if (!old) return CHARM_GPU_ENOMEM;
-    memcpy(old, f->leaf, sizeof(charm_leaf_t) * (size_t) E);
-    if (charm_forest_refine(f, fl, -1, NULL, NULL) < 0) { free(old); return CHARM_GPU_ENOMEM; }
+    int64_t *o2n = NULL;
+    int rc = refine_o2n(f, fl, &o2n);
+    if (rc) return rc;
     const int64_t En = f->n;
     double *w = (double *) malloc(sizeof(double) * (size_t) V * 4 * (size_t) En);
-    if (!w) { free(old); return CHARM_GPU_ENOMEM; }
-    int64_t k = 0;
-    for (int64_t i = 0; i < E; i++) {
-        if (fl[i] && old[i].level < CHARM_FOREST_MAXLEVEL - 1) {
-            for (int c = 0; c < 8; c++) project_down(*u, E, i, w, En, k + c, charm_leaf_child_id(&f->leaf[k + c]), V);
-            k += 8;
-        } else {
-            for (int v = 0; v < V; v++)
-                for (int b = 0; b < 4; b++) w[((int64_t) v * 4 + b) * En + k] = (*u)[((int64_t) v * 4 + b) * E + i];
-            k++;
-        }
-    }
-    free(old);
+    if (!w) { free(o2n); return CHARM_GPU_ENOMEM; }
+    refine_pass_ctx_t x = {f, o2n, E, En, V, *u, w, NULL};
+    charm_forest_parallel_for(E, refine_state_range, &x);
+    free(o2n);
     free(*u);
     *u = w;
     return CHARM_GPU_OK;
@@ -492,38 +524,42 @@ static int plan_push(struct charm_host_forest_s *h, int64_t n_out, int32_t *map)
  * copy of old leaf i (op -1) or child cid of old leaf i (op cid); the
  * centre densities *rho follow (children: NaN, never read: families made in
  * this adapt are not coarsened) */
+static void refine_plan_range(void *c, int64_t lo, int64_t hi)
+{
+    const refine_pass_ctx_t *x = (const refine_pass_ctx_t *) c;
+    for (int64_t i = lo; i < hi; i++) {
+        const int64_t k = x->o2n[i];
+        if (x->o2n[i + 1] - k == 8) {
+            for (int ch = 0; ch < 8; ch++) {
+                x->map[2 * (k + ch)] = (int32_t) i;
+                x->map[2 * (k + ch) + 1] = charm_leaf_child_id(&x->f->leaf[k + ch]);
+                x->w[k + ch] = NAN;
+            }
+        } else {
+            x->map[2 * k] = (int32_t) i;
+            x->map[2 * k + 1] = -1;
+            x->w[k] = x->u[i];
+        }
+    }
+}
+
 static int refine_plan(struct charm_host_forest_s *h, const int8_t *fl, double **rho)
 {
     charm_forest_t *f = &h->f;
     const int64_t E = f->n;
-    charm_leaf_t *old = (charm_leaf_t *) malloc(sizeof(charm_leaf_t) * (size_t) (E + 1));
-    if (!old) return CHARM_GPU_ENOMEM;
-    memcpy(old, f->leaf, sizeof(charm_leaf_t) * (size_t) E);
-    if (charm_forest_refine(f, fl, -1, NULL, NULL) < 0) { free(old); return CHARM_GPU_ENOMEM; }
+    int64_t *o2n = NULL;
+    int rc = refine_o2n(f, fl, &o2n);
+    if (rc) return rc;
     const int64_t En = f->n;
     int32_t *map = (int32_t *) malloc(sizeof(int32_t) * 2 * (size_t) (En > 0 ? En : 1));
     double *r = (double *) malloc(sizeof(double) * (size_t) (En > 0 ? En : 1));
-    if (!map || !r) { free(old); free(map); free(r); return CHARM_GPU_ENOMEM; }
-    int64_t k = 0;
-    for (int64_t i = 0; i < E; i++) {
-        if (fl[i] && old[i].level < CHARM_FOREST_MAXLEVEL - 1) {
-            for (int c = 0; c < 8; c++) {
-                map[2 * (k + c)] = (int32_t) i;
-                map[2 * (k + c) + 1] = charm_leaf_child_id(&f->leaf[k + c]);
-                r[k + c] = NAN;
-            }
-            k += 8;
-        } else {
-            map[2 * k] = (int32_t) i;
-            map[2 * k + 1] = -1;
-            r[k] = (*rho)[i];
-            k++;
-        }
-    }
-    free(old);
+    if (!map || !r) { free(o2n); free(map); free(r); return CHARM_GPU_ENOMEM; }
+    refine_pass_ctx_t x = {f, o2n, E, En, 1, *rho, r, map};
+    charm_forest_parallel_for(E, refine_plan_range, &x);
+    free(o2n);
     free(*rho);
     *rho = r;
-    int rc = plan_push(h, En, map);
+    rc = plan_push(h, En, map);
     if (rc) free(map);
     return rc;
 }
