@@ -538,6 +538,93 @@ int64_t charm_forest_coarsen(charm_forest_t *f, int minlevel, charm_forest_coars
     return nm;
 }
 
+typedef struct {
+    charm_forest_t *f;
+    int minlevel;
+    charm_forest_coarsen_fn pred;
+    void *user;
+    int8_t *merge;       /* per old leaf: a merged family starts here */
+    int64_t *off;        /* per block: merges, then the first output index */
+    charm_leaf_t *nl;
+    int64_t *n2o;
+} coarsen_ctx_t;
+
+static void coarsen_test_range(void *c, int64_t lo, int64_t hi)
+{
+    const coarsen_ctx_t *x = (const coarsen_ctx_t *) c;
+    for (int64_t b = lo; b < hi; b++) {
+        const int64_t i0 = b * kRefineBlk, i1 = (i0 + kRefineBlk < x->f->n) ? i0 + kRefineBlk : x->f->n;
+        int64_t m = 0;
+        for (int64_t i = i0; i < i1; i++) {
+            /* a family starts at child id 0, so its other members never test true */
+            int64_t idx[8];
+            for (int ch = 0; ch < 8; ch++) idx[ch] = i + ch;
+            x->merge[i] = (int8_t) (is_family(x->f, i) && x->f->leaf[i].level > x->minlevel &&
+                                    x->pred(x->user, x->f->leaf, idx));
+            m += x->merge[i];
+        }
+        x->off[b] = m;
+    }
+}
+
+static void coarsen_emit_range(void *c, int64_t lo, int64_t hi)
+{
+    const coarsen_ctx_t *x = (const coarsen_ctx_t *) c;
+    for (int64_t b = lo; b < hi; b++) {
+        const int64_t i0 = b * kRefineBlk, i1 = (i0 + kRefineBlk < x->f->n) ? i0 + kRefineBlk : x->f->n;
+        int64_t i = i0;
+        /* skip the members of a family that starts in the block before */
+        for (int64_t s = (i0 >= 7 ? i0 - 7 : 0); s < i0; s++)
+            if (x->merge[s] && s + 8 > i) i = s + 8;
+        int64_t k = x->off[b] + (i - i0);
+        while (i < i1) {
+            x->n2o[k] = i;
+            if (x->merge[i]) {
+                charm_leaf_t p = x->f->leaf[i];
+                p.level = (int8_t) (p.level - 1);
+                const int32_t len = CHARM_FOREST_QLEN(p.level);
+                p.x &= ~(len - 1); p.y &= ~(len - 1); p.z &= ~(len - 1);
+                x->nl[k++] = p;
+                i += 8;
+            } else {
+                x->nl[k++] = x->f->leaf[i++];
+            }
+        }
+    }
+}
+
+int64_t charm_forest_coarsen_map(charm_forest_t *f, int minlevel, charm_forest_coarsen_fn pred, void *user,
+                                 int64_t *new_to_old)
+{
+    if (f->n < 8) return 0;
+    const int64_t n = f->n, nblk = (n + kRefineBlk - 1) / kRefineBlk;
+    int8_t *merge = (int8_t *) calloc((size_t) n, 1);
+    int64_t *off = (int64_t *) malloc(sizeof(int64_t) * (size_t) (nblk + 1));
+    if (!merge || !off) { free(merge); free(off); return -1; }
+    coarsen_ctx_t x = {f, minlevel, pred, user, merge, off, NULL, new_to_old};
+    charm_forest_parallel_for_min(nblk, 1, coarsen_test_range, &x);
+    int64_t nm = 0;
+    for (int64_t b = 0; b < nblk; b++) {
+        const int64_t m = off[b];
+        off[b] = b * kRefineBlk - 7 * nm;
+        nm += m;
+    }
+    if (nm == 0) { free(merge); free(off); return 0; }
+    const int64_t nn = n - 7 * nm;
+    charm_leaf_t *nl = (charm_leaf_t *) malloc((size_t) nn * sizeof(charm_leaf_t));
+    if (!nl) { free(merge); free(off); return -1; }
+    x.nl = nl;
+    charm_forest_parallel_for_min(nblk, 2, coarsen_emit_range, &x);
+    new_to_old[nn] = n;
+    free(merge);
+    free(off);
+    free(f->leaf);
+    f->leaf = nl;
+    f->n = nn;
+    f->cap = nn;
+    return nm;
+}
+
 /* A leaf must be refined when some leaf two or more levels finer touches one
  * of its faces: the same-size neighbour region is split and at least one of
  * its four children next to our face is split again. */

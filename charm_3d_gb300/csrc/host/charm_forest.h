@@ -123,6 +123,14 @@ int64_t charm_forest_refine_map(charm_forest_t *f, const int8_t *flag, int maxle
 int64_t charm_forest_coarsen(charm_forest_t *f, int minlevel, charm_forest_coarsen_fn pred,
                              charm_forest_replace_fn replace, void *user);
 
+/* The same pass with pred() called from several threads at once (it must
+ * only read), no replace callback; new_to_old (required, room for the old
+ * leaf count + 1) receives each new leaf's first old index, and new_to_old[new count]
+ * = old count (a new leaf k is a merged family iff the difference to the
+ * next entry is 8); it is left untouched when nothing is merged. */
+int64_t charm_forest_coarsen_map(charm_forest_t *f, int minlevel, charm_forest_coarsen_fn pred, void *user,
+                                 int64_t *new_to_old);
+
 /* 2:1 face balance by ripple refinement.  Returns leaves refined, or -1. */
 int64_t charm_forest_balance(charm_forest_t *f, charm_forest_replace_fn replace, void *user);
 

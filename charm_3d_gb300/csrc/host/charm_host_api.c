@@ -626,6 +626,44 @@ static void refine_flags_range(void *c, int64_t lo, int64_t hi)
     }
 }
 
+/* the coarsen pass after charm_forest_coarsen_map: new leaf k is old leaf
+ * n2o[k] (op -1) or the parent of the family n2o[k] .. n2o[k] + 7, child
+ * ids 0..7 in Morton order (op 8); the state is projected (state mode) or
+ * the pass recorded (plan mode), and the new-leaf marks follow */
+typedef struct {
+    const int64_t *n2o;        /* [En + 1] */
+    int64_t E, En;
+    int V;
+    const double *u;           /* state before (state mode) */
+    double *w;                 /* state after (state mode) */
+    int32_t *map;              /* plan pass (plan mode) */
+    const int8_t *isnew;       /* [E] */
+    int8_t *isnew2;            /* [En] */
+} coarsen_pass_ctx_t;
+
+static void coarsen_pass_range(void *c, int64_t lo, int64_t hi)
+{
+    const coarsen_pass_ctx_t *x = (const coarsen_pass_ctx_t *) c;
+    static const int cid[8] = {0, 1, 2, 3, 4, 5, 6, 7};
+    for (int64_t k = lo; k < hi; k++) {
+        const int64_t i = x->n2o[k];
+        const int merged = (x->n2o[k + 1] - i == 8);
+        x->isnew2[k] = merged ? 1 : x->isnew[i];
+        if (x->map) {
+            x->map[2 * k] = (int32_t) i;
+            x->map[2 * k + 1] = merged ? 8 : -1;
+        } else if (merged) {
+            int64_t ch[8];
+            for (int j = 0; j < 8; j++) ch[j] = i + j;
+            project_up(x->u, x->E, ch, cid, x->w, x->En, k, x->V);
+        } else {
+            for (int v = 0; v < x->V; v++)
+                for (int b = 0; b < 4; b++)
+                    x->w[((int64_t) v * 4 + b) * x->En + k] = x->u[((int64_t) v * 4 + b) * x->E + i];
+        }
+    }
+}
+
 /* The adapt of charm_adapt.  State mode (u_in): the state [V][4][E] is
  * projected along, into h->state.  Plan mode (rho_in): only the centre
  * densities [E] that the coarsening criterion reads are carried, and every
@@ -691,56 +729,32 @@ static int adapt_core(struct charm_host_forest_s *h, const double *grad, double 
     /* 2. coarsen complete families (charm_coarsen_err_estimate, non-recursive) */
     {
         const int64_t E = f->n;
-        charm_leaf_t *old = (charm_leaf_t *) malloc(sizeof(charm_leaf_t) * (size_t) (E + 1));
-        if (!old) { free(u); free(rho); free(g1); free(isnew); return CHARM_GPU_ENOMEM; }
-        memcpy(old, f->leaf, sizeof(charm_leaf_t) * (size_t) E);
+        int64_t *n2o = (int64_t *) malloc(sizeof(int64_t) * (size_t) (E + 1));
+        if (!n2o) { free(u); free(rho); free(g1); free(isnew); return CHARM_GPU_ENOMEM; }
         coarsen_state_ctx_t cc = {f, g1, rho, u, E, n_comp, minlevel, err2_max, vpow};
-        int64_t nm = charm_forest_coarsen(f, minlevel, coarsen_family, NULL, &cc);
-        if (nm < 0) { free(old); free(u); free(rho); free(g1); free(isnew); return CHARM_GPU_ENOMEM; }
+        int64_t nm = charm_forest_coarsen_map(f, minlevel, coarsen_family, &cc, n2o);
+        if (nm < 0) { free(n2o); free(u); free(rho); free(g1); free(isnew); return CHARM_GPU_ENOMEM; }
         if (nm > 0) {
             const int64_t En = f->n;
             double *w = plan ? NULL : (double *) malloc(sizeof(double) * (size_t) V * 4 * (size_t) En);
             int32_t *map = plan ? (int32_t *) malloc(sizeof(int32_t) * 2 * (size_t) En) : NULL;
-            if (plan ? !map : !w) { free(old); free(u); free(rho); free(g1); free(isnew); return CHARM_GPU_ENOMEM; }
-            int64_t i = 0;
-            for (int64_t k = 0; k < En; k++) {
-                const charm_leaf_t *nl = &f->leaf[k], *ol = &old[i];
-                if (ol->level == nl->level && ol->x == nl->x && ol->y == nl->y && ol->z == nl->z && ol->tree == nl->tree) {
-                    isnew[k] = isnew[i];   /* k <= i: in place */
-                    if (plan) {
-                        map[2 * k] = (int32_t) i;
-                        map[2 * k + 1] = -1;
-                    } else {
-                        for (int v = 0; v < V; v++)
-                            for (int b = 0; b < 4; b++)
-                                w[((int64_t) v * 4 + b) * En + k] = u[((int64_t) v * 4 + b) * E + i];
-                    }
-                    i++;
-                } else {
-                    int64_t ch[8];
-                    int cid[8];
-                    for (int c = 0; c < 8; c++) { ch[c] = i + c; cid[c] = charm_leaf_child_id(&old[i + c]); }
-                    isnew[k] = 1;
-                    if (plan) {
-                        /* a family in Morton order: child ids 0..7 in turn */
-                        for (int c = 0; c < 8; c++)
-                            if (cid[c] != c) { free(map); free(old); free(rho); free(g1); free(isnew); return CHARM_GPU_EINVAL; }
-                        map[2 * k] = (int32_t) i;
-                        map[2 * k + 1] = 8;
-                    } else {
-                        project_up(u, E, ch, cid, w, En, k, V);
-                    }
-                    i += 8;
-                }
+            int8_t *isnew2 = (int8_t *) malloc((size_t) En + 1);
+            if ((plan ? !map : !w) || !isnew2) {
+                free(w); free(map); free(isnew2); free(n2o); free(u); free(rho); free(g1); free(isnew);
+                return CHARM_GPU_ENOMEM;
             }
+            coarsen_pass_ctx_t cp = {n2o, E, En, V, u, w, map, isnew, isnew2};
+            charm_forest_parallel_for(En, coarsen_pass_range, &cp);
+            free(isnew);
+            isnew = isnew2;
             if (plan) {
-                if ((rc = plan_push(h, En, map))) { free(map); free(old); free(rho); free(g1); free(isnew); return rc; }
+                if ((rc = plan_push(h, En, map))) { free(map); free(n2o); free(rho); free(g1); free(isnew); return rc; }
             } else {
                 free(u);
                 u = w;
             }
         }
-        free(old);
+        free(n2o);
     }
     free(g1);
     free(rho);   /* the balance passes do not read densities */
