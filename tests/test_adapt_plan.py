@@ -126,3 +126,35 @@ def test_restricted_ripples_equal_full_balance():
         qb, lb = fb.leaves()
         assert len(fa) == len(fb) and (qa == qb).all() and (la == lb).all(), f"round {r}"
     assert int(la.max()) - int(la.min()) >= 4
+
+
+def test_adapt_plan_matches_adapt_state_on_large_meshes():
+    """Meshes of 30-190 k leaves (the refine and coarsen passes run in blocks
+    of 4096 leaves on several threads, families straddle block edges): a
+    spherical front of refine flags moving outward, so every adapt refines,
+    coarsens and ripples; plan and state forms agree bit for bit."""
+    from charm_3d_gb300 import synthetic
+    case = synthetic("blast")
+    fa, fb = Forest(case), Forest(case)
+    mesh = fa.flatten()
+    rng = np.random.default_rng(5)
+    u = rng.standard_normal((case.n_var, 4, mesh.n_elem)) * 0.1
+    u[4, 0] += 1.0
+    coarsened = 0
+    for it in range(5):
+        r = np.sqrt(((mesh.center - 0.5) ** 2).sum(axis=0))
+        g = np.zeros((3, mesh.n_elem))
+        g[0] = np.where(np.abs(r - 0.1 - 0.01 * it) < 0.03, 50.0, 0.0)
+        rho = u[4:, 0].sum(axis=0)
+        ua = fa.adapt_state(g, case.max_err, case.min_level, case.max_level, case.n_comp, u)
+        n, plan = fb.adapt_plan(g, rho, case.max_err, case.min_level, case.max_level)
+        qa, la = fa.leaves()
+        qb, lb = fb.leaves()
+        assert n == len(fa) and (qa == qb).all() and (la == lb).all()
+        assert np.array_equal(apply_plan(plan, u), ua), f"adapt {it}"
+        for p in range(plan.n_pass):
+            m = np.ctypeslib.as_array(plan.map[p], (2 * plan.n_out[p],))
+            coarsened += int((m[1::2] == 8).sum())
+        mesh = fa.flatten()
+        u = ua
+    assert mesh.n_elem > 4 * 4096 and coarsened > 0
