@@ -1557,14 +1557,21 @@ int charm_gpu_refine_flags(charm_gpu_handle_t h, double max_err, int8_t *flags, 
         std::vector<int8_t> lev((size_t) h->E);
         CUDA_TRY(cudaMemcpy(lev.data(), h->d_level, (size_t) h->E, cudaMemcpyDeviceToHost));
         const double err2_max = max_err * max_err;
-        for (int64_t e = 0; e < h->E; e++) {
+        // the box volume and vol^(5/3) depend on the level only: the same
+        // expressions, evaluated once per level instead of once per element
+        double lvol[128], lpow[128];
+        for (int l = 0; l < 128; l++) {
             double hh[3];
-            for (int d = 0; d < 3; d++) hh[d] = ldexp(h->tree_len[d], -lev[e]);
-            const double vol = hh[0] * hh[1] * hh[2];
+            for (int d = 0; d < 3; d++) hh[d] = ldexp(h->tree_len[d], -l);
+            lvol[l] = hh[0] * hh[1] * hh[2];
+            lpow[l] = exp(log(lvol[l]) * 5. / 3.);
+        }
+        for (int64_t e = 0; e < h->E; e++) {
+            const int l = lev[e] & 127;   // leaf levels are 0..CHARM_FOREST_MAXLEVEL
             double diff2 = 0.0;
             for (int d = 0; d < 3; d++) diff2 += hg[d * h->E + e] * hg[d * h->E + e];
-            const double err2 = diff2 * (1. / 12.) * exp(log(vol) * 5. / 3.);
-            flags[e] = (err2 > err2_max * vol) ? 1 : 0;
+            const double err2 = diff2 * (1. / 12.) * lpow[l];
+            flags[e] = (err2 > err2_max * lvol[l]) ? 1 : 0;
         }
     }
     return CHARM_GPU_OK;
