@@ -71,7 +71,7 @@ def test_adapt_plan_matches_adapt_state(kind, max_err, minl, level, rounds):
         assert n_b == len(fa) and (qa == qb).all() and (la == lb).all()
         ub = apply_plan(plan, u)
         assert ub.shape == ua.shape
-        assert np.array_equal(ub, ua), f"round {r}"
+        assert np.array_equal(ub, ua), f"adapt {r}"
         mesh = fa.flatten()
         u = ua
 
@@ -97,7 +97,7 @@ def test_adapt_plan_balance_ripples():
         qb, lb = fb.leaves()
         assert n_b == len(fa) and (qa == qb).all() and (la == lb).all()
         ub = apply_plan(plan, u)
-        assert np.array_equal(ub, ua), f"round {r}"
+        assert np.array_equal(ub, ua), f"adapt {r}"
         ripple += max(0, plan.n_pass - 1)
         mesh = fa.flatten()
         u = ua
@@ -124,7 +124,7 @@ def test_restricted_ripples_equal_full_balance():
         fb.adapt(flags, 9, 9)
         qa, la = fa.leaves()
         qb, lb = fb.leaves()
-        assert len(fa) == len(fb) and (qa == qb).all() and (la == lb).all(), f"round {r}"
+        assert len(fa) == len(fb) and (qa == qb).all() and (la == lb).all(), f"adapt {r}"
     assert int(la.max()) - int(la.min()) >= 4
 
 
