@@ -484,7 +484,7 @@ static void refine_state_range(void *c, int64_t lo, int64_t hi)
 }
 
 /* refine flagged leaves one level, projecting the state */
-static int refine_state(charm_forest_t *f, const int8_t *fl, int V, double **u)
+static int refine_state(charm_forest_t *f, const int8_t *fl, int V, double **u, int64_t **o2n_out)
 {
     const int64_t E = f->n;
     int64_t *o2n = NULL;
@@ -495,7 +495,8 @@ static int refine_state(charm_forest_t *f, const int8_t *fl, int V, double **u)
     if (!w) { free(o2n); return CHARM_GPU_ENOMEM; }
     refine_pass_ctx_t x = {f, o2n, E, En, V, *u, w, NULL};
     charm_forest_parallel_for(E, refine_state_range, &x);
-    free(o2n);
+    if (o2n_out) *o2n_out = o2n;
+    else free(o2n);
     free(*u);
     *u = w;
     return CHARM_GPU_OK;
@@ -543,7 +544,7 @@ static void refine_plan_range(void *c, int64_t lo, int64_t hi)
     }
 }
 
-static int refine_plan(struct charm_host_forest_s *h, const int8_t *fl, double **rho)
+static int refine_plan(struct charm_host_forest_s *h, const int8_t *fl, double **rho, int64_t **o2n_out)
 {
     charm_forest_t *f = &h->f;
     const int64_t E = f->n;
@@ -556,7 +557,8 @@ static int refine_plan(struct charm_host_forest_s *h, const int8_t *fl, double *
     if (!map || !r) { free(o2n); free(map); free(r); return CHARM_GPU_ENOMEM; }
     refine_pass_ctx_t x = {f, o2n, E, En, 1, *rho, r, map};
     charm_forest_parallel_for(E, refine_plan_range, &x);
-    free(o2n);
+    if (o2n_out) *o2n_out = o2n;
+    else free(o2n);
     free(*rho);
     *rho = r;
     rc = plan_push(h, En, map);
@@ -664,6 +666,28 @@ static void coarsen_pass_range(void *c, int64_t lo, int64_t hi)
     }
 }
 
+/* the refine's old-to-new map o2n [E0 + 1] carries each old leaf's
+ * gradient to its new index, NaN for the children of a refined leaf */
+typedef struct {
+    const int64_t *o2n;
+    const double *grad;        /* [3][E0] */
+    int64_t E0, E1;
+    double *g1;                /* [3][E1] */
+    int8_t *isnew;             /* [E1] */
+} grad_fill_ctx_t;
+
+static void grad_fill_range(void *c, int64_t lo, int64_t hi)
+{
+    const grad_fill_ctx_t *x = (const grad_fill_ctx_t *) c;
+    for (int64_t i = lo; i < hi; i++) {
+        const int64_t k = x->o2n[i], n = x->o2n[i + 1] - k;
+        for (int64_t j = k; j < k + n; j++) {
+            for (int d = 0; d < 3; d++) x->g1[(int64_t) d * x->E1 + j] = (n == 8) ? NAN : x->grad[(int64_t) d * x->E0 + i];
+            x->isnew[j] = (int8_t) (n == 8);
+        }
+    }
+}
+
 /* The adapt of charm_adapt.  State mode (u_in): the state [V][4][E] is
  * projected along, into h->state.  Plan mode (rho_in): only the centre
  * densities [E] that the coarsening criterion reads are carried, and every
@@ -703,29 +727,23 @@ static int adapt_core(struct charm_host_forest_s *h, const double *grad, double 
         }
         charm_forest_parallel_for(E0, refine_flags_range, &rc1);
     }
-    /* the gradient of the leaves after refinement: unchanged leaves keep theirs,
-     * new children get NaN, so their family is never coarsened in this adapt */
-    int64_t E1 = E0;
-    for (int64_t i = 0; i < E0; i++) E1 += fl[i] ? 7 : 0;
-    double *g1 = (double *) malloc(sizeof(double) * 3 * (size_t) E1);
-    /* leaves that did not exist before this adapt (children made by the
-     * refine, parents made by the coarsen), in the current numbering */
-    int8_t *isnew = (int8_t *) malloc((size_t) E1 + 1);
-    if (!g1 || !isnew) { free(u); free(rho); free(fl); free(g1); free(isnew); return CHARM_GPU_ENOMEM; }
-    {
-        int64_t k = 0;
-        for (int64_t i = 0; i < E0; i++) {
-            int n = fl[i] ? 8 : 1;
-            for (int c = 0; c < n; c++) {
-                for (int d = 0; d < 3; d++) g1[(int64_t) d * E1 + k + c] = fl[i] ? NAN : grad[(int64_t) d * E0 + i];
-                isnew[k + c] = fl[i];
-            }
-            k += n;
-        }
-    }
-    int rc = plan ? refine_plan(h, fl, &rho) : refine_state(f, fl, V, &u);
+    int64_t *o2n = NULL;
+    int rc = plan ? refine_plan(h, fl, &rho, &o2n) : refine_state(f, fl, V, &u, &o2n);
     free(fl);
-    if (rc) { free(u); free(rho); free(g1); free(isnew); return rc; }
+    if (rc) { free(u); free(rho); free(o2n); return rc; }
+    /* the gradient of the leaves after refinement: unchanged leaves keep theirs,
+     * new children get NaN, so their family is never coarsened in this adapt;
+     * and the leaves that did not exist before this adapt (children made by
+     * the refine, then parents made by the coarsen), in the current numbering */
+    const int64_t E1 = f->n;
+    double *g1 = (double *) malloc(sizeof(double) * 3 * (size_t) E1);
+    int8_t *isnew = (int8_t *) malloc((size_t) E1 + 1);
+    if (!g1 || !isnew) { free(u); free(rho); free(g1); free(isnew); free(o2n); return CHARM_GPU_ENOMEM; }
+    {
+        grad_fill_ctx_t gf = {o2n, grad, E0, E1, g1, isnew};
+        charm_forest_parallel_for(E0, grad_fill_range, &gf);
+    }
+    free(o2n);
     /* 2. coarsen complete families (charm_coarsen_err_estimate, non-recursive) */
     {
         const int64_t E = f->n;
@@ -795,10 +813,10 @@ static int adapt_core(struct charm_host_forest_s *h, const double *grad, double 
         if (marks) {
             if (plan) {
                 double *dummy = (double *) calloc((size_t) nold + 1, sizeof(double));
-                rc = dummy ? refine_plan(h, bf, &dummy) : CHARM_GPU_ENOMEM;
+                rc = dummy ? refine_plan(h, bf, &dummy, NULL) : CHARM_GPU_ENOMEM;
                 free(dummy);
             } else {
-                rc = refine_state(f, bf, V, &u);
+                rc = refine_state(f, bf, V, &u, NULL);
             }
             if (!rc) {
                 /* the children made by this pass, at their new indices */
