@@ -364,6 +364,7 @@ extern "C" {
 
 int charm_gpu_objective(charm_gpu_handle_t h, const charm_gpu_objective_t *obj, double *J, double *dJdu)
 {
+    CfgLease lease(h);
     int rc = check_ready(h);
     if (rc) return rc;
     if (!obj || !J) return fail(CHARM_GPU_EINVAL, "null argument");
@@ -383,6 +384,7 @@ int charm_gpu_objective(charm_gpu_handle_t h, const charm_gpu_objective_t *obj, 
 
 int charm_gpu_residual_adjoint(charm_gpu_handle_t h, const double *rbar, double *ubar)
 {
+    CfgLease lease(h);
     int rc = check_ready(h);
     if (rc) return rc;
     if (!rbar || !ubar) return fail(CHARM_GPU_EINVAL, "null argument");
@@ -409,6 +411,7 @@ int charm_gpu_residual_adjoint(charm_gpu_handle_t h, const double *rbar, double 
 
 int charm_gpu_refine_flags_adjoint(charm_gpu_handle_t h, double max_err, int8_t *flags, double *grad_out)
 {
+    CfgLease lease(h);
     int rc = check_ready(h);
     if (rc) return rc;
     if (!flags && !grad_out) return fail(CHARM_GPU_EINVAL, "null argument");
@@ -457,6 +460,7 @@ int charm_gpu_refine_flags_adjoint(charm_gpu_handle_t h, double max_err, int8_t 
 int charm_gpu_adjoint(charm_gpu_handle_t h, int n_steps, int n_snapshots, const charm_gpu_objective_t *obj,
                       const double *dJdu_final, double *dJdu0, charm_gpu_adjoint_info_t *info)
 {
+    CfgLease lease(h);
     int rc = check_ready(h);
     if (rc) return rc;
     if (n_steps < 1 || n_snapshots < 1) return fail(CHARM_GPU_EINVAL, "n_steps and n_snapshots must be >= 1");

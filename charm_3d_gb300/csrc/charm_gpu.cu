@@ -119,7 +119,50 @@ struct charm_gpu_handle_s {
 
 namespace {
 
-const charm_gpu_handle_s *g_cfg_owner = nullptr;
+// The kernels read the solver configuration from one __constant__ symbol
+// (c_cfg, one copy per device).  Handles on the same device take turns: each
+// API call that launches kernels holds the device's CfgLease for its whole
+// launch sequence, and when another handle (or another stream) takes the
+// symbol over, its stream first waits on an event recorded after the last
+// work that read the previous contents.  So handles with different
+// configurations can be driven from several host threads and streams.
+constexpr int kMaxCfgDevices = 64;
+struct CfgSlot {
+    std::recursive_mutex mu;
+    const void *owner = nullptr;     // handle whose DevCfg c_cfg holds (nullptr: none)
+    cudaStream_t stream = nullptr;   // stream of the last launches that read c_cfg
+    bool live = false;               // `stream` may still have such work queued
+    bool fence_pending = false;      // `fence` marks such work on a stream given up since
+    cudaEvent_t fence = nullptr;
+};
+CfgSlot g_cfg_slot[kMaxCfgDevices];
+
+CfgSlot &cfg_slot(int device) { return g_cfg_slot[(device >= 0 && device < kMaxCfgDevices) ? device : 0]; }
+
+class CfgLease {
+  public:
+    explicit CfgLease(int device) : mu_(&cfg_slot(device).mu) { mu_->lock(); }
+    explicit CfgLease(const charm_gpu_handle_s *h);
+    ~CfgLease() { if (mu_) mu_->unlock(); }
+    CfgLease(const CfgLease &) = delete;
+    CfgLease &operator=(const CfgLease &) = delete;
+  private:
+    std::recursive_mutex *mu_ = nullptr;
+};
+
+// Order `next` after every queued launch that reads the current contents of
+// c_cfg (the caller holds the lease).  Returns a CUDA error or cudaSuccess.
+cudaError_t cfg_takeover(CfgSlot &s, cudaStream_t next)
+{
+    cudaError_t e = cudaSuccess;
+    if ((s.live && s.stream != next) || s.fence_pending) {
+        if (!s.fence && (e = cudaEventCreateWithFlags(&s.fence, cudaEventDisableTiming)) != cudaSuccess) return e;
+        if (s.live && s.stream != next && (e = cudaEventRecord(s.fence, s.stream)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(next, s.fence, 0)) != cudaSuccess) return e;
+    }
+    s.fence_pending = false;
+    return e;
+}
 
 int n_var(const charm_gpu_handle_s *h) { return 4 + h->cfg.n_comp; }
 
@@ -316,12 +359,26 @@ void build_devcfg(const charm_gpu_config_t *c, DevCfg *d)
     }
 }
 
+CfgLease::CfgLease(const charm_gpu_handle_s *h)
+{
+    if (h) {
+        mu_ = &cfg_slot(h->device).mu;
+        mu_->lock();
+    }
+}
+
+// Make c_cfg hold h's configuration for launches on h's stream (the caller
+// holds h's CfgLease).
 int ensure_cfg(charm_gpu_handle_s *h)
 {
-    if (g_cfg_owner == h) return CHARM_GPU_OK;
+    CfgSlot &s = cfg_slot(h->device);
+    if (s.owner == h && s.live && s.stream == h->stream) return CHARM_GPU_OK;
+    CUDA_TRY(cfg_takeover(s, h->stream));
     CUDA_TRY(cudaMemcpyToSymbolAsync(c_cfg, &h->dcfg, sizeof(DevCfg), 0, cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(p2_upload_cfg(&h->dcfg, h->stream));
-    g_cfg_owner = h;
+    s.owner = h;
+    s.stream = h->stream;
+    s.live = true;
     return CHARM_GPU_OK;
 }
 
@@ -454,8 +511,9 @@ template <int NC>
 int launch_cfl(charm_gpu_handle_s *h, const double *u)
 {
     MeshDev m = mesh_view(h);
-    const double big = 1.0e300;
-    CUDA_TRY(cudaMemcpyAsync(h->d_dt, &big, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    // the reference's reduction starts from TAU (src/models/ns/charm_model.c:50)
+    const double start = (h->cfg.tau > 0.0) ? h->cfg.tau : 1.0e300;
+    CUDA_TRY(cudaMemcpyAsync(h->d_dt, &start, sizeof(double), cudaMemcpyHostToDevice, h->stream));
     const int bs = 256;
     const int64_t nb = (h->E + bs - 1) / bs;
     TimedLaunch t;
@@ -1042,8 +1100,14 @@ int charm_gpu_destroy(charm_gpu_handle_t h)
     if (h->d_err) cudaFree(h->d_err);
     if (h->d_dt) cudaFree(h->d_dt);
     for (auto e : h->event_pool) cudaEventDestroy(e);
+    {
+        // the stream is idle: nothing queued reads c_cfg for this handle
+        CfgLease lease(h);
+        CfgSlot &s = cfg_slot(h->device);
+        if (s.owner == h) s.owner = nullptr;
+        if (s.live && s.stream == h->stream) s.live = false;
+    }
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
-    if (g_cfg_owner == h) g_cfg_owner = nullptr;
     delete h;
     return CHARM_GPU_OK;
 }
@@ -1070,24 +1134,35 @@ int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh)
         if (kind && h->nb != CHARM_GPU_BASIS) return fail(CHARM_GPU_ENOTSUP, "p2: conforming meshes only");
         cnt[a]++; cnt[b]++;
         const int fa = 2 * d + 1, fb = 2 * d;   // face ids on side 0 / side 1
+        // each element face takes exactly one record (the big side of a
+        // mortar: its first sub-face record)
+        auto claim = [&](int f, int32_t e, int8_t k, int32_t idx) {
+            if (lim_kind[f * E + e] >= 0) return false;
+            lim_kind[f * E + e] = k;
+            lim_idx[f * E + e] = idx;
+            return true;
+        };
         if (kind == 0) {
-            lim_kind[fa * E + a] = 0; lim_idx[fa * E + a] = b;
-            lim_kind[fb * E + b] = 0; lim_idx[fb * E + b] = a;
+            if (!claim(fa, a, 0, b) || !claim(fb, b, 0, a))
+                return fail(CHARM_GPU_EINVAL, "element face with more than one face record");
         } else {
             const int sub = (info >> 4) & 3;
             const int32_t small = (kind == 1) ? a : b, big = (kind == 1) ? b : a;
             const int fs = (kind == 1) ? fa : fb, fbig = (kind == 1) ? fb : fa;
-            lim_kind[fs * E + small] = (int8_t) (3 | (sub << 4)); lim_idx[fs * E + small] = big;
+            if (!claim(fs, small, (int8_t) (3 | (sub << 4)), big))
+                return fail(CHARM_GPU_EINVAL, "element face with more than one face record");
             if (sub == 0) {
                 // the 4 sub-faces of one big face must be consecutive records
                 if (i + 3 >= F) return fail(CHARM_GPU_EINVAL, "incomplete mortar");
                 for (int k = 1; k < 4; k++) {
                     const unsigned ik = mesh->face_info[i + k];
                     const int32_t bigk = (((ik >> 2) & 3) == 1) ? mesh->face_elem[F + i + k] : mesh->face_elem[i + k];
-                    if (((ik >> 4) & 3) != (unsigned) k || bigk != big || (ik & 3) != (unsigned) d)
+                    if (((ik >> 4) & 3) != (unsigned) k || bigk != big || (ik & 3) != (unsigned) d ||
+                        ((ik >> 2) & 3) != (unsigned) kind)
                         return fail(CHARM_GPU_EINVAL, "mortar sub-faces not consecutive");
                 }
-                lim_kind[fbig * E + big] = 2; lim_idx[fbig * E + big] = (int32_t) i;
+                if (!claim(fbig, big, 2, (int32_t) i))
+                    return fail(CHARM_GPU_EINVAL, "element face with more than one face record");
             }
         }
     }
@@ -1097,6 +1172,7 @@ int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh)
         if (e < 0 || e >= E || f < 0 || f > 5 || bnd < 0 || bnd >= h->cfg.n_bnd)
             return fail(CHARM_GPU_EINVAL, "boundary face record out of range");
         cnt[e]++;
+        if (lim_kind[f * E + e] >= 0) return fail(CHARM_GPU_EINVAL, "element face with more than one face record");
         lim_kind[f * E + e] = 1; lim_idx[f * E + e] = (int32_t) j;
     }
     for (int64_t k = 0; k < 6 * E; k++)
@@ -1299,6 +1375,7 @@ __global__ void __launch_bounds__(256) adapt_project_kernel(const double *__rest
 
 int charm_gpu_cell_fields(charm_gpu_handle_t h, double *out)
 {
+    CfgLease lease(h);
     int rc = check_ready(h);
     if (rc) return rc;
     if (!out) return fail(CHARM_GPU_EINVAL, "null argument");
@@ -1317,6 +1394,7 @@ int charm_gpu_cell_fields(charm_gpu_handle_t h, double *out)
 
 int charm_gpu_density_means(charm_gpu_handle_t h, double *rho)
 {
+    CfgLease lease(h);
     int rc = check_ready(h);
     if (rc) return rc;
     if (!rho) return fail(CHARM_GPU_EINVAL, "null argument");
@@ -1332,6 +1410,7 @@ int charm_gpu_density_means(charm_gpu_handle_t h, double *rho)
 
 int charm_gpu_adapt_upload(charm_gpu_handle_t h, const charm_gpu_adapt_plan_t *plan, const charm_gpu_mesh_t *mesh)
 {
+    CfgLease lease(h);
     int rc = check_ready(h);
     if (rc) return rc;
     if (!plan || !mesh || (plan->n_pass > 0 && (!plan->n_out || !plan->map))) return fail(CHARM_GPU_EINVAL, "null argument");
@@ -1414,6 +1493,7 @@ int charm_gpu_get_state(charm_gpu_handle_t h, double *u, int on_device)
 
 int charm_gpu_step(charm_gpu_handle_t h, double dt_in, double *dt_out)
 {
+    CfgLease lease(h);
     int rc = check_ready(h);
     if (rc) return rc;
     double dt;
@@ -1433,6 +1513,7 @@ int charm_gpu_step(charm_gpu_handle_t h, double dt_in, double *dt_out)
 
 int charm_gpu_run(charm_gpu_handle_t h, int nsteps, double dt_in)
 {
+    CfgLease lease(h);
     int rc = check_ready(h);
     if (rc) return rc;
     for (int s = 0; s < nsteps; s++) {
@@ -1449,6 +1530,7 @@ int charm_gpu_run(charm_gpu_handle_t h, int nsteps, double dt_in)
 
 int charm_gpu_get_dt(charm_gpu_handle_t h, double *dt)
 {
+    CfgLease lease(h);
     int rc = check_ready(h);
     if (rc) return rc;
     if (!dt) return fail(CHARM_GPU_EINVAL, "null argument");
@@ -1461,6 +1543,7 @@ int charm_gpu_get_dt(charm_gpu_handle_t h, double *dt)
 
 int charm_gpu_residual(charm_gpu_handle_t h, double *res, int on_device)
 {
+    CfgLease lease(h);
     int rc = check_ready(h);
     if (rc) return rc;
     if (!res) return fail(CHARM_GPU_EINVAL, "null argument");
@@ -1511,6 +1594,7 @@ int charm_gpu_residual(charm_gpu_handle_t h, double *res, int on_device)
 
 int charm_gpu_limit(charm_gpu_handle_t h)
 {
+    CfgLease lease(h);
     int rc = check_ready(h);
     if (rc) return rc;
     if (h->cfg.limiter != CHARM_GPU_LIM_BJ) return CHARM_GPU_OK;
@@ -1529,6 +1613,7 @@ int charm_gpu_limit(charm_gpu_handle_t h)
 
 int charm_gpu_refine_flags(charm_gpu_handle_t h, double max_err, int8_t *flags, double *grad_out)
 {
+    CfgLease lease(h);
     int rc = check_ready(h);
     if (rc) return rc;
     if (h->nb != CHARM_GPU_BASIS) return fail(CHARM_GPU_ENOTSUP, "refine flags: p1 only");
@@ -1580,8 +1665,19 @@ int charm_gpu_refine_flags(charm_gpu_handle_t h, double max_err, int8_t *flags, 
 int charm_gpu_set_stream(charm_gpu_handle_t h, void *stream)
 {
     if (!h) return fail(CHARM_GPU_EINVAL, "null handle");
-    h->stream = stream ? static_cast<cudaStream_t>(stream) : h->own_stream;
-    g_cfg_owner = nullptr;   // re-upload constants on the new stream
+    CfgLease lease(h);
+    CfgSlot &s = cfg_slot(h->device);
+    cudaStream_t next = stream ? static_cast<cudaStream_t>(stream) : h->own_stream;
+    if (s.live && s.stream == h->stream && next != h->stream) {
+        // the caller may destroy the old stream: mark its queued work now
+        CUDA_TRY(cudaSetDevice(h->device));
+        if (!s.fence) CUDA_TRY(cudaEventCreateWithFlags(&s.fence, cudaEventDisableTiming));
+        CUDA_TRY(cudaEventRecord(s.fence, h->stream));
+        s.fence_pending = true;
+        s.live = false;
+        s.owner = nullptr;   // re-upload the constants on the new stream
+    }
+    h->stream = next;
     return CHARM_GPU_OK;
 }
 
@@ -1637,6 +1733,7 @@ int charm_gpu_reset_stats(charm_gpu_handle_t h)
 
 int charm_gpu_time_run(charm_gpu_handle_t h, int nsteps, double dt_in, double *ms)
 {
+    CfgLease lease(h);
     int rc = check_ready(h);
     if (rc) return rc;
     if (!ms) return fail(CHARM_GPU_EINVAL, "null argument");
@@ -1758,6 +1855,13 @@ size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 // Per element face: (slot << 2) | tag; tag 0 = one slot, tag 1 = big side of
 // a mortar whose 4 sub-face records start at the face of `slot >> 1`.
 // Entries start at -1 (memset 0xff) and every element face must be written.
+// Element face slot idx takes its record's code; a second record for the
+// same element face marks the mesh invalid.
+__device__ __forceinline__ void static_claim(int32_t *ef, unsigned *ctl, int64_t idx, int32_t code)
+{
+    if (atomicCAS(reinterpret_cast<int *>(ef + idx), -1, (int) code) != -1) atomicOr(&ctl[kCtlBadRecord], 16u);
+}
+
 __global__ void static_table_kernel(MeshDev m, int n_bnd, int32_t *ef, unsigned *ctl)
 {
     const int64_t t = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
@@ -1769,14 +1873,14 @@ __global__ void static_table_kernel(MeshDev m, int n_bnd, int32_t *ef, unsigned 
         if (a < 0 || a >= E || b < 0 || b >= E || d > 2 || kind > 2) { atomicOr(&ctl[kCtlBadRecord], 1u); return; }
         const int fa = 2 * d + 1, fb = 2 * d;
         if (kind == 0) {
-            ef[(int64_t) fa * E + a] = (int32_t) ((2 * t) << 2);
-            ef[(int64_t) fb * E + b] = (int32_t) ((2 * t + 1) << 2);
+            static_claim(ef, ctl, (int64_t) fa * E + a, (int32_t) ((2 * t) << 2));
+            static_claim(ef, ctl, (int64_t) fb * E + b, (int32_t) ((2 * t + 1) << 2));
             return;
         }
         const int small = (kind == 1) ? a : b, big = (kind == 1) ? b : a;
         const int fs = (kind == 1) ? fa : fb, fbig = (kind == 1) ? fb : fa;
         const int64_t ss = (kind == 1) ? 2 * t : 2 * t + 1, sb = (kind == 1) ? 2 * t + 1 : 2 * t;
-        ef[(int64_t) fs * E + small] = (int32_t) (ss << 2);
+        static_claim(ef, ctl, (int64_t) fs * E + small, (int32_t) (ss << 2));
         if (sub == 0) {
             if (t + 3 >= F) { atomicOr(&ctl[kCtlBadRecord], 2u); return; }
             for (int k = 1; k < 4; k++) {
@@ -1787,13 +1891,13 @@ __global__ void static_table_kernel(MeshDev m, int n_bnd, int32_t *ef, unsigned 
                     return;
                 }
             }
-            ef[(int64_t) fbig * E + big] = (int32_t) ((sb << 2) | 1);
+            static_claim(ef, ctl, (int64_t) fbig * E + big, (int32_t) ((sb << 2) | 1));
         }
     } else if (t < F + m.n_bface) {
         const int64_t j = t - F;
         const int e = m.bface_elem[j], f = m.bface_face[j], bid = m.bface_bnd[j];
         if (e < 0 || e >= E || f < 0 || f > 5 || bid < 0 || bid >= n_bnd) { atomicOr(&ctl[kCtlBadRecord], 8u); return; }
-        ef[(int64_t) f * E + e] = (int32_t) ((2 * F + j) << 2);
+        static_claim(ef, ctl, (int64_t) f * E + e, (int32_t) ((2 * F + j) << 2));
     }
 }
 
@@ -1831,6 +1935,9 @@ static_gather_kernel(MeshDev m, const double *__restrict__ u, const T *__restric
         for (int v = 0; v < V; v++) U[v] = c[v][0] + px * c[v][1] + py * c[v][2] + pz * c[v][3];
         Prim<T, NC> p;
         cons_to_prim<T, NC>(U, p);
+        // the state check of cell_kernel: density and pressure at the Gauss points
+        if (!(p.r > T(0)) || !(p.p > T(0)))
+            set_error(&ctl[kCtlDeviceErr], isfinite((double) p.r) && isfinite((double) p.p) ? kErrNegative : kErrNonFinite);
         F[0] += U[0] * p.u + p.p; F[1] += U[0] * p.v; F[2] += U[0] * p.w; F[3] += U[0] * p.e_tot + p.p * p.u;
         G[0] += U[1] * p.u; G[1] += U[1] * p.v + p.p; G[2] += U[1] * p.w; G[3] += U[1] * p.e_tot + p.p * p.v;
         H[0] += U[2] * p.u; H[1] += U[2] * p.v; H[2] += U[2] * p.w + p.p; H[3] += U[2] * p.e_tot + p.p * p.w;
@@ -1959,7 +2066,19 @@ extern "C" int charm_gpu_residual_static(const charm_gpu_config_t *cfg, const ch
     DevCfg dcfg;
     build_devcfg(cfg, &dcfg);
     cudaError_t e;
-    g_cfg_owner = nullptr;   // handles re-upload their own configuration on their next launch
+    // take c_cfg over from any handle on this device (their queued launches
+    // finish first); every path below ends with st synchronised, so nothing
+    // of this call reads c_cfg after it returns
+    CfgLease lease(dev);
+    CfgSlot &cs = cfg_slot(dev);
+    struct Release {
+        CfgSlot &s;
+        ~Release() { s.owner = nullptr; s.live = false; }
+    } release{cs};
+    if ((e = cfg_takeover(cs, st)) != cudaSuccess) return fail(CHARM_GPU_ECUDA, cudaGetErrorString(e));
+    cs.owner = nullptr;
+    cs.stream = st;
+    cs.live = true;
     if ((e = cudaMemcpyToSymbolAsync(c_cfg, &dcfg, sizeof(DevCfg), 0, cudaMemcpyHostToDevice, st)) != cudaSuccess)
         return fail(CHARM_GPU_ECUDA, cudaGetErrorString(e));
     // clear the control words, and mark every element face unset
@@ -1986,7 +2105,9 @@ extern "C" int charm_gpu_residual_static(const charm_gpu_config_t *cfg, const ch
     if ((e = cudaMemcpyAsync(h_ctl, ctl, sizeof(h_ctl), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
         (e = cudaStreamSynchronize(st)) != cudaSuccess)
         return fail(CHARM_GPU_ECUDA, cudaGetErrorString(e));
-    if (h_ctl[kCtlBadRecord]) return fail(CHARM_GPU_EINVAL, "face record out of range or mortar records not consecutive");
+    if (h_ctl[kCtlBadRecord])
+        return fail(CHARM_GPU_EINVAL, "face record out of range, mortar records not consecutive, or an element face "
+                                      "with more than one record");
     const bool mixed = cfg->precision == CHARM_GPU_PREC_MIXED;
     switch (cfg->n_comp * 2 + (mixed ? 1 : 0)) {
     case 2: run_static<double, 1>(cfg, m, u, base, ef_off, slot_off, res, st); break;
@@ -2000,7 +2121,60 @@ extern "C" int charm_gpu_residual_static(const charm_gpu_config_t *cfg, const ch
         return fail(CHARM_GPU_ECUDA, cudaGetErrorString(e));
     if (h_ctl[kCtlMissingFace]) return fail(CHARM_GPU_EINVAL, "an element face has no face record");
     if (h_ctl[kCtlDeviceErr] & kErrNonFinite) return fail(CHARM_GPU_ENONFINITE, "non-finite state");
+    if (h_ctl[kCtlDeviceErr] & kErrNegative) return fail(CHARM_GPU_ENEGATIVE, "non-positive density or pressure");
     if (h_ctl[kCtlDeviceErr] & kErrHllc) return fail(CHARM_GPU_EHLLC, "HLLC: SL <= S* <= SR violated");
+    return CHARM_GPU_OK;
+}
+
+extern "C" int charm_gpu_point_flux(const charm_gpu_config_t *cfg, int64_t n, const double *U2, const double *normals,
+                                    double *q)
+{
+    if (!cfg || n < 0 || (n > 0 && (!U2 || !normals || !q))) return fail(CHARM_GPU_EINVAL, "null argument");
+    int rc = validate_config(cfg);
+    if (rc) return rc;
+    if (n == 0) return CHARM_GPU_OK;
+    if (n > ((int64_t) 1 << 30)) return fail(CHARM_GPU_EINVAL, "too many points");
+    const int V = 4 + cfg->n_comp;
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    DevCfg dcfg;
+    build_devcfg(cfg, &dcfg);
+    struct Bufs {
+        cudaStream_t st = nullptr;
+        double *U2 = nullptr, *nrm = nullptr, *q = nullptr;
+        unsigned *err = nullptr;
+        ~Bufs()
+        {
+            if (st) cudaStreamSynchronize(st);
+            cudaFree(U2); cudaFree(nrm); cudaFree(q); cudaFree(err);
+            if (st) cudaStreamDestroy(st);
+        }
+    } b;
+    CUDA_TRY(cudaStreamCreateWithFlags(&b.st, cudaStreamNonBlocking));
+    const size_t su = (size_t) n * 2 * V * sizeof(double), sn = (size_t) n * 3 * sizeof(double),
+                 sq = (size_t) n * V * sizeof(double);
+    if (cudaMalloc(&b.U2, su) != cudaSuccess || cudaMalloc(&b.nrm, sn) != cudaSuccess ||
+        cudaMalloc(&b.q, sq) != cudaSuccess || cudaMalloc(&b.err, sizeof(unsigned)) != cudaSuccess)
+        return fail(CHARM_GPU_ENOMEM, "cudaMalloc failed");
+    CUDA_TRY(cudaMemcpyAsync(b.U2, U2, su, cudaMemcpyHostToDevice, b.st));
+    CUDA_TRY(cudaMemcpyAsync(b.nrm, normals, sn, cudaMemcpyHostToDevice, b.st));
+    CUDA_TRY(cudaMemsetAsync(b.err, 0, sizeof(unsigned), b.st));
+    unsigned herr = 0;
+    {
+        // the point kernels have their own translation unit and so their own
+        // copy of the configuration constants: calls of this entry point
+        // take turns, handles are not affected
+        static std::mutex point_mu;
+        std::lock_guard<std::mutex> lock(point_mu);
+        const bool mixed = cfg->precision == CHARM_GPU_PREC_MIXED;
+        cudaError_t e = point_launch_flux(&dcfg, cfg->flux, cfg->n_comp, mixed, n, b.U2, b.nrm, b.q, b.err, b.st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(q, b.q, sq, cudaMemcpyDeviceToHost, b.st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, b.err, sizeof(unsigned), cudaMemcpyDeviceToHost, b.st);
+        cudaError_t e2 = cudaStreamSynchronize(b.st);
+        if (e == cudaSuccess) e = e2;
+        if (e != cudaSuccess) return fail(CHARM_GPU_ECUDA, cudaGetErrorString(e));
+    }
+    if (herr & kErrHllc) return fail(CHARM_GPU_EHLLC, "HLLC: SL <= S* <= SR violated");
     return CHARM_GPU_OK;
 }
 

@@ -507,118 +507,137 @@ __device__ void flux_hllc(const Prim<T, NC> &pa, const Prim<T, NC> &pb, const T 
     frame_out<AX, T>(nt, sn, fu, fv, fw, q);
 }
 
-// rim_orig (:8-180): exact Riemann solver (Newton on the star pressure).
+// Exact Riemann solver of the Euler equations for an ideal gas, written from
+// the published method (E. F. Toro, "Riemann Solvers and Numerical Methods
+// for Fluid Dynamics", 3rd ed., Springer 2009, ch. 4): Newton iteration on
+// the pressure function f(p) = f_L(p) + f_R(p) + u_R - u_L (Toro 4.5-4.7,
+// 4.37), the star states of each wave (4.50-4.61) and sampling at x/t = 0
+// (Toro 4.4, figs. 4.14-4.15).  The choices that fix its results are the
+// reference's (rim_orig, src/charm_fluxes.c:8-180):
+//   - initial guess: the acoustic (linearised) star pressure
+//       p0 = (p_L Z_R + p_R Z_L + (u_L - u_R) Z_L Z_R) / (Z_L + Z_R), Z = rho c;
+//   - stop when |f(p)| <= 1e-5 at the iterate just used (one further Newton
+//     update is applied), at most 5000 iterations, p floored at 1e-5;
+//   - each side's star velocity from its own wave relation, u*_L = u_L - f_L,
+//     u*_R = u_R + f_R; the star region is sampled by the sign of u*_R;
+//   - a vacuum (Toro 4.40 violated) gives the four vacuum edges and zero
+//     star states.
+// Outputs: density, specific internal energy, pressure, and the three
+// velocity components in the face frame (normal first).
 template <typename T>
-__device__ void rim_orig(T &RI, T &EI, T &PI, T &UI, T &VI, T &WI,
-                         T RB, T PB, T UB, T VB, T WB, T RE, T PE, T UE, T VE, T WE, T gam)
+struct RiemannSide {
+    T rho, p, un, c;          // density, pressure, normal velocity, sound speed
+};
+
+// f_K(p) and f_K'(p) of one side (Toro 4.6 shock, 4.7 rarefaction); g1 =
+// (gam-1)/(2 gam), g2 = (gam+1)/(2 gam).
+template <typename T>
+__device__ __forceinline__ void riemann_wave_curve(const RiemannSide<T> &k, T p, T gam, T g1, T g2, T &f, T &df)
 {
-    const T AGAM = gam - T(1);
-    const T CGAM = T(1) / gam; (void) CGAM;
-    const T DGAM = T(2) / AGAM;
-    const T GGAM = sqrt(gam * AGAM);
-    const T HGAM = AGAM / T(2);
-    const T FGAM = T(3) * gam - T(1);
-    const T OGAM = AGAM / (T(2) * gam);
-    const T QGAM = gam + T(1);
-    const T PGAM = QGAM / (T(2) * gam);
-    const T RGAM = T(4) * gam;
-    const T SGAM = gam * AGAM;
-    const T TGAM = QGAM / T(2);
-    const T eps = T(1.e-5);   // CHARM_RIM_EPS
-    T RF, RS, EF, ES, SBL, SFL, SSL, SEL, D, UF, US, P;
-    T CB = sqrt(gam * PB / RB), CE = sqrt(gam * PE / RE);
-    T EB = CB * CB / SGAM, EE = CE * CE / SGAM;
-    T RCB = RB * CB, RCE = RE * CE;
-    T DU = UB - UE;
-    US = T(0);
-    if (DU < T(-2) * (CB + CE) / AGAM) {
-        RF = RS = EF = ES = T(0);
-        SBL = UB - CB; SFL = UB + T(2) * CB / AGAM;
-        SSL = UE - T(2) * CE / AGAM; SEL = UE + CE;
-        UF = T(0);
+    const T ratio = p / k.p;
+    if (p >= k.p) {                                        // shock
+        const T a = k.rho * k.c * sqrt(g2 * ratio + g1);   // mass flux |m| through the shock
+        f = (p - k.p) / a;
+        df = ((gam + T(1)) * ratio + (T(3) * gam - T(1))) / (T(4) * gam * a * (g2 * ratio + g1));
+    } else {                                               // rarefaction
+        const T cs = k.c * exp(g1 * log(ratio));           // sound speed behind the fan
+        f = (cs - k.c) * (T(2) / (gam - T(1)));
+        df = cs / (gam * p);
+    }
+}
+
+// Star side K after the pressure p* is known: density, internal energy and
+// velocity behind wave K, and the two edges of wave K (outer, inner).
+// sgn = -1 for the left wave, +1 for the right one.
+template <typename T>
+__device__ __forceinline__ void riemann_star_side(const RiemannSide<T> &k, T ps, T gam, T sgn, T &rho, T &e, T &u,
+                                                  T &outer, T &inner)
+{
+    const T gm1 = gam - T(1);
+    if (ps >= k.p) {
+        // shock speed (Toro 4.52 / 4.59), density from mass and momentum
+        // balance across it (Rankine-Hugoniot), velocity from the mass flux
+        const T s = k.un + sgn * sqrt((T(0.5) * (gam + T(1)) * ps + T(0.5) * gm1 * k.p) / k.rho);
+        const T rel = k.un - s;
+        const T m = k.rho * rel;
+        rho = m * m / (k.p - ps + m * rel);
+        u = s + m / rho;
+        e = ps / (gm1 * rho);
+        outer = s;
+        inner = s;
     } else {
-        P = (PB * RCE + PE * RCB + DU * RCB * RCE) / (RCB + RCE);
-        int step = 0;
-        T F1, F2, FS1, FS2;
-        do {
-            if (P < eps) P = eps;
-            T PPB = P / PB;
-            if (PB <= P) {
-                T PKB = PGAM * PPB + OGAM, ZNB = RCB * sqrt(PKB);
-                F1 = (P - PB) / ZNB;
-                FS1 = (QGAM * PPB + FGAM) / (RGAM * ZNB * PKB);
-            } else {
-                T ZFB = CB * exp(log(PPB) * OGAM);
-                F1 = DGAM * (ZFB - CB);
-                FS1 = ZFB / (gam * P);
-            }
-            T PPE = P / PE;
-            if (PE <= P) {
-                T PKE = PGAM * PPE + OGAM, ZNE = RCE * sqrt(PKE);
-                F2 = (P - PE) / ZNE;
-                FS2 = (QGAM * PPE + FGAM) / (RGAM * ZNE * PKE);
-            } else {
-                T ZFE = CE * exp(log(PPE) * OGAM);
-                F2 = DGAM * (ZFE - CE);
-                FS2 = ZFE / (gam * P);
-            }
-            P = P + (DU - F1 - F2) / (FS1 + FS2);
-        } while ((fabs(DU - F1 - F2) > eps) && (++step < 5000));
-        T PPB = P / PB, PPE = P / PE;
-        T ZFB = CB * exp(log(PPB) * OGAM), ZFE = CE * exp(log(PPE) * OGAM);
-        if (PB <= P) {
-            D = UB - sqrt((TGAM * P + HGAM * PB) / RB);
-            T UBD = UB - D, RUBD = RB * UBD;
-            RF = RUBD * RUBD / (PB - P + RUBD * UBD);
-            UF = D + RUBD / RF;
-            EF = P / (AGAM * RF);
-            SBL = D; SFL = D;
-        } else {
-            EF = ZFB * ZFB / SGAM;
-            UF = UB + DGAM * (CB - ZFB);
-            RF = P / (AGAM * EF);
-            SBL = UB - CB; SFL = UF - ZFB;
-        }
-        if (PE <= P) {
-            D = UE + sqrt((TGAM * P + HGAM * PE) / RE);
-            T UED = UE - D, RUED = RE * UED;
-            RS = RUED * RUED / (PE - P + RUED * UED);
-            US = D + RUED / RS;
-            ES = P / (AGAM * RS);
-            SEL = D; SSL = D;
-        } else {
-            ES = ZFE * ZFE / SGAM;
-            US = UE - DGAM * (CE - ZFE);
-            RS = P / (AGAM * ES);
-            SSL = US + ZFE; SEL = UE + CE;
-        }
+        // isentropic fan (Toro 4.53-4.57 / 4.60-4.62)
+        const T cs = k.c * exp(log(ps / k.p) * (gm1 / (T(2) * gam)));
+        e = cs * cs / (gam * gm1);
+        u = k.un - sgn * (T(2) / gm1) * (k.c - cs);
+        rho = ps / (gm1 * e);
+        outer = k.un + sgn * k.c;        // head
+        inner = u + sgn * cs;            // tail
     }
-    if (SEL <= T(0)) { RI = RE; EI = EE; UI = UE; VI = VE; WI = WE; PI = AGAM * EI * RI; return; }
-    if (SBL >= T(0)) { RI = RB; EI = EB; UI = UB; VI = VB; WI = WB; PI = AGAM * EI * RI; return; }
-    if ((SSL >= T(0)) && (SFL <= T(0))) {
-        if (US >= T(0)) { RI = RF; EI = EF; UI = UF; VI = VB; WI = WB; }
-        else            { RI = RS; EI = ES; UI = US; VI = VE; WI = WE; }
-        PI = AGAM * EI * RI;
-        return;
-    }
-    if (SFL > T(0)) {
-        UI = (UB + DGAM * GGAM * sqrt(EB)) / (T(1) + DGAM);
-        VI = VB; WI = WB;
-        EI = UI * UI / SGAM;
-        RI = RB * exp(log(EI / EB) * (T(1) / AGAM));
+}
+
+template <typename T>
+__device__ void riemann_exact(T &rho_o, T &e_o, T &p_o, T &u_o, T &v_o, T &w_o,
+                              T rL, T pL, T uL, T vL, T wL, T rR, T pR, T uR, T vR, T wR, T gam)
+{
+    const T gm1 = gam - T(1);
+    const T g1 = gm1 / (T(2) * gam), g2 = (gam + T(1)) / (T(2) * gam);
+    const T tol = T(1.e-5);
+    const int max_iter = 5000;
+    const RiemannSide<T> L = {rL, pL, uL, sqrt(gam * pL / rL)};
+    const RiemannSide<T> R = {rR, pR, uR, sqrt(gam * pR / rR)};
+    const T du = uL - uR;
+
+    // star states behind each wave and the wave edges, left to right:
+    // xL0 <= xL1 (left wave), xR1 <= xR0 (right wave)
+    T rhoL = T(0), eL = T(0), usL = T(0), rhoR = T(0), eR = T(0), usR = T(0);
+    T xL0, xL1, xR0, xR1;
+    if (du < -(T(2) / gm1) * (L.c + R.c)) {
+        // vacuum between two rarefactions (Toro 4.40 violated)
+        xL0 = L.un - L.c; xL1 = L.un + (T(2) / gm1) * L.c;
+        xR1 = R.un - (T(2) / gm1) * R.c; xR0 = R.un + R.c;
     } else {
-        UI = (UE - DGAM * GGAM * sqrt(EE)) / (T(1) + DGAM);
-        VI = VE; WI = WE;
-        EI = UI * UI / SGAM;
-        RI = RE * exp(log(EI / EE) * (T(1) / AGAM));
+        const T zL = L.rho * L.c, zR = R.rho * R.c;
+        T p = (L.p * zR + R.p * zL + du * zL * zR) / (zL + zR);
+        for (int it = 0;;) {
+            if (p < tol) p = tol;
+            T fL, dfL, fR, dfR;
+            riemann_wave_curve<T>(L, p, gam, g1, g2, fL, dfL);
+            riemann_wave_curve<T>(R, p, gam, g1, g2, fR, dfR);
+            const T resid = du - fL - fR;          // -f(p)
+            p += resid / (dfL + dfR);
+            if (!(fabs(resid) > tol) || ++it >= max_iter) break;
+        }
+        riemann_star_side<T>(L, p, gam, T(-1), rhoL, eL, usL, xL0, xL1);
+        riemann_star_side<T>(R, p, gam, T(1), rhoR, eR, usR, xR0, xR1);
     }
-    PI = AGAM * EI * RI;
+
+    // sample the self-similar solution at x/t = 0
+    if (xR0 <= T(0)) {                                     // right of every wave
+        rho_o = rR; e_o = R.c * R.c / (gam * gm1); u_o = uR; v_o = vR; w_o = wR;
+    } else if (xL0 >= T(0)) {                              // left of every wave
+        rho_o = rL; e_o = L.c * L.c / (gam * gm1); u_o = uL; v_o = vL; w_o = wL;
+    } else if (xL1 <= T(0) && xR1 >= T(0)) {               // star region
+        if (usR >= T(0)) { rho_o = rhoL; e_o = eL; u_o = usL; v_o = vL; w_o = wL; }
+        else             { rho_o = rhoR; e_o = eR; u_o = usR; v_o = vR; w_o = wR; }
+    } else {
+        // inside a fan: the sonic point, u = c (left) or u = -c (right)
+        const T sgn = (xL1 > T(0)) ? T(-1) : T(1);
+        const RiemannSide<T> &k = (xL1 > T(0)) ? L : R;
+        const T e_k = k.c * k.c / (gam * gm1);            // the side's internal energy
+        u_o = (k.un - sgn * (T(2) / gm1) * k.c) / (T(1) + T(2) / gm1);
+        v_o = (xL1 > T(0)) ? vL : vR;
+        w_o = (xL1 > T(0)) ? wL : wR;
+        e_o = u_o * u_o / (gam * gm1);
+        rho_o = k.rho * exp(log(e_o / e_k) / gm1);
+    }
+    p_o = gm1 * e_o * rho_o;
 }
 
 // Godunov flux.  The reference's charm_calc_flux_godunov body is commented
 // out (src/charm_fluxes.c:182-253), so it leaves its outputs unset.  This is
 // the commented sketch made to work: rotate to (n,t1,t2), solve with
-// rim_orig using side 0's gamma, rotate back; species are upwinded with the
+// the exact solver above using side 0's gamma, rotate back; species are upwinded with the
 // interface mass flux.
 template <typename T, int NC>
 __device__ void flux_godunov(const Prim<T, NC> &pa, const Prim<T, NC> &pb, const T n[3], T *q)
@@ -631,7 +650,7 @@ __device__ void flux_godunov(const Prim<T, NC> &pa, const Prim<T, NC> &pb, const
         vb[j] = pb.u * nt[j][0] + pb.v * nt[j][1] + pb.w * nt[j][2];
     }
     T ri, ei, pi, uu[3];
-    rim_orig<T>(ri, ei, pi, uu[0], uu[1], uu[2], pa.r, pa.p, va[0], va[1], va[2], pb.r, pb.p, vb[0], vb[1], vb[2],
+    riemann_exact<T>(ri, ei, pi, uu[0], uu[1], uu[2], pa.r, pa.p, va[0], va[1], va[2], pb.r, pb.p, vb[0], vb[1], vb[2],
                 pa.gam);
     T uv[3];
     for (int i = 0; i < 3; i++) uv[i] = nt[0][i] * uu[0] + nt[1][i] * uu[1] + nt[2][i] * uu[2];

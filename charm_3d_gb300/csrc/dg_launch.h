@@ -62,4 +62,11 @@ template <typename T, int NC>
 void p2_launch_vflux(const MeshDev &m, const T *u, const T *vis, T *slots, int64_t nbi, unsigned nb,
                      cudaStream_t st);
 
+// ---- point fluxes (charm_point.cu) ------------------------------------------
+
+// Upload cfg to the unit's constants, then q[i] = flux between the state
+// pair U2[i] along nrm[i] (n pairs; T = double, or float for `mixed`).
+cudaError_t point_launch_flux(const DevCfg *cfg, int flux, int n_comp, bool mixed, int64_t n, const double *U2,
+                              const double *nrm, double *q, unsigned *err, cudaStream_t st);
+
 }  // namespace charm

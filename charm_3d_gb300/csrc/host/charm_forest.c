@@ -596,7 +596,9 @@ static void coarsen_emit_range(void *c, int64_t lo, int64_t hi)
 int64_t charm_forest_coarsen_map(charm_forest_t *f, int minlevel, charm_forest_coarsen_fn pred, void *user,
                                  int64_t *new_to_old)
 {
-    if (f->n < 8) return 0;
+    /* no predicate merges nothing, as in charm_forest_coarsen */
+    if (!pred || f->n < 8) return 0;
+    if (!new_to_old) return -1;
     const int64_t n = f->n, nblk = (n + kRefineBlk - 1) / kRefineBlk;
     int8_t *merge = (int8_t *) calloc((size_t) n, 1);
     int64_t *off = (int64_t *) malloc(sizeof(int64_t) * (size_t) (nblk + 1));

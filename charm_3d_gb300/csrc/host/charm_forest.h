@@ -127,7 +127,8 @@ int64_t charm_forest_coarsen(charm_forest_t *f, int minlevel, charm_forest_coars
  * only read), no replace callback; new_to_old (required, room for the old
  * leaf count + 1) receives each new leaf's first old index, and new_to_old[new count]
  * = old count (a new leaf k is a merged family iff the difference to the
- * next entry is 8); it is left untouched when nothing is merged. */
+ * next entry is 8); it is left untouched when nothing is merged.  A NULL
+ * pred merges nothing (returns 0); a NULL new_to_old returns -1. */
 int64_t charm_forest_coarsen_map(charm_forest_t *f, int minlevel, charm_forest_coarsen_fn pred, void *user,
                                  int64_t *new_to_old);
 

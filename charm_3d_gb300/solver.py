@@ -305,6 +305,22 @@ class Solver:
         abi.check(self.lib.charm_gpu_reset_stats(self.h), "charm_gpu_reset_stats")
 
 
+def point_flux(case: Case | abi.Config, U2: np.ndarray, normals: np.ndarray) -> np.ndarray:
+    """Numerical flux of the case's flux function between state pairs
+    U2[n][2][V] (conserved) along unit normals[n][3], on the current device
+    (charm_gpu_point_flux)."""
+    lib = abi.load()
+    cfg = case.config() if isinstance(case, Case) else case
+    U = np.ascontiguousarray(U2, dtype=np.float64)
+    nn = np.ascontiguousarray(normals, dtype=np.float64)
+    n = U.shape[0]
+    assert U.shape == (n, 2, 4 + cfg.n_comp) and nn.shape == (n, 3)
+    q = np.empty((n, 4 + cfg.n_comp))
+    abi.check(lib.charm_gpu_point_flux(C.byref(cfg), n, U.ctypes.data, nn.ctypes.data, q.ctypes.data),
+              "charm_gpu_point_flux")
+    return q
+
+
 def build_case(case: Case, device: int = 0, precision: str | None = None):
     """Forest + flattened mesh + solver with the case's initial state uploaded."""
     if precision is not None:

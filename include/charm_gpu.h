@@ -26,7 +26,11 @@
  *     density is the sum of the partial densities rc_i.
  *   - A handle is used by one host thread at a time; calls are ordered on the
  *     handle's CUDA stream.  `stream` arguments are cudaStream_t values passed
- *     as void* (NULL = the handle's own stream).
+ *     as void* (NULL = the handle's own stream).  Several handles may run
+ *     from several threads and streams at once: the kernels read the
+ *     configuration from one constant-memory copy per device, and a call
+ *     that switches it to another handle's configuration first waits (on
+ *     the GPU) for the launches still queued with the previous one.
  */
 #ifndef CHARM_GPU_H
 #define CHARM_GPU_H
@@ -65,8 +69,9 @@ enum { CHARM_GPU_PREC_FP64 = 0,     /* drop-in: all arithmetic in FP64 */
        CHARM_GPU_PREC_MIXED = 1 };  /* FP32 residual, FP64 state/update/dt */
 enum { CHARM_GPU_DT_TAU = 0,        /* fixed TAU: the reference's get_dt_fn
                                        (src/models/ns/charm_model.c:49) */
-       CHARM_GPU_DT_CFL = 1 };      /* CFL*volume/(|u|+c), min over cells (the
-                                       reference's unreachable code, :50-59) */
+       CHARM_GPU_DT_CFL = 1 };      /* CFL*volume/(|u|+c) at the cell centres,
+                                       min over cells and TAU (the reference's
+                                       unreachable code, :21-36, 50-59) */
 
 /* boundary types, same numbering as charm_bnd_types_t
  * (reference include/charm_globals.h:432-439) */
@@ -164,7 +169,11 @@ int charm_gpu_create(charm_gpu_handle_t *h, const charm_gpu_config_t *cfg, int d
 int charm_gpu_destroy(charm_gpu_handle_t h);
 
 /* Upload a flattened mesh (after each adapt).  The caller owns the arrays;
- * the library copies them.  Resets the state to zero. */
+ * the library copies them.  Resets the state to zero.  Invalid records
+ * (indices out of range, mortar sub-faces that are not 4 consecutive
+ * records, an element face without a record or with two) return
+ * CHARM_GPU_EINVAL before anything changes: the previous mesh and state
+ * stay as they were. */
 int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh);
 
 /* State in/out, layout [V][B][E] (reference charm_data_t.par.c,
@@ -237,10 +246,28 @@ int charm_gpu_abi_sizes(int64_t out[6]);
  * on a device (with that device current) looks up the array's address:
  * make it before any stream capture.  All calls share the array, so calls
  * that overlap on the GPU race; serialise them.  Synchronises `stream`.
+ * Errors as charm_gpu_sync reports them for a handle (non-finite state,
+ * non-positive density or pressure at a Gauss point, HLLC wave order), and
+ * CHARM_GPU_EINVAL for face records that point outside the mesh, mortar
+ * records that are not 4 consecutive sub-faces, an element face without a
+ * record or with two; `res` is then not written.
  */
 #define CHARM_GPU_STATIC_SCRATCH_BYTES ((size_t) 64 << 20)
 int charm_gpu_residual_static(const charm_gpu_config_t *cfg, const charm_gpu_mesh_t *mesh, const double *u, double *res,
                               void *stream);
+
+/*
+ * Numerical flux between n pairs of conserved states, evaluated by the same
+ * device functions as the face kernels (verification entry; the reference's
+ * counterpart is the configured flux_fn, include/charm_globals.h:238, as
+ * charm_calc_flux_{lf,hllc,godunov,cd} in src/charm_fluxes.c).  Host arrays:
+ * U2 [n][2][V] (side 0, side 1), normals [n][3] (unit, from side 0 to side
+ * 1), q [n][V].  An axis-aligned normal takes the face kernels' axis path,
+ * any other normal the general rotation.  cfg gives flux, EOS and
+ * components (precision FP64: double arithmetic; MIXED: the float
+ * instantiation of the mixed form).  Allocates and synchronises.
+ */
+int charm_gpu_point_flux(const charm_gpu_config_t *cfg, int64_t n, const double *U2, const double *normals, double *q);
 
 /* Element count, variables and basis size of the uploaded mesh. */
 int charm_gpu_dims(charm_gpu_handle_t h, int64_t *n_elem, int *n_var, int *n_basis);

@@ -1463,6 +1463,39 @@ int oracle_amr_grad(oracle_t *o, double *grad)
     return 0;
 }
 
+/* The CFL time step of the reference's get_dt (src/models/ns/charm_model.c:
+ * 21-36, 50-59; unreachable there after `return ctx->dt`): the minimum over
+ * the cells of CFL * volume / (|u| + c) with the fields at the cell centre,
+ * starting from TAU. */
+int oracle_cfl_dt(oracle_t *o, double *dt)
+{
+    double d = o->cfg.tau;
+    for (int64_t e = 0; e < o->E; e++) {
+        const elem_geom_t *g = &o->g[e];
+        double U[MAXV];
+        prim_t p;
+        get_fields(o, o->u, e, g->c, g->dh, g->c, U);
+        cons_to_prim(o, U, &p);
+        const double loc = o->cfg.cfl * g->vol / (sqrt(p.u * p.u + p.v * p.v + p.w * p.w) + p.cz);
+        if (loc < d) d = loc;
+    }
+    *dt = d;
+    return 0;
+}
+
+/* rim_orig above on n inputs (rL pL uL vL wL rR pR uR vR wR gam each) ->
+ * (r e p u v w), for the pin against the reference's own rim_orig. */
+int oracle_rim(int64_t n, const double *in, double *out)
+{
+    for (int64_t i = 0; i < n; i++) {
+        const double *a = in + 11 * i;
+        double *o = out + 6 * i;
+        rim_orig(&o[0], &o[1], &o[2], &o[3], &o[4], &o[5], a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8], a[9],
+                 a[10]);
+    }
+    return 0;
+}
+
 /* Point flux on two primitive states (r u v w p each), for unit tests. */
 int oracle_point_flux(oracle_t *o, const double *prim2, const double n[3], double *q)
 {

@@ -27,6 +27,8 @@ def load() -> C.CDLL:
         lib.oracle_point_bflux_cons.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         lib.oracle_point_vflux.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         lib.oracle_amr_grad.argtypes = [C.c_void_p, C.c_void_p]
+        lib.oracle_rim.argtypes = [C.c_int64, C.c_void_p, C.c_void_p]
+        lib.oracle_cfl_dt.argtypes = [C.c_void_p, C.c_void_p]
         _lib = lib
     return _lib
 
@@ -79,6 +81,12 @@ class Port:
     def run(self, nsteps: int, dt: float) -> None:
         self.lib.oracle_run(self.h, nsteps, dt)
 
+    def cfl_dt(self) -> float:
+        """The reference's CFL step of the current state (min with TAU)."""
+        d = C.c_double(0.0)
+        self.lib.oracle_cfl_dt(self.h, C.byref(d))
+        return d.value
+
     def amr_grad(self) -> np.ndarray:
         g = np.empty((3, self.mesh.n_elem))
         self.lib.oracle_amr_grad(self.h, g.ctypes.data)
@@ -113,3 +121,12 @@ class Port:
         q = np.zeros(4 + self.cfg.n_comp)
         self.lib.oracle_point_flux(self.h, p.ctypes.data, nn.ctypes.data, q.ctypes.data)
         return q
+
+
+def rim(inputs: np.ndarray) -> np.ndarray:
+    """The oracle's exact Riemann solver on rows (rL pL uL vL wL rR pR uR vR wR gam)
+    -> rows (r e p u v w)."""
+    a = np.ascontiguousarray(inputs, dtype=np.float64).reshape(-1, 11)
+    out = np.empty((a.shape[0], 6))
+    load().oracle_rim(a.shape[0], a.ctypes.data, out.ctypes.data)
+    return out

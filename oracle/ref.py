@@ -41,6 +41,7 @@ def load(variant: str = "ref") -> C.CDLL:
         lib.ref_adapt.restype = C.c_int64
         lib.ref_grad.argtypes = [C.c_void_p]
         lib.ref_point_flux.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.ref_rim.argtypes = [C.c_int64, C.c_void_p, C.c_void_p]
         lib.ref_refine_flags.argtypes = [C.c_void_p, C.c_int]
         lib.ref_refine_flags.restype = C.c_int64
         if variant == "plugin":
@@ -157,3 +158,11 @@ class RefSolver:
         q = np.zeros(4 + self.case.n_comp)
         self.lib.ref_point_flux(p.ctypes.data, nn.ctypes.data, q.ctypes.data)
         return q
+
+
+def rim(inputs: np.ndarray) -> np.ndarray:
+    """The reference's rim_orig on rows (rL pL uL vL wL rR pR uR vR wR gam) -> rows (r e p u v w)."""
+    a = np.ascontiguousarray(inputs, dtype=np.float64).reshape(-1, 11)
+    out = np.empty((a.shape[0], 6))
+    load("ref").ref_rim(a.shape[0], a.ctypes.data, out.ctypes.data)
+    return out

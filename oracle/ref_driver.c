@@ -476,6 +476,20 @@ int ref_grad(double *out)
 
 /* Direct calls into the reference's flux functions for point tests:
  * prim = 2 x (r u v w p) for a single-species ideal gas of the current case. */
+/* The reference's exact Riemann solver rim_orig (src/charm_fluxes.c:8-180)
+ * on n inputs (rL pL uL vL wL rR pR uR vR wR gam each) -> (r e p u v w). */
+int ref_rim(int64_t n, const double *in, double *out)
+{
+    int64_t i;
+    for (i = 0; i < n; i++) {
+        const double *a = in + 11 * i;
+        double *o = out + 6 * i;
+        rim_orig(&o[0], &o[1], &o[2], &o[3], &o[4], &o[5], a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8], a[9],
+                 a[10]);
+    }
+    return 0;
+}
+
 int ref_point_flux(const double *prim2, const double n[3], double *q)
 {
     charm_prim_t pr[2];

@@ -64,6 +64,20 @@ def small_case(kind: str, flux: str = "LF", limiter: str = "BJ", level: int = 3,
                         Boundary("SLIP", "BOUND_WALL_SLIP"),
                         Boundary("NOSLIP", "BOUND_WALL_NO_SLIP", (T_in,))]
         c.bnd_of_side = (0, 1, 2, 2, 3, 2)
+    elif kind == "massflow":
+        # mass-flow boundary (src/charm_bnd_cond.c:96-146) on both x faces with
+        # flow direction +x: inflow at -x (total temperature, mass flux,
+        # species), outflow at +x.  The state stays subsonic, so the outflow
+        # branch only reads its stored pressure param[6] and never writes it
+        # back (the write-back is not reproduced on the GPU or in the oracle).
+        c = synthetic("sod", level=level)
+        c.init = "random"
+        c.seed = 29
+        T_tot = 1.05 * 0.02869409 / 8.31446261815324
+        c.boundaries = [Boundary("MF", "BOUND_MASS_FLOW", (0.3, 1.0, T_tot, 1.0, 0.0, 0.0, 0.95, 1.0)),
+                        Boundary("OUT", "BOUND_OUTLET"),
+                        Boundary("SLIP", "BOUND_WALL_SLIP")]
+        c.bnd_of_side = (0, 0, 2, 2, 1, 2)
     elif kind == "mix2":
         # two species, mixture EOS (src/charm_eos.c:120-148), constant cp
         c = synthetic("sod", level=level)
@@ -101,7 +115,7 @@ def small_case(kind: str, flux: str = "LF", limiter: str = "BJ", level: int = 3,
         raise ValueError(kind)
     c.flux, c.limiter, c.model = flux, limiter, model
     c.steps = 3
-    if kind in ("random", "walls", "mix2", "visc", "visc_walls", "visc2", "react"):
+    if kind in ("random", "walls", "massflow", "mix2", "visc", "visc_walls", "visc2", "react"):
         # random slopes and no limiter: keep the step well inside p1 DG's CFL limit
         c.tau = 0.1 * (1.0 / 2 ** level) / 1.5
     return c

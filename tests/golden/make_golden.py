@@ -30,6 +30,7 @@ FIXTURES = {
     "vortex_hllc": ("vortex", "HLLC", "NONE", "NS", 3, 3, False),
     "walls_hllc_bj": ("walls", "HLLC", "BJ", "NS", 2, 3, False),
     "walls_cd": ("walls", "CD", "NONE", "NS", 2, 1, False),
+    "massflow_hllc": ("massflow", "HLLC", "NONE", "NS", 2, 3, False),
     "euler_lf_bj": ("random", "LF", "BJ", "EULER", 3, 2, False),
     "mix2_hllc_bj": ("mix2", "HLLC", "BJ", "NS", 2, 2, False),
     "hanging_hllc_bj": ("random", "HLLC", "BJ", "NS", 2, 2, True),
@@ -72,7 +73,7 @@ def make(name: str) -> dict:
 
 
 def point_fluxes() -> dict:
-    """Reference LF/HLLC/CD fluxes for random state pairs and random unit normals."""
+    """Reference LF/HLLC/CD fluxes for random state pairs and random unit normals, and its exact Riemann solver."""
     rng = np.random.default_rng(2024)
     n = 64
     prim = np.stack([rng.uniform(0.2, 2.0, n), rng.uniform(-1.5, 1.5, n), rng.uniform(-1.5, 1.5, n),
@@ -86,7 +87,83 @@ def point_fluxes() -> dict:
         case = small_case("random", flux, "NONE", level=1)
         ref = RefSolver(case)
         out[flux] = np.stack([ref.point_flux(prim2[i].ravel(), normals[i]) for i in range(n)])
+    # Godunov: the reference's flux function is a stub, so the fixture holds
+    # its exact solver rim_orig on the same pairs (face frame) and the flux
+    # assembled from that solution; plus rim_orig on a wide set of states
+    from oracle import ref as ref_mod
+    rin = rim_inputs(prim2, normals)
+    rout = ref_mod.rim(rin)
+    out["GODUNOV"] = np.stack([godunov_from_rim(prim2[i], normals[i], rout[i]) for i in range(n)])
+    out["rim_in"] = rim_cases()
+    out["rim_out"] = ref_mod.rim(out["rim_in"])
     return out
+
+
+GAM = 1.4
+
+
+def _frame(n: np.ndarray) -> np.ndarray:
+    """Rows n, t1, t2 of the face frame of charm_calc_flux_hllc (src/charm_fluxes.c:458-488)."""
+    nt = np.zeros((3, 3))
+    nt[0] = n
+    ri = np.hypot(n[0], n[1])
+    if ri > 1e-12:
+        nt[1] = (-n[1] / ri, n[0] / ri, 0.0)
+    else:
+        ri = np.hypot(n[1], n[2])
+        if ri > 1e-12:
+            nt[1] = (0.0, -n[2] / ri, n[1] / ri)
+        else:
+            ri = np.hypot(n[0], n[2])
+            nt[1] = (-n[2] / ri, 0.0, n[0] / ri)
+    nt[2] = np.cross(nt[0], nt[1])
+    return nt
+
+
+def godunov_from_rim(prim2: np.ndarray, n: np.ndarray, rim_out: np.ndarray) -> np.ndarray:
+    """The Godunov flux (the commented sketch of charm_calc_flux_godunov,
+    src/charm_fluxes.c:182-253, one species) assembled from the face-frame
+    solution (r e p u v w) of the exact solver."""
+    nt = _frame(n)
+    ri, ei, pi = rim_out[:3]
+    uu = rim_out[3:]
+    uv = nt.T @ uu
+    qr = ri * uu[0]
+    q = np.empty(5)
+    q[:3] = qr * uv + pi * n
+    q[3] = (ri * (ei + 0.5 * (uv @ uv)) + pi) * uu[0]
+    q[4] = qr
+    return q
+
+
+def rim_inputs(prim2: np.ndarray, normals: np.ndarray) -> np.ndarray:
+    """Exact-solver inputs (rL pL uL vL wL rR pR uR vR wR gam) of state pairs [n][2][r u v w p] in the face frame."""
+    rows = []
+    for k in range(prim2.shape[0]):
+        nt = _frame(normals[k])
+        row = []
+        for s in range(2):
+            r, u, v, w, p = prim2[k, s]
+            row += [r, p] + list(nt @ np.array([u, v, w]))
+        rows.append(row + [GAM])
+    return np.array(rows)
+
+
+def rim_cases() -> np.ndarray:
+    """Inputs of the exact Riemann solver over a wide range of states (all
+    wave patterns: shocks, rarefactions, fans across x/t = 0, supersonic
+    flow either way), no vacuum."""
+    rng = np.random.default_rng(4242)
+    n = 512
+    r = np.exp(rng.uniform(np.log(0.1), np.log(10.0), (n, 2)))
+    p = np.exp(rng.uniform(np.log(0.01), np.log(100.0), (n, 2)))
+    u = rng.uniform(-6.0, 6.0, (n, 2))
+    vt = rng.uniform(-1.0, 1.0, (n, 2, 2))
+    c = np.sqrt(GAM * p / r)
+    keep = (u[:, 1] - u[:, 0]) < 2.0 * (c[:, 0] + c[:, 1]) / (GAM - 1.0) - 1e-3
+    rows = np.concatenate([r[:, :1], p[:, :1], u[:, :1], vt[:, 0], r[:, 1:], p[:, 1:], u[:, 1:], vt[:, 1],
+                           np.full((n, 1), GAM)], axis=1)
+    return rows[keep]
 
 
 ADJ_EPS = 1e-6

@@ -11,8 +11,8 @@ from charm_3d_gb300.solver import Forest
 from .common import hanging_forest, small_case
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-NAMES = ["sod_lf_bj", "sod_step_lf_bj", "vortex_hllc", "walls_hllc_bj", "walls_cd", "euler_lf_bj", "mix2_hllc_bj",
-         "hanging_hllc_bj", "hanging_lf"]
+NAMES = ["sod_lf_bj", "sod_step_lf_bj", "vortex_hllc", "walls_hllc_bj", "walls_cd", "massflow_hllc", "euler_lf_bj",
+         "mix2_hllc_bj", "hanging_hllc_bj", "hanging_lf"]
 # viscous / reacting Navier-Stokes (the reference's diffusion and chemistry)
 VISC_NAMES = ["visc_hllc_bj", "visc_walls_lf", "visc2_hllc_hanging", "react_hllc", "react_lf_bj"]
 

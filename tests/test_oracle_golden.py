@@ -37,7 +37,7 @@ def test_oracle_steps_match_reference_fixture(name):
     assert np.isfinite(d["state"]).all()
 
 
-@pytest.mark.parametrize("flux", ["LF", "HLLC", "CD"])
+@pytest.mark.parametrize("flux", ["LF", "HLLC", "CD", "GODUNOV"])
 def test_oracle_point_fluxes_match_reference(flux):
     from .common import small_case
     from charm_3d_gb300.solver import Forest
@@ -47,6 +47,23 @@ def test_oracle_point_fluxes_match_reference(flux):
     got = np.stack([port.point_flux(d["prim2"][i].ravel(), d["normals"][i]) for i in range(d["prim2"].shape[0])])
     want = d[flux]
     assert np.abs(got - want).max() <= 1e-13 * np.abs(want).max()
+
+
+def test_oracle_exact_riemann_solver_matches_reference():
+    """The oracle's rim_orig against the reference's own rim_orig
+    (src/charm_fluxes.c:8-180) over shocks, rarefactions, sonic fans and
+    supersonic states; every sampled region occurs."""
+    from oracle.port import rim
+    d = np.load(os.path.join(GOLDEN, "point_fluxes.npz"))
+    got, want = rim(d["rim_in"]), d["rim_out"]
+    assert np.isfinite(want).all()
+    assert (np.abs(got - want) <= 1e-12 * np.abs(want) + 1e-300).all()
+    rin = d["rim_in"]
+    left = (want[:, 0] == rin[:, 0]) & (want[:, 3] == rin[:, 2])
+    right = (want[:, 0] == rin[:, 5]) & (want[:, 3] == rin[:, 7])
+    gam = rin[:, 10]
+    sonic = np.isclose(np.abs(want[:, 3]), np.sqrt(gam * want[:, 2] / want[:, 0]), rtol=1e-9)
+    assert left.sum() > 10 and right.sum() > 10 and sonic.sum() > 10 and (~(left | right | sonic)).sum() > 10
 
 
 def test_oracle_adjoint_fd_fixture():
