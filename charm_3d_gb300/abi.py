@@ -64,6 +64,24 @@ class Config(C.Structure):
                 ("react", Reaction * MAX_REACT), ("p_order", C.c_int)]
 
 
+MAX_REG = 16
+
+
+class CaseRegion(C.Structure):
+    _fields_ = [("name", C.c_char * 64), ("id", C.c_int), ("material_id", C.c_int), ("v", C.c_double * 3),
+                ("t", C.c_double), ("p", C.c_double), ("grav", C.c_double * 3), ("c", C.c_double * MAX_COMP)]
+
+
+class CaseFile(C.Structure):
+    """charm_case_t: task.yaml read by charm_case_read_yaml."""
+    _fields_ = [("cfg", Config), ("tmax", C.c_double), ("max_error", C.c_double), ("refine_period", C.c_int),
+                ("repartition_period", C.c_int), ("min_level", C.c_int), ("max_level", C.c_int),
+                ("file_output_step", C.c_int), ("log_output_step", C.c_int), ("mesh_type", C.c_char * 32),
+                ("mesh_name", C.c_char * 256), ("bnd_name", (C.c_char * 64) * MAX_BND),
+                ("comp_name", (C.c_char * 64) * MAX_COMP), ("comp_id", C.c_int * MAX_COMP), ("n_reg", C.c_int),
+                ("reg", CaseRegion * MAX_REG)]
+
+
 class Objective(C.Structure):
     _fields_ = [("kind", C.c_int32), ("pad", C.c_int32), ("lo", C.c_double * 3), ("hi", C.c_double * 3)]
 
@@ -126,6 +144,8 @@ SIGNATURES = [
     ("charm_gpu_density_means", C.c_int, [_P, _P]),
     ("charm_gpu_cell_fields", C.c_int, [_P, _P]),
     ("charm_gpu_adapt_upload", C.c_int, [_P, C.POINTER(AdaptPlan), C.POINTER(Mesh)]),
+    ("charm_case_read_yaml", C.c_int, [C.c_char_p, C.POINTER(CaseFile)]),
+    ("charm_case_parse_yaml", C.c_int, [C.c_char_p, C.POINTER(CaseFile)]),
     ("charm_host_forest_new", C.c_int, [C.POINTER(_P), _P, _P, _P, _P, C.c_int]),
     ("charm_host_forest_free", C.c_int, [_P]),
     ("charm_host_forest_count", C.c_int64, [_P]),
@@ -178,3 +198,14 @@ def check(code: int, where: str) -> None:
 
 def ptr(a: np.ndarray, ctype=C.c_double):
     return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def read_case_yaml(path: str | None = None, text: str | None = None) -> CaseFile:
+    """task.yaml (a file, or its text) read by the library's case reader."""
+    lib = load()
+    out = CaseFile()
+    if text is not None:
+        check(lib.charm_case_parse_yaml(text.encode(), C.byref(out)), "charm_case_parse_yaml")
+    else:
+        check(lib.charm_case_read_yaml(str(path).encode(), C.byref(out)), "charm_case_read_yaml")
+    return out

@@ -22,7 +22,7 @@ LIB = os.path.join(PKG, "libcharm_gpu.so")
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
 CUDA_SOURCES = ["charm_gpu.cu", "charm_p2.cu", "charm_point.cu"]
-C_SOURCES = ["host/charm_forest.c", "host/charm_host_api.c"]
+C_SOURCES = ["host/charm_forest.c", "host/charm_host_api.c", "host/charm_yaml.c", "host/charm_case.c"]
 
 
 def _nvcc() -> str:
@@ -69,8 +69,13 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
         if os.path.getmtime(LIB) >= newest:
             return LIB
     jobs = _objects(verbose_ptxas)
-    with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
-        logs = list(ex.map(lambda j: _run(j[0]), jobs))
+    # recompile an object only when it is missing or older than its source
+    # or any header (all translation units share the headers)
+    newest_header = max(os.path.getmtime(p) for p in headers)
+    todo = [j for j in jobs if force or verbose_ptxas or not os.path.exists(j[1]) or
+            os.path.getmtime(j[1]) < max(newest_header, os.path.getmtime(j[0][j[0].index("-c") + 1]))]
+    with cf.ThreadPoolExecutor(max_workers=max(1, len(todo))) as ex:
+        logs = list(ex.map(lambda j: _run(j[0]), todo))
     if verbose_ptxas:
         sys.stderr.write("".join(logs))
     objs = [o for _, o in jobs]

@@ -1056,6 +1056,9 @@ extern "C" {
 const char *charm_gpu_version(void) { return "charm_gpu 0.1 (sm_103a)"; }
 const char *charm_gpu_last_error(void) { return g_last_error.c_str(); }
 
+// the message of charm_gpu_last_error() for the host C code (case reader)
+void charm_internal_set_error(const char *msg) { g_last_error = msg ? msg : ""; }
+
 int charm_gpu_create(charm_gpu_handle_t *out, const charm_gpu_config_t *cfg, int device)
 {
     if (!out || !cfg) return fail(CHARM_GPU_EINVAL, "null argument");

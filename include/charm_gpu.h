@@ -366,6 +366,47 @@ int charm_gpu_adapt_upload(charm_gpu_handle_t h, const charm_gpu_adapt_plan_t *p
  * U, V, W, T, then f = 8 + i: the mass fraction C_i of species i. */
 int charm_gpu_cell_fields(charm_gpu_handle_t h, double *out);
 
+/* ---- case file ------------------------------------------------------------
+ * CHARM_3D's task.yaml read into the solver configuration, with the same
+ * keys, names and checks as the reference's charm_init_context_yaml
+ * (reference src/charm_init_yaml.cpp:333-428) and model initialisers
+ * (src/models/ns/charm_model_ns_init.cpp:14-89,
+ * src/models/euler/charm_model_euler_init.cpp:14-18), which need yaml-cpp.
+ * A reader of the YAML subset these files use (block and flow maps and
+ * lists, plain and quoted scalars, comments) is built in.  cfg gets the
+ * choices the step takes (flux, limiter, EOS of the material, model,
+ * components, boundaries in file order, TAU, CFL, gravity, reactions);
+ * precision FP64, p_order 1 and dt_mode TAU are set and may be changed
+ * before charm_gpu_create.  The rest of the file (time loop, AMR and output
+ * controls, mesh file, regions) is returned beside it.  Errors:
+ * CHARM_GPU_EINVAL (syntax, missing key, unknown name, the reference's
+ * checks) or CHARM_GPU_ENOTSUP (TABLE EOS, more components, boundaries or
+ * reactions than the device holds, regions with different gravity), with
+ * the message in charm_gpu_last_error(). */
+#define CHARM_CASE_MAX_REG 16
+
+typedef struct charm_case_region {   /* charm_reg_t, include/charm_globals.h */
+    char   name[64];
+    int    id, material_id;
+    double v[3], t, p, grav[3];
+    double c[CHARM_GPU_MAX_COMP];      /* concentration of each component (file order) */
+} charm_case_region_t;
+
+typedef struct charm_case {
+    charm_gpu_config_t cfg;
+    double tmax, max_error;              /* control.TMAX, MAX_ERROR */
+    int    refine_period, repartition_period, min_level, max_level, file_output_step, log_output_step;
+    char   mesh_type[32], mesh_name[256];          /* mesh.files_type, mesh.name */
+    char   bnd_name[CHARM_GPU_MAX_BND][64];        /* boundaries[i].name (cfg.bnd[i]) */
+    char   comp_name[CHARM_GPU_MAX_COMP][64];      /* components[i].name (cfg.comp[i]) */
+    int    comp_id[CHARM_GPU_MAX_COMP];
+    int    n_reg;
+    charm_case_region_t reg[CHARM_CASE_MAX_REG];
+} charm_case_t;
+
+int charm_case_read_yaml(const char *path, charm_case_t *out);
+int charm_case_parse_yaml(const char *text, charm_case_t *out);
+
 /* ---- host octree (the CPU side of the boundary) -------------------------- */
 
 typedef struct charm_host_forest_s *charm_host_forest_t;
