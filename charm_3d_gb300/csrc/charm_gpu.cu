@@ -314,6 +314,7 @@ void build_devcfg(const charm_gpu_config_t *c, DevCfg *d)
         d->ideal_gam = d->ideal_cp / d->ideal_cv;
         d->ideal_inv_cv = 1.0 / d->ideal_cv;
         d->ideal_qg = (d->ideal_gam + 1.0) / (2.0 * d->ideal_gam);
+        d->ideal_gm1 = d->ideal_gam - 1.0;
     }
     d->n_bnd = c->n_bnd;
     for (int b = 0; b < c->n_bnd; b++) {
@@ -326,6 +327,7 @@ void build_devcfg(const charm_gpu_config_t *c, DevCfg *d)
     d->ideal_cp_f = (float) d->ideal_cp; d->ideal_m_f = (float) d->ideal_m; d->ideal_cv_f = (float) d->ideal_cv;
     d->ideal_gam_f = (float) d->ideal_gam; d->ideal_inv_cv_f = (float) d->ideal_inv_cv;
     d->ideal_qg_f = (float) d->ideal_qg;
+    d->ideal_gm1_f = (float) d->ideal_gam - 1.f;   // as the float path computed it before
     for (int i = 0; i < CHARM_GPU_MAX_COMP; i++) {
         d->comp_m_f[i] = (float) d->comp_m[i];
         for (int k = 0; k < CHARM_GPU_MAX_CP; k++) d->comp_cp_f[i][k] = (float) d->comp_cp[i][k];
@@ -2178,6 +2180,26 @@ extern "C" int charm_gpu_point_flux(const charm_gpu_config_t *cfg, int64_t n, co
         if (e != cudaSuccess) return fail(CHARM_GPU_ECUDA, cudaGetErrorString(e));
     }
     if (herr & kErrHllc) return fail(CHARM_GPU_EHLLC, "HLLC: SL <= S* <= SR violated");
+    return CHARM_GPU_OK;
+}
+
+extern "C" int charm_gpu_math_check(int which, int64_t n, const double *a, const double *b, double *out)
+{
+    if (which < 0 || which > 1 || n < 0 || (n > 0 && (!b || !out || (which == 1 && !a))))
+        return fail(CHARM_GPU_EINVAL, "bad argument");
+    if (n == 0) return CHARM_GPU_OK;
+    if (n > ((int64_t) 1 << 28)) return fail(CHARM_GPU_EINVAL, "too many operands");
+    struct Bufs {
+        double *a = nullptr, *b = nullptr, *o = nullptr;
+        ~Bufs() { cudaFree(a); cudaFree(b); cudaFree(o); }
+    } d;
+    const size_t sz = (size_t) n * sizeof(double);
+    if (cudaMalloc(&d.a, sz) != cudaSuccess || cudaMalloc(&d.b, sz) != cudaSuccess || cudaMalloc(&d.o, sz) != cudaSuccess)
+        return fail(CHARM_GPU_ENOMEM, "cudaMalloc failed");
+    CUDA_TRY(cudaMemcpy(d.b, b, sz, cudaMemcpyHostToDevice));
+    if (which == 1) CUDA_TRY(cudaMemcpy(d.a, a, sz, cudaMemcpyHostToDevice));
+    CUDA_TRY(point_launch_math(which, n, d.a, d.b, d.o, nullptr));
+    CUDA_TRY(cudaMemcpy(out, d.o, sz, cudaMemcpyDeviceToHost));
     return CHARM_GPU_OK;
 }
 

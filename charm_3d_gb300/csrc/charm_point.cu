@@ -70,4 +70,21 @@ cudaError_t point_launch_flux(const DevCfg *cfg, int flux, int n_comp, bool mixe
     return cudaGetLastError();
 }
 
+// The FP64 division helpers of the flux path on given operands (which = 0:
+// rcp_nr(b); 1: qdiv(a, b)), for the check of their error against IEEE
+// division.
+__global__ void math_check_kernel(int which, int64_t n, const double *__restrict__ a, const double *__restrict__ b,
+                                  double *__restrict__ out)
+{
+    const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = (which == 0) ? rcp_nr(b[i]) : qdiv<double>(a[i], b[i]);
+}
+
+cudaError_t point_launch_math(int which, int64_t n, const double *a, const double *b, double *out, cudaStream_t st)
+{
+    math_check_kernel<<<(unsigned) ((n + 127) / 128), 128, 0, st>>>(which, n, a, b, out);
+    return cudaGetLastError();
+}
+
 }  // namespace charm

@@ -39,6 +39,7 @@ struct DevCfg {
     int    newton_t;       // comp[0] has a cp polynomial: T by Newton (src/charm_eos.c:105,129)
     double ideal_cp, ideal_m, ideal_cv, ideal_gam, ideal_inv_cv;
     double ideal_qg;       // (gam + 1) / (2 gam) of the HLLC wave-speed factor
+    double ideal_gm1;      // gam - 1
     double comp_m[kMaxComp];
     double comp_cp[kMaxComp][kMaxCp];
     int    comp_ncp[kMaxComp];
@@ -52,7 +53,7 @@ struct DevCfg {
     // FP32 mirrors (each the float rounding of the double above), read by the
     // float instantiations so that they issue no double->float conversions:
     // on GB300 those run on the narrow FP64 pipe.
-    float  ideal_cp_f, ideal_m_f, ideal_cv_f, ideal_gam_f, ideal_inv_cv_f, ideal_qg_f;
+    float  ideal_cp_f, ideal_m_f, ideal_cv_f, ideal_gam_f, ideal_inv_cv_f, ideal_qg_f, ideal_gm1_f;
     float  comp_m_f[kMaxComp];
     float  comp_cp_f[kMaxComp][kMaxCp];
     float  bnd_par_f[kMaxBnd][7 + kMaxComp];
@@ -84,14 +85,58 @@ __device__ __forceinline__ T cfgv(const double &d, const float &f)
     else return d;
 }
 
-// Quotient on the hot flux path: IEEE a/b in FP64; in the FP32 residual of
-// the mixed form the hardware reciprocal (__fdividef, within 2 ulp), whose
-// error stays far below the FP32 rounding of the residual itself.
+// FP64 reciprocal: the hardware's approximate reciprocal of the upper word
+// (rcp.approx.ftz.f64) refined by two Newton-Raphson steps
+// y <- y + y (1 - x y), each of which doubles the correct bits (the
+// textbook iteration for division, e.g. J.-M. Muller et al., Handbook of
+// Floating-Point Arithmetic, 2nd ed., 2018, sec. 4.6).  Within 1 ulp of 1/x
+// for normal x (tested against IEEE division); 4 FMAs on GB300's narrow FP64
+// pipe instead of the longer correctly rounded sequence of x / y.
+__device__ __forceinline__ double rcp_nr(double x)
+{
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    double e = fma(-x, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-x, y, 1.0);
+    return fma(y, e, y);
+}
+
+// Quotient on the hot flux path: a * rcp_nr(b) in FP64 (within 2 ulp of
+// IEEE a/b); in the FP32 residual of the mixed form the hardware reciprocal
+// (__fdividef, within 2 ulp), whose error stays far below the FP32 rounding
+// of the residual itself.
 template <typename T>
 __device__ __forceinline__ T qdiv(T a, T b)
 {
     if constexpr (sizeof(T) == sizeof(float)) return __fdividef(a, b);
-    else return a / b;
+    else return a * rcp_nr(b);
+}
+
+template <typename T>
+__device__ __forceinline__ T qrcp(T b)
+{
+    if constexpr (sizeof(T) == sizeof(float)) return __fdividef(1.f, b);
+    else return rcp_nr(b);
+}
+
+// Mass fraction clamped to [0, 1] (src/charm_globals.c:198-203).  FP64: by
+// the bit pattern on the integer pipe (positive doubles order as their
+// integer patterns), not by FP64 compares; a NaN fraction comes out as 0 or
+// 1, next to a density and velocities that are NaN as well.
+template <typename T>
+__device__ __forceinline__ T clamp01(T c)
+{
+    if constexpr (sizeof(T) == sizeof(float)) {
+        if (c < 0.f) c = 0.f;
+        if (c > 1.f) c = 1.f;
+        return c;
+    } else {
+        long long b = __double_as_longlong(c);
+        if (b < 0) b = 0;                                   // negative (and -0)
+        if (b > 0x3FF0000000000000LL) b = 0x3FF0000000000000LL;   // above 1.0
+        return __longlong_as_double(b);
+    }
 }
 
 // Square root on the hot flux path: IEEE sqrt in FP64; x * rsqrt(x) from the
@@ -111,6 +156,7 @@ __device__ __forceinline__ void set_error(unsigned *err, unsigned bit)
 template <typename T, int NC>
 struct Prim {
     T r, u, v, w, e, e_tot, p, t, cz, gam, cp, cv, m;
+    T ir;        // 1 / r (the HLLC shock factors use it)
     T c[NC];
 };
 
@@ -199,15 +245,17 @@ __device__ __forceinline__ void eos_switch(Prim<T, NC> &p, int flag)
         if (p.r < eps) p.r = eps;
         p.p  = p.r * p.e * (p.gam - T(1));
         p.cz = sqrt(p.gam * p.p / p.r);
+        p.ir = qrcp<T>(p.r);
         break;
     case 3:   // (T,p) -> (r, cz, e)
         if (p.p < eps) p.p = eps;
         p.r  = p.p * p.m / (p.t * T(kGasR));
         p.cz = sqrt(p.gam * p.p / p.r);
         p.e  = p.p / (p.r * (p.gam - T(1)));
+        p.ir = qrcp<T>(p.r);
         break;
-    default:  // 4: (r,e) -> (p, cz, T)
-        if (p.r < eps) p.r = eps;
+    default:  // 4: (r,e) -> (p, cz, T); p.ir set by the caller
+        if (p.r < eps) { p.r = eps; p.ir = T(1) / eps; }
         p.p  = p.r * p.e * (p.gam - T(1));
         p.cz = sqrt(p.gam * p.p / p.r);
         p.t  = p.e / p.cv;
@@ -230,25 +278,21 @@ __device__ __forceinline__ void cons_to_prim(const T *U, Prim<T, NC> &p)
     T r = T(0);
     for (int i = 0; i < NC; i++) r += U[4 + i];
     p.r = r;
-    T ir = qdiv<T>(T(1), r);
+    T ir = qrcp<T>(r);
+    p.ir = ir;
     p.u = U[0] * ir;
     p.v = U[1] * ir;
     p.w = U[2] * ir;
     p.e_tot = U[3] * ir;
     p.e = p.e_tot - T(0.5) * (p.u * p.u + p.v * p.v + p.w * p.w);
-    for (int i = 0; i < NC; i++) {
-        T c = U[4 + i] * ir;
-        if (c < T(0)) c = T(0);
-        if (c > T(1)) c = T(1);
-        p.c[i] = c;
-    }
+    for (int i = 0; i < NC; i++) p.c[i] = clamp01<T>(U[4 + i] * ir);
     p.t = T(0);
     if (c_cfg.ideal_fast && r >= T(kEps)) {
         // eos flag 4 for a constant-cp ideal gas (src/charm_eos.c:86-90),
-        // with 1/r and 1/cv reused instead of dividing again
+        // with 1/r, gam - 1 and 1/cv reused instead of computed again
         p.cp = cfgv<T>(c_cfg.ideal_cp, c_cfg.ideal_cp_f); p.m = cfgv<T>(c_cfg.ideal_m, c_cfg.ideal_m_f);
         p.cv = cfgv<T>(c_cfg.ideal_cv, c_cfg.ideal_cv_f); p.gam = cfgv<T>(c_cfg.ideal_gam, c_cfg.ideal_gam_f);
-        p.p = r * p.e * (p.gam - T(1));
+        p.p = r * p.e * cfgv<T>(c_cfg.ideal_gm1, c_cfg.ideal_gm1_f);
         p.cz = qsqrt<T>(p.gam * p.p * ir);
         p.t = p.e * cfgv<T>(c_cfg.ideal_inv_cv, c_cfg.ideal_inv_cv_f);
         return;
@@ -461,16 +505,21 @@ __device__ void flux_hllc(const Prim<T, NC> &pa, const Prim<T, NC> &pb, const T 
     frame_in<AX, T>(nt, sn, pa.u, pa.v, pa.w, ua, va, wa);
     frame_in<AX, T>(nt, sn, pb.u, pb.v, pb.w, ub, vb, wb);
 
-    T p_pvrs = T(0.5) * (pa.p + pb.p) - T(0.5) * (ub - ua) * T(0.25) * (pa.r + pb.r) * (pa.cz + pb.cz);
+    // PVRS star pressure (0.5 * 0.25 folded into 0.125, an exact scaling)
+    T p_pvrs = T(0.5) * (pa.p + pb.p) - T(0.125) * ((ub - ua) * (pa.r + pb.r)) * (pa.cz + pb.cz);
     T p_star = (p_pvrs > T(0)) ? p_pvrs : T(0);
-    // shock factor sqrt(1 + (gam+1)/(2 gam) (p*/p - 1)); (gam+1)/(2 gam) is a
-    // constant of the ideal gas with constant cp
+    // wave speeds c * q, q = sqrt(1 + (gam+1)/(2 gam) (p*/p - 1)) behind a
+    // shock (p* > p), else c; with c^2 = gam p / r this is
+    // c q = sqrt(gam / r * (p + (gam+1)/(2 gam) (p* - p))), which needs
+    // neither p*/p nor a second square root ((gam+1)/(2 gam) is a constant
+    // of the ideal gas with constant cp)
     const T qga = c_cfg.ideal_fast ? cfgv<T>(c_cfg.ideal_qg, c_cfg.ideal_qg_f) : qdiv<T>(pa.gam + T(1), T(2) * pa.gam);
     const T qgb = c_cfg.ideal_fast ? cfgv<T>(c_cfg.ideal_qg, c_cfg.ideal_qg_f) : qdiv<T>(pb.gam + T(1), T(2) * pb.gam);
-    const T ql = (p_star <= pa.p) ? T(1) : qsqrt<T>(T(1) + qga * (qdiv<T>(p_star, pa.p) - T(1)));
-    const T qr = (p_star <= pb.p) ? T(1) : qsqrt<T>(T(1) + qgb * (qdiv<T>(p_star, pb.p) - T(1)));
-    T sl = ua - pa.cz * ql;
-    T sr = ub + pb.cz * qr;
+    const T dpa = p_star - pa.p, dpb = p_star - pb.p;
+    const T cqa = (dpa <= T(0)) ? pa.cz : qsqrt<T>(pa.gam * pa.ir * (pa.p + qga * dpa));
+    const T cqb = (dpb <= T(0)) ? pb.cz : qsqrt<T>(pb.gam * pb.ir * (pb.p + qgb * dpb));
+    T sl = ua - cqa;
+    T sr = ub + cqb;
     if (sl > sr) { T tmp = sl; sl = sr; sr = tmp; }
     T s_star = pb.p - pa.p;
     s_star += pa.r * ua * (sl - ua);
@@ -491,7 +540,7 @@ __device__ void flux_hllc(const Prim<T, NC> &pa, const Prim<T, NC> &pb, const T 
     const T pk = ka ? pa.p : pb.p, ek = ka ? pa.e_tot : pb.e_tot, sk = ka ? sl : sr;
     const T fu_k = rk * uk * uk + pk, fv_k = rk * vk * uk, fw_k = rk * wk * uk, fe_k = (rk * ek + pk) * uk;
     if (star) {
-        const T inv = qdiv<T>(T(1), sk - s_star);
+        const T inv = qrcp<T>(sk - s_star);
         fu = f_hllc_u<T>(rk * uk, fu_k, sk, s_star, pk, rk, uk, inv);
         fv = f_hllc_v<T>(rk * vk, rk * uk * vk, sk, s_star, inv);
         fw = f_hllc_v<T>(rk * wk, rk * uk * wk, sk, s_star, inv);

@@ -41,17 +41,23 @@ static __constant__ float c_face_psf[6] = {(float) (1.0 / 6.0 - 0.5), (float) (2
 static __constant__ float c_face_ptf[6] = {(float) (1.0 / 6.0 - 0.5), (float) (1.0 / 6.0 - 0.5), (float) (2.0 / 3.0 - 0.5),
                                     (float) (1.0 / 3.0 - 0.5), (float) (5.0 / 6.0 - 0.5), (float) (5.0 / 6.0 - 0.5)};
 
+// and as double basis values (the same doubles as c_face_s[g] - 0.5)
+static __constant__ double c_face_psd[6] = {1.0 / 6.0 - 0.5, 2.0 / 3.0 - 0.5, 1.0 / 6.0 - 0.5,
+                                            5.0 / 6.0 - 0.5, 1.0 / 3.0 - 0.5, 5.0 / 6.0 - 0.5};
+static __constant__ double c_face_ptd[6] = {1.0 / 6.0 - 0.5, 1.0 / 6.0 - 0.5, 2.0 / 3.0 - 0.5,
+                                            1.0 / 3.0 - 0.5, 5.0 / 6.0 - 0.5, 5.0 / 6.0 - 0.5};
+
 template <typename T>
 __device__ __forceinline__ T face_ps(int g)
 {
     if constexpr (sizeof(T) == sizeof(float)) return c_face_psf[g];
-    else return c_face_s[g] - 0.5;
+    else return c_face_psd[g];
 }
 template <typename T>
 __device__ __forceinline__ T face_pt(int g)
 {
     if constexpr (sizeof(T) == sizeof(float)) return c_face_ptf[g];
-    else return c_face_t[g] - 0.5;
+    else return c_face_ptd[g];
 }
 
 // Cell quadrature: 2x2x2 Gauss points at +-1/sqrt(3) of the half edge, x

@@ -69,4 +69,7 @@ void p2_launch_vflux(const MeshDev &m, const T *u, const T *vis, T *slots, int64
 cudaError_t point_launch_flux(const DevCfg *cfg, int flux, int n_comp, bool mixed, int64_t n, const double *U2,
                               const double *nrm, double *q, unsigned *err, cudaStream_t st);
 
+// out[i] = rcp_nr(b[i]) (which 0) or qdiv(a[i], b[i]) (which 1), device arrays.
+cudaError_t point_launch_math(int which, int64_t n, const double *a, const double *b, double *out, cudaStream_t st);
+
 }  // namespace charm

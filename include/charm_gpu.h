@@ -269,6 +269,12 @@ int charm_gpu_residual_static(const charm_gpu_config_t *cfg, const charm_gpu_mes
  */
 int charm_gpu_point_flux(const charm_gpu_config_t *cfg, int64_t n, const double *U2, const double *normals, double *q);
 
+/* The FP64 division helpers of the flux kernels on n host operands
+ * (verification entry; no counterpart in the reference): which = 0:
+ * out = the Newton-refined reciprocal of b; 1: out = the quotient a / b as
+ * the kernels form it.  Allocates and synchronises. */
+int charm_gpu_math_check(int which, int64_t n, const double *a, const double *b, double *out);
+
 /* Element count, variables and basis size of the uploaded mesh. */
 int charm_gpu_dims(charm_gpu_handle_t h, int64_t *n_elem, int *n_var, int *n_basis);
 

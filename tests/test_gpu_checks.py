@@ -12,6 +12,8 @@
   completes with the same state as an unhurried one.
 - Corrupted face records passed to charm_gpu_upload_mesh return
   CHARM_GPU_EINVAL and leave the handle's mesh and state usable.
+- The flux kernels' FP64 reciprocal and quotient (hardware seed + Newton
+  steps) against IEEE division: within 1 and 2 ulp.
 """
 import copy
 import os
@@ -190,3 +192,26 @@ def test_upload_rejects_corrupted_faces_and_keeps_mesh():
     gpu.run(2, case.tau)
     gpu.sync()
     assert rel_l2(gpu.get_state(), port.get_state()) < 1e-12
+
+
+def _ulps(got, want):
+    """Distance in units in the last place of want."""
+    return np.abs(got - want) / np.spacing(np.abs(want))
+
+
+def test_fp64_reciprocal_and_quotient_error_bounds():
+    """The flux kernels' FP64 reciprocal (hardware seed + two Newton steps)
+    within 1 ulp of IEEE 1/x, and their quotient a * (1/b) within 2 ulp of
+    IEEE a/b, over normal operands of every magnitude the state can hold."""
+    lib = abi.load()
+    rng = np.random.default_rng(5)
+    n = 1 << 20
+    b = rng.uniform(1.0, 2.0, n) * 2.0 ** rng.integers(-300, 300, n) * rng.choice([-1.0, 1.0], n)
+    b[:4] = [1.0, 2.0, 0.75, 3.0]
+    a = rng.uniform(1.0, 2.0, n) * 2.0 ** rng.integers(-20, 20, n)
+    out = np.empty(n)
+    assert lib.charm_gpu_math_check(0, n, None, b.ctypes.data, out.ctypes.data) == abi.OK
+    assert _ulps(out, 1.0 / b).max() <= 1.0
+    assert out[0] == 1.0 and out[1] == 0.5
+    assert lib.charm_gpu_math_check(1, n, a.ctypes.data, b.ctypes.data, out.ctypes.data) == abi.OK
+    assert _ulps(out, a / b).max() <= 2.0
