@@ -463,6 +463,7 @@ int charm_gpu_adjoint(charm_gpu_handle_t h, int n_steps, int n_snapshots, const 
     CfgLease lease(h);
     int rc = check_ready(h);
     if (rc) return rc;
+    h->dt_next_valid = false;
     if (n_steps < 1 || n_snapshots < 1) return fail(CHARM_GPU_EINVAL, "n_steps and n_snapshots must be >= 1");
     if (!obj && !dJdu_final) return fail(CHARM_GPU_EINVAL, "adjoint: need an objective or dJ/du at the final state");
     if ((rc = adj_check(h))) return rc;

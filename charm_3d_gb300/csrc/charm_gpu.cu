@@ -101,6 +101,8 @@ struct charm_gpu_handle_s {
     double *d_uc = nullptr;            // stage state after chemistry [V][B][E]
     double *d_chem_rhs = nullptr;      // heat release of the stage [E]
     double *d_dt = nullptr;            // CFL step (bits as unsigned long long)
+    double *d_dt_next = nullptr;       // the next step's CFL step, reduced by the last stage of a step
+    bool dt_next_valid = false;        // d_dt_next holds the CFL step of the current state
     double *d_proj[2] = {nullptr, nullptr};   // adapt projection ping-pong states
     int32_t *d_pmap = nullptr;         // one pass of an adapt plan
     unsigned *d_err = nullptr;
@@ -198,6 +200,7 @@ void reset_mesh(charm_gpu_handle_s *h)
     for (double *q : h->d_snap) cudaFree(q);
     h->d_snap.clear();
     h->adj_valid = false;
+    h->dt_next_valid = false;
     h->n_tiles = 0;
     h->tile_smem = 0;
     h->mesh_ready = false;
@@ -480,7 +483,8 @@ int launch_face(charm_gpu_handle_s *h, const double *u)
 
 template <typename T, int NC>
 int launch_cell(charm_gpu_handle_s *h, const double *u, const double *u0, double *out, double dt,
-                const double *dt_dev, double a_new, double a_old, int mode, const double *radd = nullptr)
+                const double *dt_dev, double a_new, double a_old, int mode, const double *radd = nullptr,
+                double *dt_next = nullptr)
 {
     MeshDev m = mesh_view(h);
     const int bs = 128;
@@ -488,7 +492,8 @@ int launch_cell(charm_gpu_handle_s *h, const double *u, const double *u0, double
     TimedLaunch t;
     begin_launch(h, 1, &t);
     cell_kernel<T, NC><<<(unsigned) nb, bs, 0, h->stream>>>(m, u, static_cast<const T *>(h->d_slots), u0, out, dt,
-                                                            dt_dev, a_new, a_old, mode, h->d_err, radd);
+                                                            dt_dev, a_new, a_old, mode, h->d_err, radd,
+                                                            reinterpret_cast<unsigned long long *>(dt_next), h->cfg.cfl);
     end_launch(h, &t);
     CUDA_TRY(cudaGetLastError());
     return CHARM_GPU_OK;
@@ -496,14 +501,15 @@ int launch_cell(charm_gpu_handle_s *h, const double *u, const double *u0, double
 
 template <int NC>
 int launch_limit(charm_gpu_handle_s *h, const double *ua, const double *u0, double *out, double a_new, double a_old,
-                 double *psi_out = nullptr)
+                 double *psi_out = nullptr, double *dt_next = nullptr)
 {
     MeshDev m = mesh_view(h);
     const int bs = 128;
     const int64_t nb = (h->E + bs - 1) / bs;
     TimedLaunch t;
     begin_launch(h, 2, &t);
-    limit_kernel<NC><<<(unsigned) nb, bs, 0, h->stream>>>(m, ua, u0, out, a_new, a_old, psi_out);
+    limit_kernel<NC><<<(unsigned) nb, bs, 0, h->stream>>>(m, ua, u0, out, a_new, a_old, psi_out,
+                                                          reinterpret_cast<unsigned long long *>(dt_next), h->cfg.cfl);
     end_launch(h, &t);
     CUDA_TRY(cudaGetLastError());
     return CHARM_GPU_OK;
@@ -759,7 +765,7 @@ int launch_vflux(charm_gpu_handle_s *h, const double *u)
 
 template <typename T, int NC>
 int stage(charm_gpu_handle_s *h, const double *u, const double *u0, double *out, double dt, const double *dt_dev,
-          double a_new, double a_old)
+          double a_new, double a_old, double *dt_next = nullptr)
 {
     int rc;
     const double *radd = nullptr;
@@ -784,9 +790,16 @@ int stage(charm_gpu_handle_s *h, const double *u, const double *u0, double *out,
     if (h->cfg.limiter == CHARM_GPU_LIM_BJ) {
         rc = launch_cell<T, NC>(h, u, nullptr, h->d_ua, dt, dt_dev, 1.0, 0.0, kCellUpdate, radd);
         if (rc) return rc;
-        return launch_limit<NC>(h, h->d_ua, u0, out, a_new, a_old);
+        return launch_limit<NC>(h, h->d_ua, u0, out, a_new, a_old, nullptr, dt_next);
     }
-    return launch_cell<T, NC>(h, u, u0, out, dt, dt_dev, a_new, a_old, kCellUpdate, radd);
+    return launch_cell<T, NC>(h, u, u0, out, dt, dt_dev, a_new, a_old, kCellUpdate, radd, dt_next);
+}
+
+// The last stage's kernel also reduces the next step's CFL step (CFL mode,
+// FP64 p1): the reference's get_dt of the state this step ends with.
+bool fused_cfl(const charm_gpu_handle_s *h)
+{
+    return h->cfg.dt_mode == CHARM_GPU_DT_CFL && h->cfg.precision == CHARM_GPU_PREC_FP64 && h->nb != kNB2;
 }
 
 template <typename T, int NC>
@@ -794,22 +807,29 @@ int step_impl(charm_gpu_handle_s *h, double dt, const double *dt_dev)
 {
     int rc;
     const bool lim = h->cfg.limiter == CHARM_GPU_LIM_BJ;
+    double *next = nullptr;
+    if (fused_cfl(h)) {
+        const double start = (h->cfg.tau > 0.0) ? h->cfg.tau : 1.0e300;
+        CUDA_TRY(cudaMemcpyAsync(h->d_dt_next, &start, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        next = h->d_dt_next;
+    }
     if (h->cfg.model == CHARM_GPU_MODEL_EULER) {
-        if (lim) return stage<T, NC>(h, h->d_u, nullptr, h->d_u, dt, dt_dev, 1.0, 0.0);   // cell -> ua, limiter -> u
-        if ((rc = stage<T, NC>(h, h->d_u, nullptr, h->d_ub, dt, dt_dev, 1.0, 0.0))) return rc;
-        std::swap(h->d_u, h->d_ub);
-        return CHARM_GPU_OK;
+        if (lim) rc = stage<T, NC>(h, h->d_u, nullptr, h->d_u, dt, dt_dev, 1.0, 0.0, next);   // cell -> ua, limiter -> u
+        else if (!(rc = stage<T, NC>(h, h->d_u, nullptr, h->d_ub, dt, dt_dev, 1.0, 0.0, next)))
+            std::swap(h->d_u, h->d_ub);
+    } else if (lim) {
+        // SSP-RK3 in the reference's order (charm_model.c:259-266).  A stage
+        // never writes the buffer it reads its residual from.
+        if (!(rc = stage<T, NC>(h, h->d_u, nullptr, h->d_ub, dt, dt_dev, 1.0, 0.0)) &&
+            !(rc = stage<T, NC>(h, h->d_ub, h->d_u, h->d_ub, dt, dt_dev, 0.25, 0.75)))
+            rc = stage<T, NC>(h, h->d_ub, h->d_u, h->d_u, dt, dt_dev, 2.0 / 3.0, 1.0 / 3.0, next);
+    } else {
+        if (!(rc = stage<T, NC>(h, h->d_u, nullptr, h->d_ub, dt, dt_dev, 1.0, 0.0)) &&
+            !(rc = stage<T, NC>(h, h->d_ub, h->d_u, h->d_ua, dt, dt_dev, 0.25, 0.75)))
+            rc = stage<T, NC>(h, h->d_ua, h->d_u, h->d_u, dt, dt_dev, 2.0 / 3.0, 1.0 / 3.0, next);
     }
-    // SSP-RK3 in the reference's order (charm_model.c:259-266).  A stage
-    // never writes the buffer it reads its residual from.
-    if (lim) {
-        if ((rc = stage<T, NC>(h, h->d_u, nullptr, h->d_ub, dt, dt_dev, 1.0, 0.0))) return rc;
-        if ((rc = stage<T, NC>(h, h->d_ub, h->d_u, h->d_ub, dt, dt_dev, 0.25, 0.75))) return rc;
-        return stage<T, NC>(h, h->d_ub, h->d_u, h->d_u, dt, dt_dev, 2.0 / 3.0, 1.0 / 3.0);
-    }
-    if ((rc = stage<T, NC>(h, h->d_u, nullptr, h->d_ub, dt, dt_dev, 1.0, 0.0))) return rc;
-    if ((rc = stage<T, NC>(h, h->d_ub, h->d_u, h->d_ua, dt, dt_dev, 0.25, 0.75))) return rc;
-    return stage<T, NC>(h, h->d_ua, h->d_u, h->d_u, dt, dt_dev, 2.0 / 3.0, 1.0 / 3.0);
+    h->dt_next_valid = (rc == CHARM_GPU_OK) && next;
+    return rc;
 }
 
 // ---- mixed form on FP32 hi/lo planes ---------------------------------------
@@ -1038,8 +1058,16 @@ int check_ready(charm_gpu_handle_s *h)
 int resolve_dt(charm_gpu_handle_s *h, double dt_in, double *dt, const double **dt_dev)
 {
     *dt_dev = nullptr;
-    if (dt_in > 0) { *dt = dt_in; return CHARM_GPU_OK; }
+    if (dt_in > 0) { *dt = dt_in; h->dt_next_valid = false; return CHARM_GPU_OK; }
     if (h->cfg.dt_mode == CHARM_GPU_DT_TAU) { *dt = h->cfg.tau; return CHARM_GPU_OK; }
+    if (h->dt_next_valid) {
+        // reduced by the last stage of the previous step from this state
+        std::swap(h->d_dt, h->d_dt_next);
+        h->dt_next_valid = false;
+        *dt = 0.0;
+        *dt_dev = h->d_dt;
+        return CHARM_GPU_OK;
+    }
     int rc = cfl_dispatch(h);
     if (rc) return rc;
     *dt = 0.0;
@@ -1084,8 +1112,10 @@ int charm_gpu_create(charm_gpu_handle_t *out, const charm_gpu_config_t *cfg, int
         return fail(CHARM_GPU_ECUDA, "cudaStreamCreate failed");
     }
     h->stream = h->own_stream;
-    if (cudaMalloc(&h->d_err, sizeof(unsigned)) != cudaSuccess || cudaMalloc(&h->d_dt, sizeof(double)) != cudaSuccess) {
+    if (cudaMalloc(&h->d_err, sizeof(unsigned)) != cudaSuccess || cudaMalloc(&h->d_dt, sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&h->d_dt_next, sizeof(double)) != cudaSuccess) {
         if (h->d_err) cudaFree(h->d_err);
+        if (h->d_dt) cudaFree(h->d_dt);
         cudaStreamDestroy(h->own_stream);
         delete h;
         return fail(CHARM_GPU_ENOMEM, "cudaMalloc failed");
@@ -1104,6 +1134,7 @@ int charm_gpu_destroy(charm_gpu_handle_t h)
     free_mesh(h);
     if (h->d_err) cudaFree(h->d_err);
     if (h->d_dt) cudaFree(h->d_dt);
+    if (h->d_dt_next) cudaFree(h->d_dt_next);
     for (auto e : h->event_pool) cudaEventDestroy(e);
     {
         // the stream is idle: nothing queued reads c_cfg for this handle
@@ -1418,6 +1449,7 @@ int charm_gpu_adapt_upload(charm_gpu_handle_t h, const charm_gpu_adapt_plan_t *p
     CfgLease lease(h);
     int rc = check_ready(h);
     if (rc) return rc;
+    h->dt_next_valid = false;
     if (!plan || !mesh || (plan->n_pass > 0 && (!plan->n_out || !plan->map))) return fail(CHARM_GPU_EINVAL, "null argument");
     if (h->nb != CHARM_GPU_BASIS) return fail(CHARM_GPU_ENOTSUP, "adapt projection: p1 only");
     if (plan->n_in != h->E) return fail(CHARM_GPU_EINVAL, "adapt plan: input leaves differ from the uploaded mesh");
@@ -1470,6 +1502,7 @@ int charm_gpu_set_state(charm_gpu_handle_t h, const double *u, int on_device)
 {
     if (!h || !u) return fail(CHARM_GPU_EINVAL, "null argument");
     if (!h->mesh_ready) return fail(CHARM_GPU_ESTATE, "no mesh uploaded");
+    h->dt_next_valid = false;
     CUDA_TRY(cudaSetDevice(h->device));
     const size_t st = (size_t) n_var(h) * h->nb * h->E * sizeof(double);
     CUDA_TRY(cudaMemcpyAsync(h->d_u, u, st, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
@@ -1602,6 +1635,7 @@ int charm_gpu_limit(charm_gpu_handle_t h)
     CfgLease lease(h);
     int rc = check_ready(h);
     if (rc) return rc;
+    h->dt_next_valid = false;
     if (h->cfg.limiter != CHARM_GPU_LIM_BJ) return CHARM_GPU_OK;
     const size_t st = (size_t) n_var(h) * h->nb * h->E * sizeof(double);
     const bool mixed = h->cfg.precision == CHARM_GPU_PREC_MIXED;

@@ -281,6 +281,33 @@ face_kernel(MeshDev m, const double *__restrict__ u, T *__restrict__ slots, int6
 }
 
 // ---------------------------------------------------------------------------
+// CFL step of the state a stage kernel has just written (the reference's
+// get_dt formula, src/models/ns/charm_model.c:21-36: CFL * volume / (|u| + c)
+// from the fields at the cell centre, i.e. coefficient 0), folded into
+// *dt_next by a warp reduction and one 64-bit atomicMin per warp (positive
+// doubles order as their bit patterns).  Called by the threads still active
+// in the warp (elements past the end have already left).
+// ---------------------------------------------------------------------------
+template <int NC>
+__device__ __forceinline__ double cell_cfl_dt(const double U[4 + NC], double cfl, double vol)
+{
+    Prim<double, NC> p;
+    cons_to_prim<double, NC>(U, p);
+    const double d = cfl * vol / (sqrt(p.u * p.u + p.v * p.v + p.w * p.w) + p.cz);
+    return (d > 0.0) ? d : 1.0e300;
+}
+
+__device__ __forceinline__ void warp_min_to(double d, unsigned long long *dst)
+{
+    const unsigned mask = __activemask();
+    const unsigned long long b = (unsigned long long) __double_as_longlong(d);
+    const unsigned hi = (unsigned) (b >> 32), lo = (unsigned) b;
+    const unsigned mhi = __reduce_min_sync(mask, hi);
+    const unsigned mlo = __reduce_min_sync(mask, (hi == mhi) ? lo : 0xffffffffu);
+    if ((int) (threadIdx.x & 31) == __ffs(mask) - 1) atomicMin(dst, ((unsigned long long) mhi << 32) | mlo);
+}
+
+// ---------------------------------------------------------------------------
 // cell kernel: volume integral + gather + M^-1 + update
 // ---------------------------------------------------------------------------
 
@@ -292,7 +319,7 @@ template <typename T, int NC>
 __global__ void __launch_bounds__(128)
 cell_kernel(MeshDev m, const double *__restrict__ u, const T *__restrict__ slots, const double *u0,
             double *out, double dt, const double *__restrict__ dt_dev, double a_new, double a_old,
-            int mode, unsigned *err, const double *__restrict__ radd)
+            int mode, unsigned *err, const double *__restrict__ radd, unsigned long long *dt_next, double cfl)
 {
     constexpr int V = 4 + NC;
     const int64_t e = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
@@ -401,6 +428,7 @@ cell_kernel(MeshDev m, const double *__restrict__ u, const T *__restrict__ slots
     const double step = dt_dev ? *dt_dev : dt;
     const double minv0 = 1.0 / vol, minv1 = 12.0 / vol;
     const bool comb = (a_old != 0.0);
+    double cen[V];
 #pragma unroll
     for (int v = 0; v < V; v++) {
 #pragma unroll
@@ -410,8 +438,11 @@ cell_kernel(MeshDev m, const double *__restrict__ u, const T *__restrict__ slots
             double x = cu - step * (R[v][k] * (k == 0 ? minv0 : minv1));
             if (comb) x = a_new * x + a_old * u0[idx];
             out[idx] = x;
+            if (k == 0) cen[v] = x;
         }
     }
+    // last stage of a step in CFL mode: the next step's dt from this state
+    if (dt_next) warp_min_to(cell_cfl_dt<NC>(cen, cfl, vol), dt_next);
 }
 
 // ---------------------------------------------------------------------------
@@ -430,7 +461,7 @@ cell_kernel(MeshDev m, const double *__restrict__ u, const T *__restrict__ slots
 template <int NC>
 __global__ void __launch_bounds__(128)
 limit_kernel(MeshDev m, const double *__restrict__ ua, const double *u0, double *out,
-             double a_new, double a_old, double *__restrict__ psi_out)
+             double a_new, double a_old, double *__restrict__ psi_out, unsigned long long *dt_next, double cfl)
 {
     constexpr int V = 4 + NC;
     const int64_t e = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
@@ -512,6 +543,7 @@ limit_kernel(MeshDev m, const double *__restrict__ ua, const double *u0, double 
         for (int v = 0; v < V; v++) psi_out[(int64_t) v * E + e] = psi[v];
     }
     const bool comb = (a_old != 0.0);
+    double cen[V];
 #pragma unroll
     for (int v = 0; v < V; v++) {
 #pragma unroll
@@ -520,7 +552,14 @@ limit_kernel(MeshDev m, const double *__restrict__ ua, const double *u0, double 
             double x = (k == 0) ? c[v][0] : c[v][k] * psi[v];
             if (comb) x = a_new * x + a_old * u0[idx];
             out[idx] = x;
+            if (k == 0) cen[v] = x;
         }
+    }
+    // last stage of a step in CFL mode: the next step's dt from this state
+    if (dt_next) {
+        const int lev = m.level[e];
+        const double vol = level_h(m, lev, 0) * level_h(m, lev, 1) * level_h(m, lev, 2);
+        warp_min_to(cell_cfl_dt<NC>(cen, cfl, vol), dt_next);
     }
 }
 

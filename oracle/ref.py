@@ -42,6 +42,7 @@ def load(variant: str = "ref") -> C.CDLL:
         lib.ref_grad.argtypes = [C.c_void_p]
         lib.ref_point_flux.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         lib.ref_rim.argtypes = [C.c_int64, C.c_void_p, C.c_void_p]
+        lib.ref_cell_fields.argtypes = [C.c_void_p]
         lib.ref_refine_flags.argtypes = [C.c_void_p, C.c_int]
         lib.ref_refine_flags.restype = C.c_int64
         if variant == "plugin":
@@ -97,6 +98,12 @@ class RefSolver:
         dt = C.c_double()
         self.lib.ref_run(nsteps, C.byref(dt))
         return dt.value
+
+    def cell_fields(self) -> np.ndarray:
+        """[8 + n_comp][E]: R, P, E, E_TOT, U, V, W, T, C_i at the cell centres (the output's fields)."""
+        a = np.empty((8 + self.case.n_comp, self.n_elem))
+        self.lib.ref_cell_fields(a.ctypes.data)
+        return a
 
     def residual(self) -> np.ndarray:
         a = np.empty(self.shape())

@@ -289,6 +289,27 @@ int ref_get_state(double *u)
     return 0;
 }
 
+/* The cell-centre fields the reference's output writes per cell
+ * (charm_interpolate_cell_solution, src/charm_output.c:10-52): the same two
+ * calls, charm_get_fields at the centre and charm_param_cons_to_prim, for
+ * every leaf; out[f * E + e] for R, P, E, E_TOT, U, V, W, T, then C_i. */
+int ref_cell_fields(double *out)
+{
+    int64_t E = charm_shim_count(g_p4est), i;
+    int nc = n_comp(), j;
+    for (i = 0; i < E; i++) {
+        charm_data_t *d = (charm_data_t *) charm_shim_quad(g_p4est, i)->p.user_data;
+        charm_cons_t cons;
+        charm_prim_t prim;
+        charm_get_fields(d, d->par.g.c, &cons);
+        charm_param_cons_to_prim(g_p4est, &prim, &cons);
+        const double f[8] = {prim.r, prim.p, prim.e, prim.e_tot, prim.u, prim.v, prim.w, prim.t};
+        for (j = 0; j < 8; j++) out[j * E + i] = f[j];
+        for (j = 0; j < nc; j++) out[(8 + j) * E + i] = prim.c[j];
+    }
+    return 0;
+}
+
 static void ensure_ghost(void)
 {
     if (!g_ghost) {

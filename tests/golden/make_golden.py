@@ -246,6 +246,24 @@ def mesh_faces() -> dict:
     return {"faces_uniform": uniform, "faces_hanging": ref.faces()}
 
 
+def cell_fields() -> dict:
+    """The reference's output fields (src/charm_output.c:10-52) of the seeded
+    states of three small cases: one species, two species (MIX EOS), the
+    vortex after two steps."""
+    out = {}
+    for key, (kind, steps) in {"random": ("random", 0), "mix2": ("mix2", 0), "vortex": ("vortex", 2)}.items():
+        case = small_case(kind, "HLLC", "NONE", level=2)
+        ref = RefSolver(case)
+        mesh = Forest(case).flatten()
+        u0 = case.initial_state(mesh.center)
+        ref.set_state(u0)
+        if steps:
+            ref.run(steps)
+        out[key + "_u"] = ref.get_state()
+        out[key + "_fields"] = ref.cell_fields()
+    return out
+
+
 def main(names: list[str]) -> None:
     """All fixtures, or only the ones named on the command line."""
     for name in FIXTURES:
@@ -267,6 +285,9 @@ def main(names: list[str]) -> None:
     if not names or "amr_loop_sod" in names:
         np.savez_compressed(os.path.join(HERE, "amr_loop_sod.npz"), **amr_loop())
         print("amr_loop_sod")
+    if not names or "cell_fields" in names:
+        np.savez_compressed(os.path.join(HERE, "cell_fields.npz"), **cell_fields())
+        print("cell_fields")
     if not names or "adjoint_fd_vortex" in names:
         np.savez_compressed(os.path.join(HERE, "adjoint_fd_vortex.npz"), **adjoint_fd())
         print("adjoint_fd_vortex")

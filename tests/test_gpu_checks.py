@@ -91,26 +91,38 @@ def test_cfl_dt_matches_oracle(kind, hanging):
             assert want == tau
 
 
-def test_cfl_step_matches_oracle():
-    """Steps in CFL mode: each step takes the CFL step of its own start state."""
-    case = small_case("random", "HLLC", "NONE", level=3)
+@pytest.mark.parametrize("model,lim", [("NS", "NONE"), ("NS", "BJ"), ("EULER", "NONE"), ("EULER", "BJ")])
+def test_cfl_step_matches_oracle(model, lim):
+    """Steps in CFL mode: each step takes the CFL step of its own start state.
+    The first comes from the CFL kernel, the next ones from the reduction
+    fused into the last stage's cell or limiter kernel of the step before."""
+    case = small_case("random", "HLLC", lim, level=3, model=model)
     case.dt_mode = "CFL"
     case.cfl = 0.05
     case.tau = 1.0
-    mesh = Forest(case).flatten()
+    mesh = hanging_forest(case)[0].flatten()
     u0 = case.initial_state(mesh.center)
     gpu = Solver(case)
     gpu.upload(mesh)
     gpu.set_state(u0)
+    gpu.reset_stats()
     port = Port(case.config(), mesh)
     port.set_state(u0)
-    for _ in range(3):
+    for _ in range(4):
         dt = port.cfl_dt()
         port.step(dt)
         got = gpu.step(0.0)
         assert abs(got - dt) <= 1e-14 * dt
     gpu.sync()
     assert rel_l2(gpu.get_state(), port.get_state()) < 1e-12
+    n, _ = gpu.kernel_stats()
+    assert n[3] == 1      # one CFL kernel launch (the first step); the rest fused
+    # a new state starts over with the CFL kernel
+    gpu.set_state(u0)
+    p0 = Port(case.config(), mesh)
+    p0.set_state(u0)
+    want = p0.cfl_dt()
+    assert abs(gpu.step(0.0) - want) <= 1e-14 * want
 
 
 def test_sync_times_out_while_running_then_completes():

@@ -1,7 +1,11 @@
 """Cell-centre output fields (charm_gpu_cell_fields: the values the
 reference's output writes per cell, src/charm_output.c:10-52) against the
-same primitive-variable formulas in numpy, for both forms and both bases;
-and the VTK file written from them."""
+reference's own values (tests/golden/cell_fields.npz: its charm_get_fields
+and charm_param_cons_to_prim at every leaf centre, one and two species),
+and against the same primitive-variable formulas in numpy for both forms
+and both bases; and the VTK file written from them."""
+import os
+
 import numpy as np
 import pytest
 
@@ -11,6 +15,23 @@ from charm_3d_gb300.solver import Forest, Solver
 from .common import small_case
 
 pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.mark.parametrize("kind", ["random", "mix2", "vortex"])
+def test_cell_fields_match_reference_output(kind):
+    d = np.load(os.path.join(GOLDEN, "cell_fields.npz"))
+    case = small_case(kind, "HLLC", "NONE", level=2)
+    mesh = Forest(case).flatten()
+    g = Solver(case)
+    g.upload(mesh)
+    g.set_state(d[kind + "_u"])
+    f = g.cell_fields()
+    g.close()
+    want = d[kind + "_fields"]
+    assert f.shape == want.shape
+    scale = np.abs(want).max(axis=1, keepdims=True)
+    assert (np.abs(f - want) <= 1e-12 * scale).all(), np.abs(f - want).max(axis=1)
 
 
 @pytest.mark.parametrize("kind,prec,p_order", [("random", "FP64", 1), ("random", "MIXED", 1), ("mix2", "FP64", 1),
