@@ -80,8 +80,10 @@ struct charm_gpu_handle_s {
     void *d_slots = nullptr;           // double or float [V*B][S]
     // mixed form: FP32 hi/lo planes of u, ua, ub ([V][B][E] each)
     float *d_fh[3] = {nullptr, nullptr, nullptr}, *d_fl[3] = {nullptr, nullptr, nullptr};
-    // mixed form, block-local stage: per-tile face lists and element-face slots
-    int32_t *d_tile_fptr = nullptr, *d_tile_faces = nullptr, *d_tile_slot = nullptr;
+    // mixed form, block-local stage: per-tile face records, halo lists and element-face slots
+    int32_t *d_tile_fptr = nullptr, *d_tile_slot = nullptr, *d_tile_hptr = nullptr, *d_tile_halo = nullptr;
+    int4 *d_tile_rec = nullptr;
+    int tile_ncol = 0;
     int64_t n_tiles = 0;
     size_t tile_smem = 0;      // dynamic shared memory of tile_stage_kernel (0: use ff_stage_kernel)
     // discrete adjoint (allocated by the first adjoint call, sized by the mesh)
@@ -220,9 +222,12 @@ void free_mesh(charm_gpu_handle_s *h)
         h->d_fh[k] = h->d_fl[k] = nullptr;
     }
     if (h->d_tile_fptr) cudaFree(h->d_tile_fptr);
-    if (h->d_tile_faces) cudaFree(h->d_tile_faces);
+    if (h->d_tile_rec) cudaFree(h->d_tile_rec);
     if (h->d_tile_slot) cudaFree(h->d_tile_slot);
-    h->d_tile_fptr = h->d_tile_faces = h->d_tile_slot = nullptr;
+    if (h->d_tile_hptr) cudaFree(h->d_tile_hptr);
+    if (h->d_tile_halo) cudaFree(h->d_tile_halo);
+    h->d_tile_fptr = h->d_tile_slot = h->d_tile_hptr = h->d_tile_halo = nullptr;
+    h->d_tile_rec = nullptr;
     double **adj[] = {&h->d_adj_lam, &h->d_adj_s, &h->d_adj_acc, &h->d_adj_u1, &h->d_adj_u2, &h->d_adj_fin,
                       &h->d_adj_psi, &h->d_obj_part, &h->d_adj_psi_all};
     h->n_psi_all = 0;
@@ -900,8 +905,12 @@ int launch_tile_stage(charm_gpu_handle_s *h, int in, int u0, int out, FFCoef dt,
     MeshDev m = mesh_view(h);
     TileDev tl;
     tl.fptr = h->d_tile_fptr;
-    tl.faces = h->d_tile_faces;
+    tl.rec = h->d_tile_rec;
+    tl.hptr = h->d_tile_hptr;
+    tl.halo = h->d_tile_halo;
     tl.slot = h->d_tile_slot;
+    tl.ncol = h->tile_ncol;
+    tl.bulk = (h->E % 4 == 0) ? 1 : 0;
     // the dynamic shared memory limit is a per-device attribute of the kernel
     static int attr_smem[64] = {0};
     const int dev = h->device & 63;
@@ -1269,7 +1278,9 @@ int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh)
         }
         // tiles of kTile consecutive elements: every face touching a tile, in
         // global face order (keeps the 4 records of a mortar consecutive),
-        // and for every element face its position in the tile's list
+        // as records with the shared-memory columns of both sides; the
+        // tile's halo (outside elements that share one of its faces); for
+        // every element face its record position and kind
         const int64_t nt = (E + kTile - 1) / kTile;
         std::vector<int32_t> tcnt(nt + 1, 0);
         for (int64_t i = 0; i < F; i++) {
@@ -1280,7 +1291,7 @@ int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh)
         for (int64_t j = 0; j < Fb; j++) tcnt[mesh->bface_elem[j] / kTile]++;
         std::vector<int32_t> tptr(nt + 1, 0);
         for (int64_t t = 0; t < nt; t++) tptr[t + 1] = tptr[t] + tcnt[t];
-        std::vector<int32_t> tfaces(tptr[nt] > 0 ? tptr[nt] : 1), tslot(6 * E, -1), tfill(tptr.begin(), tptr.end() - 1);
+        std::vector<int32_t> tface(tptr[nt] > 0 ? tptr[nt] : 1), tslot(6 * E, -1), tfill(tptr.begin(), tptr.end() - 1);
         int64_t max_list = 0;
         for (int64_t t = 0; t < nt; t++) max_list = std::max<int64_t>(max_list, tcnt[t]);
         for (int64_t i = 0; i < F; i++) {
@@ -1292,15 +1303,16 @@ int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh)
                 const int64_t t = pass ? tb : ta;
                 if (pass && tb == ta) break;
                 const int32_t p = tfill[t]++;
-                tfaces[p] = (int32_t) (i << 1);
+                tface[p] = (int32_t) i;
                 const int32_t loc = p - tptr[t];
                 for (int side = 0; side < 2; side++) {
                     const int32_t e = side ? b : a;
                     if (e / kTile != t) continue;
                     const int f = side ? 2 * d : 2 * d + 1;
                     const bool big = (kind == 1 && side == 1) || (kind == 2 && side == 0);
-                    if (!big) tslot[(int64_t) f * E + e] = loc;
-                    else if (sub == 0) tslot[(int64_t) f * E + e] = loc;
+                    const bool small = (kind == 1 && side == 0) || (kind == 2 && side == 1);
+                    if (!big) tslot[(int64_t) f * E + e] = (loc << 2) | (small ? 3 : 0);
+                    else if (sub == 0) tslot[(int64_t) f * E + e] = (loc << 2) | 2;
                 }
             }
         }
@@ -1308,23 +1320,69 @@ int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh)
             const int32_t e = mesh->bface_elem[j];
             const int64_t t = e / kTile;
             const int32_t p = tfill[t]++;
-            tfaces[p] = (int32_t) ((j << 1) | 1);
-            tslot[(int64_t) mesh->bface_face[j] * E + e] = p - tptr[t];
+            tface[p] = (int32_t) (F + j);
+            tslot[(int64_t) mesh->bface_face[j] * E + e] = ((p - tptr[t]) << 2) | 1;
         }
         for (int64_t k = 0; k < 6 * E; k++)
             if (tslot[k] < 0) return fail(CHARM_GPU_EINVAL, "element face without a tile face slot");
-        const size_t smem = sizeof(float) * ((size_t) V * CHARM_GPU_BASIS * kTile + (size_t) max_list * 3 * V);
+        // records and halos
+        std::vector<int4> trec(tface.size());
+        std::vector<int32_t> hptr(nt + 1, 0), halo, col(E, -1);
+        std::vector<int64_t> stamp(E, -1);
+        int64_t max_halo = 0;
+        for (int64_t t = 0; t < nt; t++) {
+            const int64_t e0 = t * kTile;
+            auto column = [&](int32_t e) -> int32_t {
+                if (e / kTile == t) return (int32_t) (e - e0);
+                if (stamp[e] != t) {
+                    stamp[e] = t;
+                    col[e] = kTile + (int32_t) (halo.size() - hptr[t]);
+                    halo.push_back(e);
+                }
+                return col[e];
+            };
+            for (int32_t p = tptr[t]; p < tptr[t + 1]; p++) {
+                const int64_t i = tface[p];
+                int4 r;
+                if (i < F) {
+                    const int32_t a = mesh->face_elem[i], b = mesh->face_elem[F + i];
+                    const unsigned info = mesh->face_info[i];
+                    r.x = column(a);
+                    r.y = column(b);
+                    r.z = (int) info;
+                    r.w = mesh->level[(((info >> 2) & 3) == 2) ? b : a];
+                } else {
+                    const int64_t j = i - F;
+                    const int32_t e = mesh->bface_elem[j];
+                    r.x = column(e);
+                    r.y = -1;
+                    r.z = (int) mesh->bface_face[j] | ((int) mesh->bface_bnd[j] << 8) | kRecBoundary;
+                    r.w = mesh->level[e];
+                }
+                trec[p] = r;
+            }
+            hptr[t + 1] = (int32_t) halo.size();
+            max_halo = std::max<int64_t>(max_halo, hptr[t + 1] - hptr[t]);
+        }
+        if (halo.empty()) halo.push_back(0);
+        const int ncol = (int) ((kTile + max_halo + 3) & ~(int64_t) 3);   // 16-byte aligned planes
+        const size_t smem = sizeof(float) * ((size_t) V * CHARM_GPU_BASIS * ncol + (size_t) max_list * 3 * V);
         int max_optin = 0;
         CUDA_TRY(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
         if (smem <= (size_t) max_optin) {
             if ((arc = ensure_buf(h, &h->d_tile_fptr, (nt + 1) * sizeof(int32_t)))) return arc;
-            if ((arc = ensure_buf(h, &h->d_tile_faces, tfaces.size() * sizeof(int32_t)))) return arc;
+            if ((arc = ensure_buf(h, &h->d_tile_rec, trec.size() * sizeof(int4)))) return arc;
             if ((arc = ensure_buf(h, &h->d_tile_slot, (size_t) 6 * E * sizeof(int32_t)))) return arc;
+            if ((arc = ensure_buf(h, &h->d_tile_hptr, (nt + 1) * sizeof(int32_t)))) return arc;
+            if ((arc = ensure_buf(h, &h->d_tile_halo, halo.size() * sizeof(int32_t)))) return arc;
             CUDA_TRY(cudaMemcpy(h->d_tile_fptr, tptr.data(), (nt + 1) * sizeof(int32_t), cudaMemcpyHostToDevice));
-            CUDA_TRY(cudaMemcpy(h->d_tile_faces, tfaces.data(), tfaces.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+            CUDA_TRY(cudaMemcpy(h->d_tile_rec, trec.data(), trec.size() * sizeof(int4), cudaMemcpyHostToDevice));
             CUDA_TRY(cudaMemcpy(h->d_tile_slot, tslot.data(), (size_t) 6 * E * sizeof(int32_t), cudaMemcpyHostToDevice));
+            CUDA_TRY(cudaMemcpy(h->d_tile_hptr, hptr.data(), (nt + 1) * sizeof(int32_t), cudaMemcpyHostToDevice));
+            CUDA_TRY(cudaMemcpy(h->d_tile_halo, halo.data(), halo.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
             h->n_tiles = nt;
             h->tile_smem = smem;
+            h->tile_ncol = ncol;
         }
     }
     CUDA_TRY(cudaMemcpy(h->d_center, mesh->center, 3 * E * sizeof(double), cudaMemcpyHostToDevice));
@@ -1739,6 +1797,7 @@ int charm_gpu_sync(charm_gpu_handle_t h, double timeout_s)
         CUDA_TRY(cudaMemset(h->d_err, 0, sizeof(unsigned)));
         if (err & kErrNonFinite) return fail(CHARM_GPU_ENONFINITE, "non-finite state");
         if (err & kErrNegative) return fail(CHARM_GPU_ENEGATIVE, "non-positive density or pressure");
+        if (err & kErrWait) return fail(CHARM_GPU_ETIMEDOUT, "a bounded device wait (bulk copy) ran out");
         return fail(CHARM_GPU_EHLLC, "HLLC: SL <= S* <= SR violated");
     }
     return CHARM_GPU_OK;

@@ -1189,36 +1189,48 @@ __global__ void __launch_bounds__(128) amr_grad_kernel(MeshDev m, const double *
 
 // ===========================================================================
 // Mixed form, block-local: one CTA per tile of kTile Morton-consecutive
-// elements.  The tile's states are staged in shared memory; every face that
-// touches the tile is evaluated once by the CTA (faces inside the tile once
-// in total, faces on the tile boundary once by each of the two tiles, from
-// identical operands at one code location), its projections (a0, as, at per
-// variable) kept in shared memory; then each thread gathers its element's
-// faces, adds the volume integral and updates u in float-float.
+// elements.  Everything a tile's stage reads is staged in shared memory
+// before any face is evaluated:
+//   - the tile's hi coefficient planes (kTile consecutive floats per plane)
+//     by bulk asynchronous copies (cp.async.bulk, completion on an
+//     mbarrier) issued by one thread;
+//   - the halo: the hi coefficients of every element outside the tile that
+//     shares a face with it (a per-tile list built at upload), loaded by all
+//     threads at once;
+// so the face loop reads no global memory but one 16-byte record per face.
+// Every face that touches the tile is evaluated once by the CTA (faces on
+// the tile boundary once by each of the two tiles, from identical operands
+// at one code location), its projections (a0, as, at per variable) kept in
+// shared memory; then each thread gathers its element's faces, adds the
+// volume integral and updates u in float-float.
 // ===========================================================================
 constexpr int kTile = 128;
 
 struct TileDev {
-    const int32_t *fptr;    // [n_tiles + 1] into faces
-    const int32_t *faces;   // (interior face << 1) | 0, or (boundary face << 1) | 1
-    const int32_t *slot;    // [6][E]: position of the element face in its tile's face list
+    const int32_t *fptr;    // [n_tiles + 1] into rec
+    const int4    *rec;     // one record per (tile, face), see tile_face_rec
+    const int32_t *hptr;    // [n_tiles + 1] into halo
+    const int32_t *halo;    // global element ids of each tile's halo
+    const int32_t *slot;    // [6][E]: (position of the element face in its tile's records << 2) | kind
+                            // (kind: 0 conforming, 1 boundary, 2 big side of a mortar, 3 small side)
+    int ncol;               // shared-memory columns: kTile + the largest halo
+    int bulk;               // 1: the tile planes are 16-byte aligned runs (E % 4 == 0): bulk copies
 };
 
-// Coefficients of element e for the tile starting at e_begin: from shared
-// memory when e is in the tile, else from the global hi plane.
+// Face record (int4), built by the host at upload:
+//   x: shared-memory column of side 0 (interior) or of the element (boundary)
+//   y: column of side 1 (interior), -1 (boundary)
+//   z: interior: the face_info byte; boundary: face id | bnd id << 8 | 1 << 30
+//   w: level of the leaf that owns the quadrature points
+constexpr int kRecBoundary = 1 << 30;
+
 template <int V>
-__device__ __forceinline__ void tile_coef(const float *s_u, const float *__restrict__ uh, int64_t E, int64_t e_begin,
-                                          int64_t e, float c[V][kNB])
+__device__ __forceinline__ void col_coef(const float *s_u, int ncol, int col, float c[V][kNB])
 {
-    const int64_t l = e - e_begin;
-    if (l >= 0 && l < kTile) {
 #pragma unroll
-        for (int v = 0; v < V; v++)
+    for (int v = 0; v < V; v++)
 #pragma unroll
-            for (int k = 0; k < kNB; k++) c[v][k] = s_u[(v * kNB + k) * kTile + l];
-    } else {
-        load_coef_f<V>(uh, E, e, c);
-    }
+        for (int k = 0; k < kNB; k++) c[v][k] = s_u[(v * kNB + k) * ncol + col];
 }
 
 // 6-point sums of one interior (sub-)face along D: S0 = sum q, Ss = sum q*ps,
@@ -1261,21 +1273,19 @@ __device__ __forceinline__ void face_sums(const float cl[4 + NC][kNB], const flo
 }
 
 template <int NC, int FLUX, int D>
-__device__ __forceinline__ void tile_interior(const MeshDev &m, const float *s_u, const float *__restrict__ uh,
-                                              int64_t e_begin, int64_t i, float *out, unsigned *err)
+__device__ __forceinline__ void tile_interior(const MeshDev &m, const float *s_u, int ncol, int4 r, float *out,
+                                              unsigned *err)
 {
     constexpr int V = 4 + NC;
     constexpr int s = (D == 0) ? 1 : 0, t = (D == 2) ? 1 : 2;
-    const int e0 = m.face_elem[i], e1 = m.face_elem[m.n_face + i];
-    const unsigned info = m.face_info[i];
+    const unsigned info = (unsigned) r.z;
     const int kind = (info >> 2) & 3, sub = (info >> 4) & 3;
     float cl[V][kNB], cu[V][kNB];
-    tile_coef<V>(s_u, uh, m.n_elem, e_begin, e0, cl);
-    tile_coef<V>(s_u, uh, m.n_elem, e_begin, e1, cu);
+    col_coef<V>(s_u, ncol, r.x, cl);
+    col_coef<V>(s_u, ncol, r.y, cu);
     float S0[V], Ss[V], St[V];
     face_sums<NC, FLUX, D>(cl, cu, kind, sub, S0, Ss, St, err);
-    const int lev = m.level[(kind == 2) ? e1 : e0];
-    const float w = level_ht<float>(m, lev, s) * level_ht<float>(m, lev, t) * (1.f / 6.f);
+    const float w = level_ht<float>(m, r.w, s) * level_ht<float>(m, r.w, t) * (1.f / 6.f);
 #pragma unroll
     for (int v = 0; v < V; v++) {
         out[v] = w * S0[v];
@@ -1285,15 +1295,15 @@ __device__ __forceinline__ void tile_interior(const MeshDev &m, const float *s_u
 }
 
 template <int NC, int FLUX, int D>
-__device__ __forceinline__ void tile_boundary(const MeshDev &m, const float *s_u, const float *__restrict__ uh,
-                                              int64_t e_begin, int j, float *out, unsigned *err)
+__device__ __forceinline__ void tile_boundary(const MeshDev &m, const float *s_u, int ncol, int4 r, float *out,
+                                              unsigned *err)
 {
     constexpr int V = 4 + NC;
     constexpr int s = (D == 0) ? 1 : 0, t = (D == 2) ? 1 : 2;
-    const int e = m.bface_elem[j], f = m.bface_face[j], bid = m.bface_bnd[j];
+    const int f = r.z & 7, bid = (r.z >> 8) & 0xff;
     const float sg = (f & 1) ? 1.f : -1.f;
     float c[V][kNB];
-    tile_coef<V>(s_u, uh, m.n_elem, e_begin, e, c);
+    col_coef<V>(s_u, ncol, r.x, c);
     float n[3] = {0.f, 0.f, 0.f};
     n[D] = sg;
     float S0[V], Ss[V], St[V];
@@ -1317,8 +1327,7 @@ __device__ __forceinline__ void tile_boundary(const MeshDev &m, const float *s_u
             St[v] += q[v] * pt;
         }
     }
-    const int lev = m.level[e];
-    const float w = level_ht<float>(m, lev, s) * level_ht<float>(m, lev, t) * (1.f / 6.f);
+    const float w = level_ht<float>(m, r.w, s) * level_ht<float>(m, r.w, t) * (1.f / 6.f);
 #pragma unroll
     for (int v = 0; v < V; v++) {
         out[v] = w * S0[v];
@@ -1327,20 +1336,18 @@ __device__ __forceinline__ void tile_boundary(const MeshDev &m, const float *s_u
     }
 }
 
-// Add the projections of element e's two faces along D to R.
+// Add the projections of element e's two faces along D to R (code: the
+// element face's packed slot, position << 2 | kind).
 template <int NC, int D>
-__device__ __forceinline__ void tile_gather_axis(const MeshDev &m, const TileDev &tl, const float *s_f, int64_t e,
-                                                 float R[4 + NC][kNB], float R0l[4 + NC])
+__device__ __forceinline__ void tile_gather_axis(const float *s_f, const int code[6], float R[4 + NC][kNB],
+                                                 float R0l[4 + NC])
 {
     constexpr int V = 4 + NC;
     constexpr int s = (D == 0) ? 1 : 0, t = (D == 2) ? 1 : 2;
-    const int64_t E = m.n_elem;
 #pragma unroll
     for (int side = 0; side < 2; side++) {
-        const int f = 2 * D + side;
-        const int code = m.lim_kind[(int64_t) f * E + e];
-        const int kind = code & 3;
-        const int slot = tl.slot[(int64_t) f * E + e];
+        const int kind = code[2 * D + side] & 3;
+        const int slot = code[2 * D + side] >> 2;
         if (kind == 1) {   // boundary: outward normal sg * e_D
             const float sg = side ? 1.f : -1.f;
             const float *o = s_f + (int64_t) slot * 3 * V;
@@ -1372,58 +1379,133 @@ __device__ __forceinline__ void tile_gather_axis(const MeshDev &m, const TileDev
     }
 }
 
+// ---- bulk asynchronous copies into shared memory (completion on an mbarrier)
+
+__device__ __forceinline__ unsigned smem_addr(const void *p)
+{
+    return (unsigned) __cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+
+// global -> shared, `bytes` a multiple of 16, both addresses 16-byte aligned
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+}
+
+// Wait for phase `parity` of the barrier to complete, at most `tries`
+// polls; false when it did not.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity, unsigned tries)
+{
+    for (unsigned i = 0; i < tries; i++) {
+        unsigned done;
+        asm volatile("{\n\t.reg .pred p;\n\t"
+                     "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(done) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+enum : unsigned { kErrWait = 8u };   // a bounded device wait ran out
+
 template <int NC, int FLUX>
-__global__ void __launch_bounds__(kTile, 5)
+__global__ void __launch_bounds__(kTile, 4)
 tile_stage_kernel(MeshDev m, TileDev tl, const float *__restrict__ uh, const float *__restrict__ ul, const float *u0h,
                   const float *u0l, float *oh, float *ol, float dth, float dtl, const double *__restrict__ dt_dev,
                   float ah, float al, float bh, float bl, int comb, unsigned *err)
 {
     constexpr int V = 4 + NC;
-    extern __shared__ float smem[];
-    float *s_u = smem;                       // [V*4][kTile]
-    float *s_f = smem + V * kNB * kTile;     // [faces][3V]
+    extern __shared__ __align__(128) float smem[];
+    __shared__ uint64_t bar;
+    const int ncol = tl.ncol;
+    float *s_u = smem;                         // [V*4][ncol]: tile columns 0..kTile-1, then the halo
+    float *s_f = smem + V * kNB * ncol;        // [faces][3V]
     const int64_t E = m.n_elem;
     const int64_t e_begin = (int64_t) blockIdx.x * kTile;
     const int nloc = (int) min((int64_t) kTile, E - e_begin);
-    for (int i = threadIdx.x; i < V * kNB * kTile; i += kTile) {
-        const int plane = i / kTile, l = i % kTile;
-        s_u[i] = (l < nloc) ? __ldg(uh + (int64_t) plane * E + e_begin + l) : 0.f;
+    const bool bulk = tl.bulk && (nloc % 4) == 0;
+    // ---- stage: tile planes (bulk copies), halo (all threads) ----
+    if (bulk) {
+        if (threadIdx.x == 0) mbar_init(&bar, 1);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            mbar_expect_tx(&bar, (unsigned) (V * kNB * nloc * sizeof(float)));
+            for (int p = 0; p < V * kNB; p++)
+                bulk_g2s(s_u + p * ncol, uh + (int64_t) p * E + e_begin, (unsigned) (nloc * sizeof(float)), &bar);
+        }
+    } else {
+        for (int i = threadIdx.x; i < V * kNB * kTile; i += kTile) {
+            const int plane = i / kTile, l = i % kTile;
+            if (l < nloc) s_u[plane * ncol + l] = __ldg(uh + (int64_t) plane * E + e_begin + l);
+        }
+    }
+    {
+        const int h0 = tl.hptr[blockIdx.x], nh = tl.hptr[blockIdx.x + 1] - h0;
+        for (int hl = threadIdx.x; hl < nh; hl += kTile) {
+            const int64_t g = __ldg(tl.halo + h0 + hl);
+            float v[V * kNB];
+#pragma unroll
+            for (int p = 0; p < V * kNB; p++) v[p] = __ldg(uh + (int64_t) p * E + g);
+#pragma unroll
+            for (int p = 0; p < V * kNB; p++) s_u[p * ncol + kTile + hl] = v[p];
+        }
+    }
+    // the element's packed face slots, for the gather after the faces
+    int code[6] = {0, 0, 0, 0, 0, 0};
+    const int l = threadIdx.x;
+    const int64_t e = e_begin + l;
+    if (l < nloc) {
+#pragma unroll
+        for (int f = 0; f < 6; f++) code[f] = __ldg(tl.slot + (int64_t) f * E + e);
+    }
+    if (bulk && !mbar_wait(&bar, 0, 1u << 20)) {
+        // the copies did not land: report, wait (bounded) once more so that
+        // none is still writing this CTA's shared memory, and stop
+        if (threadIdx.x == 0) set_error(err, kErrWait);
+        mbar_wait(&bar, 0, 1u << 20);
+        return;
     }
     __syncthreads();
     // ---- faces of the tile ----
     const int f0 = tl.fptr[blockIdx.x], f1 = tl.fptr[blockIdx.x + 1];
     for (int j = f0 + threadIdx.x; j < f1; j += kTile) {
-        const int code = tl.faces[j];
+        const int4 r = __ldg(tl.rec + j);
         float *out = s_f + (int64_t) (j - f0) * 3 * V;
-        if (code & 1) {
-            const int jb = code >> 1;
-            switch (m.bface_face[jb] >> 1) {
-            case 0: tile_boundary<NC, FLUX, 0>(m, s_u, uh, e_begin, jb, out, err); break;
-            case 1: tile_boundary<NC, FLUX, 1>(m, s_u, uh, e_begin, jb, out, err); break;
-            default: tile_boundary<NC, FLUX, 2>(m, s_u, uh, e_begin, jb, out, err); break;
+        if (r.z & kRecBoundary) {
+            switch ((r.z & 7) >> 1) {
+            case 0: tile_boundary<NC, FLUX, 0>(m, s_u, ncol, r, out, err); break;
+            case 1: tile_boundary<NC, FLUX, 1>(m, s_u, ncol, r, out, err); break;
+            default: tile_boundary<NC, FLUX, 2>(m, s_u, ncol, r, out, err); break;
             }
         } else {
-            const int64_t i = code >> 1;
-            switch (m.face_info[i] & 3) {
-            case 0: tile_interior<NC, FLUX, 0>(m, s_u, uh, e_begin, i, out, err); break;
-            case 1: tile_interior<NC, FLUX, 1>(m, s_u, uh, e_begin, i, out, err); break;
-            default: tile_interior<NC, FLUX, 2>(m, s_u, uh, e_begin, i, out, err); break;
+            switch (r.z & 3) {
+            case 0: tile_interior<NC, FLUX, 0>(m, s_u, ncol, r, out, err); break;
+            case 1: tile_interior<NC, FLUX, 1>(m, s_u, ncol, r, out, err); break;
+            default: tile_interior<NC, FLUX, 2>(m, s_u, ncol, r, out, err); break;
             }
         }
     }
     __syncthreads();
-    if ((int) threadIdx.x >= nloc) return;
+    if (l >= nloc) return;
     // ---- element: volume integral, gather, update ----
-    const int l = threadIdx.x;
-    const int64_t e = e_begin + l;
     const int lev = m.level[e];
     const float hx = level_ht<float>(m, lev, 0), hy = level_ht<float>(m, lev, 1), hz = level_ht<float>(m, lev, 2);
     const float vol = hx * hy * hz;
     float c[V][kNB];
-#pragma unroll
-    for (int v = 0; v < V; v++)
-#pragma unroll
-        for (int k = 0; k < kNB; k++) c[v][k] = s_u[(v * kNB + k) * kTile + l];
+    col_coef<V>(s_u, ncol, l, c);
     float R[V][kNB], R0l[V];
 #pragma unroll
     for (int v = 0; v < V; v++) {
@@ -1485,9 +1567,9 @@ tile_stage_kernel(MeshDev m, TileDev tl, const float *__restrict__ uh, const flo
             }
         }
     }
-    tile_gather_axis<NC, 0>(m, tl, s_f, e, R, R0l);
-    tile_gather_axis<NC, 1>(m, tl, s_f, e, R, R0l);
-    tile_gather_axis<NC, 2>(m, tl, s_f, e, R, R0l);
+    tile_gather_axis<NC, 0>(s_f, code, R, R0l);
+    tile_gather_axis<NC, 1>(s_f, code, R, R0l);
+    tile_gather_axis<NC, 2>(s_f, code, R, R0l);
     if (dt_dev) {
         const double d = *dt_dev;
         dth = __double2float_rn(d);
@@ -1499,7 +1581,7 @@ tile_stage_kernel(MeshDev m, TileDev tl, const float *__restrict__ uh, const flo
 #pragma unroll
         for (int k = 0; k < kNB; k++) {
             const int64_t idx = (int64_t) (v * kNB + k) * E + e;
-            FF x = {uh[idx], ul[idx]};
+            FF x = {c[v][k], ul[idx]};
             FF y;
             if (k == 0) {
                 const float rh = __fmul_rn(R[v][0], minv0);
