@@ -915,12 +915,16 @@ int launch_tile_stage(charm_gpu_handle_s *h, int in, int u0, int out, FFCoef dt,
     static int attr_smem[64] = {0};
     const int dev = h->device & 63;
     if ((size_t) attr_smem[dev] < h->tile_smem) {
+        // the largest dynamic size: the opt-in limit less the kernel's static shared memory
         int max_optin = 0;
+        cudaFuncAttributes fa;
         CUDA_TRY(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
-        CUDA_TRY(cudaFuncSetAttribute(tile_stage_kernel<NC, FLUX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      max_optin));
-        attr_smem[dev] = max_optin;
+        CUDA_TRY(cudaFuncGetAttributes(&fa, tile_stage_kernel<NC, FLUX>));
+        const int dyn = max_optin - (int) fa.sharedSizeBytes;
+        CUDA_TRY(cudaFuncSetAttribute(tile_stage_kernel<NC, FLUX>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+        attr_smem[dev] = dyn;
     }
+    if ((size_t) attr_smem[dev] < h->tile_smem) return fail(CHARM_GPU_ENOTSUP, "tile stage: shared memory too small");
     const float *u0h = (u0 >= 0) ? h->d_fh[u0] : nullptr, *u0l = (u0 >= 0) ? h->d_fl[u0] : nullptr;
     TimedLaunch t;
     begin_launch(h, 1, &t);
@@ -1369,7 +1373,7 @@ int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh)
         const size_t smem = sizeof(float) * ((size_t) V * CHARM_GPU_BASIS * ncol + (size_t) max_list * 3 * V);
         int max_optin = 0;
         CUDA_TRY(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
-        if (smem <= (size_t) max_optin) {
+        if (smem + 1024 <= (size_t) max_optin) {   // 1 KB left for the kernel's static shared memory
             if ((arc = ensure_buf(h, &h->d_tile_fptr, (nt + 1) * sizeof(int32_t)))) return arc;
             if ((arc = ensure_buf(h, &h->d_tile_rec, trec.size() * sizeof(int4)))) return arc;
             if ((arc = ensure_buf(h, &h->d_tile_slot, (size_t) 6 * E * sizeof(int32_t)))) return arc;
