@@ -354,6 +354,7 @@ def finish(args, rank, world, device, case, mesh, E, V, state_bytes, t_mesh, val
     adjoint = run_adjoint(args, device) if args.adjoint_steps > 0 else None
     flame = run_flame(args, device) if args.flame_steps > 0 else None
     blast = run_blast(args, device) if args.blast_steps > 0 else None
+    tc = run_tc(args) if args.tc_reps > 0 else None
     n_launch = int(launches.sum())
     # the full records first; the one-line summaries of the extra legs last,
     # where a reader of the end of the line finds them
@@ -361,7 +362,8 @@ def finish(args, rank, world, device, case, mesh, E, V, state_bytes, t_mesh, val
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded isentropic vortex + 1e-3 density noise)",
             "config": bench_config(args, world, E, V, state_bytes, t_mesh),
-            "details": {"mixed": mixed, "adjoint": adjoint, "reacting_ns": flame, "blast_amr": blast},
+            "details": {"mixed": mixed, "adjoint": adjoint, "reacting_ns": flame, "blast_amr": blast,
+                        "p2_contraction": tc},
             "e2e": e2e,
             "roofline": roofline,
             "cpu_baseline": cpu,
@@ -369,7 +371,8 @@ def finish(args, rank, world, device, case, mesh, E, V, state_bytes, t_mesh, val
             "clocks": clk.summary(),
             "parity": parity,
             "mixed": summary_mixed(mixed), "adjoint": summary_adjoint(adjoint),
-            "reacting_ns": summary_flame(flame), "blast_amr": summary_blast(blast)}
+            "reacting_ns": summary_flame(flame), "blast_amr": summary_blast(blast),
+            "p2_contraction": summary_tc(tc)}
 
 
 def bench_config(args, world: int, E: int, V: int, state_bytes: int, t_mesh: float | None) -> dict:
@@ -415,6 +418,13 @@ def summary_flame(f):
         out.update({"mixed_ms_per_step": _r(f["mixed"]["ms_per_step"]), "x_fp64": _r(f["mixed"]["speedup_vs_fp64"]),
                     "rel_l2_density": _r(f["mixed"]["rel_l2_density_vs_fp64"], 3)})
     return out
+
+
+def summary_tc(t):
+    if not t or "tcgen05_over_fma_time" not in t:
+        return None
+    return {"fma_ms": _r(t["fma"]["ms"]), "tcgen05_ms": _r(t["tcgen05"]["ms"]),
+            "max_rel_diff": _r(t["max_rel_diff_values"], 3)}
 
 
 def summary_blast(b):
@@ -711,6 +721,38 @@ def run_blast(args, device: int) -> dict:
     return out
 
 
+def run_tc(args) -> dict:
+    """The p2 basis contraction of config 4 (64^3 = 262,144 elements, 6
+    variables, 10 coefficients at 27 cell Gauss points) on the tensor cores
+    (tcgen05, 3-term BF16 splits, six products, FP32 accumulation) and on
+    FP32 FMAs: time per launch (CUDA events, median of the event-timed
+    repetitions) and the largest difference of the two."""
+    import ctypes as C
+    from charm_3d_gb300 import abi
+    lib = abi.load()
+    E, V = 64 ** 3, 6
+    rng = np.random.default_rng(4)
+    coef = (rng.normal(size=(V, 10, E)) * 0.1 + np.eye(1, 10)[0][None, :, None]).astype(np.float32)
+    out = {"workload": f"p2 basis at the 27 cell Gauss points, {E} elements x {V} variables "
+                       f"(interpolation of the p2 cell stage; reduced to one number per element)"}
+    sums, vals = {}, {}
+    for method, name in ((0, "fma"), (1, "tcgen05")):
+        s = np.empty(E)
+        v = np.empty((E, V, 27), np.float32)
+        ms = C.c_double()
+        rc = lib.charm_gpu_p2_interp(method, E, V, coef.ctypes.data, s.ctypes.data, v.ctypes.data,
+                                     args.tc_reps, C.byref(ms))
+        if rc != 0:
+            out[name] = {"error": lib.charm_gpu_last_error().decode()}
+            continue
+        sums[name], vals[name] = s, v
+        out[name] = {"ms": ms.value, "elements_per_s": E / (ms.value * 1e-3)}
+    if len(vals) == 2:
+        out["tcgen05_over_fma_time"] = out["tcgen05"]["ms"] / out["fma"]["ms"]
+        out["max_rel_diff_values"] = float(np.abs(vals["tcgen05"] - vals["fma"]).max() / np.abs(vals["fma"]).max())
+    return out
+
+
 def probe(abi, device: int, which: int) -> float | None:
     import ctypes as C
     lib = abi.load()
@@ -769,7 +811,7 @@ def main():
     ap.add_argument("--parity-steps", type=int, default=20,
                     help="oracle steps on the level --cpu-level sample (cpu_baseline and parity; 0 skips both)")
     ap.add_argument("--brick", type=int, default=1, help="trees along x (profiling sizes)")
-    ap.add_argument("--only", default="both", choices=["both", "fp64", "mixed", "adjoint", "flame", "blast"])
+    ap.add_argument("--only", default="both", choices=["both", "fp64", "mixed", "adjoint", "flame", "blast", "tc"])
     ap.add_argument("--blast-steps", type=int, default=200, help="0 skips the AMR blast leg")
     ap.add_argument("--flame-level", type=int, default=6)
     ap.add_argument("--flame-order", type=int, default=2, choices=[1, 2], help="basis order of the reacting leg")
@@ -783,6 +825,7 @@ def main():
     ap.add_argument("--adjoint-revolve-snapshots", type=int, default=20,
                     help="checkpoints of the memory-bounded adjoint timing (0 skips it)")
     ap.add_argument("--adjoint-fd-eps", type=float, default=1e-6, help="central-difference step")
+    ap.add_argument("--tc-reps", type=int, default=20, help="timed launches of the p2 contraction leg (0 skips it)")
     ap.add_argument("--skip-e2e", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -815,6 +858,10 @@ def main():
     if args.only == "blast":
         if rank == 0:
             print(json.dumps({"only": "blast", "blast_amr": run_blast(args, local)}))
+        return
+    if args.only == "tc":
+        if rank == 0:
+            print(json.dumps({"only": "tc", "p2_contraction": run_tc(args)}))
         return
     if args.only == "flame":
         if rank == 0:

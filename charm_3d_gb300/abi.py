@@ -137,6 +137,7 @@ SIGNATURES = [
     ("charm_gpu_residual_static", C.c_int, [C.POINTER(Config), C.POINTER(Mesh), _P, _P, _P]),
     ("charm_gpu_point_flux", C.c_int, [C.POINTER(Config), C.c_int64, _P, _P, _P]),
     ("charm_gpu_math_check", C.c_int, [C.c_int, C.c_int64, _P, _P, _P]),
+    ("charm_gpu_p2_interp", C.c_int, [C.c_int, C.c_int64, C.c_int, _P, _P, _P, C.c_int, _DP]),
     ("charm_gpu_dims", C.c_int, [_P, _I64P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("charm_gpu_objective", C.c_int, [_P, C.POINTER(Objective), _DP, _P]),
     ("charm_gpu_residual_adjoint", C.c_int, [_P, _P, _P]),

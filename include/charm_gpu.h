@@ -275,6 +275,19 @@ int charm_gpu_point_flux(const charm_gpu_config_t *cfg, int64_t n, const double 
  * the kernels form it.  Allocates and synchronises. */
 int charm_gpu_math_check(int which, int64_t n, const double *a, const double *b, double *out);
 
+/* The p2 basis contraction (values of n_var = 5 or 6 variables' 10 Taylor
+ * coefficients at the 27 cell Gauss points, the first step of every p2 cell
+ * stage; reference src/charm_base_func.c:139-196) as a measurement entry with
+ * no counterpart in the reference: method 0 on FP32 FMAs, method 1 on the
+ * tensor cores (tcgen05.mma, BF16 operands split in three terms each, six
+ * products, FP32 accumulation in tensor memory).  coef: host float
+ * [n_var][10][E]; sum[e] = sum_q w_q sum_v U_v(q)^2 (host double [E]);
+ * vals (optional) the values, host float [E][n_var][27].  The kernel runs
+ * once, then `reps` times timed with CUDA events: *ms is the time of one
+ * launch.  Allocates and synchronises. */
+int charm_gpu_p2_interp(int method, int64_t E, int n_var, const float *coef, double *sum, float *vals, int reps,
+                        double *ms);
+
 /* Element count, variables and basis size of the uploaded mesh. */
 int charm_gpu_dims(charm_gpu_handle_t h, int64_t *n_elem, int *n_var, int *n_basis);
 
