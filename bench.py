@@ -508,7 +508,15 @@ def run_adjoint(args, device: int) -> dict:
     # face points across HLLC's case switches, where a difference quotient
     # mixes the two one-sided derivatives; that part of the error shrinks
     # with the step, down to the round-off of J
-    def fd_err(d, h):
+    # besides the relative error of each directional derivative, its size
+    # and the error normalised by |dJ/du restricted to the perturbed
+    # coefficients| * |d| (Cauchy-Schwarz bound of the derivative): a
+    # direction nearly orthogonal to the gradient has a small derivative, and
+    # the round-off of J / eps then dominates its relative error
+    gsub = grad[4, 0]
+    fd_abs, fd_norm = {}, {}
+
+    def fd_err(d, h, key=None):
         ad = float((grad * d).sum())
         Js = []
         for sgn in (1.0, -1.0):
@@ -516,13 +524,17 @@ def run_adjoint(args, device: int) -> dict:
             gpu.run(n, case.tau)
             Js.append(gpu.objective(obj))
         fd = (Js[0] - Js[1]) / (2 * h)
+        if key is not None:
+            fd_abs.setdefault(key, []).append(float(f"{abs(fd):.3g}"))
+            fd_norm.setdefault(key, []).append(
+                float(f"{abs(ad - fd) / (np.linalg.norm(gsub) * np.linalg.norm(d[4, 0])):.3g}"))
         return abs(ad - fd) / max(abs(fd), 1e-300)
 
     errs, errs10 = [], []
     for k in range(args.adjoint_fd):
         d = np.zeros_like(u0)
         d[4, 0] = rng.uniform(-1.0, 1.0, mesh.n_elem)
-        errs.append(fd_err(d, eps))
+        errs.append(fd_err(d, eps, "white"))
         if k < 4:
             errs10.append(fd_err(d, 0.1 * eps))
     # smooth random directions: a few random Fourier modes of the element
@@ -538,7 +550,7 @@ def run_adjoint(args, device: int) -> dict:
             ph = rng.uniform(0, 2 * np.pi)
             field += rng.uniform(-1, 1) * np.sin(2 * np.pi * (kv @ mesh.center) / L + ph)
         d[4, 0] = field
-        errs_s.append(fd_err(d, eps))
+        errs_s.append(fd_err(d, eps, "smooth"))
     gpu.close()
     return {"workload": f"vortex level {args.adjoint_level} ({mesh.n_elem} hex), HLLC, no limiter, FP64, "
                         f"J = integral of p over [{args.adjoint_box}]^3 at step {n}",
@@ -551,6 +563,8 @@ def run_adjoint(args, device: int) -> dict:
             "fd_check": {"directions": args.adjoint_fd, "eps": eps, "max_rel_err": max(errs) if errs else None,
                          "median_rel_err": float(np.median(errs)) if errs else None,
                          "per_direction": [float(f"{x:.3g}") for x in errs],
+                         "abs_fd_per_direction": fd_abs.get("white"),
+                         "err_over_gradnorm_times_dnorm": fd_norm.get("white"),
                          "eps_over_10": {"eps": 0.1 * eps, "directions": len(errs10),
                                          "per_direction": [float(f"{x:.3g}") for x in errs10]},
                          "direction": "uniform(-1, 1) on the density mean of every element (the seeded "
@@ -559,6 +573,8 @@ def run_adjoint(args, device: int) -> dict:
                                     "max_rel_err": max(errs_s) if errs_s else None,
                                     "median_rel_err": float(np.median(errs_s)) if errs_s else None,
                                     "per_direction": [float(f"{x:.3g}") for x in errs_s],
+                                    "abs_fd_per_direction": fd_abs.get("smooth"),
+                                    "err_over_gradnorm_times_dnorm": fd_norm.get("smooth"),
                                     "direction": "sum of 3 random Fourier modes (wave numbers 1..3 per axis, "
                                                  "random phase and amplitude) on the density mean"}}}
 
