@@ -157,6 +157,7 @@ template <typename T, int NC>
 struct Prim {
     T r, u, v, w, e, e_tot, p, t, cz, gam, cp, cv, m;
     T ir;        // 1 / r (the HLLC shock factors use it)
+    T re;        // r * e_tot, the conserved total energy
     T c[NC];
 };
 
@@ -283,6 +284,7 @@ __device__ __forceinline__ void cons_to_prim(const T *U, Prim<T, NC> &p)
     p.u = U[0] * ir;
     p.v = U[1] * ir;
     p.w = U[2] * ir;
+    p.re = U[3];
     p.e_tot = U[3] * ir;
     p.e = p.e_tot - T(0.5) * (p.u * p.u + p.v * p.v + p.w * p.w);
     for (int i = 0; i < NC; i++) p.c[i] = clamp01<T>(U[4 + i] * ir);
@@ -292,7 +294,9 @@ __device__ __forceinline__ void cons_to_prim(const T *U, Prim<T, NC> &p)
         // with 1/r, gam - 1 and 1/cv reused instead of computed again
         p.cp = cfgv<T>(c_cfg.ideal_cp, c_cfg.ideal_cp_f); p.m = cfgv<T>(c_cfg.ideal_m, c_cfg.ideal_m_f);
         p.cv = cfgv<T>(c_cfg.ideal_cv, c_cfg.ideal_cv_f); p.gam = cfgv<T>(c_cfg.ideal_gam, c_cfg.ideal_gam_f);
-        p.p = r * p.e * cfgv<T>(c_cfg.ideal_gm1, c_cfg.ideal_gm1_f);
+        // p = (gam - 1) r e = (gam - 1) (r e_tot - (r u.u) / 2), from the
+        // conserved values (e itself is left to the callers that use it)
+        p.p = cfgv<T>(c_cfg.ideal_gm1, c_cfg.ideal_gm1_f) * (U[3] - T(0.5) * (U[0] * p.u + U[1] * p.v + U[2] * p.w));
         p.cz = qsqrt<T>(p.gam * p.p * ir);
         p.t = p.e * cfgv<T>(c_cfg.ideal_inv_cv, c_cfg.ideal_inv_cv_f);
         return;
@@ -370,6 +374,7 @@ __device__ void bnd_cond(int bid, const Prim<T, NC> &in, Prim<T, NC> &out, const
 #undef par
     eos<T, NC>(out, 3);
     out.e_tot = out.e + T(0.5) * (out.u * out.u + out.v * out.v + out.w * out.w);
+    out.re = out.r * out.e_tot;
 }
 
 // ---- numerical fluxes (reference src/charm_fluxes.c) --------------------
@@ -406,7 +411,7 @@ __device__ __forceinline__ void flux_lf(const Prim<T, NC> &a, const Prim<T, NC> 
     q[0] = ha * ((b.r * vnb * b.u + pn<AX, T>(b.p, n, 0)) + (a.r * vna * a.u + pn<AX, T>(a.p, n, 0)) - alpha * (b.r * b.u - a.r * a.u));
     q[1] = ha * ((b.r * vnb * b.v + pn<AX, T>(b.p, n, 1)) + (a.r * vna * a.v + pn<AX, T>(a.p, n, 1)) - alpha * (b.r * b.v - a.r * a.v));
     q[2] = ha * ((b.r * vnb * b.w + pn<AX, T>(b.p, n, 2)) + (a.r * vna * a.w + pn<AX, T>(a.p, n, 2)) - alpha * (b.r * b.w - a.r * a.w));
-    q[3] = ha * (((b.r * b.e_tot + b.p) * vnb) + ((a.r * a.e_tot + a.p) * vna) - alpha * (b.r * b.e_tot - a.r * a.e_tot));
+    q[3] = ha * (((b.re + b.p) * vnb) + ((a.re + a.p) * vna) - alpha * (b.re - a.re));
     for (int i = 0; i < NC; i++)
         q[4 + i] = ha * ((b.r * vnb * b.c[i]) + (a.r * vna * a.c[i]) - alpha * (b.r * b.c[i] - a.r * a.c[i]));
 }
@@ -421,7 +426,7 @@ __device__ __forceinline__ void flux_cd(const Prim<T, NC> &a, const Prim<T, NC> 
     q[0] = ha * ((b.r * vnb * b.u + pn<AX, T>(b.p, n, 0)) + (a.r * vna * a.u + pn<AX, T>(a.p, n, 0)));
     q[1] = ha * ((b.r * vnb * b.v + pn<AX, T>(b.p, n, 1)) + (a.r * vna * a.v + pn<AX, T>(a.p, n, 1)));
     q[2] = ha * ((b.r * vnb * b.w + pn<AX, T>(b.p, n, 2)) + (a.r * vna * a.w + pn<AX, T>(a.p, n, 2)));
-    q[3] = ha * (((b.r * b.e_tot + b.p) * vnb) + ((a.r * a.e_tot + a.p) * vna));
+    q[3] = ha * (((b.re + b.p) * vnb) + ((a.re + a.p) * vna));
     for (int i = 0; i < NC; i++) q[4 + i] = ha * ((b.r * b.c[i] * vnb) + (a.r * a.c[i] * vna));
 }
 
@@ -448,18 +453,6 @@ __device__ __forceinline__ void normal_frame(const T n[3], T nt[3][3])
     nt[2][1] = -nt[0][0] * nt[1][2] + nt[0][2] * nt[1][0];
     nt[2][2] = nt[0][0] * nt[1][1] - nt[0][1] * nt[1][0];
 }
-
-// F_HLLC_U / F_HLLC_V / F_HLLC_E (:319-321), with the common divisor
-// 1/(SK - SS) computed once per star state (inv).
-template <typename T>
-__device__ __forceinline__ T f_hllc_u(T uk, T fk, T sk, T ss, T pk, T rk, T vk, T inv)
-{ return ((ss) * ((sk) * (uk) - (fk)) + (sk) * ((pk) + (rk) * ((sk) - (vk)) * ((ss) - (vk)))) * inv; }
-template <typename T>
-__device__ __forceinline__ T f_hllc_v(T uk, T fk, T sk, T ss, T inv)
-{ return ((ss) * ((sk) * (uk) - (fk))) * inv; }
-template <typename T>
-__device__ __forceinline__ T f_hllc_e(T uk, T fk, T sk, T ss, T pk, T rk, T vk, T inv)
-{ return ((ss) * ((sk) * (uk) - (fk)) + (sk) * ((pk) + (rk) * ((sk) - (vk)) * ((ss) - (vk))) * (ss)) * inv; }
 
 // _charm_calc_flux_hllc_x_1 (:324-437) on states already in the normal frame
 // (u is the normal velocity), then rotated back (:505-509).
@@ -537,21 +530,24 @@ __device__ void flux_hllc(const Prim<T, NC> &pa, const Prim<T, NC> &pb, const T 
     const bool ka = (sl >= T(0)) || (!(sr <= T(0)) && (s_star >= T(0)));
     const bool star = !(sl >= T(0)) && !(sr <= T(0));
     const T rk = ka ? pa.r : pb.r, uk = ka ? ua : ub, vk = ka ? va : vb, wk = ka ? wa : wb;
-    const T pk = ka ? pa.p : pb.p, ek = ka ? pa.e_tot : pb.e_tot, sk = ka ? sl : sr;
-    const T fu_k = rk * uk * uk + pk, fv_k = rk * vk * uk, fw_k = rk * wk * uk, fe_k = (rk * ek + pk) * uk;
+    const T pk = ka ? pa.p : pb.p, rek = ka ? pa.re : pb.re, sk = ka ? sl : sr;
     if (star) {
-        const T inv = qrcp<T>(sk - s_star);
-        fu = f_hllc_u<T>(rk * uk, fu_k, sk, s_star, pk, rk, uk, inv);
-        fv = f_hllc_v<T>(rk * vk, rk * uk * vk, sk, s_star, inv);
-        fw = f_hllc_v<T>(rk * wk, rk * uk * wk, sk, s_star, inv);
-        q[3] = f_hllc_e<T>(rk * ek, fe_k, sk, s_star, pk, rk, uk, inv);
-        for (int i = 0; i < NC; i++) {
-            const T ck = ka ? pa.c[i] : pb.c[i];
-            q[4 + i] = f_hllc_v<T>(rk * ck, rk * ck * uk, sk, s_star, inv);
-        }
+        // F_HLLC_U/V/E (:319-321) with their common factors taken out: with
+        // Q = s* (sk - uk) / (sk - s*) and M = rk Q (the star state's mass
+        // flux),  F_V(rk vk) = M vk,  F_U = M sk - rk uk (sk - uk) + pk,
+        // F_E = Q (rk ek + pk + sk rk (s* - uk))  -- the same expressions
+        // expanded, with fewer products
+        const T Q = s_star * (sk - uk) * qrcp<T>(sk - s_star);
+        const T M = rk * Q;
+        fu = M * sk - rk * uk * (sk - uk) + pk;
+        fv = M * vk;
+        fw = M * wk;
+        q[3] = Q * (rek + pk + sk * rk * (s_star - uk));
+        for (int i = 0; i < NC; i++) q[4 + i] = M * (ka ? pa.c[i] : pb.c[i]);
     } else {
-        fu = fu_k; fv = fv_k; fw = fw_k; q[3] = fe_k;
-        for (int i = 0; i < NC; i++) q[4 + i] = rk * uk * (ka ? pa.c[i] : pb.c[i]);
+        const T mk = rk * uk;
+        fu = mk * uk + pk; fv = mk * vk; fw = mk * wk; q[3] = (rek + pk) * uk;
+        for (int i = 0; i < NC; i++) q[4 + i] = mk * (ka ? pa.c[i] : pb.c[i]);
     }
     frame_out<AX, T>(nt, sn, fu, fv, fw, q);
 }

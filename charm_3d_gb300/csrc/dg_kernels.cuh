@@ -356,9 +356,10 @@ cell_kernel(MeshDev m, const double *__restrict__ u, const T *__restrict__ slots
         cons_to_prim<T, NC>(U, p);
         if (!(p.r > T(0)) || !(p.p > T(0))) set_error(err, isfinite((double) p.r) && isfinite((double) p.p) ? kErrNegative : kErrNonFinite);
         // Euler fluxes (src/models/ns/charm_model_ns_conv.c:45-65)
-        F[0] += U[0] * p.u + p.p; F[1] += U[0] * p.v; F[2] += U[0] * p.w; F[3] += U[0] * p.e_tot + p.p * p.u;
-        G[0] += U[1] * p.u; G[1] += U[1] * p.v + p.p; G[2] += U[1] * p.w; G[3] += U[1] * p.e_tot + p.p * p.v;
-        H[0] += U[2] * p.u; H[1] += U[2] * p.v; H[2] += U[2] * p.w + p.p; H[3] += U[2] * p.e_tot + p.p * p.w;
+        const auto hp = U[3] + p.p;   // r e_tot + p: the energy fluxes are u hp, v hp, w hp
+        F[0] += U[0] * p.u + p.p; F[1] += U[0] * p.v; F[2] += U[0] * p.w; F[3] += p.u * hp;
+        G[0] += U[1] * p.u; G[1] += U[1] * p.v + p.p; G[2] += U[1] * p.w; G[3] += p.v * hp;
+        H[0] += U[2] * p.u; H[1] += U[2] * p.v; H[2] += U[2] * p.w + p.p; H[3] += p.w * hp;
 #pragma unroll
         for (int i = 0; i < NC; i++) {
             F[4 + i] += U[0] * p.c[i];
@@ -921,9 +922,10 @@ ff_stage_kernel(MeshDev m, const float *__restrict__ uh, const float *__restrict
             Prim<float, NC> p;
             cons_to_prim<float, NC>(U, p);
             if (!(p.r > 0.f) || !(p.p > 0.f)) set_error(err, (isfinite(p.r) && isfinite(p.p)) ? kErrNegative : kErrNonFinite);
-            F[0] += U[0] * p.u + p.p; F[1] += U[0] * p.v; F[2] += U[0] * p.w; F[3] += U[0] * p.e_tot + p.p * p.u;
-            G[0] += U[1] * p.u; G[1] += U[1] * p.v + p.p; G[2] += U[1] * p.w; G[3] += U[1] * p.e_tot + p.p * p.v;
-            H[0] += U[2] * p.u; H[1] += U[2] * p.v; H[2] += U[2] * p.w + p.p; H[3] += U[2] * p.e_tot + p.p * p.w;
+            const auto hp = U[3] + p.p;   // r e_tot + p: the energy fluxes are u hp, v hp, w hp
+            F[0] += U[0] * p.u + p.p; F[1] += U[0] * p.v; F[2] += U[0] * p.w; F[3] += p.u * hp;
+            G[0] += U[1] * p.u; G[1] += U[1] * p.v + p.p; G[2] += U[1] * p.w; G[3] += p.v * hp;
+            H[0] += U[2] * p.u; H[1] += U[2] * p.v; H[2] += U[2] * p.w + p.p; H[3] += p.w * hp;
 #pragma unroll
             for (int i = 0; i < NC; i++) {
                 F[4 + i] += U[0] * p.c[i];
@@ -1534,9 +1536,10 @@ tile_stage_kernel(MeshDev m, TileDev tl, const float *__restrict__ uh, const flo
             Prim<float, NC> p;
             cons_to_prim<float, NC>(U, p);
             if (!(p.r > 0.f) || !(p.p > 0.f)) set_error(err, (isfinite(p.r) && isfinite(p.p)) ? kErrNegative : kErrNonFinite);
-            F[0] += U[0] * p.u + p.p; F[1] += U[0] * p.v; F[2] += U[0] * p.w; F[3] += U[0] * p.e_tot + p.p * p.u;
-            G[0] += U[1] * p.u; G[1] += U[1] * p.v + p.p; G[2] += U[1] * p.w; G[3] += U[1] * p.e_tot + p.p * p.v;
-            H[0] += U[2] * p.u; H[1] += U[2] * p.v; H[2] += U[2] * p.w + p.p; H[3] += U[2] * p.e_tot + p.p * p.w;
+            const auto hp = U[3] + p.p;   // r e_tot + p: the energy fluxes are u hp, v hp, w hp
+            F[0] += U[0] * p.u + p.p; F[1] += U[0] * p.v; F[2] += U[0] * p.w; F[3] += p.u * hp;
+            G[0] += U[1] * p.u; G[1] += U[1] * p.v + p.p; G[2] += U[1] * p.w; G[3] += p.v * hp;
+            H[0] += U[2] * p.u; H[1] += U[2] * p.v; H[2] += U[2] * p.w + p.p; H[3] += p.w * hp;
 #pragma unroll
             for (int i = 0; i < NC; i++) {
                 F[4 + i] += U[0] * p.c[i];

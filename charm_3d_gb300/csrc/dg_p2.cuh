@@ -402,9 +402,10 @@ p2_cell_kernel(MeshDev m, const T *__restrict__ u, const T *__restrict__ slots, 
         cons_to_prim<T, NC>(U, p);
         if (!(p.r > T(0)) || !(p.p > T(0))) set_error(err, isfinite(p.r) && isfinite(p.p) ? kErrNegative : kErrNonFinite);
         T F[V], G[V], H[V];
-        F[0] = U[0] * p.u + p.p; F[1] = U[0] * p.v; F[2] = U[0] * p.w; F[3] = U[0] * p.e_tot + p.p * p.u;
-        G[0] = U[1] * p.u; G[1] = U[1] * p.v + p.p; G[2] = U[1] * p.w; G[3] = U[1] * p.e_tot + p.p * p.v;
-        H[0] = U[2] * p.u; H[1] = U[2] * p.v; H[2] = U[2] * p.w + p.p; H[3] = U[2] * p.e_tot + p.p * p.w;
+        const T hp = U[3] + p.p;   // r e_tot + p: the energy fluxes are u hp, v hp, w hp
+        F[0] = U[0] * p.u + p.p; F[1] = U[0] * p.v; F[2] = U[0] * p.w; F[3] = p.u * hp;
+        G[0] = U[1] * p.u; G[1] = U[1] * p.v + p.p; G[2] = U[1] * p.w; G[3] = p.v * hp;
+        H[0] = U[2] * p.u; H[1] = U[2] * p.v; H[2] = U[2] * p.w + p.p; H[3] = p.w * hp;
 #pragma unroll
         for (int k = 0; k < NC; k++) { F[4 + k] = U[0] * p.c[k]; G[4 + k] = U[1] * p.c[k]; H[4 + k] = U[2] * p.c[k]; }
         const T w = vol * p2_cw<T>(g);
