@@ -221,6 +221,23 @@ def run_gpu(args, rank: int, world: int, device: int) -> dict | None:
 
     if args.only == "mixed":
         return run_mixed_only(args, case, mesh, u0, device, world)
+    if args.only == "dw":
+        case.precision = "DW"
+        g = Solver(case, device)
+        g.upload(mesh)
+        g.set_state(u0)
+        g.run(args.warmup, case.tau)
+        g.sync()
+        g.set_state(u0)
+        g.reset_stats()
+        g.set_timing(True)
+        msd = g.time_run(args.steps, case.tau)
+        g.set_timing(False)
+        n_l, k_ms = g.kernel_stats()
+        g.close()
+        print(json.dumps({"only": "dw", "ms_per_step": msd / args.steps, "kernel_ms": k_ms.tolist(),
+                          "launches": n_l.tolist()}))
+        return None
     # ---- plain FP64 (drop-in) ----
     case.precision = "FP64"
     gpu = Solver(case, device)
@@ -269,12 +286,37 @@ def run_gpu(args, rank: int, world: int, device: int) -> dict | None:
              "dtype": "f32 residual, f32 hi/lo state pairs (float-float update), f64 dt"}
     g32.close()
 
+    # ---- double-word form (FP64 state, FP32-pair residual) on the same steps ----
+    dwf = None
+    if not args.skip_dw:
+        case.precision = "DW"
+        gdw = Solver(case, device)
+        gdw.upload(mesh)
+        gdw.set_state(u0)
+        gdw.run(args.warmup, case.tau)
+        gdw.sync()
+        gdw.set_state(u0)
+        gdw.reset_stats()
+        gdw.set_timing(True)
+        barrier(world)
+        msdw = max_over_ranks(gdw.time_run(args.steps, case.tau), world)
+        gdw.set_timing(False)
+        _, kdw = gdw.kernel_stats()
+        udw = gdw.get_state()
+        gdw.close()
+        dwf = {"value": dof_per_step(E, V) * args.steps * world / (msdw * 1e-3), "unit": UNIT,
+               "ms_per_step": msdw / args.steps, "speedup_vs_fp64": ms / msdw,
+               "rel_l2_state_vs_fp64": float(np.linalg.norm(udw - u64) / np.linalg.norm(u64)),
+               "kernel_ms_face_cell": [float(kdw[0]), float(kdw[1])],
+               "dtype": "f64 state; fluxes and volume terms in double-word f32 pairs (~48-bit)"}
+        case.precision = "FP64"
+
     # ---- e2e through the C ABI with host buffers ----
     if args.skip_e2e:
         e2e = None
         gpu.close()
         return finish(args, rank, world, device, case, mesh, E, V, state_bytes, t_mesh, value, ms, launches, kms,
-                      mixed, e2e, clk)
+                      mixed, e2e, clk, dwf)
     import torch
     pin_in = torch.empty(u0.shape, dtype=torch.float64, pin_memory=True).numpy()
     pin_out = torch.empty(u0.shape, dtype=torch.float64, pin_memory=True).numpy()
@@ -295,7 +337,7 @@ def run_gpu(args, rank: int, world: int, device: int) -> dict | None:
            "path": "charm_gpu_set_state(host) + charm_gpu_step + charm_gpu_get_state(host), pinned buffers"}
     gpu.close()
     return finish(args, rank, world, device, case, mesh, E, V, state_bytes, t_mesh, value, ms, launches, kms, mixed,
-                  e2e, clk)
+                  e2e, clk, dwf)
 
 
 def run_mixed_only(args, case, mesh, u0, device, world):
@@ -319,7 +361,7 @@ def run_mixed_only(args, case, mesh, u0, device, world):
 
 
 def finish(args, rank, world, device, case, mesh, E, V, state_bytes, t_mesh, value, ms, launches, kms, mixed, e2e,
-           clk):
+           clk, dwf=None):
     from charm_3d_gb300 import abi
     if rank != 0:
         return None
@@ -362,15 +404,15 @@ def finish(args, rank, world, device, case, mesh, E, V, state_bytes, t_mesh, val
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded isentropic vortex + 1e-3 density noise)",
             "config": bench_config(args, world, E, V, state_bytes, t_mesh),
-            "details": {"mixed": mixed, "adjoint": adjoint, "reacting_ns": flame, "blast_amr": blast,
-                        "p2_contraction": tc},
+            "details": {"mixed": mixed, "double_word": dwf, "adjoint": adjoint, "reacting_ns": flame,
+                        "blast_amr": blast, "p2_contraction": tc},
             "e2e": e2e,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "gpu_launches": n_launch,
             "clocks": clk.summary(),
             "parity": parity,
-            "mixed": summary_mixed(mixed), "adjoint": summary_adjoint(adjoint),
+            "mixed": summary_mixed(mixed), "double_word": summary_dw(dwf), "adjoint": summary_adjoint(adjoint),
             "reacting_ns": summary_flame(flame), "blast_amr": summary_blast(blast),
             "p2_contraction": summary_tc(tc)}
 
@@ -395,6 +437,13 @@ def summary_mixed(m):
         return None
     return {"ms_per_step": _r(m["ms_per_step"]), "value": _r(m["value"]), "x_fp64": _r(m["speedup_vs_fp64"]),
             "rel_l2_density_vs_fp64": _r(m["rel_l2_density_vs_fp64"], 3), "mass_drift": _r(m["mass_drift_mixed"], 3)}
+
+
+def summary_dw(d):
+    if not d:
+        return None
+    return {"ms_per_step": _r(d["ms_per_step"]), "value": _r(d["value"]), "x_fp64": _r(d["speedup_vs_fp64"]),
+            "rel_l2_state_vs_fp64": _r(d["rel_l2_state_vs_fp64"], 3)}
 
 
 def summary_adjoint(a):
@@ -827,7 +876,7 @@ def main():
     ap.add_argument("--parity-steps", type=int, default=20,
                     help="oracle steps on the level --cpu-level sample (cpu_baseline and parity; 0 skips both)")
     ap.add_argument("--brick", type=int, default=1, help="trees along x (profiling sizes)")
-    ap.add_argument("--only", default="both", choices=["both", "fp64", "mixed", "adjoint", "flame", "blast", "tc"])
+    ap.add_argument("--only", default="both", choices=["both", "fp64", "mixed", "dw", "adjoint", "flame", "blast", "tc"])
     ap.add_argument("--blast-steps", type=int, default=200, help="0 skips the AMR blast leg")
     ap.add_argument("--flame-level", type=int, default=6)
     ap.add_argument("--flame-order", type=int, default=2, choices=[1, 2], help="basis order of the reacting leg")
@@ -843,6 +892,7 @@ def main():
     ap.add_argument("--adjoint-fd-eps", type=float, default=1e-6, help="central-difference step")
     ap.add_argument("--tc-reps", type=int, default=20, help="timed launches of the p2 contraction leg (0 skips it)")
     ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-dw", action="store_true", help="skip the double-word form's leg")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -29,7 +29,7 @@ MODEL = {"EULER": 0, "NS": 1}
 FLUX = {"LF": 0, "GODUNOV": 1, "HLLC": 2, "CD": 3}
 LIMITER = {"NONE": 0, "BJ": 1}
 EOS = {"IDEAL": 0, "MIX": 1}
-PRECISION = {"FP64": 0, "MIXED": 1}
+PRECISION = {"FP64": 0, "MIXED": 1, "DW": 2}
 DT_MODE = {"TAU": 0, "CFL": 1}
 BND = {"BOUND_INLET": 0, "BOUND_OUTLET": 1, "BOUND_WALL_SLIP": 2, "BOUND_WALL_NO_SLIP": 3, "BOUND_MASS_FLOW": 4}
 CP_TYPE = {"CONST": 0, "POLYNOM": 1}

@@ -18,6 +18,7 @@
 #include <cstring>
 #include <string>
 #include <thread>
+#include <type_traits>
 #include <utility>
 #include <algorithm>
 #include <unordered_map>
@@ -266,8 +267,15 @@ int validate_config(const charm_gpu_config_t *c)
     if (c->limiter != CHARM_GPU_LIM_NONE && c->limiter != CHARM_GPU_LIM_BJ)
         return fail(CHARM_GPU_EINVAL, "unknown limiter type");
     if (c->eos != CHARM_GPU_EOS_IDEAL && c->eos != CHARM_GPU_EOS_MIX) return fail(CHARM_GPU_EINVAL, "unknown EOS");
-    if (c->precision != CHARM_GPU_PREC_FP64 && c->precision != CHARM_GPU_PREC_MIXED)
+    if (c->precision != CHARM_GPU_PREC_FP64 && c->precision != CHARM_GPU_PREC_MIXED && c->precision != CHARM_GPU_PREC_DW)
         return fail(CHARM_GPU_EINVAL, "unknown precision");
+    if (c->precision == CHARM_GPU_PREC_DW && (c->p_order == 2 || c->use_visc || c->n_react))
+        return fail(CHARM_GPU_ENOTSUP, "double-word form: p1 convective terms only");
+    if (c->precision == CHARM_GPU_PREC_DW && c->flux == CHARM_GPU_FLUX_GODUNOV)
+        return fail(CHARM_GPU_ENOTSUP, "double-word form: LF, HLLC or CD flux");
+    if (c->precision == CHARM_GPU_PREC_DW &&
+        (c->eos != CHARM_GPU_EOS_IDEAL || c->comp[0].cp_type == CHARM_GPU_CP_POLYNOM))
+        return fail(CHARM_GPU_ENOTSUP, "double-word form: ideal gas with constant cp");
     if (c->n_comp < 1 || c->n_comp > CHARM_GPU_MAX_COMP) return fail(CHARM_GPU_EINVAL, "n_comp out of range");
     if (c->n_comp > 2) return fail(CHARM_GPU_ENOTSUP, "more than 2 species not instantiated");
     if (c->n_bnd < 0 || c->n_bnd > CHARM_GPU_MAX_BND) return fail(CHARM_GPU_EINVAL, "n_bnd out of range");
@@ -386,6 +394,7 @@ int ensure_cfg(charm_gpu_handle_s *h)
     CUDA_TRY(cfg_takeover(s, h->stream));
     CUDA_TRY(cudaMemcpyToSymbolAsync(c_cfg, &h->dcfg, sizeof(DevCfg), 0, cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(p2_upload_cfg(&h->dcfg, h->stream));
+    CUDA_TRY(dw_upload_cfg(&h->dcfg, h->stream));
     s.owner = h;
     s.stream = h->stream;
     s.live = true;
@@ -467,6 +476,12 @@ int launch_face(charm_gpu_handle_s *h, const double *u)
     T *slots = static_cast<T *>(h->d_slots);
     TimedLaunch t;
     begin_launch(h, 0, &t);
+    if constexpr (is_dw<T>) {
+        dw_launch_face<NC>(h->cfg.flux, m, u, slots, nbi, (unsigned) (nbi + nbb), h->d_err, h->stream);
+        end_launch(h, &t);
+        CUDA_TRY(cudaGetLastError());
+        return CHARM_GPU_OK;
+    } else
     switch (h->cfg.flux) {
     case CHARM_GPU_FLUX_LF:
         face_kernel<T, NC, CHARM_GPU_FLUX_LF><<<(unsigned) (nbi + nbb), bs, 0, h->stream>>>(m, u, slots, nbi, h->d_err);
@@ -496,6 +511,10 @@ int launch_cell(charm_gpu_handle_s *h, const double *u, const double *u0, double
     const int64_t nb = (h->E + bs - 1) / bs;
     TimedLaunch t;
     begin_launch(h, 1, &t);
+    if constexpr (is_dw<T>)
+        dw_launch_cell<NC>(m, u, static_cast<const T *>(h->d_slots), u0, out, dt, dt_dev, a_new, a_old, mode, h->d_err,
+                           radd, reinterpret_cast<unsigned long long *>(dt_next), h->cfg.cfl, h->stream);
+    else
     cell_kernel<T, NC><<<(unsigned) nb, bs, 0, h->stream>>>(m, u, static_cast<const T *>(h->d_slots), u0, out, dt,
                                                             dt_dev, a_new, a_old, mode, h->d_err, radd,
                                                             reinterpret_cast<unsigned long long *>(dt_next), h->cfg.cfl);
@@ -774,9 +793,9 @@ int stage(charm_gpu_handle_s *h, const double *u, const double *u0, double *out,
 {
     int rc;
     const double *radd = nullptr;
-    if constexpr (sizeof(T) == sizeof(double))
+    if constexpr (std::is_same<T, double>::value)
         if (h->nb == kNB2) return p2_stage<NC>(h, u, u0, out, dt, dt_dev, a_new, a_old, kCellUpdate);
-    if constexpr (sizeof(T) == sizeof(double)) {
+    if constexpr (std::is_same<T, double>::value) {
         if (has_visc_chem(h)) {
             if (h->cfg.n_react) {
                 if ((rc = launch_chem<NC>(h, u))) return rc;
@@ -790,7 +809,7 @@ int stage(charm_gpu_handle_s *h, const double *u, const double *u0, double *out,
     }
     rc = launch_face<T, NC>(h, u);
     if (rc) return rc;
-    if constexpr (sizeof(T) == sizeof(double))
+    if constexpr (std::is_same<T, double>::value)
         if (radd && (rc = launch_vflux<NC>(h, u))) return rc;
     if (h->cfg.limiter == CHARM_GPU_LIM_BJ) {
         rc = launch_cell<T, NC>(h, u, nullptr, h->d_ua, dt, dt_dev, 1.0, 0.0, kCellUpdate, radd);
@@ -804,7 +823,7 @@ int stage(charm_gpu_handle_s *h, const double *u, const double *u0, double *out,
 // FP64 p1): the reference's get_dt of the state this step ends with.
 bool fused_cfl(const charm_gpu_handle_s *h)
 {
-    return h->cfg.dt_mode == CHARM_GPU_DT_CFL && h->cfg.precision == CHARM_GPU_PREC_FP64 && h->nb != kNB2;
+    return h->cfg.dt_mode == CHARM_GPU_DT_CFL && h->cfg.precision != CHARM_GPU_PREC_MIXED && h->nb != kNB2;
 }
 
 template <typename T, int NC>
@@ -1043,6 +1062,7 @@ int step_dispatch(charm_gpu_handle_s *h, double dt, const double *dt_dev)
         default: return fail(CHARM_GPU_ENOTSUP, "species count not instantiated");
         }
     }
+    if (h->cfg.precision == CHARM_GPU_PREC_DW) return step_dispatch_t<dw>(h, dt, dt_dev);
     return step_dispatch_t<double>(h, dt, dt_dev);
 }
 
@@ -1678,6 +1698,11 @@ int charm_gpu_residual(charm_gpu_handle_t h, double *res, int on_device)
                 rc = launch_cell<double, 2>(h, h->d_u, nullptr, h->d_ua, 0, nullptr, 1, 0, kCellResidual, h->d_radd);
             break;
         }
+    } else if (h->cfg.precision == CHARM_GPU_PREC_DW) {
+        switch (h->cfg.n_comp) {
+        case 1: rc = launch_face<dw, 1>(h, h->d_u); if (!rc) rc = launch_cell<dw, 1>(h, h->d_u, nullptr, h->d_ua, 0, nullptr, 1, 0, kCellResidual); break;
+        default: rc = launch_face<dw, 2>(h, h->d_u); if (!rc) rc = launch_cell<dw, 2>(h, h->d_u, nullptr, h->d_ua, 0, nullptr, 1, 0, kCellResidual); break;
+        }
     } else switch (h->cfg.n_comp * 2 + (mixed ? 1 : 0)) {
     case 2: rc = launch_face<double, 1>(h, h->d_u); if (!rc) rc = launch_cell<double, 1>(h, h->d_u, nullptr, h->d_ua, 0, nullptr, 1, 0, kCellResidual); break;
     case 3: rc = launch_face<float, 1>(h, h->d_u); if (!rc) rc = launch_cell<float, 1>(h, h->d_u, nullptr, h->d_ua, 0, nullptr, 1, 0, kCellResidual); break;
@@ -2270,7 +2295,8 @@ extern "C" int charm_gpu_point_flux(const charm_gpu_config_t *cfg, int64_t n, co
         static std::mutex point_mu;
         std::lock_guard<std::mutex> lock(point_mu);
         const bool mixed = cfg->precision == CHARM_GPU_PREC_MIXED;
-        cudaError_t e = point_launch_flux(&dcfg, cfg->flux, cfg->n_comp, mixed, n, b.U2, b.nrm, b.q, b.err, b.st);
+        const bool dword = cfg->precision == CHARM_GPU_PREC_DW;
+        cudaError_t e = point_launch_flux(&dcfg, cfg->flux, cfg->n_comp, mixed, dword, n, b.U2, b.nrm, b.q, b.err, b.st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(q, b.q, sq, cudaMemcpyDeviceToHost, b.st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, b.err, sizeof(unsigned), cudaMemcpyDeviceToHost, b.st);
         cudaError_t e2 = cudaStreamSynchronize(b.st);

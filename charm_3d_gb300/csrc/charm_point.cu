@@ -56,11 +56,24 @@ void launch_point_flux(int flux, int64_t n, const double *U2, const double *nrm,
     }
 }
 
-cudaError_t point_launch_flux(const DevCfg *cfg, int flux, int n_comp, bool mixed, int64_t n, const double *U2,
-                              const double *nrm, double *q, unsigned *err, cudaStream_t st)
+cudaError_t point_launch_flux(const DevCfg *cfg, int flux, int n_comp, bool mixed, bool dword, int64_t n,
+                              const double *U2, const double *nrm, double *q, unsigned *err, cudaStream_t st)
 {
     cudaError_t e = cudaMemcpyToSymbolAsync(c_cfg, cfg, sizeof(DevCfg), 0, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;
+    if (dword) {   // LF, HLLC, CD (the form's fluxes)
+        const unsigned g = (unsigned) ((n + 127) / 128);
+        if (n_comp == 1) {
+            if (flux == CHARM_GPU_FLUX_LF) point_flux_kernel<dw, 1, CHARM_GPU_FLUX_LF><<<g, 128, 0, st>>>(n, U2, nrm, q, err);
+            else if (flux == CHARM_GPU_FLUX_CD) point_flux_kernel<dw, 1, CHARM_GPU_FLUX_CD><<<g, 128, 0, st>>>(n, U2, nrm, q, err);
+            else point_flux_kernel<dw, 1, CHARM_GPU_FLUX_HLLC><<<g, 128, 0, st>>>(n, U2, nrm, q, err);
+        } else {
+            if (flux == CHARM_GPU_FLUX_LF) point_flux_kernel<dw, 2, CHARM_GPU_FLUX_LF><<<g, 128, 0, st>>>(n, U2, nrm, q, err);
+            else if (flux == CHARM_GPU_FLUX_CD) point_flux_kernel<dw, 2, CHARM_GPU_FLUX_CD><<<g, 128, 0, st>>>(n, U2, nrm, q, err);
+            else point_flux_kernel<dw, 2, CHARM_GPU_FLUX_HLLC><<<g, 128, 0, st>>>(n, U2, nrm, q, err);
+        }
+        return cudaGetLastError();
+    }
     switch (n_comp * 2 + (mixed ? 1 : 0)) {
     case 2: launch_point_flux<double, 1>(flux, n, U2, nrm, q, err, st); break;
     case 3: launch_point_flux<float, 1>(flux, n, U2, nrm, q, err, st); break;

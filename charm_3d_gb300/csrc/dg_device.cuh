@@ -9,8 +9,10 @@
 
 #include <cstdint>
 #include <cmath>
+#include <type_traits>
 
 #include "charm_gpu.h"
+#include "dw.cuh"
 
 namespace charm {
 
@@ -79,9 +81,13 @@ static __constant__ DevCfg c_cfg;
 // Constant of the configuration in the arithmetic type T: the double for
 // T = double, its float mirror for T = float.
 template <typename T>
+constexpr bool is_dw = std::is_same<T, dw>::value;
+
+template <typename T>
 __device__ __forceinline__ T cfgv(const double &d, const float &f)
 {
-    if constexpr (sizeof(T) == sizeof(float)) return f;
+    if constexpr (is_dw<T>) return dw(d);
+    else if constexpr (sizeof(T) == sizeof(float)) return f;
     else return d;
 }
 
@@ -109,14 +115,16 @@ __device__ __forceinline__ double rcp_nr(double x)
 template <typename T>
 __device__ __forceinline__ T qdiv(T a, T b)
 {
-    if constexpr (sizeof(T) == sizeof(float)) return __fdividef(a, b);
+    if constexpr (is_dw<T>) return a / b;
+    else if constexpr (sizeof(T) == sizeof(float)) return __fdividef(a, b);
     else return a * rcp_nr(b);
 }
 
 template <typename T>
 __device__ __forceinline__ T qrcp(T b)
 {
-    if constexpr (sizeof(T) == sizeof(float)) return __fdividef(1.f, b);
+    if constexpr (is_dw<T>) return dw(1.f) / b;
+    else if constexpr (sizeof(T) == sizeof(float)) return __fdividef(1.f, b);
     else return rcp_nr(b);
 }
 
@@ -127,9 +135,9 @@ __device__ __forceinline__ T qrcp(T b)
 template <typename T>
 __device__ __forceinline__ T clamp01(T c)
 {
-    if constexpr (sizeof(T) == sizeof(float)) {
-        if (c < 0.f) c = 0.f;
-        if (c > 1.f) c = 1.f;
+    if constexpr (is_dw<T> || sizeof(T) == sizeof(float)) {
+        if (c < T(0.f)) c = T(0.f);
+        if (c > T(1.f)) c = T(1.f);
         return c;
     } else {
         long long b = __double_as_longlong(c);
@@ -144,7 +152,8 @@ __device__ __forceinline__ T clamp01(T c)
 template <typename T>
 __device__ __forceinline__ T qsqrt(T x)
 {
-    if constexpr (sizeof(T) == sizeof(float)) return (x == 0.f) ? 0.f : x * rsqrtf(x);
+    if constexpr (is_dw<T>) return sqrt(x);
+    else if constexpr (sizeof(T) == sizeof(float)) return (x == 0.f) ? 0.f : x * rsqrtf(x);
     else return sqrt(x);
 }
 
@@ -289,6 +298,24 @@ __device__ __forceinline__ void cons_to_prim(const T *U, Prim<T, NC> &p)
     p.e = p.e_tot - T(0.5) * (p.u * p.u + p.v * p.v + p.w * p.w);
     for (int i = 0; i < NC; i++) p.c[i] = clamp01<T>(U[4 + i] * ir);
     p.t = T(0);
+    if constexpr (is_dw<T>) {
+        // the double-word form runs for the ideal gas with constant cp only
+        // (configurations are checked): eos flag 4 with its density clamp
+        // (src/charm_eos.c:86-90) and the same formulas
+        p.cp = cfgv<T>(c_cfg.ideal_cp, c_cfg.ideal_cp_f); p.m = cfgv<T>(c_cfg.ideal_m, c_cfg.ideal_m_f);
+        p.cv = cfgv<T>(c_cfg.ideal_cv, c_cfg.ideal_cv_f); p.gam = cfgv<T>(c_cfg.ideal_gam, c_cfg.ideal_gam_f);
+        if (r >= T(kEps)) {
+            p.p = cfgv<T>(c_cfg.ideal_gm1, c_cfg.ideal_gm1_f) * (U[3] - T(0.5) * (U[0] * p.u + U[1] * p.v + U[2] * p.w));
+        } else {
+            p.r = T(kEps);
+            ir = T(1) / T(kEps);
+            p.ir = ir;
+            p.p = p.r * p.e * cfgv<T>(c_cfg.ideal_gm1, c_cfg.ideal_gm1_f);
+        }
+        p.cz = qsqrt<T>(p.gam * p.p * ir);
+        p.t = p.e * cfgv<T>(c_cfg.ideal_inv_cv, c_cfg.ideal_inv_cv_f);
+        return;
+    }
     if (c_cfg.ideal_fast && r >= T(kEps)) {
         // eos flag 4 for a constant-cp ideal gas (src/charm_eos.c:86-90),
         // with 1/r, gam - 1 and 1/cv reused instead of computed again

@@ -47,16 +47,24 @@ static __constant__ double c_face_psd[6] = {1.0 / 6.0 - 0.5, 2.0 / 3.0 - 0.5, 1.
 static __constant__ double c_face_ptd[6] = {1.0 / 6.0 - 0.5, 1.0 / 6.0 - 0.5, 2.0 / 3.0 - 0.5,
                                             1.0 / 3.0 - 0.5, 5.0 / 6.0 - 0.5, 5.0 / 6.0 - 0.5};
 
+// and as double-word values (hi, lo of the doubles above)
+static __constant__ dw c_face_psw[6] = {dw(1.0 / 6.0 - 0.5), dw(2.0 / 3.0 - 0.5), dw(1.0 / 6.0 - 0.5),
+                                        dw(5.0 / 6.0 - 0.5), dw(1.0 / 3.0 - 0.5), dw(5.0 / 6.0 - 0.5)};
+static __constant__ dw c_face_ptw[6] = {dw(1.0 / 6.0 - 0.5), dw(1.0 / 6.0 - 0.5), dw(2.0 / 3.0 - 0.5),
+                                        dw(1.0 / 3.0 - 0.5), dw(5.0 / 6.0 - 0.5), dw(5.0 / 6.0 - 0.5)};
+
 template <typename T>
 __device__ __forceinline__ T face_ps(int g)
 {
-    if constexpr (sizeof(T) == sizeof(float)) return c_face_psf[g];
+    if constexpr (is_dw<T>) return c_face_psw[g];
+    else if constexpr (sizeof(T) == sizeof(float)) return c_face_psf[g];
     else return c_face_psd[g];
 }
 template <typename T>
 __device__ __forceinline__ T face_pt(int g)
 {
-    if constexpr (sizeof(T) == sizeof(float)) return c_face_ptf[g];
+    if constexpr (is_dw<T>) return c_face_ptw[g];
+    else if constexpr (sizeof(T) == sizeof(float)) return c_face_ptf[g];
     else return c_face_ptd[g];
 }
 
@@ -92,7 +100,8 @@ __device__ __forceinline__ double level_h(const MeshDev &m, int lev, int d)
 template <typename T>
 __device__ __forceinline__ T level_ht(const MeshDev &m, int lev, int d)
 {
-    if constexpr (sizeof(T) == sizeof(float)) return ldexpf(m.tree_len_f[d], -lev);
+    if constexpr (is_dw<T>) return dw(ldexp(m.tree_len[d], -lev));
+    else if constexpr (sizeof(T) == sizeof(float)) return ldexpf(m.tree_len_f[d], -lev);
     else return ldexp(m.tree_len[d], -lev);
 }
 
@@ -128,6 +137,11 @@ __device__ __forceinline__ void store_pair<float>(float *slots, int64_t idx, flo
 {
     *reinterpret_cast<float2 *>(slots + idx) = make_float2(a, b);
 }
+template <>
+__device__ __forceinline__ void store_pair<dw>(dw *slots, int64_t idx, dw a, dw b)
+{
+    *reinterpret_cast<float4 *>(slots + idx) = make_float4(a.h, a.l, b.h, b.l);
+}
 
 // Interior face i along axis D (compile-time, so that the coefficient arrays
 // stay in registers).
@@ -145,7 +159,7 @@ __device__ __forceinline__ void interior_face(const MeshDev &m, const double *__
     const int lev = m.level[ep];
     const T w = level_ht<T>(m, lev, s) * level_ht<T>(m, lev, t) * (T(1) / T(6));
     // tangential offsets of the big side in a mortar
-    const T os = T((sub & 1) ? 0.25 : -0.25), ot = T((sub & 2) ? 0.25 : -0.25);
+    const T os = (sub & 1) ? T(0.25) : T(-0.25), ot = (sub & 2) ? T(0.25) : T(-0.25);
 
     T c0[V][kNB], c1[V][kNB];
     load_coef<T, V>(u, m.n_elem, e0, c0);
@@ -202,13 +216,14 @@ __device__ __forceinline__ void interior_face(const MeshDev &m, const double *__
 }
 
 // Boundary face j on axis D; sg = -1 for the lower face, +1 for the upper.
-template <typename T, int NC, int FLUX, int D>
-__device__ __forceinline__ void boundary_face(const MeshDev &m, const double *__restrict__ u, T *__restrict__ slots,
+// T: the arithmetic, S: the slot type (S = dw with T = double: the
+// double-word form evaluates its boundary faces, a surface's worth, in FP64)
+template <typename T, int NC, int FLUX, int D, typename S = T>
+__device__ __forceinline__ void boundary_face(const MeshDev &m, const double *__restrict__ u, S *__restrict__ slots,
                                               int64_t j, int e, T sg, int bid, unsigned *err)
 {
     constexpr int V = 4 + NC;
     constexpr int s = (D == 0) ? 1 : 0, t = (D == 2) ? 1 : 2;
-    const int64_t S = m.n_slot;
     const int lev = m.level[e];
     const T w = level_ht<T>(m, lev, s) * level_ht<T>(m, lev, t) * (T(1) / T(6));
     T c[V][kNB];
@@ -238,13 +253,14 @@ __device__ __forceinline__ void boundary_face(const MeshDev &m, const double *__
         }
     }
     const int64_t slot = 2 * m.n_face + j;
+    const int64_t NS = m.n_slot;
 #pragma unroll
     for (int v = 0; v < V; v++) {
         T a0 = w * S0[v];
-        slots[(int64_t) (v * kNB + 0) * S + slot] = a0;
-        slots[(int64_t) (v * kNB + 1 + D) * S + slot] = T(0.5) * sg * a0;
-        slots[(int64_t) (v * kNB + 1 + s) * S + slot] = w * Ss[v];
-        slots[(int64_t) (v * kNB + 1 + t) * S + slot] = w * St[v];
+        slots[(int64_t) (v * kNB + 0) * NS + slot] = S(a0);
+        slots[(int64_t) (v * kNB + 1 + D) * NS + slot] = S(T(0.5) * sg * a0);
+        slots[(int64_t) (v * kNB + 1 + s) * NS + slot] = S(w * Ss[v]);
+        slots[(int64_t) (v * kNB + 1 + t) * NS + slot] = S(w * St[v]);
     }
 }
 
@@ -271,11 +287,12 @@ face_kernel(MeshDev m, const double *__restrict__ u, T *__restrict__ slots, int6
         if (j >= m.n_bface) return;
         const int e = m.bface_elem[j];
         const int f = m.bface_face[j], bid = m.bface_bnd[j];
-        const T sg = (f & 1) ? T(1) : T(-1);
+        using TB = typename std::conditional<is_dw<T>, double, T>::type;
+        const TB sg = (f & 1) ? TB(1) : TB(-1);
         switch (f >> 1) {
-        case 0: boundary_face<T, NC, FLUX, 0>(m, u, slots, j, e, sg, bid, err); break;
-        case 1: boundary_face<T, NC, FLUX, 1>(m, u, slots, j, e, sg, bid, err); break;
-        default: boundary_face<T, NC, FLUX, 2>(m, u, slots, j, e, sg, bid, err); break;
+        case 0: boundary_face<TB, NC, FLUX, 0, T>(m, u, slots, j, e, sg, bid, err); break;
+        case 1: boundary_face<TB, NC, FLUX, 1, T>(m, u, slots, j, e, sg, bid, err); break;
+        default: boundary_face<TB, NC, FLUX, 2, T>(m, u, slots, j, e, sg, bid, err); break;
         }
     }
 }
@@ -346,9 +363,9 @@ cell_kernel(MeshDev m, const double *__restrict__ u, const T *__restrict__ slots
 
 #pragma unroll 1
     for (int g = 0; g < 8; g++) {
-        const T px = T((g & 1) ? kGaussPhi : -kGaussPhi);
-        const T py = T((g & 2) ? kGaussPhi : -kGaussPhi);
-        const T pz = T((g & 4) ? kGaussPhi : -kGaussPhi);
+        const T px = (g & 1) ? T(kGaussPhi) : T(-kGaussPhi);
+        const T py = (g & 2) ? T(kGaussPhi) : T(-kGaussPhi);
+        const T pz = (g & 4) ? T(kGaussPhi) : T(-kGaussPhi);
         T U[V];
 #pragma unroll
         for (int v = 0; v < V; v++) U[v] = c[v][0] + px * c[v][1] + py * c[v][2] + pz * c[v][3];

@@ -62,12 +62,25 @@ template <typename T, int NC>
 void p2_launch_vflux(const MeshDev &m, const T *u, const T *vis, T *slots, int64_t nbi, unsigned nb,
                      cudaStream_t st);
 
+// ---- double-word form (charm_dw.cu) ------------------------------------------
+
+cudaError_t dw_upload_cfg(const DevCfg *cfg, cudaStream_t st);
+// face_kernel<dw> (flux LF, CD or HLLC) and cell_kernel<dw>, arguments as theirs
+template <int NC>
+void dw_launch_face(int flux, const MeshDev &m, const double *u, dw *slots, int64_t nbi, unsigned nb, unsigned *err,
+                    cudaStream_t st);
+template <int NC>
+void dw_launch_cell(const MeshDev &m, const double *u, const dw *slots, const double *u0, double *out, double dt,
+                    const double *dt_dev, double a_new, double a_old, int mode, unsigned *err, const double *radd,
+                    unsigned long long *dt_next, double cfl, cudaStream_t st);
+
 // ---- point fluxes (charm_point.cu) ------------------------------------------
 
 // Upload cfg to the unit's constants, then q[i] = flux between the state
-// pair U2[i] along nrm[i] (n pairs; T = double, or float for `mixed`).
-cudaError_t point_launch_flux(const DevCfg *cfg, int flux, int n_comp, bool mixed, int64_t n, const double *U2,
-                              const double *nrm, double *q, unsigned *err, cudaStream_t st);
+// pair U2[i] along nrm[i] (n pairs; T = double, float for `mixed`, dw for
+// `dword`).
+cudaError_t point_launch_flux(const DevCfg *cfg, int flux, int n_comp, bool mixed, bool dword, int64_t n,
+                              const double *U2, const double *nrm, double *q, unsigned *err, cudaStream_t st);
 
 // out[i] = rcp_nr(b[i]) (which 0) or qdiv(a[i], b[i]) (which 1), device arrays.
 cudaError_t point_launch_math(int which, int64_t n, const double *a, const double *b, double *out, cudaStream_t st);

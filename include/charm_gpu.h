@@ -66,7 +66,11 @@ enum { CHARM_GPU_FLUX_LF = 0, CHARM_GPU_FLUX_GODUNOV = 1, CHARM_GPU_FLUX_HLLC = 
 enum { CHARM_GPU_LIM_NONE = 0, CHARM_GPU_LIM_BJ = 1 };  /* :370-380 */
 enum { CHARM_GPU_EOS_IDEAL = 0, CHARM_GPU_EOS_MIX = 1 };/* :174-186 */
 enum { CHARM_GPU_PREC_FP64 = 0,     /* drop-in: all arithmetic in FP64 */
-       CHARM_GPU_PREC_MIXED = 1 };  /* FP32 residual, FP64 state/update/dt */
+       CHARM_GPU_PREC_MIXED = 1,    /* FP32 residual, FP32 hi/lo state, FP64 dt */
+       CHARM_GPU_PREC_DW = 2 };     /* FP64 state; residual (fluxes, volume terms) in double-word
+                                       arithmetic on the FP32 pipe (two floats, ~48 bits), within
+                                       ~1e-13 of FP64; p1 convective terms (no viscous terms or
+                                       chemistry), no adjoint, no allocation-free residual */
 enum { CHARM_GPU_DT_TAU = 0,        /* fixed TAU: the reference's get_dt_fn
                                        (src/models/ns/charm_model.c:49) */
        CHARM_GPU_DT_CFL = 1 };      /* CFL*volume/(|u|+c) at the cell centres,
