@@ -719,6 +719,7 @@ def _blast_run(case, steps: int, device: int, precision: str):
     gpu.upload(mesh)
     gpu.set_state(u)
     dev_ms, dofs, t_adapt, step = 0.0, 0, 0.0, 0
+    parts = {"flags_s": 0.0, "plan_s": 0.0, "flatten_s": 0.0, "upload_s": 0.0}
     t0 = time.perf_counter()
     while step < steps:
         if step and step % case.refine_period == 0:
@@ -726,10 +727,19 @@ def _blast_run(case, steps: int, device: int, precision: str):
             # gradient estimate and the densities, the device projects
             ta = time.perf_counter()
             _, grad = gpu.refine_flags(case.max_err)
-            _, plan = forest.adapt_plan(grad, gpu.density_means(), case.max_err, case.min_level, case.max_level)
+            rho = gpu.density_means()
+            tb = time.perf_counter()
+            _, plan = forest.adapt_plan(grad, rho, case.max_err, case.min_level, case.max_level)
+            tc = time.perf_counter()
             mesh = forest.flatten()
+            td = time.perf_counter()
             gpu.adapt_upload(plan, mesh)
-            t_adapt += time.perf_counter() - ta
+            te = time.perf_counter()
+            parts["flags_s"] += tb - ta
+            parts["plan_s"] += tc - tb
+            parts["flatten_s"] += td - tc
+            parts["upload_s"] += te - td
+            t_adapt += te - ta
         n = min(case.refine_period - step % case.refine_period, steps - step)
         dev_ms += gpu.time_run(n, case.tau)
         dofs += dof_per_step(mesh.n_elem, case.n_var) * n
@@ -738,7 +748,7 @@ def _blast_run(case, steps: int, device: int, precision: str):
     wall = time.perf_counter() - t0
     u = gpu.get_state()
     gpu.close()
-    return forest, mesh, u, dev_ms, dofs, wall, t_adapt, (_mass(mesh, u) - mass0) / mass0
+    return forest, mesh, u, dev_ms, dofs, wall, t_adapt, (_mass(mesh, u) - mass0) / mass0, parts
 
 
 def _mass(mesh, u) -> float:
@@ -767,11 +777,12 @@ def run_blast(args, device: int) -> dict:
     for prec in ("FP64", "MIXED"):
         case = synthetic("blast")
         _, gam = case.gas_constants()
-        forest, mesh, u, dev_ms, dofs, wall, t_adapt, drift = _blast_run(case, args.blast_steps, device, prec)
+        forest, mesh, u, dev_ms, dofs, wall, t_adapt, drift, parts = _blast_run(case, args.blast_steps, device, prec)
         q, lv = forest.leaves()
         res[prec] = (q, lv, u, mesh)
         out[prec.lower()] = {"value": dofs / (dev_ms * 1e-3), "unit": UNIT, "device_ms": dev_ms,
                              "e2e_dof_updates_per_s": dofs / wall, "wall_s": wall, "adapt_s": t_adapt,
+                             "adapt_parts_s": parts,
                              "final_elements": int(mesh.n_elem), "levels": [int(lv.min()), int(lv.max())],
                              "shock_radius": _shock_radius(mesh, u, gam), "mass_drift": drift,
                              "finite": bool(np.isfinite(u).all())}

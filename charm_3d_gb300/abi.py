@@ -102,6 +102,11 @@ class Mesh(C.Structure):
                 ("bface_bnd", C.POINTER(C.c_int8))]
 
 
+class Hex(C.Structure):
+    """charm_gpu_hex_t: corners and face numbers of general hexahedra."""
+    _fields_ = [("vertex", C.POINTER(C.c_double)), ("face_face", C.POINTER(C.c_int8))]
+
+
 class AdaptPlan(C.Structure):
     """charm_gpu_adapt_plan_t: the projection passes of one adapt."""
     _fields_ = [("n_pass", C.c_int32), ("pad", C.c_int32), ("n_in", C.c_int64),
@@ -118,6 +123,7 @@ SIGNATURES = [
     ("charm_gpu_create", C.c_int, [C.POINTER(_P), C.POINTER(Config), C.c_int]),
     ("charm_gpu_destroy", C.c_int, [_P]),
     ("charm_gpu_upload_mesh", C.c_int, [_P, C.POINTER(Mesh)]),
+    ("charm_gpu_upload_mesh_hex", C.c_int, [_P, C.POINTER(Mesh), C.POINTER(Hex)]),
     ("charm_gpu_set_state", C.c_int, [_P, _P, C.c_int]),
     ("charm_gpu_get_state", C.c_int, [_P, _P, C.c_int]),
     ("charm_gpu_step", C.c_int, [_P, C.c_double, _DP]),
@@ -160,6 +166,11 @@ SIGNATURES = [
     ("charm_host_forest_flatten", C.c_int, [_P, C.POINTER(Mesh)]),
     ("charm_host_forest_leaves", C.c_int, [_P, _P, _P]),
     ("charm_host_forest_write_vtu", C.c_int, [_P, C.c_char_p, C.c_int, C.POINTER(C.c_char_p), _P]),
+    ("charm_host_forest_new_hex", C.c_int, [C.POINTER(_P), C.c_int32, _P, C.c_int32, _P, _P, C.c_int]),
+    ("charm_host_forest_new_gmsh", C.c_int, [C.POINTER(_P), C.c_char_p, C.c_int, C.c_int, C.POINTER(C.c_char_p)]),
+    ("charm_host_forest_tree_count", C.c_int, [_P]),
+    ("charm_host_forest_tree_region", C.c_int, [_P, _P]),
+    ("charm_host_forest_flatten_hex", C.c_int, [_P, C.POINTER(Mesh), C.POINTER(Hex)]),
 ]
 
 _lib = None

@@ -21,8 +21,9 @@ LIB = os.path.join(PKG, "libcharm_gpu.so")
 
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
-CUDA_SOURCES = ["charm_gpu.cu", "charm_p2.cu", "charm_point.cu", "charm_tc.cu", "charm_dw.cu"]
-C_SOURCES = ["host/charm_forest.c", "host/charm_host_api.c", "host/charm_yaml.c", "host/charm_case.c"]
+CUDA_SOURCES = ["charm_gpu.cu", "charm_p2.cu", "charm_point.cu", "charm_tc.cu", "charm_dw.cu", "charm_hex.cu"]
+C_SOURCES = ["host/charm_forest.c", "host/charm_host_api.c", "host/charm_yaml.c", "host/charm_case.c",
+             "host/charm_conn.c"]
 
 
 def _nvcc() -> str:

@@ -8,6 +8,7 @@ namespace {
 int adj_check(charm_gpu_handle_s *h)
 {
     if (h->cfg.precision != CHARM_GPU_PREC_FP64) return fail(CHARM_GPU_ENOTSUP, "adjoint: FP64 precision only");
+    if (h->hex) return fail(CHARM_GPU_ENOTSUP, "adjoint: box meshes only");
     if (h->nb != CHARM_GPU_BASIS) return fail(CHARM_GPU_ENOTSUP, "adjoint: p1 basis only");
     if (!h->dcfg.ideal_fast) return fail(CHARM_GPU_ENOTSUP, "adjoint: ideal gas with constant cp only");
     if (h->cfg.dt_mode != CHARM_GPU_DT_TAU) return fail(CHARM_GPU_ENOTSUP, "adjoint: fixed time step (TAU) only");

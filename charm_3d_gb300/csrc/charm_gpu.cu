@@ -110,6 +110,11 @@ struct charm_gpu_handle_s {
     int32_t *d_pmap = nullptr;         // one pass of an adapt plan
     unsigned *d_err = nullptr;
     bool mesh_ready = false;
+    // general hexahedra (charm_gpu_upload_mesh_hex): corners, face numbers
+    // and the geometry tables of dg_hex.cuh
+    bool hex = false;
+    double *d_hex_vert = nullptr, *d_hex_g = nullptr, *d_hex_fg = nullptr;
+    int8_t *d_hex_ff = nullptr;
     // accounting
     int64_t launches[4] = {0, 0, 0, 0};
     double ms[4] = {0, 0, 0, 0};
@@ -207,6 +212,7 @@ void reset_mesh(charm_gpu_handle_s *h)
     h->n_tiles = 0;
     h->tile_smem = 0;
     h->mesh_ready = false;
+    h->hex = false;
     h->E = h->F = h->Fb = h->S = 0;
 }
 
@@ -214,7 +220,7 @@ void free_mesh(charm_gpu_handle_s *h)
 {
     void *ptrs[] = {h->d_center, h->d_level, h->d_face_elem, h->d_face_info, h->d_bface_elem, h->d_bface_face,
                     h->d_bface_bnd, h->d_gather_ptr, h->d_gather_slot, h->d_lim_idx, h->d_lim_kind, h->d_u,
-                    h->d_ua, h->d_ub, h->d_slots};
+                    h->d_ua, h->d_ub, h->d_slots, h->d_hex_vert, h->d_hex_g, h->d_hex_fg, h->d_hex_ff};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int k = 0; k < 3; k++) {
@@ -255,7 +261,10 @@ void free_mesh(charm_gpu_handle_s *h)
     h->d_gather_ptr = nullptr; h->d_gather_slot = nullptr; h->d_lim_idx = nullptr; h->d_lim_kind = nullptr;
     h->d_u = h->d_ua = h->d_ub = nullptr;
     h->d_slots = nullptr;
+    h->d_hex_vert = h->d_hex_g = h->d_hex_fg = nullptr;
+    h->d_hex_ff = nullptr;
     h->mesh_ready = false;
+    h->hex = false;
     h->E = h->F = h->Fb = h->S = 0;
 }
 
@@ -395,6 +404,7 @@ int ensure_cfg(charm_gpu_handle_s *h)
     CUDA_TRY(cudaMemcpyToSymbolAsync(c_cfg, &h->dcfg, sizeof(DevCfg), 0, cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(p2_upload_cfg(&h->dcfg, h->stream));
     CUDA_TRY(dw_upload_cfg(&h->dcfg, h->stream));
+    CUDA_TRY(hex_upload_cfg(&h->dcfg, h->stream));
     s.owner = h;
     s.stream = h->stream;
     s.live = true;
@@ -415,6 +425,16 @@ MeshDev mesh_view(const charm_gpu_handle_s *h)
         m.tree_len_f[d] = (float) h->tree_len[d];
     }
     return m;
+}
+
+HexDev hex_view(const charm_gpu_handle_s *h)
+{
+    HexDev x;
+    x.g = h->d_hex_g;
+    x.fg = h->d_hex_fg;
+    x.face_face = h->d_hex_ff;
+    x.vert = h->d_hex_vert;
+    return x;
 }
 
 // ---- launch accounting ----------------------------------------------------
@@ -476,6 +496,14 @@ int launch_face(charm_gpu_handle_s *h, const double *u)
     T *slots = static_cast<T *>(h->d_slots);
     TimedLaunch t;
     begin_launch(h, 0, &t);
+    if constexpr (std::is_same<T, double>::value) {
+        if (h->hex) {
+            hex_launch_face<NC>(h->cfg.flux, m, hex_view(h), u, slots, h->d_err, h->stream);
+            end_launch(h, &t);
+            CUDA_TRY(cudaGetLastError());
+            return CHARM_GPU_OK;
+        }
+    }
     if constexpr (is_dw<T>) {
         dw_launch_face<NC>(h->cfg.flux, m, u, slots, nbi, (unsigned) (nbi + nbb), h->d_err, h->stream);
         end_launch(h, &t);
@@ -511,6 +539,12 @@ int launch_cell(charm_gpu_handle_s *h, const double *u, const double *u0, double
     const int64_t nb = (h->E + bs - 1) / bs;
     TimedLaunch t;
     begin_launch(h, 1, &t);
+    if (h->hex) {
+        if constexpr (std::is_same<T, double>::value)
+            hex_launch_cell<NC>(m, hex_view(h), u, static_cast<const double *>(h->d_slots), u0, out, dt, dt_dev, a_new,
+                                a_old, mode, h->d_err, reinterpret_cast<unsigned long long *>(dt_next), h->cfg.cfl,
+                                h->stream);
+    } else
     if constexpr (is_dw<T>)
         dw_launch_cell<NC>(m, u, static_cast<const T *>(h->d_slots), u0, out, dt, dt_dev, a_new, a_old, mode, h->d_err,
                            radd, reinterpret_cast<unsigned long long *>(dt_next), h->cfg.cfl, h->stream);
@@ -532,6 +566,10 @@ int launch_limit(charm_gpu_handle_s *h, const double *ua, const double *u0, doub
     const int64_t nb = (h->E + bs - 1) / bs;
     TimedLaunch t;
     begin_launch(h, 2, &t);
+    if (h->hex)
+        hex_launch_limit<NC>(m, hex_view(h), ua, u0, out, a_new, a_old, reinterpret_cast<unsigned long long *>(dt_next),
+                             h->cfg.cfl, h->stream);
+    else
     limit_kernel<NC><<<(unsigned) nb, bs, 0, h->stream>>>(m, ua, u0, out, a_new, a_old, psi_out,
                                                           reinterpret_cast<unsigned long long *>(dt_next), h->cfg.cfl);
     end_launch(h, &t);
@@ -550,6 +588,9 @@ int launch_cfl(charm_gpu_handle_s *h, const double *u)
     const int64_t nb = (h->E + bs - 1) / bs;
     TimedLaunch t;
     begin_launch(h, 3, &t);
+    if (h->hex)
+        hex_launch_cfl<NC>(m, hex_view(h), u, reinterpret_cast<unsigned long long *>(h->d_dt), h->cfg.cfl, h->stream);
+    else
     cfl_dt_kernel<NC><<<(unsigned) nb, bs, 0, h->stream>>>(m, u, h->cfg.cfl, reinterpret_cast<unsigned long long *>(h->d_dt));
     end_launch(h, &t);
     CUDA_TRY(cudaGetLastError());
@@ -1181,7 +1222,11 @@ int charm_gpu_destroy(charm_gpu_handle_t h)
     return CHARM_GPU_OK;
 }
 
-int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh)
+namespace {
+// The upload of charm_gpu_upload_mesh; with hexff (general hexahedra: the
+// face numbers of both sides of every interior record) the element faces
+// that the records claim come from there instead of the box's dir bits.
+int upload_impl(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh, const int8_t *hexff)
 {
     if (!h || !mesh) return fail(CHARM_GPU_EINVAL, "null argument");
     const int64_t E = mesh->n_elem, F = mesh->n_face, Fb = mesh->n_bface;
@@ -1202,7 +1247,8 @@ int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh)
             return fail(CHARM_GPU_EINVAL, "face record out of range");
         if (kind && h->nb != CHARM_GPU_BASIS) return fail(CHARM_GPU_ENOTSUP, "p2: conforming meshes only");
         cnt[a]++; cnt[b]++;
-        const int fa = 2 * d + 1, fb = 2 * d;   // face ids on side 0 / side 1
+        const int fa = hexff ? hexff[i] : 2 * d + 1, fb = hexff ? hexff[F + i] : 2 * d;   // face ids on side 0 / side 1
+        if (fa < 0 || fa > 5 || fb < 0 || fb > 5) return fail(CHARM_GPU_EINVAL, "face number out of range");
         // each element face takes exactly one record (the big side of a
         // mortar: its first sub-face record)
         auto claim = [&](int f, int32_t e, int8_t k, int32_t idx) {
@@ -1434,6 +1480,76 @@ int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh)
     return CHARM_GPU_OK;
 }
 
+// Jacobian of the trilinear map at the 8 Gauss points of every element, on
+// the host, before anything changes (the same map as hex_map in dg_hex.cuh).
+bool hex_jacobians_positive(const double *vert, int64_t E)
+{
+    const double s3 = 0.57735026918962576451;
+    for (int64_t e = 0; e < E; e++)
+        for (int q = 0; q < 8; q++) {
+            const double r[3] = {(q & 1) ? s3 : -s3, (q & 2) ? s3 : -s3, (q & 4) ? s3 : -s3};
+            double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+            for (int k = 0; k < 8; k++) {
+                const double sx = (k & 1) ? 1.0 : -1.0, sy = (k & 2) ? 1.0 : -1.0, sz = (k & 4) ? 1.0 : -1.0;
+                const double wx = 1.0 + sx * r[0], wy = 1.0 + sy * r[1], wz = 1.0 + sz * r[2];
+                for (int d = 0; d < 3; d++) {
+                    const double v = vert[(int64_t) (3 * k + d) * E + e];
+                    J[d][0] += wz * wy * sx * 0.125 * v;
+                    J[d][1] += wz * wx * sy * 0.125 * v;
+                    J[d][2] += wy * wx * sz * 0.125 * v;
+                }
+            }
+            const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                               J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                               J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+            if (!(det > 0.0)) return false;
+        }
+    return true;
+}
+}  // namespace
+
+int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh)
+{
+    return upload_impl(h, mesh, nullptr);
+}
+
+int charm_gpu_upload_mesh_hex(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh, const charm_gpu_hex_t *hex)
+{
+    if (!h || !mesh || !hex || !hex->vertex || (mesh->n_face > 0 && !hex->face_face))
+        return fail(CHARM_GPU_EINVAL, "null argument");
+    if (h->cfg.precision != CHARM_GPU_PREC_FP64 || h->nb != CHARM_GPU_BASIS)
+        return fail(CHARM_GPU_ENOTSUP, "general hexahedra: FP64, p1");
+    if (h->cfg.model == CHARM_GPU_MODEL_NS && (h->cfg.use_visc || h->cfg.n_react))
+        return fail(CHARM_GPU_ENOTSUP, "general hexahedra: convective terms only");
+    if (mesh->n_elem > 0 && mesh->n_elem < (int64_t) INT32_MAX && !hex_jacobians_positive(hex->vertex, mesh->n_elem))
+        return fail(CHARM_GPU_EINVAL, "element with a non-positive Jacobian");
+    int rc = upload_impl(h, mesh, hex->face_face);
+    if (rc) return rc;
+    const int64_t E = h->E, F = h->F, NR = h->F + h->Fb;
+    int arc;
+    if ((arc = ensure_buf(h, &h->d_hex_vert, 24 * E * sizeof(double))) ||
+        (arc = ensure_buf(h, &h->d_hex_g, (size_t) kHexG * E * sizeof(double))) ||
+        (arc = ensure_buf(h, &h->d_hex_fg, (size_t) kHexF * (NR ? NR : 1) * sizeof(double))) ||
+        (arc = ensure_buf(h, &h->d_hex_ff, 2 * (F ? F : 1)))) {
+        h->mesh_ready = false;
+        return arc;
+    }
+    CUDA_TRY(cudaMemcpy(h->d_hex_vert, hex->vertex, 24 * E * sizeof(double), cudaMemcpyHostToDevice));
+    if (F) CUDA_TRY(cudaMemcpy(h->d_hex_ff, hex->face_face, 2 * F, cudaMemcpyHostToDevice));
+    HexDev x = hex_view(h);
+    CUDA_TRY(cudaMemsetAsync(h->d_err, 0, sizeof(unsigned), h->stream));
+    CUDA_TRY(hex_launch_geom(mesh_view(h), x, h->d_hex_g, h->d_hex_fg, h->d_err, h->stream));
+    unsigned err = 0;
+    CUDA_TRY(cudaMemcpyAsync(&err, h->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    if (err) {
+        h->mesh_ready = false;
+        return fail(CHARM_GPU_EINVAL, "element with a non-positive Jacobian");
+    }
+    h->hex = true;
+    return CHARM_GPU_OK;
+}
+
 // ---- adapt with the state on the device ------------------------------------
 
 // rho[e] = sum of the species' coefficient-0 planes (0 + s_0 + s_1 ..., the
@@ -1531,6 +1647,7 @@ int charm_gpu_adapt_upload(charm_gpu_handle_t h, const charm_gpu_adapt_plan_t *p
     CfgLease lease(h);
     int rc = check_ready(h);
     if (rc) return rc;
+    if (h->hex) return fail(CHARM_GPU_ENOTSUP, "adapt projection: box meshes only");
     h->dt_next_valid = false;
     if (!plan || !mesh || (plan->n_pass > 0 && (!plan->n_out || !plan->map))) return fail(CHARM_GPU_EINVAL, "null argument");
     if (h->nb != CHARM_GPU_BASIS) return fail(CHARM_GPU_ENOTSUP, "adapt projection: p1 only");
@@ -1743,6 +1860,7 @@ int charm_gpu_refine_flags(charm_gpu_handle_t h, double max_err, int8_t *flags, 
     int rc = check_ready(h);
     if (rc) return rc;
     if (h->nb != CHARM_GPU_BASIS) return fail(CHARM_GPU_ENOTSUP, "refine flags: p1 only");
+    if (h->hex) return fail(CHARM_GPU_ENOTSUP, "refine flags: box meshes only");
     if (!flags && !grad_out) return fail(CHARM_GPU_EINVAL, "null argument");
     if (h->cfg.precision == CHARM_GPU_PREC_MIXED && (rc = ff_convert(h, false))) return rc;   // d_u <- hi + lo
     // the gradient goes through the (idle) slot buffer: 3*E doubles fit in it

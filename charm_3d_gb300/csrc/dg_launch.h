@@ -74,6 +74,49 @@ void dw_launch_cell(const MeshDev &m, const double *u, const dw *slots, const do
                     const double *dt_dev, double a_new, double a_old, int mode, unsigned *err, const double *radd,
                     unsigned long long *dt_next, double cfl, cudaStream_t st);
 
+// ---- general hexahedra (charm_hex.cu) -----------------------------------------
+
+// element geometry planes [kHexG][E] and face geometry planes [kHexF][F + Fb]
+// (dg_hex.cuh describes them)
+enum {
+    kGc = 0,        // centre x, y, z
+    kGdh = 3,       // dh x, y, z
+    kGvol = 6,      // volume (sum of gw*gj)
+    kGphi = 7,      // phi_1..3 at cell point q: kGphi + 3 q + (k - 1)
+    kGw = 31,       // gw*gj at cell point q
+    kGminv = 39,    // inverse mass matrix, row-major 4x4
+    kGmean = 55,    // quadrature mean of phi_1..3 (over the volume)
+    kGvert = 58,    // phi_1..3 at corner k: kGvert + 3 k + (k' - 1)
+    kGnrm = 82,     // outward unit normal of face f: kGnrm + 3 f + d
+    kHexG = 100
+};
+enum { kFn = 0, kFgp = 3, kFw = 21, kHexF = 27 };
+
+struct HexDev {
+    const double *g;          // [kHexG][E]
+    const double *fg;         // [kHexF][F + Fb]
+    const int8_t *face_face;  // [2][F]
+    const double *vert;       // [24][E]: corner k coordinate d at (3 k + d)
+};
+
+cudaError_t hex_upload_cfg(const DevCfg *cfg, cudaStream_t st);
+// element and face geometry tables of dg_hex.cuh from the corners (x.vert)
+// and face numbers (x.face_face); err: kErrNegative for a non-positive Jacobian
+cudaError_t hex_launch_geom(const MeshDev &m, const HexDev &x, double *g, double *fg, unsigned *err, cudaStream_t st);
+template <int NC>
+void hex_launch_face(int flux, const MeshDev &m, const HexDev &x, const double *u, double *slots, unsigned *err,
+                     cudaStream_t st);
+template <int NC>
+void hex_launch_cell(const MeshDev &m, const HexDev &x, const double *u, const double *slots, const double *u0,
+                     double *out, double dt, const double *dt_dev, double a_new, double a_old, int mode, unsigned *err,
+                     unsigned long long *dt_next, double cfl, cudaStream_t st);
+template <int NC>
+void hex_launch_limit(const MeshDev &m, const HexDev &x, const double *ua, const double *u0, double *out, double a_new,
+                      double a_old, unsigned long long *dt_next, double cfl, cudaStream_t st);
+template <int NC>
+void hex_launch_cfl(const MeshDev &m, const HexDev &x, const double *u, unsigned long long *dt, double cfl,
+                    cudaStream_t st);
+
 // ---- point fluxes (charm_point.cu) ------------------------------------------
 
 // Upload cfg to the unit's constants, then q[i] = flux between the state

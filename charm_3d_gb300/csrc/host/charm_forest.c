@@ -11,6 +11,7 @@
  */
 #define _POSIX_C_SOURCE 200809L
 #include "charm_forest.h"
+#include "charm_conn.h"
 
 #include <pthread.h>
 #include <stdint.h>
@@ -108,6 +109,16 @@ void charm_forest_free(charm_forest_t *f)
 {
     free(f->leaf);
     memset(f, 0, sizeof(*f));
+}
+
+int charm_forest_init_conn(charm_forest_t *f, const charm_conn_t *conn, int level)
+{
+    if (!conn || conn->n_tree < 1) return -1;
+    const int32_t ntree[3] = {conn->n_tree, 1, 1};
+    const double one[3] = {1.0, 1.0, 1.0};
+    if (charm_forest_init_uniform(f, ntree, NULL, NULL, one, level)) return -1;
+    f->conn = conn;
+    return 0;
 }
 
 int charm_forest_copy(charm_forest_t *dst, const charm_forest_t *src)
@@ -320,9 +331,60 @@ void charm_forest_face_neighbor(const charm_forest_t *f, int64_t i, int face, ch
     charm_forest_face_neighbor_k(f, NULL, i, face, nb);
 }
 
+/* Face neighbours across a tree face of an unstructured connectivity: the
+ * exterior boxes (the same-size neighbour, or the four half-size boxes on
+ * the face) are mapped into the neighbour tree and located there. */
+static void face_neighbor_conn(const charm_forest_t *f, const uint64_t *keys, int64_t i, int face,
+                               charm_face_nb_t *nb)
+{
+    const charm_leaf_t *q = &f->leaf[i];
+    const int d = face / 2, up = face & 1;
+    const int32_t len = CHARM_FOREST_QLEN(q->level);
+    int32_t p[3] = {q->x, q->y, q->z};
+    p[d] += up ? len : -len;
+    nb->wrap = 0;
+    nb->idx[0] = nb->idx[1] = nb->idx[2] = nb->idx[3] = -1;
+    int32_t t = q->tree, r[3];
+    if (p[d] >= 0 && p[d] < CHARM_FOREST_ROOT_LEN) {
+        nb->nface = face ^ 1;
+        r[0] = p[0]; r[1] = p[1]; r[2] = p[2];
+    } else {
+        const int32_t u = charm_conn_map_box(f->conn, t, face, p, len, r);
+        if (u < 0) { nb->kind = CHARM_NB_BOUNDARY; nb->nface = -1; return; }
+        nb->nface = f->conn->t2f[6 * (size_t) t + (size_t) face];
+        t = u;
+    }
+    const int64_t j = charm_forest_find_k(f, keys, t, r[0], r[1], r[2]);
+    const charm_leaf_t *n = &f->leaf[j];
+    if (n->level == q->level) { nb->kind = CHARM_NB_SAME; nb->idx[0] = j; return; }
+    if (n->level < q->level) {
+        nb->kind = (n->level == q->level - 1) ? CHARM_NB_BIGGER : CHARM_NB_UNBALANCED;
+        nb->idx[0] = j;
+        return;
+    }
+    /* the four half-size boxes on our face, in our tangential order */
+    const int s = (d == 0) ? 1 : 0, tt = (d == 2) ? 1 : 2;
+    const int32_t h = len / 2;
+    nb->kind = CHARM_NB_SMALLER;
+    for (int k = 0; k < 4; k++) {
+        int32_t c[3] = {p[0], p[1], p[2]}, m[3];
+        if (!up) c[d] += h;
+        c[s] += (k & 1) ? h : 0;
+        c[tt] += (k & 2) ? h : 0;
+        int32_t tk = q->tree;
+        if (c[d] >= 0 && c[d] < CHARM_FOREST_ROOT_LEN) { m[0] = c[0]; m[1] = c[1]; m[2] = c[2]; }
+        else tk = charm_conn_map_box(f->conn, q->tree, face, c, h, m);
+        const int64_t mk = charm_forest_find_k(f, keys, tk, m[0], m[1], m[2]);
+        nb->idx[k] = mk;
+        if (f->leaf[mk].level != q->level + 1) nb->kind = CHARM_NB_UNBALANCED;
+    }
+}
+
 void charm_forest_face_neighbor_k(const charm_forest_t *f, const uint64_t *keys, int64_t i, int face,
                                   charm_face_nb_t *nb)
 {
+    if (f->conn) { face_neighbor_conn(f, keys, i, face, nb); return; }
+    nb->nface = face ^ 1;
     const charm_leaf_t *q = &f->leaf[i];
     int d = face / 2, up = face & 1;
     int32_t len = CHARM_FOREST_QLEN(q->level);

@@ -40,6 +40,8 @@ typedef struct charm_leaf {
     int8_t  level;
 } charm_leaf_t;
 
+struct charm_conn;
+
 typedef struct charm_forest {
     int32_t ntree[3];        /* trees per axis */
     int32_t periodic[3];     /* wrap flags per axis */
@@ -48,6 +50,11 @@ typedef struct charm_forest {
     int64_t n;               /* number of leaves */
     int64_t cap;
     charm_leaf_t *leaf;      /* sorted by (tree, Morton(x,y,z)) */
+    /* unstructured hexahedral connectivity (charm_conn.h), or NULL for the
+     * brick: with it, ntree = {n_tree, 1, 1}, no periodic wrap, and a face
+     * neighbour across a tree face is found through the connectivity's
+     * coordinate map (not owned by the forest) */
+    const struct charm_conn *conn;
 } charm_forest_t;
 
 /* Kinds of face-neighbour relations, seen from one leaf. */
@@ -63,6 +70,7 @@ typedef struct charm_face_nb {
     int kind;
     int64_t idx[4];          /* neighbour leaf indices (1 or 4 used) */
     int wrap;                /* -1/0/+1: periodic wrap across the face */
+    int nface;               /* the neighbours' face on this face (face ^ 1 inside a tree and in a brick) */
 } charm_face_nb_t;
 
 /* Replace callback: n_out old leaves (indices into the old array) were
@@ -78,6 +86,10 @@ typedef int (*charm_forest_coarsen_fn)(void *user, const charm_leaf_t *leaves, c
 int  charm_forest_init_uniform(charm_forest_t *f, const int32_t ntree[3], const int32_t periodic[3],
                                const double origin[3], const double tree_len[3], int level);
 void charm_forest_free(charm_forest_t *f);
+
+/* Every tree of an unstructured connectivity refined uniformly to `level`;
+ * the forest keeps a pointer to conn, which must outlive it. */
+int  charm_forest_init_conn(charm_forest_t *f, const struct charm_conn *conn, int level);
 int  charm_forest_copy(charm_forest_t *dst, const charm_forest_t *src);
 
 /* Index of the leaf containing tree-local point (x,y,z) of tree t, or -1. */

@@ -15,11 +15,14 @@
  * src/charm_connectivity.c:457-466) are full faces with the wrap bit set.
  */
 #include "charm_gpu.h"
+#include "charm_conn.h"
 #include "charm_forest.h"
 
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+
+void charm_internal_set_error(const char *msg);   /* the library's last-error text (charm_gpu.cu) */
 
 struct charm_host_forest_s {
     charm_forest_t f;
@@ -39,14 +42,22 @@ struct charm_host_forest_s {
     int8_t  *bface_face;
     int8_t  *bface_bnd;
     int64_t  n_face, n_bface;
+    /* unstructured hexahedral mesh: the connectivity the forest points to,
+     * the boundary index of every tree face, and the flattened geometry */
+    charm_conn_t *conn;
+    int8_t  *tree_bnd;      /* [n_tree][6], -1 where a tree face has a neighbour */
+    double  *hex_vertex;    /* [8][3][E] */
+    int8_t  *hex_face_face; /* [2][n_face] */
 };
 
 static void free_flat(struct charm_host_forest_s *h)
 {
     free(h->center); free(h->level); free(h->face_elem); free(h->face_info);
     free(h->bface_elem); free(h->bface_face); free(h->bface_bnd);
+    free(h->hex_vertex); free(h->hex_face_face);
     h->center = NULL; h->level = NULL; h->face_elem = NULL; h->face_info = NULL;
     h->bface_elem = NULL; h->bface_face = NULL; h->bface_bnd = NULL;
+    h->hex_vertex = NULL; h->hex_face_face = NULL;
     h->n_face = h->n_bface = 0;
 }
 
@@ -80,6 +91,8 @@ int charm_host_forest_free(charm_host_forest_t h)
     free(h->plan_nout);
     free(h->state);
     charm_forest_free(&h->f);
+    if (h->conn) { charm_conn_free(h->conn); free(h->conn); }
+    free(h->tree_bnd);
     free(h);
     return CHARM_GPU_OK;
 }
@@ -100,6 +113,7 @@ int charm_host_forest_write_vtu(charm_host_forest_t h, const char *path, int n_f
                                 const double *fields)
 {
     if (!h || !path || n_fields < 0 || (n_fields > 0 && (!names || !fields))) return CHARM_GPU_EINVAL;
+    if (h->conn) return CHARM_GPU_ENOTSUP;
     const charm_forest_t *f = &h->f;
     const int64_t E = f->n;
     FILE *fp = fopen(path, "w");
@@ -314,6 +328,7 @@ static void flat_emit_range(void *c, int64_t lo, int64_t hi)
 int charm_host_forest_flatten(charm_host_forest_t h, charm_gpu_mesh_t *mesh)
 {
     if (!h || !mesh) return CHARM_GPU_EINVAL;
+    if (h->conn) return CHARM_GPU_ENOTSUP;   /* charm_host_forest_flatten_hex */
     const charm_forest_t *f = &h->f;
     const int64_t E = f->n;
     free_flat(h);
@@ -859,6 +874,7 @@ int charm_host_forest_adapt_state(charm_host_forest_t h, const double *grad, dou
                                   int n_comp, const double *u_in, int64_t *n_new)
 {
     if (!h || !grad || !u_in || n_comp < 1 || n_comp > CHARM_GPU_MAX_COMP) return CHARM_GPU_EINVAL;
+    if (h->conn) return CHARM_GPU_ENOTSUP;   /* the projections here are the box forms */
     return adapt_core(h, grad, max_err, minlevel, maxlevel, n_comp, u_in, NULL, n_new);
 }
 
@@ -866,6 +882,7 @@ int charm_host_forest_adapt_plan(charm_host_forest_t h, const double *grad, cons
                                  int minlevel, int maxlevel, int64_t *n_new, charm_gpu_adapt_plan_t *plan)
 {
     if (!h || !grad || !rho) return CHARM_GPU_EINVAL;
+    if (h->conn) return CHARM_GPU_ENOTSUP;
     int rc = adapt_core(h, grad, max_err, minlevel, maxlevel, 1, NULL, rho, n_new);
     if (rc) return rc;
     if (plan) {
@@ -882,5 +899,250 @@ int charm_host_forest_state(charm_host_forest_t h, const double **u_out)
     if (!h || !u_out) return CHARM_GPU_EINVAL;
     if (!h->state) return CHARM_GPU_ESTATE;
     *u_out = h->state;
+    return CHARM_GPU_OK;
+}
+
+/* ---- unstructured hexahedral meshes ------------------------------------------ */
+
+static int new_conn_forest(charm_host_forest_t *out, charm_conn_t *conn, int8_t *tree_bnd, int level)
+{
+    struct charm_host_forest_s *h = (struct charm_host_forest_s *) calloc(1, sizeof(*h));
+    if (!h) { charm_conn_free(conn); free(conn); free(tree_bnd); return CHARM_GPU_ENOMEM; }
+    h->conn = conn;
+    h->tree_bnd = tree_bnd;
+    if (charm_forest_init_conn(&h->f, conn, level)) { charm_host_forest_free(h); return CHARM_GPU_EINVAL; }
+    *out = h;
+    return CHARM_GPU_OK;
+}
+
+int charm_host_forest_new_hex(charm_host_forest_t *out, int32_t n_vert, const double *vert, int32_t n_tree,
+                              const int32_t *t2v, const int8_t *tree_bnd, int level)
+{
+    if (!out || !vert || !t2v || !tree_bnd || n_vert <= 0 || n_tree <= 0) return CHARM_GPU_EINVAL;
+    charm_conn_t *c = (charm_conn_t *) calloc(1, sizeof(*c));
+    int8_t *tb = (int8_t *) malloc(6 * (size_t) n_tree);
+    if (!c || !tb) { free(c); free(tb); return CHARM_GPU_ENOMEM; }
+    char err[256];
+    if (charm_conn_build(c, n_vert, vert, n_tree, t2v, err, (int) sizeof(err))) {
+        free(c); free(tb);
+        charm_internal_set_error(err);
+        return CHARM_GPU_EINVAL;
+    }
+    for (size_t k = 0; k < 6 * (size_t) n_tree; k++) {
+        tb[k] = (c->t2t[k] < 0) ? tree_bnd[k] : (int8_t) -1;
+        if (c->t2t[k] < 0 && tb[k] < 0) {
+            charm_conn_free(c); free(c); free(tb);
+            charm_internal_set_error("boundary tree face without a boundary index");
+            return CHARM_GPU_EINVAL;
+        }
+    }
+    return new_conn_forest(out, c, tb, level);
+}
+
+int charm_host_forest_new_gmsh(charm_host_forest_t *out, const char *path, int level, int n_bnd,
+                               const char *const *bnd_names)
+{
+    if (!out || !path || n_bnd < 0 || (n_bnd > 0 && !bnd_names)) return CHARM_GPU_EINVAL;
+    charm_conn_t *c = (charm_conn_t *) calloc(1, sizeof(*c));
+    if (!c) return CHARM_GPU_ENOMEM;
+    char err[512];
+    if (charm_conn_read_gmsh(c, path, err, (int) sizeof(err))) {
+        free(c);
+        charm_internal_set_error(err);
+        return CHARM_GPU_EINVAL;
+    }
+    int8_t *tb = (int8_t *) malloc(6 * (size_t) c->n_tree);
+    if (!tb) { charm_conn_free(c); free(c); return CHARM_GPU_ENOMEM; }
+    /* a boundary face takes the configured boundary of its patch's physical
+     * name (charm_conn_bnd_find_by_id, src/charm_connectivity.c:176-203) */
+    for (size_t k = 0; k < 6 * (size_t) c->n_tree; k++) {
+        tb[k] = -1;
+        if (c->t2t[k] >= 0) continue;
+        const char *name = (c->bnd_tag[k] >= 0) ? charm_conn_patch_name(c, 2, c->bnd_tag[k]) : NULL;
+        for (int b = 0; name && b < n_bnd; b++)
+            if (bnd_names[b] && !strcmp(bnd_names[b], name)) { tb[k] = (int8_t) b; break; }
+        if (tb[k] < 0) {
+            snprintf(err, sizeof(err), "%s: tree %lld face %d: %s%s%s", path, (long long) (k / 6), (int) (k % 6),
+                     name ? "patch '" : "boundary face without a physical quadrangle",
+                     name ? name : "", name ? "' is not a configured boundary" : "");
+            charm_conn_free(c); free(c); free(tb);
+            charm_internal_set_error(err);
+            return CHARM_GPU_EINVAL;
+        }
+    }
+    return new_conn_forest(out, c, tb, level);
+}
+
+int charm_host_forest_tree_count(charm_host_forest_t h)
+{
+    if (!h) return -1;
+    return h->conn ? h->conn->n_tree : h->f.ntree[0] * h->f.ntree[1] * h->f.ntree[2];
+}
+
+int charm_host_forest_tree_region(charm_host_forest_t h, int32_t *reg_tag)
+{
+    if (!h || !reg_tag) return CHARM_GPU_EINVAL;
+    if (!h->conn) return CHARM_GPU_ENOTSUP;
+    memcpy(reg_tag, h->conn->reg_tag, sizeof(int32_t) * (size_t) h->conn->n_tree);
+    return CHARM_GPU_OK;
+}
+
+/* Side 0 of a face between two leaves: inside a tree the leaf at the lower
+ * coordinate (its face is odd), across a tree face the leaf of the lower
+ * tree, as p4est_iterate visits a tree face from its lower tree. */
+static int is_side0(const charm_forest_t *f, int64_t i, int face, int64_t j)
+{
+    const int32_t ti = f->leaf[i].tree, tj = f->leaf[j].tree;
+    if (ti != tj) return ti < tj;
+    return face & 1;
+}
+
+typedef struct {
+    struct charm_host_forest_s *h;
+    const charm_face_nb_t *nbs;
+    int64_t E, nf;
+    int64_t *cnt;        /* [2][E]: interior records, boundary records; then offsets */
+} hex_ctx_t;
+
+static void hex_count_range(void *c, int64_t lo, int64_t hi)
+{
+    const hex_ctx_t *x = (const hex_ctx_t *) c;
+    const charm_forest_t *f = &x->h->f;
+    for (int64_t i = lo; i < hi; i++) {
+        int64_t ni = 0, nb = 0;
+        for (int face = 0; face < 6; face++) {
+            const charm_face_nb_t *n = &x->nbs[6 * i + face];
+            switch (n->kind) {
+            case CHARM_NB_BOUNDARY: nb++; break;
+            case CHARM_NB_SAME: if (is_side0(f, i, face, n->idx[0])) ni++; break;
+            case CHARM_NB_SMALLER: ni += 4; break;
+            case CHARM_NB_BIGGER: break;
+            default: nb = -1000000; break;
+            }
+        }
+        x->cnt[i] = ni;
+        x->cnt[x->E + i] = nb;
+    }
+}
+
+static void hex_emit_range(void *c, int64_t lo, int64_t hi)
+{
+    const hex_ctx_t *x = (const hex_ctx_t *) c;
+    struct charm_host_forest_s *h = x->h;
+    const charm_forest_t *f = &h->f;
+    const int64_t E = x->E, nf = x->nf;
+    const double inv = 1.0 / (double) CHARM_FOREST_ROOT_LEN;
+    for (int64_t i = lo; i < hi; i++) {
+        const charm_leaf_t *q = &f->leaf[i];
+        const int32_t len = CHARM_FOREST_QLEN(q->level);
+        /* corners by the tree's trilinear map (charm_quad_get_vertices,
+         * src/charm_geom.c:12-31), centre at the quadrant's middle
+         * (_charm_quad_calc_center, :33-37) */
+        for (int k = 0; k < 8; k++) {
+            double v[3];
+            charm_conn_point(h->conn, q->tree, (double) (q->x + ((k & 1) ? len : 0)) * inv,
+                             (double) (q->y + ((k & 2) ? len : 0)) * inv, (double) (q->z + ((k & 4) ? len : 0)) * inv, v);
+            for (int d = 0; d < 3; d++) h->hex_vertex[(int64_t) (3 * k + d) * E + i] = v[d];
+        }
+        double cc[3];
+        charm_conn_point(h->conn, q->tree, ((double) q->x + 0.5 * len) * inv, ((double) q->y + 0.5 * len) * inv,
+                         ((double) q->z + 0.5 * len) * inv, cc);
+        h->center[i] = cc[0]; h->center[E + i] = cc[1]; h->center[2 * E + i] = cc[2];
+        h->level[i] = q->level;
+        int64_t k = x->cnt[i];
+        for (int face = 0; face < 6; face++) {
+            const charm_face_nb_t *n = &x->nbs[6 * i + face];
+            if (n->kind == CHARM_NB_SAME && is_side0(f, i, face, n->idx[0])) {
+                h->face_elem[k] = (int32_t) i;
+                h->face_elem[nf + k] = (int32_t) n->idx[0];
+                h->face_info[k] = (uint8_t) (face / 2);
+                h->hex_face_face[k] = (int8_t) face;
+                h->hex_face_face[nf + k] = (int8_t) n->nface;
+                k++;
+            } else if (n->kind == CHARM_NB_SMALLER) {
+                const int big0 = is_side0(f, i, face, n->idx[0]);
+                for (int j = 0; j < 4; j++) {
+                    const int32_t a = big0 ? (int32_t) i : (int32_t) n->idx[j];
+                    const int32_t b = big0 ? (int32_t) n->idx[j] : (int32_t) i;
+                    h->face_elem[k] = a;
+                    h->face_elem[nf + k] = b;
+                    h->face_info[k] = (uint8_t) (((big0 ? face : n->nface) / 2) | ((big0 ? 2 : 1) << 2) | (j << 4));
+                    h->hex_face_face[k] = (int8_t) (big0 ? face : n->nface);
+                    h->hex_face_face[nf + k] = (int8_t) (big0 ? n->nface : face);
+                    k++;
+                }
+            }
+        }
+        int64_t kb = x->cnt[E + i];
+        for (int face = 0; face < 6; face++) {
+            if (x->nbs[6 * i + face].kind == CHARM_NB_BOUNDARY) {
+                h->bface_elem[kb] = (int32_t) i;
+                h->bface_face[kb] = (int8_t) face;
+                h->bface_bnd[kb] = h->tree_bnd[6 * (int64_t) q->tree + face];
+                kb++;
+            }
+        }
+    }
+}
+
+int charm_host_forest_flatten_hex(charm_host_forest_t h, charm_gpu_mesh_t *mesh, charm_gpu_hex_t *hex)
+{
+    if (!h || !mesh || !hex) return CHARM_GPU_EINVAL;
+    if (!h->conn) return CHARM_GPU_ENOTSUP;
+    const charm_forest_t *f = &h->f;
+    const int64_t E = f->n;
+    free_flat(h);
+    uint64_t *keys = (uint64_t *) malloc(sizeof(uint64_t) * (size_t) (E > 0 ? E : 1));
+    charm_face_nb_t *nbs = (charm_face_nb_t *) malloc(sizeof(charm_face_nb_t) * (size_t) (6 * (E > 0 ? E : 1)));
+    int64_t *cnt = (int64_t *) malloc(sizeof(int64_t) * (size_t) (2 * (E > 0 ? E : 1)));
+    if (!keys || !nbs || !cnt) { free(keys); free(nbs); free(cnt); return CHARM_GPU_ENOMEM; }
+    charm_forest_keys(f, keys);
+    nbs_ctx_t nc = {f, keys, nbs};
+    charm_forest_parallel_for_min(E, 256, nbs_range, &nc);
+    free(keys);
+    hex_ctx_t hc = {h, nbs, E, 0, cnt};
+    charm_forest_parallel_for(E, hex_count_range, &hc);
+    int64_t nf = 0, nb = 0;
+    for (int64_t i = 0; i < E; i++) {
+        const int64_t a = cnt[i], b = cnt[E + i];
+        if (b < 0) { free(nbs); free(cnt); return CHARM_GPU_EINVAL; }   /* not 2:1 balanced */
+        cnt[i] = nf; nf += a;
+        cnt[E + i] = nb; nb += b;
+    }
+    h->center = (double *) malloc((size_t) (3 * (E > 0 ? E : 1)) * sizeof(double));
+    h->level = (int8_t *) malloc((size_t) (E > 0 ? E : 1));
+    h->face_elem = (int32_t *) malloc((size_t) (2 * (nf > 0 ? nf : 1)) * sizeof(int32_t));
+    h->face_info = (uint8_t *) malloc((size_t) (nf > 0 ? nf : 1));
+    h->bface_elem = (int32_t *) malloc((size_t) (nb > 0 ? nb : 1) * sizeof(int32_t));
+    h->bface_face = (int8_t *) malloc((size_t) (nb > 0 ? nb : 1));
+    h->bface_bnd = (int8_t *) malloc((size_t) (nb > 0 ? nb : 1));
+    h->hex_vertex = (double *) malloc((size_t) (24 * (E > 0 ? E : 1)) * sizeof(double));
+    h->hex_face_face = (int8_t *) malloc((size_t) (2 * (nf > 0 ? nf : 1)));
+    if (!h->center || !h->level || !h->face_elem || !h->face_info || !h->bface_elem || !h->bface_face ||
+        !h->bface_bnd || !h->hex_vertex || !h->hex_face_face) {
+        free_flat(h);
+        free(nbs);
+        free(cnt);
+        return CHARM_GPU_ENOMEM;
+    }
+    hc.nf = nf;
+    charm_forest_parallel_for(E, hex_emit_range, &hc);
+    free(nbs);
+    free(cnt);
+    h->n_face = nf;
+    h->n_bface = nb;
+    mesh->n_elem = E;
+    mesh->center = h->center;
+    mesh->level = h->level;
+    for (int d = 0; d < 3; d++) mesh->tree_len[d] = 1.0;
+    mesh->n_face = nf;
+    mesh->face_elem = h->face_elem;
+    mesh->face_info = h->face_info;
+    mesh->n_bface = nb;
+    mesh->bface_elem = h->bface_elem;
+    mesh->bface_face = h->bface_face;
+    mesh->bface_bnd = h->bface_bnd;
+    hex->vertex = h->hex_vertex;
+    hex->face_face = h->hex_face_face;
     return CHARM_GPU_OK;
 }

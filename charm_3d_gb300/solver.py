@@ -19,7 +19,7 @@ from .case import Case
 class MeshArrays:
     """Owned numpy copies of a flattened mesh plus the ctypes view of them."""
 
-    def __init__(self, m: abi.Mesh):
+    def __init__(self, m: abi.Mesh, hex: abi.Hex | None = None):
         E, F, Fb = m.n_elem, m.n_face, m.n_bface
         self.n_elem, self.n_face, self.n_bface = E, F, Fb
         self.tree_len = tuple(m.tree_len)
@@ -30,7 +30,26 @@ class MeshArrays:
         self.bface_elem = np.ctypeslib.as_array(m.bface_elem, (Fb,)).copy() if Fb else np.zeros(0, np.int32)
         self.bface_face = np.ctypeslib.as_array(m.bface_face, (Fb,)).copy() if Fb else np.zeros(0, np.int8)
         self.bface_bnd = np.ctypeslib.as_array(m.bface_bnd, (Fb,)).copy() if Fb else np.zeros(0, np.int8)
+        # general hexahedra: corners [8][3][E] (p4est corner order) and the
+        # face numbers of both sides of every interior record [2][F]
+        self.vertex = self.face_face = None
+        if hex is not None:
+            self.vertex = np.ctypeslib.as_array(hex.vertex, (24 * E,)).reshape(8, 3, E).copy()
+            self.face_face = (np.ctypeslib.as_array(hex.face_face, (2 * F,)).reshape(2, F).copy() if F
+                              else np.zeros((2, 0), np.int8))
         self._struct = None
+
+    @property
+    def is_hex(self) -> bool:
+        return self.vertex is not None
+
+    def hex_struct(self) -> abi.Hex:
+        x = abi.Hex()
+        self._keep_hex = [np.ascontiguousarray(self.vertex, dtype=np.float64),
+                          np.ascontiguousarray(self.face_face, dtype=np.int8)]
+        x.vertex = abi.ptr(self._keep_hex[0])
+        x.face_face = abi.ptr(self._keep_hex[1], C.c_int8)
+        return x
 
     def struct(self) -> abi.Mesh:
         m = abi.Mesh()
@@ -52,7 +71,46 @@ class MeshArrays:
 
 
 class Forest:
-    """The CPU octree of a brick case (charm_host_forest_* in the C ABI)."""
+    """The CPU octree (charm_host_forest_* in the C ABI): a brick of cubic
+    trees for a Case, or one tree per hexahedron of an unstructured mesh
+    (Forest.from_gmsh, Forest.from_hex)."""
+
+    hex = False
+
+    @classmethod
+    def from_gmsh(cls, path: str, level: int, bnd_names: list[str]) -> "Forest":
+        """Forest over a gmsh 2.x hexahedral mesh; boundary patches bind to
+        bnd_names[k] (the configuration's boundary k) by physical name."""
+        self = cls.__new__(cls)
+        self.lib = abi.load()
+        self.h = C.c_void_p()
+        self.hex = True
+        arr = (C.c_char_p * max(1, len(bnd_names)))(*[n.encode() for n in bnd_names])
+        abi.check(self.lib.charm_host_forest_new_gmsh(C.byref(self.h), str(path).encode(), level, len(bnd_names), arr),
+                  "charm_host_forest_new_gmsh")
+        return self
+
+    @classmethod
+    def from_hex(cls, vert: np.ndarray, t2v: np.ndarray, tree_bnd: np.ndarray, level: int) -> "Forest":
+        """Forest over hexahedra given by vertices [n][3] and corner lists
+        [T][8] (p4est order); tree_bnd [T][6]: boundary index of each tree
+        face without a neighbour."""
+        self = cls.__new__(cls)
+        self.lib = abi.load()
+        self.h = C.c_void_p()
+        self.hex = True
+        v = np.ascontiguousarray(vert, dtype=np.float64)
+        t = np.ascontiguousarray(t2v, dtype=np.int32)
+        b = np.ascontiguousarray(tree_bnd, dtype=np.int8)
+        abi.check(self.lib.charm_host_forest_new_hex(C.byref(self.h), len(v), v.ctypes.data, len(t), t.ctypes.data,
+                                                     b.ctypes.data, level), "charm_host_forest_new_hex")
+        return self
+
+    def tree_regions(self) -> np.ndarray:
+        n = int(self.lib.charm_host_forest_tree_count(self.h))
+        r = np.empty(n, np.int32)
+        abi.check(self.lib.charm_host_forest_tree_region(self.h, r.ctypes.data), "charm_host_forest_tree_region")
+        return r
 
     def __init__(self, case: Case, level: int | None = None):
         self.lib = abi.load()
@@ -83,6 +141,11 @@ class Forest:
 
     def flatten(self) -> MeshArrays:
         m = abi.Mesh()
+        if self.hex:
+            x = abi.Hex()
+            abi.check(self.lib.charm_host_forest_flatten_hex(self.h, C.byref(m), C.byref(x)),
+                      "charm_host_forest_flatten_hex")
+            return MeshArrays(m, x)
         abi.check(self.lib.charm_host_forest_flatten(self.h, C.byref(m)), "charm_host_forest_flatten")
         return MeshArrays(m)
 
@@ -162,7 +225,11 @@ class Solver:
     def upload(self, mesh: MeshArrays) -> None:
         self.mesh = mesh
         s = mesh.struct()
-        abi.check(self.lib.charm_gpu_upload_mesh(self.h, C.byref(s)), "charm_gpu_upload_mesh")
+        if mesh.is_hex:
+            x = mesh.hex_struct()
+            abi.check(self.lib.charm_gpu_upload_mesh_hex(self.h, C.byref(s), C.byref(x)), "charm_gpu_upload_mesh_hex")
+        else:
+            abi.check(self.lib.charm_gpu_upload_mesh(self.h, C.byref(s)), "charm_gpu_upload_mesh")
         self.n_elem = mesh.n_elem
 
     def shape(self) -> tuple[int, int, int]:

@@ -162,6 +162,26 @@ typedef struct charm_gpu_mesh {
     const int8_t  *bface_bnd;   /* [n_bface] index into charm_gpu_config_t.bnd */
 } charm_gpu_mesh_t;
 
+/*
+ * General (trilinear) hexahedra: the leaves of a forest over an unstructured
+ * hexahedral mesh (one tree per hexahedron of a gmsh file, reference
+ * src/charm_connectivity.c:315-519), mapped into space through each tree's
+ * corner vertices (p4est_qcoord_to_vertex, as src/charm_geom.c:12-31 uses
+ * it).  With a mesh of such elements, charm_gpu_mesh_t's center holds the
+ * element centres (informative), level and tree_len are not used, face_info
+ * keeps its kind and sub bits (dir: side 0's face / 2), and for every
+ * interior face record the faces of both sides are given here; quadrature
+ * points, weights, normals, the Taylor basis centre and scale and the mass
+ * matrix of every element are computed from the corners as the reference
+ * computes them (charm_geom_quad_calc, src/charm_geom.c:496-530).
+ */
+typedef struct charm_gpu_hex {
+    const double *vertex;      /* [8][3][n_elem]: corner k (p4est order, k = ix + 2 iy + 4 iz),
+                                  coordinate d of element e at vertex[(3 k + d) n_elem + e] */
+    const int8_t *face_face;   /* [2][n_face]: face number (0..5) of interior face record i on
+                                  side 0 (face_face[i]) and side 1 (face_face[n_face + i]) */
+} charm_gpu_hex_t;
+
 typedef struct charm_gpu_handle_s *charm_gpu_handle_t;
 
 /* Library version and the text of the last error on this thread. */
@@ -179,6 +199,14 @@ int charm_gpu_destroy(charm_gpu_handle_t h);
  * CHARM_GPU_EINVAL before anything changes: the previous mesh and state
  * stay as they were. */
 int charm_gpu_upload_mesh(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh);
+
+/* Upload a mesh of general hexahedra (see charm_gpu_hex_t); otherwise as
+ * charm_gpu_upload_mesh, with the same record checks, and also
+ * CHARM_GPU_EINVAL for an element whose corners give a non-positive
+ * Jacobian at a quadrature point (the reference asserts gj != 0,
+ * src/charm_geom.c:124).  FP64, p1, convective terms: CHARM_GPU_ENOTSUP for
+ * the mixed and double-word forms, p2, viscous terms and chemistry. */
+int charm_gpu_upload_mesh_hex(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh, const charm_gpu_hex_t *hex);
 
 /* State in/out, layout [V][B][E] (reference charm_data_t.par.c,
  * include/charm_globals.h:329-338).  `on_device` != 0: `u` is a device pointer. */
@@ -439,6 +467,39 @@ int charm_host_forest_new(charm_host_forest_t *f, const int32_t ntree[3], const 
                           const double origin[3], const double tree_len[3], int level);
 int charm_host_forest_free(charm_host_forest_t f);
 int64_t charm_host_forest_count(charm_host_forest_t f);
+
+/* Forest over an unstructured hexahedral mesh, one tree per hexahedron,
+ * uniform `level` (the reference's charm_conn_reader_msh +
+ * p4est_connectivity_complete + p4est_new_ext, src/charm_connectivity.c:315-519,
+ * src/charm_3d.c:36).  From arrays: n_vert vertices [3], n_tree hexahedra
+ * with their corner vertices in p4est order [8], and tree_bnd [6*n_tree],
+ * the boundary index of every tree face that has no neighbour.  Tree faces
+ * are matched by their vertex sets; a face shared by more than two trees
+ * or whose corners do not match as a square's symmetry returns
+ * CHARM_GPU_EINVAL. */
+int charm_host_forest_new_hex(charm_host_forest_t *f, int32_t n_vert, const double *vert, int32_t n_tree,
+                              const int32_t *t2v, const int8_t *tree_bnd, int level);
+
+/* The same from a gmsh 2.x ASCII file: 8-node hexahedra are the trees, and
+ * 4-node quadrangles name boundary faces by physical tag; a boundary face
+ * takes the configured boundary whose name (bnd_names[k] for
+ * charm_gpu_config_t.bnd[k]) is its patch's physical name
+ * (charm_conn_bnd_find_by_id, src/charm_connectivity.c:176-203).  A
+ * boundary face without a quadrangle or whose name is not configured
+ * returns CHARM_GPU_EINVAL with the face in the error text. */
+int charm_host_forest_new_gmsh(charm_host_forest_t *f, const char *path, int level, int n_bnd,
+                               const char *const *bnd_names);
+
+/* Trees of the forest, and for an unstructured mesh the physical tag of
+ * each tree's hexahedron (its region). */
+int charm_host_forest_tree_count(charm_host_forest_t f);
+int charm_host_forest_tree_region(charm_host_forest_t f, int32_t *reg_tag);
+
+/* Flatten an unstructured forest (charm_host_forest_flatten is for bricks):
+ * the same records, interior faces by leaf and face (side 0: the lower
+ * coordinate inside a tree, the lower tree across a tree face), plus the
+ * corners and face numbers of charm_gpu_hex_t.  Arrays stay owned by f. */
+int charm_host_forest_flatten_hex(charm_host_forest_t f, charm_gpu_mesh_t *mesh, charm_gpu_hex_t *hex);
 
 /* Boundary id per domain side (-x,+x,-y,+y,-z,+z) used when flattening. */
 int charm_host_forest_set_bnd(charm_host_forest_t f, const int8_t bnd_of_side[6]);

@@ -94,7 +94,8 @@ def build(force: bool = False) -> dict[str, str]:
     plugin_src = os.path.join(ROOT, "charm_3d_gb300", "csrc", "plugin", "charm_model_gpu.c")
     glue_src = os.path.join(HERE, "ref_plugin_glue.c")
     ours = [os.path.join(HERE, "p4est_shim", "p4est_shim.c"), os.path.join(HERE, "ref_driver.c"),
-            os.path.join(ROOT, "charm_3d_gb300", "csrc", "host", "charm_forest.c")]
+            os.path.join(ROOT, "charm_3d_gb300", "csrc", "host", "charm_forest.c"),
+            os.path.join(ROOT, "charm_3d_gb300", "csrc", "host", "charm_conn.c")]
     deps = ours + [os.path.join(HERE, "p4est_shim", f) for f in os.listdir(os.path.join(HERE, "p4est_shim"))]
     deps += [__file__, plugin_src, glue_src]
     if not force and all(os.path.exists(p) for p in libs.values()):

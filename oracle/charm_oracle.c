@@ -53,6 +53,7 @@ typedef struct {
     double c[3], dh[3], vol;
     double qgp[NQMAX][3], qgj[NQMAX];
     double a_inv[NBMAX][NBMAX];
+    double v[8][3];                 /* corners of a general hexahedron (p4est order) */
 } elem_geom_t;
 
 typedef struct oracle {
@@ -61,6 +62,8 @@ typedef struct oracle {
     int64_t E, F, Fb;
     int V;
     elem_geom_t *g;
+    int hex;                        /* general hexahedra: geometry from the corners */
+    int8_t *face_face;              /* [2][F] face numbers of both sides (hex) */
     int32_t *face_elem;
     uint8_t *face_info;
     int32_t *bface_elem;
@@ -626,7 +629,8 @@ static void face_points(const oracle_t *o, const elem_geom_t *g, int f, double g
     }
     static const int ftv[6][4] = {{0, 2, 4, 6}, {1, 3, 5, 7}, {0, 1, 4, 5}, {2, 3, 6, 7}, {0, 1, 2, 3}, {4, 5, 6, 7}};
     double v8[8][3], v[4][3];
-    elem_vertices(g, v8);
+    if (o->hex) memcpy(v8, g->v, sizeof(v8));
+    else elem_vertices(g, v8);
     for (int i = 0; i < 4; i++)
         for (int k = 0; k < 3; k++) v[i][k] = v8[ftv[f][i]][k];
     const double a = 2.0 / 3.0, b = 1.0 / 6.0;
@@ -652,6 +656,90 @@ static void outward_normal(int f, double n[3])
 {
     n[0] = n[1] = n[2] = 0.;
     n[f / 2] = (f & 1) ? 1. : -1.;
+}
+
+/* The same on a general hexahedron: the normal of the plane through the
+ * face's first three corners (_charm_face_calc_normal, src/charm_geom.c:
+ * 181-211), turned to point from the cell centre to the face centre as the
+ * face callbacks turn it (src/models/ns/charm_model_ns_conv.c:226-241). */
+static void hex_normal(const elem_geom_t *g, int f, double n[3])
+{
+    static const int ftv[6][4] = {{0, 2, 4, 6}, {1, 3, 5, 7}, {0, 1, 4, 5}, {2, 3, 6, 7}, {0, 1, 2, 3}, {4, 5, 6, 7}};
+    double a[3], b[3], l[3];
+    for (int k = 0; k < 3; k++) {
+        a[k] = g->v[ftv[f][1]][k] - g->v[ftv[f][0]][k];
+        b[k] = g->v[ftv[f][2]][k] - g->v[ftv[f][0]][k];
+        l[k] = (g->v[ftv[f][0]][k] + g->v[ftv[f][1]][k] + g->v[ftv[f][2]][k] + g->v[ftv[f][3]][k]) / 4. - g->c[k];
+    }
+    n[0] = a[1] * b[2] - a[2] * b[1];
+    n[1] = a[2] * b[0] - a[0] * b[2];
+    n[2] = a[0] * b[1] - a[1] * b[0];
+    const double nl = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    for (int k = 0; k < 3; k++) n[k] /= nl;
+    if (n[0] * l[0] + n[1] * l[1] + n[2] * l[2] < 0)
+        for (int k = 0; k < 3; k++) n[k] *= -1.0;
+}
+
+static void elem_normal(const oracle_t *o, int64_t e, int f, double n[3])
+{
+    if (o->hex) hex_normal(&o->g[e], f, n);
+    else outward_normal(f, n);
+}
+
+/* Geometry of a general hexahedron from its corners (charm_geom_quad_calc,
+ * src/charm_geom.c:496-530): the 8 Gauss points of the trilinear map with
+ * the determinants of its Jacobian (_charm_quad_calc_gp_at_point, :40-128),
+ * dh = the corners' bounding box (:157-169), the centre, the volume and the
+ * inverted mass matrix.  Returns -1 for a non-positive determinant. */
+static int hex_elem_geom(const oracle_t *o, elem_geom_t *g, const double v[8][3])
+{
+    const double s3 = 1. / sqrt(3.);
+    memcpy(g->v, v, sizeof(g->v));
+    const double r0[3] = {0., 0., 0.};
+    trilinear(v, r0, g->c);
+    for (int k = 0; k < 3; k++) {
+        double lo = v[0][k], hi = v[0][k];
+        for (int i = 1; i < 8; i++) {
+            if (lo > v[i][k]) lo = v[i][k];
+            if (hi < v[i][k]) hi = v[i][k];
+        }
+        g->dh[k] = hi - lo;
+    }
+    g->vol = 0.;
+    for (int q = 0; q < 8; q++) {
+        const double ref[3] = {(q & 1) ? s3 : -s3, (q & 2) ? s3 : -s3, (q & 4) ? s3 : -s3};
+        trilinear(v, ref, g->qgp[q]);
+        /* Jacobian: d/dksi, d/deta, d/dmu of the trilinear map */
+        double jac[3][3] = {{0.}};
+        for (int dir = 0; dir < 3; dir++) {
+            int vi = 0;
+            for (int iz = 0; iz < 2; iz++)
+                for (int iy = 0; iy < 2; iy++)
+                    for (int ix = 0; ix < 2; ix++) {
+                        const int idx[3] = {ix, iy, iz};
+                        double f = 1. / 8.;
+                        for (int a = 0; a < 3; a++)
+                            f *= (a == dir) ? (idx[a] ? 1. : -1.) : (idx[a] ? 1. + ref[a] : 1. - ref[a]);
+                        for (int k = 0; k < 3; k++) jac[k][dir] += f * v[vi][k];
+                        vi++;
+                    }
+        }
+        const double det = jac[0][0] * (jac[1][1] * jac[2][2] - jac[1][2] * jac[2][1]) -
+                           jac[0][1] * (jac[1][0] * jac[2][2] - jac[1][2] * jac[2][0]) +
+                           jac[0][2] * (jac[1][0] * jac[2][1] - jac[1][1] * jac[2][0]);
+        if (!(det > 0.)) return -1;
+        g->qgj[q] = det;   /* gw = 1 */
+        g->vol += det;
+    }
+    double a[NBMAX][NBMAX];
+    for (int i = 0; i < NB; i++)
+        for (int j = 0; j < NB; j++) {
+            a[i][j] = 0.;
+            for (int q = 0; q < NQ; q++)
+                a[i][j] += g->qgj[q] * base_func(g->qgp[q], i, g->c, g->dh) * base_func(g->qgp[q], j, g->c, g->dh);
+        }
+    matr_inv(NB, a, g->a_inv);
+    return 0;
 }
 
 /* ---- state helpers ---------------------------------------------------------- */
@@ -736,15 +824,21 @@ static void residual(oracle_t *o, const double *u, double *res)
         const int32_t e[2] = {o->face_elem[f], o->face_elem[o->F + f]};
         const int d = o->face_info[f] & 3, kind = (o->face_info[f] >> 2) & 3;
         double c1[3];
-        side1_center(o, f, c1);
+        if (o->hex) memcpy(c1, o->g[e[1]].c, sizeof(c1));
+        else side1_center(o, f, c1);
         const double *cs[2] = {o->g[e[0]].c, c1};
         /* points on side 0's face (conforming / side 0 small) or side 1's face */
         const int hs = (kind == 2) ? 1 : 0;
         elem_geom_t pg = o->g[e[hs]];
         memcpy(pg.c, cs[hs], sizeof(double) * 3);
         double gp[NFQMAX][3], gwj[NFQMAX], n[3];
-        face_points(o, &pg, hs ? 2 * d : 2 * d + 1, gp, gwj);
-        outward_normal(2 * d + 1, n);
+        if (o->hex) {   /* the side's own face numbers; n from side 0's face */
+            face_points(o, &pg, o->face_face[hs ? o->F + f : f], gp, gwj);
+            hex_normal(&o->g[e[0]], o->face_face[f], n);
+        } else {
+            face_points(o, &pg, hs ? 2 * d : 2 * d + 1, gp, gwj);
+            outward_normal(2 * d + 1, n);
+        }
         for (int q = 0; q < NFQ; q++) {
             prim_t pr[2];
             for (int s = 0; s < 2; s++) {
@@ -768,7 +862,7 @@ static void residual(oracle_t *o, const double *u, double *res)
         const elem_geom_t *g = &o->g[e];
         double gp[NFQMAX][3], gwj[NFQMAX], n[3];
         face_points(o, g, f, gp, gwj);
-        outward_normal(f, n);
+        elem_normal(o, e, f, n);
         for (int q = 0; q < NFQ; q++) {
             double U[MAXV];
             prim_t pr[2];
@@ -1232,7 +1326,7 @@ static void limiter(oracle_t *o, double *u)
         const int f = o->bface_face[j];
         double n[3];
         prim_t pr[2];
-        outward_normal(f, n);
+        elem_normal(o, e, f, n);
         cons_to_prim(o, &self[e * V], &pr[0]);
         bnd_cond(o, o->bface_bnd[j], &pr[0], &pr[1], n);
         prim_to_cons(o, &pr[1], &o->lim_nb[(e * 6 + f) * V]);
@@ -1241,14 +1335,15 @@ static void limiter(oracle_t *o, double *u)
     for (int64_t f = 0; f < o->F; f++) {
         const int32_t e0 = o->face_elem[f], e1 = o->face_elem[o->F + f];
         const int d = o->face_info[f] & 3, kind = (o->face_info[f] >> 2) & 3;
+        const int f0 = o->hex ? o->face_face[f] : 2 * d + 1, f1 = o->hex ? o->face_face[o->F + f] : 2 * d;
         if (kind == 0) {
-            memcpy(&o->lim_nb[(e0 * 6 + 2 * d + 1) * V], &self[e1 * V], sizeof(double) * V);
-            memcpy(&o->lim_nb[(e1 * 6 + 2 * d) * V], &self[e0 * V], sizeof(double) * V);
+            memcpy(&o->lim_nb[(e0 * 6 + f0) * V], &self[e1 * V], sizeof(double) * V);
+            memcpy(&o->lim_nb[(e1 * 6 + f1) * V], &self[e0 * V], sizeof(double) * V);
             continue;
         }
         /* hanging: each of the 4 records; the big side is done once (sub 0) */
         const int32_t small = (kind == 1) ? e0 : e1, big = (kind == 1) ? e1 : e0;
-        const int fs = (kind == 1) ? 2 * d + 1 : 2 * d, fbig = (kind == 1) ? 2 * d : 2 * d + 1;
+        const int fs = (kind == 1) ? f0 : f1, fbig = (kind == 1) ? f1 : f0;
         double cb[MAXV];
         get_fields(o, u, big, o->g[big].c, o->g[big].dh, o->g[big].c, cb);   /* value at the big centre */
         memcpy(&o->lim_nb[(small * 6 + fs) * V], cb, sizeof(double) * V);
@@ -1282,7 +1377,8 @@ static void limiter(oracle_t *o, double *u)
             }
             psi[v] = 1.;
         }
-        elem_vertices(g, v8);
+        if (o->hex) memcpy(v8, g->v, sizeof(v8));
+        else elem_vertices(g, v8);
         for (int i = 0; i < 8; i++) {
             double fv[MAXV];
             get_fields(o, u, e, g->c, g->dh, v8[i], fv);
@@ -1307,6 +1403,7 @@ void oracle_free(oracle_t *o)
 {
     if (!o) return;
     free(o->g); free(o->face_elem); free(o->face_info); free(o->bface_elem); free(o->bface_face); free(o->bface_bnd);
+    free(o->face_face);
     free(o->u); free(o->u_old); free(o->res); free(o->lim_nb); free(o->vis); free(o->dif); free(o->chem_rhs);
     free(o);
 }
@@ -1350,6 +1447,27 @@ oracle_t *oracle_new(const charm_gpu_config_t *cfg, const charm_gpu_mesh_t *m)
     memcpy(o->bface_elem, m->bface_elem, sizeof(int32_t) * (size_t) o->Fb);
     memcpy(o->bface_face, m->bface_face, (size_t) o->Fb);
     memcpy(o->bface_bnd, m->bface_bnd, (size_t) o->Fb);
+    return o;
+}
+
+/* The oracle on general hexahedra (charm_gpu_hex_t): every element's
+ * geometry from its corners; p1, convective terms.  NULL for a
+ * non-positive Jacobian or an unsupported configuration. */
+oracle_t *oracle_new_hex(const charm_gpu_config_t *cfg, const charm_gpu_mesh_t *m, const charm_gpu_hex_t *x)
+{
+    if (cfg->p_order == 2 || cfg->use_visc || cfg->n_react) return NULL;
+    oracle_t *o = oracle_new(cfg, m);
+    if (!o) return NULL;
+    o->hex = 1;
+    o->face_face = (int8_t *) malloc(2 * (size_t) (o->F + 1));
+    if (!o->face_face) { oracle_free(o); return NULL; }
+    memcpy(o->face_face, x->face_face, 2 * (size_t) o->F);
+    for (int64_t e = 0; e < o->E; e++) {
+        double v[8][3];
+        for (int k = 0; k < 8; k++)
+            for (int d = 0; d < 3; d++) v[k][d] = x->vertex[(int64_t) (3 * k + d) * o->E + e];
+        if (hex_elem_geom(o, &o->g[e], v)) { oracle_free(o); return NULL; }
+    }
     return o;
 }
 
@@ -1415,6 +1533,7 @@ int oracle_run(oracle_t *o, int nsteps, double dt)
  * boundary faces the right state is the boundary condition's ghost. */
 int oracle_amr_grad(oracle_t *o, double *grad)
 {
+    if (o->hex) return -1;   /* box meshes */
     const int64_t E = o->E;
     memset(grad, 0, sizeof(double) * 3 * (size_t) E);
     for (int64_t j = 0; j < o->Fb; j++) {   /* _charm_amr_par_calc_face_iter_bnd (:362-423) */

@@ -16,6 +16,8 @@ def load() -> C.CDLL:
         lib = C.CDLL(build_oracle.build())
         lib.oracle_new.restype = C.c_void_p
         lib.oracle_new.argtypes = [C.c_void_p, C.c_void_p]
+        lib.oracle_new_hex.restype = C.c_void_p
+        lib.oracle_new_hex.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         lib.oracle_free.argtypes = [C.c_void_p]
         for name in ("oracle_set_state", "oracle_get_state", "oracle_residual"):
             getattr(lib, name).argtypes = [C.c_void_p, C.c_void_p]
@@ -41,9 +43,13 @@ class Port:
         self.mesh = mesh
         self._m = mesh.struct()
         self.cfg = cfg
-        self.h = self.lib.oracle_new(C.addressof(cfg), C.addressof(self._m))
+        if getattr(mesh, "is_hex", False):   # general hexahedra: geometry from the corners
+            self._x = mesh.hex_struct()
+            self.h = self.lib.oracle_new_hex(C.addressof(cfg), C.addressof(self._m), C.addressof(self._x))
+        else:
+            self.h = self.lib.oracle_new(C.addressof(cfg), C.addressof(self._m))
         if not self.h:
-            raise MemoryError("oracle_new failed")
+            raise MemoryError("oracle_new failed (or a general hexahedron with a non-positive Jacobian)")
         self.shape = (4 + cfg.n_comp, 10 if cfg.p_order == 2 else 4, mesh.n_elem)
 
     def close(self):
