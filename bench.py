@@ -43,6 +43,11 @@ STAGES = 3
 L2_BYTES = 129e6
 
 
+# counted FP64 flops per face quadrature point of face_kernel<double, 1, HLLC>
+# (profiles/face_kernel_fp64_instruction_mix_vortex_32k.md)
+FP64_FLOPS_PER_FACE_POINT = 245.1
+
+
 def peaks() -> dict:
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -385,13 +390,21 @@ def finish(args, rank, world, device, case, mesh, E, V, state_bytes, t_mesh, val
     # (the slot buffer: 2 sides x V x 4 coefficients x 8 B per face)
     traffic = 1111392000 + 1960973056 if (names[dom] == "face" and E == 2 ** 21 and V == 5) else None
     fp64_peak = probe(abi, device, 0)
+    # FP64 flops of the face kernel (HLLC, one species) per face point, from
+    # the thread-level DFMA / DADD / DMUL counts of one ncu capture of this
+    # kernel on the level-5 vortex (an FMA counted as 2 flops):
+    # 2 x 83.4 + 25.4 + 52.8 = 245.1 per point, 6 points per face record
+    fp64 = {"peak_tflops_measured": fp64_peak, "flops_per_face_point_counted": FP64_FLOPS_PER_FACE_POINT}
+    if names[dom] == "face" and V == 5 and case.flux == "HLLC":
+        tf = FP64_FLOPS_PER_FACE_POINT * 6 * F / (per_launch_ms * 1e-3) / 1e12
+        fp64.update({"achieved_tflops": tf, "frac": tf / fp64_peak if fp64_peak else None,
+                     "note": "the plain FP64 path is bound by the FP64 pipe (profiles/)"})
     roofline = {"bound": "hbm", "kernel": names[dom] + "_kernel<double>", "achieved": achieved,
                 "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
                 "peak_src": pk["src"], "traffic": traffic,
                 "algorithmic_bytes_per_launch": alg[names[dom]], "launch_ms": per_launch_ms,
                 "kernel_share": {n: float(kms[i] / kms.sum()) for i, n in enumerate(names)},
-                "fp64_pipe": {"peak_tflops_measured": fp64_peak,
-                              "note": "plain FP64 path is bound by the FP64 pipe, see profiles/"}}
+                "fp64_pipe": fp64}
     cpu, parity = parity_vs_oracle(args.cpu_level, args.parity_steps, device) if args.parity_steps > 0 else (None, None)
     adjoint = run_adjoint(args, device) if args.adjoint_steps > 0 else None
     flame = run_flame(args, device) if args.flame_steps > 0 else None

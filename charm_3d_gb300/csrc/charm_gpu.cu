@@ -29,6 +29,7 @@
 #include "dg_adjoint.cuh"
 #include "dg_visc.cuh"
 #include "dg_launch.h"
+#include "charm_forest.h"
 
 using namespace charm;
 
@@ -115,6 +116,14 @@ struct charm_gpu_handle_s {
     bool hex = false;
     double *d_hex_vert = nullptr, *d_hex_g = nullptr, *d_hex_fg = nullptr;
     int8_t *d_hex_ff = nullptr;
+    // back-to-back steps replayed as a CUDA graph (charm_gpu_run): the
+    // executable graph of two steps, the step and state buffers it was
+    // captured with, and the launches per kernel class it contains
+    cudaGraphExec_t run_graph = nullptr;
+    double run_graph_dt = 0.0;
+    cudaStream_t run_graph_stream = nullptr;
+    std::vector<void *> run_graph_bufs;
+    int64_t run_graph_launches[4] = {0, 0, 0, 0};
     // accounting
     int64_t launches[4] = {0, 0, 0, 0};
     double ms[4] = {0, 0, 0, 0};
@@ -196,8 +205,16 @@ int ensure_buf(charm_gpu_handle_s *h, P **p, size_t bytes)
 
 // Drop what belongs to the previous mesh but is not a reusable buffer: the
 // adjoint's buffers and checkpoints (sized by the run), the flags.
+void drop_run_graph(charm_gpu_handle_s *h)
+{
+    if (h->run_graph) cudaGraphExecDestroy(h->run_graph);   // freed when its launches complete
+    h->run_graph = nullptr;
+    h->run_graph_bufs.clear();
+}
+
 void reset_mesh(charm_gpu_handle_s *h)
 {
+    drop_run_graph(h);
     double **adj[] = {&h->d_adj_lam, &h->d_adj_s, &h->d_adj_acc, &h->d_adj_u1, &h->d_adj_u2, &h->d_adj_fin,
                       &h->d_adj_psi, &h->d_obj_part, &h->d_adj_psi_all};
     for (double **q : adj) {
@@ -218,6 +235,7 @@ void reset_mesh(charm_gpu_handle_s *h)
 
 void free_mesh(charm_gpu_handle_s *h)
 {
+    drop_run_graph(h);
     void *ptrs[] = {h->d_center, h->d_level, h->d_face_elem, h->d_face_info, h->d_bface_elem, h->d_bface_face,
                     h->d_bface_bnd, h->d_gather_ptr, h->d_gather_slot, h->d_lim_idx, h->d_lim_kind, h->d_u,
                     h->d_ua, h->d_ub, h->d_slots, h->d_hex_vert, h->d_hex_g, h->d_hex_fg, h->d_hex_ff};
@@ -1149,6 +1167,94 @@ int resolve_dt(charm_gpu_handle_s *h, double dt_in, double *dt, const double **d
     return CHARM_GPU_OK;
 }
 
+// fn(lo, hi) over [0, n) on the host octree's worker pool (persistent
+// threads; serial below its minimum chunk)
+template <typename Fn>
+void host_for(int64_t n, int64_t min_chunk, Fn &&fn)
+{
+    if (n <= 0) return;
+    using F = typename std::remove_reference<Fn>::type;
+    charm_forest_parallel_for_min(
+        n, min_chunk, [](void *c, int64_t lo, int64_t hi) { (*static_cast<F *>(c))(lo, hi); }, (void *) &fn);
+}
+
+// the first error of a parallel check (code and a static message)
+struct UploadError {
+    int code = 0;
+    const char *msg = "";
+    bool set() const { return __atomic_load_n(&code, __ATOMIC_RELAXED) != 0; }
+    void raise(int c, const char *m)
+    {
+        int expect = 0;
+        if (__atomic_compare_exchange_n(&code, &expect, c, false, __ATOMIC_ACQ_REL, __ATOMIC_RELAXED)) msg = m;
+    }
+};
+
+// The state and stage buffers a step reads and writes (a step may swap them)
+std::vector<void *> step_buffers(const charm_gpu_handle_s *h)
+{
+    return {h->d_u, h->d_ua, h->d_ub, h->d_fh[0], h->d_fh[1], h->d_fh[2], h->d_fl[0], h->d_fl[1], h->d_fl[2],
+            h->d_slots, h->d_uc};
+}
+
+// Back-to-back steps with a fixed dt (given, or TAU) as a CUDA graph: two
+// steps are captured once (a step that swaps its state buffers has swapped
+// them back after two), kept for later runs with the same dt, buffers and
+// stream, and replayed nsteps / 2 times; *done gets the steps launched.
+// Not used when kernels are being timed one by one, when the error word is
+// checked every few steps, or in CFL mode (the step then reads and swaps a
+// device-side dt); a capture the driver refuses falls back to launches.
+int run_as_graph(charm_gpu_handle_s *h, int nsteps, double dt_in, int *done)
+{
+    *done = 0;
+    const bool fixed_dt = dt_in > 0.0 || h->cfg.dt_mode == CHARM_GPU_DT_TAU;
+    if (nsteps < 4 || !fixed_dt || h->timing || h->cfg.check_every > 0) return CHARM_GPU_OK;
+    const double dt = dt_in > 0.0 ? dt_in : h->cfg.tau;
+    const std::vector<void *> bufs = step_buffers(h);
+    if (!(h->run_graph && h->run_graph_dt == dt && h->run_graph_stream == h->stream && h->run_graph_bufs == bufs)) {
+        drop_run_graph(h);
+        int64_t l0[4];
+        std::memcpy(l0, h->launches, sizeof(l0));
+        cudaGraph_t g = nullptr;
+        if (cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            return CHARM_GPU_OK;
+        }
+        int rc = 0;
+        for (int s = 0; s < 2 && !rc; s++) {
+            double d;
+            const double *dd;
+            if (!(rc = resolve_dt(h, dt, &d, &dd))) rc = step_dispatch(h, d, dd);
+        }
+        const cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
+        cudaGraphExec_t ge = nullptr;
+        const bool ok = !rc && ec == cudaSuccess && g && step_buffers(h) == bufs &&
+                        cudaGraphInstantiate(&ge, g, 0) == cudaSuccess;
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();   // a refused capture leaves no sticky error
+        for (int k = 0; k < 4; k++) h->run_graph_launches[k] = h->launches[k] - l0[k];
+        std::memcpy(h->launches, l0, sizeof(l0));   // nothing ran during the capture
+        if (!ok) {
+            // restore the buffers a captured step may have swapped
+            h->d_u = (double *) bufs[0]; h->d_ua = (double *) bufs[1]; h->d_ub = (double *) bufs[2];
+            for (int k = 0; k < 3; k++) { h->d_fh[k] = (float *) bufs[3 + k]; h->d_fl[k] = (float *) bufs[6 + k]; }
+            if (ge) cudaGraphExecDestroy(ge);
+            return CHARM_GPU_OK;
+        }
+        h->run_graph = ge;
+        h->run_graph_dt = dt;
+        h->run_graph_stream = h->stream;
+        h->run_graph_bufs = bufs;
+    }
+    h->dt_next_valid = false;
+    for (int i = 0; i + 2 <= nsteps; i += 2) {
+        CUDA_TRY(cudaGraphLaunch(h->run_graph, h->stream));
+        for (int k = 0; k < 4; k++) h->launches[k] += h->run_graph_launches[k];
+        *done += 2;
+    }
+    return CHARM_GPU_OK;
+}
+
 }  // namespace
 
 // ============================================================================
@@ -1235,72 +1341,112 @@ int upload_impl(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh, const int8_t
     if (!mesh->center || !mesh->level || (F && (!mesh->face_elem || !mesh->face_info)) ||
         (Fb && (!mesh->bface_elem || !mesh->bface_face || !mesh->bface_bnd)))
         return fail(CHARM_GPU_EINVAL, "null mesh array");
-    // ---- validate indices and build the element tables on the host ----
+    // ---- validate indices and build the element tables on the host, on the
+    // host octree's worker threads (the loops touch every face record and
+    // element; serially they were most of an adapt's upload) ----
     std::vector<int32_t> cnt(E + 1, 0);
     std::vector<int32_t> lim_idx(6 * E, -1);
     std::vector<int8_t> lim_kind(6 * E, -1);
-    for (int64_t i = 0; i < F; i++) {
-        const int32_t a = mesh->face_elem[i], b = mesh->face_elem[F + i];
-        const unsigned info = mesh->face_info[i];
-        const int d = info & 3, kind = (info >> 2) & 3;
-        if (a < 0 || a >= E || b < 0 || b >= E || d > 2 || kind > 2)
-            return fail(CHARM_GPU_EINVAL, "face record out of range");
-        if (kind && h->nb != CHARM_GPU_BASIS) return fail(CHARM_GPU_ENOTSUP, "p2: conforming meshes only");
-        cnt[a]++; cnt[b]++;
-        const int fa = hexff ? hexff[i] : 2 * d + 1, fb = hexff ? hexff[F + i] : 2 * d;   // face ids on side 0 / side 1
-        if (fa < 0 || fa > 5 || fb < 0 || fb > 5) return fail(CHARM_GPU_EINVAL, "face number out of range");
-        // each element face takes exactly one record (the big side of a
-        // mortar: its first sub-face record)
-        auto claim = [&](int f, int32_t e, int8_t k, int32_t idx) {
-            if (lim_kind[f * E + e] >= 0) return false;
-            lim_kind[f * E + e] = k;
-            lim_idx[f * E + e] = idx;
-            return true;
-        };
-        if (kind == 0) {
-            if (!claim(fa, a, 0, b) || !claim(fb, b, 0, a))
-                return fail(CHARM_GPU_EINVAL, "element face with more than one face record");
-        } else {
+    UploadError uerr;
+    // each element face takes exactly one record (the big side of a mortar:
+    // its first sub-face record); a second claim is an error
+    auto claim = [&](int f, int32_t e, int8_t k, int32_t idx) {
+        int32_t expect = -1;
+        if (!__atomic_compare_exchange_n(&lim_idx[(int64_t) f * E + e], &expect, idx, false, __ATOMIC_RELAXED,
+                                         __ATOMIC_RELAXED))
+            return false;
+        lim_kind[(int64_t) f * E + e] = k;
+        return true;
+    };
+    host_for(F, 4096, [&](int64_t lo, int64_t hi) {
+        for (int64_t i = lo; i < hi && !uerr.set(); i++) {
+            const int32_t a = mesh->face_elem[i], b = mesh->face_elem[F + i];
+            const unsigned info = mesh->face_info[i];
+            const int d = info & 3, kind = (info >> 2) & 3;
+            if (a < 0 || a >= E || b < 0 || b >= E || d > 2 || kind > 2) {
+                uerr.raise(CHARM_GPU_EINVAL, "face record out of range");
+                return;
+            }
+            if (kind && h->nb != CHARM_GPU_BASIS) { uerr.raise(CHARM_GPU_ENOTSUP, "p2: conforming meshes only"); return; }
+            __atomic_fetch_add(&cnt[a], 1, __ATOMIC_RELAXED);
+            __atomic_fetch_add(&cnt[b], 1, __ATOMIC_RELAXED);
+            const int fa = hexff ? hexff[i] : 2 * d + 1, fb = hexff ? hexff[F + i] : 2 * d;   // side 0 / side 1
+            if (fa < 0 || fa > 5 || fb < 0 || fb > 5) { uerr.raise(CHARM_GPU_EINVAL, "face number out of range"); return; }
+            if (kind == 0) {
+                if (!claim(fa, a, 0, b) || !claim(fb, b, 0, a)) {
+                    uerr.raise(CHARM_GPU_EINVAL, "element face with more than one face record");
+                    return;
+                }
+                continue;
+            }
             const int sub = (info >> 4) & 3;
             const int32_t small = (kind == 1) ? a : b, big = (kind == 1) ? b : a;
             const int fs = (kind == 1) ? fa : fb, fbig = (kind == 1) ? fb : fa;
-            if (!claim(fs, small, (int8_t) (3 | (sub << 4)), big))
-                return fail(CHARM_GPU_EINVAL, "element face with more than one face record");
+            if (!claim(fs, small, (int8_t) (3 | (sub << 4)), big)) {
+                uerr.raise(CHARM_GPU_EINVAL, "element face with more than one face record");
+                return;
+            }
             if (sub == 0) {
                 // the 4 sub-faces of one big face must be consecutive records
-                if (i + 3 >= F) return fail(CHARM_GPU_EINVAL, "incomplete mortar");
+                if (i + 3 >= F) { uerr.raise(CHARM_GPU_EINVAL, "incomplete mortar"); return; }
                 for (int k = 1; k < 4; k++) {
                     const unsigned ik = mesh->face_info[i + k];
                     const int32_t bigk = (((ik >> 2) & 3) == 1) ? mesh->face_elem[F + i + k] : mesh->face_elem[i + k];
                     if (((ik >> 4) & 3) != (unsigned) k || bigk != big || (ik & 3) != (unsigned) d ||
-                        ((ik >> 2) & 3) != (unsigned) kind)
-                        return fail(CHARM_GPU_EINVAL, "mortar sub-faces not consecutive");
+                        ((ik >> 2) & 3) != (unsigned) kind) {
+                        uerr.raise(CHARM_GPU_EINVAL, "mortar sub-faces not consecutive");
+                        return;
+                    }
                 }
-                if (!claim(fbig, big, 2, (int32_t) i))
-                    return fail(CHARM_GPU_EINVAL, "element face with more than one face record");
+                if (!claim(fbig, big, 2, (int32_t) i)) {
+                    uerr.raise(CHARM_GPU_EINVAL, "element face with more than one face record");
+                    return;
+                }
             }
         }
-    }
-    for (int64_t j = 0; j < Fb; j++) {
-        const int32_t e = mesh->bface_elem[j];
-        const int f = mesh->bface_face[j], bnd = mesh->bface_bnd[j];
-        if (e < 0 || e >= E || f < 0 || f > 5 || bnd < 0 || bnd >= h->cfg.n_bnd)
-            return fail(CHARM_GPU_EINVAL, "boundary face record out of range");
-        cnt[e]++;
-        if (lim_kind[f * E + e] >= 0) return fail(CHARM_GPU_EINVAL, "element face with more than one face record");
-        lim_kind[f * E + e] = 1; lim_idx[f * E + e] = (int32_t) j;
-    }
-    for (int64_t k = 0; k < 6 * E; k++)
-        if (lim_kind[k] < 0) return fail(CHARM_GPU_EINVAL, "element face without a face record");
+    });
+    if (uerr.set()) return fail(uerr.code, uerr.msg);
+    host_for(Fb, 4096, [&](int64_t lo, int64_t hi) {
+        for (int64_t j = lo; j < hi && !uerr.set(); j++) {
+            const int32_t e = mesh->bface_elem[j];
+            const int f = mesh->bface_face[j], bnd = mesh->bface_bnd[j];
+            if (e < 0 || e >= E || f < 0 || f > 5 || bnd < 0 || bnd >= h->cfg.n_bnd) {
+                uerr.raise(CHARM_GPU_EINVAL, "boundary face record out of range");
+                return;
+            }
+            __atomic_fetch_add(&cnt[e], 1, __ATOMIC_RELAXED);
+            if (!claim(f, e, 1, (int32_t) j)) {
+                uerr.raise(CHARM_GPU_EINVAL, "element face with more than one face record");
+                return;
+            }
+        }
+    });
+    if (uerr.set()) return fail(uerr.code, uerr.msg);
+    host_for(6 * E, 16384, [&](int64_t lo, int64_t hi) {
+        for (int64_t k = lo; k < hi; k++)
+            if (lim_idx[k] < 0) { uerr.raise(CHARM_GPU_EINVAL, "element face without a face record"); return; }
+    });
+    if (uerr.set()) return fail(uerr.code, uerr.msg);
     std::vector<int32_t> ptr(E + 1, 0);
     for (int64_t e = 0; e < E; e++) ptr[e + 1] = ptr[e] + cnt[e];
-    std::vector<int32_t> slot(ptr[E]);
+    // the element-owned gather: every element's slots in increasing slot
+    // order (interior sides 2i, 2i+1 by face, then boundary 2F + j), the
+    // order in which the cell kernels add them
+    std::vector<int32_t> slot(ptr[E] > 0 ? ptr[E] : 1);
     std::vector<int32_t> fill(ptr.begin(), ptr.end() - 1);
-    for (int64_t i = 0; i < F; i++) {
-        slot[fill[mesh->face_elem[i]]++] = (int32_t) (2 * i);
-        slot[fill[mesh->face_elem[F + i]]++] = (int32_t) (2 * i + 1);
-    }
-    for (int64_t j = 0; j < Fb; j++) slot[fill[mesh->bface_elem[j]]++] = (int32_t) (2 * F + j);
+    host_for(F, 4096, [&](int64_t lo, int64_t hi) {
+        for (int64_t i = lo; i < hi; i++) {
+            slot[__atomic_fetch_add(&fill[mesh->face_elem[i]], 1, __ATOMIC_RELAXED)] = (int32_t) (2 * i);
+            slot[__atomic_fetch_add(&fill[mesh->face_elem[F + i]], 1, __ATOMIC_RELAXED)] = (int32_t) (2 * i + 1);
+        }
+    });
+    host_for(Fb, 4096, [&](int64_t lo, int64_t hi) {
+        for (int64_t j = lo; j < hi; j++)
+            slot[__atomic_fetch_add(&fill[mesh->bface_elem[j]], 1, __ATOMIC_RELAXED)] = (int32_t) (2 * F + j);
+    });
+    host_for(E, 4096, [&](int64_t lo, int64_t hi) {
+        for (int64_t e = lo; e < hi; e++) std::sort(slot.begin() + ptr[e], slot.begin() + ptr[e + 1]);
+    });
     int64_t S = 2 * F + Fb;
     S += (S & 1);
 
@@ -1352,88 +1498,95 @@ int upload_impl(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh, const int8_t
         // tile's halo (outside elements that share one of its faces); for
         // every element face its record position and kind
         const int64_t nt = (E + kTile - 1) / kTile;
-        std::vector<int32_t> tcnt(nt + 1, 0);
-        for (int64_t i = 0; i < F; i++) {
-            const int64_t t0 = mesh->face_elem[i] / kTile, t1 = mesh->face_elem[F + i] / kTile;
-            tcnt[t0]++;
-            if (t1 != t0) tcnt[t1]++;
-        }
-        for (int64_t j = 0; j < Fb; j++) tcnt[mesh->bface_elem[j] / kTile]++;
-        std::vector<int32_t> tptr(nt + 1, 0);
-        for (int64_t t = 0; t < nt; t++) tptr[t + 1] = tptr[t] + tcnt[t];
-        std::vector<int32_t> tface(tptr[nt] > 0 ? tptr[nt] : 1), tslot(6 * E, -1), tfill(tptr.begin(), tptr.end() - 1);
-        int64_t max_list = 0;
-        for (int64_t t = 0; t < nt; t++) max_list = std::max<int64_t>(max_list, tcnt[t]);
-        for (int64_t i = 0; i < F; i++) {
-            const int32_t a = mesh->face_elem[i], b = mesh->face_elem[F + i];
-            const unsigned info = mesh->face_info[i];
-            const int d = info & 3, kind = (info >> 2) & 3, sub = (info >> 4) & 3;
-            const int64_t ta = a / kTile, tb = b / kTile;
-            for (int pass = 0; pass < 2; pass++) {
-                const int64_t t = pass ? tb : ta;
-                if (pass && tb == ta) break;
-                const int32_t p = tfill[t]++;
-                tface[p] = (int32_t) i;
-                const int32_t loc = p - tptr[t];
+        // a tile's records: every record of its elements (from their gather
+        // slots), sorted (interior faces by index, then boundary records as
+        // F + j: the 4 records of a mortar stay consecutive), each once; its
+        // halo: the outside elements of those records, sorted
+        auto rec_of = [&](int32_t sl) -> int32_t { return sl < 2 * F ? sl >> 1 : (int32_t) (F + (sl - 2 * F)); };
+        auto tile_lists = [&](int64_t t, std::vector<int32_t> &list, std::vector<int32_t> &hl) {
+            const int64_t e0 = t * kTile, e1 = std::min<int64_t>(E, e0 + kTile);
+            list.clear();
+            hl.clear();
+            for (int64_t e = e0; e < e1; e++)
+                for (int32_t j = ptr[e]; j < ptr[e + 1]; j++) list.push_back(rec_of(slot[j]));
+            std::sort(list.begin(), list.end());
+            list.erase(std::unique(list.begin(), list.end()), list.end());
+            for (const int32_t r : list) {
+                if (r >= F) continue;   // a boundary record's element is in the tile
                 for (int side = 0; side < 2; side++) {
-                    const int32_t e = side ? b : a;
-                    if (e / kTile != t) continue;
-                    const int f = side ? 2 * d : 2 * d + 1;
-                    const bool big = (kind == 1 && side == 1) || (kind == 2 && side == 0);
-                    const bool small = (kind == 1 && side == 0) || (kind == 2 && side == 1);
-                    if (!big) tslot[(int64_t) f * E + e] = (loc << 2) | (small ? 3 : 0);
-                    else if (sub == 0) tslot[(int64_t) f * E + e] = (loc << 2) | 2;
+                    const int32_t e = mesh->face_elem[side * F + r];
+                    if (e < e0 || e >= e1) hl.push_back(e);
                 }
             }
-        }
-        for (int64_t j = 0; j < Fb; j++) {
-            const int32_t e = mesh->bface_elem[j];
-            const int64_t t = e / kTile;
-            const int32_t p = tfill[t]++;
-            tface[p] = (int32_t) (F + j);
-            tslot[(int64_t) mesh->bface_face[j] * E + e] = ((p - tptr[t]) << 2) | 1;
-        }
-        for (int64_t k = 0; k < 6 * E; k++)
-            if (tslot[k] < 0) return fail(CHARM_GPU_EINVAL, "element face without a tile face slot");
-        // records and halos
-        std::vector<int4> trec(tface.size());
-        std::vector<int32_t> hptr(nt + 1, 0), halo, col(E, -1);
-        std::vector<int64_t> stamp(E, -1);
-        int64_t max_halo = 0;
+            std::sort(hl.begin(), hl.end());
+            hl.erase(std::unique(hl.begin(), hl.end()), hl.end());
+        };
+        std::vector<int32_t> tptr(nt + 1, 0), hptr(nt + 1, 0);
+        host_for(nt, 64, [&](int64_t lo, int64_t hi) {
+            std::vector<int32_t> list, hl;
+            for (int64_t t = lo; t < hi; t++) {
+                tile_lists(t, list, hl);
+                tptr[t + 1] = (int32_t) list.size();
+                hptr[t + 1] = (int32_t) hl.size();
+            }
+        });
+        int64_t max_list = 0, max_halo = 0;
         for (int64_t t = 0; t < nt; t++) {
-            const int64_t e0 = t * kTile;
-            auto column = [&](int32_t e) -> int32_t {
-                if (e / kTile == t) return (int32_t) (e - e0);
-                if (stamp[e] != t) {
-                    stamp[e] = t;
-                    col[e] = kTile + (int32_t) (halo.size() - hptr[t]);
-                    halo.push_back(e);
-                }
-                return col[e];
-            };
-            for (int32_t p = tptr[t]; p < tptr[t + 1]; p++) {
-                const int64_t i = tface[p];
-                int4 r;
-                if (i < F) {
-                    const int32_t a = mesh->face_elem[i], b = mesh->face_elem[F + i];
-                    const unsigned info = mesh->face_info[i];
-                    r.x = column(a);
-                    r.y = column(b);
-                    r.z = (int) info;
-                    r.w = mesh->level[(((info >> 2) & 3) == 2) ? b : a];
-                } else {
-                    const int64_t j = i - F;
-                    const int32_t e = mesh->bface_elem[j];
-                    r.x = column(e);
-                    r.y = -1;
-                    r.z = (int) mesh->bface_face[j] | ((int) mesh->bface_bnd[j] << 8) | kRecBoundary;
-                    r.w = mesh->level[e];
-                }
-                trec[p] = r;
-            }
-            hptr[t + 1] = (int32_t) halo.size();
-            max_halo = std::max<int64_t>(max_halo, hptr[t + 1] - hptr[t]);
+            max_list = std::max<int64_t>(max_list, tptr[t + 1]);
+            max_halo = std::max<int64_t>(max_halo, hptr[t + 1]);
+            tptr[t + 1] += tptr[t];
+            hptr[t + 1] += hptr[t];
         }
+        std::vector<int4> trec(tptr[nt] > 0 ? tptr[nt] : 1);
+        std::vector<int32_t> tslot(6 * E, -1), halo(hptr[nt] > 0 ? hptr[nt] : 1, 0);
+        host_for(nt, 64, [&](int64_t lo, int64_t hi) {
+            std::vector<int32_t> list, hl;
+            for (int64_t t = lo; t < hi; t++) {
+                tile_lists(t, list, hl);
+                const int64_t e0 = t * kTile, e1 = std::min<int64_t>(E, e0 + kTile);
+                std::copy(hl.begin(), hl.end(), halo.begin() + hptr[t]);
+                auto column = [&](int32_t e) -> int32_t {
+                    if (e >= e0 && e < e1) return (int32_t) (e - e0);
+                    return kTile + (int32_t) (std::lower_bound(hl.begin(), hl.end(), e) - hl.begin());
+                };
+                for (size_t loc = 0; loc < list.size(); loc++) {
+                    const int32_t r = list[loc];
+                    int4 rec;
+                    if (r < F) {
+                        const int32_t a = mesh->face_elem[r], b = mesh->face_elem[F + r];
+                        const unsigned info = mesh->face_info[r];
+                        const int d = info & 3, kind = (info >> 2) & 3, sub = (info >> 4) & 3;
+                        rec.x = column(a);
+                        rec.y = column(b);
+                        rec.z = (int) info;
+                        rec.w = mesh->level[(kind == 2) ? b : a];
+                        for (int side = 0; side < 2; side++) {
+                            const int32_t e = side ? b : a;
+                            if (e < e0 || e >= e1) continue;
+                            const int f = side ? 2 * d : 2 * d + 1;
+                            const bool big = (kind == 1 && side == 1) || (kind == 2 && side == 0);
+                            const bool small = (kind == 1 && side == 0) || (kind == 2 && side == 1);
+                            if (!big) tslot[(int64_t) f * E + e] = ((int32_t) loc << 2) | (small ? 3 : 0);
+                            else if (sub == 0) tslot[(int64_t) f * E + e] = ((int32_t) loc << 2) | 2;
+                        }
+                    } else {
+                        const int64_t j = r - F;
+                        const int32_t e = mesh->bface_elem[j];
+                        rec.x = column(e);
+                        rec.y = -1;
+                        rec.z = (int) mesh->bface_face[j] | ((int) mesh->bface_bnd[j] << 8) | kRecBoundary;
+                        rec.w = mesh->level[e];
+                        tslot[(int64_t) mesh->bface_face[j] * E + e] = ((int32_t) loc << 2) | 1;
+                    }
+                    trec[tptr[t] + loc] = rec;
+                }
+            }
+        });
+        host_for(6 * E, 16384, [&](int64_t lo, int64_t hi) {
+            for (int64_t k = lo; k < hi; k++)
+                if (tslot[k] < 0) { uerr.raise(CHARM_GPU_EINVAL, "element face without a tile face slot"); return; }
+        });
+        if (uerr.set()) return fail(uerr.code, uerr.msg);
         if (halo.empty()) halo.push_back(0);
         const int ncol = (int) ((kTile + max_halo + 3) & ~(int64_t) 3);   // 16-byte aligned planes
         const size_t smem = sizeof(float) * ((size_t) V * CHARM_GPU_BASIS * ncol + (size_t) max_list * 3 * V);
@@ -1753,7 +1906,9 @@ int charm_gpu_run(charm_gpu_handle_t h, int nsteps, double dt_in)
     CfgLease lease(h);
     int rc = check_ready(h);
     if (rc) return rc;
-    for (int s = 0; s < nsteps; s++) {
+    int done = 0;
+    if ((rc = run_as_graph(h, nsteps, dt_in, &done))) return rc;
+    for (int s = done; s < nsteps; s++) {
         double dt;
         const double *dt_dev;
         if ((rc = resolve_dt(h, dt_in, &dt, &dt_dev))) return rc;
@@ -1860,8 +2015,34 @@ int charm_gpu_refine_flags(charm_gpu_handle_t h, double max_err, int8_t *flags, 
     int rc = check_ready(h);
     if (rc) return rc;
     if (h->nb != CHARM_GPU_BASIS) return fail(CHARM_GPU_ENOTSUP, "refine flags: p1 only");
-    if (h->hex) return fail(CHARM_GPU_ENOTSUP, "refine flags: box meshes only");
     if (!flags && !grad_out) return fail(CHARM_GPU_EINVAL, "null argument");
+    if (h->hex) {
+        // general hexahedra: the estimate from the face tables, the criterion
+        // with each element's own (quadrature) volume
+        double *d_grad = h->d_ua;
+        TimedLaunch t;
+        begin_launch(h, 3, &t);
+        if (h->cfg.n_comp == 1) hex_launch_amr_grad<1>(mesh_view(h), hex_view(h), h->d_u, d_grad, h->stream);
+        else hex_launch_amr_grad<2>(mesh_view(h), hex_view(h), h->d_u, d_grad, h->stream);
+        end_launch(h, &t);
+        CUDA_TRY(cudaGetLastError());
+        std::vector<double> g(grad_out ? 0 : (size_t) (3 * h->E)), vol((size_t) h->E);
+        double *hg = grad_out ? grad_out : g.data();
+        CUDA_TRY(cudaMemcpyAsync(hg, d_grad, sizeof(double) * 3 * h->E, cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(cudaMemcpyAsync(vol.data(), h->d_hex_g + (size_t) kGvol * h->E, sizeof(double) * h->E,
+                                 cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+        if (flags) {
+            const double err2_max = max_err * max_err;
+            for (int64_t e = 0; e < h->E; e++) {   // charm_refine_err_estimate (src/charm_amr.c:12-48)
+                double diff2 = 0.0;
+                for (int d = 0; d < 3; d++) diff2 += hg[d * h->E + e] * hg[d * h->E + e];
+                const double err2 = diff2 * (1. / 12.) * exp(log(vol[e]) * 5. / 3.);
+                flags[e] = (err2 > err2_max * vol[e]) ? 1 : 0;
+            }
+        }
+        return CHARM_GPU_OK;
+    }
     if (h->cfg.precision == CHARM_GPU_PREC_MIXED && (rc = ff_convert(h, false))) return rc;   // d_u <- hi + lo
     // the gradient goes through the (idle) slot buffer: 3*E doubles fit in it
     MeshDev m = mesh_view(h);

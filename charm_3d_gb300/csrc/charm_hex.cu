@@ -65,6 +65,12 @@ void hex_launch_cfl(const MeshDev &m, const HexDev &x, const double *u, unsigned
     hex_cfl_kernel<NC><<<blocks(m.n_elem), 128, 0, st>>>(m, x, u, dt, cfl);
 }
 
+template <int NC>
+void hex_launch_amr_grad(const MeshDev &m, const HexDev &x, const double *u, double *grad, cudaStream_t st)
+{
+    hex_amr_grad_kernel<NC><<<blocks(m.n_elem), 128, 0, st>>>(m, x, u, grad);
+}
+
 #define CHARM_HEX_INST(NC)                                                                                              \
     template void hex_launch_face<NC>(int, const MeshDev &, const HexDev &, const double *, double *, unsigned *,       \
                                       cudaStream_t);                                                                    \
@@ -74,7 +80,8 @@ void hex_launch_cfl(const MeshDev &m, const HexDev &x, const double *u, unsigned
     template void hex_launch_limit<NC>(const MeshDev &, const HexDev &, const double *, const double *, double *,      \
                                        double, double, unsigned long long *, double, cudaStream_t);                     \
     template void hex_launch_cfl<NC>(const MeshDev &, const HexDev &, const double *, unsigned long long *, double,    \
-                                     cudaStream_t);
+                                     cudaStream_t);                                                                     \
+    template void hex_launch_amr_grad<NC>(const MeshDev &, const HexDev &, const double *, double *, cudaStream_t);
 CHARM_HEX_INST(1)
 CHARM_HEX_INST(2)
 

@@ -511,6 +511,65 @@ hex_limit_kernel(MeshDev m, HexDev x, const double *__restrict__ ua, const doubl
     if (dt_next) warp_min_to(cell_cfl_dt<NC>(cen, cfl, hex_g(x, E, kGvol, e)), dt_next);
 }
 
+// ---------------------------------------------------------------------------
+// density-gradient estimate of charm_adapt on general hexahedra
+// (src/charm_amr.c:350-573): grad_e = (1/vol_e) * the sum over e's face
+// records of +-0.5 (r_L + r_R) n gw gj at the face points (side 0 adds,
+// side 1 subtracts; a boundary's right state is its ghost).  Each element
+// walks its own records through the gather table: deterministic, no atomics.
+// ---------------------------------------------------------------------------
+template <int NC>
+__global__ void __launch_bounds__(128)
+hex_amr_grad_kernel(MeshDev m, HexDev x, const double *__restrict__ u, double *__restrict__ grad)
+{
+    constexpr int V = 4 + NC;
+    const int64_t e = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t E = m.n_elem, F = m.n_face, NR = m.n_face + m.n_bface;
+    if (e >= E) return;
+    double g[3] = {0.0, 0.0, 0.0};
+    for (int32_t j = m.gather_ptr[e]; j < m.gather_ptr[e + 1]; j++) {
+        const int64_t sl = m.gather_slot[j];
+        const bool inner = sl < 2 * F;
+        const int64_t r = inner ? (sl >> 1) : F + (sl - 2 * F);
+        const double sg = (inner && (sl & 1)) ? -1.0 : 1.0;
+        const int64_t e0 = inner ? m.face_elem[r] : e, e1 = inner ? m.face_elem[F + r] : e;
+        double c0[3], c1[3], h0[3], h1[3], n[3];
+        for (int d = 0; d < 3; d++) {
+            c0[d] = hex_g(x, E, kGc + d, e0); h0[d] = hex_g(x, E, kGdh + d, e0);
+            c1[d] = hex_g(x, E, kGc + d, e1); h1[d] = hex_g(x, E, kGdh + d, e1);
+            n[d] = __ldg(x.fg + (int64_t) (kFn + d) * NR + r);
+        }
+        double a0[V][kNB], a1[V][kNB];
+        load_coef<double, V>(u, E, e0, a0);
+        load_coef<double, V>(u, E, e1, a1);
+        const int bid = inner ? 0 : m.bface_bnd[r - F];
+#pragma unroll 1
+        for (int q = 0; q < 6; q++) {
+            double p0[3], p1[3];
+            for (int d = 0; d < 3; d++) {
+                const double gp = __ldg(x.fg + (int64_t) (kFgp + 3 * q + d) * NR + r);
+                p0[d] = (gp - c0[d]) / h0[d];
+                p1[d] = (gp - c1[d]) / h1[d];
+            }
+            const double wq = __ldg(x.fg + (int64_t) (kFw + q) * NR + r);
+            double U0[V], U1[V];
+#pragma unroll
+            for (int v = 0; v < V; v++) {
+                U0[v] = a0[v][0] + p0[0] * a0[v][1] + p0[1] * a0[v][2] + p0[2] * a0[v][3];
+                U1[v] = a1[v][0] + p1[0] * a1[v][1] + p1[1] * a1[v][2] + p1[2] * a1[v][3];
+            }
+            Prim<double, NC> q0, q1;
+            cons_to_prim<double, NC>(U0, q0);
+            if (inner) cons_to_prim<double, NC>(U1, q1);
+            else bnd_cond<double, NC>(bid, q0, q1, n);
+            const double qr = 0.5 * (q0.r + q1.r);
+            for (int d = 0; d < 3; d++) g[d] += sg * (qr * wq * n[d]);
+        }
+    }
+    const double vol = hex_g(x, E, kGvol, e);
+    for (int d = 0; d < 3; d++) grad[(int64_t) d * E + e] = g[d] / vol;
+}
+
 // CFL step of the first step (the reference's get_dt, charm_model.c:21-36)
 template <int NC>
 __global__ void __launch_bounds__(128)

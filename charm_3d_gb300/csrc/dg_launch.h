@@ -116,6 +116,9 @@ void hex_launch_limit(const MeshDev &m, const HexDev &x, const double *ua, const
 template <int NC>
 void hex_launch_cfl(const MeshDev &m, const HexDev &x, const double *u, unsigned long long *dt, double cfl,
                     cudaStream_t st);
+// density-gradient estimate of the refine criterion, grad [3][E]
+template <int NC>
+void hex_launch_amr_grad(const MeshDev &m, const HexDev &x, const double *u, double *grad, cudaStream_t st);
 
 // ---- point fluxes (charm_point.cu) ------------------------------------------
 

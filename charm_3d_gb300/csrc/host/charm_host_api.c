@@ -456,6 +456,153 @@ static void project_up(const double *u, int64_t E, const int64_t ch[8], const in
     }
 }
 
+/* ---- general hexahedra: leaf geometry and the quadrature projections ---- */
+
+/* Geometry of a leaf of an unstructured forest (charm_geom_quad_calc,
+ * src/charm_geom.c:40-172, 496-530): corners through the tree's trilinear
+ * map, the 8 Gauss points of the leaf's own trilinear map with their
+ * Jacobian determinants (gw = 1), dh = the corners' bounding box, the
+ * centre, the volume and the inverse of the 4x4 mass matrix. */
+typedef struct {
+    double c[3], dh[3], vol;
+    double xq[8][3], wq[8];
+    double ainv[4][4];
+} hexg_t;
+
+static void hex_leaf_geom(const charm_conn_t *conn, const charm_leaf_t *q, hexg_t *g)
+{
+    const double inv = 1.0 / (double) CHARM_FOREST_ROOT_LEN;
+    const int32_t len = CHARM_FOREST_QLEN(q->level);
+    double v[8][3];
+    for (int k = 0; k < 8; k++)
+        charm_conn_point(conn, q->tree, (double) (q->x + ((k & 1) ? len : 0)) * inv,
+                         (double) (q->y + ((k & 2) ? len : 0)) * inv, (double) (q->z + ((k & 4) ? len : 0)) * inv, v[k]);
+    const double s3 = 0.57735026918962576451;
+    for (int q8 = -1; q8 < 8; q8++) {
+        const double r[3] = {q8 < 0 ? 0.0 : ((q8 & 1) ? s3 : -s3), q8 < 0 ? 0.0 : ((q8 & 2) ? s3 : -s3),
+                             q8 < 0 ? 0.0 : ((q8 & 4) ? s3 : -s3)};
+        double x[3] = {0, 0, 0}, J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        for (int k = 0; k < 8; k++) {
+            const double sx = (k & 1) ? 1.0 : -1.0, sy = (k & 2) ? 1.0 : -1.0, sz = (k & 4) ? 1.0 : -1.0;
+            const double wx = 1.0 + sx * r[0], wy = 1.0 + sy * r[1], wz = 1.0 + sz * r[2];
+            for (int d = 0; d < 3; d++) {
+                x[d] += wz * wy * wx * 0.125 * v[k][d];
+                J[d][0] += wz * wy * sx * 0.125 * v[k][d];
+                J[d][1] += wz * wx * sy * 0.125 * v[k][d];
+                J[d][2] += wy * wx * sz * 0.125 * v[k][d];
+            }
+        }
+        if (q8 < 0) { memcpy(g->c, x, sizeof(x)); continue; }
+        memcpy(g->xq[q8], x, sizeof(x));
+        g->wq[q8] = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                    J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+    }
+    for (int d = 0; d < 3; d++) {
+        double lo = v[0][d], hi = v[0][d];
+        for (int k = 1; k < 8; k++) {
+            if (lo > v[k][d]) lo = v[k][d];
+            if (hi < v[k][d]) hi = v[k][d];
+        }
+        g->dh[d] = hi - lo;
+    }
+    g->vol = 0.0;
+    for (int q8 = 0; q8 < 8; q8++) g->vol += g->wq[q8];
+    double a[4][4];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) {
+            double acc = 0.0;
+            for (int q8 = 0; q8 < 8; q8++) {
+                const double pi = i ? (g->xq[q8][i - 1] - g->c[i - 1]) / g->dh[i - 1] : 1.0;
+                const double pj = j ? (g->xq[q8][j - 1] - g->c[j - 1]) / g->dh[j - 1] : 1.0;
+                acc += g->wq[q8] * pi * pj;
+            }
+            a[i][j] = acc;
+            g->ainv[i][j] = (i == j) ? 1.0 : 0.0;
+        }
+    for (int i = 0; i < 4; i++) {   /* Gauss-Jordan with partial pivoting (charm_matr_inv) */
+        int p = i;
+        for (int r = i + 1; r < 4; r++)
+            if (fabs(a[r][i]) > fabs(a[p][i])) p = r;
+        for (int j = 0; p != i && j < 4; j++) {
+            double t = a[i][j]; a[i][j] = a[p][j]; a[p][j] = t;
+            t = g->ainv[i][j]; g->ainv[i][j] = g->ainv[p][j]; g->ainv[p][j] = t;
+        }
+        const double piv = a[i][i];
+        for (int j = 0; j < 4; j++) { a[i][j] /= piv; g->ainv[i][j] /= piv; }
+        for (int r = 0; r < 4; r++) {
+            if (r == i) continue;
+            const double fct = a[r][i];
+            for (int j = 0; j < 4; j++) { a[r][j] -= fct * a[i][j]; g->ainv[r][j] -= fct * g->ainv[i][j]; }
+        }
+    }
+}
+
+static double hex_phi(const hexg_t *g, const double x[3], int k)
+{   /* charm_base_func, src/charm_base_func.c:8-20 */
+    return k ? (x[k - 1] - g->c[k - 1]) / g->dh[k - 1] : 1.0;
+}
+
+/* charm_replace_quads (src/charm_amr.c:206-307) on general hexahedra: the
+ * L2 projection of the source leaves' fields onto the target leaf's basis,
+ * by the quadrature of the target (refine: one child from its parent) or
+ * of each source (coarsen: the parent from its 8 children):
+ * w_t = A_t^-1 sum_q gw gj phi_t(x_q) u_s(x_q). */
+static void hex_project_down(const hexg_t *P, const hexg_t *C, const double *u, int64_t E, int64_t p, double *w,
+                             int64_t En, int64_t c, int V)
+{
+    for (int v = 0; v < V; v++) {
+        double rhs[4] = {0, 0, 0, 0};
+        for (int q = 0; q < 8; q++) {
+            double up = 0.0;
+            for (int n = 0; n < 4; n++) up += u[((int64_t) v * 4 + n) * E + p] * hex_phi(P, C->xq[q], n);
+            for (int m = 0; m < 4; m++) rhs[m] += C->wq[q] * hex_phi(C, C->xq[q], m) * up;
+        }
+        for (int k = 0; k < 4; k++)
+            w[((int64_t) v * 4 + k) * En + c] =
+                C->ainv[k][0] * rhs[0] + C->ainv[k][1] * rhs[1] + C->ainv[k][2] * rhs[2] + C->ainv[k][3] * rhs[3];
+    }
+}
+
+static void hex_project_up(const hexg_t *P, const hexg_t C[8], const double *u, int64_t E, int64_t i0, double *w,
+                           int64_t En, int64_t k, int V)
+{
+    for (int v = 0; v < V; v++) {
+        double rhs[4] = {0, 0, 0, 0};
+        for (int i = 0; i < 8; i++)
+            for (int q = 0; q < 8; q++) {
+                double uc = 0.0;
+                for (int n = 0; n < 4; n++) uc += u[((int64_t) v * 4 + n) * E + i0 + i] * hex_phi(&C[i], C[i].xq[q], n);
+                for (int m = 0; m < 4; m++) rhs[m] += C[i].wq[q] * hex_phi(P, C[i].xq[q], m) * uc;
+            }
+        for (int b = 0; b < 4; b++)
+            w[((int64_t) v * 4 + b) * En + k] =
+                P->ainv[b][0] * rhs[0] + P->ainv[b][1] * rhs[1] + P->ainv[b][2] * rhs[2] + P->ainv[b][3] * rhs[3];
+    }
+}
+
+static double hex_leaf_vol(const charm_conn_t *conn, const charm_leaf_t *q)
+{
+    hexg_t g;
+    hex_leaf_geom(conn, q, &g);
+    return g.vol;
+}
+
+static void parent_of(const charm_leaf_t *c, charm_leaf_t *p)
+{
+    const int32_t len = CHARM_FOREST_QLEN(c->level);
+    p->x = c->x & ~len; p->y = c->y & ~len; p->z = c->z & ~len;
+    p->tree = c->tree;
+    p->level = (int8_t) (c->level - 1);
+}
+
+static void child_leaf(const charm_leaf_t *p, int cid, charm_leaf_t *c)
+{
+    const int32_t h = CHARM_FOREST_QLEN(p->level + 1);
+    c->x = p->x + ((cid & 1) ? h : 0); c->y = p->y + ((cid & 2) ? h : 0); c->z = p->z + ((cid & 4) ? h : 0);
+    c->tree = p->tree;
+    c->level = (int8_t) (p->level + 1);
+}
+
 /* refine flagged leaves one level (charm_forest_refine_map); o2n[E] gets
  * each old leaf's first new index (the identity when nothing is refined) */
 static int refine_o2n(charm_forest_t *f, const int8_t *fl, int64_t **o2n)
@@ -487,7 +634,16 @@ static void refine_state_range(void *c, int64_t lo, int64_t hi)
     const refine_pass_ctx_t *x = (const refine_pass_ctx_t *) c;
     for (int64_t i = lo; i < hi; i++) {
         const int64_t k = x->o2n[i];
-        if (x->o2n[i + 1] - k == 8) {
+        if (x->o2n[i + 1] - k == 8 && x->f->conn) {
+            charm_leaf_t pl;
+            hexg_t P, C;
+            parent_of(&x->f->leaf[k], &pl);
+            hex_leaf_geom(x->f->conn, &pl, &P);
+            for (int ch = 0; ch < 8; ch++) {
+                hex_leaf_geom(x->f->conn, &x->f->leaf[k + ch], &C);
+                hex_project_down(&P, &C, x->u, x->E, i, x->w, x->En, k + ch, x->V);
+            }
+        } else if (x->o2n[i + 1] - k == 8) {
             for (int ch = 0; ch < 8; ch++)
                 project_down(x->u, x->E, i, x->w, x->En, k + ch, charm_leaf_child_id(&x->f->leaf[k + ch]), x->V);
         } else {
@@ -599,7 +755,10 @@ static int coarsen_family(void *user, const charm_leaf_t *leaves, const int64_t 
     if (leaves[idx[0]].level <= c->minlevel) return 0;
     double h[3];
     leaf_h(c->f, leaves[idx[0]].level, h);
-    const double vol = h[0] * h[1] * h[2];
+    /* the first child's volume stands for every child (as the reference's
+     * "the quadrant's volume is also its volume fraction"); each child's
+     * own estimate uses its own volume */
+    const double vol = c->f->conn ? hex_leaf_vol(c->f->conn, &leaves[idx[0]]) : h[0] * h[1] * h[2];
     double r[8], parentu = 0.;
     for (int i = 0; i < 8; i++) {
         double ri = 0.;   /* prim.r at the centre: sum of the partial-density means, eos flag 4 clamp */
@@ -612,7 +771,9 @@ static int coarsen_family(void *user, const charm_leaf_t *leaves, const int64_t 
     }
     double err2 = 0.;
     for (int i = 0; i < 8; i++) {
-        const double childerr2 = err_sqr(c->grad, c->E, idx[i], c->vpow[leaves[idx[0]].level]);
+        const double vp = c->f->conn ? exp(log(hex_leaf_vol(c->f->conn, &leaves[idx[i]])) * 5. / 3.)
+                                     : c->vpow[leaves[idx[0]].level];
+        const double childerr2 = err_sqr(c->grad, c->E, idx[i], vp);
         if (childerr2 > c->err2_max * vol) return 0;
         err2 += childerr2;
         const double diff = (parentu - r[i]) * (parentu - r[i]);
@@ -639,7 +800,12 @@ static void refine_flags_range(void *c, int64_t lo, int64_t hi)
     for (int64_t i = lo; i < hi; i++) {
         const int l = x->f->leaf[i].level;
         if (l >= x->ml) continue;
-        x->fl[i] = err_sqr(x->grad, x->E, i, x->vpow[l]) > x->err2_max * x->vol[l];
+        if (x->f->conn) {   /* each leaf's own volume */
+            const double vol = hex_leaf_vol(x->f->conn, &x->f->leaf[i]);
+            x->fl[i] = err_sqr(x->grad, x->E, i, exp(log(vol) * 5. / 3.)) > x->err2_max * vol;
+        } else {
+            x->fl[i] = err_sqr(x->grad, x->E, i, x->vpow[l]) > x->err2_max * x->vol[l];
+        }
     }
 }
 
@@ -648,6 +814,7 @@ static void refine_flags_range(void *c, int64_t lo, int64_t hi)
  * ids 0..7 in Morton order (op 8); the state is projected (state mode) or
  * the pass recorded (plan mode), and the new-leaf marks follow */
 typedef struct {
+    const charm_forest_t *f;   /* coarsened */
     const int64_t *n2o;        /* [En + 1] */
     int64_t E, En;
     int V;
@@ -669,6 +836,15 @@ static void coarsen_pass_range(void *c, int64_t lo, int64_t hi)
         if (x->map) {
             x->map[2 * k] = (int32_t) i;
             x->map[2 * k + 1] = merged ? 8 : -1;
+        } else if (merged && x->f->conn) {
+            hexg_t P, C[8];
+            hex_leaf_geom(x->f->conn, &x->f->leaf[k], &P);
+            for (int j = 0; j < 8; j++) {
+                charm_leaf_t cl;
+                child_leaf(&x->f->leaf[k], j, &cl);
+                hex_leaf_geom(x->f->conn, &cl, &C[j]);
+            }
+            hex_project_up(&P, C, x->u, x->E, i, x->w, x->En, k, x->V);
         } else if (merged) {
             int64_t ch[8];
             for (int j = 0; j < 8; j++) ch[j] = i + j;
@@ -776,7 +952,7 @@ static int adapt_core(struct charm_host_forest_s *h, const double *grad, double 
                 free(w); free(map); free(isnew2); free(n2o); free(u); free(rho); free(g1); free(isnew);
                 return CHARM_GPU_ENOMEM;
             }
-            coarsen_pass_ctx_t cp = {n2o, E, En, V, u, w, map, isnew, isnew2};
+            coarsen_pass_ctx_t cp = {f, n2o, E, En, V, u, w, map, isnew, isnew2};
             charm_forest_parallel_for(En, coarsen_pass_range, &cp);
             free(isnew);
             isnew = isnew2;
@@ -874,7 +1050,6 @@ int charm_host_forest_adapt_state(charm_host_forest_t h, const double *grad, dou
                                   int n_comp, const double *u_in, int64_t *n_new)
 {
     if (!h || !grad || !u_in || n_comp < 1 || n_comp > CHARM_GPU_MAX_COMP) return CHARM_GPU_EINVAL;
-    if (h->conn) return CHARM_GPU_ENOTSUP;   /* the projections here are the box forms */
     return adapt_core(h, grad, max_err, minlevel, maxlevel, n_comp, u_in, NULL, n_new);
 }
 
@@ -882,7 +1057,7 @@ int charm_host_forest_adapt_plan(charm_host_forest_t h, const double *grad, cons
                                  int minlevel, int maxlevel, int64_t *n_new, charm_gpu_adapt_plan_t *plan)
 {
     if (!h || !grad || !rho) return CHARM_GPU_EINVAL;
-    if (h->conn) return CHARM_GPU_ENOTSUP;
+    if (h->conn) return CHARM_GPU_ENOTSUP;   /* the device projection is the box form */
     int rc = adapt_core(h, grad, max_err, minlevel, maxlevel, 1, NULL, rho, n_new);
     if (rc) return rc;
     if (plan) {

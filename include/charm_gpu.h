@@ -219,7 +219,12 @@ int charm_gpu_get_state(charm_gpu_handle_t h, double *u, int on_device);
  * taken.  Replaces charm_timestep_single_fn_t. */
 int charm_gpu_step(charm_gpu_handle_t h, double dt_in, double *dt_out);
 
-/* n steps back to back (no host round trip between them). */
+/* n steps back to back (no host round trip between them).  With a fixed
+ * step (dt_in > 0, or the TAU mode), no per-kernel timing and no periodic
+ * error-word check, the steps are replayed as a CUDA graph of two steps,
+ * captured on the handle's stream by the first such run and kept for later
+ * runs with the same step, stream and mesh (an upload drops it); results
+ * and launch counts are those of the steps launched one by one. */
 int charm_gpu_run(charm_gpu_handle_t h, int nsteps, double dt_in);
 
 /* Time step of the configured mode (replaces charm_get_timestep_fn_t). */
@@ -235,7 +240,8 @@ int charm_gpu_limit(charm_gpu_handle_t h);
 /* Density-gradient refinement indicator of charm_adapt
  * (reference src/charm_amr.c:12-48, 350-573): flags[e] = 1 where
  * |grad rho|^2/12 * V^(5/3) > max_err^2 * V.  grad_out ([3][E], may be NULL)
- * receives the gradient estimate. */
+ * receives the gradient estimate.  On general hexahedra V is each element's
+ * quadrature volume and the estimate uses the faces' own normals. */
 int charm_gpu_refine_flags(charm_gpu_handle_t h, double max_err, int8_t *flags, double *grad_out);
 
 /* Stream control and synchronisation.  charm_gpu_sync waits at most
@@ -517,7 +523,10 @@ int charm_host_forest_adapt(charm_host_forest_t f, const int8_t *flags, int minl
  * their centre densities; level > minlevel; families refined in this same
  * adapt are not coarsened), then 2:1 face balance.  The state is projected
  * parent <-> children as charm_replace_quads does (:206-307; exact for p1
- * on boxes).  grad: [3][E] from charm_gpu_refine_flags; u_in: [V][B][E]
+ * on boxes; on an unstructured forest by the quadrature of the trilinear
+ * cells, each leaf's own volume in the criteria, and the first child's for
+ * a family as the reference takes it).  grad: [3][E] from
+ * charm_gpu_refine_flags; u_in: [V][B][E]
  * of the leaves before the adapt.  The new state ([V][B][n_new]) is returned
  * by charm_host_forest_state and stays valid until the next adapt or free. */
 int charm_host_forest_adapt_state(charm_host_forest_t f, const double *grad, double max_err, int minlevel, int maxlevel,

@@ -1533,7 +1533,6 @@ int oracle_run(oracle_t *o, int nsteps, double dt)
  * boundary faces the right state is the boundary condition's ghost. */
 int oracle_amr_grad(oracle_t *o, double *grad)
 {
-    if (o->hex) return -1;   /* box meshes */
     const int64_t E = o->E;
     memset(grad, 0, sizeof(double) * 3 * (size_t) E);
     for (int64_t j = 0; j < o->Fb; j++) {   /* _charm_amr_par_calc_face_iter_bnd (:362-423) */
@@ -1542,7 +1541,7 @@ int oracle_amr_grad(oracle_t *o, double *grad)
         const elem_geom_t *g = &o->g[e];
         double gp[NFQMAX][3], gwj[NFQMAX], n[3];
         face_points(o, g, f, gp, gwj);
-        outward_normal(f, n);
+        elem_normal(o, e, f, n);
         for (int q = 0; q < NFQ; q++) {
             double U[MAXV];
             prim_t pr[2];
@@ -1557,14 +1556,20 @@ int oracle_amr_grad(oracle_t *o, double *grad)
         const int32_t e[2] = {o->face_elem[f], o->face_elem[o->F + f]};
         const int d = o->face_info[f] & 3, kind = (o->face_info[f] >> 2) & 3;
         double c1[3];
-        side1_center(o, f, c1);
+        if (o->hex) memcpy(c1, o->g[e[1]].c, sizeof(c1));
+        else side1_center(o, f, c1);
         const double *cs[2] = {o->g[e[0]].c, c1};
         const int hs = (kind == 2) ? 1 : 0;
         elem_geom_t pg = o->g[e[hs]];
         memcpy(pg.c, cs[hs], sizeof(double) * 3);
         double gp[NFQMAX][3], gwj[NFQMAX], n[3];
-        face_points(o, &pg, hs ? 2 * d : 2 * d + 1, gp, gwj);
-        outward_normal(2 * d + 1, n);
+        if (o->hex) {
+            face_points(o, &pg, o->face_face[hs ? o->F + f : f], gp, gwj);
+            hex_normal(&o->g[e[0]], o->face_face[f], n);
+        } else {
+            face_points(o, &pg, hs ? 2 * d : 2 * d + 1, gp, gwj);
+            outward_normal(2 * d + 1, n);
+        }
         for (int q = 0; q < NFQ; q++) {
             prim_t pr[2];
             for (int s = 0; s < 2; s++) {
@@ -1579,6 +1584,81 @@ int oracle_amr_grad(oracle_t *o, double *grad)
     }
     for (int64_t e = 0; e < E; e++)          /* _charm_amr_par_calc_quad_iter_fn (:564-573) */
         for (int k = 0; k < 3; k++) grad[k * E + e] /= o->g[e].vol;
+    return 0;
+}
+
+/* charm_replace_quads (src/charm_amr.c:206-307) for one family of general
+ * hexahedra, p1: parent corners vp [8][3] and child corners vc [8][8][3]
+ * (child ids in Morton order).  down != 0: the 8 children [8][V][4] from
+ * the parent's coefficients [V][4] (refinement); down == 0: the parent
+ * from the children's (coarsening).  ar[m][n] = sum over the target's (or
+ * each source's) Gauss points of gw gj phi_m phi_n, then A^-1 (ar u).
+ * Returns -1 for a non-positive Jacobian. */
+int oracle_hex_project(const charm_gpu_config_t *cfg, const double *vp, const double *vc, int down, const double *src,
+                       double *dst)
+{
+    oracle_t o;
+    memset(&o, 0, sizeof(o));
+    o.cfg = *cfg;
+    o.nb = 4; o.nq = 8; o.nfq = 6;
+    o.V = 4 + cfg->n_comp;
+    oracle_t *op = &o;
+    elem_geom_t P, C[8];
+    double v[8][3];
+    memcpy(v, vp, sizeof(v));
+    if (hex_elem_geom(op, &P, v)) return -1;
+    for (int i = 0; i < 8; i++) {
+        memcpy(v, vc + 24 * i, sizeof(v));
+        if (hex_elem_geom(op, &C[i], v)) return -1;
+    }
+    const int V = o.V;
+#define NB_ 4
+    if (down) {
+        for (int i = 0; i < 8; i++) {
+            double ar[NB_][NB_];
+            for (int m = 0; m < NB_; m++)
+                for (int n = 0; n < NB_; n++) {
+                    ar[m][n] = 0.;
+                    for (int q = 0; q < 8; q++)
+                        ar[m][n] += C[i].qgj[q] * base_func(C[i].qgp[q], m, C[i].c, C[i].dh) *
+                                    base_func(C[i].qgp[q], n, P.c, P.dh);
+                }
+            for (int vv = 0; vv < V; vv++) {
+                double rhs[NB_];
+                for (int m = 0; m < NB_; m++) {
+                    rhs[m] = 0.;
+                    for (int n = 0; n < NB_; n++) rhs[m] += ar[m][n] * src[vv * NB_ + n];
+                }
+                for (int k = 0; k < NB_; k++) {
+                    double x = 0.;
+                    for (int m = 0; m < NB_; m++) x += C[i].a_inv[k][m] * rhs[m];
+                    dst[(i * V + vv) * NB_ + k] = x;
+                }
+            }
+        }
+    } else {
+        for (int vv = 0; vv < V; vv++) {
+            double rhs[NB_] = {0., 0., 0., 0.};
+            for (int i = 0; i < 8; i++) {
+                double ar[NB_][NB_];
+                for (int m = 0; m < NB_; m++)
+                    for (int n = 0; n < NB_; n++) {
+                        ar[m][n] = 0.;
+                        for (int q = 0; q < 8; q++)
+                            ar[m][n] += C[i].qgj[q] * base_func(C[i].qgp[q], m, P.c, P.dh) *
+                                        base_func(C[i].qgp[q], n, C[i].c, C[i].dh);
+                    }
+                for (int m = 0; m < NB_; m++)
+                    for (int n = 0; n < NB_; n++) rhs[m] += ar[m][n] * src[(i * V + vv) * NB_ + n];
+            }
+            for (int k = 0; k < NB_; k++) {
+                double x = 0.;
+                for (int m = 0; m < NB_; m++) x += P.a_inv[k][m] * rhs[m];
+                dst[vv * NB_ + k] = x;
+            }
+        }
+    }
+#undef NB_
     return 0;
 }
 

@@ -31,6 +31,7 @@ def load() -> C.CDLL:
         lib.oracle_amr_grad.argtypes = [C.c_void_p, C.c_void_p]
         lib.oracle_rim.argtypes = [C.c_int64, C.c_void_p, C.c_void_p]
         lib.oracle_cfl_dt.argtypes = [C.c_void_p, C.c_void_p]
+        lib.oracle_hex_project.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
         _lib = lib
     return _lib
 
@@ -135,4 +136,21 @@ def rim(inputs: np.ndarray) -> np.ndarray:
     a = np.ascontiguousarray(inputs, dtype=np.float64).reshape(-1, 11)
     out = np.empty((a.shape[0], 6))
     load().oracle_rim(a.shape[0], a.ctypes.data, out.ctypes.data)
+    return out
+
+
+def hex_project(cfg, parent_corners: np.ndarray, child_corners: np.ndarray, down: bool, src: np.ndarray) -> np.ndarray:
+    """The reference's charm_replace_quads on one family of general
+    hexahedra (oracle_hex_project): corners [8][3] and [8][8][3]; down: the
+    children [8][V][4] from the parent [V][4], else the parent from the
+    children."""
+    lib = load()
+    V = 4 + cfg.n_comp
+    vp = np.ascontiguousarray(parent_corners, dtype=np.float64)
+    vc = np.ascontiguousarray(child_corners, dtype=np.float64)
+    a = np.ascontiguousarray(src, dtype=np.float64)
+    out = np.empty((8, V, 4) if down else (V, 4))
+    if lib.oracle_hex_project(C.addressof(cfg), vp.ctypes.data, vc.ctypes.data, 1 if down else 0, a.ctypes.data,
+                              out.ctypes.data):
+        raise ValueError("non-positive Jacobian")
     return out

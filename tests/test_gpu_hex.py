@@ -20,7 +20,9 @@ from charm_3d_gb300.solver import Forest, Solver
 from oracle.port import Port
 
 from .common import rel_l2, rel_max, small_case
-from .hexmesh import SIDE_PATCHES, WEDGE_PATCHES, block_forest, block_mesh, wedge_mesh
+from charm_3d_gb300.hexmesh import ramp_channel
+
+from .hexmesh import WEDGE_PATCHES, block_forest, block_mesh, wedge_mesh
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-12
@@ -77,30 +79,8 @@ def test_hex_mortars_across_rotated_trees_match_oracle(model):
 
 
 def ramp_case(level: int = 0, n: int = 3):
-    """The sample case's physics on the ramp channel: Euler, HLLC, BJ, air at
-    300 K and 101325 Pa entering at 697.7082 m/s (samples/klin_amr/task.yaml's
-    values), outlet, slip walls; seeded +-1 % density noise."""
-    case = synthetic("sod", level=level)
-    case.model, case.flux, case.limiter = "EULER", "HLLC", "BJ"
-    T, P, V = 300.0, 101325.0, 697.7082
-    case.boundaries = [Boundary("LEFT", "BOUND_INLET", (V, 0.0, 0.0, T, P)), Boundary("RIGHT", "BOUND_OUTLET"),
-                       Boundary("BOTTOM", "BOUND_WALL_SLIP"), Boundary("TOP", "BOUND_WALL_SLIP"),
-                       Boundary("FRONT", "BOUND_WALL_SLIP"), Boundary("BACK", "BOUND_WALL_SLIP")]
-    m = wedge_mesh(n, rotate=True, seed=9)
-    forest = Forest.from_hex(m.vert, m.trees, m.tree_bnd(WEDGE_PATCHES), level)
-    mesh = forest.flatten()
-    comp = case.components[0]
-    rho = P * comp.m / (8.31446261815324 * T)
-    E = mesh.n_elem
-    rng = np.random.default_rng(4)
-    r = rho * (1.0 + 0.01 * rng.uniform(-1, 1, E))
-    one = np.ones(E)
-    u0 = np.zeros((case.n_var, 4, E))
-    u0[:, 0, :] = case.cons_from_prim(r, V * one, 0 * one, 0 * one, P * one)
-    # CFL 0.1 with the smallest edge (the ramp block's cells) and |u| + c
-    h = 1000.0 / n / 2 ** level
-    case.tau = 0.1 * h / (V + np.sqrt(1.4 * P / rho))
-    return case, forest, mesh, u0
+    """The sample case's physics on the ramp channel (charm_3d_gb300.hexmesh.ramp_channel)."""
+    return ramp_channel(level, n, rotate=True, seed=9)
 
 
 @pytest.mark.parametrize("level,n", [(0, 3), (1, 3), (0, 10)])
@@ -180,3 +160,67 @@ def test_hex_upload_rejects_inverted_elements_and_keeps_the_mesh():
     gpu.sync()
     port.run(2, case.tau)
     assert rel_l2(gpu.get_state(), port.get_state()) < TOL
+
+
+def _amr_loop(case, forest, u0, steps, period, max_err, max_level, gpu_side):
+    """The AMR time loop of the sample case (charm_model_ns_timestep_single's
+    adapt every REFINE_PERIOD steps, src/charm_amr.c:575-610) on an
+    unstructured forest: the density-gradient estimate from the GPU or the
+    oracle, the host octree's adapt with the quadrature projections, then
+    the steps on the new mesh."""
+    mesh = forest.flatten()
+    u = u0
+    n_adapt = 0
+    for step in range(steps):
+        if step and step % period == 0:
+            if gpu_side:
+                grad = solver.refine_flags(max_err)[1]
+                u = solver.get_state()
+            else:
+                grad = solver.amr_grad()
+                u = solver.get_state()
+            n0 = len(forest)
+            u = forest.adapt_state(grad, max_err, 0, max_level, case.n_comp, u)
+            n_adapt += len(forest) != n0
+            mesh = forest.flatten()
+        if step == 0 or (step % period == 0):
+            if gpu_side:
+                solver = Solver(case)
+                solver.upload(mesh)
+            else:
+                solver = Port(case.config(), mesh)
+            solver.set_state(u)
+        solver.step(case.tau)
+    if gpu_side:
+        solver.sync()
+    return solver.get_state(), forest.leaves(), n_adapt
+
+
+def test_hex_refine_indicator_matches_oracle():
+    case, forest, mesh, u0 = ramp_case(0)
+    gpu = Solver(case)
+    gpu.upload(mesh)
+    port = Port(case.config(), mesh)
+    gpu.set_state(u0)
+    port.set_state(u0)
+    gpu.run(4, case.tau)
+    port.run(4, case.tau)
+    gpu.sync()
+    port.set_state(gpu.get_state())
+    _, grad = gpu.refine_flags(0.01)
+    assert rel_max(grad, port.amr_grad()) < TOL
+
+
+def test_hex_amr_loop_matches_oracle():
+    """The sample case's controls (MAX_ERROR 0.01, MAX_LEVEL 1, REFINE_PERIOD
+    10) on the ramp channel over 40 steps: the same leaves and states 1e-12
+    apart."""
+    case, _, _, u0 = ramp_case(0)
+    m = wedge_mesh(3, rotate=True, seed=9)
+    fo = Forest.from_hex(m.vert, m.trees, m.tree_bnd(WEDGE_PATCHES), 0)
+    fg = Forest.from_hex(m.vert, m.trees, m.tree_bnd(WEDGE_PATCHES), 0)
+    uo, (qo, lo), nao = _amr_loop(case, fo, u0, 40, 10, 0.01, 1, False)
+    ug, (qg, lg), nag = _amr_loop(case, fg, u0, 40, 10, 0.01, 1, True)
+    assert nao > 0 and (lo == 1).any(), "the shock off the ramp refines"
+    assert np.array_equal(qo, qg) and np.array_equal(lo, lg)
+    assert rel_l2(ug, uo) < TOL

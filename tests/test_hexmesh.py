@@ -16,7 +16,7 @@ from charm_3d_gb300.abi import EINVAL, CharmGpuError
 from charm_3d_gb300.solver import Forest
 from oracle.port import Port
 
-from .common import rel_max
+from .common import rel_max, small_case
 from .hexmesh import (FACE_CORNERS, SIDE_PATCHES, WEDGE_PATCHES, block_forest, block_mesh, keystone, wedge_mesh,
                       write_gmsh)
 
@@ -251,3 +251,59 @@ def test_generated_ramp_channel_is_the_reference_sample_mesh():
     assert sample.n_elem == ours.n_elem == 800
     assert corner_sets(sample) == corner_sets(ours)
     assert patches(sample) == patches(ours)
+
+
+def _leaf_key(q, lv):
+    return (int(q[3]), int(q[0]), int(q[1]), int(q[2]), int(lv))
+
+
+@pytest.mark.parametrize("mode", ["refine", "coarsen"])
+def test_host_adapt_projects_like_the_reference_on_hexahedra(mode):
+    """charm_host_forest_adapt_state on an unstructured forest: every new
+    leaf's coefficients are the oracle's restatement of charm_replace_quads
+    (src/charm_amr.c:206-307, quadrature on the trilinear cells) applied to
+    its family, and the refine/coarsen decisions follow the reference's
+    criteria with each leaf's own volume."""
+    from oracle.port import hex_project
+    case = small_case("random", "HLLC", "BJ")
+    forest, _ = block_forest(case, level=1, seed=8)
+    old = forest.flatten()
+    qo, lvo = forest.leaves()
+    E = old.n_elem
+    u0 = case.initial_state(old.center)
+    if mode == "refine":   # a large gradient in tree 0 only: its leaves refine
+        grad = np.zeros((3, E))
+        grad[0, qo[:, 3] == 0] = 1.0e3
+        u1 = forest.adapt_state(grad, 0.01, 0, 2, case.n_comp, u0)
+    else:                  # no gradient, equal densities: every family coarsens
+        u0[4:, 0, :] = 1.0
+        grad = np.zeros((3, E))
+        u1 = forest.adapt_state(grad, 10.0, 0, 2, case.n_comp, u0)
+    new = forest.flatten()
+    qn, lvn = forest.leaves()
+    old_at = {_leaf_key(q, l): i for i, (q, l) in enumerate(zip(qo, lvo))}
+    cfg = case.config()
+    checked = 0
+    for k, (q, l) in enumerate(zip(qn, lvn)):
+        if _leaf_key(q, l) in old_at:
+            assert np.array_equal(u1[:, :, k], u0[:, :, old_at[_leaf_key(q, l)]])
+            continue
+        if mode == "refine":
+            h = 1 << (19 - int(l))
+            parent = (int(q[3]), int(q[0]) & ~h, int(q[1]) & ~h, int(q[2]) & ~h, int(l) - 1)
+            p = old_at[parent]
+            cid = (1 if q[0] & h else 0) | (2 if q[1] & h else 0) | (4 if q[2] & h else 0)
+            # the parent's children, in Morton order, are the new leaves k - cid .. k - cid + 7
+            kids = np.arange(k - cid, k - cid + 8)
+            want = hex_project(cfg, old.vertex[:, :, p], new.vertex[:, :, kids].transpose(2, 0, 1), True,
+                               u0[:, :, p])[cid]
+        else:
+            h = 1 << (19 - int(l) - 1)
+            kids = [old_at[(int(q[3]), int(q[0]) + (c & 1) * h, int(q[1]) + ((c >> 1) & 1) * h,
+                            int(q[2]) + ((c >> 2) & 1) * h, int(l) + 1)] for c in range(8)]
+            want = hex_project(cfg, new.vertex[:, :, k], old.vertex[:, :, kids].transpose(2, 0, 1), False,
+                               u0[:, :, kids].transpose(2, 0, 1))
+        assert rel_max(u1[:, :, k], want) < 1e-13, k
+        checked += 1
+    assert checked > 0
+    assert new.n_elem == (E + 7 * 8 if mode == "refine" else E // 8)
