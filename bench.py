@@ -11,9 +11,16 @@ Lines printed (rank 0, one JSON object each run):
   * our arm: plain FP64 path (the drop-in) as `value`, with
       - `e2e`: the same metric through the C ABI with host buffers (state
         H2D + step + state D2H every step),
-      - `mixed`: the FP32-residual / FP64-state form on the same steps with
-        its error against the FP64 path,
-      - `roofline`, `cpu_baseline`, `clocks`, `gpu_launches`.
+      - `mixed`: the FP32-residual / FP32 hi-lo-state form on the same steps
+        with its error against the FP64 path; `double_word`: the FP32-pair
+        form held to the drop-in's bar,
+      - `roofline` (HBM, and the FP64 pipe's counted rate), `cpu_baseline`,
+        `clocks`, `gpu_launches`, `parity` (the FP64 state vs the oracle),
+      - summaries of the legs on the other configurations: `adjoint`
+        (config 5), `reacting_ns` (config 4, p2), `blast_amr` (config 3),
+        `p2_contraction` (tensor cores vs FMA) and `hex_sample` (the
+        reference's sample case on its trilinear hexahedra); their full
+        records are in `details`.
   * --impl reference: the reference's CPU algorithm (the oracle
     restatement, all host cores) on a bounded sample of the same workload.
 
@@ -409,7 +416,9 @@ def finish(args, rank, world, device, case, mesh, E, V, state_bytes, t_mesh, val
     adjoint = run_adjoint(args, device) if args.adjoint_steps > 0 else None
     flame = run_flame(args, device) if args.flame_steps > 0 else None
     blast = run_blast(args, device) if args.blast_steps > 0 else None
+    blast_rel = run_blast(args, device, relative=0.1) if args.blast_steps > 0 else None
     tc = run_tc(args) if args.tc_reps > 0 else None
+    hexs = run_hex(args, device) if args.hex_steps > 0 else None
     n_launch = int(launches.sum())
     # the full records first; the one-line summaries of the extra legs last,
     # where a reader of the end of the line finds them
@@ -418,7 +427,8 @@ def finish(args, rank, world, device, case, mesh, E, V, state_bytes, t_mesh, val
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded isentropic vortex + 1e-3 density noise)",
             "config": bench_config(args, world, E, V, state_bytes, t_mesh),
             "details": {"mixed": mixed, "double_word": dwf, "adjoint": adjoint, "reacting_ns": flame,
-                        "blast_amr": blast, "p2_contraction": tc},
+                        "blast_amr": blast, "blast_amr_relative": blast_rel, "p2_contraction": tc,
+                        "hex_sample": hexs},
             "e2e": e2e,
             "roofline": roofline,
             "cpu_baseline": cpu,
@@ -427,7 +437,8 @@ def finish(args, rank, world, device, case, mesh, E, V, state_bytes, t_mesh, val
             "parity": parity,
             "mixed": summary_mixed(mixed), "double_word": summary_dw(dwf), "adjoint": summary_adjoint(adjoint),
             "reacting_ns": summary_flame(flame), "blast_amr": summary_blast(blast),
-            "p2_contraction": summary_tc(tc)}
+            "blast_amr_relative": summary_blast(blast_rel), "p2_contraction": summary_tc(tc),
+            "hex_sample": summary_hex(hexs)}
 
 
 def bench_config(args, world: int, E: int, V: int, state_bytes: int, t_mesh: float | None) -> dict:
@@ -482,6 +493,13 @@ def summary_flame(f):
     return out
 
 
+def summary_hex(x):
+    if not x:
+        return None
+    return {"value": _r(x["value"]), "ms_per_step": _r(x["ms_per_step"]), "elements": x["elements"],
+            "parity_rel_l2": _r(x["parity"]["oracle_rel_l2"])}
+
+
 def summary_tc(t):
     if not t or "tcgen05_over_fma_time" not in t:
         return None
@@ -494,7 +512,8 @@ def summary_blast(b):
         return None
     return {"fp64_value": _r(b["fp64"]["value"]), "mixed_value": _r(b["mixed"]["value"]),
             "mixed_e2e": _r(b["mixed"]["e2e_dof_updates_per_s"]), "mixed_adapt_share":
-                _r(b["mixed"]["adapt_s"] / b["mixed"]["wall_s"], 3), "same_mesh": b["same_mesh"]}
+                _r(b["mixed"]["adapt_s"] / b["mixed"]["wall_s"], 3), "same_mesh": b["same_mesh"],
+            "final_elements": b["mixed"]["final_elements"]}
 
 
 def run_adjoint(args, device: int) -> dict:
@@ -718,10 +737,12 @@ def run_flame(args, device: int) -> dict:
     return out
 
 
-def _blast_run(case, steps: int, device: int, precision: str):
+def _blast_run(case, steps: int, device: int, precision: str, relative: float = 0.0):
     """The AMR time loop of charm_model_ns_timestep_single on the GPU: the
-    reference criterion (charm_gpu_refine_flags) and the host octree's adapt
-    with projection every refine_period steps, then upload and continue."""
+    reference criterion (charm_gpu_refine_flags; or, with relative > 0, the
+    configuration's |grad rho| h / rho > relative, charm_gpu_refine_flags_relative)
+    and the host octree's adapt with projection every refine_period steps,
+    then upload and continue."""
     from charm_3d_gb300.solver import Forest, Solver
     case.precision = precision
     forest = Forest(case)
@@ -739,10 +760,15 @@ def _blast_run(case, steps: int, device: int, precision: str):
             # the state stays on the device: the host plans the adapt from the
             # gradient estimate and the densities, the device projects
             ta = time.perf_counter()
-            _, grad = gpu.refine_flags(case.max_err)
-            rho = gpu.density_means()
-            tb = time.perf_counter()
-            _, plan = forest.adapt_plan(grad, rho, case.max_err, case.min_level, case.max_level)
+            if relative > 0.0:
+                flags, _ = gpu.refine_flags_relative(relative, True)
+                tb = time.perf_counter()
+                _, plan = forest.adapt_plan_flags(flags, case.min_level, case.max_level)
+            else:
+                _, grad = gpu.refine_flags(case.max_err)
+                rho = gpu.density_means()
+                tb = time.perf_counter()
+                _, plan = forest.adapt_plan(grad, rho, case.max_err, case.min_level, case.max_level)
             tc = time.perf_counter()
             mesh = forest.flatten()
             td = time.perf_counter()
@@ -780,17 +806,22 @@ def _shock_radius(mesh, u, gam):
     return float(r[hot].max()) if hot.any() else 0.0
 
 
-def run_blast(args, device: int) -> dict:
+def run_blast(args, device: int, relative: float = 0.0) -> dict:
     """Spherical blast on AMR (base level 5, max 8, refine every 10 steps),
-    HLLC + BJ limiter: FP64 and the mixed form on the same loop."""
+    HLLC + BJ limiter: FP64 and the mixed form on the same loop; the
+    reference's refine criterion, or with relative > 0 the configuration's
+    |grad rho| h / rho > relative per cell."""
     from charm_3d_gb300 import synthetic
-    out = {"workload": f"blast p=1 in r<0.1, p=0.1 outside, rho=1 +-1% noise; levels 5..8, reference refine "
-                       f"criterion every 10 steps, HLLC, BJ limiter, {args.blast_steps} steps"}
+    crit = (f"|grad rho| h / rho > {relative} per cell (coarsen below half of it)" if relative > 0.0
+            else "reference refine criterion")
+    out = {"workload": f"blast p=1 in r<0.1, p=0.1 outside, rho=1 +-1% noise; levels 5..8, {crit} "
+                       f"every 10 steps, HLLC, BJ limiter, {args.blast_steps} steps"}
     res = {}
     for prec in ("FP64", "MIXED"):
         case = synthetic("blast")
         _, gam = case.gas_constants()
-        forest, mesh, u, dev_ms, dofs, wall, t_adapt, drift, parts = _blast_run(case, args.blast_steps, device, prec)
+        forest, mesh, u, dev_ms, dofs, wall, t_adapt, drift, parts = _blast_run(case, args.blast_steps, device, prec,
+                                                                                relative)
         q, lv = forest.leaves()
         res[prec] = (q, lv, u, mesh)
         out[prec.lower()] = {"value": dofs / (dev_ms * 1e-3), "unit": UNIT, "device_ms": dev_ms,
@@ -808,6 +839,54 @@ def run_blast(args, device: int) -> dict:
         out["rel_l2_density_mixed_vs_fp64"] = float(np.linalg.norm(rho1 - rho0) / np.linalg.norm(rho0))
     out["speedup_mixed_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
     return out
+
+
+def run_hex(args, device: int) -> dict:
+    """The reference's sample case (samples/klin_amr: Euler, HLLC, BJ,
+    inlet / outlet / slip walls) on its 800-hexahedron ramp geometry, the
+    trees refined uniformly to --hex-level, on the general-hexahedron
+    kernels (FP64): device time of --hex-steps steps, kernel shares, and
+    the state against the oracle after 10 steps at level 0."""
+    from charm_3d_gb300.hexmesh import ramp_channel
+    from charm_3d_gb300.solver import Solver
+    from oracle.port import Port
+    case, _, mesh, u0 = ramp_channel(args.hex_level, 10)
+    g = Solver(case, device)
+    g.upload(mesh)
+    g.set_state(u0)
+    g.run(args.warmup, case.tau)
+    g.sync()
+    g.set_state(u0)
+    g.reset_stats()
+    g.set_timing(True)
+    ms = g.time_run(args.hex_steps, case.tau)
+    g.set_timing(False)
+    n_l, k_ms = g.kernel_stats()
+    u = g.get_state()
+    g.close()
+    E, V = mesh.n_elem, case.n_var
+    # parity on the sample's own size: 10 steps, GPU vs oracle
+    c0, _, m0, v0 = ramp_channel(0, 10)
+    gp = Solver(c0, device)
+    gp.upload(m0)
+    gp.set_state(v0)
+    gp.run(10, c0.tau)
+    gp.sync()
+    port = Port(c0.config(), m0)
+    port.set_state(v0)
+    port.run(10, c0.tau)
+    a, b = gp.get_state(), port.get_state()
+    gp.close()
+    names = ["face", "cell", "limiter", "other"]
+    # Euler model: one stage per step
+    dofs = E * V * 4 * args.hex_steps
+    return {"workload": f"samples/klin_amr geometry (800 trilinear hexahedra, ramp 10 deg) at level {args.hex_level} "
+                        f"({E} elements), Euler, HLLC, BJ, inlet/outlet/slip, FP64, forward Euler steps",
+            "value": dofs / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms / args.hex_steps, "elements": E,
+            "kernel_share": {n: float(k_ms[i] / k_ms.sum()) for i, n in enumerate(names)},
+            "finite": bool(np.isfinite(u).all()),
+            "parity": {"oracle_rel_l2": float(np.linalg.norm(a - b) / np.linalg.norm(b)), "elements": int(m0.n_elem),
+                       "steps": 10}}
 
 
 def run_tc(args) -> dict:
@@ -900,7 +979,8 @@ def main():
     ap.add_argument("--parity-steps", type=int, default=20,
                     help="oracle steps on the level --cpu-level sample (cpu_baseline and parity; 0 skips both)")
     ap.add_argument("--brick", type=int, default=1, help="trees along x (profiling sizes)")
-    ap.add_argument("--only", default="both", choices=["both", "fp64", "mixed", "dw", "adjoint", "flame", "blast", "tc"])
+    ap.add_argument("--only", default="both",
+                    choices=["both", "fp64", "mixed", "dw", "adjoint", "flame", "blast", "tc", "hex"])
     ap.add_argument("--blast-steps", type=int, default=200, help="0 skips the AMR blast leg")
     ap.add_argument("--flame-level", type=int, default=6)
     ap.add_argument("--flame-order", type=int, default=2, choices=[1, 2], help="basis order of the reacting leg")
@@ -915,6 +995,8 @@ def main():
                     help="checkpoints of the memory-bounded adjoint timing (0 skips it)")
     ap.add_argument("--adjoint-fd-eps", type=float, default=1e-6, help="central-difference step")
     ap.add_argument("--tc-reps", type=int, default=20, help="timed launches of the p2 contraction leg (0 skips it)")
+    ap.add_argument("--hex-level", type=int, default=3, help="uniform level of the sample-geometry leg")
+    ap.add_argument("--hex-steps", type=int, default=20, help="timed steps of the sample-geometry leg (0 skips it)")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-dw", action="store_true", help="skip the double-word form's leg")
     args = ap.parse_args()
@@ -947,7 +1029,12 @@ def main():
         return
     if args.only == "blast":
         if rank == 0:
-            print(json.dumps({"only": "blast", "blast_amr": run_blast(args, local)}))
+            print(json.dumps({"only": "blast", "blast_amr": run_blast(args, local),
+                              "blast_amr_relative": run_blast(args, local, relative=0.1)}))
+        return
+    if args.only == "hex":
+        if rank == 0:
+            print(json.dumps({"only": "hex", "hex_sample": run_hex(args, local)}))
         return
     if args.only == "tc":
         if rank == 0:

@@ -150,6 +150,7 @@ SIGNATURES = [
     ("charm_gpu_adjoint", C.c_int, [_P, C.c_int, C.c_int, C.POINTER(Objective), _P, _P, C.POINTER(AdjointInfo)]),
     ("charm_gpu_refine_flags_adjoint", C.c_int, [_P, C.c_double, _P, _P]),
     ("charm_gpu_density_means", C.c_int, [_P, _P]),
+    ("charm_gpu_refine_flags_relative", C.c_int, [_P, C.c_double, C.c_int, _P, _P]),
     ("charm_gpu_cell_fields", C.c_int, [_P, _P]),
     ("charm_gpu_adapt_upload", C.c_int, [_P, C.POINTER(AdaptPlan), C.POINTER(Mesh)]),
     ("charm_case_read_yaml", C.c_int, [C.c_char_p, C.POINTER(CaseFile)]),
@@ -163,6 +164,7 @@ SIGNATURES = [
     ("charm_host_forest_state", C.c_int, [_P, C.POINTER(_DP)]),
     ("charm_host_forest_adapt_plan", C.c_int, [_P, _P, _P, C.c_double, C.c_int, C.c_int, _I64P,
                                                C.POINTER(AdaptPlan)]),
+    ("charm_host_forest_adapt_plan_flags", C.c_int, [_P, _P, C.c_int, C.c_int, _I64P, C.POINTER(AdaptPlan)]),
     ("charm_host_forest_flatten", C.c_int, [_P, C.POINTER(Mesh)]),
     ("charm_host_forest_leaves", C.c_int, [_P, _P, _P]),
     ("charm_host_forest_write_vtu", C.c_int, [_P, C.c_char_p, C.c_int, C.POINTER(C.c_char_p), _P]),

@@ -316,7 +316,8 @@ int validate_config(const charm_gpu_config_t *c)
             return fail(CHARM_GPU_EINVAL, "unknown boundary type");
     if (c->p_order < 0 || c->p_order > 2) return fail(CHARM_GPU_EINVAL, "p_order must be 1 or 2");
     if (c->p_order == 2) {
-        if (c->limiter != CHARM_GPU_LIM_NONE) return fail(CHARM_GPU_ENOTSUP, "p2: limiter not supported");
+        if (c->limiter != CHARM_GPU_LIM_NONE && c->precision != CHARM_GPU_PREC_FP64)
+            return fail(CHARM_GPU_ENOTSUP, "p2: the limiter runs in the FP64 form only");
         if (c->dt_mode != CHARM_GPU_DT_TAU) return fail(CHARM_GPU_ENOTSUP, "p2: fixed time step (TAU) only");
     }
     if (c->n_react < 0 || c->n_react > CHARM_GPU_MAX_REACT) return fail(CHARM_GPU_EINVAL, "bad reaction count");
@@ -764,6 +765,17 @@ int launch_p2_vflux(charm_gpu_handle_s *h, const T *u)
 
 // one FP64 p2 stage (or, with mode kCellResidual, the residual without chemistry)
 template <int NC>
+int launch_p2_limit(charm_gpu_handle_s *h, const double *ua, const double *u0, double *out, double a_new, double a_old)
+{
+    TimedLaunch t;
+    begin_launch(h, 2, &t);
+    p2_launch_limit<NC>(mesh_view(h), ua, u0, out, a_new, a_old, h->stream);
+    end_launch(h, &t);
+    CUDA_TRY(cudaGetLastError());
+    return CHARM_GPU_OK;
+}
+
+template <int NC>
 int p2_stage(charm_gpu_handle_s *h, const double *u, const double *u0, double *out, double dt, const double *dt_dev,
              double a_new, double a_old, int mode)
 {
@@ -853,7 +865,13 @@ int stage(charm_gpu_handle_s *h, const double *u, const double *u0, double *out,
     int rc;
     const double *radd = nullptr;
     if constexpr (std::is_same<T, double>::value)
-        if (h->nb == kNB2) return p2_stage<NC>(h, u, u0, out, dt, dt_dev, a_new, a_old, kCellUpdate);
+        if (h->nb == kNB2) {
+            if (h->cfg.limiter == CHARM_GPU_LIM_BJ) {   // cell update -> ua, limiter + combination -> out
+                if ((rc = p2_stage<NC>(h, u, nullptr, h->d_ua, dt, dt_dev, 1.0, 0.0, kCellUpdate))) return rc;
+                return launch_p2_limit<NC>(h, h->d_ua, u0, out, a_new, a_old);
+            }
+            return p2_stage<NC>(h, u, u0, out, dt, dt_dev, a_new, a_old, kCellUpdate);
+        }
     if constexpr (std::is_same<T, double>::value) {
         if (has_visc_chem(h)) {
             if (h->cfg.n_react) {
@@ -1795,6 +1813,41 @@ int charm_gpu_density_means(charm_gpu_handle_t h, double *rho)
     return CHARM_GPU_OK;
 }
 
+int charm_gpu_refine_flags_relative(charm_gpu_handle_t h, double threshold, int per_cell, int8_t *flags,
+                                    double *grad_out)
+{
+    if (!h || !flags) return fail(CHARM_GPU_EINVAL, "null argument");
+    if (!(threshold > 0.0)) return fail(CHARM_GPU_EINVAL, "threshold must be positive");
+    if (!h->mesh_ready) return fail(CHARM_GPU_ESTATE, "no mesh uploaded");
+    const int64_t E = h->E;
+    std::vector<double> g(grad_out ? 0 : (size_t) (3 * E)), rho((size_t) E), vol((size_t) E);
+    double *hg = grad_out ? grad_out : g.data();
+    int rc = charm_gpu_refine_flags(h, 1.0, nullptr, hg);   // the gradient estimate of charm_adapt
+    if (!rc) rc = charm_gpu_density_means(h, rho.data());
+    if (rc) return rc;
+    if (per_cell) {
+        CUDA_TRY(cudaSetDevice(h->device));
+        if (h->hex) {
+            CUDA_TRY(cudaMemcpy(vol.data(), h->d_hex_g + (size_t) kGvol * E, sizeof(double) * E, cudaMemcpyDeviceToHost));
+        } else {
+            std::vector<int8_t> lev((size_t) E);
+            CUDA_TRY(cudaMemcpy(lev.data(), h->d_level, (size_t) E, cudaMemcpyDeviceToHost));
+            for (int64_t e = 0; e < E; e++) {
+                double v = 1.0;
+                for (int d = 0; d < 3; d++) v *= ldexp(h->tree_len[d], -lev[e]);
+                vol[e] = v;
+            }
+        }
+    }
+    for (int64_t e = 0; e < E; e++) {
+        const double gn = sqrt(hg[e] * hg[e] + hg[E + e] * hg[E + e] + hg[2 * E + e] * hg[2 * E + e]);
+        const double r = rho[e] > 1.0e-12 ? rho[e] : 1.0e-12;
+        const double ind = gn * (per_cell ? cbrt(vol[e]) : 1.0) / r;
+        flags[e] = (ind > threshold) ? 1 : (ind <= 0.5 * threshold ? -1 : 0);
+    }
+    return CHARM_GPU_OK;
+}
+
 int charm_gpu_adapt_upload(charm_gpu_handle_t h, const charm_gpu_adapt_plan_t *plan, const charm_gpu_mesh_t *mesh)
 {
     CfgLease lease(h);
@@ -2000,6 +2053,11 @@ int charm_gpu_limit(charm_gpu_handle_t h)
     const bool mixed = h->cfg.precision == CHARM_GPU_PREC_MIXED;
     if (mixed && (rc = ff_convert(h, false))) return rc;   // d_u <- hi + lo
     CUDA_TRY(cudaMemcpyAsync(h->d_ua, h->d_u, st, cudaMemcpyDeviceToDevice, h->stream));
+    if (h->nb == kNB2) {
+        rc = (h->cfg.n_comp == 1) ? launch_p2_limit<1>(h, h->d_ua, nullptr, h->d_u, 1.0, 0.0)
+                                  : launch_p2_limit<2>(h, h->d_ua, nullptr, h->d_u, 1.0, 0.0);
+        return rc;
+    }
     switch (h->cfg.n_comp) {
     case 1: rc = launch_limit<1>(h, h->d_ua, nullptr, h->d_u, 1.0, 0.0); break;
     case 2: rc = launch_limit<2>(h, h->d_ua, nullptr, h->d_u, 1.0, 0.0); break;

@@ -40,6 +40,18 @@ void p2_launch_cell(const MeshDev &m, const T *u, const T *slots, const T *u0, T
     p2_cell_kernel<T, NC><<<nb, 128, 0, st>>>(m, u, slots, u0, out, up, err, radd);
 }
 
+template <int NC>
+void p2_launch_limit(const MeshDev &m, const double *ua, const double *u0, double *out, double a_new, double a_old,
+                     cudaStream_t st)
+{
+    const unsigned nb = (unsigned) ((m.n_elem + 127) / 128);
+    p2_limit_kernel<NC><<<nb, 128, 0, st>>>(m, ua, u0, out, a_new, a_old);
+}
+template void p2_launch_limit<1>(const MeshDev &, const double *, const double *, double *, double, double,
+                                 cudaStream_t);
+template void p2_launch_limit<2>(const MeshDev &, const double *, const double *, double *, double, double,
+                                 cudaStream_t);
+
 template <typename S, int NC>
 void p2_launch_chem(const MeshDev &m, StIn<S> in, StOut<S> out, double *chem_rhs, cudaStream_t st)
 {

@@ -513,13 +513,24 @@ __device__ __forceinline__ void frame_out(const T nt[3][3], T s, T fu, T fv, T f
     }
 }
 
+// frame (optional, general normals only): the rows of normal_frame(n),
+// computed once per face by a caller that evaluates many points of it
 template <typename T, int NC, int AX = -1>
-__device__ void flux_hllc(const Prim<T, NC> &pa, const Prim<T, NC> &pb, const T n[3], T *q, unsigned *err)
+__device__ void flux_hllc(const Prim<T, NC> &pa, const Prim<T, NC> &pb, const T n[3], T *q, unsigned *err,
+                          const T (*frame)[3] = nullptr)
 {
     T nt[3][3];
     T sn = T(1);
-    if constexpr (AX < 0) normal_frame<T>(n, nt);
-    else sn = n[AX];
+    if constexpr (AX < 0) {
+        if (frame) {
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) nt[i][j] = frame[i][j];
+        } else {
+            normal_frame<T>(n, nt);
+        }
+    } else {
+        sn = n[AX];
+    }
     // velocities in the (n, t1, t2) frame
     T ua, va, wa, ub, vb, wb;
     frame_in<AX, T>(nt, sn, pa.u, pa.v, pa.w, ua, va, wa);
@@ -712,10 +723,16 @@ __device__ void riemann_exact(T &rho_o, T &e_o, T &p_o, T &u_o, T &v_o, T &w_o,
 // the exact solver above using side 0's gamma, rotate back; species are upwinded with the
 // interface mass flux.
 template <typename T, int NC>
-__device__ void flux_godunov(const Prim<T, NC> &pa, const Prim<T, NC> &pb, const T n[3], T *q)
+__device__ void flux_godunov(const Prim<T, NC> &pa, const Prim<T, NC> &pb, const T n[3], T *q,
+                             const T (*frame)[3] = nullptr)
 {
     T nt[3][3];
-    normal_frame<T>(n, nt);
+    if (frame) {
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) nt[i][j] = frame[i][j];
+    } else {
+        normal_frame<T>(n, nt);
+    }
     T va[3], vb[3];
     for (int j = 0; j < 3; j++) {
         va[j] = pa.u * nt[j][0] + pa.v * nt[j][1] + pa.w * nt[j][2];
@@ -735,12 +752,13 @@ __device__ void flux_godunov(const Prim<T, NC> &pa, const Prim<T, NC> &pb, const
 }
 
 template <int FLUX, typename T, int NC, int AX = -1>
-__device__ __forceinline__ void num_flux(const Prim<T, NC> &a, const Prim<T, NC> &b, const T n[3], T *q, unsigned *err)
+__device__ __forceinline__ void num_flux(const Prim<T, NC> &a, const Prim<T, NC> &b, const T n[3], T *q, unsigned *err,
+                                         const T (*frame)[3] = nullptr)
 {
     if (FLUX == CHARM_GPU_FLUX_LF) flux_lf<T, NC, AX>(a, b, n, q);
-    else if (FLUX == CHARM_GPU_FLUX_HLLC) flux_hllc<T, NC, AX>(a, b, n, q, err);
+    else if (FLUX == CHARM_GPU_FLUX_HLLC) flux_hllc<T, NC, AX>(a, b, n, q, err, frame);
     else if (FLUX == CHARM_GPU_FLUX_CD) flux_cd<T, NC, AX>(a, b, n, q);
-    else flux_godunov<T, NC>(a, b, n, q);
+    else flux_godunov<T, NC>(a, b, n, q, frame);
 }
 
 }  // namespace charm

@@ -5,8 +5,8 @@
 // constants; here every element and face carries its own geometry, computed
 // once per mesh upload from the element corners by the reference's
 // formulas (src/charm_geom.c):
-//   element planes  double [kHexG][E]: centre and dh (the corner bounding
-//                   box), volume, the basis values phi_1..3 and the weights
+//   element planes  double [kHexG][E]: centre, dh (the corner bounding
+//                   box) and 1/dh, volume, the basis values phi_1..3 and the weights
 //                   gw*gj at the 8 Gauss points of the trilinear map
 //                   (_charm_quad_calc_gp, :40-172), the inverse of the full
 //                   4x4 mass matrix (charm_geom_quad_calc, :496-530), the
@@ -96,6 +96,7 @@ __global__ void __launch_bounds__(128) hex_geom_kernel(HexDev x, int64_t E, doub
         dh[d] = hi - lo;
         put(kGc + d, c[d]);
         put(kGdh + d, dh[d]);
+        put(kGidh + d, 1.0 / dh[d]);
     }
     const double s3 = 0.57735026918962576451;   // 1/sqrt(3)
     double phi[8][4], w[8], vol = 0.0;
@@ -244,16 +245,19 @@ hex_face_kernel(MeshDev m, HexDev x, const double *__restrict__ u, double *__res
     const int64_t e0 = inner ? m.face_elem[r] : m.bface_elem[r - F];
     const int64_t e1 = inner ? m.face_elem[F + r] : e0;
     const int ns = inner ? 2 : 1;
-    double c0[3], c1[3], h0[3], h1[3];
+    double c0[3], c1[3], h0[3], h1[3];   // centres and 1/dh of both sides
     for (int d = 0; d < 3; d++) {
-        c0[d] = hex_g(x, E, kGc + d, e0); h0[d] = hex_g(x, E, kGdh + d, e0);
-        c1[d] = hex_g(x, E, kGc + d, e1); h1[d] = hex_g(x, E, kGdh + d, e1);
+        c0[d] = hex_g(x, E, kGc + d, e0); h0[d] = hex_g(x, E, kGidh + d, e0);
+        c1[d] = hex_g(x, E, kGc + d, e1); h1[d] = hex_g(x, E, kGidh + d, e1);
     }
     double a0[V][kNB], a1[V][kNB];
     load_coef<double, V>(u, E, e0, a0);
     if (inner) load_coef<double, V>(u, E, e1, a1);
     double n[3];
     for (int d = 0; d < 3; d++) n[d] = __ldg(x.fg + (int64_t) (kFn + d) * NR + r);
+    // the flux frame of the face's normal, once for its 6 points
+    double nt[3][3];
+    normal_frame<double>(n, nt);
     const int bid = inner ? 0 : m.bface_bnd[r - F];
     double acc[2][V][kNB];
 #pragma unroll
@@ -270,8 +274,8 @@ hex_face_kernel(MeshDev m, HexDev x, const double *__restrict__ u, double *__res
         double p0[4], p1[4];
         p0[0] = p1[0] = 1.0;
         for (int d = 0; d < 3; d++) {
-            p0[1 + d] = (gp[d] - c0[d]) / h0[d];
-            p1[1 + d] = (gp[d] - c1[d]) / h1[d];
+            p0[1 + d] = (gp[d] - c0[d]) * h0[d];
+            p1[1 + d] = (gp[d] - c1[d]) * h1[d];
         }
         double U0[V], U1[V];
 #pragma unroll
@@ -284,7 +288,7 @@ hex_face_kernel(MeshDev m, HexDev x, const double *__restrict__ u, double *__res
         if (inner) cons_to_prim<double, NC>(U1, q1);
         else bnd_cond<double, NC>(bid, q0, q1, n);
         double fl[V];
-        num_flux<FLUX, double, NC, -1>(q0, q1, n, fl, err);
+        num_flux<FLUX, double, NC, -1>(q0, q1, n, fl, err, nt);
 #pragma unroll
         for (int v = 0; v < V; v++)
 #pragma unroll
@@ -320,7 +324,7 @@ hex_cell_kernel(MeshDev m, HexDev x, const double *__restrict__ u, const double 
     if (e >= E) return;
     double c[V][kNB];
     load_coef<double, V>(u, E, e, c);
-    const double idh[3] = {1.0 / hex_g(x, E, kGdh + 0, e), 1.0 / hex_g(x, E, kGdh + 1, e), 1.0 / hex_g(x, E, kGdh + 2, e)};
+    const double idh[3] = {hex_g(x, E, kGidh, e), hex_g(x, E, kGidh + 1, e), hex_g(x, E, kGidh + 2, e)};
     double R[V][kNB];
 #pragma unroll
     for (int v = 0; v < V; v++)
@@ -533,10 +537,10 @@ hex_amr_grad_kernel(MeshDev m, HexDev x, const double *__restrict__ u, double *_
         const int64_t r = inner ? (sl >> 1) : F + (sl - 2 * F);
         const double sg = (inner && (sl & 1)) ? -1.0 : 1.0;
         const int64_t e0 = inner ? m.face_elem[r] : e, e1 = inner ? m.face_elem[F + r] : e;
-        double c0[3], c1[3], h0[3], h1[3], n[3];
+        double c0[3], c1[3], h0[3], h1[3], n[3];   // centres and 1/dh of both sides
         for (int d = 0; d < 3; d++) {
-            c0[d] = hex_g(x, E, kGc + d, e0); h0[d] = hex_g(x, E, kGdh + d, e0);
-            c1[d] = hex_g(x, E, kGc + d, e1); h1[d] = hex_g(x, E, kGdh + d, e1);
+            c0[d] = hex_g(x, E, kGc + d, e0); h0[d] = hex_g(x, E, kGidh + d, e0);
+            c1[d] = hex_g(x, E, kGc + d, e1); h1[d] = hex_g(x, E, kGidh + d, e1);
             n[d] = __ldg(x.fg + (int64_t) (kFn + d) * NR + r);
         }
         double a0[V][kNB], a1[V][kNB];
@@ -548,8 +552,8 @@ hex_amr_grad_kernel(MeshDev m, HexDev x, const double *__restrict__ u, double *_
             double p0[3], p1[3];
             for (int d = 0; d < 3; d++) {
                 const double gp = __ldg(x.fg + (int64_t) (kFgp + 3 * q + d) * NR + r);
-                p0[d] = (gp - c0[d]) / h0[d];
-                p1[d] = (gp - c1[d]) / h1[d];
+                p0[d] = (gp - c0[d]) * h0[d];
+                p1[d] = (gp - c1[d]) * h1[d];
             }
             const double wq = __ldg(x.fg + (int64_t) (kFw + q) * NR + r);
             double U0[V], U1[V];

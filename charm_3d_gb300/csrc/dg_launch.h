@@ -53,6 +53,10 @@ void p2_launch_cell(const MeshDev &m, const T *u, const T *slots, const T *u0, T
                     unsigned *err, const T *radd, cudaStream_t st);
 template <typename S, int NC>
 void p2_launch_chem(const MeshDev &m, StIn<S> in, StOut<S> out, double *chem_rhs, cudaStream_t st);
+// Barth-Jespersen limiter on the p2 basis + SSP combination (FP64)
+template <int NC>
+void p2_launch_limit(const MeshDev &m, const double *ua, const double *u0, double *out, double a_new, double a_old,
+                     cudaStream_t st);
 // diffusion coefficients (FP64 from the state; u_lo: the lo plane of the
 // mixed form), lifting and the viscous volume terms
 template <typename T, int NC>
@@ -88,7 +92,8 @@ enum {
     kGmean = 55,    // quadrature mean of phi_1..3 (over the volume)
     kGvert = 58,    // phi_1..3 at corner k: kGvert + 3 k + (k' - 1)
     kGnrm = 82,     // outward unit normal of face f: kGnrm + 3 f + d
-    kHexG = 100
+    kGidh = 100,    // 1 / dh x, y, z
+    kHexG = 103
 };
 enum { kFn = 0, kFgp = 3, kFw = 21, kHexF = 27 };
 

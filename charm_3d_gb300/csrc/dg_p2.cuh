@@ -981,4 +981,108 @@ p2_vvol_kernel(MeshDev m, const T *__restrict__ u, const T *__restrict__ vis, co
         for (int k = 0; k < kNB2; k++) radd[(int64_t) (v * kNB2 + k) * E + e] = R[v][k];
 }
 
+// ---------------------------------------------------------------------------
+// Barth-Jespersen limiter on the p2 basis (src/limiters/charm_limiter_bj.c,
+// whose loops run over CHARM_BASE_FN_COUNT) + SSP combination, FP64: the
+// own and neighbour values are quadrature means (c_0 + (c_4 + c_5 + c_6)/12
+// on a box), a hanging neighbour's is its centre value c_0, psi is the
+// minimum over the 8 corners of the p2 field, and coefficients 1..9 are
+// scaled by it.
+// ---------------------------------------------------------------------------
+template <int NC>
+__global__ void __launch_bounds__(128)
+p2_limit_kernel(MeshDev m, const double *__restrict__ ua, const double *u0, double *out, double a_new, double a_old)
+{
+    constexpr int V = 4 + NC;
+    const int64_t e = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t E = m.n_elem;
+    if (e >= E) return;
+    auto mean = [&](int64_t x, double *U) {
+#pragma unroll
+        for (int v = 0; v < V; v++) {
+            double s = 0.0;
+#pragma unroll
+            for (int k = 0; k < kNB2; k++) s += __ldg(ua + (int64_t) (v * kNB2 + k) * E + x) * c_p2.mean[k];
+            U[v] = s;
+        }
+    };
+    double own[V], umin[V], umax[V];
+    mean(e, own);
+#pragma unroll
+    for (int v = 0; v < V; v++) umin[v] = umax[v] = own[v];
+#pragma unroll 1
+    for (int f = 0; f < 6; f++) {
+        const int kind = m.lim_kind[(int64_t) f * E + e] & 3;
+        const int idx = m.lim_idx[(int64_t) f * E + e];
+        double nbv[V];
+        if (kind == 0) {
+            mean(idx, nbv);
+        } else if (kind == 3) {
+#pragma unroll
+            for (int v = 0; v < V; v++) nbv[v] = __ldg(ua + (int64_t) (v * kNB2) * E + idx);
+        } else if (kind == 2) {
+            double svol = 0.0;
+#pragma unroll
+            for (int v = 0; v < V; v++) nbv[v] = 0.0;
+            for (int k = 0; k < 4; k++) {
+                const int64_t fi = idx + k;
+                const unsigned info = m.face_info[fi];
+                const int small = (((info >> 2) & 3) == 1) ? m.face_elem[fi] : m.face_elem[m.n_face + fi];
+                const int ls = m.level[small];
+                const double vs = level_h(m, ls, 0) * level_h(m, ls, 1) * level_h(m, ls, 2);
+                svol += vs;
+#pragma unroll
+                for (int v = 0; v < V; v++) nbv[v] += __ldg(ua + (int64_t) (v * kNB2) * E + small) * vs;
+            }
+#pragma unroll
+            for (int v = 0; v < V; v++) nbv[v] /= svol;
+        } else {
+            const int fb = m.bface_face[idx], bid = m.bface_bnd[idx];
+            double n[3] = {0.0, 0.0, 0.0};
+            n[fb >> 1] = (fb & 1) ? 1.0 : -1.0;
+            Prim<double, NC> pin, pout;
+            cons_to_prim<double, NC>(own, pin);
+            bnd_cond<double, NC>(bid, pin, pout, n);
+            prim_to_cons<double, NC>(pout, nbv);
+        }
+#pragma unroll
+        for (int v = 0; v < V; v++) {
+            if (umin[v] > nbv[v]) umin[v] = nbv[v];
+            if (umax[v] < nbv[v]) umax[v] = nbv[v];
+        }
+    }
+    double psi[V];
+#pragma unroll
+    for (int v = 0; v < V; v++) psi[v] = 1.0;
+#pragma unroll 1
+    for (int vx = 0; vx < 8; vx++) {
+        double ph[kNB2];
+        basis10<double>((vx & 1) ? 0.5 : -0.5, (vx & 2) ? 0.5 : -0.5, (vx & 4) ? 0.5 : -0.5, ph);
+#pragma unroll
+        for (int v = 0; v < V; v++) {
+            double f = 0.0;
+#pragma unroll
+            for (int k = 0; k < kNB2; k++) f += __ldg(ua + (int64_t) (v * kNB2 + k) * E + e) * ph[k];
+            const double df = f - own[v];
+            double pt = 1.0;
+            if (fabs(df) > kEps) {
+                if (df > 0) pt = fmin(1.0, (umax[v] - own[v]) / df);
+                else if (df < 0) pt = fmin(1.0, (umin[v] - own[v]) / df);
+            }
+            if (pt < psi[v]) psi[v] = pt;
+        }
+    }
+    const bool comb = (a_old != 0.0);
+#pragma unroll
+    for (int v = 0; v < V; v++)
+#pragma unroll
+        for (int k = 0; k < kNB2; k++) {
+            const int64_t i = (int64_t) (v * kNB2 + k) * E + e;
+            double y = __ldg(ua + i);
+            if (k) y *= psi[v];
+            if (comb) y = a_new * y + a_old * u0[i];
+            out[i] = y;
+        }
+}
+
 }  // namespace charm

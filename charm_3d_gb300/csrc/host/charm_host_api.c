@@ -746,6 +746,7 @@ typedef struct {
     int nc, minlevel;
     double err2_max;
     const double *vpow;        /* vol^(5/3) per level */
+    const int8_t *xflags;      /* caller's flags per current leaf (0 for new leaves), or NULL */
 } coarsen_state_ctx_t;
 
 /* charm_coarsen_err_estimate (src/charm_amr.c:90-142) */
@@ -753,6 +754,11 @@ static int coarsen_family(void *user, const charm_leaf_t *leaves, const int64_t 
 {
     const coarsen_state_ctx_t *c = (const coarsen_state_ctx_t *) user;
     if (leaves[idx[0]].level <= c->minlevel) return 0;
+    if (c->xflags) {   /* the caller's criterion: every child flagged -1 */
+        for (int i = 0; i < 8; i++)
+            if (c->xflags[idx[i]] != -1) return 0;
+        return 1;
+    }
     double h[3];
     leaf_h(c->f, leaves[idx[0]].level, h);
     /* the first child's volume stands for every child (as the reference's
@@ -865,6 +871,8 @@ typedef struct {
     int64_t E0, E1;
     double *g1;                /* [3][E1] */
     int8_t *isnew;             /* [E1] */
+    const int8_t *xf;          /* caller's flags [E0], or NULL */
+    int8_t *xf1;               /* [E1]: carried over, 0 for new leaves */
 } grad_fill_ctx_t;
 
 static void grad_fill_range(void *c, int64_t lo, int64_t hi)
@@ -875,6 +883,7 @@ static void grad_fill_range(void *c, int64_t lo, int64_t hi)
         for (int64_t j = k; j < k + n; j++) {
             for (int d = 0; d < 3; d++) x->g1[(int64_t) d * x->E1 + j] = (n == 8) ? NAN : x->grad[(int64_t) d * x->E0 + i];
             x->isnew[j] = (int8_t) (n == 8);
+            if (x->xf) x->xf1[j] = (n == 8) ? (int8_t) 0 : x->xf[i];
         }
     }
 }
@@ -884,7 +893,7 @@ static void grad_fill_range(void *c, int64_t lo, int64_t hi)
  * densities [E] that the coarsening criterion reads are carried, and every
  * projection is recorded as a pass of h's plan instead. */
 static int adapt_core(struct charm_host_forest_s *h, const double *grad, double max_err, int minlevel, int maxlevel,
-                      int n_comp, const double *u_in, const double *rho_in, int64_t *n_new)
+                      int n_comp, const double *u_in, const double *rho_in, const int8_t *xflags, int64_t *n_new)
 {
     charm_forest_t *f = &h->f;
     const int V = 4 + n_comp;
@@ -908,8 +917,11 @@ static int adapt_core(struct charm_host_forest_s *h, const double *grad, double 
     if (!fl) { free(u); free(rho); return CHARM_GPU_ENOMEM; }
     double vpow[CHARM_FOREST_MAXLEVEL + 1];
     level_vpow(f, vpow);
-    /* 1. refine (charm_refine_err_estimate, non-recursive, maxlevel) */
-    {
+    /* 1. refine (charm_refine_err_estimate, non-recursive, maxlevel; or the
+     * caller's flags) */
+    if (xflags) {
+        for (int64_t i = 0; i < E0; i++) fl[i] = (xflags[i] == 1 && f->leaf[i].level < ml) ? 1 : 0;
+    } else {
         refine_flags_ctx_t rc1 = {f, grad, E0, ml, err2_max, vpow, {0}, fl};
         for (int l = 0; l <= CHARM_FOREST_MAXLEVEL; l++) {
             double hh[3];
@@ -929,9 +941,13 @@ static int adapt_core(struct charm_host_forest_s *h, const double *grad, double 
     const int64_t E1 = f->n;
     double *g1 = (double *) malloc(sizeof(double) * 3 * (size_t) E1);
     int8_t *isnew = (int8_t *) malloc((size_t) E1 + 1);
-    if (!g1 || !isnew) { free(u); free(rho); free(g1); free(isnew); free(o2n); return CHARM_GPU_ENOMEM; }
+    int8_t *xf1 = xflags ? (int8_t *) malloc((size_t) E1 + 1) : NULL;
+    if (!g1 || !isnew || (xflags && !xf1)) {
+        free(u); free(rho); free(g1); free(isnew); free(o2n); free(xf1);
+        return CHARM_GPU_ENOMEM;
+    }
     {
-        grad_fill_ctx_t gf = {o2n, grad, E0, E1, g1, isnew};
+        grad_fill_ctx_t gf = {o2n, grad, E0, E1, g1, isnew, xflags, xf1};
         charm_forest_parallel_for(E0, grad_fill_range, &gf);
     }
     free(o2n);
@@ -940,7 +956,7 @@ static int adapt_core(struct charm_host_forest_s *h, const double *grad, double 
         const int64_t E = f->n;
         int64_t *n2o = (int64_t *) malloc(sizeof(int64_t) * (size_t) (E + 1));
         if (!n2o) { free(u); free(rho); free(g1); free(isnew); return CHARM_GPU_ENOMEM; }
-        coarsen_state_ctx_t cc = {f, g1, rho, u, E, n_comp, minlevel, err2_max, vpow};
+        coarsen_state_ctx_t cc = {f, g1, rho, u, E, n_comp, minlevel, err2_max, vpow, xf1};
         int64_t nm = charm_forest_coarsen_map(f, minlevel, coarsen_family, &cc, n2o);
         if (nm < 0) { free(n2o); free(u); free(rho); free(g1); free(isnew); return CHARM_GPU_ENOMEM; }
         if (nm > 0) {
@@ -966,6 +982,7 @@ static int adapt_core(struct charm_host_forest_s *h, const double *grad, double 
         free(n2o);
     }
     free(g1);
+    free(xf1);
     free(rho);   /* the balance passes do not read densities */
     rho = NULL;
     /* 3. 2:1 face balance, one level per pass (p4est_balance_ext with
@@ -1050,7 +1067,7 @@ int charm_host_forest_adapt_state(charm_host_forest_t h, const double *grad, dou
                                   int n_comp, const double *u_in, int64_t *n_new)
 {
     if (!h || !grad || !u_in || n_comp < 1 || n_comp > CHARM_GPU_MAX_COMP) return CHARM_GPU_EINVAL;
-    return adapt_core(h, grad, max_err, minlevel, maxlevel, n_comp, u_in, NULL, n_new);
+    return adapt_core(h, grad, max_err, minlevel, maxlevel, n_comp, u_in, NULL, NULL, n_new);
 }
 
 int charm_host_forest_adapt_plan(charm_host_forest_t h, const double *grad, const double *rho, double max_err,
@@ -1058,7 +1075,32 @@ int charm_host_forest_adapt_plan(charm_host_forest_t h, const double *grad, cons
 {
     if (!h || !grad || !rho) return CHARM_GPU_EINVAL;
     if (h->conn) return CHARM_GPU_ENOTSUP;   /* the device projection is the box form */
-    int rc = adapt_core(h, grad, max_err, minlevel, maxlevel, 1, NULL, rho, n_new);
+    int rc = adapt_core(h, grad, max_err, minlevel, maxlevel, 1, NULL, rho, NULL, n_new);
+    if (rc) return rc;
+    if (plan) {
+        plan->n_pass = h->plan_n;
+        plan->n_in = h->plan_n_in;
+        plan->n_out = h->plan_nout;
+        plan->map = (const int32_t *const *) h->plan_map;
+    }
+    return CHARM_GPU_OK;
+}
+
+int charm_host_forest_adapt_plan_flags(charm_host_forest_t h, const int8_t *flags, int minlevel, int maxlevel,
+                                       int64_t *n_new, charm_gpu_adapt_plan_t *plan)
+{
+    if (!h || !flags) return CHARM_GPU_EINVAL;
+    if (h->conn) return CHARM_GPU_ENOTSUP;   /* the device projection is the box form */
+    const int64_t E = h->f.n;
+    /* the criteria are not evaluated: a zero gradient and unit densities
+     * only fill the arrays the adapt carries */
+    double *zg = (double *) calloc((size_t) 3 * (size_t) (E > 0 ? E : 1), sizeof(double));
+    double *one = (double *) malloc(sizeof(double) * (size_t) (E > 0 ? E : 1));
+    if (!zg || !one) { free(zg); free(one); return CHARM_GPU_ENOMEM; }
+    for (int64_t i = 0; i < E; i++) one[i] = 1.0;
+    int rc = adapt_core(h, zg, 0.0, minlevel, maxlevel, 1, NULL, one, flags, n_new);
+    free(zg);
+    free(one);
     if (rc) return rc;
     if (plan) {
         plan->n_pass = h->plan_n;

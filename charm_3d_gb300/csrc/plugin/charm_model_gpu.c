@@ -22,8 +22,11 @@
  *
  * Flattening walks the forest with p4est_iterate, so the face list is the
  * one the reference's own face callbacks see.  Single MPI rank: ghost
- * quadrants are rejected.  Geometry: axis-aligned hexahedra (bricks of
- * cube trees); other meshes are rejected with CHARM_GPU_ENOTSUP.
+ * quadrants are rejected.  Geometry: a forest of axis-aligned boxes (bricks
+ * of cube trees) goes to the box kernels; any other forest (the
+ * tree-per-hexahedron connectivity of a gmsh mesh, trees in any
+ * orientation) goes to the general-hexahedron kernels with every leaf's
+ * corners from p4est_qcoord_to_vertex and p4est's own face sides.
  */
 #include "charm_globals.h"
 #include "charm_amr.h"
@@ -54,6 +57,14 @@ typedef struct {
     int8_t *bface_face, *bface_bnd;
     double tree_len[3];
     double *state;         /* [V][B][E] staging buffer */
+    /* general hexahedra: set when a leaf is not an axis-aligned box of the
+     * common tree scale or a face joins other than opposite box faces */
+    int hex;
+    double *vertex;        /* [8][3][E] leaf corners */
+    int32_t *hface_elem0, *hface_elem1, *hface_all;
+    uint8_t *hface_info;
+    int8_t *hface_face0, *hface_face1, *hface_face_all;
+    int64_t n_hface, cap_hface;
 } charm_gpu_plugin_t;
 
 static charm_gpu_plugin_t g_gpu;
@@ -84,12 +95,30 @@ static void flat_volume(p4est_iter_volume_info_t *info, void *user)
     flat_ctx_t *fc = (flat_ctx_t *) user;
     charm_data_t *d = charm_get_quad_data(info->quad);
     int64_t i = local_index(info->p4est, info->treeid, info->quadid);
+    const int64_t E = g_gpu.n_elem;
     int k;
-    if (i < 0 || i >= g_gpu.n_elem) { fc->err = 1; return; }
-    for (k = 0; k < 3; k++) g_gpu.center[k * g_gpu.n_elem + i] = d->par.g.c[k];
+    if (i < 0 || i >= E) { fc->err = 1; return; }
+    for (k = 0; k < 3; k++) g_gpu.center[k * E + i] = d->par.g.c[k];
     g_gpu.level[i] = info->quad->level;
+    /* the leaf's corners, as charm_quad_get_vertices computes them
+     * (src/charm_geom.c:12-31) */
+    p4est_qcoord_t l = P4EST_QUADRANT_LEN(info->quad->level);
+    double v[8][3];
+    for (k = 0; k < 8; k++) {
+        p4est_qcoord_to_vertex(info->p4est->connectivity, info->treeid, info->quad->x + ((k & 1) ? l : 0),
+                               info->quad->y + ((k & 2) ? l : 0), info->quad->z + ((k & 4) ? l : 0), v[k]);
+        for (int dd = 0; dd < 3; dd++) g_gpu.vertex[(int64_t) (3 * k + dd) * E + i] = v[k][dd];
+    }
+    /* a box: every corner at the lower or upper end of each axis as its
+     * corner bits say, edges of the common tree scale */
     if (i == 0)
         for (k = 0; k < 3; k++) g_gpu.tree_len[k] = ldexp(d->par.g.dh[k], info->quad->level);
+    for (int dd = 0; dd < 3; dd++) {
+        const double lo = v[0][dd], hi = v[7][dd];
+        if (fabs(ldexp(hi - lo, info->quad->level) - g_gpu.tree_len[dd]) > 1e-12 * g_gpu.tree_len[dd]) g_gpu.hex = 1;
+        for (k = 0; k < 8; k++)
+            if (v[k][dd] != (((k >> dd) & 1) ? hi : lo)) g_gpu.hex = 1;
+    }
 }
 
 static void push_face(int64_t a, int64_t b, unsigned info)
@@ -104,6 +133,25 @@ static void push_face(int64_t a, int64_t b, unsigned info)
     g_gpu.face_elem1[g_gpu.n_face] = (int32_t) b;
     g_gpu.face_info[g_gpu.n_face] = (uint8_t) info;
     g_gpu.n_face++;
+}
+
+/* a record of the general-hexahedron form: p4est's side order, both faces */
+static void push_hface(int64_t a, int64_t b, unsigned info, int fa, int fb)
+{
+    if (g_gpu.n_hface == g_gpu.cap_hface) {
+        g_gpu.cap_hface = g_gpu.cap_hface ? 2 * g_gpu.cap_hface : 1024;
+        g_gpu.hface_elem0 = (int32_t *) realloc(g_gpu.hface_elem0, sizeof(int32_t) * (size_t) g_gpu.cap_hface);
+        g_gpu.hface_elem1 = (int32_t *) realloc(g_gpu.hface_elem1, sizeof(int32_t) * (size_t) g_gpu.cap_hface);
+        g_gpu.hface_info = (uint8_t *) realloc(g_gpu.hface_info, (size_t) g_gpu.cap_hface);
+        g_gpu.hface_face0 = (int8_t *) realloc(g_gpu.hface_face0, (size_t) g_gpu.cap_hface);
+        g_gpu.hface_face1 = (int8_t *) realloc(g_gpu.hface_face1, (size_t) g_gpu.cap_hface);
+    }
+    g_gpu.hface_elem0[g_gpu.n_hface] = (int32_t) a;
+    g_gpu.hface_elem1[g_gpu.n_hface] = (int32_t) b;
+    g_gpu.hface_info[g_gpu.n_hface] = (uint8_t) info;
+    g_gpu.hface_face0[g_gpu.n_hface] = (int8_t) fa;
+    g_gpu.hface_face1[g_gpu.n_hface] = (int8_t) fb;
+    g_gpu.n_hface++;
 }
 
 static void push_bface(int64_t e, int face, int bnd)
@@ -141,6 +189,28 @@ static void flat_face(p4est_iter_face_info_t *info, void *user)
         return;
     }
     p4est_iter_face_side_t *s1 = p4est_iter_fside_array_index_int(sides, 1);
+    /* the general-hexahedron records keep p4est's side order (side 0 gives
+     * the normal, as in the reference's face callbacks) */
+    if (s0->is_hanging || s1->is_hanging) {
+        const int h0 = s0->is_hanging;
+        p4est_iter_face_side_t *hs = h0 ? s0 : s1, *fs = h0 ? s1 : s0;
+        if (fs->is.full.is_ghost) { fc->err = 3; return; }
+        const int64_t big = local_index(info->p4est, fs->treeid, fs->is.full.quadid);
+        for (int k = 0; k < 4; k++) {
+            if (hs->is.hanging.is_ghost[k]) { fc->err = 3; return; }
+            const int64_t sm = local_index(info->p4est, hs->treeid, hs->is.hanging.quadid[k]);
+            const unsigned bits = (unsigned) (s0->face / 2) | ((h0 ? 1u : 2u) << 2) | ((unsigned) k << 4);
+            if (h0) push_hface(sm, big, bits, s0->face, s1->face);
+            else push_hface(big, sm, bits, s0->face, s1->face);
+        }
+    } else {
+        if (s0->is.full.is_ghost || s1->is.full.is_ghost) { fc->err = 3; return; }
+        push_hface(local_index(info->p4est, s0->treeid, s0->is.full.quadid),
+                   local_index(info->p4est, s1->treeid, s1->is.full.quadid), (unsigned) (s0->face / 2), s0->face,
+                   s1->face);
+    }
+    /* a box forest joins a leaf's face 2 dir + 1 to the other's face 2 dir */
+    if ((s0->face ^ 1) != s1->face) g_gpu.hex = 1;
     /* order the sides so that side 0 is the leaf whose face 2*dir+1 is on the face */
     if (!(s0->face & 1)) {
         p4est_iter_face_side_t *t = s0;
@@ -181,10 +251,12 @@ int charm_model_gpu_flatten(p4est_t *p4est, charm_gpu_mesh_t *mesh)
 {
     flat_ctx_t fc = {p4est, 0};
     g_gpu.n_elem = p4est->local_num_quadrants;
-    g_gpu.n_face = g_gpu.n_bface = 0;
+    g_gpu.n_face = g_gpu.n_bface = g_gpu.n_hface = 0;
+    g_gpu.hex = 0;
     g_gpu.center = (double *) realloc(g_gpu.center, sizeof(double) * 3 * (size_t) g_gpu.n_elem);
     g_gpu.level = (int8_t *) realloc(g_gpu.level, (size_t) g_gpu.n_elem);
-    if (!g_gpu.center || !g_gpu.level) return CHARM_GPU_ENOMEM;
+    g_gpu.vertex = (double *) realloc(g_gpu.vertex, sizeof(double) * 24 * (size_t) g_gpu.n_elem);
+    if (!g_gpu.center || !g_gpu.level || !g_gpu.vertex) return CHARM_GPU_ENOMEM;
     p4est_iterate(p4est, NULL, &fc, flat_volume, NULL, NULL, NULL);
     if (fc.err) return CHARM_GPU_EINVAL;
     p4est_iterate(p4est, NULL, &fc, NULL, flat_face, NULL, NULL);
@@ -204,7 +276,31 @@ int charm_model_gpu_flatten(p4est_t *p4est, charm_gpu_mesh_t *mesh)
     mesh->bface_elem = g_gpu.bface_elem;
     mesh->bface_face = g_gpu.bface_face;
     mesh->bface_bnd = g_gpu.bface_bnd;
+    /* the general-hexahedron form of the same faces */
+    const int64_t nh = g_gpu.n_hface;
+    g_gpu.hface_all = (int32_t *) realloc(g_gpu.hface_all, sizeof(int32_t) * 2 * (size_t) (nh + 1));
+    g_gpu.hface_face_all = (int8_t *) realloc(g_gpu.hface_face_all, 2 * (size_t) (nh + 1));
+    if (!g_gpu.hface_all || !g_gpu.hface_face_all) return CHARM_GPU_ENOMEM;
+    if (nh) {
+        memcpy(g_gpu.hface_all, g_gpu.hface_elem0, sizeof(int32_t) * (size_t) nh);
+        memcpy(g_gpu.hface_all + nh, g_gpu.hface_elem1, sizeof(int32_t) * (size_t) nh);
+        memcpy(g_gpu.hface_face_all, g_gpu.hface_face0, (size_t) nh);
+        memcpy(g_gpu.hface_face_all + nh, g_gpu.hface_face1, (size_t) nh);
+    }
     return CHARM_GPU_OK;
+}
+
+/* After charm_model_gpu_flatten: 1 when the forest needs the
+ * general-hexahedron kernels, and then that form of the mesh (the face
+ * records in p4est's side order with both sides' faces, and the corners). */
+int charm_model_gpu_flatten_hex(charm_gpu_mesh_t *mesh, charm_gpu_hex_t *hex)
+{
+    mesh->n_face = g_gpu.n_hface;
+    mesh->face_elem = g_gpu.hface_all;
+    mesh->face_info = g_gpu.hface_info;
+    hex->vertex = g_gpu.vertex;
+    hex->face_face = g_gpu.hface_face_all;
+    return g_gpu.hex;
 }
 
 /* ---- configuration from the reference context ------------------------------- */
@@ -334,9 +430,12 @@ int charm_model_gpu_download(p4est_t *p4est)
 static int upload_all(p4est_t *p4est)
 {
     charm_gpu_mesh_t mesh;
+    charm_gpu_hex_t hex;
     int rc = charm_model_gpu_flatten(p4est, &mesh);
     if (rc) return rc;
-    if ((rc = charm_gpu_upload_mesh(g_gpu.h, &mesh))) return rc;
+    if (charm_model_gpu_flatten_hex(&mesh, &hex)) rc = charm_gpu_upload_mesh_hex(g_gpu.h, &mesh, &hex);
+    else rc = charm_gpu_upload_mesh(g_gpu.h, &mesh);
+    if (rc) return rc;
     if ((rc = transfer(p4est, 0))) return rc;
     g_gpu.mesh_valid = 1;
     return CHARM_GPU_OK;
@@ -410,5 +509,7 @@ void charm_model_gpu_finalize(p4est_t *p4est)
     }
     free(g_gpu.center); free(g_gpu.level); free(g_gpu.face_elem0); free(g_gpu.face_elem1); free(g_gpu.face_all);
     free(g_gpu.face_info); free(g_gpu.bface_elem); free(g_gpu.bface_face); free(g_gpu.bface_bnd); free(g_gpu.state);
+    free(g_gpu.vertex); free(g_gpu.hface_elem0); free(g_gpu.hface_elem1); free(g_gpu.hface_all); free(g_gpu.hface_info);
+    free(g_gpu.hface_face0); free(g_gpu.hface_face1); free(g_gpu.hface_face_all);
     memset(&g_gpu, 0, sizeof(g_gpu));
 }

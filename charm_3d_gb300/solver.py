@@ -183,6 +183,16 @@ class Forest:
                   "charm_host_forest_adapt_plan")
         return n.value, plan
 
+    def adapt_plan_flags(self, flags: np.ndarray, minlevel: int, maxlevel: int) -> tuple[int, abi.AdaptPlan]:
+        """adapt_plan driven by flags (+1 refine, -1 coarsening candidate),
+        e.g. from Solver.refine_flags_relative."""
+        f = np.ascontiguousarray(flags, dtype=np.int8)
+        n = C.c_int64()
+        plan = abi.AdaptPlan()
+        abi.check(self.lib.charm_host_forest_adapt_plan_flags(self.h, f.ctypes.data, minlevel, maxlevel, C.byref(n),
+                                                              C.byref(plan)), "charm_host_forest_adapt_plan_flags")
+        return n.value, plan
+
     def write_vtu(self, path: str, fields: np.ndarray, names: list[str]) -> None:
         """Leaves as a VTK XML unstructured grid with cell data `fields` [n][E] named `names`."""
         f = np.ascontiguousarray(fields, dtype=np.float64)
@@ -320,6 +330,15 @@ class Solver:
         grad = np.empty((3, self.n_elem))
         abi.check(self.lib.charm_gpu_refine_flags(self.h, max_err, flags.ctypes.data, grad.ctypes.data),
                   "charm_gpu_refine_flags")
+        return flags, grad
+
+    def refine_flags_relative(self, threshold: float, per_cell: bool = True) -> tuple[np.ndarray, np.ndarray]:
+        """Flags of the |grad rho| * L / rho criterion (+1 refine, -1 coarsen
+        candidate, 0 keep) and the gradient estimate [3][E]."""
+        flags = np.empty(self.n_elem, np.int8)
+        grad = np.empty((3, self.n_elem))
+        abi.check(self.lib.charm_gpu_refine_flags_relative(self.h, threshold, 1 if per_cell else 0, flags.ctypes.data,
+                                                           grad.ctypes.data), "charm_gpu_refine_flags_relative")
         return flags, grad
 
     def cell_fields(self) -> np.ndarray:

@@ -410,6 +410,17 @@ typedef struct {
  * (before its clamp). */
 int charm_gpu_density_means(charm_gpu_handle_t h, double *rho);
 
+/* The refine criterion of the benchmark configuration's AMR case (no
+ * counterpart in the reference, whose criterion is charm_gpu_refine_flags'):
+ * the indicator |grad rho| * L / rho with the gradient estimate of
+ * charm_gpu_refine_flags, rho the centre density (charm_gpu_density_means)
+ * and L = 1 (the domain's units) or, with per_cell != 0, the element's edge
+ * V^(1/3); flags[e] = +1 where it is above threshold, -1 where it is at most
+ * threshold / 2 (a coarsening candidate), else 0.  The flags drive
+ * charm_host_forest_adapt_plan_flags.  grad_out ([3][E]) may be NULL. */
+int charm_gpu_refine_flags_relative(charm_gpu_handle_t h, double threshold, int per_cell, int8_t *flags,
+                                    double *grad_out);
+
 /* Carry the device state through `plan` (p1 projections of
  * charm_replace_quads, src/charm_amr.c:206-307, the arithmetic of
  * charm_host_forest_adapt_state) and upload `mesh`, the flattened forest
@@ -540,6 +551,15 @@ int charm_host_forest_state(charm_host_forest_t f, const double **u_out);
  * adapt or free of f).  Same forest as charm_host_forest_adapt_state. */
 int charm_host_forest_adapt_plan(charm_host_forest_t f, const double *grad, const double *rho, double max_err,
                                  int minlevel, int maxlevel, int64_t *n_new, charm_gpu_adapt_plan_t *plan);
+
+/* The adapt of charm_host_forest_adapt_plan driven by caller's flags instead
+ * of the reference's criteria (e.g. from charm_gpu_refine_flags_relative):
+ * refine the leaves flagged +1 (level < maxlevel), coarsen complete families
+ * whose 8 flags are -1 (level > minlevel; families refined in this adapt
+ * are not coarsened), then 2:1 face balance; the projections are recorded
+ * as the plan, as there.  Bricks only (CHARM_GPU_ENOTSUP otherwise). */
+int charm_host_forest_adapt_plan_flags(charm_host_forest_t f, const int8_t *flags, int minlevel, int maxlevel,
+                                       int64_t *n_new, charm_gpu_adapt_plan_t *plan);
 
 /* Flatten into a mesh view whose arrays live inside the forest object and
  * stay valid until the next adapt/flatten/free. */

@@ -1,12 +1,17 @@
 /*
  * p4est-subset shim: implementation (oracle build only, see p4est_to_p8est.h).
  *
- * One rank, a brick of trees, leaves held by the host octree of the GPU
- * library (charm_3d_gb300/csrc/host/charm_forest.c).  Behaviour kept from
- * p4est because CHARM_3D's arithmetic depends on it:
+ * One rank, a brick of trees or an unstructured hexahedral connectivity
+ * (one tree per hexahedron, trees in any face orientation), leaves held by
+ * the host octree of the GPU library (charm_3d_gb300/csrc/host/charm_forest.c,
+ * charm_conn.c).  Behaviour kept from p4est because CHARM_3D's arithmetic
+ * depends on it:
  *   - p4est_iterate face sides: side 0 at the lower coordinate (its face
- *     2*dir+1), side 1 at the upper; a hanging side lists its 4 small
- *     quadrants in z-order on the face; boundary faces have one side;
+ *     2*dir+1), side 1 at the upper inside a tree and in a brick; across
+ *     the faces of an unstructured connectivity side 0 is the leaf of the
+ *     lower tree, as p4est visits a tree face from its lower tree; a hanging
+ *     side lists its 4 small quadrants in z-order on the face; boundary
+ *     faces have one side;
  *   - p4est_qcoord_to_vertex: trilinear map of the tree's 8 vertices;
  *   - refine/coarsen/balance call init_fn for new quadrants and replace_fn
  *     with (outgoing, incoming) families; balance refines one level at a
@@ -23,6 +28,7 @@
  *     the reference never initialised are NaN rather than stale values.
  */
 #include "p4est_to_p8est.h"
+#include "charm_conn.h"
 #include "charm_forest.h"
 
 #include <stdarg.h>
@@ -207,9 +213,38 @@ p4est_connectivity_t *charm_shim_conn_brick(int nx, int ny, int nz, const int pe
     return c;
 }
 
+/* Unstructured connectivity: n_tree hexahedra with their corner vertices in
+ * p4est order; tree faces matched by their vertex sets (the role of
+ * p4est_connectivity_complete).  NULL when the faces do not match. */
+p4est_connectivity_t *charm_shim_conn_hex(int32_t n_vert, const double *vert, int32_t n_tree, const int32_t *t2v,
+                                          size_t attr_bytes)
+{
+    charm_conn_t *hc = (charm_conn_t *) calloc(1, sizeof(charm_conn_t));
+    char err[256];
+    if (!hc || charm_conn_build(hc, n_vert, vert, n_tree, t2v, err, (int) sizeof(err))) {
+        fprintf(stderr, "p4est shim: %s\n", hc ? err : "out of memory");
+        free(hc);
+        return NULL;
+    }
+    p4est_connectivity_t *c = (p4est_connectivity_t *) calloc(1, sizeof(*c));
+    c->num_trees = n_tree;
+    c->num_vertices = n_vert;
+    c->vertices = (double *) malloc(sizeof(double) * 3 * (size_t) n_vert);
+    memcpy(c->vertices, vert, sizeof(double) * 3 * (size_t) n_vert);
+    c->tree_to_vertex = (p4est_topidx_t *) malloc(sizeof(p4est_topidx_t) * 8 * (size_t) n_tree);
+    for (int64_t k = 0; k < 8 * (int64_t) n_tree; k++) c->tree_to_vertex[k] = t2v[k];
+    c->brick[0] = n_tree; c->brick[1] = 1; c->brick[2] = 1;
+    for (int d = 0; d < 3; d++) c->tree_len[d] = 1.0;
+    c->tree_attr_bytes = attr_bytes;
+    c->tree_to_attr = (char *) calloc((size_t) n_tree, attr_bytes > 0 ? attr_bytes : 1);
+    c->hexconn = hc;
+    return c;
+}
+
 void charm_shim_conn_destroy(p4est_connectivity_t *c)
 {
     if (!c) return;
+    if (c->hexconn) { charm_conn_free((charm_conn_t *) c->hexconn); free(c->hexconn); }
     free(c->vertices); free(c->tree_to_vertex); free(c->tree_to_attr); free(c);
 }
 
@@ -257,7 +292,8 @@ p4est_t *p4est_new_ext(sc_MPI_Comm mpicomm, p4est_connectivity_t *conn, p4est_lo
     p->first_local_tree = 0;
     p->last_local_tree = conn->num_trees - 1;
     p->shim = (struct charm_shim_state *) calloc(1, sizeof(struct charm_shim_state));
-    charm_forest_init_uniform(&p->shim->f, conn->brick, conn->periodic, conn->origin, conn->tree_len, min_level);
+    if (conn->hexconn) charm_forest_init_conn(&p->shim->f, (const charm_conn_t *) conn->hexconn, min_level);
+    else charm_forest_init_uniform(&p->shim->f, conn->brick, conn->periodic, conn->origin, conn->tree_len, min_level);
     int64_t n = p->shim->f.n;
     p->shim->q = (p4est_quadrant_t *) calloc((size_t) n, sizeof(p4est_quadrant_t));
     for (int64_t i = 0; i < n; i++) {
@@ -611,6 +647,47 @@ void p4est_iterate(p4est_t *p, p4est_ghost_t *g, void *ud, p4est_iter_volume_t v
     p4est_quadrant_t *ghq = g ? (p4est_quadrant_t *) g->ghosts.array : NULL;
     charm_face_nb_t nb;
     p4est_iter_face_side_t sides[2];
+    if (f->conn) {   /* unstructured connectivity: no periodic wrap, faces of any orientation */
+        for (int64_t i = 0; i < f->n; i++) {
+            const int32_t ti = f->leaf[i].tree;
+            for (int face = 0; face < 6; face++) {
+                charm_forest_face_neighbor(f, i, face, &nb);
+                if (nb.kind == CHARM_NB_BOUNDARY) {
+                    side_full(&sides[0], ti, face, &s->q[i], 0, tree_local(p, i));
+                    call_face(p, g, ud, face_fn, 1, sides, 1);
+                    continue;
+                }
+                if (nb.kind == CHARM_NB_BIGGER) continue;   /* presented from the big side */
+                if (nb.kind != CHARM_NB_SAME && nb.kind != CHARM_NB_SMALLER) {
+                    fprintf(stderr, "p4est shim: forest is not 2:1 face balanced\n");
+                    abort();
+                }
+                const int32_t tj = f->leaf[nb.idx[0]].tree;
+                const int lower = (ti != tj) ? (ti < tj) : (face & 1);   /* this leaf is side 0 */
+                if (nb.kind == CHARM_NB_SAME) {
+                    if (!lower) continue;
+                    const int64_t j = nb.idx[0];
+                    side_full(&sides[0], ti, face, &s->q[i], 0, tree_local(p, i));
+                    side_full(&sides[1], tj, nb.nface, &s->q[j], 0, tree_local(p, j));
+                    call_face(p, g, ud, face_fn, 2, sides, ti != tj);
+                    continue;
+                }
+                p4est_quadrant_t *hq[4];
+                int8_t hg[4] = {0, 0, 0, 0};
+                p4est_locidx_t hid[4];
+                for (int k = 0; k < 4; k++) { hq[k] = &s->q[nb.idx[k]]; hid[k] = tree_local(p, nb.idx[k]); }
+                if (lower) {
+                    side_full(&sides[0], ti, face, &s->q[i], 0, tree_local(p, i));
+                    side_hanging(&sides[1], tj, nb.nface, hq, hg, hid);
+                } else {
+                    side_hanging(&sides[0], tj, nb.nface, hq, hg, hid);
+                    side_full(&sides[1], ti, face, &s->q[i], 0, tree_local(p, i));
+                }
+                call_face(p, g, ud, face_fn, 2, sides, ti != tj);
+            }
+        }
+        return;
+    }
     for (int64_t i = 0; i < f->n; i++) {
         const int32_t ti = f->leaf[i].tree;
         for (int face = 0; face < 6; face++) {

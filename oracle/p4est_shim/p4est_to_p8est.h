@@ -115,6 +115,9 @@ typedef struct p4est_connectivity {
     int32_t periodic[3];
     double origin[3];
     double tree_len[3];
+    /* unstructured hexahedral connectivity (charm_conn_t of the host
+     * octree), or NULL for the brick */
+    void *hexconn;
 } p4est_connectivity_t;
 
 typedef struct p4est_tree {

@@ -29,6 +29,8 @@ def load(variant: str = "ref") -> C.CDLL:
         lib = C.CDLL(paths[variant], mode=C.RTLD_LOCAL)
         lib.ref_setup.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
                                   C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int]
+        lib.ref_setup_hex.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int,
+                                      C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int]
         lib.ref_count.restype = C.c_int64
         lib.ref_set_state.argtypes = [C.c_void_p]
         lib.ref_get_state.argtypes = [C.c_void_p]
@@ -47,15 +49,18 @@ def load(variant: str = "ref") -> C.CDLL:
         lib.ref_refine_flags.restype = C.c_int64
         if variant == "plugin":
             lib.ref_plugin_flatten.argtypes = [C.c_void_p]
+            lib.ref_plugin_flatten_hex.argtypes = [C.c_void_p, C.c_void_p]
             lib.ref_plugin_config.argtypes = [C.c_int, C.c_void_p]
         _libs[variant] = lib
     return _libs[variant]
 
 
 class RefSolver:
-    """The reference's own time step on a brick case (one at a time per variant)."""
+    """The reference's own time step on a brick case, or with hexmesh =
+    (vertices, tree corners, tree-face boundaries) on an unstructured
+    hexahedral mesh (one at a time per variant)."""
 
-    def __init__(self, case, variant: str = "ref"):
+    def __init__(self, case, variant: str = "ref", hexmesh=None):
         self.lib = load(variant)
         self.case = case
         self.cfg = case.config()
@@ -66,6 +71,18 @@ class RefSolver:
         reg.t, reg.p = r["t"], r["p"]
         for k, v in enumerate(r["c"]):
             reg.c[k] = v
+        self.n_var = 4 + case.n_comp
+        if hexmesh is not None:
+            vert, t2v, tb = hexmesh
+            self._keep = [np.ascontiguousarray(vert, np.float64), np.ascontiguousarray(t2v, np.int32),
+                          np.ascontiguousarray(tb, np.int8)]
+            v, t, b = self._keep
+            rc = self.lib.ref_setup_hex(C.addressof(self.cfg), len(v), v.ctypes.data, len(t), t.ctypes.data,
+                                        b.ctypes.data, case.level, C.addressof(reg), case.max_err, case.min_level,
+                                        case.max_level, case.refine_period)
+            if rc:
+                raise RuntimeError(f"ref_setup_hex failed: {rc}")
+            return
         self._keep = [np.array(case.brick, np.int32), np.array(case.periodic, np.int32),
                       np.array(case.origin, np.float64), np.array(case.tree_len, np.float64),
                       np.array(case.bnd_of_side, np.int8)]
@@ -150,6 +167,17 @@ class RefSolver:
         if rc:
             raise RuntimeError(f"charm_model_gpu_flatten: {rc}")
         return MeshArrays(m)
+
+    def plugin_flatten_hex(self):
+        """(needs general hexahedra, mesh in that form) as the plugin builds it."""
+        from charm_3d_gb300 import abi
+        from charm_3d_gb300.solver import MeshArrays
+        m = abi.Mesh()
+        x = abi.Hex()
+        rc = self.lib.ref_plugin_flatten_hex(C.addressof(m), C.addressof(x))
+        if rc < 0:
+            raise RuntimeError("charm_model_gpu_flatten failed")
+        return bool(rc), MeshArrays(m, x)
 
     def plugin_config(self, precision: int = 0):
         from charm_3d_gb300 import abi

@@ -22,6 +22,8 @@
 #include "charm_gpu.h"
 
 /* shim extras (p4est_shim.c) */
+p4est_connectivity_t *charm_shim_conn_hex(int32_t n_vert, const double *vert, int32_t n_tree, const int32_t *t2v,
+                                          size_t attr_bytes);
 p4est_connectivity_t *charm_shim_conn_brick(int nx, int ny, int nz, const int periodic[3], const double origin[3],
                                             const double tree_len[3], size_t attr_bytes);
 void charm_shim_conn_destroy(p4est_connectivity_t *c);
@@ -106,9 +108,10 @@ typedef struct ref_region {
     double c[CHARM_GPU_MAX_COMP];
 } ref_region_t;
 
-int ref_setup(const charm_gpu_config_t *cfg, const int32_t brick[3], const int32_t periodic[3],
-              const double origin[3], const double tree_len[3], int level, const int8_t bnd_of_side[6],
-              const ref_region_t *region, double max_err, int min_level, int max_level, int refine_period)
+/* The context charm_init_context_yaml builds from a case (everything but the
+ * mesh). */
+static int build_ctx(const charm_gpu_config_t *cfg, const ref_region_t *region, double max_err, int min_level,
+                     int max_level, int refine_period)
 {
     int i, k;
     free_case();
@@ -217,7 +220,17 @@ int ref_setup(const charm_gpu_config_t *cfg, const int32_t brick[3], const int32
         ctx->timestep_single_fn = charm_model_ns_timestep_single;
     }
     ctx->timestep = 0;
+    return 0;
+}
 
+int ref_setup(const charm_gpu_config_t *cfg, const int32_t brick[3], const int32_t periodic[3],
+              const double origin[3], const double tree_len[3], int level, const int8_t bnd_of_side[6],
+              const ref_region_t *region, double max_err, int min_level, int max_level, int refine_period)
+{
+    int i, k;
+    int rc = build_ctx(cfg, region, max_err, min_level, max_level, refine_period);
+    if (rc) return rc;
+    charm_ctx_t *ctx = &g_ctx;
     /* mesh: brick of trees with boundary attributes on the domain sides */
     g_conn = charm_shim_conn_brick(brick[0], brick[1], brick[2], (const int *) periodic, origin, tree_len,
                                    sizeof(charm_tree_attr_t));
@@ -234,6 +247,35 @@ int ref_setup(const charm_gpu_config_t *cfg, const int32_t brick[3], const int32
                 }
                 a->reg = (charm_reg_t *) sc_array_index(ctx->reg, 0);
             }
+    charm_shim_ghost_shift = ghost_shift;
+    g_p4est = p4est_new_ext(0, g_conn, 0, level, 1, sizeof(charm_data_t), charm_init_initial_condition, ctx);
+    charm_set_p4est(g_p4est);
+    g_step = 0;
+    g_dt = 0.0;
+    return 0;
+}
+
+/* The case on an unstructured hexahedral mesh (the connectivity that
+ * charm_conn_reader_msh builds, src/charm_connectivity.c:315-519): n_tree
+ * hexahedra with corner vertices in p4est order, tree_bnd [6 n_tree] the
+ * boundary of every tree face without a neighbour (-1 elsewhere). */
+int ref_setup_hex(const charm_gpu_config_t *cfg, int32_t n_vert, const double *vert, int32_t n_tree,
+                  const int32_t *t2v, const int8_t *tree_bnd, int level, const ref_region_t *region, double max_err,
+                  int min_level, int max_level, int refine_period)
+{
+    int rc = build_ctx(cfg, region, max_err, min_level, max_level, refine_period);
+    if (rc) return rc;
+    charm_ctx_t *ctx = &g_ctx;
+    g_conn = charm_shim_conn_hex(n_vert, vert, n_tree, t2v, sizeof(charm_tree_attr_t));
+    if (!g_conn) return 3;
+    for (int t = 0; t < n_tree; t++) {
+        charm_tree_attr_t *a = (charm_tree_attr_t *) &g_conn->tree_to_attr[sizeof(charm_tree_attr_t) * t];
+        for (int f = 0; f < 6; f++) {
+            const int b = tree_bnd[6 * t + f];
+            a->bnd[f] = (b >= 0) ? (charm_bnd_t *) sc_array_index(ctx->bnd, (size_t) b) : NULL;
+        }
+        a->reg = (charm_reg_t *) sc_array_index(ctx->reg, 0);
+    }
     charm_shim_ghost_shift = ghost_shift;
     g_p4est = p4est_new_ext(0, g_conn, 0, level, 1, sizeof(charm_data_t), charm_init_initial_condition, ctx);
     charm_set_p4est(g_p4est);

@@ -22,6 +22,7 @@ sys.path.insert(0, ROOT)
 from charm_3d_gb300.solver import Forest  # noqa: E402
 from oracle.ref import RefSolver  # noqa: E402
 from tests.common import amr_case, hanging_forest, pressure_box_J, small_case  # noqa: E402
+from tests.golden_cases import HEX_AMR_STEPS, HEX_NAMES, hex_case  # noqa: E402
 
 # name: (kind, flux, limiter, model, level, steps, hanging)
 FIXTURES = {
@@ -264,6 +265,35 @@ def cell_fields() -> dict:
     return out
 
 
+def hex_fixture(name: str) -> dict:
+    """The reference's own code on general hexahedra (its connectivity of
+    one tree per hexahedron, the trilinear geometry of src/charm_geom.c):
+    residual and steps of tests/golden_cases.HEX_NAMES, or (hex_ramp_amr)
+    HEX_AMR_STEPS steps of its AMR time loop on the ramp with the sample
+    case's controls (MAX_ERROR 0.01, MAX_LEVEL 1, REFINE_PERIOD 10)."""
+    case, forest, mesh, u0, (vert, t2v, tb) = hex_case(name)
+    if name == "hex_ramp_amr":
+        case.max_err, case.min_level, case.max_level, case.refine_period = 0.01, 0, 1, 10
+        ref = RefSolver(case, "patched", hexmesh=(vert, t2v, tb))
+        ref.set_state(u0)
+        ref.run(HEX_AMR_STEPS)
+        return {"u0": u0, "leaves": ref.leaves(), "state": ref.get_state(), "steps": np.array(HEX_AMR_STEPS)}
+    geo, kind, flux, lim, model, level, steps, refine = HEX_NAMES[name]
+    ref = RefSolver(case, "patched" if refine else "ref", hexmesh=(vert, t2v, tb))
+    if refine:
+        rng = np.random.default_rng(5)
+        flags = (rng.uniform(size=int(ref.n_elem)) < 0.3).astype(np.int8)
+        assert ref.refine_flags(flags, level + 1) == len(forest)
+    q, lv = forest.leaves()
+    rl = ref.leaves()
+    assert (rl[:, :4] == q).all() and (rl[:, 4] == lv).all(), "reference forest differs from host octree"
+    ref.set_state(u0)
+    res = ref.residual()
+    ref.set_state(u0)
+    dt = ref.run(steps)
+    return {"u0": u0, "residual": res, "state": ref.get_state(), "steps": np.array(steps), "dt": np.array(dt)}
+
+
 def main(names: list[str]) -> None:
     """All fixtures, or only the ones named on the command line."""
     for name in FIXTURES:
@@ -288,6 +318,10 @@ def main(names: list[str]) -> None:
     if not names or "cell_fields" in names:
         np.savez_compressed(os.path.join(HERE, "cell_fields.npz"), **cell_fields())
         print("cell_fields")
+    for name in list(HEX_NAMES) + ["hex_ramp_amr"]:
+        if not names or name in names:
+            np.savez_compressed(os.path.join(HERE, name + ".npz"), **hex_fixture(name))
+            print(name)
     if not names or "adjoint_fd_vortex" in names:
         np.savez_compressed(os.path.join(HERE, "adjoint_fd_vortex.npz"), **adjoint_fd())
         print("adjoint_fd_vortex")

@@ -158,3 +158,33 @@ def test_adapt_plan_matches_adapt_state_on_large_meshes():
         mesh = fa.flatten()
         u = ua
     assert mesh.n_elem > 4 * 4096 and coarsened > 0
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_plan_driven_by_flags_is_the_flag_adapt(seed):
+    """charm_host_forest_adapt_plan_flags (refine +1, coarsen families of -1,
+    balance) gives the forest of charm_host_forest_adapt with the same
+    flags, and its plan carries the mass of a state (the p1 projections
+    keep it up to rounding)."""
+    case = small_case("random", "HLLC", "BJ", level=3)
+    rng = np.random.default_rng(seed)
+    pre = (rng.uniform(size=8 ** 3) < 0.3).astype(np.int8)
+    a, b = Forest(case), Forest(case)
+    a.adapt(pre, 2, 5)   # a mesh with mortars
+    b.adapt(pre, 2, 5)
+    n = len(a)
+    lv0 = a.leaves()[1]
+    flags = rng.choice(np.array([-1, 0, 1], np.int8), size=n, p=[0.6, 0.3, 0.1])
+    u = case.initial_state(a.flatten().center)
+    a.adapt(flags, 2, 5)
+    n_new, plan = b.adapt_plan_flags(flags, 2, 5)
+    qa, la = a.leaves()
+    qb, lb = b.leaves()
+    assert n_new == len(a) and np.array_equal(qa, qb) and np.array_equal(la, lb)
+    assert plan.n_in == n and n_new != n
+    w = apply_plan(plan, u)
+
+    def mass(x, lv):
+        return float((x[4, 0] * 8.0 ** (-lv.astype(np.float64))).sum())
+
+    assert abs(mass(w, lb) - mass(u, lv0)) < 1e-13 * mass(u, lv0)

@@ -71,9 +71,33 @@ def test_p2_flame_matches_oracle():
     assert rel_l2(gpu.get_state(), port.get_state()) < FP64_TOL
 
 
+@pytest.mark.parametrize("kind,flux,model", [("random", "HLLC", "NS"), ("walls", "LF", "NS"), ("mix2", "HLLC", "NS"),
+                                             ("random", "HLLC", "EULER")])
+def test_p2_limiter_steps_match_oracle(kind, flux, model):
+    """The Barth-Jespersen limiter on the p2 basis (the reference's loops
+    over CHARM_BASE_FN_COUNT, src/limiters/charm_limiter_bj.c:241-315):
+    quadrature means, the p2 field at the corners, coefficients 1..9
+    scaled; alone and inside the SSP-RK3 steps."""
+    case = small_case(kind, flux, "BJ", level=2, model=model)
+    case.p_order, case.precision = 2, "FP64"
+    _, gpu, port, u0 = _pair(case)
+    gpu.limit()
+    port.limit()
+    lim = port.get_state()
+    assert not np.array_equal(lim, u0), "the limiter acts on this state"
+    assert rel_l2(gpu.get_state(), lim) < FP64_TOL
+    gpu.set_state(u0)
+    port.set_state(u0)
+    gpu.run(3, case.tau)
+    gpu.sync()
+    port.run(3, case.tau)
+    assert rel_l2(gpu.get_state(), port.get_state()) < FP64_TOL
+
+
 def test_p2_rejected_where_not_built():
     case = _p2("random", "HLLC", level=1)
     case.limiter = "BJ"
+    case.precision = "MIXED"
     with pytest.raises(CharmGpuError):
         Solver(case)
     case = _p2("random", "HLLC", level=2)

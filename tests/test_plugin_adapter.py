@@ -54,3 +54,39 @@ def test_plugin_config_matches_case(kind, flux, lim):
     want = case.config()
     want.model = abi.MODEL["NS"]
     assert bytes(got) == bytes(want)
+
+
+def _hex_faces(mesh):
+    fe, ff = mesh.face_elem, mesh.face_face
+    kind = (mesh.face_info >> 2) & 3
+    return sorted(zip(fe[0].tolist(), fe[1].tolist(), ff[0].tolist(), ff[1].tolist(), kind.tolist()))
+
+
+@pytest.mark.parametrize("name", ["hex_ramp_hllc_bj", "hex_ramp_hanging", "hex_block_walls"])
+def test_plugin_takes_general_hexahedra_from_p4est(name):
+    """On the tree-per-hexahedron forest of an unstructured mesh the plugin
+    switches to the general-hexahedron form: p4est's face sides (side 0
+    gives the normal) with both faces, and every leaf's corners from
+    p4est_qcoord_to_vertex; the same records as the host octree's
+    flatten, the same corners."""
+    from .golden_cases import HEX_NAMES, hex_case
+    case, forest, mesh, _, (vert, t2v, tb) = hex_case(name)
+    ref = RefSolver(case, "plugin", hexmesh=(vert, t2v, tb))
+    if HEX_NAMES[name][7]:
+        rng = np.random.default_rng(5)
+        ref.refine_flags((rng.uniform(size=int(ref.n_elem)) < 0.3).astype(np.int8), HEX_NAMES[name][5] + 1)
+    is_hex, got = ref.plugin_flatten_hex()
+    assert is_hex
+    assert got.n_elem == mesh.n_elem
+    assert np.allclose(got.vertex, mesh.vertex, rtol=1e-14, atol=1e-12)
+    assert _hex_faces(got) == _hex_faces(mesh)
+    bg = sorted(zip(got.bface_elem.tolist(), got.bface_face.tolist(), got.bface_bnd.tolist()))
+    bw = sorted(zip(mesh.bface_elem.tolist(), mesh.bface_face.tolist(), mesh.bface_bnd.tolist()))
+    assert bg == bw
+
+
+def test_plugin_keeps_the_box_form_on_bricks():
+    case = small_case("random", "HLLC", "BJ", level=2)
+    ref = RefSolver(case, "plugin")
+    is_hex, _ = ref.plugin_flatten_hex()
+    assert not is_hex
