@@ -473,7 +473,8 @@ def summary_dw(d):
 def summary_adjoint(a):
     if not a:
         return None
-    out = {"x_forward": _r(a["adjoint_over_forward"]), "snapshots": a["n_snapshots"],
+    out = {"x_forward": _r(a["adjoint_over_forward"]),
+           "reverse_step_x_forward_step": _r(a["reverse_step_over_forward_step"]), "snapshots": a["n_snapshots"],
            "fd_max": _r(a["fd_check"]["max_rel_err"], 3), "fd_median": _r(a["fd_check"]["median_rel_err"], 3)}
     if a.get("revolve"):
         out["revolve_x_forward"] = _r(a["revolve"]["adjoint_over_forward"])
@@ -637,6 +638,9 @@ def run_adjoint(args, device: int) -> dict:
                         f"J = integral of p over [{args.adjoint_box}]^3 at step {n}",
             "n_steps": n, "n_snapshots": snaps, "J": info.J, "J_forward": J_fwd,
             "forward_s": t_fwd, "adjoint_s": t_adj, "adjoint_over_forward": t_adj / t_fwd,
+            # the reverse step alone (the adjoint's own forward sweep runs the
+            # forward run's kernels, so it takes the forward run's time)
+            "reverse_step_over_forward_step": (t_adj - t_fwd) / t_fwd,
             "forward_s_runs": t_fwds, "adjoint_s_runs": t_adjs,
             "adjoint_whole_domain_J_over_forward": t_dense / t_fwd,
             "forward_steps_in_adjoint": int(info.forward_steps), "snapshots_held": int(info.snapshots),

@@ -60,6 +60,21 @@ ADJ_HD double rcp(double x)
 #endif
 }
 
+// 1 / x with one Newton-Raphson step from the hardware seed: the relative
+// error squares once (about 1e-13 and below), which the derivatives of the
+// reverse sweep carry without loss at their 1e-6 bar; the plain quotient on
+// the host.
+ADJ_HD double rcp1(double x)
+{
+#ifdef __CUDA_ARCH__
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    return fma(y, fma(-x, y, 1.0), y);
+#else
+    return 1.0 / x;
+#endif
+}
+
 // Ideal gas with constant cp (the only EOS the adjoint supports).
 struct Gas {
     double gam;      // cp / cv
@@ -91,15 +106,23 @@ ADJ_HD void zero(PrBar<NC> &b)
     for (int i = 0; i < NC; i++) b.c[i] = 0.0;
 }
 
+// Parts of the primitive state a caller uses besides r, velocities,
+// energies, p and the fractions: the sound speed (fluxes) and the
+// temperature (boundary states).  Leaving one out skips its arithmetic in
+// prim and its (zero) adjoint in prim_vjp.
+// kPrRcp1: 1 / r by rcp1 (inside the flux and volume derivatives; the
+// objective and the boundary states keep the full reciprocal).
+enum { kPrCz = 1, kPrT = 2, kPrAll = 3, kPrRcp1 = 4 };
+
 // U = (ru, rv, rw, re, rc_0 ..) -> primitive state (eos flag 4 of an ideal
 // gas with constant cp).
-template <int NC>
+template <int NC, int PARTS = kPrAll>
 ADJ_HD void prim(const double *U, const Gas &g, Pr<NC> &p)
 {
     double r = 0.0;
     for (int i = 0; i < NC; i++) r += U[4 + i];
     p.r = r;
-    const double ir = rcp(r);
+    const double ir = (PARTS & kPrRcp1) ? rcp1(r) : rcp(r);
     p.ir = ir;
     p.u = U[0] * ir;
     p.v = U[1] * ir;
@@ -108,26 +131,45 @@ ADJ_HD void prim(const double *U, const Gas &g, Pr<NC> &p)
     p.e = p.e_tot - 0.5 * (p.u * p.u + p.v * p.v + p.w * p.w);
     p.clamp = 0;
     for (int i = 0; i < NC; i++) {
+#ifdef __CUDA_ARCH__
+        // the forward path's clamp to [0, 1] on the bit pattern (integer
+        // pipe; -0 counts as below 0 there too)
+        long long b = __double_as_longlong(U[4 + i] * ir);
+        const bool below = b < 0, above = b > 0x3FF0000000000000LL;
+        if (below) b = 0;
+        if (above) b = 0x3FF0000000000000LL;
+        if (below || above) p.clamp |= 1u << i;
+        p.c[i] = __longlong_as_double(b);
+#else
         double c = U[4 + i] * ir;
         if (c < 0.0) { c = 0.0; p.clamp |= 1u << i; }
         if (c > 1.0) { c = 1.0; p.clamp |= 1u << i; }
         p.c[i] = c;
+#endif
     }
     p.p = r * p.e * (g.gam - 1.0);
-    const double x = g.gam * p.p * ir;
-    p.icz = (x > 0.0) ? rsq(x) : 0.0;
-    p.cz = (x > 0.0) ? x * p.icz : sqrt(x);
-    p.t = p.e * g.inv_cv;
+    p.icz = p.cz = p.t = 0.0;
+    if (PARTS & kPrCz) {
+        const double x = g.gam * p.p * ir;
+        p.icz = (x > 0.0) ? rsq(x) : 0.0;
+        // sqrt(x) from the reciprocal square root; x <= 0 (a state the
+        // forward path reports) gives 0 or NaN like sqrt, without a second
+        // square root
+        p.cz = (x > 0.0) ? x * p.icz : ((x == 0.0) ? 0.0 : NAN);
+    }
+    if (PARTS & kPrT) p.t = p.e * g.inv_cv;
 }
 
-// Ub += (d prim / d U)^T b
-template <int NC>
+// Ub += (d prim / d U)^T b (b.cz, b.t taken as zero for the parts not in
+// PARTS); ASSIGN: Ub = (d prim / d U)^T b, which saves the additions to a
+// zeroed Ub (x + 0 is not x in IEEE arithmetic when x = -0, so they stay).
+template <int NC, int PARTS = kPrAll, bool ASSIGN = false>
 ADJ_HD void prim_vjp(const double *U, const Pr<NC> &p, const Gas &g, PrBar<NC> b, double *Ub)
 {
     const double ir = p.ir;
     double b_ir = 0.0;
-    b.e += b.t * g.inv_cv;                                   // t = e / cv
-    if (p.cz > 0.0) {                                        // cz = sqrt(gam p ir)
+    if (PARTS & kPrT) b.e += b.t * g.inv_cv;                 // t = e / cv
+    if ((PARTS & kPrCz) && p.cz > 0.0) {                     // cz = sqrt(gam p ir)
         const double d = 0.5 * g.gam * p.icz;
         b.p += b.cz * d * ir;
         b_ir += b.cz * d * p.p;
@@ -138,18 +180,29 @@ ADJ_HD void prim_vjp(const double *U, const Pr<NC> &p, const Gas &g, PrBar<NC> b
     b.u -= b.e * p.u;
     b.v -= b.e * p.v;
     b.w -= b.e * p.w;
-    for (int i = 0; i < NC; i++)
-        if (!((p.clamp >> i) & 1u)) {                        // c_i = rc_i / r
-            Ub[4 + i] += b.c[i] * ir;
-            b_ir += b.c[i] * U[4 + i];
-        }
-    Ub[0] += b.u * ir;
-    Ub[1] += b.v * ir;
-    Ub[2] += b.w * ir;
-    Ub[3] += b.e_tot * ir;
+    double bc[NC];                                           // c_i = rc_i / r
+    for (int i = 0; i < NC; i++) {
+        const bool free_c = !((p.clamp >> i) & 1u);
+        bc[i] = free_c ? b.c[i] : 0.0;
+        if (free_c) b_ir += b.c[i] * U[4 + i];
+    }
+    if (ASSIGN) {
+        Ub[0] = b.u * ir;
+        Ub[1] = b.v * ir;
+        Ub[2] = b.w * ir;
+        Ub[3] = b.e_tot * ir;
+    } else {
+        Ub[0] += b.u * ir;
+        Ub[1] += b.v * ir;
+        Ub[2] += b.w * ir;
+        Ub[3] += b.e_tot * ir;
+    }
     b_ir += b.u * U[0] + b.v * U[1] + b.w * U[2] + b.e_tot * U[3];
     b.r -= b_ir * ir * ir;                                   // ir = 1 / r
-    for (int i = 0; i < NC; i++) Ub[4 + i] += b.r;           // r = sum rc_i
+    for (int i = 0; i < NC; i++) {                           // r = sum rc_i
+        if (ASSIGN) Ub[4 + i] = bc[i] * ir + b.r;
+        else Ub[4 + i] += bc[i] * ir + b.r;
+    }
 }
 
 // Euler volume fluxes F_d(U) (src/models/ns/charm_model_ns_conv.c:45-65):
@@ -340,21 +393,21 @@ ADJ_HD void flux_hllc_vjp(const Pr<NC> &a, const Pr<NC> &b, const double n[3], c
     const double p_star = (p_pvrs > 0.0) ? p_pvrs : 0.0;
     const double kq = (gam + 1.0) / (2.0 * gam);   // loop-invariant: hoisted by the compiler
     const bool shock_a = !(p_star <= a.p), shock_b = !(p_star <= b.p);
-    // ql = sqrt(1 + kq (p*/pa - 1)) and its reverse need 1/pa and 1/ql
-    const double ipa = shock_a ? rcp(a.p) : 0.0, ipb = shock_b ? rcp(b.p) : 0.0;
-    const double ra = shock_a ? p_star * ipa : 1.0, rb = shock_b ? p_star * ipb : 1.0;
-    const double xa = 1.0 + kq * (ra - 1.0), xb = 1.0 + kq * (rb - 1.0);
-    const double iqa = shock_a ? rsq(xa) : 1.0, iqb = shock_b ? rsq(xb) : 1.0;
-    const double ql = shock_a ? xa * iqa : 1.0;
-    const double qr = shock_b ? xb * iqb : 1.0;
-    const double sl0 = ua - a.cz * ql, sr0 = ub + b.cz * qr;
+    // c q of each side, q = sqrt(1 + kq (p*/p - 1)) on a shock side: as
+    // sqrt(Q), Q = gam / r (p + kq (p* - p)) (one square root, no 1/p, as the
+    // forward flux evaluates it); c where q = 1
+    const double gia = gam * a.ir, gib = gam * b.ir;
+    const double Qa = gia * (a.p + kq * (p_star - a.p)), Qb = gib * (b.p + kq * (p_star - b.p));
+    const double iqa = shock_a ? rsq(Qa) : 0.0, iqb = shock_b ? rsq(Qb) : 0.0;
+    const double cqa = shock_a ? Qa * iqa : a.cz, cqb = shock_b ? Qb * iqb : b.cz;
+    const double sl0 = ua - cqa, sr0 = ub + cqb;
     const bool swap = sl0 > sr0;
     const double sl = swap ? sr0 : sl0, sr = swap ? sl0 : sr0;
     double num = b.p - a.p;
     num += a.r * ua * (sl - ua);
     num -= b.r * ub * (sr - ub);
     const double den = a.r * (sl - ua) - b.r * (sr - ub);
-    const double iden = rcp(den);
+    const double iden = rcp1(den);
     double ss = num * iden;
     int clamp = 0;
     if (ss < sl) { ss = sl; clamp = 1; }
@@ -374,13 +427,14 @@ ADJ_HD void flux_hllc_vjp(const Pr<NC> &a, const Pr<NC> &b, const double n[3], c
             fu = rk * uk * uk + pk; fv = rk * vk * uk; fw = rk * wk * uk;
             q[3] = (rk * ek + pk) * uk;
             for (int i = 0; i < NC; i++) q[4 + i] = rk * uk * ck[i];
-        } else {
-            const double inv = rcp(sk - ss);
-            fu = (ss * (sk * (rk * uk) - (rk * uk * uk + pk)) + sk * (pk + rk * (sk - uk) * (ss - uk))) * inv;
-            fv = (ss * (sk * (rk * vk) - rk * uk * vk)) * inv;
-            fw = (ss * (sk * (rk * wk) - rk * uk * wk)) * inv;
-            q[3] = (ss * (sk * (rk * ek) - (rk * ek + pk) * uk) + sk * (pk + rk * (sk - uk) * (ss - uk)) * ss) * inv;
-            for (int i = 0; i < NC; i++) q[4 + i] = (ss * (sk * (rk * ck[i]) - rk * ck[i] * uk)) * inv;
+        } else {   // the factored star flux of the reverse below
+            const double X = sk - uk, Y = ss - uk, G = rcp(sk - ss);
+            const double rX = rk * X, mf = ss * (rX * G), P = pk + rX * Y;
+            fu = mf * ss + P;
+            fv = mf * vk;
+            fw = mf * wk;
+            q[3] = mf * (ek + Y * ss) + ss * (G * Y) * pk + P * ss;
+            for (int i = 0; i < NC; i++) q[4 + i] = mf * ck[i];
         }
         frame_out<AX>(nt, sn, fu, fv, fw, q);
     }
@@ -406,35 +460,35 @@ ADJ_HD void flux_hllc_vjp(const Pr<NC> &a, const Pr<NC> &b, const double n[3], c
             ckb[i] += x * rk * uk;
         }
     } else {
-        const double X = sk - uk, Y = ss - uk, G = rcp(sk - ss), G2 = G * G;
-        // h(phi) = ss rk phi X G for phi = vk, wk, c_i: the adjoints of ss,
-        // sk, uk, rk are linear in sum(bar * phi)
-        const double KX = ss * X * G, K = rk * KX;
-        double sc = fvb * vk + fwb * wk;
+        // The star flux of :374-435, S_k (S_k U_k - F_k) / (S_k - S*) + S_k p*
+        // D* / (S_k - S*), equals S* U*_k + p* D* for any S* (the clamped one
+        // included), with U*_k = m (1, S*, v_k, w_k, c_k, E*), m = r_k X G:
+        //   X = s_k - u_k, Y = s* - u_k, G = 1 / (s_k - s*), mf = s* m,
+        //   P = p_k + r_k X Y,  fu = mf s* + P,  fv = mf v_k,  fw = mf w_k,
+        //   fc_i = mf c_i,  qe = mf T + Z p_k + P s*,  T = e_k + Y s*,  Z = s* G Y
+        // (e_k the specific total energy); the reverse of that form.
+        const double X = sk - uk, Y = ss - uk, G = rcp1(sk - ss);
+        const double rX = rk * X, m = rX * G, mf = ss * m, P = pk + rX * Y;
+        const double T = ek + Y * ss, GY = G * Y, Z = ss * GY;
+        double mfb = fub * ss + fvb * vk + fwb * wk + qeb * T;
         for (int i = 0; i < NC; i++) {
-            sc += qb[4 + i] * ck[i];
-            ckb[i] += qb[4 + i] * K;
+            mfb += qb[4 + i] * ck[i];
+            ckb[i] += qb[4 + i] * mf;
         }
-        vkb += fvb * K;
-        wkb += fwb * K;
-        ssb += sc * rk * X * sk * G2;
-        skb -= sc * ss * rk * Y * G2;
-        ukb -= sc * ss * rk * G;
-        rkb += sc * KX;
-        // fu = ss rk uk X G + pk + sk rk X Y G
-        ssb += fub * (rk * uk * X * sk * G2 + sk * rk * X * X * G2);
-        skb += fub * (-ss * rk * uk * Y * G2 + rk * Y * G * (X + sk - sk * X * G));
-        ukb += fub * (ss * rk * G * (X - uk) - sk * rk * G * (X + Y));
-        rkb += fub * (ss * uk * X * G + sk * X * Y * G);
-        pkb += fub;
-        // qe = ss X G W, W = rk ek + pk + sk rk Y
-        const double W = rk * ek + pk + sk * rk * Y;
-        ssb += qeb * (X * W * sk * G2 + ss * X * G * sk * rk);
-        skb += qeb * (ss * (-W * Y * G2 + X * G * rk * Y));
-        ukb += qeb * (ss * G * (-W - X * sk * rk));
-        rkb += qeb * (ss * X * G * (ek + sk * Y));
-        ekb += qeb * (ss * X * G * rk);
-        pkb += qeb * (ss * X * G);
+        vkb += fvb * mf;
+        wkb += fwb * mf;
+        const double Pb = fub + qeb * ss, Tb = qeb * mf, Zb = qeb * pk;
+        pkb += Pb + qeb * Z;
+        ekb += Tb;
+        const double mb = mfb * ss;
+        const double Yb = Tb * ss + Zb * ss * G + Pb * rX;
+        const double Gb = Zb * ss * Y + mb * rX;
+        const double W = Pb * Y + mb * G;            // X^ / r_k and r_k^ / X of P and m
+        ssb += fub * mf + qeb * P + Tb * Y + Zb * GY + mfb * m + Gb * G * G + Yb;
+        rkb += X * W;
+        const double Xb = rk * W;
+        skb += Xb - Gb * G * G;
+        ukb -= Xb + Yb;
     }
     // wave speeds
     double slb = 0.0, srb = 0.0;
@@ -451,20 +505,24 @@ ADJ_HD void flux_hllc_vjp(const Pr<NC> &a, const Pr<NC> &b, const double n[3], c
         bb.r -= denb * (sr - ub); srb -= denb * b.r; ubb += denb * b.r;
     }
     const double sl0b = swap ? srb : slb, sr0b = swap ? slb : srb;
-    uab += sl0b; ab.cz -= sl0b * ql;
-    const double qlb = -sl0b * a.cz;
-    ubb += sr0b; bb.cz += sr0b * qr;
-    const double qrb = sr0b * b.cz;
+    uab += sl0b;
+    ubb += sr0b;
     double pstarb = 0.0;
-    if (shock_a) {   // ql = sqrt(1 + kq (p*/pa - 1)): d ql / d p* = kq / (2 ql pa)
-        const double d = 0.5 * kq * iqa * ipa;
-        pstarb += qlb * d;
-        ab.p -= qlb * d * ra;
+    if (shock_a) {   // c q = sqrt(Q): Q^ = (c q)^ / (2 c q); Q = gam ir (p (1 - kq) + kq p*)
+        const double Qab = -0.5 * sl0b * iqa;
+        pstarb += Qab * gia * kq;
+        ab.p += Qab * gia * (1.0 - kq);
+        ab.r -= Qab * Qa * a.ir;                     // ir = 1 / r
+    } else {
+        ab.cz -= sl0b;
     }
     if (shock_b) {
-        const double d = 0.5 * kq * iqb * ipb;
-        pstarb += qrb * d;
-        bb.p -= qrb * d * rb;
+        const double Qbb = 0.5 * sr0b * iqb;
+        pstarb += Qbb * gib * kq;
+        bb.p += Qbb * gib * (1.0 - kq);
+        bb.r -= Qbb * Qb * b.ir;
+    } else {
+        bb.cz += sr0b;
     }
     if (p_pvrs > 0.0) {
         const double D = ub - ua, Rs = 0.25 * (a.r + b.r), Cs = a.cz + b.cz;
@@ -524,6 +582,7 @@ ADJ_HD void bnd(int type, const double *par, const Pr<NC> &in, const double n[3]
     pressure_clamped = out.p < g.eps;
     if (pressure_clamped) out.p = g.eps;
     out.r = out.p * g.m / (out.t * g.R);
+    out.ir = 1.0 / out.r;   // the HLLC wave speeds use 1 / r of each side
     out.cz = sqrt(g.gam * out.p / out.r);
     out.e = out.p / (out.r * (g.gam - 1.0));
     out.e_tot = out.e + 0.5 * (out.u * out.u + out.v * out.v + out.w * out.w);
@@ -577,23 +636,23 @@ ADJ_HD void num_flux_vjp(int flux, const Pr<NC> &a, const Pr<NC> &b, const doubl
     else flux_lf_vjp<NC, AX>(a, b, n, flux == kFluxCD, qb, ab, bb, q);
 }
 
-// Interior point: (Ua, Ub) -> q; Uab/Ubb += (dq/dU)^T qb.
+// Interior point: (Ua, Ub) -> q; Uab/Ubb = (dq/dU)^T qb.
 template <int NC, int AX = -1>
 ADJ_HD void point_vjp(int flux, const double *Ua, const double *Ub, const double n[3], const Gas &g,
                       const double *qb, double *Uab, double *Ubb, double *q)
 {
     Pr<NC> a, b;
-    prim<NC>(Ua, g, a);
-    prim<NC>(Ub, g, b);
+    prim<NC, kPrCz | kPrRcp1>(Ua, g, a);
+    prim<NC, kPrCz | kPrRcp1>(Ub, g, b);
     PrBar<NC> ab, bb;
     zero<NC>(ab);
     zero<NC>(bb);
     num_flux_vjp<NC, AX>(flux, a, b, n, g, qb, ab, bb, q);
-    prim_vjp<NC>(Ua, a, g, ab, Uab);
-    prim_vjp<NC>(Ub, b, g, bb, Ubb);
+    prim_vjp<NC, kPrCz, true>(Ua, a, g, ab, Uab);
+    prim_vjp<NC, kPrCz, true>(Ub, b, g, bb, Ubb);
 }
 
-// Boundary point: U -> q(U, ghost(U)); Uab += (dq/dU)^T qb.
+// Boundary point: U -> q(U, ghost(U)); Uab = (dq/dU)^T qb.
 template <int NC, int AX = -1>
 ADJ_HD void bpoint_vjp(int flux, int type, const double *par, const double *U, const double n[3], const Gas &g,
                        const double *qb, double *Uab, double *q)
@@ -607,7 +666,7 @@ ADJ_HD void bpoint_vjp(int flux, int type, const double *par, const double *U, c
     zero<NC>(ob);
     num_flux_vjp<NC, AX>(flux, a, o, n, g, qb, ab, ob, q);
     bnd_vjp<NC>(type, o, pc, n, g, ob, ab);
-    prim_vjp<NC>(U, a, g, ab, Uab);
+    prim_vjp<NC, kPrAll, true>(U, a, g, ab, Uab);
 }
 
 // Volume point: U -> F_d(U), d = 0..2; Uab += sum_d (dF_d/dU)^T a[d].
@@ -615,11 +674,11 @@ template <int NC>
 ADJ_HD void vpoint_vjp(const double *U, const Gas &g, const double a[3][4 + NC], double *Uab)
 {
     Pr<NC> p;
-    prim<NC>(U, g, p);
+    prim<NC, kPrRcp1>(U, g, p);
     PrBar<NC> b;
     zero<NC>(b);
     vflux_vjp<NC>(U, p, a, b, Uab);
-    prim_vjp<NC>(U, p, g, b, Uab);
+    prim_vjp<NC, 0>(U, p, g, b, Uab);
 }
 
 }  // namespace adj

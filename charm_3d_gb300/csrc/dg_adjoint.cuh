@@ -113,7 +113,6 @@ __device__ __forceinline__ void adj_interior(const MeshDev &m, const double *__r
             Ub[v] = __ldg(u + p0 + e1) - 0.5 * __ldg(u + p0 + (int64_t) (1 + D) * E + e1) +
                     ps1 * __ldg(u + p0 + (int64_t) (1 + s) * E + e1) + pt1 * __ldg(u + p0 + (int64_t) (1 + t) * E + e1);
             qb[v] = A[v] + B[v] * ps + C[v] * pt;
-            Uab[v] = Ubb[v] = 0.0;
         }
         adj::point_vjp<NC, D>(FLUX, Ua, Ub, n, gas, qb, Uab, Ubb, nullptr);
 #pragma unroll
@@ -186,7 +185,6 @@ __device__ __forceinline__ void adj_boundary(const MeshDev &m, const double *__r
         for (int v = 0; v < V; v++) {
             U[v] = c[v][0] + 0.5 * sg * c[v][1 + D] + ps * c[v][1 + s] + pt * c[v][1 + t];
             qb[v] = A[v] + B[v] * ps + C[v] * pt;
-            Ub[v] = 0.0;
         }
         adj::bpoint_vjp<NC, D>(FLUX, type, par, U, n, gas, qb, Ub, nullptr);
 #pragma unroll
@@ -385,12 +383,12 @@ adj_objective_kernel(MeshDev m, const double *__restrict__ u, double lo0, double
                     Ub[v] = 0.0;
                 }
                 adj::Pr<NC> p;
-                adj::prim<NC>(U, gas, p);
+                adj::prim<NC, 0>(U, gas, p);
                 Je += w8 * p.p;
                 adj::PrBar<NC> b;
                 adj::zero<NC>(b);
                 b.p = w8;
-                adj::prim_vjp<NC>(U, p, gas, b, Ub);
+                adj::prim_vjp<NC, 0>(U, p, gas, b, Ub);
 #pragma unroll
                 for (int v = 0; v < V; v++) {
                     lam[v][0] += Ub[v];
