@@ -2,11 +2,13 @@
  * GPU model plugin for CHARM_3D: a drop-in timestep_single_fn / get_dt_fn.
  *
  * Compiled inside the reference's tree (it includes the reference's own
- * charm_globals.h and p4est), it replaces the pair that
- * charm_model_ns_init registers (reference
- * src/models/ns/charm_model_ns_init.cpp:79-88):
+ * charm_globals.h and p4est), it replaces the pair that the model's init
+ * registers, charm_model_ns_init (reference
+ * src/models/ns/charm_model_ns_init.cpp:79-88) or charm_model_euler_init
+ * (src/models/euler/charm_model_euler_init.cpp:18), and steps the model
+ * it replaced (SSP-RK3 or forward Euler):
  *
- *     charm_model_gpu_init(ctx, CHARM_GPU_PREC_FP64);
+ *     charm_model_gpu_init(ctx, CHARM_GPU_PREC_FP64, 0);
  *
  * after charm_init_context_yaml() has filled ctx from task.yaml.  The time
  * loop (charm_timesteps, src/charm_timesteps.c:23-51) is unchanged.
@@ -33,6 +35,7 @@
 #include "charm_eos.h"
 #include "charm_fluxes.h"
 #include "charm_limiter.h"
+#include "charm_models.h"
 #include "charm_gpu.h"
 
 #include <math.h>
@@ -43,6 +46,7 @@
 typedef struct {
     charm_gpu_handle_t h;
     int precision;
+    int model;             /* CHARM_GPU_MODEL_* of the pair the plugin replaced */
     int device;
     int mesh_valid;        /* forest unchanged since the last upload */
     int device_newer;      /* HBM holds a newer state than the quadrants */
@@ -305,12 +309,26 @@ int charm_model_gpu_flatten_hex(charm_gpu_mesh_t *mesh, charm_gpu_hex_t *hex)
 
 /* ---- configuration from the reference context ------------------------------- */
 
+void charm_model_gpu_timestep_single(p4est_t *p4est, charm_real_t *dt, p4est_ghost_t **_ghost,
+                                     charm_data_t **_ghost_data);
+
+/* The model of a context, told apart as the reference does, by the step its
+ * model init registered: charm_model_euler_init's forward-Euler step
+ * (src/models/euler/charm_model_euler_init.cpp:18) or the NS model's
+ * SSP-RK3 step; once the plugin pair is registered, the model it replaced. */
+static int model_of(const charm_ctx_t *ctx)
+{
+    if (ctx->timestep_single_fn == charm_model_euler_timestep_single) return CHARM_GPU_MODEL_EULER;
+    if (ctx->timestep_single_fn == charm_model_gpu_timestep_single) return g_gpu.model;
+    return CHARM_GPU_MODEL_NS;
+}
+
 int charm_model_gpu_config(charm_ctx_t *ctx, int precision, charm_gpu_config_t *cfg)
 {
     size_t i;
     int k;
     memset(cfg, 0, sizeof(*cfg));
-    cfg->model = CHARM_GPU_MODEL_NS;
+    cfg->model = model_of(ctx);
     if (ctx->flux_fn == charm_calc_flux_lf) cfg->flux = CHARM_GPU_FLUX_LF;
     else if (ctx->flux_fn == charm_calc_flux_hllc) cfg->flux = CHARM_GPU_FLUX_HLLC;
     else if (ctx->flux_fn == charm_calc_flux_cd) cfg->flux = CHARM_GPU_FLUX_CD;
@@ -354,9 +372,11 @@ int charm_model_gpu_config(charm_ctx_t *ctx, int precision, charm_gpu_config_t *
     }
     cfg->tau = ctx->dt;
     cfg->cfl = ctx->CFL;
-    cfg->t_ref = ctx->model.ns.t_ref;
-    cfg->use_visc = ctx->model.ns.use_visc;
-    cfg->use_diff = ctx->model.ns.use_diff;
+    if (cfg->model == CHARM_GPU_MODEL_NS) {   /* ctx->model is a union: the ns member only for NS */
+        cfg->t_ref = ctx->model.ns.t_ref;
+        cfg->use_visc = ctx->model.ns.use_visc;
+        cfg->use_diff = ctx->model.ns.use_diff;
+    }
     cfg->p_order = CHARM_BASE_FN_COUNT == 10 ? 2 : 1;   /* include/charm_def.h:177 */
     cfg->n_react = 0;
     if (ctx->reactions) {   /* charm_reaction_t list of src/models/ns/charm_model_ns_init.cpp:58-77 */
@@ -489,11 +509,13 @@ void charm_model_gpu_timestep_single(p4est_t *p4est, charm_real_t *dt, p4est_gho
     g_gpu.device_newer = 1;
 }
 
-/* Register the plugin pair in place of the NS model's (call after
+/* Register the plugin pair in place of the model's (call after
  * charm_init_context_yaml).  precision: CHARM_GPU_PREC_FP64 or _MIXED. */
 void charm_model_gpu_init(charm_ctx_t *ctx, int precision, int device)
 {
+    const int model = model_of(ctx);
     memset(&g_gpu, 0, sizeof(g_gpu));
+    g_gpu.model = model;
     g_gpu.precision = precision;
     g_gpu.device = device;
     ctx->timestep_single_fn = charm_model_gpu_timestep_single;

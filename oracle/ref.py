@@ -51,6 +51,7 @@ def load(variant: str = "ref") -> C.CDLL:
             lib.ref_plugin_flatten.argtypes = [C.c_void_p]
             lib.ref_plugin_flatten_hex.argtypes = [C.c_void_p, C.c_void_p]
             lib.ref_plugin_config.argtypes = [C.c_int, C.c_void_p]
+            lib.ref_plugin_use_gpu.argtypes = [C.c_int]
         _libs[variant] = lib
     return _libs[variant]
 
@@ -186,6 +187,15 @@ class RefSolver:
         if rc:
             raise RuntimeError(f"charm_model_gpu_config: {rc}")
         return cfg
+
+    def plugin_use_gpu(self, precision: int = 0) -> None:
+        """Step through the GPU model plugin from now on (charm_model_gpu_init)."""
+        self.lib.ref_plugin_use_gpu(precision)
+
+    def plugin_finish(self) -> int:
+        """The plugin's state back into the quadrants, its handle released;
+        the plugin's status (0 or a CHARM_GPU_* code)."""
+        return int(self.lib.ref_plugin_finish())
 
     def point_flux(self, prim2, n) -> np.ndarray:
         p = np.ascontiguousarray(prim2, dtype=np.float64)

@@ -46,13 +46,18 @@ def test_plugin_flatten_matches_host_octree(kind, hang):
     assert bg == bw
 
 
-@pytest.mark.parametrize("kind,flux,lim", [("walls", "HLLC", "BJ"), ("mix2", "LF", "NONE"), ("random", "CD", "BJ")])
-def test_plugin_config_matches_case(kind, flux, lim):
-    case = small_case(kind, flux, lim, level=1)
+@pytest.mark.parametrize("kind,flux,lim,model", [("walls", "HLLC", "BJ", "NS"), ("mix2", "LF", "NONE", "NS"),
+                                                 ("random", "CD", "BJ", "NS"), ("random", "HLLC", "BJ", "EULER")])
+def test_plugin_config_matches_case(kind, flux, lim, model):
+    """The model comes from the step the reference's model init registered
+    (forward Euler for charm_model_euler_init, SSP-RK3 for the NS model)."""
+    case = small_case(kind, flux, lim, level=1, model=model)
     ref = RefSolver(case, "plugin")
     got = ref.plugin_config(abi.PRECISION["FP64"])
     want = case.config()
-    want.model = abi.MODEL["NS"]
+    assert want.model == abi.MODEL[model]
+    if model == "EULER":
+        want.t_ref = 0.0   # ctx->model.ns is not the Euler model's member (t_ref is unused on its step)
     assert bytes(got) == bytes(want)
 
 
