@@ -20,7 +20,9 @@ from .common import rel_max, small_case
 from .hexmesh import (FACE_CORNERS, SIDE_PATCHES, WEDGE_PATCHES, block_forest, block_mesh, keystone, wedge_mesh,
                       write_gmsh)
 
-REF = os.environ.get("CHARM_REFERENCE", "/root/reference")
+from oracle.build_ref import reference_root  # noqa: E402
+
+REF = reference_root() or ""
 
 
 def face_center(mesh, e, f):
