@@ -480,9 +480,12 @@ hex_limit_kernel(MeshDev m, HexDev x, const double *__restrict__ ua, const doubl
             if (umax[v] < nbv[v]) umax[v] = nbv[v];
         }
     }
-    double psi[V];
+    // psi over the 8 corners: the largest and the most negative difference
+    // per variable, then two quotients (bj_side_psi: the reference's
+    // per-corner minimum, bit for bit)
+    double psi[V], dmax[V], dmin[V];
 #pragma unroll
-    for (int v = 0; v < V; v++) psi[v] = 1.0;
+    for (int v = 0; v < V; v++) dmax[v] = dmin[v] = 0.0;
 #pragma unroll 1
     for (int k = 0; k < 8; k++) {
         const double p1 = hex_g(x, E, kGvert + 3 * k, e), p2 = hex_g(x, E, kGvert + 3 * k + 1, e),
@@ -491,14 +494,12 @@ hex_limit_kernel(MeshDev m, HexDev x, const double *__restrict__ ua, const doubl
         for (int v = 0; v < V; v++) {
             const double f = c[v][0] + p1 * c[v][1] + p2 * c[v][2] + p3 * c[v][3];
             const double df = f - own[v];
-            double pt = 1.0;
-            if (fabs(df) > kEps) {
-                if (df > 0) pt = fmin(1.0, (umax[v] - own[v]) / df);
-                else if (df < 0) pt = fmin(1.0, (umin[v] - own[v]) / df);
-            }
-            if (pt < psi[v]) psi[v] = pt;
+            dmax[v] = fmax(dmax[v], df);
+            dmin[v] = fmin(dmin[v], df);
         }
     }
+#pragma unroll
+    for (int v = 0; v < V; v++) psi[v] = bj_side_psi(dmax[v], dmin[v], umin[v] - own[v], umax[v] - own[v]);
     const bool comb = (a_old != 0.0);
     double cen[V];
 #pragma unroll

@@ -476,6 +476,27 @@ cell_kernel(MeshDev m, const double *__restrict__ u, const T *__restrict__ slots
 // mean equals c_0 up to rounding.  Species get the same treatment as the
 // other variables at hanging faces (the reference leaves those slots stale,
 // src/limiters/charm_limiter_bj.c:174-193).
+// Barth-Jespersen scaling from the 8 vertex differences of each variable
+// (bj_side_psi).
+template <int V>
+__device__ __forceinline__ void bj_psi8(const double c[V][kNB], const double umin[V], const double umax[V],
+                                        double psi[V])
+{
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+        double dmax = 0.0, dmin = 0.0;
+#pragma unroll
+        for (int vx = 0; vx < 8; vx++) {
+            const double sx = (vx & 1) ? 0.5 : -0.5, sy = (vx & 2) ? 0.5 : -0.5, sz = (vx & 4) ? 0.5 : -0.5;
+            const double f = c[v][0] + sx * c[v][1] + sy * c[v][2] + sz * c[v][3];
+            const double df = f - c[v][0];
+            dmax = fmax(dmax, df);
+            dmin = fmin(dmin, df);
+        }
+        psi[v] = bj_side_psi(dmax, dmin, umin[v] - c[v][0], umax[v] - c[v][0]);
+    }
+}
+
 template <int NC>
 __global__ void __launch_bounds__(128)
 limit_kernel(MeshDev m, const double *__restrict__ ua, const double *u0, double *out,
@@ -539,23 +560,7 @@ limit_kernel(MeshDev m, const double *__restrict__ ua, const double *u0, double 
 
     // psi over the 8 vertices (charm_limiter_bj.c:275-299); basis = +-1/2
     double psi[V];
-#pragma unroll
-    for (int v = 0; v < V; v++) psi[v] = 1.0;
-#pragma unroll
-    for (int vx = 0; vx < 8; vx++) {
-        const double sx = (vx & 1) ? 0.5 : -0.5, sy = (vx & 2) ? 0.5 : -0.5, sz = (vx & 4) ? 0.5 : -0.5;
-#pragma unroll
-        for (int v = 0; v < V; v++) {
-            const double f = c[v][0] + sx * c[v][1] + sy * c[v][2] + sz * c[v][3];
-            const double df = f - c[v][0];
-            double pt = 1.0;
-            if (fabs(df) > kEps) {
-                if (df > 0) pt = fmin(1.0, (umax[v] - c[v][0]) / df);
-                else if (df < 0) pt = fmin(1.0, (umin[v] - c[v][0]) / df);
-            }
-            if (pt < psi[v]) psi[v] = pt;
-        }
-    }
+    bj_psi8<V>(c, umin, umax, psi);
     if (psi_out) {   // the scaling, kept for the adjoint (frozen active set)
 #pragma unroll
         for (int v = 0; v < V; v++) psi_out[(int64_t) v * E + e] = psi[v];
@@ -1069,22 +1074,24 @@ ff_limit_kernel(MeshDev m, const float *__restrict__ ah_, const float *__restric
             umax[v] = fmaxf(umax[v], nbv[v]);
         }
     }
+    // psi from the largest and the most negative vertex difference per
+    // variable: two correctly rounded quotients, monotone in the
+    // difference, give the per-vertex minimum (as bj_side_psi in FP64)
     float psi[V];
 #pragma unroll
-    for (int v = 0; v < V; v++) psi[v] = 1.f;
+    for (int v = 0; v < V; v++) {
+        float dmax = 0.f, dmin = 0.f;
 #pragma unroll
-    for (int vx = 0; vx < 8; vx++) {
-        const float sx = (vx & 1) ? 0.5f : -0.5f, sy = (vx & 2) ? 0.5f : -0.5f, sz = (vx & 4) ? 0.5f : -0.5f;
-#pragma unroll
-        for (int v = 0; v < V; v++) {
+        for (int vx = 0; vx < 8; vx++) {
+            const float sx = (vx & 1) ? 0.5f : -0.5f, sy = (vx & 2) ? 0.5f : -0.5f, sz = (vx & 4) ? 0.5f : -0.5f;
             const float df = sx * c[v][1] + sy * c[v][2] + sz * c[v][3];
-            float pt = 1.f;
-            if (fabsf(df) > (float) kEps) {
-                if (df > 0.f) pt = fminf(1.f, (umax[v] - c[v][0]) / df);
-                else pt = fminf(1.f, (umin[v] - c[v][0]) / df);
-            }
-            psi[v] = fminf(psi[v], pt);
+            dmax = fmaxf(dmax, df);
+            dmin = fminf(dmin, df);
         }
+        float p = 1.f;
+        if (dmax > (float) kEps) p = fminf(p, fminf(1.f, (umax[v] - c[v][0]) / dmax));
+        if (dmin < -(float) kEps) p = fminf(p, fminf(1.f, (umin[v] - c[v][0]) / dmin));
+        psi[v] = p;
     }
 #pragma unroll
     for (int v = 0; v < V; v++) {

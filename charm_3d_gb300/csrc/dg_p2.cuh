@@ -1051,9 +1051,12 @@ p2_limit_kernel(MeshDev m, const double *__restrict__ ua, const double *u0, doub
             if (umax[v] < nbv[v]) umax[v] = nbv[v];
         }
     }
-    double psi[V];
+    // psi over the 8 corners: the largest and the most negative difference
+    // per variable, then two quotients (bj_side_psi: the reference's
+    // per-corner minimum, bit for bit)
+    double psi[V], dmax[V], dmin[V];
 #pragma unroll
-    for (int v = 0; v < V; v++) psi[v] = 1.0;
+    for (int v = 0; v < V; v++) dmax[v] = dmin[v] = 0.0;
 #pragma unroll 1
     for (int vx = 0; vx < 8; vx++) {
         double ph[kNB2];
@@ -1064,14 +1067,12 @@ p2_limit_kernel(MeshDev m, const double *__restrict__ ua, const double *u0, doub
 #pragma unroll
             for (int k = 0; k < kNB2; k++) f += __ldg(ua + (int64_t) (v * kNB2 + k) * E + e) * ph[k];
             const double df = f - own[v];
-            double pt = 1.0;
-            if (fabs(df) > kEps) {
-                if (df > 0) pt = fmin(1.0, (umax[v] - own[v]) / df);
-                else if (df < 0) pt = fmin(1.0, (umin[v] - own[v]) / df);
-            }
-            if (pt < psi[v]) psi[v] = pt;
+            dmax[v] = fmax(dmax[v], df);
+            dmin[v] = fmin(dmin[v], df);
         }
     }
+#pragma unroll
+    for (int v = 0; v < V; v++) psi[v] = bj_side_psi(dmax[v], dmin[v], umin[v] - own[v], umax[v] - own[v]);
     const bool comb = (a_old != 0.0);
 #pragma unroll
     for (int v = 0; v < V; v++)
