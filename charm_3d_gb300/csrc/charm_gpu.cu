@@ -374,6 +374,8 @@ void build_devcfg(const charm_gpu_config_t *c, DevCfg *d)
     d->ideal_gm1_f = (float) d->ideal_gam - 1.f;   // as the float path computed it before
     for (int i = 0; i < CHARM_GPU_MAX_COMP; i++) {
         d->comp_m_f[i] = (float) d->comp_m[i];
+        d->comp_inv_m[i] = d->comp_m[i] != 0.0 ? 1.0 / d->comp_m[i] : 0.0;
+        d->comp_inv_m_f[i] = (float) d->comp_inv_m[i];
         for (int k = 0; k < CHARM_GPU_MAX_CP; k++) d->comp_cp_f[i][k] = (float) d->comp_cp[i][k];
     }
     for (int b = 0; b < CHARM_GPU_MAX_BND; b++)

@@ -57,6 +57,9 @@ struct DevCfg {
     // on GB300 those run on the narrow FP64 pipe.
     float  ideal_cp_f, ideal_m_f, ideal_cv_f, ideal_gam_f, ideal_inv_cv_f, ideal_qg_f, ideal_gm1_f;
     float  comp_m_f[kMaxComp];
+    // 1 / m of each component (the mixture EOS multiplies instead of dividing)
+    double comp_inv_m[kMaxComp];
+    float  comp_inv_m_f[kMaxComp];
     float  comp_cp_f[kMaxComp][kMaxCp];
     float  bnd_par_f[kMaxBnd][7 + kMaxComp];
     float  grav_f[3];
@@ -253,17 +256,21 @@ __device__ __forceinline__ void eos_props(Prim<T, NC> &p, int flag)
     if (c_cfg.eos == CHARM_GPU_EOS_IDEAL) {
         p.cp = comp_cp<T>(0, t);
         p.m  = cfgv<T>(c_cfg.comp_m[0], c_cfg.comp_m_f[0]);
+        p.cv  = p.cp - qdiv<T>(T(kGasR), p.m);
     } else {
+        // the mixture's 1/m = sum c_i / m_i, with the stored 1/m_i; cv = cp -
+        // R/m as cp - R (1/m); the quotients of the flux path's reciprocal
+        // (within 2 ulp of the reference's divisions)
         T cp = T(0), M_ = T(0);
         for (int i = 0; i < NC; i++) {
-            M_ += p.c[i] / cfgv<T>(c_cfg.comp_m[i], c_cfg.comp_m_f[i]);
+            M_ += p.c[i] * cfgv<T>(c_cfg.comp_inv_m[i], c_cfg.comp_inv_m_f[i]);
             cp += p.c[i] * comp_cp<T>(i, t);
         }
         p.cp = cp;
-        p.m  = T(1) / M_;
+        p.m  = qrcp<T>(M_);
+        p.cv = p.cp - T(kGasR) * M_;
     }
-    p.cv  = p.cp - T(kGasR) / p.m;
-    p.gam = p.cp / p.cv;
+    p.gam = qdiv<T>(p.cp, p.cv);
 }
 
 // _charm_mat_eos_switch (:57-96).  Only the flags used on the path.
@@ -288,8 +295,8 @@ __device__ __forceinline__ void eos_switch(Prim<T, NC> &p, int flag)
     default:  // 4: (r,e) -> (p, cz, T); p.ir set by the caller
         if (p.r < eps) { p.r = eps; p.ir = T(1) / eps; }
         p.p  = p.r * p.e * (p.gam - T(1));
-        p.cz = sqrt(p.gam * p.p / p.r);
-        p.t  = p.e / p.cv;
+        p.cz = sqrt(p.gam * p.p * p.ir);
+        p.t  = qdiv<T>(p.e, p.cv);
         break;
     }
 }
