@@ -63,7 +63,7 @@ __device__ __forceinline__ void transport(const Prim<T, NC> &p, T &mu, T &kt)
         const bool sk = c_cfg.comp_kp_type[i] == CHARM_GPU_LAW_SUTHERLAND;
         const T f = (sm || sk) ? sutherland<T>(i, p.t) : T(1);
         const T ml0 = cfgv<T>(c_cfg.comp_ml0[i], c_cfg.comp_ml0_f[i]), kp0 = cfgv<T>(c_cfg.comp_kp0[i], c_cfg.comp_kp0_f[i]);
-        const T cm = qdiv<T>(p.c[i], cfgv<T>(c_cfg.comp_m[i], c_cfg.comp_m_f[i]));
+        const T cm = p.c[i] * cfgv<T>(c_cfg.comp_inv_m[i], c_cfg.comp_inv_m_f[i]);
         s += cm;
         m += cm * (sm ? ml0 * f : ml0);
         k += p.c[i] * (sk ? kp0 * f : kp0);
@@ -88,7 +88,10 @@ __device__ __forceinline__ void vgrad_q(T mu, T kt, T fr, T ft, T fu, T fv, T fw
                                         const T n[3], T q[9])
 {
     const T lambda = T(0);   // charm_get_visc_lambda (src/charm_globals.c:509-512)
-    const T lp = (lambda + T(4) * mu / T(3)), lm = (lambda - T(2) * mu / T(3));
+    // 4 mu / 3 and 2 mu / 3 as products with 1/3 (within 1 ulp; a quotient
+    // by 3 would be a full division at every face point)
+    const T third = T(1.0 / 3.0);
+    const T lp = (lambda + T(4) * mu * third), lm = (lambda - T(2) * mu * third);
     q[0] = lp * fu * n[0] + lm * fv * n[1] + lm * fw * n[2];
     q[1] = lm * fu * n[0] + lp * fv * n[1] + lm * fw * n[2];
     q[2] = lm * fu * n[0] + lm * fv * n[1] + lp * fw * n[2];
