@@ -1298,20 +1298,69 @@ __device__ __forceinline__ void face_sums(const float cl[4 + NC][kNB], const flo
     }
 }
 
-template <int NC, int FLUX, int D>
+// Momentum components (x, y, z) of a face along axis D into the face frame
+// (normal, t1, t2) of the flux (frame_in of dg_device.cuh: D = 1 gives
+// (y, -x, z), D = 2 gives (z, -y, x)) and back (frame_out): signed
+// permutations, exact.
+__device__ __forceinline__ void tile_rot_in(int D, float &a, float &b, float &c)
+{
+    const float x = a, y = b, z = c;
+    a = (D == 0) ? x : (D == 1) ? y : z;
+    b = (D == 0) ? y : (D == 1) ? -x : -y;
+    c = (D == 2) ? x : z;
+}
+
+__device__ __forceinline__ void tile_rot_out(int D, float &a, float &b, float &c)
+{
+    const float fu = a, fv = b, fw = c;
+    a = (D == 0) ? fu : (D == 1) ? -fv : fw;
+    b = (D == 0) ? fv : (D == 1) ? fu : -fv;
+    c = (D == 2) ? fu : fw;
+}
+
+// Interior (sub-)face of a tile, its axis D read at run time: the
+// coefficients of both leaves reordered into the face frame (mean, slope
+// along the normal, along s, along t) and their momentum components
+// rotated by tile_rot_in, then the 6-point sums of a face along x, whose
+// momentum components tile_rot_out turns back.  One inlined face path
+// serves all three axes, which keeps the face loop of tile_stage_kernel
+// within the instruction cache.
+template <int NC, int FLUX>
 __device__ __forceinline__ void tile_interior(const MeshDev &m, const float *s_u, int ncol, int4 r, float *out,
                                               unsigned *err)
 {
     constexpr int V = 4 + NC;
-    constexpr int s = (D == 0) ? 1 : 0, t = (D == 2) ? 1 : 2;
     const unsigned info = (unsigned) r.z;
+    const int D = info & 3, s = (D == 0) ? 1 : 0, t = (D == 2) ? 1 : 2;
     const int kind = (info >> 2) & 3, sub = (info >> 4) & 3;
     float cl[V][kNB], cu[V][kNB];
-    col_coef<V>(s_u, ncol, r.x, cl);
-    col_coef<V>(s_u, ncol, r.y, cu);
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+        const int b = v * kNB;
+        cl[v][0] = s_u[b * ncol + r.x];
+        cl[v][1] = s_u[(b + 1 + D) * ncol + r.x];
+        cl[v][2] = s_u[(b + 1 + s) * ncol + r.x];
+        cl[v][3] = s_u[(b + 1 + t) * ncol + r.x];
+        cu[v][0] = s_u[b * ncol + r.y];
+        cu[v][1] = s_u[(b + 1 + D) * ncol + r.y];
+        cu[v][2] = s_u[(b + 1 + s) * ncol + r.y];
+        cu[v][3] = s_u[(b + 1 + t) * ncol + r.y];
+    }
+#pragma unroll
+    for (int k = 0; k < kNB; k++) {
+        tile_rot_in(D, cl[0][k], cl[1][k], cl[2][k]);
+        tile_rot_in(D, cu[0][k], cu[1][k], cu[2][k]);
+    }
     float S0[V], Ss[V], St[V];
-    face_sums<NC, FLUX, D>(cl, cu, kind, sub, S0, Ss, St, err);
-    const float w = level_ht<float>(m, r.w, s) * level_ht<float>(m, r.w, t) * (1.f / 6.f);
+    face_sums<NC, FLUX, 0>(cl, cu, kind, sub, S0, Ss, St, err);
+    tile_rot_out(D, S0[0], S0[1], S0[2]);
+    tile_rot_out(D, Ss[0], Ss[1], Ss[2]);
+    tile_rot_out(D, St[0], St[1], St[2]);
+    // the tangential edges (s is axis 0 or 1, t axis 1 or 2), chosen by
+    // value: no run-time index into the kernel's parameters
+    const float Ls = (s == 0) ? m.tree_len_f[0] : m.tree_len_f[1];
+    const float Lt = (t == 1) ? m.tree_len_f[1] : m.tree_len_f[2];
+    const float w = ldexpf(Ls, -r.w) * ldexpf(Lt, -r.w) * (1.f / 6.f);
 #pragma unroll
     for (int v = 0; v < V; v++) {
         out[v] = w * S0[v];
@@ -1517,11 +1566,7 @@ tile_stage_kernel(MeshDev m, TileDev tl, const float *__restrict__ uh, const flo
             default: tile_boundary<NC, FLUX, 2>(m, s_u, ncol, r, out, err); break;
             }
         } else {
-            switch (r.z & 3) {
-            case 0: tile_interior<NC, FLUX, 0>(m, s_u, ncol, r, out, err); break;
-            case 1: tile_interior<NC, FLUX, 1>(m, s_u, ncol, r, out, err); break;
-            default: tile_interior<NC, FLUX, 2>(m, s_u, ncol, r, out, err); break;
-            }
+            tile_interior<NC, FLUX>(m, s_u, ncol, r, out, err);
         }
     }
     __syncthreads();
