@@ -1541,13 +1541,14 @@ int upload_impl(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh, const int8_t
             std::sort(hl.begin(), hl.end());
             hl.erase(std::unique(hl.begin(), hl.end()), hl.end());
         };
+        // each tile's lists once, kept for the fill below
         std::vector<int32_t> tptr(nt + 1, 0), hptr(nt + 1, 0);
+        std::vector<std::vector<int32_t>> lists((size_t) nt), halos((size_t) nt);
         host_for(nt, 64, [&](int64_t lo, int64_t hi) {
-            std::vector<int32_t> list, hl;
             for (int64_t t = lo; t < hi; t++) {
-                tile_lists(t, list, hl);
-                tptr[t + 1] = (int32_t) list.size();
-                hptr[t + 1] = (int32_t) hl.size();
+                tile_lists(t, lists[t], halos[t]);
+                tptr[t + 1] = (int32_t) lists[t].size();
+                hptr[t + 1] = (int32_t) halos[t].size();
             }
         });
         int64_t max_list = 0, max_halo = 0;
@@ -1560,9 +1561,8 @@ int upload_impl(charm_gpu_handle_t h, const charm_gpu_mesh_t *mesh, const int8_t
         std::vector<int4> trec(tptr[nt] > 0 ? tptr[nt] : 1);
         std::vector<int32_t> tslot(6 * E, -1), halo(hptr[nt] > 0 ? hptr[nt] : 1, 0);
         host_for(nt, 64, [&](int64_t lo, int64_t hi) {
-            std::vector<int32_t> list, hl;
             for (int64_t t = lo; t < hi; t++) {
-                tile_lists(t, list, hl);
+                const std::vector<int32_t> &list = lists[t], &hl = halos[t];
                 const int64_t e0 = t * kTile, e1 = std::min<int64_t>(E, e0 + kTile);
                 std::copy(hl.begin(), hl.end(), halo.begin() + hptr[t]);
                 auto column = [&](int32_t e) -> int32_t {
