@@ -283,7 +283,8 @@ int charm_gpu_abi_sizes(int64_t out[6]);
  * meshes are rejected with CHARM_GPU_EINVAL and a message.  The first call
  * on a device (with that device current) looks up the array's address:
  * make it before any stream capture.  All calls share the array, so calls
- * that overlap on the GPU race; serialise them.  Synchronises `stream`.
+ * that overlap on the GPU race; serialise them.  Synchronises `stream` to
+ * read its error words, so no call can be captured into a CUDA graph.
  * Errors as charm_gpu_sync reports them for a handle (non-finite state,
  * non-positive density or pressure at a Gauss point, HLLC wave order), and
  * CHARM_GPU_EINVAL for face records that point outside the mesh, mortar
