@@ -38,8 +38,9 @@ __device__ __forceinline__ void adj_rbar(const MeshDev &m, const double *__restr
     if (scale_minv) {
         const int lev = m.level[e];
         const double vol = level_h(m, lev, 0) * level_h(m, lev, 1) * level_h(m, lev, 2);
-        s0 = coef / vol;
-        s1 = coef * 12.0 / vol;
+        const double iv = rcp_nr(vol);   // the flux path's reciprocal: no division per element side
+        s0 = coef * iv;
+        s1 = coef * 12.0 * iv;
     }
 #pragma unroll
     for (int v = 0; v < V; v++)
@@ -253,9 +254,9 @@ adj_cell_kernel(MeshDev m, const double *__restrict__ u, const double *sh, doubl
         adj_rbar<V>(m, sh, e, coef, scale_minv, rb);
 #pragma unroll
         for (int v = 0; v < V; v++) {
-            a[0][v] = -(w8 / hx) * rb[v][1];
-            a[1][v] = -(w8 / hy) * rb[v][2];
-            a[2][v] = -(w8 / hz) * rb[v][3];
+            a[0][v] = -(hy * hz * 0.125) * rb[v][1];   // (vol / 8) / h_a as a product
+            a[1][v] = -(hx * hz * 0.125) * rb[v][2];
+            a[2][v] = -(hx * hy * 0.125) * rb[v][3];
 #pragma unroll
             for (int k = 0; k < kNB; k++) lam[v][k] = base * __ldg(sh + (int64_t) (v * kNB + k) * E + e);
         }
