@@ -169,7 +169,8 @@ __device__ __forceinline__ T qsqrt(T x)
 // rounded value: the minimum over the positive side is the one quotient
 // by the largest df_k, over the negative side the one by the most
 // negative df_k.  Two divisions per variable instead of eight; the same
-// psi bit for bit.
+// psi (where both bounds equal u0 a zero whose sign the reference takes
+// from the first vertex it visits; +0 here).
 __device__ __forceinline__ double bj_side_psi(double dmax, double dmin, double lo, double hi)
 {
     double psi = 1.0;

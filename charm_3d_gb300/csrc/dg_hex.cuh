@@ -482,7 +482,7 @@ hex_limit_kernel(MeshDev m, HexDev x, const double *__restrict__ ua, const doubl
     }
     // psi over the 8 corners: the largest and the most negative difference
     // per variable, then two quotients (bj_side_psi: the reference's
-    // per-corner minimum, bit for bit)
+    // per-corner minimum)
     double psi[V], dmax[V], dmin[V];
 #pragma unroll
     for (int v = 0; v < V; v++) dmax[v] = dmin[v] = 0.0;

@@ -1053,7 +1053,7 @@ p2_limit_kernel(MeshDev m, const double *__restrict__ ua, const double *u0, doub
     }
     // psi over the 8 corners: the largest and the most negative difference
     // per variable, then two quotients (bj_side_psi: the reference's
-    // per-corner minimum, bit for bit)
+    // per-corner minimum)
     double psi[V], dmax[V], dmin[V];
 #pragma unroll
     for (int v = 0; v < V; v++) dmax[v] = dmin[v] = 0.0;
