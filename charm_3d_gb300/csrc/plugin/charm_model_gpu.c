@@ -509,12 +509,25 @@ void charm_model_gpu_timestep_single(p4est_t *p4est, charm_real_t *dt, p4est_gho
     g_gpu.device_newer = 1;
 }
 
+/* The handle and every flattened array, released (the state on the device
+ * is not brought back). */
+static void release_all(void)
+{
+    if (g_gpu.h) charm_gpu_destroy(g_gpu.h);
+    free(g_gpu.center); free(g_gpu.level); free(g_gpu.face_elem0); free(g_gpu.face_elem1); free(g_gpu.face_all);
+    free(g_gpu.face_info); free(g_gpu.bface_elem); free(g_gpu.bface_face); free(g_gpu.bface_bnd); free(g_gpu.state);
+    free(g_gpu.vertex); free(g_gpu.hface_elem0); free(g_gpu.hface_elem1); free(g_gpu.hface_all); free(g_gpu.hface_info);
+    free(g_gpu.hface_face0); free(g_gpu.hface_face1); free(g_gpu.hface_face_all);
+    memset(&g_gpu, 0, sizeof(g_gpu));
+}
+
 /* Register the plugin pair in place of the model's (call after
- * charm_init_context_yaml).  precision: CHARM_GPU_PREC_FP64 or _MIXED. */
+ * charm_init_context_yaml).  precision: CHARM_GPU_PREC_FP64 or _MIXED.  A
+ * second call releases what the first one's run held. */
 void charm_model_gpu_init(charm_ctx_t *ctx, int precision, int device)
 {
     const int model = model_of(ctx);
-    memset(&g_gpu, 0, sizeof(g_gpu));
+    release_all();
     g_gpu.model = model;
     g_gpu.precision = precision;
     g_gpu.device = device;
@@ -525,13 +538,6 @@ void charm_model_gpu_init(charm_ctx_t *ctx, int precision, int device)
 /* Download the final state and release the GPU handle. */
 void charm_model_gpu_finalize(p4est_t *p4est)
 {
-    if (g_gpu.h) {
-        charm_model_gpu_download(p4est);
-        charm_gpu_destroy(g_gpu.h);
-    }
-    free(g_gpu.center); free(g_gpu.level); free(g_gpu.face_elem0); free(g_gpu.face_elem1); free(g_gpu.face_all);
-    free(g_gpu.face_info); free(g_gpu.bface_elem); free(g_gpu.bface_face); free(g_gpu.bface_bnd); free(g_gpu.state);
-    free(g_gpu.vertex); free(g_gpu.hface_elem0); free(g_gpu.hface_elem1); free(g_gpu.hface_all); free(g_gpu.hface_info);
-    free(g_gpu.hface_face0); free(g_gpu.hface_face1); free(g_gpu.hface_face_all);
-    memset(&g_gpu, 0, sizeof(g_gpu));
+    if (g_gpu.h) charm_model_gpu_download(p4est);
+    release_all();
 }

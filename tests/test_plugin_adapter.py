@@ -95,3 +95,18 @@ def test_plugin_keeps_the_box_form_on_bricks():
     ref = RefSolver(case, "plugin")
     is_hex, _ = ref.plugin_flatten_hex()
     assert not is_hex
+
+
+def test_plugin_init_again_and_finish_release_what_it_holds():
+    """charm_model_gpu_init a second time releases the flattened arrays of
+    the first (no handle exists before a step, so nothing reaches a GPU),
+    and charm_model_gpu_finalize releases the rest; the flattening still
+    works between them."""
+    case = small_case("random", "HLLC", "BJ", level=2)
+    ref = RefSolver(case, "plugin")
+    first = _faces(ref.plugin_flatten())
+    ref.plugin_use_gpu(abi.PRECISION["FP64"])
+    again = _faces(ref.plugin_flatten())
+    ref.plugin_use_gpu(abi.PRECISION["FP64"])
+    assert ref.plugin_finish() == 0
+    assert first == again
