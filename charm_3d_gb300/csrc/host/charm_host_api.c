@@ -48,7 +48,38 @@ struct charm_host_forest_s {
     int8_t  *tree_bnd;      /* [n_tree][6], -1 where a tree face has a neighbour */
     double  *hex_vertex;    /* [8][3][E] */
     int8_t  *hex_face_face; /* [2][n_face] */
+    /* flatten's scratch (keys, face-neighbour records, counts), kept between
+     * flattens: an adapt loop reuses touched pages instead of faulting in
+     * ~290 B per leaf each time */
+    uint64_t *s_keys;
+    charm_face_nb_t *s_nbs;
+    int64_t *s_cnt;
+    int64_t s_cap;
+    /* capacities of the box flatten's arrays (leaves, faces, boundary faces),
+     * which keep their memory from one flatten to the next */
+    int64_t cap_e, cap_f, cap_b;
 };
+
+static void free_scratch(struct charm_host_forest_s *h)
+{
+    free(h->s_keys); free(h->s_nbs); free(h->s_cnt);
+    h->s_keys = NULL; h->s_nbs = NULL; h->s_cnt = NULL;
+    h->s_cap = 0;
+}
+
+/* scratch for E leaves (grown by a quarter when it grows) */
+static int ensure_scratch(struct charm_host_forest_s *h, int64_t E)
+{
+    if (E <= h->s_cap && h->s_keys) return 0;
+    free_scratch(h);
+    const int64_t cap = (E > 0 ? E : 1) + (E >> 2);
+    h->s_keys = (uint64_t *) malloc(sizeof(uint64_t) * (size_t) cap);
+    h->s_nbs = (charm_face_nb_t *) malloc(sizeof(charm_face_nb_t) * (size_t) (6 * cap));
+    h->s_cnt = (int64_t *) malloc(sizeof(int64_t) * (size_t) (4 * cap));
+    if (!h->s_keys || !h->s_nbs || !h->s_cnt) { free_scratch(h); return -1; }
+    h->s_cap = cap;
+    return 0;
+}
 
 static void free_flat(struct charm_host_forest_s *h)
 {
@@ -59,6 +90,55 @@ static void free_flat(struct charm_host_forest_s *h)
     h->bface_elem = NULL; h->bface_face = NULL; h->bface_bnd = NULL;
     h->hex_vertex = NULL; h->hex_face_face = NULL;
     h->n_face = h->n_bface = 0;
+    h->cap_e = h->cap_f = h->cap_b = 0;
+}
+
+/* After an adapt: the flattened arrays describe the old forest.  A box
+ * forest keeps their memory for the next flatten (which overwrites them);
+ * an unstructured one releases them. */
+static void stale_flat(struct charm_host_forest_s *h)
+{
+    if (h->conn) free_flat(h);
+    else h->n_face = h->n_bface = 0;
+}
+
+/* capacity for n items, grown by a quarter beyond n */
+static int64_t grown(int64_t n) { return (n > 0 ? n : 1) + (n >> 2); }
+
+/* realloc that keeps *p on failure; -1 then */
+static int re_alloc(void **p, size_t bytes)
+{
+    void *q = realloc(*p, bytes);
+    if (!q) return -1;
+    *p = q;
+    return 0;
+}
+
+/* The box flatten's arrays with room for E leaves, nf faces and nb boundary
+ * faces, kept with their pages when they are large enough already. */
+static int ensure_flat(struct charm_host_forest_s *h, int64_t E, int64_t nf, int64_t nb)
+{
+    int bad = 0;
+    if (E > h->cap_e || !h->center) {
+        const int64_t c = grown(E);
+        bad |= re_alloc((void **) &h->center, sizeof(double) * 3 * (size_t) c);
+        bad |= re_alloc((void **) &h->level, (size_t) c);
+        if (!bad) h->cap_e = c;
+    }
+    if (nf > h->cap_f || !h->face_elem) {
+        const int64_t c = grown(nf);
+        bad |= re_alloc((void **) &h->face_elem, sizeof(int32_t) * 2 * (size_t) c);
+        bad |= re_alloc((void **) &h->face_info, (size_t) c);
+        if (!bad) h->cap_f = c;
+    }
+    if (nb > h->cap_b || !h->bface_elem) {
+        const int64_t c = grown(nb);
+        bad |= re_alloc((void **) &h->bface_elem, sizeof(int32_t) * (size_t) c);
+        bad |= re_alloc((void **) &h->bface_face, (size_t) c);
+        bad |= re_alloc((void **) &h->bface_bnd, (size_t) c);
+        if (!bad) h->cap_b = c;
+    }
+    return bad ? -1 : 0;
 }
 
 int charm_host_forest_new(charm_host_forest_t *out, const int32_t ntree[3], const int32_t periodic[3],
@@ -90,6 +170,7 @@ int charm_host_forest_free(charm_host_forest_t h)
     free(h->plan_map);
     free(h->plan_nout);
     free(h->state);
+    free_scratch(h);
     charm_forest_free(&h->f);
     if (h->conn) { charm_conn_free(h->conn); free(h->conn); }
     free(h->tree_bnd);
@@ -230,7 +311,7 @@ int charm_host_forest_adapt(charm_host_forest_t h, const int8_t *flags, int minl
     }
     free(refine); free(coarse_old); free(cflag); free(old_level);
     if (charm_forest_balance(&h->f, NULL, NULL) < 0) return CHARM_GPU_ENOMEM;
-    free_flat(h);
+    stale_flat(h);
     if (n_new) *n_new = h->f.n;
     return CHARM_GPU_OK;
 }
@@ -331,17 +412,15 @@ int charm_host_forest_flatten(charm_host_forest_t h, charm_gpu_mesh_t *mesh)
     if (h->conn) return CHARM_GPU_ENOTSUP;   /* charm_host_forest_flatten_hex */
     const charm_forest_t *f = &h->f;
     const int64_t E = f->n;
-    free_flat(h);
     /* every leaf's six face-neighbour relations, found once (binary searches
      * on precomputed Morton keys) and read by the passes below */
-    uint64_t *keys = (uint64_t *) malloc(sizeof(uint64_t) * (size_t) (E > 0 ? E : 1));
-    charm_face_nb_t *nbs = (charm_face_nb_t *) malloc(sizeof(charm_face_nb_t) * (size_t) (6 * (E > 0 ? E : 1)));
-    int64_t *cnt = (int64_t *) malloc(sizeof(int64_t) * (size_t) (4 * (E > 0 ? E : 1)));
-    if (!keys || !nbs || !cnt) { free(keys); free(nbs); free(cnt); return CHARM_GPU_ENOMEM; }
+    if (ensure_scratch(h, E)) return CHARM_GPU_ENOMEM;
+    uint64_t *keys = h->s_keys;
+    charm_face_nb_t *nbs = h->s_nbs;
+    int64_t *cnt = h->s_cnt;
     charm_forest_keys(f, keys);
     nbs_ctx_t nc = {f, keys, nbs};
     charm_forest_parallel_for_min(E, 256, nbs_range, &nc);
-    free(keys);
     /* count, then turn the counts into offsets */
     flat_ctx_t fc = {h, nbs, E, 0, cnt};
     charm_forest_parallel_for(E, flat_count_range, &fc);
@@ -354,28 +433,18 @@ int charm_host_forest_flatten(charm_host_forest_t h, charm_gpu_mesh_t *mesh)
         }
     for (int64_t i = 0; i < E; i++) {
         const int64_t n = cnt[3 * E + i];
-        if (n < 0) { free(nbs); free(cnt); return CHARM_GPU_EINVAL; }   /* not 2:1 balanced */
+        if (n < 0) return CHARM_GPU_EINVAL;   /* not 2:1 balanced */
         cnt[3 * E + i] = nb;
         nb += n;
     }
-    h->center = (double *) malloc((size_t) (3 * (E > 0 ? E : 1)) * sizeof(double));
-    h->level = (int8_t *) malloc((size_t) (E > 0 ? E : 1));
-    h->face_elem = (int32_t *) malloc((size_t) (2 * (nf > 0 ? nf : 1)) * sizeof(int32_t));
-    h->face_info = (uint8_t *) malloc((size_t) (nf > 0 ? nf : 1));
-    h->bface_elem = (int32_t *) malloc((size_t) (nb > 0 ? nb : 1) * sizeof(int32_t));
-    h->bface_face = (int8_t *) malloc((size_t) (nb > 0 ? nb : 1));
-    h->bface_bnd = (int8_t *) malloc((size_t) (nb > 0 ? nb : 1));
-    if (!h->center || !h->level || !h->face_elem || !h->face_info || !h->bface_elem || !h->bface_face ||
-        !h->bface_bnd) {
+    /* the arrays keep their memory between flattens (the mesh pointers of
+     * the previous flatten are invalid from here on, as before) */
+    if (ensure_flat(h, E, nf, nb)) {
         free_flat(h);
-        free(nbs);
-        free(cnt);
         return CHARM_GPU_ENOMEM;
     }
     fc.nf = nf;
     charm_forest_parallel_for(E, flat_emit_range, &fc);
-    free(nbs);
-    free(cnt);
     h->n_face = nf;
     h->n_bface = nb;
     mesh->n_elem = E;
@@ -1058,7 +1127,7 @@ static int adapt_core(struct charm_host_forest_s *h, const double *grad, double 
         free(h->state);
         h->state = u;
     }
-    free_flat(h);
+    stale_flat(h);
     if (n_new) *n_new = f->n;
     return CHARM_GPU_OK;
 }
